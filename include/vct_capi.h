@@ -1,0 +1,290 @@
+/*
+ * vct_capi.h -- C ABI of the GB300-native voxel cone tracing core.
+ *
+ * Every entry point is a drop-in for one pass (or one helper recorder) of
+ * Snowapril/vk_voxel_cone_tracing.  The reference records Vulkan commands into
+ * a VkCommandBuffer; here each call enqueues CUDA kernels on the caller's
+ * stream (`stream` is a cudaStream_t passed as void*, NULL = legacy default
+ * stream).  All buffer pointers are DEVICE pointers unless the parameter name
+ * ends in `_host`.  Nothing is allocated behind the caller's back except where
+ * a function says so (texture objects, `vct_texture_*`).
+ *
+ * Parameter structs keep the reference's byte layouts (std140 / push-constant
+ * layouts of the GLSL blocks); the static asserts at the end of this header
+ * pin their sizes.  Images keep the reference's 3D atlas layout:
+ *   width  = (R + 2) * 6 faces, height = (R + 2) * 6 clip levels, depth = R + 2,
+ *   texel (x, y, z) at linear index (z * height + y) * width + x,
+ *   RGBA8 texels as uint32 little-endian (R in the low byte), exactly the
+ *   R32_UINT alias the reference uses for its atomic averages
+ *   (VFS/RenderPass/Clipmap/Voxelizer.cpp:249-287).
+ *
+ * Status codes: every function returns VCT_OK or a negative VCT_E_* code;
+ * vct_last_error() returns a message for the calling thread's last failure.
+ */
+#ifndef VCT_CAPI_H
+#define VCT_CAPI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status */
+#define VCT_OK 0
+#define VCT_E_BAD_ARG -1      /* null pointer, size out of range, bad enum */
+#define VCT_E_CUDA -2         /* a CUDA runtime call failed (message kept) */
+#define VCT_E_OVERFLOW -3     /* fragment list / node pool capacity exceeded */
+#define VCT_E_TIMEOUT -4      /* a bounded device-side wait gave up */
+#define VCT_E_UNSUPPORTED -5  /* configuration this build does not handle */
+
+/* Engine constants, VFS/Util/EngineConfig.h:19-33. */
+#define VCT_FACE_COUNT 6
+#define VCT_CLIP_LEVEL_COUNT 6
+#define VCT_VOXEL_BORDER 2       /* DEFAULT_VOXEL_BORDER: one texel per side */
+#define VCT_BORDER_WIDTH 1       /* BORDER_WIDTH specialisation constant     */
+#define VCT_DOWNSAMPLE_REGION_SIZE 10
+#define VCT_VOXEL_EXTENT_L0 16
+#define VCT_MIN_OCTREE_NODE_NUM 1000000u
+#define VCT_MAX_OCTREE_NODE_NUM 500000000u
+
+/* ------------------------------------------------------- reference structs */
+
+/* ClipmapRegion, VFS/RenderPass/Clipmap/ClipmapRegion.h:10-19. */
+typedef struct vct_clipmap_region {
+    int32_t min_corner[3];
+    uint32_t extent[3];
+    float voxel_size;
+} vct_clipmap_region;
+
+/* Voxelizer::VoxelizationDesc, VFS/RenderPass/Clipmap/Voxelizer.h:69-78 (64 B: four vec3 + scalar pairs). */
+typedef struct vct_voxelization_desc {
+    float region_min_corner[3];
+    uint32_t clip_level;
+    float region_max_corner[3];
+    float clip_max_extent;
+    float prev_region_min_corner[3];
+    float voxel_size;
+    float prev_region_max_corner[3];
+    int32_t clipmap_resolution;
+} vct_voxelization_desc;
+
+/* DownSampler::DownSampleDesc, VFS/RenderPass/Clipmap/DownSampler.h:49-55 (24 B). */
+typedef struct vct_downsample_desc {
+    int32_t prev_region_min_corner[3];
+    int32_t clip_level;
+    int32_t clipmap_resolution;
+    int32_t downsample_region_size;
+} vct_downsample_desc;
+
+/* ClipmapCleaner::ImageCleaningDesc, VFS/RenderPass/Clipmap/ClipmapCleaner.h:40-47 (36 B). */
+typedef struct vct_image_cleaning_desc {
+    int32_t region_min_corner[3];
+    int32_t clip_level;
+    uint32_t clip_max_extent[3];
+    int32_t clipmap_resolution;
+    uint32_t face_count;
+} vct_image_cleaning_desc;
+
+/* CopyAlpha::CopyAlphaDesc, VFS/RenderPass/Clipmap/CopyAlpha.h:30-35 (12 B). */
+typedef struct vct_copy_alpha_desc {
+    int32_t clip_level;
+    int32_t clipmap_resolution;
+    int32_t face_count;
+} vct_copy_alpha_desc;
+
+/* BorderWrapper::BorderWrappingDesc, VFS/RenderPass/Clipmap/BorderWrapper.h:39-44 (16 B). */
+typedef struct vct_border_wrapping_desc {
+    uint32_t clipmap_resolution;
+    uint32_t clip_border_width;
+    uint32_t face_count;
+    uint32_t clip_region_count;
+} vct_border_wrapping_desc;
+
+/* VoxelConeTracingPass::VoxelConeTracingDesc,
+ * VFS/RenderPass/Clipmap/VoxelConeTracingPass.h:46-59 (52 B); the push
+ * constant block of VFS/Shaders/voxelConeTracing.frag:56-69. */
+typedef struct vct_cone_tracing_desc {
+    float volume_center[3];
+    uint32_t rendering_mode;
+    float voxel_size;
+    float volume_dimension;
+    float trace_start_offset;
+    float indirect_diffuse_intensity;
+    float ambient_occlusion_factor;
+    float min_trace_step_factor;
+    float indirect_specular_intensity;
+    float occlusion_decay;
+    int32_t enable_32_cones;
+} vct_cone_tracing_desc;
+
+/* Rendering modes, VFS/Shaders/voxelConeTracing.frag:47-55. */
+#define VCT_MODE_DIFFUSE_ONLY 0
+#define VCT_MODE_SPECULAR_ONLY 1
+#define VCT_MODE_NORMAL_ONLY 2
+#define VCT_MODE_MIN_LEVEL_ONLY 3
+#define VCT_MODE_DIRECT_CONTRIBUTION_ONLY 4
+#define VCT_MODE_INDIRECT_DIFFUSE_ONLY 5
+#define VCT_MODE_INDIRECT_SPECULAR_ONLY 6
+#define VCT_MODE_AMBIENT_OCCLUSION_ONLY 7
+#define VCT_MODE_GI_OUTPUT 8
+
+/* CamMatrix uniform block, VFS/Shaders/voxelConeTracing.frag:18-24 (144 B).
+ * Matrices are column-major like glm / GLSL. */
+typedef struct vct_cam_matrix {
+    float view_proj[16];
+    float view_proj_inv[16];
+    float eye_pos[3];
+    int32_t padding;
+} vct_cam_matrix;
+
+/* DirectionalLightDesc, VFS/Shaders/light.glsl:8-13 (32 B). */
+typedef struct vct_directional_light_desc {
+    float direction[3];
+    float intensity;
+    float color[3];
+    int32_t padding;
+} vct_directional_light_desc;
+
+/* DirectionalLightShadowDesc, VFS/Shaders/light.glsl:15-20 (136 B as the C++
+ * side of the reference lays it out: glm::mat4 view, proj; float zNear, zFar). */
+typedef struct vct_directional_light_shadow_desc {
+    float view[16];
+    float proj[16];
+    float z_near;
+    float z_far;
+} vct_directional_light_shadow_desc;
+
+/* GltfShadeMaterial, VFS/Shaders/gltf.glsl:8-26 (80 B). */
+typedef struct vct_gltf_shade_material {
+    float pbr_base_color_factor[4];
+    int32_t pbr_base_color_texture;
+    float pbr_metallic_factor;
+    float pbr_roughness_factor;
+    int32_t pbr_metallic_roughness_texture;
+    int32_t emissive_texture;
+    int32_t alpha_mode;
+    float alpha_cutoff;
+    int32_t double_sided;
+    float emissive_factor[3];
+    int32_t normal_texture;
+    float normal_texture_scale;
+    int32_t occlusion_texture;
+    float occlusion_texture_strength;
+    int32_t padding;
+} vct_gltf_shade_material;
+
+/* One G-buffer texel set of the cone-tracing pass (80 B).  Replaces the
+ * G-buffer images the pass samples (VFS/RenderPass/GBufferPass.cpp:179-194,
+ * VFS/Shaders/voxelConeTracing.frag:145-163): the world position that
+ * worldPosFromDepth() would reconstruct, the depth test value (1.0 = sky,
+ * the fragment is discarded and its outputs are left untouched), and the
+ * texel values of the diffuse (RGBA8: albedo, perceptual roughness),
+ * normal (RGBA16F: n * 0.5 + 0.5), specular (RGBA8: F0, metallic) and
+ * emission (RGBA16F) attachments, already converted to float. */
+typedef struct vct_surface_sample {
+    float position[3];
+    float depth;
+    float normal_texel[3];
+    float pad0;
+    float diffuse_texel[4];
+    float specular_texel[4];
+    float emission_texel[3];
+    float pad1;
+} vct_surface_sample;
+
+/* Shadow map binding: a D32_SFLOAT depth image (row-major, width x height)
+ * sampled with linear filtering and CLAMP_TO_BORDER opaque black
+ * (VFS/RenderPass/Clipmap/VoxelConeTracingPass.cpp:294). */
+typedef struct vct_shadow_map {
+    const float* depth;
+    int32_t width;
+    int32_t height;
+} vct_shadow_map;
+
+/* ------------------------------------------------------------ helpers */
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* vct_last_error(void);
+
+/* Library version string and the device architecture it was built for. */
+const char* vct_version(void);
+
+/* Number of texels (uint32 words) of one RGBA8 clipmap atlas of resolution R. */
+int64_t vct_atlas_texels(int32_t clipmap_resolution);
+
+/* Per-level clip regions, VoxelizationPass::createVoxelClipmap +
+ * calculateChangeDelta (VFS/RenderPass/Clipmap/VoxelizationPass.cpp:335-357,
+ * 438-448) fed by Application::updateClipRegionBoundingBox
+ * (VFS/Application.cpp:116-128).  Host-side; writes 6 regions. */
+int vct_clip_regions(const float camera_pos_host[3], int32_t clipmap_resolution,
+                     int32_t voxel_extent_l0, vct_clipmap_region regions_host[6]);
+
+/* ------------------------------------------------------- clipmap passes */
+
+/* ClipmapCleaner::cmdClear{Opacity,Radiance}ClipRegion
+ * (VFS/RenderPass/Clipmap/ClipmapCleaner.cpp:93-133, clipmapCleaning.comp):
+ * zero `face_count` faces of a toroidal region of one level. */
+int vct_clear_region(uint32_t* atlas, const vct_image_cleaning_desc* desc, void* stream);
+
+/* CopyAlpha::cmdImageCopyAlpha (VFS/RenderPass/Clipmap/CopyAlpha.cpp:92-146,
+ * copyAlphaImage.comp): dst.a := src.a over the R^3 interior of one level. */
+int vct_copy_alpha(uint32_t* dst_atlas, const uint32_t* src_atlas,
+                   const vct_copy_alpha_desc* desc, void* stream);
+
+/* DownSampler::cmdDownSample{Opacity,Radiance}
+ * (VFS/RenderPass/Clipmap/DownSampler.cpp:115-168, opacityDownSample.comp,
+ * radianceDownSample.comp): one anisotropic 2x2x2 level, in place. */
+#define VCT_DOWNSAMPLE_OPACITY 0
+#define VCT_DOWNSAMPLE_RADIANCE 1
+int vct_downsample(uint32_t* atlas, const vct_downsample_desc* desc, int32_t mode,
+                   void* stream);
+
+/* All levels 1..5 of one atlas in sequence, each from its predecessor, with
+ * the same per-level descs the reference uploads; `regions` are the 6 clip
+ * regions (host memory). */
+int vct_downsample_all(uint32_t* atlas, const vct_clipmap_region regions_host[6],
+                       int32_t clipmap_resolution, int32_t mode, void* stream);
+
+/* BorderWrapper::cmdWrappingOpacityBorder (VFS/RenderPass/Clipmap/BorderWrapper.cpp:123-151,
+ * borderWrapping.comp): copy toroidal neighbours into border texels. */
+int vct_wrap_border(uint32_t* atlas, const vct_border_wrapping_desc* desc, void* stream);
+
+/* VoxelConeTracingPass::onUpdate (VFS/RenderPass/Clipmap/VoxelConeTracingPass.cpp:75-106)
+ * executing voxelConeTracing.frag per G-buffer sample.  `radiance_atlas` is
+ * the RGBA8 atlas in the layout above; outputs are RGBA32F (4 floats per
+ * sample) like the pass's two attachments.  `cone_steps` (optional, may be
+ * NULL) receives += the number of traceCone loop iterations executed.
+ * Exact form: FP32 arithmetic, trilinear weights in FP32 (no 8-bit filter
+ * weights), reads the linear atlas. */
+int vct_cone_trace(const vct_cone_tracing_desc* desc, const vct_cam_matrix* cam,
+                   const uint32_t* radiance_atlas, int32_t clipmap_resolution,
+                   const vct_shadow_map* shadow, const vct_directional_light_desc* light,
+                   const vct_directional_light_shadow_desc* light_shadow,
+                   const vct_surface_sample* samples, int64_t sample_count,
+                   float* diffuse_out, float* specular_out,
+                   unsigned long long* cone_steps, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#ifdef __cplusplus
+#define VCT_STATIC_ASSERT(c, m) static_assert(c, m)
+#else
+#define VCT_STATIC_ASSERT(c, m) _Static_assert(c, m)
+#endif
+VCT_STATIC_ASSERT(sizeof(vct_voxelization_desc) == 64, "VoxelizationDesc is 64 B");
+VCT_STATIC_ASSERT(sizeof(vct_downsample_desc) == 24, "DownSampleDesc is 24 B");
+VCT_STATIC_ASSERT(sizeof(vct_image_cleaning_desc) == 36, "ImageCleaningDesc is 36 B");
+VCT_STATIC_ASSERT(sizeof(vct_copy_alpha_desc) == 12, "CopyAlphaDesc is 12 B");
+VCT_STATIC_ASSERT(sizeof(vct_border_wrapping_desc) == 16, "BorderWrappingDesc is 16 B");
+VCT_STATIC_ASSERT(sizeof(vct_cone_tracing_desc) == 52, "VoxelConeTracingDesc is 52 B");
+VCT_STATIC_ASSERT(sizeof(vct_cam_matrix) == 144, "CamMatrix is 144 B");
+VCT_STATIC_ASSERT(sizeof(vct_directional_light_desc) == 32, "DirectionalLightDesc is 32 B");
+VCT_STATIC_ASSERT(sizeof(vct_directional_light_shadow_desc) == 136, "DirectionalLightShadowDesc is 136 B");
+VCT_STATIC_ASSERT(sizeof(vct_gltf_shade_material) == 80, "GltfShadeMaterial is 80 B");
+VCT_STATIC_ASSERT(sizeof(vct_surface_sample) == 80, "surface sample is 80 B");
+
+#endif /* VCT_CAPI_H */

@@ -1,0 +1,164 @@
+"""ctypes binding of the CPU oracle (libvct_oracle.so) -- TEST INFRASTRUCTURE ONLY.
+
+The oracle is a C++ restatement of the reference's shader arithmetic
+(clipmap_oracle.hpp and friends).  Only ``tests/``, ``__graft_entry__.smoke()``
+and bench.py's CPU-baseline leg import this module; the CUDA product path
+never does.  ``build()`` compiles the oracle with g++ (-ffp-contract=off so
+no multiply-add is fused, -fopenmp for the timed CPU baseline).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+BUILD = HERE / "_build"
+LIB = BUILD / "libvct_oracle.so"
+SOURCES = ["vct_oracle.cpp"]
+HEADERS = ["oracle_common.hpp", "clipmap_oracle.hpp", "raster_oracle.hpp", "svo_oracle.hpp"]
+
+P = C.c_void_p
+
+
+def _deps():
+    return [HERE / s for s in SOURCES] + [HERE / h for h in HEADERS if (HERE / h).exists()] + [Path(__file__)]
+
+
+def build(force: bool = False) -> Path:
+    if not force and LIB.exists() and all(p.stat().st_mtime <= LIB.stat().st_mtime for p in _deps()):
+        return LIB
+    BUILD.mkdir(exist_ok=True)
+    cxx = os.environ.get("CXX", "g++")
+    tmp = LIB.with_suffix(".so.tmp")
+    cmd = [cxx, "-std=c++17", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
+           *[str(HERE / s) for s in SOURCES], "-o", str(tmp)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{' '.join(cmd)}\n{r.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+_L = None
+
+
+def lib():
+    global _L
+    if _L is None:
+        build()
+        L = C.CDLL(str(LIB))
+        L.vcto_num_threads.restype = C.c_int
+        L.vcto_set_threads.argtypes = [C.c_int]
+        L.vcto_clip_regions.argtypes = [P, C.c_int, C.c_int, P]
+        L.vcto_clear_region.argtypes = [P, C.c_int, P, P, C.c_int, C.c_int]
+        L.vcto_copy_alpha.argtypes = [P, P, C.c_int, C.c_int, C.c_int]
+        L.vcto_wrap_border.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int]
+        L.vcto_downsample.argtypes = [P, C.c_int, P, C.c_int, C.c_int, C.c_int]
+        L.vcto_cone_trace.restype = C.c_uint64
+        L.vcto_cone_trace.argtypes = [C.c_int, P, P, P, C.c_int, P, C.c_int, C.c_int, P, P, P, C.c_int64,
+                                      C.c_int64, P, P, P]
+        L.vcto_cone_trace_f4.restype = C.c_uint64
+        L.vcto_cone_trace_f4.argtypes = [P, P, P, C.c_int, P, C.c_int, C.c_int, P, P, P, C.c_int64, C.c_int64,
+                                         P, P]
+        L.vcto_procedural_atlas.argtypes = [P, C.c_int64, C.c_uint32, C.c_double]
+        _L = L
+    return _L
+
+
+def _p(a: np.ndarray | None):
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def set_threads(n: int) -> None:
+    lib().vcto_set_threads(int(n))
+
+
+def num_threads() -> int:
+    return int(lib().vcto_num_threads())
+
+
+def clip_regions(cam, R: int, extent_l0: int = 16) -> np.ndarray:
+    """6 regions as an int/float record array: min_corner(3 i32), extent(3 u32), voxel_size(f32)."""
+    out = np.zeros(6 * 7, dtype=np.int32)
+    cam = np.asarray(cam, dtype=np.float32)
+    lib().vcto_clip_regions(_p(cam), R, extent_l0, _p(out))
+    return out.reshape(6, 7)
+
+
+def region_voxel_size(regions: np.ndarray, level: int) -> float:
+    return float(regions[level, 6:7].view(np.float32)[0])
+
+
+def clear_region(atlas: np.ndarray, R: int, region_min, extent, level: int, faces: int = 6) -> None:
+    lib().vcto_clear_region(_p(atlas), R, _p(np.asarray(region_min, np.int32)), _p(np.asarray(extent, np.uint32)),
+                            level, faces)
+
+
+def copy_alpha(dst: np.ndarray, src: np.ndarray, R: int, level: int, faces: int = 6) -> None:
+    lib().vcto_copy_alpha(_p(dst), _p(src), R, level, faces)
+
+
+def wrap_border(atlas: np.ndarray, R: int, border_width_desc: int = 2, faces: int = 6, regions: int = 6) -> None:
+    lib().vcto_wrap_border(_p(atlas), R, border_width_desc, faces, regions)
+
+
+def downsample(atlas: np.ndarray, R: int, prev_min, level: int, mode: int, band: int = 10) -> None:
+    lib().vcto_downsample(_p(atlas), R, _p(np.asarray(prev_min, np.int32)), level, band, mode)
+
+
+def procedural_atlas(R: int, seed: int = 3, fill: float = 0.05) -> np.ndarray:
+    """The benchmark's hash-random atlas (identical to scene.procedural_atlas_torch) built in C++."""
+    shape = (R + 2, 6 * (R + 2), 6 * (R + 2))
+    out = np.empty(shape, np.uint32)
+    lib().vcto_procedural_atlas(_p(out), out.size, seed & 0xFFFFFFFF, fill)
+    return out
+
+
+def default_light_bytes() -> bytes:
+    """DirectionalLightDesc{direction (0.3,-1,0.2), intensity 1, colour 1}: the configurations' light."""
+    return np.array([0.3, -1.0, 0.2, 1.0, 1.0, 1.0, 1.0, 0.0], np.float32).tobytes()
+
+
+def cone_trace(precision: int, desc_bytes: bytes, eye, atlas: np.ndarray, R: int, samples: np.ndarray,
+               shadow: np.ndarray | None = None, shadow_desc_bytes: bytes | None = None,
+               light_bytes: bytes | None = None, begin: int = 0, end: int | None = None):
+    """Trace samples [begin, end) with the FP32 (precision=32) or FP64 (64) restatement.
+
+    Returns (diffuse[n,4] f64, specular[n,4] f64, steps, written[n] u8)."""
+    n = samples.shape[0]
+    end = n if end is None else end
+    dout = np.zeros((n, 4), np.float64)
+    sout = np.zeros((n, 4), np.float64)
+    written = np.zeros(n, np.uint8)
+    desc = np.frombuffer(desc_bytes, np.uint8).copy()
+    sd = np.frombuffer(shadow_desc_bytes or bytes(136), np.uint8).copy()
+    light = np.frombuffer(light_bytes or default_light_bytes(), np.uint8).copy()
+    eye = np.asarray(eye, np.float32)
+    sh, sw = (shadow.shape if shadow is not None else (0, 0))
+    steps = lib().vcto_cone_trace(precision, _p(desc), _p(eye), _p(atlas), R, _p(shadow), sw, sh, _p(sd),
+                                  _p(light), _p(samples), begin, end, _p(dout), _p(sout), _p(written))
+    return dout, sout, int(steps), written
+
+
+def cone_trace_f4(desc_bytes: bytes, eye, atlas4: np.ndarray, R: int, samples: np.ndarray,
+                  shadow: np.ndarray | None = None, shadow_desc_bytes: bytes | None = None,
+                  light_bytes: bytes | None = None, begin: int = 0, end: int | None = None):
+    n = samples.shape[0]
+    end = n if end is None else end
+    dout = np.zeros((n, 4), np.float64)
+    sout = np.zeros((n, 4), np.float64)
+    desc = np.frombuffer(desc_bytes, np.uint8).copy()
+    sd = np.frombuffer(shadow_desc_bytes or bytes(136), np.uint8).copy()
+    light = np.frombuffer(light_bytes or default_light_bytes(), np.uint8).copy()
+    eye = np.asarray(eye, np.float32)
+    sh, sw = (shadow.shape if shadow is not None else (0, 0))
+    steps = lib().vcto_cone_trace_f4(_p(desc), _p(eye), _p(atlas4), R, _p(shadow), sw, sh, _p(sd), _p(light),
+                                     _p(samples), begin, end, _p(dout), _p(sout))
+    return dout, sout, int(steps)

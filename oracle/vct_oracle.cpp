@@ -1,0 +1,124 @@
+// vct_oracle.cpp -- TEST INFRASTRUCTURE ONLY.
+//
+// C entry points over the CPU restatement (clipmap_oracle.hpp, svo_oracle.hpp,
+// raster_oracle.hpp) for the Python test harness and bench.py's CPU-baseline
+// leg (ctypes).  The CUDA product library never links or calls this file.
+#include <omp.h>
+
+#include "clipmap_oracle.hpp"
+
+using namespace vcto;
+
+extern "C" {
+
+int vcto_num_threads(void) { return omp_get_max_threads(); }
+void vcto_set_threads(int n) {
+    if (n > 0) omp_set_num_threads(n);
+}
+
+void vcto_clip_regions(const float cam[3], int R, int extent_l0, Region out[6]) { clip_regions(cam, R, extent_l0, out); }
+
+void vcto_clear_region(uint32_t* atlas, int R, const int32_t region_min[3], const uint32_t extent[3], int level,
+                       int face_count) {
+    clear_region(atlas, R, region_min, extent, level, face_count);
+}
+
+void vcto_copy_alpha(uint32_t* dst, const uint32_t* src, int R, int level, int face_count) {
+    copy_alpha(dst, src, R, level, face_count);
+}
+
+void vcto_wrap_border(uint32_t* atlas, int R, int border_width_desc, int face_count, int region_count) {
+    wrap_border(atlas, R, border_width_desc, face_count, region_count);
+}
+
+void vcto_downsample(uint32_t* atlas, int R, const int prev_min[3], int level, int band, int mode) {
+    downsample(atlas, R, prev_min, level, band, mode);
+}
+
+// Cone trace over an RGBA8 atlas.  precision: 32 = FP32 mirror, 64 = FP64.
+// Samples [begin, end) are traced; outputs are 4 doubles per sample.
+// Returns the number of traceCone loop iterations executed.
+uint64_t vcto_cone_trace(int precision, const TraceDesc* desc, const float eye[3], const uint32_t* atlas, int R,
+                         const float* shadow, int sw, int sh, const ShadowDesc* sd, const LightDesc* light,
+                         const SurfaceSample* samples, int64_t begin, int64_t end, double* out_d, double* out_s,
+                         uint8_t* written) {
+    Atlas A(R);
+    uint64_t total = 0;
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : total)
+    for (int64_t i = begin; i < end; ++i) {
+        bool ok;
+        if (precision == 64) {
+            Rgba8Fetch<double> f{atlas, A};
+            ClipmapTracer<double, Rgba8Fetch<double>> tr{*desc, f, A};
+            double d[4], s[4];
+            ok = trace_sample<double>(tr, eye, shadow, sw, sh, *sd, *light, samples[i], d, s);
+            if (ok)
+                for (int c = 0; c < 4; ++c) {
+                    out_d[4 * i + c] = d[c];
+                    out_s[4 * i + c] = s[c];
+                }
+            total += tr.steps;
+        } else {
+            Rgba8Fetch<float> f{atlas, A};
+            ClipmapTracer<float, Rgba8Fetch<float>> tr{*desc, f, A};
+            float d[4], s[4];
+            ok = trace_sample<float>(tr, eye, shadow, sw, sh, *sd, *light, samples[i], d, s);
+            if (ok)
+                for (int c = 0; c < 4; ++c) {
+                    out_d[4 * i + c] = d[c];
+                    out_s[4 * i + c] = s[c];
+                }
+            total += tr.steps;
+        }
+        if (written) written[i] = ok ? 1 : 0;
+    }
+    return total;
+}
+
+// Cone trace over a float4 atlas (unquantised storage) in FP64: the error
+// reference for the FP16-storage form.
+uint64_t vcto_cone_trace_f4(const TraceDesc* desc, const float eye[3], const float* atlas4, int R, const float* shadow,
+                            int sw, int sh, const ShadowDesc* sd, const LightDesc* light, const SurfaceSample* samples,
+                            int64_t begin, int64_t end, double* out_d, double* out_s) {
+    Atlas A(R);
+    uint64_t total = 0;
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : total)
+    for (int64_t i = begin; i < end; ++i) {
+        Float4Fetch<double> f{atlas4, A};
+        ClipmapTracer<double, Float4Fetch<double>> tr{*desc, f, A};
+        double d[4], s[4];
+        if (trace_sample<double>(tr, eye, shadow, sw, sh, *sd, *light, samples[i], d, s))
+            for (int c = 0; c < 4; ++c) {
+                out_d[4 * i + c] = d[c];
+                out_s[4 * i + c] = s[c];
+            }
+        total += tr.steps;
+    }
+    return total;
+}
+
+// The benchmark's hash-random sparse atlas (same words as
+// vk_voxel_cone_tracing_gb300.scene.procedural_atlas_words), OpenMP-parallel.
+static inline uint64_t fmix32(uint64_t h) {
+    const uint64_t m = 0xFFFFFFFFull;
+    h ^= h >> 16;
+    h = (h * 0x85EBCA6Bull) & m;
+    h ^= h >> 13;
+    h = (h * 0xC2B2AE35ull) & m;
+    h ^= h >> 16;
+    return h;
+}
+void vcto_procedural_atlas(uint32_t* out, int64_t n, uint32_t seed, double fill) {
+    const uint64_t m = 0xFFFFFFFFull;
+    const uint64_t thr = (uint64_t)(int64_t)(fill * 65536.0);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        uint64_t h = fmix32((((uint64_t)i * 0x9E3779B1ull) & m) ^ (uint64_t)seed);
+        uint64_t h2 = fmix32((h * 0x27D4EB2Full + 0x165667B1ull) & m);
+        bool occ = (h & 0xFFFF) < thr;
+        uint64_t alpha = 64 + ((h >> 16) % 192);
+        out[i] = occ ? (uint32_t)((h2 & 0xFFFFFF) | (alpha << 24)) : 0u;
+    }
+}
+
+}  // extern "C"

@@ -1,0 +1,166 @@
+"""ctypes binding of ``include/vct_capi.h`` (libvct_gb300.so).
+
+Struct classes mirror the C structs byte for byte (their sizes are asserted
+against the header's static asserts in the tests).  ``lib()`` loads the
+in-tree CUDA library and raises if it is missing: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "libvct_gb300.so"
+
+VCT_OK = 0
+VCT_E_BAD_ARG = -1
+VCT_E_CUDA = -2
+VCT_E_OVERFLOW = -3
+VCT_E_TIMEOUT = -4
+VCT_E_UNSUPPORTED = -5
+
+FACE_COUNT = 6
+CLIP_LEVEL_COUNT = 6
+VOXEL_BORDER = 2
+DOWNSAMPLE_REGION_SIZE = 10
+VOXEL_EXTENT_L0 = 16
+
+DOWNSAMPLE_OPACITY = 0
+DOWNSAMPLE_RADIANCE = 1
+
+MODE_GI_OUTPUT = 8
+
+f3 = C.c_float * 3
+f4 = C.c_float * 4
+f16 = C.c_float * 16
+i3 = C.c_int32 * 3
+u3 = C.c_uint32 * 3
+
+
+class ClipmapRegion(C.Structure):
+    _fields_ = [("min_corner", i3), ("extent", u3), ("voxel_size", C.c_float)]
+
+
+class VoxelizationDesc(C.Structure):
+    _fields_ = [("region_min_corner", f3), ("clip_level", C.c_uint32), ("region_max_corner", f3),
+                ("clip_max_extent", C.c_float), ("prev_region_min_corner", f3), ("voxel_size", C.c_float),
+                ("prev_region_max_corner", f3), ("clipmap_resolution", C.c_int32)]
+
+
+class DownSampleDesc(C.Structure):
+    _fields_ = [("prev_region_min_corner", i3), ("clip_level", C.c_int32), ("clipmap_resolution", C.c_int32),
+                ("downsample_region_size", C.c_int32)]
+
+
+class ImageCleaningDesc(C.Structure):
+    _fields_ = [("region_min_corner", i3), ("clip_level", C.c_int32), ("clip_max_extent", u3),
+                ("clipmap_resolution", C.c_int32), ("face_count", C.c_uint32)]
+
+
+class CopyAlphaDesc(C.Structure):
+    _fields_ = [("clip_level", C.c_int32), ("clipmap_resolution", C.c_int32), ("face_count", C.c_int32)]
+
+
+class BorderWrappingDesc(C.Structure):
+    _fields_ = [("clipmap_resolution", C.c_uint32), ("clip_border_width", C.c_uint32), ("face_count", C.c_uint32),
+                ("clip_region_count", C.c_uint32)]
+
+
+class ConeTracingDesc(C.Structure):
+    _fields_ = [("volume_center", f3), ("rendering_mode", C.c_uint32), ("voxel_size", C.c_float),
+                ("volume_dimension", C.c_float), ("trace_start_offset", C.c_float),
+                ("indirect_diffuse_intensity", C.c_float), ("ambient_occlusion_factor", C.c_float),
+                ("min_trace_step_factor", C.c_float), ("indirect_specular_intensity", C.c_float),
+                ("occlusion_decay", C.c_float), ("enable_32_cones", C.c_int32)]
+
+
+class CamMatrix(C.Structure):
+    _fields_ = [("view_proj", f16), ("view_proj_inv", f16), ("eye_pos", f3), ("padding", C.c_int32)]
+
+
+class DirectionalLightDesc(C.Structure):
+    _fields_ = [("direction", f3), ("intensity", C.c_float), ("color", f3), ("padding", C.c_int32)]
+
+
+class DirectionalLightShadowDesc(C.Structure):
+    _fields_ = [("view", f16), ("proj", f16), ("z_near", C.c_float), ("z_far", C.c_float)]
+
+
+class GltfShadeMaterial(C.Structure):
+    _fields_ = [("pbr_base_color_factor", f4), ("pbr_base_color_texture", C.c_int32),
+                ("pbr_metallic_factor", C.c_float), ("pbr_roughness_factor", C.c_float),
+                ("pbr_metallic_roughness_texture", C.c_int32), ("emissive_texture", C.c_int32),
+                ("alpha_mode", C.c_int32), ("alpha_cutoff", C.c_float), ("double_sided", C.c_int32),
+                ("emissive_factor", f3), ("normal_texture", C.c_int32), ("normal_texture_scale", C.c_float),
+                ("occlusion_texture", C.c_int32), ("occlusion_texture_strength", C.c_float),
+                ("padding", C.c_int32)]
+
+
+class ShadowMap(C.Structure):
+    _fields_ = [("depth", C.c_void_p), ("width", C.c_int32), ("height", C.c_int32)]
+
+
+STRUCT_SIZES = {
+    ClipmapRegion: 28, VoxelizationDesc: 64, DownSampleDesc: 24, ImageCleaningDesc: 36, CopyAlphaDesc: 12,
+    BorderWrappingDesc: 16, ConeTracingDesc: 52, CamMatrix: 144, DirectionalLightDesc: 32,
+    DirectionalLightShadowDesc: 136, GltfShadeMaterial: 80,
+}
+
+# Every entry point of include/vct_capi.h: name -> (restype, argtypes).
+P = C.c_void_p
+_SIGS: dict[str, tuple] = {
+    "vct_last_error": (C.c_char_p, []),
+    "vct_version": (C.c_char_p, []),
+    "vct_atlas_texels": (C.c_int64, [C.c_int32]),
+    "vct_clip_regions": (C.c_int, [P, C.c_int32, C.c_int32, P]),
+    "vct_clear_region": (C.c_int, [P, P, P]),
+    "vct_copy_alpha": (C.c_int, [P, P, P, P]),
+    "vct_downsample": (C.c_int, [P, P, C.c_int32, P]),
+    "vct_downsample_all": (C.c_int, [P, P, C.c_int32, C.c_int32, P]),
+    "vct_wrap_border": (C.c_int, [P, P, P]),
+    "vct_cone_trace": (C.c_int, [P, P, P, C.c_int32, P, P, P, P, C.c_int64, P, P, P, P]),
+}
+
+
+class VctError(RuntimeError):
+    def __init__(self, fn: str, code: int, msg: str):
+        super().__init__(f"{fn} failed with status {code}: {msg}")
+        self.code = code
+
+
+_LIB: C.CDLL | None = None
+
+
+def declared_symbols() -> list[str]:
+    """Function names declared in include/vct_capi.h (parsed from the header)."""
+    import re
+    text = (PKG.parent / "include" / "vct_capi.h").read_text()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?[a-z0-9_]+\s*\*?\s*(vct_[a-z0-9_]+)\s*\(", text, re.M)))
+
+
+def lib() -> C.CDLL:
+    """Load libvct_gb300.so (raises if it has not been built)."""
+    global _LIB
+    if _LIB is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} is missing: run `python -c 'import __graft_entry__ as g; g.build()'`")
+        L = C.CDLL(str(LIB_PATH))
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+def check(fn: str, rc: int) -> None:
+    if rc != VCT_OK:
+        raise VctError(fn, rc, lib().vct_last_error().decode())
+
+
+def call(fn: str, *args) -> None:
+    check(fn, getattr(lib(), fn)(*args))
+
+
+def ref(s: C.Structure) -> C.c_void_p:
+    return C.cast(C.pointer(s), C.c_void_p)

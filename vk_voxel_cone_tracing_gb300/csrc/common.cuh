@@ -1,0 +1,64 @@
+// common.cuh -- shared device/host helpers of the GB300 voxel cone tracing core.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/vct_capi.h"
+
+namespace vct {
+
+// ---------------------------------------------------------------- errors
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+
+#define VCT_CHECK_ARG(cond, msg)                              \
+    do {                                                       \
+        if (!(cond)) return ::vct::fail(VCT_E_BAD_ARG, (msg)); \
+    } while (0)
+#define VCT_CUDA_TRY(expr)                                   \
+    do {                                                      \
+        cudaError_t e_ = (expr);                              \
+        if (e_ != cudaSuccess) return ::vct::cuda_fail(e_, #expr); \
+    } while (0)
+#define VCT_LAUNCH_CHECK() VCT_CUDA_TRY(cudaGetLastError())
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// ------------------------------------------------------------- geometry
+// The reference atlas: width (R+2)*6, height (R+2)*6, depth R+2.
+struct AtlasDims {
+    int R, rb, W, H, D;
+    __host__ __device__ explicit AtlasDims(int res) : R(res), rb(res + 2), W((res + 2) * 6), H((res + 2) * 6), D(res + 2) {}
+    __host__ __device__ int64_t index(int x, int y, int z) const { return ((int64_t)z * H + y) * W + x; }
+    __host__ __device__ int64_t texels() const { return (int64_t)W * H * D; }
+};
+
+inline bool valid_resolution(int R) { return R >= 8 && R <= 1024 && (R & (R - 1)) == 0; }
+
+// ------------------------------------------------------------- unorm8
+__device__ __forceinline__ float unorm8_load(uint32_t v, int c) {
+    return (float)((v >> (8 * c)) & 0xffu) / 255.0f;
+}
+__device__ __forceinline__ float4 unpack_rgba8(uint32_t v) {
+    return make_float4((float)(v & 0xffu) / 255.0f, (float)((v >> 8) & 0xffu) / 255.0f,
+                       (float)((v >> 16) & 0xffu) / 255.0f, (float)(v >> 24) / 255.0f);
+}
+// Pinned store rule: round-half-up of clamp(x, 0, 1) * 255.
+__device__ __forceinline__ uint32_t unorm8_store(float x) {
+    float c = fminf(fmaxf(x, 0.0f), 1.0f);
+    return (uint32_t)floorf(__fadd_rn(__fmul_rn(c, 255.0f), 0.5f));
+}
+__device__ __forceinline__ uint32_t pack_rgba8(float4 c) {
+    return unorm8_store(c.x) | (unorm8_store(c.y) << 8) | (unorm8_store(c.z) << 16) | (unorm8_store(c.w) << 24);
+}
+
+// GLSL mix(x, y, a) = x * (1 - a) + y * a, without contraction.
+__device__ __forceinline__ float mix_rn(float x, float y, float a) {
+    return __fadd_rn(__fmul_rn(x, __fsub_rn(1.0f, a)), __fmul_rn(y, a));
+}
+
+}  // namespace vct
