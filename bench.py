@@ -187,15 +187,33 @@ def run_ours(args, world, rank, local):
     clipmap.cmd_downsample_all(atlas, R, creg, 1)
     torch.cuda.synchronize()
 
-    samples_np = make_samples(N_SAMPLES, seed=100 + rank)  # weak scaling: one frame per rank
+    samples_np = make_samples(args.samples, seed=100 + rank)  # weak scaling: one frame per rank
     samples = clipmap.samples_to_device(samples_np, dev)
     n = samples.shape[0]
     dout = torch.empty((n, 4), dtype=torch.float32, device=dev)
     sout = torch.empty((n, 4), dtype=torch.float32, device=dev)
     steps_ctr = torch.zeros(1, dtype=torch.int64, device=dev)
 
+    tex = None
+    tex_src = atlas
+    if args.form in ("tex", "fp16"):
+        from vk_voxel_cone_tracing_gb300 import capi
+        if args.form == "fp16":
+            tex_src = clipmap.to_rgba16f(atlas, R)
+            clipmap.cmd_downsample_rgba16f_all(tex_src, R, creg, 1)
+        tex = clipmap.RadianceTexture(R, capi.TEX_RGBA8 if args.form == "tex" else capi.TEX_RGBA16F)
+        scratch = clipmap.fast_scratch(n, dev)
+
+    def trace(inp, counter=None):
+        if tex is None:
+            clipmap.cone_trace(desc, EYE, atlas, R, inp, diffuse=dout, specular=sout, steps=counter)
+        else:
+            tex.update(tex_src)  # the texture copy of the clipmap is refreshed every step
+            clipmap.cone_trace_fast(desc, EYE, tex, inp, diffuse=dout, specular=sout, steps=counter,
+                                    scratch=scratch)
+
     def step(counter=None):
-        clipmap.cone_trace(desc, EYE, atlas, R, samples, diffuse=dout, specular=sout, steps=counter)
+        trace(samples, counter)
 
     # counting run: the number of cone samples one step executes
     step(steps_ctr)
@@ -231,7 +249,7 @@ def run_ours(args, world, rank, local):
     d_in = torch.empty_like(samples)
     for _ in range(max(1, args.warmup)):
         d_in.copy_(h_samples, non_blocking=True)
-        clipmap.cone_trace(desc, EYE, atlas, R, d_in, diffuse=dout, specular=sout)
+        trace(d_in)
         h_d.copy_(dout, non_blocking=True)
         h_s.copy_(sout, non_blocking=True)
     torch.cuda.synchronize()
@@ -239,7 +257,7 @@ def run_ours(args, world, rank, local):
     e0.record(stream)
     for _ in range(args.steps):
         d_in.copy_(h_samples, non_blocking=True)
-        clipmap.cone_trace(desc, EYE, atlas, R, d_in, diffuse=dout, specular=sout)
+        trace(d_in)
         h_d.copy_(dout, non_blocking=True)
         h_s.copy_(sout, non_blocking=True)
     e1.record(stream)
@@ -256,7 +274,7 @@ def run_ours(args, world, rank, local):
         avg_launch_s = statistics.mean(per) * 1e-3
         achieved = cone_samples * bpcs / avg_launch_s / 1e9
         traffic = None
-        prof = ROOT / "profiles" / "cone_trace_exact_r256.txt"
+        prof = ROOT / "profiles" / f"cone_trace_{args.form}_r{R}.txt"
         if prof.exists():
             for line in prof.read_text().splitlines():
                 if line.startswith("dram_bytes_per_launch_full:"):
@@ -284,7 +302,7 @@ def run_ours(args, world, rank, local):
             "e2e": {"value": cone_samples * world / (e2e_ms * 1e-3), "unit": "cone samples/s",
                     "h2d_bytes_per_step": int(samples.numel() * 4),
                     "d2h_bytes_per_step": int((dout.numel() + sout.numel()) * 4)},
-            "gpu_launches": args.steps,
+            "gpu_launches": args.steps * (1 if tex is None else 3),
             "clocks": clocks.summary(),
         }
         print(json.dumps(line), flush=True)
@@ -299,6 +317,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--form", default="exact", choices=["exact", "tex", "fp16"])
+    ap.add_argument("--samples", type=int, default=N_SAMPLES)
     ap.add_argument("--R", type=int, default=R_DEFAULT)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")

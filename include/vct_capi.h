@@ -266,6 +266,44 @@ int vct_cone_trace(const vct_cone_tracing_desc* desc, const vct_cam_matrix* cam,
                    float* diffuse_out, float* specular_out,
                    unsigned long long* cone_steps, void* stream);
 
+/* ------------------------------------------- texture-sampled (fast) form */
+
+/* A hardware-filtered copy of a radiance atlas: a 3D CUDA array with
+ * normalized coordinates, WRAP addressing and linear filtering (the
+ * reference's VoxelSampler, VFS/RenderPass/Clipmap/Voxelizer.cpp:279).
+ * vct_texture_create allocates the array (W x H x D texels of 4 or 8 B);
+ * vct_texture_update copies a linear atlas of the texture's format into it. */
+typedef struct vct_texture_s* vct_texture;
+#define VCT_TEX_RGBA8 0
+#define VCT_TEX_RGBA16F 1
+int vct_texture_create(int32_t clipmap_resolution, int32_t format, vct_texture* out);
+int vct_texture_update(vct_texture tex, const void* atlas, void* stream);
+int vct_texture_destroy(vct_texture tex);
+
+/* FP16-storage form of the radiance clipmap (4 halves per texel, same
+ * layout): conversion of an RGBA8 atlas, and the anisotropic downsample of
+ * radianceDownSample.comp / opacityDownSample.comp with FP32 arithmetic and
+ * RGBA16F storage (no 8-bit quantisation of the mips). */
+int vct_atlas_rgba8_to_rgba16f(const uint32_t* src, uint16_t* dst, int32_t clipmap_resolution, void* stream);
+int vct_downsample_rgba16f(uint16_t* atlas, const vct_downsample_desc* desc, int32_t mode, void* stream);
+
+/* Bytes of caller-provided scratch vct_cone_trace_fast needs for
+ * `sample_count` samples (-1 if the count is out of range). */
+int64_t vct_cone_trace_fast_scratch_bytes(int64_t sample_count);
+
+/* VoxelConeTracingPass::onUpdate (VFS/RenderPass/Clipmap/VoxelConeTracingPass.cpp:75-106),
+ * GB300 form: samples visited in Morton order, diffuse cones compacted per
+ * warp, specular cones bucketed by roughness, the clipmap sampled through
+ * `radiance` (hardware trilinear filter), FP32 compositing.  Same inputs and
+ * outputs as vct_cone_trace; `scratch` is 256-byte aligned device memory of
+ * at least vct_cone_trace_fast_scratch_bytes(sample_count) bytes. */
+int vct_cone_trace_fast(const vct_cone_tracing_desc* desc, const vct_cam_matrix* cam, vct_texture radiance,
+                        const vct_shadow_map* shadow, const vct_directional_light_desc* light,
+                        const vct_directional_light_shadow_desc* light_shadow,
+                        const vct_surface_sample* samples, int64_t sample_count,
+                        float* diffuse_out, float* specular_out, unsigned long long* cone_steps,
+                        void* scratch, size_t scratch_bytes, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

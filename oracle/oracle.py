@@ -64,6 +64,7 @@ def lib():
         L.vcto_cone_trace_f4.restype = C.c_uint64
         L.vcto_cone_trace_f4.argtypes = [P, P, P, C.c_int, P, C.c_int, C.c_int, P, P, P, C.c_int64, C.c_int64,
                                          P, P]
+        L.vcto_downsample_f4.argtypes = [P, C.c_int, P, C.c_int, C.c_int, C.c_int]
         L.vcto_procedural_atlas.argtypes = [P, C.c_int64, C.c_uint32, C.c_double]
         _L = L
     return _L
@@ -119,6 +120,17 @@ def procedural_atlas(R: int, seed: int = 3, fill: float = 0.05) -> np.ndarray:
     out = np.empty(shape, np.uint32)
     lib().vcto_procedural_atlas(_p(out), out.size, seed & 0xFFFFFFFF, fill)
     return out
+
+
+def downsample_f4(atlas4: np.ndarray, R: int, prev_min, level: int, mode: int, band: int = 10) -> None:
+    """One level on float4 storage with FP64 arithmetic (reference for the RGBA16F mips)."""
+    assert atlas4.dtype == np.float32
+    lib().vcto_downsample_f4(_p(atlas4), R, _p(np.asarray(prev_min, np.int32)), level, band, mode)
+
+
+def rgba8_to_f4(atlas: np.ndarray) -> np.ndarray:
+    a = atlas.astype(np.uint32)
+    return (np.stack([(a >> (8 * c)) & 0xFF for c in range(4)], -1).astype(np.float32) / np.float32(255.0))
 
 
 def default_light_bytes() -> bytes:

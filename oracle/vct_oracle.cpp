@@ -35,6 +35,10 @@ void vcto_downsample(uint32_t* atlas, int R, const int prev_min[3], int level, i
     downsample(atlas, R, prev_min, level, band, mode);
 }
 
+void vcto_downsample_f4(float* atlas4, int R, const int prev_min[3], int level, int band, int mode) {
+    downsample_f4<double>(atlas4, R, prev_min, level, band, mode);
+}
+
 // Cone trace over an RGBA8 atlas.  precision: 32 = FP32 mirror, 64 = FP64.
 // Samples [begin, end) are traced; outputs are 4 doubles per sample.
 // Returns the number of traceCone loop iterations executed.

@@ -30,6 +30,9 @@ DOWNSAMPLE_RADIANCE = 1
 
 MODE_GI_OUTPUT = 8
 
+TEX_RGBA8 = 0
+TEX_RGBA16F = 1
+
 f3 = C.c_float * 3
 f4 = C.c_float * 4
 f16 = C.c_float * 16
@@ -119,6 +122,13 @@ _SIGS: dict[str, tuple] = {
     "vct_downsample_all": (C.c_int, [P, P, C.c_int32, C.c_int32, P]),
     "vct_wrap_border": (C.c_int, [P, P, P]),
     "vct_cone_trace": (C.c_int, [P, P, P, C.c_int32, P, P, P, P, C.c_int64, P, P, P, P]),
+    "vct_texture_create": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
+    "vct_texture_update": (C.c_int, [P, P, P]),
+    "vct_texture_destroy": (C.c_int, [P]),
+    "vct_atlas_rgba8_to_rgba16f": (C.c_int, [P, P, C.c_int32, P]),
+    "vct_downsample_rgba16f": (C.c_int, [P, P, C.c_int32, P]),
+    "vct_cone_trace_fast_scratch_bytes": (C.c_int64, [C.c_int64]),
+    "vct_cone_trace_fast": (C.c_int, [P, P, P, P, P, P, P, C.c_int64, P, P, P, P, C.c_size_t, P]),
 }
 
 

@@ -113,3 +113,94 @@ def cone_trace(desc: capi.ConeTracingDesc, eye, radiance: torch.Tensor, R: int, 
     capi.call("vct_cone_trace", capi.ref(desc), capi.ref(cam), _ptr(radiance), R, capi.ref(sm), capi.ref(light),
               capi.ref(sd), _ptr(samples), n, _ptr(diffuse), _ptr(specular), _ptr(steps), _stream())
     return diffuse, specular
+
+
+# ----------------------------------------------------------------- fast form
+
+class RadianceTexture:
+    """Hardware-filtered copy of a radiance atlas (vct_texture_*): RGBA8 or RGBA16F."""
+
+    def __init__(self, R: int, fmt: int = capi.TEX_RGBA8):
+        self.R = R
+        self.fmt = fmt
+        h = C.c_void_p()
+        capi.call("vct_texture_create", R, fmt, C.byref(h))
+        self.handle = h
+
+    def update(self, atlas: torch.Tensor) -> "RadianceTexture":
+        capi.call("vct_texture_update", self.handle, _ptr(atlas), _stream())
+        return self
+
+    def close(self) -> None:
+        if self.handle:
+            capi.call("vct_texture_destroy", self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def new_atlas_rgba16f(R: int, device="cuda") -> torch.Tensor:
+    """Zeroed RGBA16F atlas: 4 halves per texel, shape (R+2, 6(R+2), 6(R+2)*4) as int16."""
+    d, h, w = atlas_shape(R)
+    return torch.zeros((d, h, w * 4), dtype=torch.int16, device=device)
+
+
+def to_rgba16f(atlas: torch.Tensor, R: int, out: torch.Tensor | None = None) -> torch.Tensor:
+    out = new_atlas_rgba16f(R, atlas.device) if out is None else out
+    capi.call("vct_atlas_rgba8_to_rgba16f", _ptr(atlas), _ptr(out), R, _stream())
+    return out
+
+
+def cmd_downsample_rgba16f(atlas16: torch.Tensor, R: int, prev_region_min, level: int, mode: int,
+                           band: int = capi.DOWNSAMPLE_REGION_SIZE) -> None:
+    d = capi.DownSampleDesc(capi.i3(*prev_region_min), level, R, band)
+    capi.call("vct_downsample_rgba16f", _ptr(atlas16), capi.ref(d), mode, _stream())
+
+
+def cmd_downsample_rgba16f_all(atlas16: torch.Tensor, R: int, regions, mode: int) -> None:
+    for level in range(1, 6):
+        prev = regions[level - 1].min_corner
+        cmd_downsample_rgba16f(atlas16, R, (prev[0], prev[1], prev[2]), level, mode)
+
+
+def fast_scratch(n: int, device="cuda") -> torch.Tensor:
+    nbytes = capi.lib().vct_cone_trace_fast_scratch_bytes(n)
+    if nbytes < 0:
+        raise ValueError(f"sample count {n} out of range")
+    return torch.empty(nbytes + 256, dtype=torch.uint8, device=device)
+
+
+def _aligned(t: torch.Tensor, align: int = 256) -> int:
+    p = t.data_ptr()
+    return (p + align - 1) // align * align
+
+
+def cone_trace_fast(desc: capi.ConeTracingDesc, eye, tex: RadianceTexture, samples: torch.Tensor,
+                    light: capi.DirectionalLightDesc | None = None, shadow: torch.Tensor | None = None,
+                    shadow_desc: capi.DirectionalLightShadowDesc | None = None,
+                    diffuse: torch.Tensor | None = None, specular: torch.Tensor | None = None,
+                    steps: torch.Tensor | None = None, scratch: torch.Tensor | None = None):
+    """GB300 form of VoxelConeTracingPass: same inputs/outputs as cone_trace, sampling `tex`."""
+    n = samples.shape[0]
+    if diffuse is None:
+        diffuse = torch.zeros((n, 4), dtype=torch.float32, device=samples.device)
+    if specular is None:
+        specular = torch.zeros((n, 4), dtype=torch.float32, device=samples.device)
+    if scratch is None:
+        scratch = fast_scratch(n, samples.device)
+    base = _aligned(scratch)
+    avail = scratch.data_ptr() + scratch.numel() - base
+    cam = cam_matrix(eye)
+    light = light or capi.DirectionalLightDesc(capi.f3(0.3, -1.0, 0.2), 1.0, capi.f3(1, 1, 1), 0)
+    sm = capi.ShadowMap(None, 0, 0)
+    if shadow is not None:
+        sm = capi.ShadowMap(shadow.data_ptr(), shadow.shape[1], shadow.shape[0])
+    sd = shadow_desc or capi.DirectionalLightShadowDesc()
+    capi.call("vct_cone_trace_fast", capi.ref(desc), capi.ref(cam), tex.handle, capi.ref(sm), capi.ref(light),
+              capi.ref(sd), _ptr(samples), n, _ptr(diffuse), _ptr(specular), _ptr(steps), C.c_void_p(base),
+              avail, _stream())
+    return diffuse, specular

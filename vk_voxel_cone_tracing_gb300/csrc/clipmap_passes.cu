@@ -228,7 +228,7 @@ extern "C" int vct_downsample(uint32_t* atlas, const vct_downsample_desc* d, int
     VCT_CHECK_ARG(valid_resolution(d->clipmap_resolution), "vct_downsample: resolution must be a power of two in [8,1024]");
     VCT_CHECK_ARG(d->clip_level >= 1 && d->clip_level < VCT_CLIP_LEVEL_COUNT, "vct_downsample: clip level must be 1..5");
     VCT_CHECK_ARG(mode == VCT_DOWNSAMPLE_OPACITY || mode == VCT_DOWNSAMPLE_RADIANCE, "vct_downsample: bad mode");
-    VCT_CHECK_ARG(d->downsample_region_size >= 0 && d->downsample_region_size < (d->clipmap_resolution >> 2),
+    VCT_CHECK_ARG(d->downsample_region_size >= 0 && d->downsample_region_size <= 4096,
                   "vct_downsample: downsample band out of range");
     AtlasDims A(d->clipmap_resolution);
     const int half = A.R >> 1;

@@ -1,0 +1,210 @@
+// textures.cu -- hardware-filtered 3D texture of the radiance clipmap, and the
+// FP16-storage atlas kernels (RGBA8 -> RGBA16F conversion, anisotropic
+// downsample with FP32 arithmetic and RGBA16F storage).
+//
+// The fast cone tracer samples the atlas through a CUDA texture object: a 3D
+// cudaArray with normalized coordinates, WRAP addressing and linear
+// filtering -- the same sampler state as the reference's VoxelSampler
+// (VFS/RenderPass/Clipmap/Voxelizer.cpp:279: REPEAT, LINEAR, one mip level).
+#include <cuda_fp16.h>
+
+#include "common.cuh"
+
+struct vct_texture_s {
+    int R = 0;
+    int format = 0;
+    cudaArray_t array = nullptr;
+    cudaTextureObject_t tex = 0;
+};
+
+namespace vct {
+
+cudaTextureObject_t texture_object(const vct_texture_s* t) { return t->tex; }
+int texture_resolution(const vct_texture_s* t) { return t->R; }
+int texture_format(const vct_texture_s* t) { return t->format; }
+
+__device__ __forceinline__ uint16_t h_bits(float x) { return __half_as_ushort(__float2half_rn(x)); }
+__device__ __forceinline__ float h_val(uint16_t b) { return __half2float(__ushort_as_half(b)); }
+
+__global__ void k_rgba8_to_rgba16f(const uint32_t* __restrict__ src, uint2* __restrict__ dst, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        float4 c = unpack_rgba8(__ldg(src + i));
+        uint2 o;
+        o.x = (uint32_t)h_bits(c.x) | ((uint32_t)h_bits(c.y) << 16);
+        o.y = (uint32_t)h_bits(c.z) | ((uint32_t)h_bits(c.w) << 16);
+        dst[i] = o;
+    }
+}
+
+__device__ __forceinline__ int ds_wrap16(int p, int R) { return (p + R * (abs(p / R) + 1)) & (R - 1); }
+
+__constant__ int c_pairs16[6][4][2] = {
+    {{0, 1}, {2, 3}, {4, 5}, {6, 7}}, {{1, 0}, {3, 2}, {5, 4}, {7, 6}}, {{0, 2}, {1, 3}, {4, 6}, {5, 7}},
+    {{2, 0}, {3, 1}, {6, 4}, {7, 5}}, {{0, 4}, {1, 5}, {2, 6}, {3, 7}}, {{4, 0}, {5, 1}, {6, 2}, {7, 3}}};
+
+__device__ __forceinline__ float4 load_h4(const uint2* p, int64_t i) {
+    uint2 v = p[i];
+    return make_float4(h_val(v.x & 0xffff), h_val(v.x >> 16), h_val(v.y & 0xffff), h_val(v.y >> 16));
+}
+__device__ __forceinline__ void store_h4(uint2* p, int64_t i, float4 c) {
+    uint2 o;
+    o.x = (uint32_t)h_bits(c.x) | ((uint32_t)h_bits(c.y) << 16);
+    o.y = (uint32_t)h_bits(c.z) | ((uint32_t)h_bits(c.w) << 16);
+    p[i] = o;
+}
+
+// Same composite and band blend as the RGBA8 downsample (opacityDownSample.comp /
+// radianceDownSample.comp), FP32 arithmetic, RGBA16F storage.
+template <int MODE>
+__global__ void k_downsample_f16(uint2* __restrict__ atlas, AtlasDims A, int3 pmin, int level, int band) {
+    const int half = A.R >> 1;
+    const int64_t n = (int64_t)half * half * half;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        const int g[3] = {(int)(t % half), (int)((t / half) % half), (int)(t / ((int64_t)half * half))};
+        const int pm[3] = {pmin.x, pmin.y, pmin.z};
+        int cur[3], wpos[3], ps[3];
+        float dist[3];
+        bool any_ge = false;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            cur[a] = (pm[a] >> 1) + g[a];
+            wpos[a] = ds_wrap16(cur[a], A.R) + 1;
+            ps[a] = ds_wrap16(cur[a] << 1, A.R) + 1;
+            float center = (float)(pm[a] >> 1) + (float)(half >> 1);
+            dist[a] = fabsf((float)cur[a] + 0.5f - center) - 0.5f;
+            any_ge |= dist[a] >= (float)((half >> 1) - band);
+        }
+        wpos[1] += A.rb * level;
+        ps[1] += A.rb * (level - 1);
+        float lerp = 0.0f;
+        if (any_ge)
+            lerp = (fmaxf(dist[0], fmaxf(dist[1], dist[2])) - (float)((half >> 1) - band) + 1.0f) *
+                   (1.0f / ((float)band + 1.0f));
+        for (int f = 0; f < 6; ++f) {
+            float4 v[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+                v[i] = load_h4(atlas, A.index(ps[0] + (i & 1) + A.rb * f, ps[1] + ((i >> 1) & 1), ps[2] + ((i >> 2) & 1)));
+            const int64_t wi = A.index(wpos[0] + A.rb * f, wpos[1], wpos[2]);
+            float4 own = load_h4(atlas, wi);
+            float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float4 a0 = v[c_pairs16[f][k][0]], a1 = v[c_pairs16[f][k][1]];
+                const float tt = 1.0f - a0.w;
+                if (MODE == 0) {
+                    s.w += a0.w + tt * a1.w;
+                } else {
+                    s.x += a0.x + tt * a1.x;
+                    s.y += a0.y + tt * a1.y;
+                    s.z += a0.z + tt * a1.z;
+                    s.w += a0.w + tt * a1.w;
+                }
+            }
+            if (MODE == 0) {
+                float a = s.w * 0.25f * (1.0f - lerp) + own.x * lerp;
+                own.w = a;
+                own.y = a;
+                store_h4(atlas, wi, own);
+            } else {
+                float4 o = make_float4(s.x * 0.25f * (1.0f - lerp) + own.x * lerp, s.y * 0.25f * (1.0f - lerp) + own.y * lerp,
+                                       s.z * 0.25f * (1.0f - lerp) + own.z * lerp, s.w * 0.25f * (1.0f - lerp) + own.w * lerp);
+                store_h4(atlas, wi, o);
+            }
+        }
+    }
+}
+
+static int grid_for16(int64_t n, int block) {
+    int64_t g = (n + block - 1) / block;
+    return (int)(g > 152 * 64 ? 152 * 64 : (g < 1 ? 1 : g));
+}
+
+}  // namespace vct
+
+using namespace vct;
+
+extern "C" int vct_texture_create(int32_t R, int32_t format, vct_texture_s** out) {
+    VCT_CHECK_ARG(out, "vct_texture_create: null output handle");
+    *out = nullptr;
+    VCT_CHECK_ARG(valid_resolution(R), "vct_texture_create: resolution must be a power of two in [8,1024]");
+    VCT_CHECK_ARG(format == 0 || format == 1, "vct_texture_create: format must be VCT_TEX_RGBA8 or VCT_TEX_RGBA16F");
+    AtlasDims A(R);
+    auto* t = new vct_texture_s();
+    t->R = R;
+    t->format = format;
+    cudaChannelFormatDesc ch = format == 0 ? cudaCreateChannelDesc<uchar4>() : cudaCreateChannelDescHalf4();
+    cudaError_t e = cudaMalloc3DArray(&t->array, &ch, make_cudaExtent(A.W, A.H, A.D));
+    if (e != cudaSuccess) {
+        delete t;
+        return cuda_fail(e, "cudaMalloc3DArray (radiance texture)");
+    }
+    cudaResourceDesc rd = {};
+    rd.resType = cudaResourceTypeArray;
+    rd.res.array.array = t->array;
+    cudaTextureDesc td = {};
+    td.addressMode[0] = td.addressMode[1] = td.addressMode[2] = cudaAddressModeWrap;
+    td.filterMode = cudaFilterModeLinear;
+    td.readMode = format == 0 ? cudaReadModeNormalizedFloat : cudaReadModeElementType;
+    td.normalizedCoords = 1;
+    e = cudaCreateTextureObject(&t->tex, &rd, &td, nullptr);
+    if (e != cudaSuccess) {
+        cudaFreeArray(t->array);
+        delete t;
+        return cuda_fail(e, "cudaCreateTextureObject (radiance texture)");
+    }
+    *out = t;
+    return VCT_OK;
+}
+
+extern "C" int vct_texture_update(vct_texture_s* t, const void* atlas, void* stream) {
+    VCT_CHECK_ARG(t && atlas, "vct_texture_update: null argument");
+    AtlasDims A(t->R);
+    const size_t texel = t->format == 0 ? 4 : 8;
+    cudaMemcpy3DParms p = {};
+    p.srcPtr = make_cudaPitchedPtr(const_cast<void*>(atlas), A.W * texel, A.W, A.H);
+    p.dstArray = t->array;
+    p.extent = make_cudaExtent(A.W, A.H, A.D);
+    p.kind = cudaMemcpyDeviceToDevice;
+    VCT_CUDA_TRY(cudaMemcpy3DAsync(&p, as_stream(stream)));
+    return VCT_OK;
+}
+
+extern "C" int vct_texture_destroy(vct_texture_s* t) {
+    if (!t) return VCT_OK;
+    cudaError_t e1 = cudaDestroyTextureObject(t->tex);
+    cudaError_t e2 = cudaFreeArray(t->array);
+    delete t;
+    if (e1 != cudaSuccess) return cuda_fail(e1, "cudaDestroyTextureObject");
+    if (e2 != cudaSuccess) return cuda_fail(e2, "cudaFreeArray");
+    return VCT_OK;
+}
+
+extern "C" int vct_atlas_rgba8_to_rgba16f(const uint32_t* src, uint16_t* dst, int32_t R, void* stream) {
+    VCT_CHECK_ARG(src && dst && valid_resolution(R), "vct_atlas_rgba8_to_rgba16f: bad argument");
+    VCT_CHECK_ARG(((uintptr_t)dst & 7) == 0, "vct_atlas_rgba8_to_rgba16f: destination must be 8-byte aligned");
+    const int64_t n = AtlasDims(R).texels();
+    k_rgba8_to_rgba16f<<<grid_for16(n, 256), 256, 0, as_stream(stream)>>>(src, reinterpret_cast<uint2*>(dst), n);
+    VCT_LAUNCH_CHECK();
+    return VCT_OK;
+}
+
+extern "C" int vct_downsample_rgba16f(uint16_t* atlas, const vct_downsample_desc* d, int32_t mode, void* stream) {
+    VCT_CHECK_ARG(atlas && d, "vct_downsample_rgba16f: null argument");
+    VCT_CHECK_ARG(((uintptr_t)atlas & 7) == 0, "vct_downsample_rgba16f: atlas must be 8-byte aligned");
+    VCT_CHECK_ARG(valid_resolution(d->clipmap_resolution), "vct_downsample_rgba16f: bad resolution");
+    VCT_CHECK_ARG(d->clip_level >= 1 && d->clip_level < VCT_CLIP_LEVEL_COUNT, "vct_downsample_rgba16f: clip level must be 1..5");
+    VCT_CHECK_ARG(mode == 0 || mode == 1, "vct_downsample_rgba16f: bad mode");
+    VCT_CHECK_ARG(d->downsample_region_size >= 0 && d->downsample_region_size <= 4096, "vct_downsample_rgba16f: bad band");
+    AtlasDims A(d->clipmap_resolution);
+    const int half = A.R >> 1;
+    const int64_t n = (int64_t)half * half * half;
+    int3 pm = make_int3(d->prev_region_min_corner[0], d->prev_region_min_corner[1], d->prev_region_min_corner[2]);
+    uint2* a = reinterpret_cast<uint2*>(atlas);
+    if (mode == 0)
+        k_downsample_f16<0><<<grid_for16(n, 128), 128, 0, as_stream(stream)>>>(a, A, pm, d->clip_level, d->downsample_region_size);
+    else
+        k_downsample_f16<1><<<grid_for16(n, 128), 128, 0, as_stream(stream)>>>(a, A, pm, d->clip_level, d->downsample_region_size);
+    VCT_LAUNCH_CHECK();
+    return VCT_OK;
+}

@@ -1,0 +1,426 @@
+// trace_fast.cu -- the GB300 form of voxelConeTracing.frag.
+//
+// Same pass contract and arithmetic as the exact tracer, reorganised for the
+// hardware:
+//   1. samples are visited in Morton order of their position (a 30-bit key,
+//      radix-sorted), so neighbouring lanes march through the same texels and
+//      the taps hit L1/TEX and L2 instead of HBM;
+//   2. diffuse cones are compacted per warp: the (sample, cone) pairs with
+//      cos >= 0 of 32 samples are dealt to the 32 lanes in rounds, so no lane
+//      idles on a back-facing cone; every sample's cone results are summed by
+//      its owner lane in cone order (the shader's order);
+//   3. specular cones (57..780 marching steps, depending on the aperture) run
+//      in their own kernel over a list sorted by the 8-bit roughness texel
+//      (stable, so Morton order is kept inside a bucket): the lanes of a warp
+//      march equally long cones;
+//   4. the clipmap is sampled through a 3D texture object (hardware trilinear
+//      filter, WRAP addressing = the reference's REPEAT sampler), RGBA8 or
+//      RGBA16F storage, FP32 compositing.
+// Scratch memory (sort keys, orders, cub temporary storage) is provided by
+// the caller; vct_cone_trace_fast_scratch_bytes() gives its size.
+#include <cub/cub.cuh>
+
+#include "trace_common.cuh"
+
+struct vct_texture_s;
+
+namespace vct {
+
+cudaTextureObject_t texture_object(const vct_texture_s* t);
+int texture_resolution(const vct_texture_s* t);
+int texture_format(const vct_texture_s* t);
+int fill_trace_params(TraceParams& P, const vct_cone_tracing_desc* desc, const vct_cam_matrix* cam,
+                      const vct_shadow_map* shadow, const vct_directional_light_desc* light,
+                      const vct_directional_light_shadow_desc* light_shadow);
+
+struct FastConsts {
+    float uvs, inv_uvs, min_radius, inv_min_radius, decay, start_off;
+    float coef_diffuse, sf_diffuse, aperture_diffuse;
+    float cx, cy, cz;
+    float inv_ext[kClipLevels];
+    float ax, bx, ay, az, bz;
+    float by[kClipLevels];
+    int ncones;
+    int need_diffuse, need_specular;
+};
+
+struct FastArgs {
+    TraceParams P;
+    FastConsts C;
+    cudaTextureObject_t tex;
+    const vct_surface_sample* __restrict__ samples;
+    int64_t n;
+    float* __restrict__ dout;
+    float* __restrict__ sout;
+    unsigned long long* steps;
+};
+
+__device__ __forceinline__ float4 fma4(float4 a, float s, float4 b) {
+    return make_float4(fmaf(a.x, s, b.x), fmaf(a.y, s, b.y), fmaf(a.z, s, b.z), fmaf(a.w, s, b.w));
+}
+
+// sampleClipmap at integer level l: three face taps along the cone's signs.
+__device__ __forceinline__ float4 sample_level(cudaTextureObject_t tex, const FastConsts& C, float3 p, int l, float fox,
+                                               float foy, float foz, float3 wt) {
+    const float ie = C.inv_ext[l];
+    float fx = p.x * ie, fy = p.y * ie, fz = p.z * ie;
+    fx -= floorf(fx);
+    fy -= floorf(fy);
+    fz -= floorf(fz);
+    const float sx = fmaf(fx, C.ax, C.bx), sy = fmaf(fy, C.ay, C.by[l]), sz = fmaf(fz, C.az, C.bz);
+    float4 a = tex3D<float4>(tex, sx + fox, sy, sz);
+    float4 b = tex3D<float4>(tex, sx + foy, sy, sz);
+    float4 c = tex3D<float4>(tex, sx + foz, sy, sz);
+    float4 r = make_float4(a.x * wt.x, a.y * wt.x, a.z * wt.x, a.w * wt.x);
+    r = fma4(b, wt.y, r);
+    return fma4(c, wt.z, r);
+}
+
+// traceCone (voxelConeTracing.frag:341-392); the upper-level fetch is skipped
+// when curLevel is integral (mix(x, x, 0) == x).
+__device__ __forceinline__ float4 trace_cone_fast(cudaTextureObject_t tex, const FastConsts& C, float3 start, float3 dir,
+                                                  float coef, float start_level, float step_factor,
+                                                  unsigned long long& steps) {
+    float4 result = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float uvs = C.uvs;
+    float vs = uvs * exp2f(start_level);
+    const float off = vs * C.start_off * 0.5f;
+    start = f3(fmaf(dir.x, off, start.x), fmaf(dir.y, off, start.y), fmaf(dir.z, off, start.z));
+    float step = 0.0f, diameter = uvs, occlusion = 0.0f, seg = vs;
+    const float fox = dir.x > 0.0f ? 0.0f : 1.0f / 6.0f;
+    const float foy = dir.y > 0.0f ? 2.0f / 6.0f : 3.0f / 6.0f;
+    const float foz = dir.z > 0.0f ? 4.0f / 6.0f : 5.0f / 6.0f;
+    const float3 wt = f3(dir.x * dir.x, dir.y * dir.y, dir.z * dir.z);
+    unsigned int it = 0;
+    while (step < kMaxTraceDistance && occlusion < 1.0f) {
+        ++it;
+        const float3 pos = f3(fmaf(dir.x, step, start.x), fmaf(dir.y, step, start.y), fmaf(dir.z, step, start.z));
+        const float dx = C.cx - pos.x, dy = C.cy - pos.y, dz = C.cz - pos.z;
+        const float dist = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+        const float min_level = ceilf(log2f(dist * C.inv_min_radius));
+        float cl = log2f(diameter * C.inv_uvs);
+        cl = fminf(fmaxf(fmaxf(start_level, cl), min_level), (float)(kClipLevels - 1));
+        const float flo = floorf(cl);
+        const int lo = (int)flo;
+        const float fr = cl - flo;
+        float4 s = sample_level(tex, C, pos, lo, fox, foy, foz, wt);
+        if (fr > 0.0f) {
+            const float4 h = sample_level(tex, C, pos, lo + 1, fox, foy, foz, wt);
+            s = make_float4(fmaf(h.x - s.x, fr, s.x), fmaf(h.y - s.y, fr, s.y), fmaf(h.z - s.z, fr, s.z),
+                            fmaf(h.w - s.w, fr, s.w));
+        }
+        vs = uvs * exp2f(cl);
+        const float corr = __fdividef(seg, vs);
+        const float opacity = __saturatef(1.0f - exp2f(corr * __log2f(1.0f - s.w)));
+        const float k = __saturatef(1.0f - result.w);
+        result = make_float4(fmaf(k * s.x, corr, result.x), fmaf(k * s.y, corr, result.y),
+                             fmaf(k * s.z, corr, result.z), fmaf(k, opacity, result.w));
+        occlusion = fmaf(1.0f - occlusion, __fdividef(opacity, fmaf(step + vs, C.decay, 1.0f)), occlusion);
+        const float prev = step;
+        step = fmaf(fmaxf(diameter, uvs), step_factor, step);
+        seg = step - prev;
+        diameter = step * coef;
+    }
+    steps += it;
+    return make_float4(result.x, result.y, result.z, 1.0f - occlusion);
+}
+
+// 30-bit Morton key of the sample position in level-0 voxels around the volume centre.
+__device__ __forceinline__ uint32_t spread10(uint32_t v) {
+    v &= 0x3ffu;
+    v = (v | (v << 16)) & 0x030000FFu;
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+__global__ void k_morton_keys(const vct_surface_sample* __restrict__ s, int64_t n, FastConsts C,
+                              uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float* p = s[i].position;
+        const float q = 0.5f * C.inv_uvs;  // two level-0 voxels per cell
+        int x = __float2int_rd((p[0] - C.cx) * q) + 512, y = __float2int_rd((p[1] - C.cy) * q) + 512,
+            z = __float2int_rd((p[2] - C.cz) * q) + 512;
+        x = min(max(x, 0), 1023);
+        y = min(max(y, 0), 1023);
+        z = min(max(z, 0), 1023);
+        keys[i] = spread10(x) | (spread10(y) << 1) | (spread10(z) << 2);
+        vals[i] = (uint32_t)i;
+    }
+}
+
+constexpr int kWarpsPerBlock = 8;
+
+__global__ void __launch_bounds__(256) k_trace_diffuse(FastArgs A, const uint32_t* __restrict__ order,
+                                                       uint32_t* __restrict__ spec_key,
+                                                       unsigned int* __restrict__ spec_count) {
+    __shared__ float4 s_start[kWarpsPerBlock][32];
+    __shared__ float4 s_norm[kWarpsPerBlock][32];
+    __shared__ int s_incl[kWarpsPerBlock][32];
+    __shared__ uint32_t s_mask[kWarpsPerBlock][32];
+    __shared__ float4 s_res[kWarpsPerBlock][32];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const TraceParams& P = A.P;
+    const FastConsts& C = A.C;
+    const bool c32 = C.ncones == 32;
+    unsigned long long steps = 0;
+    const int64_t nwarps = (int64_t)gridDim.x * kWarpsPerBlock;
+    for (int64_t base = ((int64_t)blockIdx.x * kWarpsPerBlock + w) * 32; base < A.n; base += nwarps * 32) {
+        const int64_t pos = base + lane;
+        bool valid = pos < A.n;
+        const uint32_t idx = valid ? __ldg(order + pos) : 0u;
+        GSample g;
+        float min_level = 0.0f;
+        float3 start = f3(0.f, 0.f, 0.f);
+        uint32_t mask = 0;
+        if (valid) {
+            g = load_sample(A.samples + idx, P.eye);
+            valid = g.depth != 1.0f;
+        }
+        if (valid) {
+            min_level = calc_min_level(P.d, g.wp);
+            const float vs = C.uvs * exp2f(min_level);
+            start = g.wp + g.normal * (vs * C.start_off);
+            if (C.need_diffuse)
+                for (int c = 0; c < C.ncones; ++c) {
+                    const float3 dir = c32 ? f3(c_dirs32[c][0], c_dirs32[c][1], c_dirs32[c][2])
+                                           : f3(c_dirs16[c][0], c_dirs16[c][1], c_dirs16[c][2]);
+                    if (!(dot3(g.normal, dir) < 0.0f)) mask |= 1u << c;
+                }
+        }
+        const int cnt = __popc(mask);
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        const int excl = incl - cnt;
+        s_start[w][lane] = make_float4(start.x, start.y, start.z, min_level);
+        s_norm[w][lane] = valid ? make_float4(g.normal.x, g.normal.y, g.normal.z, 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
+        s_incl[w][lane] = incl;
+        s_mask[w][lane] = mask;
+        __syncwarp();
+        float4 acc = make_float4(0.f, 0.f, 0.f, 1.f);
+        for (int r0 = 0; r0 < total; r0 += 32) {
+            const int k = r0 + lane;
+            float4 res = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (k < total) {
+                int lo = 0, hi = 31;  // first lane with incl > k
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (s_incl[w][mid] > k) hi = mid;
+                    else lo = mid + 1;
+                }
+                const uint32_t m = s_mask[w][lo];
+                const int j = k - (s_incl[w][lo] - __popc(m));
+                const int cone = (int)__fns(m, 0, j + 1);
+                const float3 dir = c32 ? f3(c_dirs32[cone][0], c_dirs32[cone][1], c_dirs32[cone][2])
+                                       : f3(c_dirs16[cone][0], c_dirs16[cone][1], c_dirs16[cone][2]);
+                const float4 st = s_start[w][lo];
+                const float4 nn = s_norm[w][lo];
+                const float cos_t = nn.x * dir.x + nn.y * dir.y + nn.z * dir.z;
+                const float4 r =
+                    trace_cone_fast(A.tex, C, f3(st.x, st.y, st.z), dir, C.coef_diffuse, st.w, C.sf_diffuse, steps);
+                res = make_float4(r.x * cos_t, r.y * cos_t, r.z * cos_t, r.w * cos_t);
+            }
+            s_res[w][lane] = res;
+            __syncwarp();
+            const int a = max(excl, r0), b = min(incl, r0 + 32);
+            for (int q = a; q < b; ++q) {
+                const float4 v = s_res[w][q - r0];
+                acc = make_float4(acc.x + v.x, acc.y + v.y, acc.z + v.z, acc.w + v.w);
+            }
+            __syncwarp();
+        }
+        bool spec = false;
+        if (valid) {
+            const vct_cone_tracing_desc& d = P.d;
+            const float inv_n = 1.0f / (float)C.ncones;
+            float4 ind = make_float4(acc.x * inv_n, acc.y * inv_n, acc.z * inv_n, acc.w * inv_n);
+            ind.w = ind.w * d.ambient_occlusion_factor;
+            ind.x = ind.x * (g.diffuse_color.x * d.indirect_diffuse_intensity);
+            ind.y = ind.y * (g.diffuse_color.y * d.indirect_diffuse_intensity);
+            ind.z = ind.z * (g.diffuse_color.z * d.indirect_diffuse_intensity);
+            const float3 direct = direct_term(P, g);
+            spec = C.need_specular && has_specular_cone(g);
+            float4 dd[2];
+            write_outputs(P, g, min_level, ind, f3(0.f, 0.f, 0.f), direct, reinterpret_cast<float*>(&dd[0]),
+                          reinterpret_cast<float*>(&dd[1]));
+            reinterpret_cast<float4*>(A.dout)[idx] = dd[0];
+            if (!spec) reinterpret_cast<float4*>(A.sout)[idx] = dd[1];
+        }
+        if (pos < A.n) spec_key[pos] = spec ? (uint32_t)__float2uint_rn(g.roughness * 255.0f) : 256u;
+        const unsigned bal = __ballot_sync(0xffffffffu, spec);
+        if (lane == 0 && bal) atomicAdd(spec_count, (unsigned)__popc(bal));
+    }
+    if (A.steps) {
+        for (int o = 16; o > 0; o >>= 1) steps += __shfl_xor_sync(0xffffffffu, steps, o);
+        if (lane == 0 && steps) atomicAdd(A.steps, steps);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_trace_specular(FastArgs A, const uint32_t* __restrict__ list,
+                                                        const unsigned int* __restrict__ spec_count) {
+    const TraceParams& P = A.P;
+    const FastConsts& C = A.C;
+    const int64_t m = *spec_count;
+    unsigned long long steps = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t idx = __ldg(list + i);
+        const GSample g = load_sample(A.samples + idx, P.eye);
+        const float min_level = calc_min_level(P.d, g.wp);
+        const float vs = C.uvs * exp2f(min_level);
+        const float3 start = g.wp + g.normal * (vs * C.start_off);
+        const float3 sdir = reflect3(f3(-g.view.x, -g.view.y, -g.view.z), g.normal);
+        const float ap = fmaxf(g.roughness, kMinSpecularAperture);
+        const float coef = 2.0f * tanf(ap * 0.5f);
+        const float4 r = trace_cone_fast(A.tex, C, start, sdir, coef, min_level, C.uvs, steps);
+        const float isi = P.d.indirect_specular_intensity;
+        reinterpret_cast<float4*>(A.sout)[idx] =
+            make_float4(r.x * g.specular_color.x * isi, r.y * g.specular_color.y * isi,
+                        r.z * g.specular_color.z * isi, 1.0f);
+    }
+    if (A.steps) {
+        for (int o = 16; o > 0; o >>= 1) steps += __shfl_xor_sync(0xffffffffu, steps, o);
+        if ((threadIdx.x & 31) == 0 && steps) atomicAdd(A.steps, steps);
+    }
+}
+
+// ------------------------------------------------------------- scratch layout
+struct FastScratch {
+    uint32_t *keys_in, *keys_out, *vals_in, *order, *spec_key, *spec_key_out, *spec_list;
+    unsigned int* spec_count;
+    void* temp;
+    size_t temp_bytes;
+    size_t total;
+};
+
+static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+static int plan_scratch(int64_t n, void* base, FastScratch& s) {
+    size_t t1 = 0, t2 = 0;
+    cudaError_t e = cub::DeviceRadixSort::SortPairs(nullptr, t1, (uint32_t*)nullptr, (uint32_t*)nullptr,
+                                                    (uint32_t*)nullptr, (uint32_t*)nullptr, (int)n, 0, 30);
+    if (e != cudaSuccess) return cuda_fail(e, "cub::DeviceRadixSort::SortPairs (size query)");
+    e = cub::DeviceRadixSort::SortPairs(nullptr, t2, (uint32_t*)nullptr, (uint32_t*)nullptr, (uint32_t*)nullptr,
+                                        (uint32_t*)nullptr, (int)n, 0, 9);
+    if (e != cudaSuccess) return cuda_fail(e, "cub::DeviceRadixSort::SortPairs (size query)");
+    const size_t arr = align256(sizeof(uint32_t) * (size_t)n);
+    char* p = (char*)base;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        char* q = p ? p + off : nullptr;
+        off += align256(bytes);
+        return q;
+    };
+    s.keys_in = (uint32_t*)take(arr);
+    s.keys_out = (uint32_t*)take(arr);
+    s.vals_in = (uint32_t*)take(arr);
+    s.order = (uint32_t*)take(arr);
+    s.spec_key = (uint32_t*)take(arr);
+    s.spec_key_out = (uint32_t*)take(arr);
+    s.spec_list = (uint32_t*)take(arr);
+    s.spec_count = (unsigned int*)take(256);
+    s.temp_bytes = t1 > t2 ? t1 : t2;
+    s.temp = take(s.temp_bytes);
+    s.total = off;
+    return VCT_OK;
+}
+
+static void fill_fast_consts(FastConsts& C, const vct_cone_tracing_desc& d) {
+    C.uvs = d.voxel_size;
+    C.inv_uvs = 1.0f / d.voxel_size;
+    C.min_radius = d.voxel_size * d.volume_dimension * 0.5f;
+    C.inv_min_radius = 1.0f / C.min_radius;
+    C.decay = d.occlusion_decay;
+    C.start_off = d.trace_start_offset;
+    const bool c32 = d.enable_32_cones != 0;
+    C.ncones = c32 ? 32 : 16;
+    C.aperture_diffuse = c32 ? kAperture32 : kAperture16;
+    C.coef_diffuse = 2.0f * tanf(C.aperture_diffuse * 0.5f);
+    C.sf_diffuse = d.min_trace_step_factor > kMinTraceStepFactor ? d.min_trace_step_factor : kMinTraceStepFactor;
+    C.cx = d.volume_center[0];
+    C.cy = d.volume_center[1];
+    C.cz = d.volume_center[2];
+    const float dim = d.volume_dimension;
+    for (int l = 0; l < kClipLevels; ++l) C.inv_ext[l] = 1.0f / (d.voxel_size * exp2f((float)l) * dim);
+    // sx = ((f*dim + 1)/(dim+2))/6, sy = (((f*dim + 1)/(dim+2)) + l)/6, sz = (f*dim + 1)/(dim+2)
+    C.ax = dim / ((dim + 2.0f) * 6.0f);
+    C.bx = 1.0f / ((dim + 2.0f) * 6.0f);
+    C.ay = C.ax;
+    for (int l = 0; l < kClipLevels; ++l) C.by[l] = (1.0f / (dim + 2.0f) + (float)l) / 6.0f;
+    C.az = dim / (dim + 2.0f);
+    C.bz = 1.0f / (dim + 2.0f);
+    const uint32_t mode = d.rendering_mode;
+    C.need_diffuse = (mode == 4 || mode == 5 || mode == 7 || mode > 8 || mode == 8) ? 1 : 0;
+    C.need_specular = (mode == 6 || mode >= 8) ? 1 : 0;
+}
+
+}  // namespace vct
+
+using namespace vct;
+
+extern "C" int64_t vct_cone_trace_fast_scratch_bytes(int64_t n) {
+    if (n < 0 || n > 0x7fffffffLL) return -1;
+    FastScratch s;
+    if (plan_scratch(n < 1 ? 1 : n, nullptr, s) != VCT_OK) return -1;
+    return (int64_t)s.total;
+}
+
+extern "C" int vct_cone_trace_fast(const vct_cone_tracing_desc* desc, const vct_cam_matrix* cam,
+                                   vct_texture_s* radiance, const vct_shadow_map* shadow,
+                                   const vct_directional_light_desc* light,
+                                   const vct_directional_light_shadow_desc* light_shadow,
+                                   const vct_surface_sample* samples, int64_t n, float* dout, float* sout,
+                                   unsigned long long* cone_steps, void* scratch, size_t scratch_bytes,
+                                   void* stream) {
+    VCT_CHECK_ARG(radiance, "vct_cone_trace_fast: null radiance texture");
+    VCT_CHECK_ARG(n >= 0 && n <= 0x7fffffffLL, "vct_cone_trace_fast: sample count out of range");
+    if (n == 0) return VCT_OK;
+    VCT_CHECK_ARG(samples && dout && sout, "vct_cone_trace_fast: null sample or output buffer");
+    VCT_CHECK_ARG(((uintptr_t)samples & 15) == 0 && ((uintptr_t)dout & 15) == 0 && ((uintptr_t)sout & 15) == 0,
+                  "vct_cone_trace_fast: sample/output buffers must be 16-byte aligned");
+    VCT_CHECK_ARG(scratch && ((uintptr_t)scratch & 255) == 0, "vct_cone_trace_fast: scratch must be 256-byte aligned");
+    FastArgs A;
+    int rc = fill_trace_params(A.P, desc, cam, shadow, light, light_shadow);
+    if (rc != VCT_OK) return rc;
+    VCT_CHECK_ARG((float)texture_resolution(radiance) == desc->volume_dimension,
+                  "vct_cone_trace_fast: volume dimension differs from the texture's clipmap resolution");
+    FastScratch S;
+    rc = plan_scratch(n, scratch, S);
+    if (rc != VCT_OK) return rc;
+    VCT_CHECK_ARG(scratch_bytes >= S.total, "vct_cone_trace_fast: scratch buffer too small");
+    fill_fast_consts(A.C, *desc);
+    A.tex = texture_object(radiance);
+    A.samples = samples;
+    A.n = n;
+    A.dout = dout;
+    A.sout = sout;
+    A.steps = cone_steps;
+    cudaStream_t st = as_stream(stream);
+    const int block = 256;
+    int64_t g = (n + block - 1) / block;
+    const int grid_keys = (int)(g > 152 * 32 ? 152 * 32 : g);
+    k_morton_keys<<<grid_keys, block, 0, st>>>(samples, n, A.C, S.keys_in, S.vals_in);
+    VCT_LAUNCH_CHECK();
+    size_t tb = S.temp_bytes;
+    VCT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(S.temp, tb, S.keys_in, S.keys_out, S.vals_in, S.order, (int)n, 0, 30, st));
+    VCT_CUDA_TRY(cudaMemsetAsync(S.spec_count, 0, sizeof(unsigned int), st));
+    int64_t gd = (n + 255) / 256;
+    const int grid_d = (int)(gd > 152 * 8 ? 152 * 8 : gd);
+    k_trace_diffuse<<<grid_d, 256, 0, st>>>(A, S.order, S.spec_key, S.spec_count);
+    VCT_LAUNCH_CHECK();
+    if (A.C.need_specular) {
+        tb = S.temp_bytes;
+        VCT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(S.temp, tb, S.spec_key, S.spec_key_out, S.order, S.spec_list,
+                                                     (int)n, 0, 9, st));
+        int64_t gs = (n + 127) / 128;
+        const int grid_s = (int)(gs > 152 * 16 ? 152 * 16 : gs);
+        k_trace_specular<<<grid_s, 128, 0, st>>>(A, S.spec_list, S.spec_count);
+        VCT_LAUNCH_CHECK();
+    }
+    return VCT_OK;
+}
