@@ -304,6 +304,89 @@ int vct_cone_trace_fast(const vct_cone_tracing_desc* desc, const vct_cam_matrix*
                         float* diffuse_out, float* specular_out, unsigned long long* cone_steps,
                         void* scratch, size_t scratch_bytes, void* stream);
 
+/* ------------------------------------------------ scene and raster passes */
+
+/* Scene in the reference's vertex-input layout (VFS/SceneManager.cpp:124-204,
+ * VFS/GLTFScene.cpp:457-490): separate fp32 position / normal streams, uint32
+ * indices, a material index per triangle (the per-draw push constant
+ * uMaterialIndex), GltfShadeMaterial records, 1x1 RGBA8 textures indexed by
+ * the materials' texture ids, and optional per-instance NodeMatrix {model,
+ * itModel} (column-major, 32 floats) selected per triangle.  Device pointers. */
+typedef struct vct_scene {
+    const float* positions;
+    const float* normals;
+    const uint32_t* indices;
+    int64_t vertex_count;
+    int64_t triangle_count;
+    const uint32_t* triangle_material;
+    const vct_gltf_shade_material* materials;
+    int32_t material_count;
+    const uint32_t* textures;
+    int32_t texture_count;
+    const float* node_matrices;
+    const uint32_t* triangle_instance;
+    int32_t instance_count;
+} vct_scene;
+
+/* Device scratch arena for the raster passes (tile counts, prefix sums,
+ * injection records, sort buffers).  Created by the caller; the passes grow
+ * it with cudaMalloc when it is too small (synchronising the device first). */
+typedef struct vct_workspace_s* vct_workspace;
+int vct_workspace_create(size_t initial_bytes, vct_workspace* out);
+int vct_workspace_destroy(vct_workspace ws);
+int64_t vct_workspace_bytes(vct_workspace ws);
+
+/* Host math of Voxelizer::setViewProjection (VFS/RenderPass/Clipmap/Voxelizer.cpp:394-423):
+ * the three dominant-axis view-projection matrices of a region (48 floats). */
+int vct_voxelization_view_proj(const vct_clipmap_region* region, float out_host[48]);
+/* Voxelizer::cmdVoxelize's VoxelizationDesc for one level (Voxelizer.cpp:330-354). */
+int vct_voxelization_desc_for(const vct_clipmap_region regions_host[6], int32_t level, int32_t clipmap_resolution,
+                              vct_voxelization_desc* out_host);
+/* DirectionalLight::setTransform (VFS/DirectionalLight.cpp:21-47): view and
+ * +-16 orthographic projection of a directional light. */
+int vct_directional_light_shadow(const float origin_host[3], const float direction_host[3], float z_near,
+                                 float z_far, vct_directional_light_shadow_desc* out_host);
+
+/* vkCmdClearColorImage of a whole atlas to 0 (VoxelizationPass.cpp:104-125). */
+int vct_clear_atlas(uint32_t* atlas, int32_t clipmap_resolution, void* stream);
+
+/* VoxelizationPass::onUpdate + msaaVoxelizer.{vert,geom,frag}
+ * (VFS/RenderPass/Clipmap/VoxelizationPass.cpp:190-212): rasterise every
+ * triangle into each clip level of `level_mask` (bit l = level l) and store
+ * 1.0 into the 6 face copies of each covered voxel.  Does not clear. */
+int vct_voxelize_opacity(const vct_scene* scene, const vct_clipmap_region regions_host[6], int32_t clipmap_resolution,
+                         uint32_t* opacity_atlas, uint32_t level_mask, vct_workspace ws, void* stream);
+
+/* ReflectiveShadowMapPass depth (VFS/RenderPass/ReflectiveShadowMapPass.cpp,
+ * reflectiveShadowPass.vert:40-50): clear to 1.0, rasterise with depth test
+ * LESS into a width x height D32 map. */
+int vct_shadow_depth(const vct_scene* scene, const vct_directional_light_shadow_desc* light_shadow, float* depth,
+                     int32_t width, int32_t height, vct_workspace ws, void* stream);
+
+/* RadianceInjectionPass::onUpdate + msaaInjectRadiance.{vert,geom,frag}
+ * (VFS/RenderPass/Clipmap/RadianceInjectionPass.cpp:134-159): light each
+ * covered sample and fold it into the RGBA8 running average of its faces.
+ * VCT_INJECT_DETERMINISTIC folds in the traversal order (triangle, level,
+ * tile, pixel, sample) -- bit-exact against the CPU oracle;
+ * VCT_INJECT_ATOMIC runs the reference's CAS loop (order-dependent). */
+#define VCT_INJECT_DETERMINISTIC 0
+#define VCT_INJECT_ATOMIC 1
+int vct_inject_radiance(const vct_scene* scene, const vct_clipmap_region regions_host[6], int32_t clipmap_resolution,
+                        const vct_shadow_map* shadow, const vct_directional_light_desc* light,
+                        const vct_directional_light_shadow_desc* light_shadow, uint32_t* radiance_atlas,
+                        uint32_t level_mask, int32_t mode, vct_workspace ws, void* stream);
+
+/* SparseVoxelizer::preVoxelize + cmdVoxelize (VFS/RenderPass/Octree/SparseVoxelizer.cpp:248-326)
+ * with voxelizer.{vert,geom,frag}: count pass, host readback of the count
+ * into *count_host, write pass of packed uint2 fragments in traversal order.
+ * capacity == 0 only counts.  Fragments discarded by the light test keep a
+ * zeroed slot (the reference increments its counter before that discard). */
+int vct_svo_fragments(const vct_scene* scene, int32_t octree_level, const float bb_min_host[3],
+                      const float bb_max_host[3], const vct_shadow_map* shadow,
+                      const vct_directional_light_desc* light,
+                      const vct_directional_light_shadow_desc* light_shadow, uint32_t* fragments,
+                      int64_t capacity, int64_t* count_host, vct_workspace ws, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -65,6 +65,16 @@ def lib():
         L.vcto_cone_trace_f4.argtypes = [P, P, P, C.c_int, P, C.c_int, C.c_int, P, P, P, C.c_int64, C.c_int64,
                                          P, P]
         L.vcto_downsample_f4.argtypes = [P, C.c_int, P, C.c_int, C.c_int, C.c_int]
+        L.vcto_voxel_view_proj.argtypes = [P, P]
+        L.vcto_voxelization_desc.argtypes = [P, C.c_int, C.c_int, P]
+        L.vcto_light_shadow_desc.argtypes = [P, P, C.c_float, C.c_float, P]
+        L.vcto_voxelize_opacity.argtypes = [P, C.c_int, P, P, C.c_int]
+        L.vcto_shadow_depth.argtypes = [P, P, P, C.c_int, C.c_int]
+        L.vcto_inject_radiance.argtypes = [P, C.c_int, P, P, C.c_int, C.c_int, P, P, P, C.c_int]
+        L.vcto_svo_fragments.restype = C.c_int64
+        L.vcto_svo_fragments.argtypes = [P, C.c_int, P, P, P, C.c_int, C.c_int, P, P, P, C.c_int64]
+        L.vcto_svo_build.restype = C.c_int
+        L.vcto_svo_build.argtypes = [P, C.c_int64, C.c_int, P, C.c_int64, P]
         L.vcto_procedural_atlas.argtypes = [P, C.c_int64, C.c_uint32, C.c_double]
         _L = L
     return _L
@@ -174,3 +184,107 @@ def cone_trace_f4(desc_bytes: bytes, eye, atlas4: np.ndarray, R: int, samples: n
     steps = lib().vcto_cone_trace_f4(_p(desc), _p(eye), _p(atlas4), R, _p(shadow), sw, sh, _p(sd), _p(light),
                                      _p(samples), begin, end, _p(dout), _p(sout))
     return dout, sout, int(steps)
+
+
+# ------------------------------------------------------------ raster passes
+
+class SceneView(C.Structure):
+    """Mirror of vcto::SceneView / vct_scene (host pointers)."""
+    _fields_ = [("positions", P), ("normals", P), ("indices", P), ("vertex_count", C.c_int64),
+                ("triangle_count", C.c_int64), ("triangle_material", P), ("materials", P),
+                ("material_count", C.c_int32), ("textures", P), ("texture_count", C.c_int32),
+                ("node_matrices", P), ("triangle_instance", P), ("instance_count", C.c_int32)]
+
+
+def scene_view(scene):
+    """SceneView over a vk_voxel_cone_tracing_gb300.scene.Scene (arrays kept alive on the returned object)."""
+    keep = [np.ascontiguousarray(scene.positions, np.float32), np.ascontiguousarray(scene.normals, np.float32),
+            np.ascontiguousarray(scene.indices, np.uint32), np.ascontiguousarray(scene.tri_material, np.uint32),
+            np.ascontiguousarray(scene.materials), np.ascontiguousarray(scene.textures, np.uint32)]
+    sv = SceneView(_p(keep[0]), _p(keep[1]), _p(keep[2]), keep[0].shape[0], keep[2].shape[0], _p(keep[3]),
+                   _p(keep[4]), keep[4].shape[0], _p(keep[5]), keep[5].shape[0], None, None, 0)
+    sv._keep = keep
+    return sv
+
+
+def _regions_arg(regions: np.ndarray) -> np.ndarray:
+    return np.ascontiguousarray(regions, np.int32)
+
+
+def voxel_view_proj(region_row: np.ndarray) -> np.ndarray:
+    out = np.zeros(48, np.float32)
+    lib().vcto_voxel_view_proj(_p(np.ascontiguousarray(region_row, np.int32)), _p(out))
+    return out.reshape(3, 16)
+
+
+def voxelization_desc(regions: np.ndarray, level: int, R: int) -> bytes:
+    out = np.zeros(16, np.int32)
+    lib().vcto_voxelization_desc(_p(_regions_arg(regions)), level, R, _p(out))
+    return out.tobytes()
+
+
+def light_shadow_desc(origin, direction, z_near: float = 0.1, z_far: float = 30.0) -> bytes:
+    out = np.zeros(34, np.float32)
+    lib().vcto_light_shadow_desc(_p(np.asarray(origin, np.float32)), _p(np.asarray(direction, np.float32)),
+                                 z_near, z_far, _p(out))
+    return out.tobytes()
+
+
+def voxelize_opacity(scene, R: int, regions: np.ndarray, level_mask: int = 0x3F,
+                     atlas: np.ndarray | None = None) -> np.ndarray:
+    if atlas is None:
+        atlas = np.zeros((R + 2, 6 * (R + 2), 6 * (R + 2)), np.uint32)
+    sv = scene_view(scene)
+    lib().vcto_voxelize_opacity(C.byref(sv), R, _p(_regions_arg(regions)), _p(atlas), level_mask)
+    return atlas
+
+
+def shadow_depth(scene, shadow_desc_bytes: bytes, W: int, H: int) -> np.ndarray:
+    depth = np.empty((H, W), np.float32)
+    sd = np.frombuffer(shadow_desc_bytes, np.uint8).copy()
+    sv = scene_view(scene)
+    lib().vcto_shadow_depth(C.byref(sv), _p(sd), _p(depth), W, H)
+    return depth
+
+
+def inject_radiance(scene, R: int, regions: np.ndarray, shadow: np.ndarray | None, shadow_desc_bytes: bytes,
+                    light_bytes: bytes | None = None, level_mask: int = 0x3F,
+                    atlas: np.ndarray | None = None) -> np.ndarray:
+    if atlas is None:
+        atlas = np.zeros((R + 2, 6 * (R + 2), 6 * (R + 2)), np.uint32)
+    sd = np.frombuffer(shadow_desc_bytes, np.uint8).copy()
+    light = np.frombuffer(light_bytes or default_light_bytes(), np.uint8).copy()
+    sh, sw = (shadow.shape if shadow is not None else (0, 0))
+    sv = scene_view(scene)
+    lib().vcto_inject_radiance(C.byref(sv), R, _p(_regions_arg(regions)), _p(shadow), sw, sh, _p(sd), _p(light),
+                               _p(atlas), level_mask)
+    return atlas
+
+
+def svo_fragments(scene, level: int, bb_min, bb_max, shadow: np.ndarray | None, shadow_desc_bytes: bytes,
+                  light_bytes: bytes | None = None, capacity: int | None = None):
+    sd = np.frombuffer(shadow_desc_bytes, np.uint8).copy()
+    light = np.frombuffer(light_bytes or default_light_bytes(), np.uint8).copy()
+    sh, sw = (shadow.shape if shadow is not None else (0, 0))
+    sv = scene_view(scene)
+    bmin = np.asarray(bb_min, np.float32)
+    bmax = np.asarray(bb_max, np.float32)
+    if capacity is None:
+        capacity = int(lib().vcto_svo_fragments(C.byref(sv), level, _p(bmin), _p(bmax), _p(shadow), sw, sh, _p(sd),
+                                                _p(light), None, 0))
+    frags = np.zeros((max(capacity, 1), 2), np.uint32)
+    n = int(lib().vcto_svo_fragments(C.byref(sv), level, _p(bmin), _p(bmax), _p(shadow), sw, sh, _p(sd), _p(light),
+                                     _p(frags), capacity))
+    return frags[:min(n, capacity)], n
+
+
+def svo_build(frags: np.ndarray, level: int, capacity: int | None = None):
+    F = frags.shape[0]
+    if capacity is None:
+        capacity = min(max(8 * F, 1_000_000), 500_000_000)
+    pool = np.zeros((capacity, 2), np.uint32)
+    nodes = np.zeros(1, np.int64)
+    rc = lib().vcto_svo_build(_p(np.ascontiguousarray(frags, np.uint32)), F, level, _p(pool), capacity, _p(nodes))
+    if rc != 0:
+        raise RuntimeError("oracle svo_build: node pool capacity exceeded")
+    return pool[:int(nodes[0])], int(nodes[0])

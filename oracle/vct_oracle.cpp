@@ -6,6 +6,8 @@
 #include <omp.h>
 
 #include "clipmap_oracle.hpp"
+#include "raster_oracle.hpp"
+#include "svo_oracle.hpp"
 
 using namespace vcto;
 
@@ -123,6 +125,43 @@ void vcto_procedural_atlas(uint32_t* out, int64_t n, uint32_t seed, double fill)
         uint64_t alpha = 64 + ((h >> 16) % 192);
         out[i] = occ ? (uint32_t)((h2 & 0xFFFFFF) | (alpha << 24)) : 0u;
     }
+}
+
+// ---------------------------------------------------------- raster passes
+void vcto_voxel_view_proj(const Region* region, float out[48]) {
+    Mat4 m[3];
+    voxel_view_proj(*region, m);
+    for (int i = 0; i < 3; ++i) std::memcpy(out + 16 * i, m[i].m, 64);
+}
+void vcto_voxelization_desc(const Region regions[6], int level, int R, VoxDesc* out) {
+    *out = voxelization_desc(regions, level, R);
+}
+void vcto_light_shadow_desc(const float origin[3], const float direction[3], float z_near, float z_far,
+                            ShadowDesc* out) {
+    light_shadow_desc(origin, direction, z_near, z_far, *out);
+}
+void vcto_voxelize_opacity(const SceneView* s, int R, const Region regions[6], uint32_t* atlas, int level_mask) {
+    voxelize_opacity(*s, R, regions, atlas, level_mask);
+}
+void vcto_shadow_depth(const SceneView* s, const ShadowDesc* sd, float* depth, int W, int H) {
+    shadow_depth(*s, *sd, depth, W, H);
+}
+void vcto_inject_radiance(const SceneView* s, int R, const Region regions[6], const float* shadow, int sw, int sh,
+                          const ShadowDesc* sd, const LightDesc* light, uint32_t* radiance, int level_mask) {
+    inject_radiance(*s, R, regions, shadow, sw, sh, *sd, *light, radiance, level_mask);
+}
+int64_t vcto_svo_fragments(const SceneView* s, int level, const float bb_min[3], const float bb_max[3],
+                           const float* shadow, int sw, int sh, const ShadowDesc* sd, const LightDesc* light,
+                           uint32_t* frags, int64_t capacity) {
+    return svo_fragments(*s, level, bb_min, bb_max, shadow, sw, sh, *sd, *light, frags, capacity);
+}
+int vcto_svo_build(const uint32_t* frags, int64_t F, int level, uint32_t* pool, int64_t capacity,
+                   int64_t* node_count) {
+    int rc = svo_subdivide(frags, F, level, pool, capacity, node_count);
+    if (rc != 0) return rc;
+    svo_leaf_write(frags, F, level, pool);
+    svo_mip_write(frags, F, level, pool);
+    return 0;
 }
 
 }  // extern "C"

@@ -1,0 +1,106 @@
+// glm_golden.cpp -- golden-vector generator (see make_golden.py).
+//
+// Evaluates, with the reference's vendored glm and its defines, the host-side
+// math of the path: VoxelizationPass::createVoxelClipmap/calculateChangeDelta
+// (VFS/RenderPass/Clipmap/VoxelizationPass.cpp:335-357, 438-448) fed by
+// Application::updateClipRegionBoundingBox (VFS/Application.cpp:116-128),
+// Voxelizer::setViewProjection (VFS/RenderPass/Clipmap/Voxelizer.cpp:394-423)
+// and DirectionalLight::setTransform (VFS/DirectionalLight.cpp:21-47).  The
+// calls below are written here from those functions' arguments; nothing of
+// the reference is compiled.  Prints JSON with every float as its bit pattern.
+#define GLM_FORCE_SIZE_T_LENGTH
+#define GLM_FORCE_DEPTH_ZERO_TO_ONE
+#define GLM_FORCE_LEFT_HANDED
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <glm/glm.hpp>
+#include <glm/gtc/matrix_transform.hpp>
+
+static uint32_t bits(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    return u;
+}
+
+static void print_mat(const glm::mat4& m) {
+    std::printf("[");
+    for (int c = 0; c < 4; ++c)
+        for (int r = 0; r < 4; ++r) std::printf("%u%s", bits(m[c][r]), (c == 3 && r == 3) ? "" : ",");
+    std::printf("]");
+}
+
+struct Region {
+    glm::ivec3 minCorner;
+    glm::uvec3 extent;
+    float voxelSize;
+};
+
+int main() {
+    const float cams[][3] = {{0.f, 0.f, 0.f}, {1.3f, 2.7f, -5.1f}, {-40.2f, 3.3f, 17.9f}, {0.37f, -0.51f, 8.9f}};
+    const uint32_t resolutions[] = {64, 128, 256};
+    const int32_t minChange[6] = {2, 2, 2, 2, 2, 1};
+    std::printf("{\"regions\":[");
+    bool first = true;
+    for (auto& cam : cams)
+        for (uint32_t R : resolutions) {
+            Region regs[6];
+            for (int l = 0; l < 6; ++l) {
+                const uint32_t half = R >> 1;
+                regs[l].minCorner = -glm::ivec3(half);
+                regs[l].extent = glm::uvec3(R, R, R);
+                regs[l].voxelSize = (16u * (1u << l)) / static_cast<float>(R);
+                glm::vec3 center(cam[0], cam[1], cam[2]);
+                const float halfSize = static_cast<float>((16u >> 1) * (1u << l));
+                glm::vec3 bbMin = center - halfSize;
+                glm::vec3 deltaW = bbMin - (glm::vec3(regs[l].minCorner) * regs[l].voxelSize);
+                const float minChangeW = regs[l].voxelSize * minChange[l];
+                glm::ivec3 delta = glm::ivec3(glm::trunc(deltaW / minChangeW)) * minChange[l];
+                regs[l].minCorner += delta;
+            }
+            for (int l = 0; l < 6; ++l) {
+                const Region& region = regs[l];
+                Region ext = region;
+                ext.extent = ext.extent + 2u;
+                ext.minCorner -= 1;
+                const glm::vec3 regionGlobal = glm::vec3(ext.extent) * ext.voxelSize;
+                const glm::vec3 minCornerGlobal = glm::vec3(ext.minCorner) * ext.voxelSize;
+                const glm::vec3 eye = minCornerGlobal + glm::vec3(0.0f, 0.0f, regionGlobal.z);
+                glm::mat4 vp[3];
+                vp[0] = glm::ortho(-regionGlobal.z, regionGlobal.z, -regionGlobal.y, regionGlobal.y, 0.1f, regionGlobal.x) *
+                        glm::lookAt(eye, eye + glm::vec3(1.0f, 0.0f, 0.0f), glm::vec3(0.0f, 1.0f, 0.0f));
+                vp[1] = glm::ortho(-regionGlobal.x, regionGlobal.x, -regionGlobal.z, regionGlobal.z, 0.1f, regionGlobal.y) *
+                        glm::lookAt(eye, eye + glm::vec3(0.0f, 1.0f, 0.0f), glm::vec3(0.0f, 0.0f, -1.0f));
+                vp[2] = glm::ortho(-regionGlobal.x, regionGlobal.x, -regionGlobal.y, regionGlobal.y, 0.1f, regionGlobal.z) *
+                        glm::lookAt(minCornerGlobal, minCornerGlobal + glm::vec3(0.0f, 0.0f, 1.0f), glm::vec3(0.0f, 1.0f, 0.0f));
+                std::printf("%s{\"cam\":[%u,%u,%u],\"R\":%u,\"level\":%d,\"min_corner\":[%d,%d,%d],\"voxel_size\":%u,\"view_proj\":[",
+                            first ? "" : ",", bits(cam[0]), bits(cam[1]), bits(cam[2]), R, l, region.minCorner.x,
+                            region.minCorner.y, region.minCorner.z, bits(region.voxelSize));
+                first = false;
+                for (int i = 0; i < 3; ++i) {
+                    print_mat(vp[i]);
+                    if (i < 2) std::printf(",");
+                }
+                std::printf("]}");
+            }
+        }
+    std::printf("],\"lights\":[");
+    const float lights[][6] = {{0.f, 30.f, -5.3f, 0.f, -1.f, 0.2f}, {0.f, 20.f, 0.f, 0.3f, -1.f, 0.2f},
+                               {4.2f, 14.f, -4.0f, 0.3f, -1.f, 0.2f}};
+    first = true;
+    for (auto& L : lights) {
+        glm::vec3 origin(L[0], L[1], L[2]);
+        glm::vec3 dir = glm::normalize(glm::vec3(L[3], L[4], L[5]));
+        glm::mat4 view = glm::lookAt(origin, origin + dir, glm::vec3(0.0f, 1.0f, 0.0f));
+        glm::mat4 proj = glm::ortho(-16.0f, 16.0f, -16.0f, 16.0f, 0.1f, 30.0f);
+        std::printf("%s{\"origin\":[%u,%u,%u],\"direction\":[%u,%u,%u],\"view\":", first ? "" : ",", bits(L[0]),
+                    bits(L[1]), bits(L[2]), bits(L[3]), bits(L[4]), bits(L[5]));
+        first = false;
+        print_mat(view);
+        std::printf(",\"proj\":");
+        print_mat(proj);
+        std::printf("}");
+    }
+    std::printf("]}\n");
+    return 0;
+}

@@ -30,6 +30,9 @@ DOWNSAMPLE_RADIANCE = 1
 
 MODE_GI_OUTPUT = 8
 
+INJECT_DETERMINISTIC = 0
+INJECT_ATOMIC = 1
+
 TEX_RGBA8 = 0
 TEX_RGBA16F = 1
 
@@ -99,6 +102,14 @@ class GltfShadeMaterial(C.Structure):
                 ("padding", C.c_int32)]
 
 
+class Scene(C.Structure):
+    _fields_ = [("positions", C.c_void_p), ("normals", C.c_void_p), ("indices", C.c_void_p),
+                ("vertex_count", C.c_int64), ("triangle_count", C.c_int64), ("triangle_material", C.c_void_p),
+                ("materials", C.c_void_p), ("material_count", C.c_int32), ("textures", C.c_void_p),
+                ("texture_count", C.c_int32), ("node_matrices", C.c_void_p), ("triangle_instance", C.c_void_p),
+                ("instance_count", C.c_int32)]
+
+
 class ShadowMap(C.Structure):
     _fields_ = [("depth", C.c_void_p), ("width", C.c_int32), ("height", C.c_int32)]
 
@@ -106,7 +117,7 @@ class ShadowMap(C.Structure):
 STRUCT_SIZES = {
     ClipmapRegion: 28, VoxelizationDesc: 64, DownSampleDesc: 24, ImageCleaningDesc: 36, CopyAlphaDesc: 12,
     BorderWrappingDesc: 16, ConeTracingDesc: 52, CamMatrix: 144, DirectionalLightDesc: 32,
-    DirectionalLightShadowDesc: 136, GltfShadeMaterial: 80,
+    DirectionalLightShadowDesc: 136, GltfShadeMaterial: 80, Scene: 104,
 }
 
 # Every entry point of include/vct_capi.h: name -> (restype, argtypes).
@@ -129,6 +140,17 @@ _SIGS: dict[str, tuple] = {
     "vct_downsample_rgba16f": (C.c_int, [P, P, C.c_int32, P]),
     "vct_cone_trace_fast_scratch_bytes": (C.c_int64, [C.c_int64]),
     "vct_cone_trace_fast": (C.c_int, [P, P, P, P, P, P, P, C.c_int64, P, P, P, P, C.c_size_t, P]),
+    "vct_workspace_create": (C.c_int, [C.c_size_t, C.POINTER(C.c_void_p)]),
+    "vct_workspace_destroy": (C.c_int, [P]),
+    "vct_workspace_bytes": (C.c_int64, [P]),
+    "vct_voxelization_view_proj": (C.c_int, [P, P]),
+    "vct_voxelization_desc_for": (C.c_int, [P, C.c_int32, C.c_int32, P]),
+    "vct_directional_light_shadow": (C.c_int, [P, P, C.c_float, C.c_float, P]),
+    "vct_clear_atlas": (C.c_int, [P, C.c_int32, P]),
+    "vct_voxelize_opacity": (C.c_int, [P, P, C.c_int32, P, C.c_uint32, P, P]),
+    "vct_shadow_depth": (C.c_int, [P, P, P, C.c_int32, C.c_int32, P, P]),
+    "vct_inject_radiance": (C.c_int, [P, P, C.c_int32, P, P, P, P, C.c_uint32, C.c_int32, P, P]),
+    "vct_svo_fragments": (C.c_int, [P, C.c_int32, P, P, P, P, P, P, C.c_int64, C.POINTER(C.c_int64), P, P]),
 }
 
 

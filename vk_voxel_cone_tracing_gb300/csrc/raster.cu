@@ -1,0 +1,998 @@
+// raster.cu -- the rasterisation-driven passes as CUDA kernels:
+//   vct_voxelize_opacity  (VoxelizationPass + msaaVoxelizer.*),
+//   vct_shadow_depth      (ReflectiveShadowMapPass depth, reflectiveShadowPass.vert),
+//   vct_inject_radiance   (RadianceInjectionPass + msaaInjectRadiance.*),
+//   vct_svo_fragments     (SparseVoxelizer + voxelizer.*).
+//
+// The fixed-function rasteriser is restated in software with a pinned rule
+// (the reference's MSAA pattern and shading rate are implementation-defined):
+// 8x MSAA at the Vulkan standard sample locations (one centre sample for the
+// depth-only pass), vertices snapped to 1/256 pixel, exact 64-bit edge
+// functions with a one-owner tie rule, depth clip [0,1], barycentrics in
+// FP64, the fragment shader at every covered sample.
+//
+// Work decomposition: one item per (triangle, clip level); each item's
+// bounding box is cut into 8x8-pixel tiles; one thread walks one tile (pixels
+// row-major, samples in index order).  Items' tile counts are prefix-summed
+// and the tile kernel finds its item by binary search, so no per-tile list is
+// materialised.  Order-dependent passes (RGBA8 running averages, the SVO
+// fragment list) use a count pass + prefix sum + write pass, which fixes the
+// traversal order (item, tile, pixel, sample); the injection's records are
+// then stably sorted by texel and folded sequentially per texel, which
+// reproduces the serial order of the reference's CAS loops bit for bit.
+// Compiled with -fmad=false: the fragment arithmetic is the FP32 GLSL in its
+// written order.
+#include <cub/cub.cuh>
+
+#include "trace_common.cuh"
+
+struct vct_workspace_s {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+};
+
+namespace vct {
+
+// ------------------------------------------------------------------ math
+struct M4 {
+    float m[16];
+};
+
+__host__ __device__ inline float4 mat_vec4(const float* M, float x, float y, float z, float w) {
+    float r[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        float a = M[i] * x + M[4 + i] * y;
+        float b = M[8 + i] * z + M[12 + i] * w;
+        r[i] = a + b;
+    }
+    return make_float4(r[0], r[1], r[2], r[3]);
+}
+
+__host__ __device__ inline M4 mat_mul4(const float* A, const float* B) {
+    M4 R;
+    for (int i = 0; i < 4; ++i)
+        for (int r = 0; r < 4; ++r) {
+            float s = A[r] * B[i * 4 + 0];
+            s = s + A[4 + r] * B[i * 4 + 1];
+            s = s + A[8 + r] * B[i * 4 + 2];
+            s = s + A[12 + r] * B[i * 4 + 3];
+            R.m[i * 4 + r] = s;
+        }
+    return R;
+}
+
+__host__ __device__ inline float3 cross3h(float3 a, float3 b) {
+    return make_float3(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
+}
+__host__ __device__ inline float dot3h(float3 a, float3 b) {
+    float t0 = a.x * b.x, t1 = a.y * b.y, t2 = a.z * b.z;
+    return (t0 + t1) + t2;
+}
+__host__ __device__ inline float3 normalize3h(float3 v) {
+    float inv = 1.0f / sqrtf(dot3h(v, v));
+    return make_float3(v.x * inv, v.y * inv, v.z * inv);
+}
+
+// glm::lookAtLH and glm::orthoLH_ZO (column-major).
+__host__ inline M4 look_at_lh(float3 eye, float3 center, float3 up) {
+    float3 f = normalize3h(make_float3(center.x - eye.x, center.y - eye.y, center.z - eye.z));
+    float3 s = normalize3h(cross3h(up, f));
+    float3 u = cross3h(f, s);
+    M4 R = {};
+    R.m[0] = s.x; R.m[4] = s.y; R.m[8] = s.z;
+    R.m[1] = u.x; R.m[5] = u.y; R.m[9] = u.z;
+    R.m[2] = f.x; R.m[6] = f.y; R.m[10] = f.z;
+    R.m[12] = -dot3h(s, eye);
+    R.m[13] = -dot3h(u, eye);
+    R.m[14] = -dot3h(f, eye);
+    R.m[15] = 1.0f;
+    return R;
+}
+__host__ inline M4 ortho_lh_zo(float l, float r, float b, float t, float n, float f) {
+    M4 R = {};
+    R.m[0] = 2.0f / (r - l);
+    R.m[5] = 2.0f / (t - b);
+    R.m[10] = 1.0f / (f - n);
+    R.m[12] = -(r + l) / (r - l);
+    R.m[13] = -(t + b) / (t - b);
+    R.m[14] = -n / (f - n);
+    R.m[15] = 1.0f;
+    return R;
+}
+
+// Voxelizer::setViewProjection over the extended region (min - 1, extent + 2).
+__host__ void voxel_view_proj(const vct_clipmap_region& r, float out[48]) {
+    const float vs = r.voxel_size;
+    float3 rg = make_float3((float)(r.extent[0] + 2u) * vs, (float)(r.extent[1] + 2u) * vs, (float)(r.extent[2] + 2u) * vs);
+    float3 mcg = make_float3((float)(r.min_corner[0] - 1) * vs, (float)(r.min_corner[1] - 1) * vs,
+                             (float)(r.min_corner[2] - 1) * vs);
+    float3 eye = make_float3(mcg.x + 0.0f, mcg.y + 0.0f, mcg.z + rg.z);
+    M4 v0 = look_at_lh(eye, make_float3(eye.x + 1.0f, eye.y + 0.0f, eye.z + 0.0f), make_float3(0.f, 1.f, 0.f));
+    M4 v1 = look_at_lh(eye, make_float3(eye.x + 0.0f, eye.y + 1.0f, eye.z + 0.0f), make_float3(0.f, 0.f, -1.f));
+    M4 v2 = look_at_lh(mcg, make_float3(mcg.x + 0.0f, mcg.y + 0.0f, mcg.z + 1.0f), make_float3(0.f, 1.f, 0.f));
+    M4 p0 = ortho_lh_zo(-rg.z, rg.z, -rg.y, rg.y, 0.1f, rg.x);
+    M4 p1 = ortho_lh_zo(-rg.x, rg.x, -rg.z, rg.z, 0.1f, rg.y);
+    M4 p2 = ortho_lh_zo(-rg.x, rg.x, -rg.y, rg.y, 0.1f, rg.z);
+    M4 m0 = mat_mul4(p0.m, v0.m), m1 = mat_mul4(p1.m, v1.m), m2 = mat_mul4(p2.m, v2.m);
+    memcpy(out, m0.m, 64);
+    memcpy(out + 16, m1.m, 64);
+    memcpy(out + 32, m2.m, 64);
+}
+
+__host__ vct_voxelization_desc voxelization_desc(const vct_clipmap_region* regions, int level, int R) {
+    vct_voxelization_desc d;
+    memset(&d, 0, sizeof(d));
+    const vct_clipmap_region& r = regions[level];
+    for (int a = 0; a < 3; ++a) {
+        d.region_min_corner[a] = (float)r.min_corner[a] * r.voxel_size - 1e-6f;
+        d.region_max_corner[a] = (float)(r.min_corner[a] + (int32_t)r.extent[a]) * r.voxel_size + 1e-6f;
+    }
+    d.clip_level = (uint32_t)level;
+    d.clip_max_extent = (float)r.extent[0] * r.voxel_size;
+    d.voxel_size = r.voxel_size;
+    if (level > 0) {
+        const vct_clipmap_region& p = regions[level - 1];
+        for (int a = 0; a < 3; ++a) {
+            d.prev_region_min_corner[a] = (float)p.min_corner[a] * p.voxel_size;
+            d.prev_region_max_corner[a] = (float)(p.min_corner[a] + (int32_t)p.extent[a]) * p.voxel_size;
+        }
+    }
+    d.clipmap_resolution = R;
+    return d;
+}
+
+// ------------------------------------------------------------------ scene
+struct WTri {
+    float3 p[3], n[3];
+    uint32_t material;
+};
+
+__device__ inline WTri world_triangle(const vct_scene& s, int64_t t) {
+    WTri w;
+    const uint32_t inst = s.triangle_instance ? __ldg(s.triangle_instance + t) : 0u;
+    const float* model = s.node_matrices ? s.node_matrices + 32 * (int64_t)inst : nullptr;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const uint32_t vi = __ldg(s.indices + 3 * t + k);
+        const float* p = s.positions + 3 * (int64_t)vi;
+        const float* n = s.normals + 3 * (int64_t)vi;
+        float px = __ldg(p), py = __ldg(p + 1), pz = __ldg(p + 2);
+        float nx = __ldg(n), ny = __ldg(n + 1), nz = __ldg(n + 2);
+        if (model) {
+            float4 wp = mat_vec4(model, px, py, pz, 1.0f);
+            float4 wn = mat_vec4(model + 16, nx, ny, nz, 0.0f);
+            w.p[k] = make_float3(wp.x, wp.y, wp.z);
+            w.n[k] = make_float3(wn.x, wn.y, wn.z);
+        } else {
+            float4 wp = make_float4(px, py, pz, 1.0f);
+            float4 wn = make_float4(nx, ny, nz, 0.0f);
+            // identity model: mat_vec4 with the identity is exact, keep the values
+            w.p[k] = make_float3(wp.x, wp.y, wp.z);
+            w.n[k] = make_float3(wn.x, wn.y, wn.z);
+        }
+    }
+    w.material = s.triangle_material ? __ldg(s.triangle_material + t) : 0u;
+    return w;
+}
+
+__device__ inline int dominant_axis(const float3 p[3]) {
+    float3 e1 = make_float3(p[1].x - p[0].x, p[1].y - p[0].y, p[1].z - p[0].z);
+    float3 e2 = make_float3(p[2].x - p[0].x, p[2].y - p[0].y, p[2].z - p[0].z);
+    float3 c = cross3h(e1, e2);
+    float nx = fabsf(c.x), ny = fabsf(c.y), nz = fabsf(c.z);
+    return (nx > ny && nx > nz) ? 0 : ((ny > nz) ? 1 : 2);
+}
+
+__device__ inline float4 texture_1x1(const vct_scene& s, int32_t id) {
+    if (!s.textures || id < 0 || id >= s.texture_count) return make_float4(0.f, 0.f, 0.f, 0.f);
+    return unpack_rgba8(__ldg(s.textures + id));
+}
+
+// ------------------------------------------------------------- rasteriser
+__constant__ int c_sample_loc8[8][2] = {{144, 80}, {112, 176}, {208, 144}, {80, 48},
+                                        {48, 208}, {16, 112}, {176, 240}, {240, 16}};
+
+struct RSetup {
+    long long X[3], Y[3];
+    float z[3];
+    int order[3];
+    long long area;
+    int px0, py0, px1, py1;
+    int owned;  // bit i: edge i owns its samples
+    bool ok;
+};
+
+__device__ inline long long floor_div256(long long v) { return v >= 0 ? v / 256 : -((-v + 255) / 256); }
+
+__device__ inline RSetup raster_setup(const float4 c[3], int W, int H) {
+    RSetup r;
+    const float hw = (float)W * 0.5f, hh = (float)H * 0.5f;
+    long long X[3], Y[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        X[k] = __float2ll_rn((hw * c[k].x + hw) * 256.0f);
+        Y[k] = __float2ll_rn((hh * c[k].y + hh) * 256.0f);
+    }
+    long long area = (X[1] - X[0]) * (Y[2] - Y[0]) - (Y[1] - Y[0]) * (X[2] - X[0]);
+    r.ok = area != 0;
+    if (!r.ok) return r;
+    int o1 = 1, o2 = 2;
+    if (area < 0) {
+        o1 = 2;
+        o2 = 1;
+        area = -area;
+    }
+    const int o[3] = {0, o1, o2};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        r.X[k] = X[o[k]];
+        r.Y[k] = Y[o[k]];
+        r.z[k] = c[o[k]].z;
+        r.order[k] = o[k];
+    }
+    r.area = area;
+    r.owned = 0;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const int a = (i + 1) % 3, b = (i + 2) % 3;
+        const long long dy = r.Y[b] - r.Y[a], dx = r.X[b] - r.X[a];
+        if (dy > 0 || (dy == 0 && dx > 0)) r.owned |= 1 << i;
+    }
+    long long mnx = min(r.X[0], min(r.X[1], r.X[2])), mxx = max(r.X[0], max(r.X[1], r.X[2]));
+    long long mny = min(r.Y[0], min(r.Y[1], r.Y[2])), mxy = max(r.Y[0], max(r.Y[1], r.Y[2]));
+    long long px0 = max(floor_div256(mnx), 0LL), px1 = min(floor_div256(mxx), (long long)W - 1);
+    long long py0 = max(floor_div256(mny), 0LL), py1 = min(floor_div256(mxy), (long long)H - 1);
+    if (px0 > px1 || py0 > py1) {
+        r.ok = false;
+        return r;
+    }
+    r.px0 = (int)px0;
+    r.px1 = (int)px1;
+    r.py0 = (int)py0;
+    r.py1 = (int)py1;
+    return r;
+}
+
+__device__ inline uint32_t tiles_of(const RSetup& r) {
+    if (!r.ok) return 0u;
+    return (uint32_t)(((r.px1 - r.px0) >> 3) + 1) * (uint32_t)(((r.py1 - r.py0) >> 3) + 1);
+}
+
+__device__ inline bool raster_test(const RSetup& r, long long sx, long long sy, double b[3], float& z) {
+    long long e[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const int a = (i + 1) % 3, c = (i + 2) % 3;
+        e[i] = (r.X[c] - r.X[a]) * (sy - r.Y[a]) - (r.Y[c] - r.Y[a]) * (sx - r.X[a]);
+        if (e[i] < 0 || (e[i] == 0 && !((r.owned >> i) & 1))) return false;
+    }
+    double bo[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) bo[i] = (double)e[i] / (double)r.area;
+    z = (float)((bo[0] * (double)r.z[0] + bo[1] * (double)r.z[1]) + bo[2] * (double)r.z[2]);
+    if (!(z >= 0.0f && z <= 1.0f)) return false;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) b[r.order[i]] = bo[i];
+    return true;
+}
+
+__device__ inline float3 interp3(const double b[3], const float3 v[3]) {
+    return make_float3((float)((b[0] * (double)v[0].x + b[1] * (double)v[1].x) + b[2] * (double)v[2].x),
+                       (float)((b[0] * (double)v[0].y + b[1] * (double)v[1].y) + b[2] * (double)v[2].y),
+                       (float)((b[0] * (double)v[0].z + b[1] * (double)v[1].z) + b[2] * (double)v[2].z));
+}
+
+// Walk tile `t` of a set-up triangle in the pinned order.
+template <class F>
+__device__ inline void raster_tile(const RSetup& r, uint32_t t, int nsamples, F&& frag) {
+    const int tw = ((r.px1 - r.px0) >> 3) + 1;
+    const int tx = r.px0 + 8 * (int)(t % (uint32_t)tw), ty = r.py0 + 8 * (int)(t / (uint32_t)tw);
+    const int xe = min(tx + 7, r.px1), ye = min(ty + 7, r.py1);
+    for (int py = ty; py <= ye; ++py)
+        for (int px = tx; px <= xe; ++px)
+            for (int s = 0; s < nsamples; ++s) {
+                long long sx, sy;
+                if (nsamples == 1) {
+                    sx = (long long)px * 256 + 128;
+                    sy = (long long)py * 256 + 128;
+                } else {
+                    sx = (long long)px * 256 + c_sample_loc8[s][0];
+                    sy = (long long)py * 256 + c_sample_loc8[s][1];
+                }
+                double b[3];
+                float z;
+                if (raster_test(r, sx, sy, b, z)) frag(px, py, b, z);
+            }
+}
+
+// ------------------------------------------------------------ pass params
+enum Kind { K_OPACITY = 0, K_INJECT = 1, K_SHADOW = 2, K_SVO = 3 };
+enum Phase { P_DIRECT = 0, P_COUNT = 1, P_WRITE = 2 };
+
+struct RasterArgs {
+    vct_scene s;
+    int kind;
+    int R;                 // clipmap resolution (clipmap passes) or octree resolution (SVO)
+    int W, H;              // viewport
+    int nlevels;           // clip levels rasterised per triangle
+    int levels[6];
+    float vp[6][3][16];    // per level, per axis view-projection
+    vct_voxelization_desc vd[6];
+    float pv[16];          // shadow pass: proj * view
+    // lighting (injection / SVO)
+    TraceParams light;     // light, shadow map and its desc (trace-shared struct)
+    float ldir[3];
+    // SVO normalisation
+    float center[3], ev;
+    // outputs
+    uint32_t* atlas;
+    float* depth;
+    uint32_t* frags;
+    int64_t frag_capacity;
+    int64_t items;
+};
+
+__device__ inline void item_of(const RasterArgs& A, int64_t item, int64_t& tri, int& lvl) {
+    tri = item / A.nlevels;
+    lvl = A.levels[item % A.nlevels];
+}
+
+// Clip-space vertices of item (tri, level) for the pass.
+__device__ inline bool item_setup(const RasterArgs& A, const WTri& w, int lvl, RSetup& rs, float3 pos[3]) {
+    float4 c[3];
+    if (A.kind == K_SHADOW) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) c[k] = mat_vec4(A.pv, w.p[k].x, w.p[k].y, w.p[k].z, 1.0f);
+    } else if (A.kind == K_SVO) {
+        float3 q[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            q[k] = make_float3((w.p[k].x - A.center[0]) / A.ev, (w.p[k].y - A.center[1]) / A.ev,
+                               (w.p[k].z - A.center[2]) / A.ev);
+            pos[k] = make_float3((q[k].x + 1.0f) * 0.5f, (q[k].y + 1.0f) * 0.5f, (q[k].z + 1.0f) * 0.5f);
+        }
+        const int axis = dominant_axis(q);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float a = axis == 0 ? q[k].y : q[k].x;
+            const float b = axis == 2 ? q[k].y : q[k].z;
+            c[k] = make_float4(a, b, 1.0f, 1.0f);
+        }
+    } else {
+        const int axis = dominant_axis(w.p);
+        const float* M = A.vp[lvl][axis];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) c[k] = mat_vec4(M, w.p[k].x, w.p[k].y, w.p[k].z, 1.0f);
+    }
+    rs = raster_setup(c, A.W, A.H);
+    return rs.ok;
+}
+
+__device__ inline int3 clip_image_coords(const vct_voxelization_desc& d, float3 wp) {
+    const float c = d.voxel_size * 0.25f;
+    const float lo = d.region_min_corner[0] + c, hi = d.region_max_corner[0] - c;
+    float p[3] = {fminf(fmaxf(wp.x, lo), hi), fminf(fmaxf(wp.y, lo), hi), fminf(fmaxf(wp.z, lo), hi)};
+    const int R = d.clipmap_resolution;
+    int ic[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float q = p[a] / d.clip_max_extent;
+        float f = q - floorf(q);
+        ic[a] = ((int)(f * (float)R)) % R;
+    }
+    return make_int3(ic[0] + 1, ic[1] + 1 + (R + 2) * (int)d.clip_level, ic[2] + 1);
+}
+
+__device__ inline uint32_t conv_rgba8(float x, float y, float z, float w) {
+    return (((uint32_t)w & 0xffu) << 24) | (((uint32_t)z & 0xffu) << 16) | (((uint32_t)y & 0xffu) << 8) |
+           ((uint32_t)x & 0xffu);
+}
+
+// The CAS-loop body of imageAtomicRGBA8Avg / atomicRGBA8Avg for one observed value.
+__device__ inline uint32_t rgba8_avg_fold(uint32_t cur, float vr, float vg, float vb, float va) {
+    if (cur == 0u) return conv_rgba8(vr, vg, vb, va);
+    float rx = (float)(cur & 0xffu), ry = (float)((cur >> 8) & 0xffu), rz = (float)((cur >> 16) & 0xffu),
+          rw = (float)(cur >> 24);
+    rx = rx * rw;
+    ry = ry * rw;
+    rz = rz * rw;
+    float cx = rx + vr, cy = ry + vg, cz = rz + vb, cw = rw + va;
+    cx = cx / cw;
+    cy = cy / cw;
+    cz = cz / cw;
+    return conv_rgba8(cx, cy, cz, cw);
+}
+
+// The reference's CAS loop itself (faithful atomic mode), bounded: gives up
+// after 1<<20 retries (never observed) and reports through `err`.
+__device__ inline void rgba8_avg_atomic(uint32_t* cell, float vr, float vg, float vb, float va, int* err) {
+    uint32_t prev = 0u, newv = conv_rgba8(vr, vg, vb, va), cur;
+    int guard = 0;
+    while ((cur = atomicCAS(cell, prev, newv)) != prev) {
+        prev = cur;
+        newv = rgba8_avg_fold(cur, vr, vg, vb, va);
+        if (++guard > (1 << 20)) {
+            atomicExch(err, 1);
+            return;
+        }
+    }
+}
+
+struct InjRecord {  // one face update of the injection, in traversal order
+    uint32_t key;
+    float r, g, b;
+};
+
+// Injection fragment (msaaInjectRadiance.frag:68-155) -> up to 6 face updates.
+// Returns the number of updates; writes them to upd[] (key, r, g, b) with a = 1.
+__device__ inline int inject_fragment(const RasterArgs& A, const WTri& w, const vct_gltf_shade_material& mat,
+                                      int lvl, const double b[3], InjRecord upd[6]) {
+    const vct_voxelization_desc& d = A.vd[lvl];
+    const float3 wp = interp3(b, w.p);
+    const int3 ic = clip_image_coords(d, wp);
+    if (mat.occlusion_texture > -1 && texture_1x1(A.s, mat.occlusion_texture).x < 0.1f) return 0;
+    const AtlasDims AD(A.R);
+    const int rb = A.R + 2;
+    const bool emissive = mat.emissive_factor[0] > 0.0f || mat.emissive_factor[1] > 0.0f || mat.emissive_factor[2] > 0.0f;
+    if (emissive) {
+        float e[3] = {mat.emissive_factor[0], mat.emissive_factor[1], mat.emissive_factor[2]};
+        if (mat.emissive_texture > -1) {
+            float4 tx = texture_1x1(A.s, mat.emissive_texture);
+            e[0] = e[0] + tx.x;
+            e[1] = e[1] + tx.y;
+            e[2] = e[2] + tx.z;
+        }
+        for (int k = 0; k < 3; ++k) e[k] = fminf(fmaxf(e[k], 0.0f), 1.0f) * 255.0f;
+        for (int f = 0; f < 6; ++f) upd[f] = InjRecord{(uint32_t)AD.index(ic.x + rb * f, ic.y, ic.z), e[0], e[1], e[2]};
+        return 6;
+    }
+    float4 color = make_float4(mat.pbr_base_color_factor[0], mat.pbr_base_color_factor[1], mat.pbr_base_color_factor[2],
+                               mat.pbr_base_color_factor[3]);
+    if (mat.pbr_base_color_texture > -1) {
+        float4 tx = texture_1x1(A.s, mat.pbr_base_color_texture);
+        color = make_float4(color.x * tx.x, color.y * tx.y, color.z * tx.z, color.w * tx.w);
+    }
+    const float3 nrm = normalize3h(interp3(b, w.n));
+    const float3 ld = make_float3(A.ldir[0], A.ldir[1], A.ldir[2]);
+    const float NdotL = fminf(fmaxf(dot3h(nrm, ld), 0.001f), 1.0f);
+    const float vis = calc_visibility(A.light, wp);
+    float lc[3];
+    for (int k = 0; k < 3; ++k) lc[k] = 0.0f + NdotL * vis * A.light.light.color[k] * A.light.light.intensity;
+    if (lc[0] == 0.0f && lc[1] == 0.0f && lc[2] == 0.0f) return 0;
+    float rad[3] = {lc[0] * color.x * color.w, lc[1] * color.y * color.w, lc[2] * color.z * color.w};
+    for (int k = 0; k < 3; ++k) rad[k] = fminf(fmaxf(rad[k], 0.0f), 1.0f);
+    const int face[3] = {-nrm.x > 0.0f ? 0 : 1, -nrm.y > 0.0f ? 2 : 3, -nrm.z > 0.0f ? 4 : 5};
+    const float wgt[3] = {fabsf(nrm.x), fabsf(nrm.y), fabsf(nrm.z)};
+    for (int k = 0; k < 3; ++k)
+        upd[k] = InjRecord{(uint32_t)AD.index(ic.x + rb * face[k], ic.y, ic.z), rad[0] * wgt[k] * 255.0f,
+                           rad[1] * wgt[k] * 255.0f, rad[2] * wgt[k] * 255.0f};
+    return 3;
+}
+
+// SVO fragment (voxelizer.frag:48-103).  Returns 0 if the occlusion texture
+// discards it (no slot), 1 with `*valid` false if the light test discards it
+// after the counter increment (slot left untouched), else 1 and the packed pair.
+__device__ inline int svo_fragment(const RasterArgs& A, const WTri& w, const vct_gltf_shade_material& mat,
+                                   const float3 pos[3], const double b[3], bool* valid, uint2* out) {
+    if (mat.occlusion_texture > -1 && texture_1x1(A.s, mat.occlusion_texture).x < 0.1f) return 0;
+    *valid = false;
+    const float3 fp = interp3(b, pos);
+    float rad[4] = {1.0f, 1.0f, 1.0f, 1.0f};
+    const bool emissive = mat.emissive_factor[0] > 0.0f || mat.emissive_factor[1] > 0.0f || mat.emissive_factor[2] > 0.0f;
+    if (emissive) {
+        float e[3] = {mat.emissive_factor[0], mat.emissive_factor[1], mat.emissive_factor[2]};
+        if (mat.emissive_texture > -1) {
+            float4 tx = texture_1x1(A.s, mat.emissive_texture);
+            e[0] = e[0] + tx.x;
+            e[1] = e[1] + tx.y;
+            e[2] = e[2] + tx.z;
+        }
+        for (int k = 0; k < 3; ++k) rad[k] = fminf(fmaxf(e[k], 0.0f), 1.0f);
+    } else {
+        float4 color = make_float4(0.f, 0.f, 0.f, 1.f);
+        if (mat.pbr_base_color_texture > -1) {
+            float4 tx = texture_1x1(A.s, mat.pbr_base_color_texture);
+            color = make_float4(tx.x * mat.pbr_base_color_factor[0], tx.y * mat.pbr_base_color_factor[1],
+                                tx.z * mat.pbr_base_color_factor[2], tx.w * mat.pbr_base_color_factor[3]);
+        }
+        const float3 nrm = normalize3h(interp3(b, w.n));
+        const float3 ld = make_float3(A.ldir[0], A.ldir[1], A.ldir[2]);
+        const float NdotL = fminf(fmaxf(dot3h(nrm, ld), 0.001f), 1.0f);
+        const float vis = calc_visibility(A.light, fp);
+        float lc[3];
+        for (int k = 0; k < 3; ++k) lc[k] = 0.0f + NdotL * vis * A.light.light.color[k] * A.light.light.intensity;
+        if (lc[0] == 0.0f && lc[1] == 0.0f && lc[2] == 0.0f) return 1;
+        const float cc[3] = {color.x, color.y, color.z};
+        for (int k = 0; k < 3; ++k) rad[k] = fminf(fmaxf(lc[k] * cc[k] * color.w, 0.0f), 1.0f);
+        rad[3] = 1.0f;
+    }
+    const float res = (float)A.R;
+    const uint32_t vx = (uint32_t)fminf(fmaxf(fp.x * res, 0.0f), res);
+    const uint32_t vy = (uint32_t)fminf(fmaxf(fp.y * res, 0.0f), res);
+    const uint32_t vz = (uint32_t)fminf(fmaxf(fp.z * res, 0.0f), res);
+    const uint32_t rgba = conv_rgba8(rad[0] * 255.0f, rad[1] * 255.0f, rad[2] * 255.0f, rad[3] * 255.0f);
+    out->x = vx | (vy << 12) | ((vz & 0xffu) << 24);
+    out->y = ((vz >> 8) << 28) | (rgba & 0xfffffffu);
+    *valid = true;
+    return 1;
+}
+
+// ---------------------------------------------------------------- kernels
+__global__ void k_item_tiles(RasterArgs A, uint32_t* __restrict__ tiles) {
+    for (int64_t item = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; item < A.items;
+         item += (int64_t)gridDim.x * blockDim.x) {
+        int64_t tri;
+        int lvl;
+        item_of(A, item, tri, lvl);
+        WTri w = world_triangle(A.s, tri);
+        RSetup rs;
+        float3 pos[3];
+        tiles[item] = item_setup(A, w, lvl, rs, pos) ? tiles_of(rs) : 0u;
+    }
+}
+
+template <int PHASE>
+__global__ void __launch_bounds__(128) k_raster_tiles(RasterArgs A, const uint32_t* __restrict__ tile_end,
+                                                      uint32_t* __restrict__ counts, const uint32_t* __restrict__ offs,
+                                                      InjRecord* __restrict__ recs, int* __restrict__ err) {
+    const uint32_t total = A.items > 0 ? tile_end[A.items - 1] : 0u;
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+        int64_t lo = 0, hi = A.items - 1;  // first item with tile_end > g
+        while (lo < hi) {
+            const int64_t mid = (lo + hi) >> 1;
+            if (tile_end[mid] > g) hi = mid;
+            else lo = mid + 1;
+        }
+        const int64_t item = lo;
+        const uint32_t local = g - (item > 0 ? tile_end[item - 1] : 0u);
+        int64_t tri;
+        int lvl;
+        item_of(A, item, tri, lvl);
+        const WTri w = world_triangle(A.s, tri);
+        RSetup rs;
+        float3 pos[3];
+        if (!item_setup(A, w, lvl, rs, pos)) continue;
+        const vct_gltf_shade_material mat =
+            A.s.materials ? A.s.materials[min((int)w.material, A.s.material_count - 1)] : vct_gltf_shade_material{};
+        uint32_t n = 0;
+        uint32_t base = (PHASE == P_WRITE) ? offs[g] : 0u;
+        if (A.kind == K_OPACITY) {
+            const vct_voxelization_desc& d = A.vd[lvl];
+            const AtlasDims AD(A.R);
+            raster_tile(rs, local, 8, [&](int, int, const double* b, float) {
+                const float3 wp = interp3(b, w.p);
+                if (wp.x < d.region_min_corner[0] || wp.y < d.region_min_corner[1] || wp.z < d.region_min_corner[2] ||
+                    wp.x > d.region_max_corner[0] || wp.y > d.region_max_corner[1] || wp.z > d.region_max_corner[2])
+                    return;
+                if (mat.occlusion_texture > -1 && texture_1x1(A.s, mat.occlusion_texture).x < 0.1f) return;
+                const int3 ic = clip_image_coords(d, wp);
+                for (int f = 0; f < 6; ++f) A.atlas[AD.index(ic.x + (A.R + 2) * f, ic.y, ic.z)] = 0xFFFFFFFFu;
+            });
+        } else if (A.kind == K_SHADOW) {
+            raster_tile(rs, local, 1, [&](int px, int py, const double*, float z) {
+                atomicMin(reinterpret_cast<unsigned int*>(A.depth) + (int64_t)py * A.W + px, __float_as_uint(z));
+            });
+        } else if (A.kind == K_INJECT) {
+            raster_tile(rs, local, 8, [&](int, int, const double* b, float) {
+                InjRecord upd[6];
+                const int k = inject_fragment(A, w, mat, lvl, b, upd);
+                if (PHASE == P_DIRECT) {
+                    for (int i = 0; i < k; ++i) rgba8_avg_atomic(A.atlas + upd[i].key, upd[i].r, upd[i].g, upd[i].b, 1.0f, err);
+                } else if (PHASE == P_WRITE) {
+                    for (int i = 0; i < k; ++i) recs[base + n + i] = upd[i];
+                }
+                n += k;
+            });
+        } else {  // K_SVO
+            raster_tile(rs, local, 8, [&](int, int, const double* b, float) {
+                bool valid;
+                uint2 v;
+                const int k = svo_fragment(A, w, mat, pos, b, &valid, &v);
+                if (PHASE == P_WRITE && k && valid) {
+                    const uint64_t slot = (uint64_t)base + n;
+                    if ((int64_t)slot < A.frag_capacity) reinterpret_cast<uint2*>(A.frags)[slot] = v;
+                }
+                n += k;
+            });
+        }
+        if (PHASE == P_COUNT) counts[g] = n;
+    }
+}
+
+// Sequential per-texel fold of the stably sorted injection records.
+__global__ void k_inject_fold(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ order,
+                              const InjRecord* __restrict__ recs, uint32_t n, uint32_t* __restrict__ atlas) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t key = keys[i];
+        if (i > 0 && keys[i - 1] == key) continue;
+        uint32_t cell = atlas[key];
+        for (uint32_t j = i; j < n && keys[j] == key; ++j) {
+            const InjRecord& r = recs[order[j]];
+            cell = rgba8_avg_fold(cell, r.r, r.g, r.b, 1.0f);
+        }
+        atlas[key] = cell;
+    }
+}
+
+__global__ void k_iota(uint32_t* v, uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[i] = i;
+}
+__global__ void k_rec_keys(const InjRecord* r, uint32_t* k, uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) k[i] = r[i].key;
+}
+__global__ void k_fill_f32(float* p, int64_t n, float v) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = v;
+}
+
+// ---------------------------------------------------------------- host side
+static int grid_of(int64_t n, int block, int cap = 152 * 32) {
+    int64_t g = (n + block - 1) / block;
+    return (int)(g < 1 ? 1 : (g > cap ? cap : g));
+}
+
+static int ws_reserve(vct_workspace_s* ws, size_t bytes) {
+    if (ws->bytes >= bytes) return VCT_OK;
+    if (ws->ptr) {
+        VCT_CUDA_TRY(cudaDeviceSynchronize());
+        VCT_CUDA_TRY(cudaFree(ws->ptr));
+        ws->ptr = nullptr;
+        ws->bytes = 0;
+    }
+    size_t want = bytes + bytes / 4;
+    VCT_CUDA_TRY(cudaMalloc(&ws->ptr, want));
+    ws->bytes = want;
+    return VCT_OK;
+}
+
+static size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
+
+static int check_scene(const vct_scene* s) {
+    VCT_CHECK_ARG(s, "null scene");
+    VCT_CHECK_ARG(s->triangle_count >= 0 && s->triangle_count < (1LL << 31), "scene triangle count out of range");
+    if (s->triangle_count == 0) return VCT_OK;
+    VCT_CHECK_ARG(s->positions && s->normals && s->indices, "scene positions / normals / indices are required");
+    VCT_CHECK_ARG(s->materials && s->material_count > 0, "scene needs at least one material");
+    VCT_CHECK_ARG(!s->node_matrices || s->instance_count > 0, "node matrices given without an instance count");
+    return VCT_OK;
+}
+
+// Tile counting + prefix sum shared by every pass.  On return tile_end (in the
+// workspace) holds inclusive sums; *total receives the tile count (host).
+static int plan_tiles(RasterArgs& A, vct_workspace_s* ws, size_t& off, uint32_t** tile_end, uint32_t* total,
+                      cudaStream_t st) {
+    const size_t n = (size_t)A.items;
+    size_t scan_bytes = 0;
+    VCT_CUDA_TRY(cub::DeviceScan::InclusiveSum(nullptr, scan_bytes, (uint32_t*)nullptr, (uint32_t*)nullptr, (int)n));
+    const size_t need = a256(4 * n) * 2 + a256(scan_bytes) + 256;
+    int rc = ws_reserve(ws, need);
+    if (rc != VCT_OK) return rc;
+    char* base = (char*)ws->ptr;
+    uint32_t* counts = (uint32_t*)base;
+    *tile_end = (uint32_t*)(base + a256(4 * n));
+    void* tmp = base + 2 * a256(4 * n);
+    off = 2 * a256(4 * n) + a256(scan_bytes);
+    k_item_tiles<<<grid_of(n, 128), 128, 0, st>>>(A, counts);
+    VCT_LAUNCH_CHECK();
+    VCT_CUDA_TRY(cub::DeviceScan::InclusiveSum(tmp, scan_bytes, counts, *tile_end, (int)n, st));
+    VCT_CUDA_TRY(cudaMemcpyAsync(total, *tile_end + (n - 1), 4, cudaMemcpyDeviceToHost, st));
+    VCT_CUDA_TRY(cudaStreamSynchronize(st));
+    return VCT_OK;
+}
+
+static void fill_clipmap_levels(RasterArgs& A, const vct_clipmap_region* regions, int R, uint32_t level_mask) {
+    A.nlevels = 0;
+    for (int l = 0; l < 6; ++l) {
+        voxel_view_proj(regions[l], &A.vp[l][0][0]);
+        A.vd[l] = voxelization_desc(regions, l, R);
+        if ((level_mask >> l) & 1u) A.levels[A.nlevels++] = l;
+    }
+}
+
+static int fill_light(RasterArgs& A, const vct_shadow_map* shadow, const vct_directional_light_desc* light,
+                      const vct_directional_light_shadow_desc* light_shadow) {
+    VCT_CHECK_ARG(light, "null light");
+    memset(&A.light, 0, sizeof(A.light));
+    A.light.light = *light;
+    if (shadow && shadow->depth) {
+        VCT_CHECK_ARG(light_shadow, "shadow map given without its light shadow desc");
+        VCT_CHECK_ARG(shadow->width > 0 && shadow->height > 0, "bad shadow map size");
+        A.light.shadow = shadow->depth;
+        A.light.shadow_w = shadow->width;
+        A.light.shadow_h = shadow->height;
+        A.light.shadow_desc = *light_shadow;
+    }
+    float3 l = normalize3h(make_float3(-light->direction[0], -light->direction[1], -light->direction[2]));
+    A.ldir[0] = l.x;
+    A.ldir[1] = l.y;
+    A.ldir[2] = l.z;
+    return VCT_OK;
+}
+
+}  // namespace vct
+
+using namespace vct;
+
+extern "C" int vct_workspace_create(size_t initial_bytes, vct_workspace_s** out) {
+    VCT_CHECK_ARG(out, "vct_workspace_create: null output");
+    auto* w = new vct_workspace_s();
+    if (initial_bytes) {
+        cudaError_t e = cudaMalloc(&w->ptr, initial_bytes);
+        if (e != cudaSuccess) {
+            delete w;
+            return cuda_fail(e, "cudaMalloc (workspace)");
+        }
+        w->bytes = initial_bytes;
+    }
+    *out = w;
+    return VCT_OK;
+}
+
+extern "C" int vct_workspace_destroy(vct_workspace_s* w) {
+    if (!w) return VCT_OK;
+    cudaError_t e = w->ptr ? cudaFree(w->ptr) : cudaSuccess;
+    delete w;
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFree (workspace)");
+    return VCT_OK;
+}
+
+extern "C" int64_t vct_workspace_bytes(vct_workspace_s* w) { return w ? (int64_t)w->bytes : -1; }
+
+extern "C" int vct_voxelization_view_proj(const vct_clipmap_region* region, float out[48]) {
+    VCT_CHECK_ARG(region && out, "vct_voxelization_view_proj: null argument");
+    voxel_view_proj(*region, out);
+    return VCT_OK;
+}
+
+extern "C" int vct_voxelization_desc_for(const vct_clipmap_region regions[6], int32_t level, int32_t R,
+                                         vct_voxelization_desc* out) {
+    VCT_CHECK_ARG(regions && out && level >= 0 && level < 6, "vct_voxelization_desc_for: bad argument");
+    *out = voxelization_desc(regions, level, R);
+    return VCT_OK;
+}
+
+extern "C" int vct_directional_light_shadow(const float origin[3], const float direction[3], float z_near, float z_far,
+                                            vct_directional_light_shadow_desc* out) {
+    VCT_CHECK_ARG(origin && direction && out, "vct_directional_light_shadow: null argument");
+    VCT_CHECK_ARG(z_far > z_near, "vct_directional_light_shadow: far must exceed near");
+    float3 o = make_float3(origin[0], origin[1], origin[2]);
+    float3 d = normalize3h(make_float3(direction[0], direction[1], direction[2]));
+    M4 view = look_at_lh(o, make_float3(o.x + d.x, o.y + d.y, o.z + d.z), make_float3(0.f, 1.f, 0.f));
+    M4 proj = ortho_lh_zo(-16.0f, 16.0f, -16.0f, 16.0f, z_near, z_far);
+    memcpy(out->view, view.m, 64);
+    memcpy(out->proj, proj.m, 64);
+    out->z_near = z_near;
+    out->z_far = z_far;
+    return VCT_OK;
+}
+
+extern "C" int vct_clear_atlas(uint32_t* atlas, int32_t R, void* stream) {
+    VCT_CHECK_ARG(atlas && valid_resolution(R), "vct_clear_atlas: bad argument");
+    VCT_CUDA_TRY(cudaMemsetAsync(atlas, 0, sizeof(uint32_t) * AtlasDims(R).texels(), as_stream(stream)));
+    return VCT_OK;
+}
+
+extern "C" int vct_voxelize_opacity(const vct_scene* scene, const vct_clipmap_region regions[6], int32_t R,
+                                    uint32_t* atlas, uint32_t level_mask, vct_workspace_s* ws, void* stream) {
+    int rc = check_scene(scene);
+    if (rc != VCT_OK) return rc;
+    VCT_CHECK_ARG(regions && atlas && ws && valid_resolution(R), "vct_voxelize_opacity: bad argument");
+    VCT_CHECK_ARG((level_mask & ~0x3Fu) == 0, "vct_voxelize_opacity: level mask has bits above level 5");
+    if (scene->triangle_count == 0 || level_mask == 0) return VCT_OK;
+    RasterArgs A;
+    memset(&A, 0, sizeof(A));
+    A.s = *scene;
+    A.kind = K_OPACITY;
+    A.R = R;
+    A.W = A.H = R + 2;
+    fill_clipmap_levels(A, regions, R, level_mask);
+    A.items = scene->triangle_count * A.nlevels;
+    A.atlas = atlas;
+    cudaStream_t st = as_stream(stream);
+    size_t off;
+    uint32_t* tile_end;
+    uint32_t total;
+    rc = plan_tiles(A, ws, off, &tile_end, &total, st);
+    if (rc != VCT_OK) return rc;
+    if (total) k_raster_tiles<P_DIRECT><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, nullptr, nullptr, nullptr, nullptr);
+    VCT_LAUNCH_CHECK();
+    return VCT_OK;
+}
+
+extern "C" int vct_shadow_depth(const vct_scene* scene, const vct_directional_light_shadow_desc* sd, float* depth,
+                                int32_t W, int32_t H, vct_workspace_s* ws, void* stream) {
+    int rc = check_scene(scene);
+    if (rc != VCT_OK) return rc;
+    VCT_CHECK_ARG(sd && depth && ws && W > 0 && H > 0 && W <= 32768 && H <= 32768, "vct_shadow_depth: bad argument");
+    cudaStream_t st = as_stream(stream);
+    const int64_t npx = (int64_t)W * H;
+    k_fill_f32<<<grid_of(npx, 256), 256, 0, st>>>(depth, npx, 1.0f);
+    VCT_LAUNCH_CHECK();
+    if (scene->triangle_count == 0) return VCT_OK;
+    RasterArgs A;
+    memset(&A, 0, sizeof(A));
+    A.s = *scene;
+    A.kind = K_SHADOW;
+    A.W = W;
+    A.H = H;
+    A.nlevels = 1;
+    A.levels[0] = 0;
+    M4 pv = mat_mul4(sd->proj, sd->view);
+    memcpy(A.pv, pv.m, 64);
+    A.items = scene->triangle_count;
+    A.depth = depth;
+    size_t off;
+    uint32_t* tile_end;
+    uint32_t total;
+    rc = plan_tiles(A, ws, off, &tile_end, &total, st);
+    if (rc != VCT_OK) return rc;
+    if (total) k_raster_tiles<P_DIRECT><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, nullptr, nullptr, nullptr, nullptr);
+    VCT_LAUNCH_CHECK();
+    return VCT_OK;
+}
+
+extern "C" int vct_inject_radiance(const vct_scene* scene, const vct_clipmap_region regions[6], int32_t R,
+                                   const vct_shadow_map* shadow, const vct_directional_light_desc* light,
+                                   const vct_directional_light_shadow_desc* light_shadow, uint32_t* atlas,
+                                   uint32_t level_mask, int32_t mode, vct_workspace_s* ws, void* stream) {
+    int rc = check_scene(scene);
+    if (rc != VCT_OK) return rc;
+    VCT_CHECK_ARG(regions && atlas && ws && valid_resolution(R), "vct_inject_radiance: bad argument");
+    VCT_CHECK_ARG(mode == VCT_INJECT_DETERMINISTIC || mode == VCT_INJECT_ATOMIC, "vct_inject_radiance: bad mode");
+    VCT_CHECK_ARG((level_mask & ~0x3Fu) == 0, "vct_inject_radiance: level mask has bits above level 5");
+    if (scene->triangle_count == 0 || level_mask == 0) return VCT_OK;
+    RasterArgs A;
+    memset(&A, 0, sizeof(A));
+    A.s = *scene;
+    A.kind = K_INJECT;
+    A.R = R;
+    A.W = A.H = R + 2;
+    fill_clipmap_levels(A, regions, R, level_mask);
+    rc = fill_light(A, shadow, light, light_shadow);
+    if (rc != VCT_OK) return rc;
+    A.items = scene->triangle_count * A.nlevels;
+    A.atlas = atlas;
+    cudaStream_t st = as_stream(stream);
+    size_t off;
+    uint32_t* tile_end;
+    uint32_t total;
+    rc = plan_tiles(A, ws, off, &tile_end, &total, st);
+    if (rc != VCT_OK) return rc;
+    if (total == 0) return VCT_OK;
+    if (mode == VCT_INJECT_ATOMIC) {
+        int* err = (int*)((char*)ws->ptr + off);
+        VCT_CUDA_TRY(cudaMemsetAsync(err, 0, 4, st));
+        k_raster_tiles<P_DIRECT><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, nullptr, nullptr, nullptr, err);
+        VCT_LAUNCH_CHECK();
+        int herr = 0;
+        VCT_CUDA_TRY(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st));
+        VCT_CUDA_TRY(cudaStreamSynchronize(st));
+        if (herr) return fail(VCT_E_TIMEOUT, "vct_inject_radiance: a CAS loop gave up after 2^20 retries");
+        return VCT_OK;
+    }
+    // deterministic: count -> scan -> write records -> stable sort by texel -> fold
+    size_t scan_bytes = 0;
+    VCT_CUDA_TRY(cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, (uint32_t*)nullptr, (uint32_t*)nullptr, (int)total));
+    const size_t head = off;
+    size_t need = head + a256(4 * (size_t)total) * 2 + a256(scan_bytes) + 256;
+    // keep tile_end valid across a possible growth: grow first, then recount
+    if (ws->bytes < need) {
+        rc = ws_reserve(ws, need);
+        if (rc != VCT_OK) return rc;
+        rc = plan_tiles(A, ws, off, &tile_end, &total, st);
+        if (rc != VCT_OK) return rc;
+    }
+    char* base = (char*)ws->ptr;
+    uint32_t* counts = (uint32_t*)(base + head);
+    uint32_t* offs = (uint32_t*)(base + head + a256(4 * (size_t)total));
+    void* tmp = base + head + 2 * a256(4 * (size_t)total);
+    k_raster_tiles<P_COUNT><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, counts, nullptr, nullptr, nullptr);
+    VCT_LAUNCH_CHECK();
+    VCT_CUDA_TRY(cub::DeviceScan::ExclusiveSum(tmp, scan_bytes, counts, offs, (int)total, st));
+    uint32_t last[2];
+    VCT_CUDA_TRY(cudaMemcpyAsync(&last[0], offs + (total - 1), 4, cudaMemcpyDeviceToHost, st));
+    VCT_CUDA_TRY(cudaMemcpyAsync(&last[1], counts + (total - 1), 4, cudaMemcpyDeviceToHost, st));
+    VCT_CUDA_TRY(cudaStreamSynchronize(st));
+    const uint64_t nrec64 = (uint64_t)last[0] + last[1];
+    if (nrec64 == 0) return VCT_OK;
+    if (nrec64 >= (1ull << 31)) return fail(VCT_E_OVERFLOW, "vct_inject_radiance: more than 2^31 face updates");
+    const uint32_t nrec = (uint32_t)nrec64;
+    size_t sort_bytes = 0;
+    VCT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(nullptr, sort_bytes, (uint32_t*)nullptr, (uint32_t*)nullptr,
+                                                 (uint32_t*)nullptr, (uint32_t*)nullptr, (int)nrec, 0, 32));
+    const size_t rec_off = head + a256(4 * (size_t)total) * 2 + a256(scan_bytes);
+    need = rec_off + a256(sizeof(InjRecord) * nrec) + 4 * a256(4 * (size_t)nrec) + a256(sort_bytes) + 256;
+    if (ws->bytes < need) {
+        // grow and redo the counting passes (their buffers move with the arena)
+        rc = ws_reserve(ws, need);
+        if (rc != VCT_OK) return rc;
+        return vct_inject_radiance(scene, regions, R, shadow, light, light_shadow, atlas, level_mask, mode, ws, stream);
+    }
+    base = (char*)ws->ptr;
+    InjRecord* recs = (InjRecord*)(base + rec_off);
+    uint32_t* kin = (uint32_t*)(base + rec_off + a256(sizeof(InjRecord) * nrec));
+    uint32_t* kout = kin + a256(4 * (size_t)nrec) / 4;
+    uint32_t* vin = kout + a256(4 * (size_t)nrec) / 4;
+    uint32_t* vout = vin + a256(4 * (size_t)nrec) / 4;
+    void* stmp = (char*)(vout + a256(4 * (size_t)nrec) / 4);
+    k_raster_tiles<P_WRITE><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, nullptr, offs, recs, nullptr);
+    VCT_LAUNCH_CHECK();
+    k_rec_keys<<<grid_of(nrec, 256), 256, 0, st>>>(recs, kin, nrec);
+    k_iota<<<grid_of(nrec, 256), 256, 0, st>>>(vin, nrec);
+    VCT_LAUNCH_CHECK();
+    const int key_bits = 32 - __builtin_clz((unsigned)AtlasDims(R).texels());
+    VCT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(stmp, sort_bytes, kin, kout, vin, vout, (int)nrec, 0, key_bits, st));
+    k_inject_fold<<<grid_of(nrec, 256), 256, 0, st>>>(kout, vout, recs, nrec, atlas);
+    VCT_LAUNCH_CHECK();
+    return VCT_OK;
+}
+
+extern "C" int vct_svo_fragments(const vct_scene* scene, int32_t octree_level, const float bb_min[3],
+                                 const float bb_max[3], const vct_shadow_map* shadow,
+                                 const vct_directional_light_desc* light,
+                                 const vct_directional_light_shadow_desc* light_shadow, uint32_t* frags,
+                                 int64_t capacity, int64_t* count, vct_workspace_s* ws, void* stream) {
+    int rc = check_scene(scene);
+    if (rc != VCT_OK) return rc;
+    VCT_CHECK_ARG(count && bb_min && bb_max && ws, "vct_svo_fragments: null argument");
+    VCT_CHECK_ARG(octree_level >= 1 && octree_level <= 11, "vct_svo_fragments: octree level must be 1..11");
+    VCT_CHECK_ARG(capacity >= 0 && (capacity == 0 || frags), "vct_svo_fragments: bad fragment buffer");
+    *count = 0;
+    if (scene->triangle_count == 0) return VCT_OK;
+    RasterArgs A;
+    memset(&A, 0, sizeof(A));
+    A.s = *scene;
+    A.kind = K_SVO;
+    A.R = 1 << octree_level;
+    A.W = A.H = A.R;
+    A.nlevels = 1;
+    A.levels[0] = 0;
+    rc = fill_light(A, shadow, light, light_shadow);
+    if (rc != VCT_OK) return rc;
+    float ext[3];
+    for (int a = 0; a < 3; ++a) {
+        ext[a] = bb_max[a] - bb_min[a];
+        A.center[a] = (bb_min[a] + bb_max[a]) * 0.5f;
+    }
+    A.ev = fmaxf(ext[0], fmaxf(ext[1], ext[2])) * 0.5f;
+    VCT_CHECK_ARG(A.ev > 0.0f, "vct_svo_fragments: empty scene bounding box");
+    A.items = scene->triangle_count;
+    A.frags = frags;
+    A.frag_capacity = capacity;
+    cudaStream_t st = as_stream(stream);
+    size_t off;
+    uint32_t* tile_end;
+    uint32_t total;
+    rc = plan_tiles(A, ws, off, &tile_end, &total, st);
+    if (rc != VCT_OK) return rc;
+    if (total == 0) return VCT_OK;
+    size_t scan_bytes = 0;
+    VCT_CUDA_TRY(cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, (uint32_t*)nullptr, (uint32_t*)nullptr, (int)total));
+    const size_t need = off + a256(4 * (size_t)total) * 2 + a256(scan_bytes) + 256;
+    if (ws->bytes < need) {
+        rc = ws_reserve(ws, need);
+        if (rc != VCT_OK) return rc;
+        return vct_svo_fragments(scene, octree_level, bb_min, bb_max, shadow, light, light_shadow, frags, capacity,
+                                 count, ws, stream);
+    }
+    char* base = (char*)ws->ptr;
+    uint32_t* counts = (uint32_t*)(base + off);
+    uint32_t* offs = (uint32_t*)(base + off + a256(4 * (size_t)total));
+    void* tmp = base + off + 2 * a256(4 * (size_t)total);
+    // count pass (SparseVoxelizer::preVoxelize), host readback of the count
+    k_raster_tiles<P_COUNT><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, counts, nullptr, nullptr, nullptr);
+    VCT_LAUNCH_CHECK();
+    VCT_CUDA_TRY(cub::DeviceScan::ExclusiveSum(tmp, scan_bytes, counts, offs, (int)total, st));
+    uint32_t last[2];
+    VCT_CUDA_TRY(cudaMemcpyAsync(&last[0], offs + (total - 1), 4, cudaMemcpyDeviceToHost, st));
+    VCT_CUDA_TRY(cudaMemcpyAsync(&last[1], counts + (total - 1), 4, cudaMemcpyDeviceToHost, st));
+    VCT_CUDA_TRY(cudaStreamSynchronize(st));
+    *count = (int64_t)last[0] + last[1];
+    if (capacity == 0) return VCT_OK;  // count-only call
+    if (*count > capacity) return fail(VCT_E_OVERFLOW, "vct_svo_fragments: fragment list capacity too small");
+    // write pass (SparseVoxelizer::cmdVoxelize); discarded slots stay zero
+    VCT_CUDA_TRY(cudaMemsetAsync(frags, 0, sizeof(uint32_t) * 2 * (size_t)*count, st));
+    k_raster_tiles<P_WRITE><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, nullptr, offs, nullptr, nullptr);
+    VCT_LAUNCH_CHECK();
+    return VCT_OK;
+}

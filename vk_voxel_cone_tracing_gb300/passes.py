@@ -1,0 +1,121 @@
+"""Python face of the rasterisation-driven passes (voxelise, shadow depth,
+radiance injection, SVO fragment list) over torch device tensors.
+
+``DeviceScene`` uploads a ``scene.Scene`` into the vct_scene layout;
+``Workspace`` owns the device scratch arena the raster passes use.  Every
+function calls the CUDA library through the C ABI on the current stream.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import capi
+from .clipmap import _ptr, _stream
+
+
+class Workspace:
+    """vct_workspace: device scratch arena grown on demand by the raster passes."""
+
+    def __init__(self, initial_bytes: int = 0):
+        h = C.c_void_p()
+        capi.call("vct_workspace_create", initial_bytes, C.byref(h))
+        self.handle = h
+
+    @property
+    def nbytes(self) -> int:
+        return int(capi.lib().vct_workspace_bytes(self.handle))
+
+    def close(self):
+        if self.handle:
+            capi.call("vct_workspace_destroy", self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class DeviceScene:
+    """A scene.Scene resident on the GPU, with its vct_scene descriptor."""
+
+    def __init__(self, scene, device="cuda"):
+        self.positions = torch.from_numpy(np.ascontiguousarray(scene.positions, np.float32)).to(device)
+        self.normals = torch.from_numpy(np.ascontiguousarray(scene.normals, np.float32)).to(device)
+        self.indices = torch.from_numpy(np.ascontiguousarray(scene.indices, np.uint32).view(np.int32)).to(device)
+        self.tri_material = torch.from_numpy(np.ascontiguousarray(scene.tri_material, np.uint32).view(np.int32)).to(device)
+        self.materials = torch.from_numpy(np.ascontiguousarray(scene.materials).view(np.uint8)).to(device)
+        self.textures = torch.from_numpy(np.ascontiguousarray(scene.textures, np.uint32).view(np.int32)).to(device)
+        self.desc = capi.Scene(self.positions.data_ptr(), self.normals.data_ptr(), self.indices.data_ptr(),
+                               scene.positions.shape[0], scene.indices.shape[0], self.tri_material.data_ptr(),
+                               self.materials.data_ptr(), scene.materials.shape[0], self.textures.data_ptr(),
+                               scene.textures.shape[0], None, None, 0)
+        p = scene.positions
+        self.bb_min = p.min(0).astype(np.float32)
+        self.bb_max = p.max(0).astype(np.float32)
+
+    @property
+    def triangle_count(self) -> int:
+        return int(self.desc.triangle_count)
+
+
+def light_desc(direction=(0.3, -1.0, 0.2), intensity=1.0, color=(1.0, 1.0, 1.0)) -> capi.DirectionalLightDesc:
+    return capi.DirectionalLightDesc(capi.f3(*direction), intensity, capi.f3(*color), 0)
+
+
+def light_shadow_desc(origin, direction, z_near=0.1, z_far=30.0) -> capi.DirectionalLightShadowDesc:
+    out = capi.DirectionalLightShadowDesc()
+    o = (C.c_float * 3)(*origin)
+    d = (C.c_float * 3)(*direction)
+    capi.call("vct_directional_light_shadow", C.cast(o, C.c_void_p), C.cast(d, C.c_void_p), z_near, z_far,
+              capi.ref(out))
+    return out
+
+
+def clear_atlas(atlas: torch.Tensor, R: int) -> None:
+    capi.call("vct_clear_atlas", _ptr(atlas), R, _stream())
+
+
+def voxelize_opacity(dscene: DeviceScene, regions, R: int, atlas: torch.Tensor, ws: Workspace,
+                     level_mask: int = 0x3F) -> None:
+    capi.call("vct_voxelize_opacity", capi.ref(dscene.desc), C.cast(regions, C.c_void_p), R, _ptr(atlas),
+              level_mask, ws.handle, _stream())
+
+
+def shadow_depth(dscene: DeviceScene, sd: capi.DirectionalLightShadowDesc, depth: torch.Tensor, ws: Workspace) -> None:
+    H, W = depth.shape
+    capi.call("vct_shadow_depth", capi.ref(dscene.desc), capi.ref(sd), _ptr(depth), W, H, ws.handle, _stream())
+
+
+def _shadow_map(depth: torch.Tensor | None) -> capi.ShadowMap:
+    if depth is None:
+        return capi.ShadowMap(None, 0, 0)
+    return capi.ShadowMap(depth.data_ptr(), depth.shape[1], depth.shape[0])
+
+
+def inject_radiance(dscene: DeviceScene, regions, R: int, depth: torch.Tensor | None,
+                    light: capi.DirectionalLightDesc, sd: capi.DirectionalLightShadowDesc, atlas: torch.Tensor,
+                    ws: Workspace, level_mask: int = 0x3F, mode: int = capi.INJECT_DETERMINISTIC) -> None:
+    sm = _shadow_map(depth)
+    capi.call("vct_inject_radiance", capi.ref(dscene.desc), C.cast(regions, C.c_void_p), R, capi.ref(sm),
+              capi.ref(light), capi.ref(sd), _ptr(atlas), level_mask, mode, ws.handle, _stream())
+
+
+def svo_fragments(dscene: DeviceScene, level: int, depth: torch.Tensor | None, light: capi.DirectionalLightDesc,
+                  sd: capi.DirectionalLightShadowDesc, ws: Workspace, bb_min=None, bb_max=None):
+    """Count pass + write pass; returns an (F, 2) int32 tensor of packed fragments."""
+    bmin = (C.c_float * 3)(*(dscene.bb_min if bb_min is None else bb_min))
+    bmax = (C.c_float * 3)(*(dscene.bb_max if bb_max is None else bb_max))
+    sm = _shadow_map(depth)
+    count = C.c_int64(0)
+    capi.call("vct_svo_fragments", capi.ref(dscene.desc), level, C.cast(bmin, C.c_void_p), C.cast(bmax, C.c_void_p),
+              capi.ref(sm), capi.ref(light), capi.ref(sd), None, 0, C.byref(count), ws.handle, _stream())
+    frags = torch.empty((max(count.value, 1), 2), dtype=torch.int32, device=dscene.positions.device)
+    capi.call("vct_svo_fragments", capi.ref(dscene.desc), level, C.cast(bmin, C.c_void_p), C.cast(bmax, C.c_void_p),
+              capi.ref(sm), capi.ref(light), capi.ref(sd), _ptr(frags), count.value, C.byref(count), ws.handle,
+              _stream())
+    return frags[:count.value]
