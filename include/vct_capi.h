@@ -387,6 +387,45 @@ int vct_svo_fragments(const vct_scene* scene, int32_t octree_level, const float 
                       const vct_directional_light_shadow_desc* light_shadow, uint32_t* fragments,
                       int64_t capacity, int64_t* count_host, vct_workspace ws, void* stream);
 
+/* ------------------------------------------------ sparse voxel octree */
+
+/* OctreeBuilder::initialize pool size: clamp(8 * fragments, 1e6, 5e8) nodes
+ * (VFS/RenderPass/Octree/OctreeBuilder.cpp:110-113). */
+int64_t vct_svo_pool_capacity(int64_t fragment_count);
+
+/* OctreeBuilder::cmdBuild (VFS/RenderPass/Octree/OctreeBuilder.cpp:205-345):
+ * per level init / flag / allocate / advance the window, RGBA8 leaf average,
+ * isotropic mips, over a uint2 node pool {MSB flag | child block, RGBA8}.
+ * VCT_SVO_DETERMINISTIC allocates child blocks in breadth-first index order
+ * and folds leaf colours in fragment order (bit-exact against the oracle);
+ * VCT_SVO_ATOMIC uses the reference's atomic allocation and CAS loops
+ * (equal to the deterministic pool after vct_svo_canonicalize, except for
+ * leaf colours averaged in a different order).  *node_count_host receives
+ * the number of nodes in use. */
+#define VCT_SVO_DETERMINISTIC 0
+#define VCT_SVO_ATOMIC 1
+int vct_svo_build(const uint32_t* fragments, int64_t fragment_count, int32_t octree_level, uint32_t* node_pool,
+                  int64_t pool_capacity, int32_t mode, int64_t* node_count_host, vct_workspace ws, void* stream);
+
+/* Relabel a node pool's child blocks into breadth-first order (the order a
+ * scan allocation produces), so pools built with racy allocation compare
+ * bit for bit.  `pool_out` must not alias `pool_in`. */
+int vct_svo_canonicalize(const uint32_t* pool_in, int64_t node_count, int32_t octree_level, uint32_t* pool_out,
+                         vct_workspace ws, void* stream);
+
+/* OctreeVoxelConeTracing::onUpdate (VFS/RenderPass/Octree/OctreeVoxelConeTracing.cpp:74-104)
+ * running voxelConeTracing_Octree.frag: the cone loop of vct_cone_trace
+ * sampling the node pool by point location.  `bb_min/bb_max` is the scene box
+ * the shader normalises positions with (it hard-codes Sponza's,
+ * voxelConeTracing_Octree.frag:321-322); desc->volume_dimension is the pool's
+ * root resolution (the pass passes 256). */
+int vct_svo_cone_trace(const vct_cone_tracing_desc* desc, const vct_cam_matrix* cam, const uint32_t* node_pool,
+                       int64_t node_count, const float bb_min_host[3], const float bb_max_host[3],
+                       const vct_shadow_map* shadow, const vct_directional_light_desc* light,
+                       const vct_directional_light_shadow_desc* light_shadow,
+                       const vct_surface_sample* samples, int64_t sample_count, float* diffuse_out,
+                       float* specular_out, unsigned long long* cone_steps, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

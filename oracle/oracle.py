@@ -75,6 +75,9 @@ def lib():
         L.vcto_svo_fragments.argtypes = [P, C.c_int, P, P, P, C.c_int, C.c_int, P, P, P, C.c_int64]
         L.vcto_svo_build.restype = C.c_int
         L.vcto_svo_build.argtypes = [P, C.c_int64, C.c_int, P, C.c_int64, P]
+        L.vcto_svo_trace.restype = C.c_uint64
+        L.vcto_svo_trace.argtypes = [C.c_int, P, P, P, P, P, P, C.c_int, C.c_int, P, P, P, C.c_int64, C.c_int64,
+                                     P, P]
         L.vcto_procedural_atlas.argtypes = [P, C.c_int64, C.c_uint32, C.c_double]
         _L = L
     return _L
@@ -288,3 +291,25 @@ def svo_build(frags: np.ndarray, level: int, capacity: int | None = None):
     if rc != 0:
         raise RuntimeError("oracle svo_build: node pool capacity exceeded")
     return pool[:int(nodes[0])], int(nodes[0])
+
+
+SPONZA_BB_MIN = (-15.367, -1.011, -9.462)   # voxelConeTracing_Octree.frag:321
+SPONZA_BB_MAX = (14.399, 11.43, 8.84)       # voxelConeTracing_Octree.frag:322
+
+
+def svo_trace(precision: int, desc_bytes: bytes, eye, pool: np.ndarray, samples: np.ndarray,
+              bb_min=SPONZA_BB_MIN, bb_max=SPONZA_BB_MAX, shadow: np.ndarray | None = None,
+              shadow_desc_bytes: bytes | None = None, light_bytes: bytes | None = None):
+    """voxelConeTracing_Octree.frag over a node pool ((n, 2) uint32); returns (diffuse, specular, steps)."""
+    n = samples.shape[0]
+    dout = np.zeros((n, 4), np.float64)
+    sout = np.zeros((n, 4), np.float64)
+    desc = np.frombuffer(desc_bytes, np.uint8).copy()
+    sd = np.frombuffer(shadow_desc_bytes or bytes(136), np.uint8).copy()
+    light = np.frombuffer(light_bytes or default_light_bytes(), np.uint8).copy()
+    sh, sw = (shadow.shape if shadow is not None else (0, 0))
+    steps = lib().vcto_svo_trace(precision, _p(desc), _p(np.asarray(eye, np.float32)),
+                                 _p(np.ascontiguousarray(pool, np.uint32)), _p(np.asarray(bb_min, np.float32)),
+                                 _p(np.asarray(bb_max, np.float32)), _p(shadow), sw, sh, _p(sd), _p(light),
+                                 _p(samples), 0, n, _p(dout), _p(sout))
+    return dout, sout, int(steps)

@@ -164,4 +164,40 @@ int vcto_svo_build(const uint32_t* frags, int64_t F, int level, uint32_t* pool, 
     return 0;
 }
 
+uint64_t vcto_svo_trace(int precision, const TraceDesc* desc, const float eye[3], const uint32_t* pool,
+                        const float bb_min[3], const float bb_max[3], const float* shadow, int sw, int sh,
+                        const ShadowDesc* sd, const LightDesc* light, const SurfaceSample* samples, int64_t begin,
+                        int64_t end, double* out_d, double* out_s) {
+    SvoTraceScene S;
+    S.pool = pool;
+    for (int a = 0; a < 3; ++a) {
+        S.bb_min[a] = bb_min[a];
+        S.bb_max[a] = bb_max[a];
+    }
+    uint64_t total = 0;
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : total)
+    for (int64_t i = begin; i < end; ++i) {
+        if (precision == 64) {
+            SvoTracer<double> tr{*desc, S};
+            double d[4], s[4];
+            if (trace_sample_svo<double>(tr, eye, shadow, sw, sh, *sd, *light, samples[i], d, s))
+                for (int c = 0; c < 4; ++c) {
+                    out_d[4 * i + c] = d[c];
+                    out_s[4 * i + c] = s[c];
+                }
+            total += tr.steps;
+        } else {
+            SvoTracer<float> tr{*desc, S};
+            float d[4], s[4];
+            if (trace_sample_svo<float>(tr, eye, shadow, sw, sh, *sd, *light, samples[i], d, s))
+                for (int c = 0; c < 4; ++c) {
+                    out_d[4 * i + c] = d[c];
+                    out_s[4 * i + c] = s[c];
+                }
+            total += tr.steps;
+        }
+    }
+    return total;
+}
+
 }  // extern "C"

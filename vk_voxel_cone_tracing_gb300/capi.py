@@ -33,6 +33,9 @@ MODE_GI_OUTPUT = 8
 INJECT_DETERMINISTIC = 0
 INJECT_ATOMIC = 1
 
+SVO_DETERMINISTIC = 0
+SVO_ATOMIC = 1
+
 TEX_RGBA8 = 0
 TEX_RGBA16F = 1
 
@@ -151,6 +154,10 @@ _SIGS: dict[str, tuple] = {
     "vct_shadow_depth": (C.c_int, [P, P, P, C.c_int32, C.c_int32, P, P]),
     "vct_inject_radiance": (C.c_int, [P, P, C.c_int32, P, P, P, P, C.c_uint32, C.c_int32, P, P]),
     "vct_svo_fragments": (C.c_int, [P, C.c_int32, P, P, P, P, P, P, C.c_int64, C.POINTER(C.c_int64), P, P]),
+    "vct_svo_pool_capacity": (C.c_int64, [C.c_int64]),
+    "vct_svo_build": (C.c_int, [P, C.c_int64, C.c_int32, P, C.c_int64, C.c_int32, C.POINTER(C.c_int64), P, P]),
+    "vct_svo_canonicalize": (C.c_int, [P, C.c_int64, C.c_int32, P, P, P]),
+    "vct_svo_cone_trace": (C.c_int, [P, P, P, C.c_int64, P, P, P, P, P, P, C.c_int64, P, P, P, P]),
 }
 
 

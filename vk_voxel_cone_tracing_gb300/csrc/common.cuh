@@ -8,7 +8,16 @@
 
 #include "../../include/vct_capi.h"
 
+// Device scratch arena of the raster / SVO passes (vct_workspace).
+struct vct_workspace_s {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+};
+
 namespace vct {
+
+// Grow `ws` to at least `bytes` (synchronises the device before freeing).
+int workspace_reserve(vct_workspace_s* ws, size_t bytes);
 
 // ---------------------------------------------------------------- errors
 void set_error(const std::string& msg);

@@ -26,11 +26,6 @@
 
 #include "trace_common.cuh"
 
-struct vct_workspace_s {
-    void* ptr = nullptr;
-    size_t bytes = 0;
-};
-
 namespace vct {
 
 // ------------------------------------------------------------------ math
@@ -631,7 +626,7 @@ static int grid_of(int64_t n, int block, int cap = 152 * 32) {
     return (int)(g < 1 ? 1 : (g > cap ? cap : g));
 }
 
-static int ws_reserve(vct_workspace_s* ws, size_t bytes) {
+int workspace_reserve(vct_workspace_s* ws, size_t bytes) {
     if (ws->bytes >= bytes) return VCT_OK;
     if (ws->ptr) {
         VCT_CUDA_TRY(cudaDeviceSynchronize());
@@ -665,7 +660,7 @@ static int plan_tiles(RasterArgs& A, vct_workspace_s* ws, size_t& off, uint32_t*
     size_t scan_bytes = 0;
     VCT_CUDA_TRY(cub::DeviceScan::InclusiveSum(nullptr, scan_bytes, (uint32_t*)nullptr, (uint32_t*)nullptr, (int)n));
     const size_t need = a256(4 * n) * 2 + a256(scan_bytes) + 256;
-    int rc = ws_reserve(ws, need);
+    int rc = workspace_reserve(ws, need);
     if (rc != VCT_OK) return rc;
     char* base = (char*)ws->ptr;
     uint32_t* counts = (uint32_t*)base;
@@ -877,7 +872,7 @@ extern "C" int vct_inject_radiance(const vct_scene* scene, const vct_clipmap_reg
     size_t need = head + a256(4 * (size_t)total) * 2 + a256(scan_bytes) + 256;
     // keep tile_end valid across a possible growth: grow first, then recount
     if (ws->bytes < need) {
-        rc = ws_reserve(ws, need);
+        rc = workspace_reserve(ws, need);
         if (rc != VCT_OK) return rc;
         rc = plan_tiles(A, ws, off, &tile_end, &total, st);
         if (rc != VCT_OK) return rc;
@@ -904,7 +899,7 @@ extern "C" int vct_inject_radiance(const vct_scene* scene, const vct_clipmap_reg
     need = rec_off + a256(sizeof(InjRecord) * nrec) + 4 * a256(4 * (size_t)nrec) + a256(sort_bytes) + 256;
     if (ws->bytes < need) {
         // grow and redo the counting passes (their buffers move with the arena)
-        rc = ws_reserve(ws, need);
+        rc = workspace_reserve(ws, need);
         if (rc != VCT_OK) return rc;
         return vct_inject_radiance(scene, regions, R, shadow, light, light_shadow, atlas, level_mask, mode, ws, stream);
     }
@@ -970,7 +965,7 @@ extern "C" int vct_svo_fragments(const vct_scene* scene, int32_t octree_level, c
     VCT_CUDA_TRY(cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, (uint32_t*)nullptr, (uint32_t*)nullptr, (int)total));
     const size_t need = off + a256(4 * (size_t)total) * 2 + a256(scan_bytes) + 256;
     if (ws->bytes < need) {
-        rc = ws_reserve(ws, need);
+        rc = workspace_reserve(ws, need);
         if (rc != VCT_OK) return rc;
         return vct_svo_fragments(scene, octree_level, bb_min, bb_max, shadow, light, light_shadow, frags, capacity,
                                  count, ws, stream);

@@ -119,3 +119,48 @@ def svo_fragments(dscene: DeviceScene, level: int, depth: torch.Tensor | None, l
               capi.ref(sm), capi.ref(light), capi.ref(sd), _ptr(frags), count.value, C.byref(count), ws.handle,
               _stream())
     return frags[:count.value]
+
+
+def svo_pool_capacity(fragment_count: int) -> int:
+    return int(capi.lib().vct_svo_pool_capacity(fragment_count))
+
+
+def svo_build(frags: torch.Tensor, level: int, ws: Workspace, mode: int = capi.SVO_DETERMINISTIC,
+              capacity: int | None = None):
+    """OctreeBuilder::cmdBuild over an (F, 2) fragment tensor; returns (pool[(n, 2) int32], n)."""
+    F = frags.shape[0]
+    cap = svo_pool_capacity(F) if capacity is None else capacity
+    pool = torch.empty((cap, 2), dtype=torch.int32, device=frags.device)
+    n = C.c_int64(0)
+    capi.call("vct_svo_build", _ptr(frags) if F else None, F, level, _ptr(pool), cap, mode, C.byref(n), ws.handle,
+              _stream())
+    return pool, int(n.value)
+
+
+def svo_canonicalize(pool: torch.Tensor, node_count: int, level: int, ws: Workspace) -> torch.Tensor:
+    out = torch.zeros((node_count, 2), dtype=torch.int32, device=pool.device)
+    capi.call("vct_svo_canonicalize", _ptr(pool), node_count, level, _ptr(out), ws.handle, _stream())
+    return out
+
+
+SPONZA_BB_MIN = (-15.367, -1.011, -9.462)   # voxelConeTracing_Octree.frag:321
+SPONZA_BB_MAX = (14.399, 11.43, 8.84)       # voxelConeTracing_Octree.frag:322
+
+
+def svo_cone_trace(desc: capi.ConeTracingDesc, eye, pool: torch.Tensor, node_count: int, samples: torch.Tensor,
+                   bb_min=SPONZA_BB_MIN, bb_max=SPONZA_BB_MAX, light: capi.DirectionalLightDesc | None = None,
+                   shadow: torch.Tensor | None = None, shadow_desc: capi.DirectionalLightShadowDesc | None = None,
+                   steps: torch.Tensor | None = None):
+    from .clipmap import cam_matrix
+    n = samples.shape[0]
+    dout = torch.zeros((n, 4), dtype=torch.float32, device=samples.device)
+    sout = torch.zeros((n, 4), dtype=torch.float32, device=samples.device)
+    light = light or light_desc()
+    sd = shadow_desc or capi.DirectionalLightShadowDesc()
+    sm = _shadow_map(shadow)
+    bmin = (C.c_float * 3)(*bb_min)
+    bmax = (C.c_float * 3)(*bb_max)
+    capi.call("vct_svo_cone_trace", capi.ref(desc), capi.ref(cam_matrix(eye)), _ptr(pool), node_count,
+              C.cast(bmin, C.c_void_p), C.cast(bmax, C.c_void_p), capi.ref(sm), capi.ref(light), capi.ref(sd),
+              _ptr(samples), n, _ptr(dout), _ptr(sout), _ptr(steps), _stream())
+    return dout, sout
