@@ -1,17 +1,26 @@
 #!/usr/bin/env python3
-"""Headline benchmark: cone samples/s of the clipmap cone tracer at R = 256.
+"""Headline benchmark of the voxel cone tracing core on one GPU.
 
-One step = one VoxelConeTracingPass over 1920x1080 G-buffer samples (16
-diffuse cones + one specular cone per sample, VXAO) against a 6-level x 6-face
-RGBA8 radiance clipmap of resolution 256 (a 2.47 GB atlas, larger than L2)
-whose mips were produced by the radiance downsample pass.  A "cone sample" is
-one iteration of traceCone's marching loop (voxelConeTracing.frag:361-389).
+Workload (configuration 2 of the reference's benchmark set, at the headline
+clipmap resolution 256): a seeded procedural hall of 1,000,000 fp32 triangles
+(instanced columns, arches, clutter; one RGBA8 albedo per triangle), camera at
+(0, 5, 0), 6 clip levels x 6 faces of 256^3 (RGBA8 opacity and radiance
+atlases, 2.47 GB each -- larger than L2), a directional light (0.3, -1, 0.2)
+with a 2048^2 shadow map, and 1920x1080 area-uniform G-buffer samples with
+face normals, roughness U(0.1, 0.9) and metallic U(0, 1): 16 diffuse cones,
+one specular cone and VXAO per sample.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--form exact|tex|fp16]
+Metric: cone samples/s of the cone-tracing pass (one cone sample = one
+iteration of traceCone's marching loop, voxelConeTracing.frag:361-389).  The
+line also reports the frame time of voxelise + shadow + inject + mips and of
+the SVO build (fragments + subdivide + leaf + mips) at 256^3.
 
-Prints one JSON line (rank 0).  ``--impl reference`` times the CPU
-restatement of the shader (the reference itself is Vulkan/GLSL and cannot run
-here) on a bounded sample of the same workload with every host thread.
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--form tex|fp16|exact]
+
+``--impl reference`` runs the CPU restatement of the reference's shaders (the
+reference itself is GLSL under Vulkan, which this machine cannot run) on the
+same workload: it builds the same clipmap on the host cores and times the
+trace over a bounded prefix of the samples.
 """
 from __future__ import annotations
 
@@ -32,9 +41,12 @@ sys.path.insert(0, str(ROOT))
 
 R_DEFAULT = 256
 N_SAMPLES = 1920 * 1080
-SEED_ATLAS = 3
-FILL = 0.05
-EYE = (0.0, 1.0, -6.0)
+SVO_LEVEL = 8
+CAMERA = (0.0, 5.0, 0.0)
+EYE = (0.0, 5.0, -12.0)
+LIGHT_DIR = (0.3, -1.0, 0.2)
+SHADOW_RES = 2048
+SCENE_SEED, SAMPLE_SEED = 2, 12
 BYTES_PER_CONE_SAMPLE = {"exact": 192, "tex": 192, "fp16": 384}
 METRIC = "cone samples/s (clipmap cone trace @256^3, 16 diffuse + specular cones)"
 
@@ -51,6 +63,12 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def light_origin():
+    d = np.asarray(LIGHT_DIR, np.float64)
+    d /= np.linalg.norm(d)
+    return tuple((np.asarray(CAMERA) - 15.0 * d).astype(np.float32).tolist())
+
+
 class Clocks:
     """Samples nvidia-smi SM clocks and throttle reasons during the timed region."""
 
@@ -65,10 +83,10 @@ class Clocks:
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.thread = threading.Thread(target=self._read, daemon=True)
-            self.thread.start()
+            threading.Thread(target=self._read, daemon=True).start()
+            time.sleep(0.3)
         except OSError:
             self.proc = None
         return self
@@ -90,8 +108,9 @@ class Clocks:
         rows = [r for r in self.rows if len(r) >= 9]
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        num = lambda s: s.replace(".", "", 1).isdigit()
+        sm = [float(r[1]) for r in rows if num(r[1])]
+        mx = [float(r[2]) for r in rows if num(r[2])]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
@@ -99,53 +118,65 @@ class Clocks:
 
 
 def dist_setup():
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return world, rank, local
+    return (int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")),
+            int(os.environ.get("LOCAL_RANK", "0")))
 
 
-def make_samples(n: int, seed: int):
-    from vk_voxel_cone_tracing_gb300.scene import random_samples
-    return random_samples(n, (0.0, 0.0, 0.0), 8.0, seed=seed, specular_fraction=0.5)
+def make_inputs(n_samples: int, sample_seed: int):
+    from vk_voxel_cone_tracing_gb300.scene import hall_scene, surface_samples
+    scene = hall_scene(seed=SCENE_SEED)
+    samples = surface_samples(scene, n_samples, seed=sample_seed)
+    return scene, samples
 
 
-def trace_desc_for(R: int):
-    from oracle import oracle
+def trace_desc_for(regions_np: np.ndarray, R: int):
     from vk_voxel_cone_tracing_gb300.clipmap import trace_desc
     from vk_voxel_cone_tracing_gb300.scene import default_trace_desc
-    regions = oracle.clip_regions((0.0, 0.0, 0.0), R)
-    return regions, trace_desc(**default_trace_desc(regions, R))
+    return trace_desc(**default_trace_desc(regions_np, R))
 
 
-def cpu_trace_rate(R: int, samples, target_s: float = 12.0, threads: int | None = None):
+def cpu_trace_rate(R, desc, radiance, shadow, sd_bytes, samples, target_s):
     """Cone samples/s of the FP32 CPU restatement over a bounded prefix of `samples`."""
     from oracle import oracle
-    if threads:
-        oracle.set_threads(threads)
-    regions, desc = trace_desc_for(R)
-    atlas = oracle.procedural_atlas(R, SEED_ATLAS, FILL)
-    for level in range(1, 6):
-        oracle.downsample(atlas, R, regions[level - 1, 0:3], level, 1)
-    n_probe = min(2048, samples.shape[0])
+    n_probe = min(1024, samples.shape[0])
     t0 = time.perf_counter()
-    _, _, st, _ = oracle.cone_trace(32, bytes(desc), EYE, atlas, R, samples, end=n_probe)
+    oracle.cone_trace(32, bytes(desc), EYE, radiance, R, samples, shadow=shadow, shadow_desc_bytes=sd_bytes,
+                      end=n_probe)
     dt = time.perf_counter() - t0
     n = int(min(samples.shape[0], max(n_probe, n_probe * target_s / max(dt, 1e-3))))
     t0 = time.perf_counter()
-    _, _, steps, _ = oracle.cone_trace(32, bytes(desc), EYE, atlas, R, samples, end=n)
+    _, _, steps, _ = oracle.cone_trace(32, bytes(desc), EYE, radiance, R, samples, shadow=shadow,
+                                       shadow_desc_bytes=sd_bytes, end=n)
     dt = time.perf_counter() - t0
     return steps / dt, n, steps, dt, oracle.num_threads()
 
 
 def run_reference(args, world, rank):
+    """The reference's path on the host cores: the C++ restatement of its shaders."""
     if rank != 0:
         return
-    samples = make_samples(N_SAMPLES, seed=100)
-    rates = []
-    info = None
+    from oracle import oracle
+    R = args.R
+    scene, samples = make_inputs(N_SAMPLES, SAMPLE_SEED)
+    t0 = time.perf_counter()
+    regions = oracle.clip_regions(CAMERA, R)
+    opacity = oracle.voxelize_opacity(scene, R, regions)
+    for level in range(1, 6):
+        oracle.downsample(opacity, R, regions[level - 1, 0:3], level, 0)
+    oracle.wrap_border(opacity, R)
+    sd = oracle.light_shadow_desc(light_origin(), LIGHT_DIR)
+    shadow = oracle.shadow_depth(scene, sd, SHADOW_RES, SHADOW_RES)
+    radiance = oracle.inject_radiance(scene, R, regions, shadow, sd)
+    for level in range(6):
+        oracle.copy_alpha(radiance, opacity, R, level)
+    for level in range(1, 6):
+        oracle.downsample(radiance, R, regions[level - 1, 0:3], level, 1)
+    frame_s = time.perf_counter() - t0
+    desc = trace_desc_for(regions, R)
+    rates, info = [], None
     for i in range(args.warmup + args.steps):
-        rate, n, steps, dt, cores = cpu_trace_rate(args.R, samples, target_s=args.cpu_seconds / max(1, args.steps))
+        rate, n, steps, dt, cores = cpu_trace_rate(R, desc, radiance, shadow, sd, samples,
+                                                   args.cpu_seconds / max(1, args.steps))
         if i >= args.warmup:
             rates.append(rate)
             info = (n, steps, dt, cores)
@@ -155,23 +186,36 @@ def run_reference(args, world, rank):
         "impl": "reference", "metric": METRIC, "value": v, "unit": "cone samples/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"clipmap cone trace R={args.R}, 1920x1080 G-buffer samples (bounded prefix)",
-                   "samples_traced": n, "cone_samples": steps},
+        "config": {"workload": f"hall scene 1M triangles, clipmap R={R}, 1920x1080 G-buffer samples "
+                               f"(trace timed over a bounded prefix)", "samples_traced": n, "cone_samples": steps,
+                   "frame_ms_cpu": frame_s * 1e3},
         "cpu_baseline": {"value": v, "unit": "cone samples/s", "cores": cores, "kind": "port",
-                         "sample": f"first {n} of {N_SAMPLES} samples, FP32 C++ restatement of voxelConeTracing.frag"},
+                         "sample": f"first {n} of {N_SAMPLES} samples, FP32 C++ restatement of "
+                                   "voxelConeTracing.frag; frame built by the restated passes"},
         "e2e": {"value": v, "unit": "cone samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "the reference runs GLSL through Vulkan; no graphics stack exists on this machine, so its CPU "
-                "restatement is timed",
+        "note": "the reference's passes are GLSL under Vulkan, which this machine cannot run; the CPU "
+                "restatement of its shaders is timed on all host threads",
     }
     print(json.dumps(line), flush=True)
+
+
+def events_ms(stream, fn, reps):
+    import torch
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(reps + 1)]
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    for i in range(reps):
+        fn()
+        ev[i + 1].record(stream)
+    torch.cuda.synchronize()
+    return [ev[i].elapsed_time(ev[i + 1]) for i in range(reps)], ev[0].elapsed_time(ev[-1])
 
 
 def run_ours(args, world, rank, local):
     import torch
     import torch.distributed as dist
 
-    from vk_voxel_cone_tracing_gb300 import build, clipmap
-    from vk_voxel_cone_tracing_gb300.scene import procedural_atlas_torch
+    from vk_voxel_cone_tracing_gb300 import build, capi, clipmap, passes
 
     build.build()
     torch.cuda.set_device(local)
@@ -179,91 +223,99 @@ def run_ours(args, world, rank, local):
     if world > 1:
         dist.init_process_group("nccl", device_id=dev)
     R = args.R
-    regions, desc = trace_desc_for(R)
-    creg = clipmap.clip_regions((0.0, 0.0, 0.0), R)
+    log(f"[bench] generating the scene and {args.samples} samples")
+    scene, samples_np = make_inputs(args.samples, SAMPLE_SEED + rank)  # weak scaling: one frame per rank
+    ds = passes.DeviceScene(scene, dev)
+    ws = passes.Workspace()
+    opacity = clipmap.new_atlas(R, dev)
+    radiance = clipmap.new_atlas(R, dev)
+    shadow = torch.empty((SHADOW_RES, SHADOW_RES), dtype=torch.float32, device=dev)
+    light = passes.light_desc(LIGHT_DIR)
+    lsd = passes.light_shadow_desc(light_origin(), LIGHT_DIR)
+    stream = torch.cuda.current_stream()
 
-    log(f"[bench] building R={R} atlas on {dev}")
-    atlas = procedural_atlas_torch(R, SEED_ATLAS, FILL, device=dev)
-    clipmap.cmd_downsample_all(atlas, R, creg, 1)
+    def frame():
+        return passes.clipmap_frame(ds, CAMERA, R, opacity, radiance, shadow, light, lsd, ws)
+
+    regs = frame()
     torch.cuda.synchronize()
+    regions_np = clipmap.regions_to_numpy(regs)
+    desc = trace_desc_for(regions_np, R)
 
-    samples_np = make_samples(args.samples, seed=100 + rank)  # weak scaling: one frame per rank
     samples = clipmap.samples_to_device(samples_np, dev)
     n = samples.shape[0]
     dout = torch.empty((n, 4), dtype=torch.float32, device=dev)
     sout = torch.empty((n, 4), dtype=torch.float32, device=dev)
     steps_ctr = torch.zeros(1, dtype=torch.int64, device=dev)
-
-    tex = None
-    tex_src = atlas
+    tex, tex_src, scratch = None, radiance, None
     if args.form in ("tex", "fp16"):
-        from vk_voxel_cone_tracing_gb300 import capi
         if args.form == "fp16":
-            tex_src = clipmap.to_rgba16f(atlas, R)
-            clipmap.cmd_downsample_rgba16f_all(tex_src, R, creg, 1)
+            tex_src = clipmap.to_rgba16f(radiance, R)
+            clipmap.cmd_downsample_rgba16f_all(tex_src, R, regs, 1)
         tex = clipmap.RadianceTexture(R, capi.TEX_RGBA8 if args.form == "tex" else capi.TEX_RGBA16F)
         scratch = clipmap.fast_scratch(n, dev)
 
     def trace(inp, counter=None):
         if tex is None:
-            clipmap.cone_trace(desc, EYE, atlas, R, inp, diffuse=dout, specular=sout, steps=counter)
+            clipmap.cone_trace(desc, EYE, radiance, R, inp, light=light, shadow=shadow, shadow_desc=lsd,
+                               diffuse=dout, specular=sout, steps=counter)
         else:
             tex.update(tex_src)  # the texture copy of the clipmap is refreshed every step
-            clipmap.cone_trace_fast(desc, EYE, tex, inp, diffuse=dout, specular=sout, steps=counter,
-                                    scratch=scratch)
+            clipmap.cone_trace_fast(desc, EYE, tex, inp, light=light, shadow=shadow, shadow_desc=lsd, diffuse=dout,
+                                    specular=sout, steps=counter, scratch=scratch)
 
-    def step(counter=None):
-        trace(samples, counter)
-
-    # counting run: the number of cone samples one step executes
-    step(steps_ctr)
+    trace(samples, steps_ctr)
     torch.cuda.synchronize()
     cone_samples = int(steps_ctr.item())
     for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
+        trace(samples)
     if world > 1:
         dist.barrier()
-    stream = torch.cuda.current_stream()
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
     with Clocks(local) as clocks:
-        torch.cuda.synchronize()
-        ev[0].record(stream)
-        for i in range(args.steps):
-            step()
-            ev[i + 1].record(stream)
-        torch.cuda.synchronize()
-    per = [ev[i].elapsed_time(ev[i + 1]) for i in range(args.steps)]
-    total_ms = ev[0].elapsed_time(ev[-1])
+        per, total_ms = events_ms(stream, lambda: trace(samples), args.steps)
     t = torch.tensor([total_ms], device=dev)
     if world > 1:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    total_ms = float(t.item())
-    ms = total_ms / args.steps
+    ms = float(t.item()) / args.steps
     value = cone_samples * world / (ms * 1e-3)
 
-    # end to end through the C ABI: pinned host samples -> device, trace, outputs -> pinned host
+    # voxelise + shadow + inject + mips of one frame, and the SVO build at 256^3
+    for _ in range(2):
+        frame()
+    frame_per, _ = events_ms(stream, frame, max(3, args.steps))
+    frags = passes.svo_fragments(ds, SVO_LEVEL, shadow, light, lsd, ws)
+    pool_cap = passes.svo_pool_capacity(frags.shape[0])
+    pool = torch.empty((pool_cap, 2), dtype=torch.int32, device=dev)
+    import ctypes as C
+    nodes = C.c_int64(0)
+
+    def svo():
+        f = passes.svo_fragments(ds, SVO_LEVEL, shadow, light, lsd, ws)
+        capi.call("vct_svo_build", f.data_ptr(), f.shape[0], SVO_LEVEL, pool.data_ptr(), pool_cap,
+                  capi.SVO_DETERMINISTIC, C.byref(nodes), ws.handle, C.c_void_p(stream.cuda_stream))
+
+    svo()
+    svo_per, _ = events_ms(stream, svo, max(3, args.steps))
+    frame_ms = statistics.median(frame_per)
+    svo_ms = statistics.median(svo_per)
+
+    # end to end: host G-buffer -> device, frame, trace, outputs -> host
     h_samples = samples.cpu().pin_memory()
-    h_d = torch.empty_like(dout, device="cpu").pin_memory()
-    h_s = torch.empty_like(sout, device="cpu").pin_memory()
+    h_d = torch.empty(dout.shape, dtype=torch.float32).pin_memory()
+    h_s = torch.empty(sout.shape, dtype=torch.float32).pin_memory()
     d_in = torch.empty_like(samples)
+
+    def e2e_step():
+        d_in.copy_(h_samples, non_blocking=True)
+        frame()
+        trace(d_in)
+        h_d.copy_(dout, non_blocking=True)
+        h_s.copy_(sout, non_blocking=True)
+
     for _ in range(max(1, args.warmup)):
-        d_in.copy_(h_samples, non_blocking=True)
-        trace(d_in)
-        h_d.copy_(dout, non_blocking=True)
-        h_s.copy_(sout, non_blocking=True)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        d_in.copy_(h_samples, non_blocking=True)
-        trace(d_in)
-        h_d.copy_(dout, non_blocking=True)
-        h_s.copy_(sout, non_blocking=True)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1) / args.steps
-    te = torch.tensor([e2e_ms], device=dev)
+        e2e_step()
+    _, e2e_total = events_ms(stream, e2e_step, args.steps)
+    te = torch.tensor([e2e_total / args.steps], device=dev)
     if world > 1:
         dist.all_reduce(te, op=dist.ReduceOp.MAX)
     e2e_ms = float(te.item())
@@ -271,41 +323,53 @@ def run_ours(args, world, rank, local):
     if rank == 0:
         peak, peak_kind = measured_peaks()
         bpcs = BYTES_PER_CONE_SAMPLE[args.form]
-        avg_launch_s = statistics.mean(per) * 1e-3
-        achieved = cone_samples * bpcs / avg_launch_s / 1e9
+        achieved = cone_samples * bpcs / (statistics.mean(per) * 1e-3) / 1e9
         traffic = None
         prof = ROOT / "profiles" / f"cone_trace_{args.form}_r{R}.txt"
         if prof.exists():
             for line in prof.read_text().splitlines():
                 if line.startswith("dram_bytes_per_launch_full:"):
                     traffic = float(line.split(":")[1])
-        log(f"[bench] cone samples/step={cone_samples} ms/step={ms:.3f} e2e ms={e2e_ms:.3f}")
+        log(f"[bench] cone samples/step={cone_samples} trace ms={ms:.3f} frame ms={frame_ms:.3f} "
+            f"svo ms={svo_ms:.3f} e2e ms={e2e_ms:.3f}")
         cpu = None
         if not args.no_cpu:
-            rate, ncpu, st, dt, cores = cpu_trace_rate(R, samples_np, target_s=args.cpu_seconds)
+            rad_np = radiance.cpu().numpy().view(np.uint32)
+            sh_np = shadow.cpu().numpy()
+            rate, ncpu, st, dt, cores = cpu_trace_rate(R, desc, rad_np, sh_np, bytes(lsd), samples_np, args.cpu_seconds)
             cpu = {"value": rate, "unit": "cone samples/s", "cores": cores, "kind": "port",
-                   "sample": f"first {ncpu} of {n} samples ({st} cone samples, {dt:.1f} s), FP32 C++ restatement"}
+                   "sample": f"first {ncpu} of {n} samples ({st} cone samples, {dt:.1f} s) traced by the FP32 C++ "
+                             "restatement on the same clipmap"}
+        # kernels launched per trace step: texture copy (memcpy), Morton keys, 2 cub radix sorts
+        # (histogram + scan + 4 onesweep passes for 30 bits, 2 for 9 bits), diffuse, specular
+        launches = 1 if tex is None else 12
         line = {
             "metric": METRIC, "value": value, "unit": "cone samples/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"clipmap cone trace R={R}: 6 levels x 6 faces RGBA8 radiance atlas "
-                                   f"({atlas.numel() * 4 / 1e9:.2f} GB, hash-random {FILL:.0%} occupancy + "
-                                   f"radiance mips), 1920x1080 G-buffer samples, 16 diffuse + specular cones",
+            "config": {"workload": f"hall scene ({scene.triangle_count} fp32 triangles), clipmap R={R} "
+                                   "(6 levels x 6 faces, RGBA8 opacity + radiance atlases of 2.47 GB), "
+                                   "1920x1080 G-buffer samples, 16 diffuse + 1 specular cone + VXAO",
                        "form": args.form, "R": R, "samples_per_step": n, "cone_samples_per_step": cone_samples,
-                       "l2": "inputs larger than L2 (2.47 GB atlas)"},
+                       "l2": "inputs larger than L2 (2.47 GB clipmap)",
+                       "voxelize_inject_mip_ms": frame_ms, "svo_ms": svo_ms, "svo_level": SVO_LEVEL,
+                       "svo_fragments": int(frags.shape[0]), "svo_nodes": int(nodes.value),
+                       "voxelize_svo_mip_ms": frame_ms + svo_ms},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "note": f"{bpcs} B algorithmic texel bytes per cone sample over the {peak_kind} HBM copy "
-                                 "peak; the taps are served mostly by L1/L2, so frac > 1 is possible"},
+                         "note": f"{bpcs} B of algorithmic texel reads per cone sample over the {peak_kind} HBM "
+                                 "copy peak; the taps are served mostly from L1/TEX and L2"},
             "cpu_baseline": cpu,
             "e2e": {"value": cone_samples * world / (e2e_ms * 1e-3), "unit": "cone samples/s",
                     "h2d_bytes_per_step": int(samples.numel() * 4),
-                    "d2h_bytes_per_step": int((dout.numel() + sout.numel()) * 4)},
-            "gpu_launches": args.steps * (1 if tex is None else 3),
+                    "d2h_bytes_per_step": int((dout.numel() + sout.numel()) * 4),
+                    "step": "G-buffer upload + voxelise/shadow/inject/mips + trace + output readback"},
+            "gpu_launches": args.steps * launches,
             "clocks": clocks.summary(),
         }
         print(json.dumps(line), flush=True)
+    if tex is not None:
+        tex.close()
     if world > 1:
         dist.destroy_process_group()
 
@@ -313,13 +377,13 @@ def run_ours(args, world, rank, local):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--form", default="exact", choices=["exact", "tex", "fp16"])
+    ap.add_argument("--form", default="tex", choices=["exact", "tex", "fp16"])
     ap.add_argument("--samples", type=int, default=N_SAMPLES)
     ap.add_argument("--R", type=int, default=R_DEFAULT)
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     world, rank, local = dist_setup()

@@ -426,6 +426,32 @@ int vct_svo_cone_trace(const vct_cone_tracing_desc* desc, const vct_cam_matrix* 
                        const vct_surface_sample* samples, int64_t sample_count, float* diffuse_out,
                        float* specular_out, unsigned long long* cone_steps, void* stream);
 
+/* ------------------------------------------------------------ one frame */
+
+/* Per-frame inputs of the clipmap method (Application::run and the passes it
+ * drives): camera position (clip regions), clipmap resolution, frame index
+ * (radiance levels are refreshed every 2^level frames), injection mode,
+ * directional light with its shadow projection, shadow-map size (0 = no
+ * shadow pass: visibility 1). */
+typedef struct vct_frame_desc {
+    float camera_pos[3];
+    int32_t clipmap_resolution;
+    int32_t frame_index;
+    int32_t inject_mode;
+    int32_t shadow_width;
+    int32_t shadow_height;
+    vct_directional_light_desc light;
+    vct_directional_light_shadow_desc light_shadow;
+} vct_frame_desc;
+
+/* Application::run's pre-pass sequence (VFS/Application.cpp:142-201):
+ * VoxelizationPass (clear, voxelise all levels, opacity mips, border wrap),
+ * RSMPass depth, RadianceInjectionPass (clear due levels, inject, copy alpha,
+ * radiance mips).  Writes the 6 clip regions to regions_out (may be NULL). */
+int vct_clipmap_frame(const vct_scene* scene, const vct_frame_desc* frame, uint32_t* opacity_atlas,
+                      uint32_t* radiance_atlas, float* shadow_depth, vct_clipmap_region regions_out_host[6],
+                      vct_workspace ws, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

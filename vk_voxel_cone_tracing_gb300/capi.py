@@ -113,6 +113,12 @@ class Scene(C.Structure):
                 ("instance_count", C.c_int32)]
 
 
+class FrameDesc(C.Structure):
+    _fields_ = [("camera_pos", f3), ("clipmap_resolution", C.c_int32), ("frame_index", C.c_int32),
+                ("inject_mode", C.c_int32), ("shadow_width", C.c_int32), ("shadow_height", C.c_int32),
+                ("light", DirectionalLightDesc), ("light_shadow", DirectionalLightShadowDesc)]
+
+
 class ShadowMap(C.Structure):
     _fields_ = [("depth", C.c_void_p), ("width", C.c_int32), ("height", C.c_int32)]
 
@@ -158,6 +164,7 @@ _SIGS: dict[str, tuple] = {
     "vct_svo_build": (C.c_int, [P, C.c_int64, C.c_int32, P, C.c_int64, C.c_int32, C.POINTER(C.c_int64), P, P]),
     "vct_svo_canonicalize": (C.c_int, [P, C.c_int64, C.c_int32, P, P, P]),
     "vct_svo_cone_trace": (C.c_int, [P, P, P, C.c_int64, P, P, P, P, P, P, C.c_int64, P, P, P, P]),
+    "vct_clipmap_frame": (C.c_int, [P, P, P, P, P, P, P, P]),
 }
 
 

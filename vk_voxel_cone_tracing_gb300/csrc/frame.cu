@@ -1,0 +1,72 @@
+// frame.cu -- one frame of the 3D-clipmap method in the reference's pass order
+// (Application::run, VFS/Application.cpp:142-201, with the passes built in
+// Application::buildClipmapMethodPasses, :406-522):
+//
+//   VoxelizationPass       clear opacity, voxelise every level, opacity
+//                          mips 1..5, opacity border wrap
+//   RSMPass                directional-light depth map
+//   RadianceInjectionPass  for each level due this frame (frame % 2^level == 0):
+//                          clear, inject; then copy-alpha and radiance mips
+//
+// Host-side orchestration only: every step is one of the C-ABI passes, run
+// on the caller's stream.
+#include "common.cuh"
+
+extern "C" int vct_clipmap_frame(const vct_scene* scene, const vct_frame_desc* f, uint32_t* opacity,
+                                 uint32_t* radiance, float* shadow_depth, vct_clipmap_region regions_out[6],
+                                 vct_workspace_s* ws, void* stream) {
+    VCT_CHECK_ARG(scene && f && opacity && radiance && ws, "vct_clipmap_frame: null argument");
+    VCT_CHECK_ARG(!f->shadow_width || shadow_depth, "vct_clipmap_frame: shadow map size given without a buffer");
+    const int R = f->clipmap_resolution;
+    vct_clipmap_region regions[6];
+    int rc = vct_clip_regions(f->camera_pos, R, VCT_VOXEL_EXTENT_L0, regions);
+    if (rc != VCT_OK) return rc;
+    if (regions_out)
+        for (int l = 0; l < 6; ++l) regions_out[l] = regions[l];
+
+    // VoxelizationPass (full revoxelisation every frame, VoxelizationPass.cpp:79-125)
+    if ((rc = vct_clear_atlas(opacity, R, stream)) != VCT_OK) return rc;
+    if ((rc = vct_voxelize_opacity(scene, regions, R, opacity, 0x3Fu, ws, stream)) != VCT_OK) return rc;
+    if ((rc = vct_downsample_all(opacity, regions, R, VCT_DOWNSAMPLE_OPACITY, stream)) != VCT_OK) return rc;
+    vct_border_wrapping_desc bw = {(uint32_t)R, VCT_VOXEL_BORDER, VCT_FACE_COUNT, VCT_CLIP_LEVEL_COUNT};
+    if ((rc = vct_wrap_border(opacity, &bw, stream)) != VCT_OK) return rc;
+
+    // RSMPass: the depth map the injection's visibility samples
+    vct_shadow_map sm = {nullptr, 0, 0};
+    if (f->shadow_width > 0) {
+        if ((rc = vct_shadow_depth(scene, &f->light_shadow, shadow_depth, f->shadow_width, f->shadow_height, ws,
+                                   stream)) != VCT_OK)
+            return rc;
+        sm.depth = shadow_depth;
+        sm.width = f->shadow_width;
+        sm.height = f->shadow_height;
+    }
+
+    // RadianceInjectionPass (RadianceInjectionPass.cpp:64-159), level cadence 2^level frames
+    uint32_t due = 0;
+    for (int l = 0; l < 6; ++l)
+        if (f->frame_index % (1 << l) == 0) due |= 1u << l;
+    for (int l = 0; l < 6; ++l) {
+        if (!((due >> l) & 1u)) continue;
+        vct_image_cleaning_desc c = {{0, 0, 0}, l, {(uint32_t)R, (uint32_t)R, (uint32_t)R}, R, VCT_FACE_COUNT};
+        if ((rc = vct_clear_region(radiance, &c, stream)) != VCT_OK) return rc;
+    }
+    if ((rc = vct_inject_radiance(scene, regions, R, &sm, &f->light, &f->light_shadow, radiance, due, f->inject_mode,
+                                  ws, stream)) != VCT_OK)
+        return rc;
+    for (int l = 0; l < 6; ++l) {
+        if (!((due >> l) & 1u)) continue;
+        vct_copy_alpha_desc ca = {l, R, VCT_FACE_COUNT};
+        if ((rc = vct_copy_alpha(radiance, opacity, &ca, stream)) != VCT_OK) return rc;
+    }
+    for (int l = 1; l < 6; ++l) {
+        if (!((due >> l) & 1u)) continue;
+        vct_downsample_desc d;
+        for (int a = 0; a < 3; ++a) d.prev_region_min_corner[a] = regions[l - 1].min_corner[a];
+        d.clip_level = l;
+        d.clipmap_resolution = R;
+        d.downsample_region_size = VCT_DOWNSAMPLE_REGION_SIZE;
+        if ((rc = vct_downsample(radiance, &d, VCT_DOWNSAMPLE_RADIANCE, stream)) != VCT_OK) return rc;
+    }
+    return VCT_OK;
+}

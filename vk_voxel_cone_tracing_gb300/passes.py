@@ -164,3 +164,23 @@ def svo_cone_trace(desc: capi.ConeTracingDesc, eye, pool: torch.Tensor, node_cou
               C.cast(bmin, C.c_void_p), C.cast(bmax, C.c_void_p), capi.ref(sm), capi.ref(light), capi.ref(sd),
               _ptr(samples), n, _ptr(dout), _ptr(sout), _ptr(steps), _stream())
     return dout, sout
+
+
+def clipmap_frame(dscene: DeviceScene, camera_pos, R: int, opacity: torch.Tensor, radiance: torch.Tensor,
+                  shadow: torch.Tensor | None, light: capi.DirectionalLightDesc,
+                  light_shadow: capi.DirectionalLightShadowDesc, ws: Workspace, frame_index: int = 0,
+                  inject_mode: int = capi.INJECT_DETERMINISTIC):
+    """vct_clipmap_frame: voxelise, mips, border, shadow depth, inject, copy alpha, radiance mips."""
+    f = capi.FrameDesc()
+    f.camera_pos = capi.f3(*camera_pos)
+    f.clipmap_resolution = R
+    f.frame_index = frame_index
+    f.inject_mode = inject_mode
+    f.shadow_width = shadow.shape[1] if shadow is not None else 0
+    f.shadow_height = shadow.shape[0] if shadow is not None else 0
+    f.light = light
+    f.light_shadow = light_shadow
+    regs = (capi.ClipmapRegion * 6)()
+    capi.call("vct_clipmap_frame", capi.ref(dscene.desc), capi.ref(f), _ptr(opacity), _ptr(radiance),
+              _ptr(shadow), C.cast(regs, C.c_void_p), ws.handle, _stream())
+    return regs
