@@ -452,6 +452,26 @@ int vct_clipmap_frame(const vct_scene* scene, const vct_frame_desc* frame, uint3
                       uint32_t* radiance_atlas, float* shadow_depth, vct_clipmap_region regions_out_host[6],
                       vct_workspace ws, void* stream);
 
+/* ------------------------------------------ allocation-free fast trace */
+
+/* No counterpart in the reference.  vct_cone_trace_fast for callers that
+ * cannot allocate device memory (hosts that own all GPU memory through their
+ * own allocator, frame loops that must not call cudaMalloc): the same pass,
+ * with its scratch in a static device array of VCT_NOALLOC_SCRATCH_BYTES that
+ * the library holds on every GPU that loads it, for up to
+ * VCT_NOALLOC_MAX_SAMPLES samples (larger counts are rejected with
+ * VCT_E_BAD_ARG).  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress); make it before any stream capture.  Calls
+ * share the array: calls that overlap on the GPU race and must be serialised
+ * by the caller. */
+#define VCT_NOALLOC_MAX_SAMPLES 1048576
+#define VCT_NOALLOC_SCRATCH_BYTES (48u << 20)
+int vct_cone_trace_fast_noalloc(const vct_cone_tracing_desc* desc, const vct_cam_matrix* cam, vct_texture radiance,
+                                const vct_shadow_map* shadow, const vct_directional_light_desc* light,
+                                const vct_directional_light_shadow_desc* light_shadow,
+                                const vct_surface_sample* samples, int64_t sample_count, float* diffuse_out,
+                                float* specular_out, unsigned long long* cone_steps, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -36,6 +36,9 @@ INJECT_ATOMIC = 1
 SVO_DETERMINISTIC = 0
 SVO_ATOMIC = 1
 
+NOALLOC_MAX_SAMPLES = 1048576
+NOALLOC_SCRATCH_BYTES = 48 << 20
+
 TEX_RGBA8 = 0
 TEX_RGBA16F = 1
 
@@ -165,6 +168,7 @@ _SIGS: dict[str, tuple] = {
     "vct_svo_canonicalize": (C.c_int, [P, C.c_int64, C.c_int32, P, P, P]),
     "vct_svo_cone_trace": (C.c_int, [P, P, P, C.c_int64, P, P, P, P, P, P, C.c_int64, P, P, P, P]),
     "vct_clipmap_frame": (C.c_int, [P, P, P, P, P, P, P, P]),
+    "vct_cone_trace_fast_noalloc": (C.c_int, [P, P, P, P, P, P, P, C.c_int64, P, P, P, P]),
 }
 
 
