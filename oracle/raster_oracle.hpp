@@ -20,8 +20,8 @@
 //     the triangle for which the edge runs (dy > 0) or (dy == 0 and dx > 0)
 //     after orienting the triangle counter-clockwise (one owner per shared
 //     edge); zero-area triangles produce nothing; no culling;
-//   * depth clip 0 <= z <= 1; attributes interpolated with barycentrics
-//     e_i / area in FP64, rounded to FP32;
+//   * depth clip 0 <= z <= 1; barycentrics b_i = float(e_i) * (1 / float(area))
+//     and attributes (b0 a0 + b1 a1) + b2 a2, all FP32 without fused multiply-add;
 //   * the fragment shader runs at every covered sample (sample-rate shading);
 //   * traversal order (the order of atomic-average folds and fragment-list
 //     appends): triangles in index order, then clip levels, then 8x8-pixel
@@ -275,6 +275,7 @@ struct RasterSetup {
     float z[3];
     int order[3];  // original vertex index of each oriented vertex
     int64_t area;
+    float inv_area;
     int px0, py0, px1, py1;  // inclusive pixel bbox, clipped to the viewport
     bool owned[3];
     bool ok;
@@ -309,6 +310,7 @@ inline RasterSetup raster_setup(const V4<float> c[3], int W, int H) {
         r.order[k] = o[k];
     }
     r.area = area;
+    r.inv_area = 1.0f / (float)area;
     for (int i = 0; i < 3; ++i) {  // edge i runs from vertex i+1 to vertex i+2
         const int a = (i + 1) % 3, b = (i + 2) % 3;
         const int64_t dy = r.Y[b] - r.Y[a], dx = r.X[b] - r.X[a];
@@ -332,27 +334,35 @@ inline RasterSetup raster_setup(const V4<float> c[3], int W, int H) {
     return r;
 }
 
-// Coverage of sample S (in 1/256 pixel); on success writes barycentrics of the
-// ORIGINAL vertex order into b[3] (FP64) and the interpolated depth.
-inline bool raster_test(const RasterSetup& r, int64_t sx, int64_t sy, double b[3], float& z) {
-    int64_t e[3];
+// Coverage of sample S (in 1/256 pixel): the exact edge tests only.
+inline bool raster_cover(const RasterSetup& r, int64_t sx, int64_t sy, int64_t e[3]) {
     for (int i = 0; i < 3; ++i) {
         const int a = (i + 1) % 3, c = (i + 2) % 3;
         e[i] = (r.X[c] - r.X[a]) * (sy - r.Y[a]) - (r.Y[c] - r.Y[a]) * (sx - r.X[a]);
         if (e[i] < 0 || (e[i] == 0 && !r.owned[i])) return false;
     }
-    double bo[3];
-    for (int i = 0; i < 3; ++i) bo[i] = (double)e[i] / (double)r.area;
-    z = (float)((bo[0] * (double)r.z[0] + bo[1] * (double)r.z[1]) + bo[2] * (double)r.z[2]);
+    return true;
+}
+
+// Barycentrics of a covered sample in the ORIGINAL vertex order and its
+// depth; false if the depth clip rejects it.
+inline bool raster_interp(const RasterSetup& r, const int64_t e[3], float b[3], float& z) {
+    float bo[3];
+    for (int i = 0; i < 3; ++i) bo[i] = (float)e[i] * r.inv_area;
+    z = (bo[0] * r.z[0] + bo[1] * r.z[1]) + bo[2] * r.z[2];
     if (!(z >= 0.0f && z <= 1.0f)) return false;
     for (int i = 0; i < 3; ++i) b[r.order[i]] = bo[i];
     return true;
 }
 
-inline V3<float> interp3(const double b[3], const V3<float> v[3]) {
-    return V3<float>((float)((b[0] * (double)v[0].x + b[1] * (double)v[1].x) + b[2] * (double)v[2].x),
-                     (float)((b[0] * (double)v[0].y + b[1] * (double)v[1].y) + b[2] * (double)v[2].y),
-                     (float)((b[0] * (double)v[0].z + b[1] * (double)v[1].z) + b[2] * (double)v[2].z));
+inline bool raster_test(const RasterSetup& r, int64_t sx, int64_t sy, float b[3], float& z) {
+    int64_t e[3];
+    return raster_cover(r, sx, sy, e) && raster_interp(r, e, b, z);
+}
+
+inline V3<float> interp3(const float b[3], const V3<float> v[3]) {
+    return V3<float>((b[0] * v[0].x + b[1] * v[1].x) + b[2] * v[2].x, (b[0] * v[0].y + b[1] * v[1].y) + b[2] * v[2].y,
+                     (b[0] * v[0].z + b[1] * v[1].z) + b[2] * v[2].z);
 }
 
 // Visit every covered sample of a set-up triangle in the pinned order.
@@ -371,7 +381,7 @@ inline void raster_visit(const RasterSetup& r, int nsamples, F&& frag) {
                             sx = (int64_t)px * 256 + kSampleLoc8[s][0];
                             sy = (int64_t)py * 256 + kSampleLoc8[s][1];
                         }
-                        double b[3];
+                        float b[3];
                         float z;
                         if (raster_test(r, sx, sy, b, z)) frag(px, py, s, b, z);
                     }
@@ -420,7 +430,7 @@ inline void voxelize_opacity(const SceneView& s, int R, const Region regions[6],
             clip_vertices(w, vp, c);
             RasterSetup rs = raster_setup(c, R + 2, R + 2);
             if (!rs.ok) continue;
-            raster_visit(rs, 8, [&](int, int, int, const double* b, float) {
+            raster_visit(rs, 8, [&](int, int, int, const float* b, float) {
                 V3<float> wp = interp3(b, w.p);
                 if (wp.x < d.region_min[0] || wp.y < d.region_min[1] || wp.z < d.region_min[2] ||
                     wp.x > d.region_max[0] || wp.y > d.region_max[1] || wp.z > d.region_max[2])
@@ -447,7 +457,7 @@ inline void shadow_depth(const SceneView& s, const ShadowDesc& sd, float* depth,
         for (int k = 0; k < 3; ++k) c[k] = mat_vec4(pv, w.p[k].x, w.p[k].y, w.p[k].z, 1.0f);
         RasterSetup rs = raster_setup(c, W, H);
         if (!rs.ok) continue;
-        raster_visit(rs, 1, [&](int px, int py, int, const double*, float z) {
+        raster_visit(rs, 1, [&](int px, int py, int, const float*, float z) {
             float& d = depth[(int64_t)py * W + px];
             if (z < d) d = z;
         });
@@ -493,7 +503,7 @@ inline void inject_radiance(const SceneView& s, int R, const Region regions[6], 
             clip_vertices(w, vp, c);
             RasterSetup rs = raster_setup(c, rb, rb);
             if (!rs.ok) continue;
-            raster_visit(rs, 8, [&](int, int, int, const double* b, float) {
+            raster_visit(rs, 8, [&](int, int, int, const float* b, float) {
                 V3<float> wp = interp3(b, w.p);
                 I3 ic = clip_image_coords(d, wp);
                 if (mat.occlusion_texture > -1 && texture_1x1(s, mat.occlusion_texture).x < 0.1f) return;
@@ -572,7 +582,7 @@ inline int64_t svo_fragments(const SceneView& s, int octree_level, const float b
         }
         RasterSetup rs = raster_setup(c, res, res);
         if (!rs.ok) continue;
-        raster_visit(rs, 8, [&](int, int, int, const double* b, float) {
+        raster_visit(rs, 8, [&](int, int, int, const float* b, float) {
             if (mat.occlusion_texture > -1 && texture_1x1(s, mat.occlusion_texture).x < 0.1f) return;
             const int64_t slot = cur++;
             V3<float> fp = interp3(b, pos);

@@ -8,8 +8,8 @@
 // (the reference's MSAA pattern and shading rate are implementation-defined):
 // 8x MSAA at the Vulkan standard sample locations (one centre sample for the
 // depth-only pass), vertices snapped to 1/256 pixel, exact 64-bit edge
-// functions with a one-owner tie rule, depth clip [0,1], barycentrics in
-// FP64, the fragment shader at every covered sample.
+// functions with a one-owner tie rule, depth clip [0,1], FP32 barycentrics
+// float(e_i) * (1 / float(area)), the fragment shader at every covered sample.
 //
 // Work decomposition: one item per (triangle, clip level); each item's
 // bounding box is cut into 8x8-pixel tiles; one thread walks one tile (pixels
@@ -193,6 +193,7 @@ struct RSetup {
     float z[3];
     int order[3];
     long long area;
+    float inv_area;
     int px0, py0, px1, py1;
     int owned;  // bit i: edge i owns its samples
     bool ok;
@@ -227,6 +228,7 @@ __device__ inline RSetup raster_setup(const float4 c[3], int W, int H) {
         r.order[k] = o[k];
     }
     r.area = area;
+    r.inv_area = 1.0f / (float)area;
     r.owned = 0;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
@@ -254,7 +256,7 @@ __device__ inline uint32_t tiles_of(const RSetup& r) {
     return (uint32_t)(((r.px1 - r.px0) >> 3) + 1) * (uint32_t)(((r.py1 - r.py0) >> 3) + 1);
 }
 
-__device__ inline bool raster_test(const RSetup& r, long long sx, long long sy, double b[3], float& z) {
+__device__ inline bool raster_test(const RSetup& r, long long sx, long long sy, float b[3], float& z) {
     long long e[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
@@ -262,20 +264,19 @@ __device__ inline bool raster_test(const RSetup& r, long long sx, long long sy, 
         e[i] = (r.X[c] - r.X[a]) * (sy - r.Y[a]) - (r.Y[c] - r.Y[a]) * (sx - r.X[a]);
         if (e[i] < 0 || (e[i] == 0 && !((r.owned >> i) & 1))) return false;
     }
-    double bo[3];
+    float bo[3];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) bo[i] = (double)e[i] / (double)r.area;
-    z = (float)((bo[0] * (double)r.z[0] + bo[1] * (double)r.z[1]) + bo[2] * (double)r.z[2]);
+    for (int i = 0; i < 3; ++i) bo[i] = (float)e[i] * r.inv_area;
+    z = (bo[0] * r.z[0] + bo[1] * r.z[1]) + bo[2] * r.z[2];
     if (!(z >= 0.0f && z <= 1.0f)) return false;
 #pragma unroll
     for (int i = 0; i < 3; ++i) b[r.order[i]] = bo[i];
     return true;
 }
 
-__device__ inline float3 interp3(const double b[3], const float3 v[3]) {
-    return make_float3((float)((b[0] * (double)v[0].x + b[1] * (double)v[1].x) + b[2] * (double)v[2].x),
-                       (float)((b[0] * (double)v[0].y + b[1] * (double)v[1].y) + b[2] * (double)v[2].y),
-                       (float)((b[0] * (double)v[0].z + b[1] * (double)v[1].z) + b[2] * (double)v[2].z));
+__device__ inline float3 interp3(const float b[3], const float3 v[3]) {
+    return make_float3((b[0] * v[0].x + b[1] * v[1].x) + b[2] * v[2].x, (b[0] * v[0].y + b[1] * v[1].y) + b[2] * v[2].y,
+                       (b[0] * v[0].z + b[1] * v[1].z) + b[2] * v[2].z);
 }
 
 // Walk tile `t` of a set-up triangle in the pinned order.
@@ -295,7 +296,7 @@ __device__ inline void raster_tile(const RSetup& r, uint32_t t, int nsamples, F&
                     sx = (long long)px * 256 + c_sample_loc8[s][0];
                     sy = (long long)py * 256 + c_sample_loc8[s][1];
                 }
-                double b[3];
+                float b[3];
                 float z;
                 if (raster_test(r, sx, sy, b, z)) frag(px, py, b, z);
             }
@@ -326,6 +327,7 @@ struct RasterArgs {
     uint32_t* frags;
     int64_t frag_capacity;
     int64_t items;
+    uint32_t invalid_key;  // injection record key that sorts past every texel
 };
 
 __device__ inline void item_of(const RasterArgs& A, int64_t item, int64_t& tri, int& lvl) {
@@ -422,7 +424,7 @@ struct InjRecord {  // one face update of the injection, in traversal order
 // Injection fragment (msaaInjectRadiance.frag:68-155) -> up to 6 face updates.
 // Returns the number of updates; writes them to upd[] (key, r, g, b) with a = 1.
 __device__ inline int inject_fragment(const RasterArgs& A, const WTri& w, const vct_gltf_shade_material& mat,
-                                      int lvl, const double b[3], InjRecord upd[6]) {
+                                      int lvl, const float b[3], InjRecord upd[6]) {
     const vct_voxelization_desc& d = A.vd[lvl];
     const float3 wp = interp3(b, w.p);
     const int3 ic = clip_image_coords(d, wp);
@@ -469,7 +471,7 @@ __device__ inline int inject_fragment(const RasterArgs& A, const WTri& w, const 
 // discards it (no slot), 1 with `*valid` false if the light test discards it
 // after the counter increment (slot left untouched), else 1 and the packed pair.
 __device__ inline int svo_fragment(const RasterArgs& A, const WTri& w, const vct_gltf_shade_material& mat,
-                                   const float3 pos[3], const double b[3], bool* valid, uint2* out) {
+                                   const float3 pos[3], const float b[3], bool* valid, uint2* out) {
     if (mat.occlusion_texture > -1 && texture_1x1(A.s, mat.occlusion_texture).x < 0.1f) return 0;
     *valid = false;
     const float3 fp = interp3(b, pos);
@@ -514,7 +516,7 @@ __device__ inline int svo_fragment(const RasterArgs& A, const WTri& w, const vct
 }
 
 // ---------------------------------------------------------------- kernels
-__global__ void k_item_tiles(RasterArgs A, uint32_t* __restrict__ tiles) {
+__global__ void k_item_tiles(const __grid_constant__ RasterArgs A, uint32_t* __restrict__ tiles) {
     for (int64_t item = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; item < A.items;
          item += (int64_t)gridDim.x * blockDim.x) {
         int64_t tri;
@@ -527,8 +529,8 @@ __global__ void k_item_tiles(RasterArgs A, uint32_t* __restrict__ tiles) {
     }
 }
 
-template <int PHASE>
-__global__ void __launch_bounds__(128) k_raster_tiles(RasterArgs A, const uint32_t* __restrict__ tile_end,
+template <int KIND, int PHASE>
+__global__ void __launch_bounds__(128) k_raster_tiles(const __grid_constant__ RasterArgs A, const uint32_t* __restrict__ tile_end,
                                                       uint32_t* __restrict__ counts, const uint32_t* __restrict__ offs,
                                                       InjRecord* __restrict__ recs, int* __restrict__ err) {
     const uint32_t total = A.items > 0 ? tile_end[A.items - 1] : 0u;
@@ -552,10 +554,10 @@ __global__ void __launch_bounds__(128) k_raster_tiles(RasterArgs A, const uint32
             A.s.materials ? A.s.materials[min((int)w.material, A.s.material_count - 1)] : vct_gltf_shade_material{};
         uint32_t n = 0;
         uint32_t base = (PHASE == P_WRITE) ? offs[g] : 0u;
-        if (A.kind == K_OPACITY) {
+        if (KIND == K_OPACITY) {
             const vct_voxelization_desc& d = A.vd[lvl];
             const AtlasDims AD(A.R);
-            raster_tile(rs, local, 8, [&](int, int, const double* b, float) {
+            raster_tile(rs, local, 8, [&](int, int, const float* b, float) {
                 const float3 wp = interp3(b, w.p);
                 if (wp.x < d.region_min_corner[0] || wp.y < d.region_min_corner[1] || wp.z < d.region_min_corner[2] ||
                     wp.x > d.region_max_corner[0] || wp.y > d.region_max_corner[1] || wp.z > d.region_max_corner[2])
@@ -564,31 +566,44 @@ __global__ void __launch_bounds__(128) k_raster_tiles(RasterArgs A, const uint32
                 const int3 ic = clip_image_coords(d, wp);
                 for (int f = 0; f < 6; ++f) A.atlas[AD.index(ic.x + (A.R + 2) * f, ic.y, ic.z)] = 0xFFFFFFFFu;
             });
-        } else if (A.kind == K_SHADOW) {
-            raster_tile(rs, local, 1, [&](int px, int py, const double*, float z) {
+        } else if (KIND == K_SHADOW) {
+            raster_tile(rs, local, 1, [&](int px, int py, const float*, float z) {
                 atomicMin(reinterpret_cast<unsigned int*>(A.depth) + (int64_t)py * A.W + px, __float_as_uint(z));
             });
-        } else if (A.kind == K_INJECT) {
-            raster_tile(rs, local, 8, [&](int, int, const double* b, float) {
+        } else if (KIND == K_INJECT) {
+            // Every covered sample owns 3 face records (6 for emissive materials);
+            // the count pass only counts coverage, the write pass shades and marks
+            // discarded fragments' records invalid (they sort past every texel).
+            if (mat.occlusion_texture > -1 && texture_1x1(A.s, mat.occlusion_texture).x < 0.1f) continue;
+            const bool emissive =
+                mat.emissive_factor[0] > 0.0f || mat.emissive_factor[1] > 0.0f || mat.emissive_factor[2] > 0.0f;
+            const uint32_t per = emissive ? 6u : 3u;
+            raster_tile(rs, local, 8, [&](int, int, const float* b, float) {
+                if (PHASE == P_COUNT) {
+                    n += per;
+                    return;
+                }
                 InjRecord upd[6];
                 const int k = inject_fragment(A, w, mat, lvl, b, upd);
                 if (PHASE == P_DIRECT) {
                     for (int i = 0; i < k; ++i) rgba8_avg_atomic(A.atlas + upd[i].key, upd[i].r, upd[i].g, upd[i].b, 1.0f, err);
-                } else if (PHASE == P_WRITE) {
-                    for (int i = 0; i < k; ++i) recs[base + n + i] = upd[i];
+                } else {
+                    for (uint32_t i = 0; i < per; ++i)
+                        recs[base + n + i] = (int)i < k ? upd[i] : InjRecord{A.invalid_key, 0.f, 0.f, 0.f};
                 }
-                n += k;
+                n += per;
             });
         } else {  // K_SVO
-            raster_tile(rs, local, 8, [&](int, int, const double* b, float) {
-                bool valid;
-                uint2 v;
-                const int k = svo_fragment(A, w, mat, pos, b, &valid, &v);
-                if (PHASE == P_WRITE && k && valid) {
+            if (mat.occlusion_texture > -1 && texture_1x1(A.s, mat.occlusion_texture).x < 0.1f) continue;
+            raster_tile(rs, local, 8, [&](int, int, const float* b, float) {
+                if (PHASE == P_WRITE) {
+                    bool valid;
+                    uint2 v;
+                    svo_fragment(A, w, mat, pos, b, &valid, &v);
                     const uint64_t slot = (uint64_t)base + n;
-                    if ((int64_t)slot < A.frag_capacity) reinterpret_cast<uint2*>(A.frags)[slot] = v;
+                    if (valid && (int64_t)slot < A.frag_capacity) reinterpret_cast<uint2*>(A.frags)[slot] = v;
                 }
-                n += k;
+                n += 1;
             });
         }
         if (PHASE == P_COUNT) counts[g] = n;
@@ -597,10 +612,11 @@ __global__ void __launch_bounds__(128) k_raster_tiles(RasterArgs A, const uint32
 
 // Sequential per-texel fold of the stably sorted injection records.
 __global__ void k_inject_fold(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ order,
-                              const InjRecord* __restrict__ recs, uint32_t n, uint32_t* __restrict__ atlas) {
+                              const InjRecord* __restrict__ recs, uint32_t n, uint32_t invalid_key,
+                              uint32_t* __restrict__ atlas) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t key = keys[i];
-        if (i > 0 && keys[i - 1] == key) continue;
+        if (key == invalid_key || (i > 0 && keys[i - 1] == key)) continue;
         uint32_t cell = atlas[key];
         for (uint32_t j = i; j < n && keys[j] == key; ++j) {
             const InjRecord& r = recs[order[j]];
@@ -789,7 +805,7 @@ extern "C" int vct_voxelize_opacity(const vct_scene* scene, const vct_clipmap_re
     uint32_t total;
     rc = plan_tiles(A, ws, off, &tile_end, &total, st);
     if (rc != VCT_OK) return rc;
-    if (total) k_raster_tiles<P_DIRECT><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, nullptr, nullptr, nullptr, nullptr);
+    if (total) k_raster_tiles<K_OPACITY, P_DIRECT><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, nullptr, nullptr, nullptr, nullptr);
     VCT_LAUNCH_CHECK();
     return VCT_OK;
 }
@@ -821,7 +837,7 @@ extern "C" int vct_shadow_depth(const vct_scene* scene, const vct_directional_li
     uint32_t total;
     rc = plan_tiles(A, ws, off, &tile_end, &total, st);
     if (rc != VCT_OK) return rc;
-    if (total) k_raster_tiles<P_DIRECT><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, nullptr, nullptr, nullptr, nullptr);
+    if (total) k_raster_tiles<K_SHADOW, P_DIRECT><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, nullptr, nullptr, nullptr, nullptr);
     VCT_LAUNCH_CHECK();
     return VCT_OK;
 }
@@ -841,6 +857,10 @@ extern "C" int vct_inject_radiance(const vct_scene* scene, const vct_clipmap_reg
     A.s = *scene;
     A.kind = K_INJECT;
     A.R = R;
+    {  // all-ones key of the smallest width that covers every texel index
+        const uint32_t texels = (uint32_t)AtlasDims(R).texels();
+        A.invalid_key = 0xffffffffu >> __builtin_clz(texels);
+    }
     A.W = A.H = R + 2;
     fill_clipmap_levels(A, regions, R, level_mask);
     rc = fill_light(A, shadow, light, light_shadow);
@@ -857,7 +877,7 @@ extern "C" int vct_inject_radiance(const vct_scene* scene, const vct_clipmap_reg
     if (mode == VCT_INJECT_ATOMIC) {
         int* err = (int*)((char*)ws->ptr + off);
         VCT_CUDA_TRY(cudaMemsetAsync(err, 0, 4, st));
-        k_raster_tiles<P_DIRECT><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, nullptr, nullptr, nullptr, err);
+        k_raster_tiles<K_INJECT, P_DIRECT><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, nullptr, nullptr, nullptr, err);
         VCT_LAUNCH_CHECK();
         int herr = 0;
         VCT_CUDA_TRY(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st));
@@ -881,7 +901,7 @@ extern "C" int vct_inject_radiance(const vct_scene* scene, const vct_clipmap_reg
     uint32_t* counts = (uint32_t*)(base + head);
     uint32_t* offs = (uint32_t*)(base + head + a256(4 * (size_t)total));
     void* tmp = base + head + 2 * a256(4 * (size_t)total);
-    k_raster_tiles<P_COUNT><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, counts, nullptr, nullptr, nullptr);
+    k_raster_tiles<K_INJECT, P_COUNT><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, counts, nullptr, nullptr, nullptr);
     VCT_LAUNCH_CHECK();
     VCT_CUDA_TRY(cub::DeviceScan::ExclusiveSum(tmp, scan_bytes, counts, offs, (int)total, st));
     uint32_t last[2];
@@ -910,14 +930,14 @@ extern "C" int vct_inject_radiance(const vct_scene* scene, const vct_clipmap_reg
     uint32_t* vin = kout + a256(4 * (size_t)nrec) / 4;
     uint32_t* vout = vin + a256(4 * (size_t)nrec) / 4;
     void* stmp = (char*)(vout + a256(4 * (size_t)nrec) / 4);
-    k_raster_tiles<P_WRITE><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, nullptr, offs, recs, nullptr);
+    k_raster_tiles<K_INJECT, P_WRITE><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, nullptr, offs, recs, nullptr);
     VCT_LAUNCH_CHECK();
     k_rec_keys<<<grid_of(nrec, 256), 256, 0, st>>>(recs, kin, nrec);
     k_iota<<<grid_of(nrec, 256), 256, 0, st>>>(vin, nrec);
     VCT_LAUNCH_CHECK();
-    const int key_bits = 32 - __builtin_clz((unsigned)AtlasDims(R).texels());
+    const int key_bits = 32 - __builtin_clz((unsigned)A.invalid_key);
     VCT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(stmp, sort_bytes, kin, kout, vin, vout, (int)nrec, 0, key_bits, st));
-    k_inject_fold<<<grid_of(nrec, 256), 256, 0, st>>>(kout, vout, recs, nrec, atlas);
+    k_inject_fold<<<grid_of(nrec, 256), 256, 0, st>>>(kout, vout, recs, nrec, A.invalid_key, atlas);
     VCT_LAUNCH_CHECK();
     return VCT_OK;
 }
@@ -975,7 +995,7 @@ extern "C" int vct_svo_fragments(const vct_scene* scene, int32_t octree_level, c
     uint32_t* offs = (uint32_t*)(base + off + a256(4 * (size_t)total));
     void* tmp = base + off + 2 * a256(4 * (size_t)total);
     // count pass (SparseVoxelizer::preVoxelize), host readback of the count
-    k_raster_tiles<P_COUNT><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, counts, nullptr, nullptr, nullptr);
+    k_raster_tiles<K_SVO, P_COUNT><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, counts, nullptr, nullptr, nullptr);
     VCT_LAUNCH_CHECK();
     VCT_CUDA_TRY(cub::DeviceScan::ExclusiveSum(tmp, scan_bytes, counts, offs, (int)total, st));
     uint32_t last[2];
@@ -987,7 +1007,7 @@ extern "C" int vct_svo_fragments(const vct_scene* scene, int32_t octree_level, c
     if (*count > capacity) return fail(VCT_E_OVERFLOW, "vct_svo_fragments: fragment list capacity too small");
     // write pass (SparseVoxelizer::cmdVoxelize); discarded slots stay zero
     VCT_CUDA_TRY(cudaMemsetAsync(frags, 0, sizeof(uint32_t) * 2 * (size_t)*count, st));
-    k_raster_tiles<P_WRITE><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, nullptr, offs, nullptr, nullptr);
+    k_raster_tiles<K_SVO, P_WRITE><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, nullptr, offs, nullptr, nullptr);
     VCT_LAUNCH_CHECK();
     return VCT_OK;
 }

@@ -46,11 +46,31 @@ __global__ void k_init(uint2* pool, uint64_t begin, uint64_t num) {
         pool[begin + i] = make_uint2(0u, 0u);
 }
 
-__global__ void k_flag(uint2* pool, const uint2* __restrict__ frags, int64_t F, uint32_t res) {
+// Child slot a fragment takes at descent step k (resolution 2^(L-1-k)).  The
+// node shaders descend from the root subtracting the resolution where
+// pos >= resolution; for the halved position p <= 2^(L-1) that is: step 0
+// takes the upper child only when p == 2^(L-1) (and leaves p = 0), later
+// steps take bit (L-1-k) of the remaining p.  So the node a fragment reaches
+// at depth i is the depth-(i-1) node's child block plus slot(i-1): one step
+// per level from a per-fragment cursor instead of a descent from the root.
+__device__ inline uint32_t slot_at(uint3 p, int L, int k) {
+    const uint32_t top = 1u << (L - 1);
+    if (k == 0) return (p.z >= top ? 1u : 0u) | (p.x >= top ? 2u : 0u) | (p.y >= top ? 4u : 0u);
+    const uint3 q = make_uint3(p.x >= top ? p.x - top : p.x, p.y >= top ? p.y - top : p.y, p.z >= top ? p.z - top : p.z);
+    const int b = L - 1 - k;
+    return ((q.z >> b) & 1u) | (((q.x >> b) & 1u) << 1) | (((q.y >> b) & 1u) << 2);
+}
+
+// octreeNodeFlag.comp for level i through the cursor; the flag is written
+// only if not yet set (the shader's racy |= is idempotent either way).
+__global__ void k_flag_level(uint2* pool, const uint2* __restrict__ frags, int64_t F, int L, int level,
+                             uint32_t* __restrict__ cursor) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < F; i += (int64_t)gridDim.x * blockDim.x) {
-        uint32_t r;
-        const uint32_t idx = descend(pool, frag_pos(__ldg(frags + i)), res, 1u, r);
-        atomicOr(&pool[idx].x, 0x80000000u);
+        const uint3 p = frag_pos(__ldg(frags + i));
+        const uint32_t slot = slot_at(p, L, level - 1);
+        const uint32_t node = level == 1 ? slot : (pool[cursor[i]].x & 0x7fffffffu) + slot;
+        cursor[i] = node;
+        if (!(pool[node].x & 0x80000000u)) atomicOr(&pool[node].x, 0x80000000u);
     }
 }
 
@@ -106,13 +126,12 @@ __device__ inline uint32_t avg_fold(uint32_t cur, uint32_t v) {
     return conv_u8x4(cx, cy, cz, cw);
 }
 
-// Leaf of each fragment (0xffffffff if the descent does not reach resolution 1).
-__global__ void k_leaf_keys(const uint2* __restrict__ pool, const uint2* __restrict__ frags, int64_t F, uint32_t res,
-                            uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+// Leaf of each fragment: its cursor after the last level (the depth-L node
+// octreeNodeLeafWrite.comp's descent reaches at resolution 1).
+__global__ void k_leaf_keys(const uint32_t* __restrict__ cursor, int64_t F, uint32_t* __restrict__ keys,
+                            uint32_t* __restrict__ vals) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < F; i += (int64_t)gridDim.x * blockDim.x) {
-        uint32_t r;
-        const uint32_t idx = descend(pool, frag_pos(__ldg(frags + i)), res, 1u, r);
-        keys[i] = (r == 1u) ? idx : 0xffffffffu;
+        keys[i] = cursor[i];
         vals[i] = (uint32_t)i;
     }
 }
@@ -128,12 +147,11 @@ __global__ void k_leaf_fold(uint2* pool, const uint2* __restrict__ frags, const 
     }
 }
 
-__global__ void k_leaf_atomic(uint2* pool, const uint2* __restrict__ frags, int64_t F, uint32_t res, int* err) {
+__global__ void k_leaf_atomic(uint2* pool, const uint2* __restrict__ frags, int64_t F,
+                              const uint32_t* __restrict__ cursor, int* err) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < F; i += (int64_t)gridDim.x * blockDim.x) {
         const uint2 f = __ldg(frags + i);
-        uint32_t r;
-        const uint32_t idx = descend(pool, frag_pos(f), res, 1u, r);
-        if (r != 1u) continue;
+        const uint32_t idx = cursor[i];
         const uint32_t v = f.y & 0xfffffffu;
         uint32_t prev = 0u, newv = avg_fold(0u, v), cur;
         int guard = 0;
@@ -240,7 +258,7 @@ extern "C" int vct_svo_build(const uint32_t* fragments, int64_t F, int32_t L, ui
     VCT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(nullptr, sort_bytes, (uint32_t*)nullptr, (uint32_t*)nullptr,
                                                  (uint32_t*)nullptr, (uint32_t*)nullptr, (int)Fs, 0, 32));
     const size_t cap_arr = a256s(4 * (size_t)capacity), f_arr = a256s(4 * (size_t)Fs);
-    const size_t need = 2 * cap_arr + a256s(scan_bytes) + 256 + 4 * f_arr + a256s(sort_bytes);
+    const size_t need = 2 * cap_arr + a256s(scan_bytes) + 256 + 5 * f_arr + a256s(sort_bytes);
     int rc = workspace_reserve(ws, need);
     if (rc != VCT_OK) return rc;
     char* b = (char*)ws->ptr;
@@ -253,7 +271,8 @@ extern "C" int vct_svo_build(const uint32_t* fragments, int64_t F, int32_t L, ui
     uint32_t* kout = (uint32_t*)(fb + f_arr);
     uint32_t* vin = (uint32_t*)(fb + 2 * f_arr);
     uint32_t* vout = (uint32_t*)(fb + 3 * f_arr);
-    void* stmp = fb + 4 * f_arr;
+    uint32_t* cursor = (uint32_t*)(fb + 4 * f_arr);
+    void* stmp = fb + 5 * f_arr;
 
     uint64_t begin = 0, num = 8, count = 0;
     uint64_t wbegin[12], wnum[12];
@@ -263,7 +282,7 @@ extern "C" int vct_svo_build(const uint32_t* fragments, int64_t F, int32_t L, ui
         wbegin[i] = begin;
         wnum[i] = num;
         k_init<<<grid_n(num), 256, 0, st>>>(pool, begin, num);
-        if (F) k_flag<<<grid_n(F), 256, 0, st>>>(pool, frags, F, res);
+        if (F) k_flag_level<<<grid_n(F), 256, 0, st>>>(pool, frags, F, L, i, cursor);
         VCT_LAUNCH_CHECK();
         if (i != L) {
             uint64_t ones = 0;
@@ -291,7 +310,7 @@ extern "C" int vct_svo_build(const uint32_t* fragments, int64_t F, int32_t L, ui
     // leaf colours
     if (F) {
         if (mode == VCT_SVO_DETERMINISTIC) {
-            k_leaf_keys<<<grid_n(F), 256, 0, st>>>(pool, frags, F, res, kin, vin);
+            k_leaf_keys<<<grid_n(F), 256, 0, st>>>(cursor, F, kin, vin);
             VCT_LAUNCH_CHECK();
             size_t tb = sort_bytes;
             VCT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(stmp, tb, kin, kout, vin, vout, (int)F, 0, 32, st));
@@ -300,7 +319,7 @@ extern "C" int vct_svo_build(const uint32_t* fragments, int64_t F, int32_t L, ui
         } else {
             int* err = (int*)flags;
             VCT_CUDA_TRY(cudaMemsetAsync(err, 0, 4, st));
-            k_leaf_atomic<<<grid_n(F), 256, 0, st>>>(pool, frags, F, res, err);
+            k_leaf_atomic<<<grid_n(F), 256, 0, st>>>(pool, frags, F, cursor, err);
             VCT_LAUNCH_CHECK();
             int herr = 0;
             VCT_CUDA_TRY(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st));
