@@ -30,18 +30,14 @@ __global__ void k_clear_region(uint32_t* __restrict__ atlas, AtlasDims A, int3 r
 // ------------------------------------------------------------- copy alpha
 // copyAlphaImage.comp:16-30: dst.a = src.a over the R^3 interior, all faces.
 // Thread per texel of one face row (x fastest) -> coalesced 4-byte RMW.
+// blockIdx.y = face; R is a power of two, so the (x, y, z) split is shifts.
 __global__ void k_copy_alpha(uint32_t* __restrict__ dst, const uint32_t* __restrict__ src, AtlasDims A, int level,
-                             int faces) {
-    const int64_t per_face = (int64_t)A.R * A.R * A.R;
-    const int64_t n = per_face * faces;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
-        int x = (int)(t % A.R);
-        int64_t r = t / A.R;
-        int y = (int)(r % A.R);
-        r /= A.R;
-        int z = (int)(r % A.R);
-        int f = (int)(r / A.R);
-        int64_t i = A.index(x + 1 + A.rb * f, y + 1 + level * A.rb, z + 1);
+                             int lg) {
+    const int f = blockIdx.y;
+    const uint32_t n = 1u << (3 * lg), m = (1u << lg) - 1u;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int x = (int)(t & m), y = (int)((t >> lg) & m), z = (int)(t >> (2 * lg));
+        const int64_t i = A.index(x + 1 + A.rb * f, y + 1 + level * A.rb, z + 1);
         dst[i] = (dst[i] & 0x00ffffffu) | (__ldg(src + i) & 0xff000000u);
     }
 }
@@ -82,14 +78,13 @@ __constant__ int c_pairs[6][4][2] = {
     {{2, 0}, {3, 1}, {6, 4}, {7, 5}}, {{0, 4}, {1, 5}, {2, 6}, {3, 7}}, {{4, 0}, {5, 1}, {6, 2}, {7, 3}}};
 
 template <int MODE>
-__global__ void k_downsample(uint32_t* __restrict__ atlas, AtlasDims A, int3 pmin, int level, int band) {
+__global__ void k_downsample(uint32_t* __restrict__ atlas, AtlasDims A, int3 pmin, int level, int band, int lgh) {
     const int half = A.R >> 1;
-    const int64_t n = (int64_t)half * half * half;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
-        const int gx = (int)(t % half);
-        const int64_t r = t / half;
-        const int gy = (int)(r % half);
-        const int gz = (int)(r / half);
+    const uint32_t n = 1u << (3 * lgh), m = (1u << lgh) - 1u;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int gx = (int)(t & m);
+        const int gy = (int)((t >> lgh) & m);
+        const int gz = (int)(t >> (2 * lgh));
         const int cur[3] = {(pmin.x >> 1) + gx, (pmin.y >> 1) + gy, (pmin.z >> 1) + gz};
         const int pm[3] = {pmin.x, pmin.y, pmin.z};
         int wpos[3], ps[3];
@@ -201,9 +196,11 @@ extern "C" int vct_copy_alpha(uint32_t* dst, const uint32_t* src, const vct_copy
     VCT_CHECK_ARG(d->face_count >= 0 && d->face_count <= VCT_FACE_COUNT, "vct_copy_alpha: face count out of range");
     VCT_CHECK_ARG(dst != src, "vct_copy_alpha: source and destination atlases must differ");
     AtlasDims A(d->clipmap_resolution);
-    const int64_t n = (int64_t)A.R * A.R * A.R * d->face_count;
-    if (n == 0) return VCT_OK;
-    k_copy_alpha<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(dst, src, A, d->clip_level, d->face_count);
+    if (d->face_count == 0) return VCT_OK;
+    const int lg = 31 - __builtin_clz((unsigned)A.R);
+    const int64_t n = (int64_t)A.R * A.R * A.R;
+    dim3 grid((unsigned)grid_for(n, 256), (unsigned)d->face_count);
+    k_copy_alpha<<<grid, 256, 0, as_stream(stream)>>>(dst, src, A, d->clip_level, lg);
     VCT_LAUNCH_CHECK();
     return VCT_OK;
 }
@@ -234,10 +231,11 @@ extern "C" int vct_downsample(uint32_t* atlas, const vct_downsample_desc* d, int
     const int half = A.R >> 1;
     const int64_t n = (int64_t)half * half * half;
     int3 pm = make_int3(d->prev_region_min_corner[0], d->prev_region_min_corner[1], d->prev_region_min_corner[2]);
+    const int lgh = 31 - __builtin_clz((unsigned)half);
     if (mode == VCT_DOWNSAMPLE_OPACITY)
-        k_downsample<0><<<grid_for(n, 128), 128, 0, as_stream(stream)>>>(atlas, A, pm, d->clip_level, d->downsample_region_size);
+        k_downsample<0><<<grid_for(n, 128), 128, 0, as_stream(stream)>>>(atlas, A, pm, d->clip_level, d->downsample_region_size, lgh);
     else
-        k_downsample<1><<<grid_for(n, 128), 128, 0, as_stream(stream)>>>(atlas, A, pm, d->clip_level, d->downsample_region_size);
+        k_downsample<1><<<grid_for(n, 128), 128, 0, as_stream(stream)>>>(atlas, A, pm, d->clip_level, d->downsample_region_size, lgh);
     VCT_LAUNCH_CHECK();
     return VCT_OK;
 }

@@ -618,9 +618,22 @@ __global__ void k_inject_fold(const uint32_t* __restrict__ keys, const uint32_t*
         const uint32_t key = keys[i];
         if (key == invalid_key || (i > 0 && keys[i - 1] == key)) continue;
         uint32_t cell = atlas[key];
-        for (uint32_t j = i; j < n && keys[j] == key; ++j) {
-            const InjRecord& r = recs[order[j]];
-            cell = rgba8_avg_fold(cell, r.r, r.g, r.b, 1.0f);
+        uint32_t j = i;
+        // the fold is a serial chain per texel; fetch four records ahead of it
+        for (;;) {
+            InjRecord r4[4];
+            bool in[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const uint32_t jj = j + u;
+                in[u] = jj < n && keys[jj] == key;
+                if (in[u]) r4[u] = recs[order[jj]];
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (in[u]) cell = rgba8_avg_fold(cell, r4[u].r, r4[u].g, r4[u].b, 1.0f);
+            if (!in[3]) break;
+            j += 4;
         }
         atlas[key] = cell;
     }

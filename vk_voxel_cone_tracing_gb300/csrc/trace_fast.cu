@@ -10,9 +10,9 @@
 //      idles on a back-facing cone; every sample's cone results are summed by
 //      its owner lane in cone order (the shader's order);
 //   3. specular cones (57..780 marching steps, depending on the aperture) run
-//      in their own kernel over a list sorted by the 8-bit roughness texel
-//      (stable, so Morton order is kept inside a bucket): the lanes of a warp
-//      march equally long cones;
+//      in their own kernel, one cone per warp with consecutive steps on
+//      consecutive lanes (the steps of one cone are a fraction of a voxel
+//      apart, so the 32 lanes share texels) and warp scans for the composite;
 //   4. the clipmap is sampled through a 3D texture object (hardware trilinear
 //      filter, WRAP addressing = the reference's REPEAT sampler), RGBA8 or
 //      RGBA16F storage, FP32 compositing.
@@ -252,7 +252,7 @@ __global__ void __launch_bounds__(256) k_trace_diffuse(FastArgs A, const uint32_
             reinterpret_cast<float4*>(A.dout)[idx] = dd[0];
             if (!spec) reinterpret_cast<float4*>(A.sout)[idx] = dd[1];
         }
-        if (pos < A.n) spec_key[pos] = spec ? (uint32_t)__float2uint_rn(g.roughness * 255.0f) : 256u;
+        if (pos < A.n) spec_key[pos] = spec ? 0u : 256u;
         const unsigned bal = __ballot_sync(0xffffffffu, spec);
         if (lane == 0 && bal) atomicAdd(spec_count, (unsigned)__popc(bal));
     }
@@ -262,14 +262,119 @@ __global__ void __launch_bounds__(256) k_trace_diffuse(FastArgs A, const uint32_
     }
 }
 
-__global__ void __launch_bounds__(128) k_trace_specular(FastArgs A, const uint32_t* __restrict__ list,
-                                                        const unsigned int* __restrict__ spec_count) {
+// One cone marched by a whole warp: lane j takes step k0 + j of each chunk of
+// 32.  The step schedule (step, diameter, segment length) depends only on the
+// step index, not on the samples, so every lane runs the scalar recurrence of
+// traceCone for the chunk (identical SIMT work, exact schedule) and keeps its
+// own step.  The front-to-back composite result += (1 - result.a) * src is
+// the associative "over" operator and 1 - occlusion is the product of
+// (1 - x_k): both are warp scans.  The march stops at the first step whose
+// occlusion reaches 1 or whose distance reaches maxDistance, like the loop.
+__device__ __forceinline__ float4 trace_cone_warp(cudaTextureObject_t tex, const FastConsts& C, float3 start,
+                                                  float3 dir, float coef, float start_level, float step_factor,
+                                                  unsigned long long& steps) {
+    const int lane = threadIdx.x & 31;
+    const float uvs = C.uvs;
+    const float vs0 = uvs * exp2f(start_level);
+    const float off = vs0 * C.start_off * 0.5f;
+    start = f3(fmaf(dir.x, off, start.x), fmaf(dir.y, off, start.y), fmaf(dir.z, off, start.z));
+    const float fox = dir.x > 0.0f ? 0.0f : 1.0f / 6.0f;
+    const float foy = dir.y > 0.0f ? 2.0f / 6.0f : 3.0f / 6.0f;
+    const float foz = dir.z > 0.0f ? 4.0f / 6.0f : 5.0f / 6.0f;
+    const float3 wt = f3(dir.x * dir.x, dir.y * dir.y, dir.z * dir.z);
+    // carried state: composite (C, A), transmittance T, schedule (st, dm, sg)
+    float cr = 0.f, cg = 0.f, cb = 0.f, ca = 0.f, ct = 1.0f;
+    float st = 0.0f, dm = uvs, sg = vs0;
+    unsigned long long it = 0;
+    for (;;) {
+        float my_st = 0.f, my_dm = 0.f, my_sg = 0.f;
+#pragma unroll 8
+        for (int j = 0; j < 32; ++j) {
+            if (j == lane) {
+                my_st = st;
+                my_dm = dm;
+                my_sg = sg;
+            }
+            const float nst = fmaf(fmaxf(dm, uvs), step_factor, st);
+            sg = nst - st;
+            st = nst;
+            dm = st * coef;
+        }
+        const bool valid = my_st < kMaxTraceDistance;
+        float sr = 0.f, sgc = 0.f, sbc = 0.f, sa = 0.f, tx = 1.0f;
+        if (valid) {
+            const float3 pos = f3(fmaf(dir.x, my_st, start.x), fmaf(dir.y, my_st, start.y), fmaf(dir.z, my_st, start.z));
+            const float dx = C.cx - pos.x, dy = C.cy - pos.y, dz = C.cz - pos.z;
+            const float dist = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+            const float min_level = ceilf(log2f(dist * C.inv_min_radius));
+            float cl = log2f(my_dm * C.inv_uvs);
+            cl = fminf(fmaxf(fmaxf(start_level, cl), min_level), (float)(kClipLevels - 1));
+            const float flo = floorf(cl);
+            const int lo = (int)flo;
+            const float fr = cl - flo;
+            float4 smp = sample_level(tex, C, pos, lo, fox, foy, foz, wt);
+            if (fr > 0.0f) {
+                const float4 h = sample_level(tex, C, pos, lo + 1, fox, foy, foz, wt);
+                smp = make_float4(fmaf(h.x - smp.x, fr, smp.x), fmaf(h.y - smp.y, fr, smp.y),
+                                  fmaf(h.z - smp.z, fr, smp.z), fmaf(h.w - smp.w, fr, smp.w));
+            }
+            const float vs = uvs * exp2f(cl);
+            const float corr = __fdividef(my_sg, vs);
+            const float opacity = __saturatef(1.0f - exp2f(corr * __log2f(1.0f - smp.w)));
+            sr = smp.x * corr;
+            sgc = smp.y * corr;
+            sbc = smp.z * corr;
+            sa = opacity;
+            tx = 1.0f - __fdividef(opacity, fmaf(my_st + vs, C.decay, 1.0f));
+        }
+        // inclusive warp scans: over-composite of (rgb, a) and product of transmittance
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const float pr = __shfl_up_sync(0xffffffffu, sr, o), pg = __shfl_up_sync(0xffffffffu, sgc, o);
+            const float pb = __shfl_up_sync(0xffffffffu, sbc, o), pa = __shfl_up_sync(0xffffffffu, sa, o);
+            const float pt = __shfl_up_sync(0xffffffffu, tx, o);
+            if (lane >= o) {
+                const float k = 1.0f - pa;
+                sr = fmaf(k, sr, pr);
+                sgc = fmaf(k, sgc, pg);
+                sbc = fmaf(k, sbc, pb);
+                sa = fmaf(k, sa, pa);
+                tx = tx * pt;
+            }
+        }
+        // combine with the carried state
+        const float k = 1.0f - ca;
+        const float tr = fmaf(k, sr, cr), tg = fmaf(k, sgc, cg), tb = fmaf(k, sbc, cb), ta = fmaf(k, sa, ca);
+        const float tt = ct * tx;
+        // executed lanes: valid ones up to (and including) the first whose occlusion reaches 1
+        const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+        const unsigned omask = __ballot_sync(0xffffffffu, valid && (1.0f - tt) >= 1.0f);
+        int last = 31 - __clz(vmask);  // vmask is a prefix of lanes (the step grows)
+        if (omask) last = min(last, __ffs(omask) - 1);
+        if (vmask == 0u) break;
+        cr = __shfl_sync(0xffffffffu, tr, last);
+        cg = __shfl_sync(0xffffffffu, tg, last);
+        cb = __shfl_sync(0xffffffffu, tb, last);
+        ca = __shfl_sync(0xffffffffu, ta, last);
+        ct = __shfl_sync(0xffffffffu, tt, last);
+        it += (unsigned long long)(last + 1);
+        if (last < 31 || omask) break;
+    }
+    if (lane == 0) steps += it;
+    return make_float4(cr, cg, cb, ct);
+}
+
+// One warp per specular cone of the list (the list is kept in Morton order).
+__global__ void __launch_bounds__(256) k_trace_specular_warp(FastArgs A, const uint32_t* __restrict__ list,
+                                                             const unsigned int* __restrict__ spec_count) {
     const TraceParams& P = A.P;
     const FastConsts& C = A.C;
+    const int lane = threadIdx.x & 31;
     const int64_t m = *spec_count;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     unsigned long long steps = 0;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t idx = __ldg(list + i);
+    for (int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < m; c += nwarps) {
+        const uint32_t idx = __ldg(list + c);
         const GSample g = load_sample(A.samples + idx, P.eye);
         const float min_level = calc_min_level(P.d, g.wp);
         const float vs = C.uvs * exp2f(min_level);
@@ -277,15 +382,17 @@ __global__ void __launch_bounds__(128) k_trace_specular(FastArgs A, const uint32
         const float3 sdir = reflect3(f3(-g.view.x, -g.view.y, -g.view.z), g.normal);
         const float ap = fmaxf(g.roughness, kMinSpecularAperture);
         const float coef = 2.0f * tanf(ap * 0.5f);
-        const float4 r = trace_cone_fast(A.tex, C, start, sdir, coef, min_level, C.uvs, steps);
-        const float isi = P.d.indirect_specular_intensity;
-        reinterpret_cast<float4*>(A.sout)[idx] =
-            make_float4(r.x * g.specular_color.x * isi, r.y * g.specular_color.y * isi,
-                        r.z * g.specular_color.z * isi, 1.0f);
+        const float4 r = trace_cone_warp(A.tex, C, start, sdir, coef, min_level, C.uvs, steps);
+        if (lane == 0) {
+            const float isi = P.d.indirect_specular_intensity;
+            reinterpret_cast<float4*>(A.sout)[idx] =
+                make_float4(r.x * g.specular_color.x * isi, r.y * g.specular_color.y * isi,
+                            r.z * g.specular_color.z * isi, 1.0f);
+        }
     }
     if (A.steps) {
         for (int o = 16; o > 0; o >>= 1) steps += __shfl_xor_sync(0xffffffffu, steps, o);
-        if ((threadIdx.x & 31) == 0 && steps) atomicAdd(A.steps, steps);
+        if (lane == 0 && steps) atomicAdd(A.steps, steps);
     }
 }
 
@@ -415,11 +522,12 @@ extern "C" int vct_cone_trace_fast(const vct_cone_tracing_desc* desc, const vct_
     VCT_LAUNCH_CHECK();
     if (A.C.need_specular) {
         tb = S.temp_bytes;
+        // stable partition (one radix pass on bit 8): specular samples first, Morton order kept
         VCT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(S.temp, tb, S.spec_key, S.spec_key_out, S.order, S.spec_list,
-                                                     (int)n, 0, 9, st));
-        int64_t gs = (n + 127) / 128;
-        const int grid_s = (int)(gs > 152 * 16 ? 152 * 16 : gs);
-        k_trace_specular<<<grid_s, 128, 0, st>>>(A, S.spec_list, S.spec_count);
+                                                     (int)n, 8, 9, st));
+        int64_t gw = (n * 32 + 255) / 256;
+        const int grid_s = (int)(gw > 152 * 64 ? 152 * 64 : gw);
+        k_trace_specular_warp<<<grid_s, 256, 0, st>>>(A, S.spec_list, S.spec_count);
         VCT_LAUNCH_CHECK();
     }
     return VCT_OK;
