@@ -104,6 +104,40 @@ def test_inject_radiance_deterministic_bit_exact(cuda, oracle, scene, dscene, ws
     assert (diff[:, 3] == 0).all()
 
 
+def test_inject_long_runs_into_prefilled_atlas_bit_exact(cuda, oracle):
+    """400 stacked quads inside one level-0 voxel layer put about 800 face
+    records on most texels they touch (far past the 256-step alpha wrap of the
+    running average), and the atlas starts from random texels (random alpha
+    counters), so the per-texel fold meets every starting phase."""
+    torch = cuda
+    from vk_voxel_cone_tracing_gb300 import capi, clipmap, passes
+    from vk_voxel_cone_tracing_gb300.scene import _pack
+    R = 32
+    rng = np.random.default_rng(5)
+    quads = []
+    for i in range(400):
+        x = np.float32(-2.0 + 0.001 * i)
+        a, b, c, d = [x, -4, -6], [x, 8, -6], [x, 8, 6], [x, -4, 6]
+        quads += [[a, c, b], [a, d, c]]
+    stack = _pack(np.array(quads, np.float32), rng)
+    dstack = passes.DeviceScene(stack)
+    ws = passes.Workspace()
+    regions = oracle.clip_regions(CAM, R)
+    start = rng.integers(0, 2 ** 32, size=(R + 2, 6 * (R + 2), 6 * (R + 2)), dtype=np.uint64).astype(np.uint32)
+    want = oracle.inject_radiance(stack, R, regions, None, bytes(capi.DirectionalLightShadowDesc()),
+                                  atlas=start.copy())
+    atlas = torch.from_numpy(start.view(np.int32).copy()).cuda()
+    passes.inject_radiance(dstack, clipmap.clip_regions(CAM, R), R, None, passes.light_desc(LIGHT_DIR),
+                           capi.DirectionalLightShadowDesc(), atlas, ws, mode=capi.INJECT_DETERMINISTIC)
+    torch.cuda.synchronize()
+    got = _u32(atlas)
+    assert np.count_nonzero(want != start) > 1000
+    assert np.array_equal(got, want), f"{np.count_nonzero(got != want)} texels differ"
+    # from a zero atlas the alpha byte is the record count mod 256: 800 -> 32
+    zero = oracle.inject_radiance(stack, R, regions, None, bytes(capi.DirectionalLightShadowDesc()))
+    assert np.count_nonzero(((zero >> 24) & 0xFF) == 32) > 1000
+
+
 def test_svo_fragments_bit_exact(cuda, oracle, scene, dscene, ws):
     torch = cuda
     from vk_voxel_cone_tracing_gb300 import passes

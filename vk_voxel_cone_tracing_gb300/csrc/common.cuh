@@ -49,12 +49,24 @@ struct AtlasDims {
 inline bool valid_resolution(int R) { return R >= 8 && R <= 1024 && (R & (R - 1)) == 0; }
 
 // ------------------------------------------------------------- unorm8
-__device__ __forceinline__ float unorm8_load(uint32_t v, int c) {
-    return (float)((v >> (8 * c)) & 0xffu) / 255.0f;
+// Byte b -> the IEEE quotient b / 255 (the unorm8 decode), computed as one
+// multiply by RN(1/255) followed by one Markstein correction step
+// (P. Markstein, "IA-64 and Elementary Functions", 2000): q0 = b * r,
+// e = b - 255 * q0 (exact through the fused multiply-add), q = q0 + e * r.
+// Equal to the correctly rounded quotient for all 256 bytes (checked
+// exhaustively in exact rational arithmetic by the test suite); a plain
+// b * RN(1/255) is one ulp off for 126 of them.
+__device__ __forceinline__ float unorm8_decode(uint32_t b) {
+    const float x = (float)b;
+    const float r = __uint_as_float(0x3b808081u);  // RN(1/255)
+    const float q0 = __fmul_rn(x, r);
+    const float e = __fmaf_rn(-q0, 255.0f, x);
+    return __fmaf_rn(e, r, q0);
 }
+__device__ __forceinline__ float unorm8_load(uint32_t v, int c) { return unorm8_decode((v >> (8 * c)) & 0xffu); }
 __device__ __forceinline__ float4 unpack_rgba8(uint32_t v) {
-    return make_float4((float)(v & 0xffu) / 255.0f, (float)((v >> 8) & 0xffu) / 255.0f,
-                       (float)((v >> 16) & 0xffu) / 255.0f, (float)(v >> 24) / 255.0f);
+    return make_float4(unorm8_decode(v & 0xffu), unorm8_decode((v >> 8) & 0xffu), unorm8_decode((v >> 16) & 0xffu),
+                       unorm8_decode(v >> 24));
 }
 // Pinned store rule: round-half-up of clamp(x, 0, 1) * 255.
 __device__ __forceinline__ uint32_t unorm8_store(float x) {

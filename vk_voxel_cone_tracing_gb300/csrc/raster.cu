@@ -16,13 +16,17 @@
 // row-major, samples in index order).  Items' tile counts are prefix-summed
 // and the tile kernel finds its item by binary search, so no per-tile list is
 // materialised.  Order-dependent passes (RGBA8 running averages, the SVO
-// fragment list) use a count pass + prefix sum + write pass, which fixes the
-// traversal order (item, tile, pixel, sample); the injection's records are
-// then stably sorted by texel and folded sequentially per texel, which
+// fragment list) use a coverage count pass + prefix sum + an emit pass that
+// writes one compact descriptor per covered sample in traversal order (item,
+// tile, pixel, sample); a shading kernel then runs one thread per covered
+// sample, so neighbouring lanes shade neighbouring samples of one triangle
+// (their shadow-map taps share cache lines).  The injection's records are
+// stably sorted by texel and folded sequentially per texel run, which
 // reproduces the serial order of the reference's CAS loops bit for bit.
 // Compiled with -fmad=false: the fragment arithmetic is the FP32 GLSL in its
 // written order.
 #include <cub/cub.cuh>
+#include <thrust/iterator/counting_iterator.h>
 
 #include "trace_common.cuh"
 
@@ -191,7 +195,7 @@ __constant__ int c_sample_loc8[8][2] = {{144, 80}, {112, 176}, {208, 144}, {80, 
 struct RSetup {
     long long X[3], Y[3];
     float z[3];
-    int order[3];
+    bool swapped;  // vertices 1 and 2 exchanged to make the winding counter-clockwise
     long long area;
     float inv_area;
     int px0, py0, px1, py1;
@@ -213,20 +217,19 @@ __device__ inline RSetup raster_setup(const float4 c[3], int W, int H) {
     long long area = (X[1] - X[0]) * (Y[2] - Y[0]) - (Y[1] - Y[0]) * (X[2] - X[0]);
     r.ok = area != 0;
     if (!r.ok) return r;
-    int o1 = 1, o2 = 2;
-    if (area < 0) {
-        o1 = 2;
-        o2 = 1;
-        area = -area;
-    }
-    const int o[3] = {0, o1, o2};
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        r.X[k] = X[o[k]];
-        r.Y[k] = Y[o[k]];
-        r.z[k] = c[o[k]].z;
-        r.order[k] = o[k];
-    }
+    // counter-clockwise vertex order: swap vertices 1 and 2 of a clockwise triangle
+    const bool sw = area < 0;
+    if (sw) area = -area;
+    r.X[0] = X[0];
+    r.Y[0] = Y[0];
+    r.z[0] = c[0].z;
+    r.X[1] = sw ? X[2] : X[1];
+    r.Y[1] = sw ? Y[2] : Y[1];
+    r.z[1] = sw ? c[2].z : c[1].z;
+    r.X[2] = sw ? X[1] : X[2];
+    r.Y[2] = sw ? Y[1] : Y[2];
+    r.z[2] = sw ? c[1].z : c[2].z;
+    r.swapped = sw;
     r.area = area;
     r.inv_area = 1.0f / (float)area;
     r.owned = 0;
@@ -269,8 +272,9 @@ __device__ inline bool raster_test(const RSetup& r, long long sx, long long sy, 
     for (int i = 0; i < 3; ++i) bo[i] = (float)e[i] * r.inv_area;
     z = (bo[0] * r.z[0] + bo[1] * r.z[1]) + bo[2] * r.z[2];
     if (!(z >= 0.0f && z <= 1.0f)) return false;
-#pragma unroll
-    for (int i = 0; i < 3; ++i) b[r.order[i]] = bo[i];
+    b[0] = bo[0];
+    b[1] = r.swapped ? bo[2] : bo[1];
+    b[2] = r.swapped ? bo[1] : bo[2];
     return true;
 }
 
@@ -422,11 +426,11 @@ struct InjRecord {  // one face update of the injection, in traversal order
 };
 
 // Injection fragment (msaaInjectRadiance.frag:68-155) -> up to 6 face updates.
+// `wp` and `n` are the interpolated world position and (unnormalised) normal.
 // Returns the number of updates; writes them to upd[] (key, r, g, b) with a = 1.
-__device__ inline int inject_fragment(const RasterArgs& A, const WTri& w, const vct_gltf_shade_material& mat,
-                                      int lvl, const float b[3], InjRecord upd[6]) {
+__device__ inline int inject_fragment(const RasterArgs& A, const vct_gltf_shade_material& mat, int lvl, float3 wp,
+                                      float3 n, InjRecord upd[6]) {
     const vct_voxelization_desc& d = A.vd[lvl];
-    const float3 wp = interp3(b, w.p);
     const int3 ic = clip_image_coords(d, wp);
     if (mat.occlusion_texture > -1 && texture_1x1(A.s, mat.occlusion_texture).x < 0.1f) return 0;
     const AtlasDims AD(A.R);
@@ -450,7 +454,7 @@ __device__ inline int inject_fragment(const RasterArgs& A, const WTri& w, const 
         float4 tx = texture_1x1(A.s, mat.pbr_base_color_texture);
         color = make_float4(color.x * tx.x, color.y * tx.y, color.z * tx.z, color.w * tx.w);
     }
-    const float3 nrm = normalize3h(interp3(b, w.n));
+    const float3 nrm = normalize3h(n);
     const float3 ld = make_float3(A.ldir[0], A.ldir[1], A.ldir[2]);
     const float NdotL = fminf(fmaxf(dot3h(nrm, ld), 0.001f), 1.0f);
     const float vis = calc_visibility(A.light, wp);
@@ -467,14 +471,15 @@ __device__ inline int inject_fragment(const RasterArgs& A, const WTri& w, const 
     return 3;
 }
 
-// SVO fragment (voxelizer.frag:48-103).  Returns 0 if the occlusion texture
-// discards it (no slot), 1 with `*valid` false if the light test discards it
-// after the counter increment (slot left untouched), else 1 and the packed pair.
-__device__ inline int svo_fragment(const RasterArgs& A, const WTri& w, const vct_gltf_shade_material& mat,
-                                   const float3 pos[3], const float b[3], bool* valid, uint2* out) {
+// SVO fragment (voxelizer.frag:48-103).  `fp` is the interpolated normalised
+// position and `n` the interpolated (unnormalised) normal.  Returns 0 if the
+// occlusion texture discards it (no slot), 1 with `*valid` false if the light
+// test discards it after the counter increment (slot left untouched), else 1
+// and the packed pair.
+__device__ inline int svo_fragment(const RasterArgs& A, const vct_gltf_shade_material& mat, float3 fp, float3 n,
+                                   bool* valid, uint2* out) {
     if (mat.occlusion_texture > -1 && texture_1x1(A.s, mat.occlusion_texture).x < 0.1f) return 0;
     *valid = false;
-    const float3 fp = interp3(b, pos);
     float rad[4] = {1.0f, 1.0f, 1.0f, 1.0f};
     const bool emissive = mat.emissive_factor[0] > 0.0f || mat.emissive_factor[1] > 0.0f || mat.emissive_factor[2] > 0.0f;
     if (emissive) {
@@ -493,7 +498,7 @@ __device__ inline int svo_fragment(const RasterArgs& A, const WTri& w, const vct
             color = make_float4(tx.x * mat.pbr_base_color_factor[0], tx.y * mat.pbr_base_color_factor[1],
                                 tx.z * mat.pbr_base_color_factor[2], tx.w * mat.pbr_base_color_factor[3]);
         }
-        const float3 nrm = normalize3h(interp3(b, w.n));
+        const float3 nrm = normalize3h(n);
         const float3 ld = make_float3(A.ldir[0], A.ldir[1], A.ldir[2]);
         const float NdotL = fminf(fmaxf(dot3h(nrm, ld), 0.001f), 1.0f);
         const float vis = calc_visibility(A.light, fp);
@@ -529,10 +534,39 @@ __global__ void k_item_tiles(const __grid_constant__ RasterArgs A, uint32_t* __r
     }
 }
 
+// One covered sample of the injection or SVO pass, compacted in traversal
+// order for the shading kernels: the interpolated position (world space for
+// the injection, the normalised [0,1] cube for the SVO), the output slot (the
+// first face record of the injection, the fragment-list slot of the SVO),
+// the interpolated unnormalised normal, and level | material << 3.
+struct FragDesc {
+    float4 p;  // x, y, z, slot (bits)
+    float4 n;  // x, y, z, meta (bits)
+};
+
+__device__ inline vct_gltf_shade_material material_of(const vct_scene& s, uint32_t mi) {
+    return s.materials ? s.materials[min((int)mi, s.material_count - 1)] : vct_gltf_shade_material{};
+}
+
+__device__ inline bool item_discarded(const RasterArgs& A, const vct_gltf_shade_material& mat) {
+    // occlusion textures are 1x1, so their discard test is per material
+    return mat.occlusion_texture > -1 && texture_1x1(A.s, mat.occlusion_texture).x < 0.1f;
+}
+
+__device__ inline uint32_t inject_per_fragment(const vct_gltf_shade_material& mat) {
+    const bool emissive = mat.emissive_factor[0] > 0.0f || mat.emissive_factor[1] > 0.0f || mat.emissive_factor[2] > 0.0f;
+    return emissive ? 6u : 3u;
+}
+
+// Tile kernels.  A thread takes one 8x8 pixel tile of one (triangle, level)
+// item, found by binary search over the inclusive tile sums.  P_DIRECT writes
+// the pass's output directly (opacity, shadow depth, atomic injection);
+// P_COUNT counts covered samples and their records per tile (injection, SVO);
+// P_WRITE emits the FragDesc of each covered sample at its scanned position.
 template <int KIND, int PHASE>
 __global__ void __launch_bounds__(128) k_raster_tiles(const __grid_constant__ RasterArgs A, const uint32_t* __restrict__ tile_end,
-                                                      uint32_t* __restrict__ counts, const uint32_t* __restrict__ offs,
-                                                      InjRecord* __restrict__ recs, int* __restrict__ err) {
+                                                      uint2* __restrict__ counts, const uint2* __restrict__ offs,
+                                                      FragDesc* __restrict__ frags, int* __restrict__ err) {
     const uint32_t total = A.items > 0 ? tile_end[A.items - 1] : 0u;
     for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
         int64_t lo = 0, hi = A.items - 1;  // first item with tile_end > g
@@ -549,12 +583,10 @@ __global__ void __launch_bounds__(128) k_raster_tiles(const __grid_constant__ Ra
         const WTri w = world_triangle(A.s, tri);
         RSetup rs;
         float3 pos[3];
-        if (!item_setup(A, w, lvl, rs, pos)) continue;
-        const vct_gltf_shade_material mat =
-            A.s.materials ? A.s.materials[min((int)w.material, A.s.material_count - 1)] : vct_gltf_shade_material{};
-        uint32_t n = 0;
-        uint32_t base = (PHASE == P_WRITE) ? offs[g] : 0u;
+        const bool ok = item_setup(A, w, lvl, rs, pos);
+        const vct_gltf_shade_material mat = material_of(A.s, w.material);
         if (KIND == K_OPACITY) {
+            if (!ok) continue;
             const vct_voxelization_desc& d = A.vd[lvl];
             const AtlasDims AD(A.R);
             raster_tile(rs, local, 8, [&](int, int, const float* b, float) {
@@ -562,89 +594,146 @@ __global__ void __launch_bounds__(128) k_raster_tiles(const __grid_constant__ Ra
                 if (wp.x < d.region_min_corner[0] || wp.y < d.region_min_corner[1] || wp.z < d.region_min_corner[2] ||
                     wp.x > d.region_max_corner[0] || wp.y > d.region_max_corner[1] || wp.z > d.region_max_corner[2])
                     return;
-                if (mat.occlusion_texture > -1 && texture_1x1(A.s, mat.occlusion_texture).x < 0.1f) return;
+                if (item_discarded(A, mat)) return;
                 const int3 ic = clip_image_coords(d, wp);
                 for (int f = 0; f < 6; ++f) A.atlas[AD.index(ic.x + (A.R + 2) * f, ic.y, ic.z)] = 0xFFFFFFFFu;
             });
         } else if (KIND == K_SHADOW) {
+            if (!ok) continue;
             raster_tile(rs, local, 1, [&](int px, int py, const float*, float z) {
                 atomicMin(reinterpret_cast<unsigned int*>(A.depth) + (int64_t)py * A.W + px, __float_as_uint(z));
             });
-        } else if (KIND == K_INJECT) {
-            // Every covered sample owns 3 face records (6 for emissive materials);
-            // the count pass only counts coverage, the write pass shades and marks
-            // discarded fragments' records invalid (they sort past every texel).
-            if (mat.occlusion_texture > -1 && texture_1x1(A.s, mat.occlusion_texture).x < 0.1f) continue;
-            const bool emissive =
-                mat.emissive_factor[0] > 0.0f || mat.emissive_factor[1] > 0.0f || mat.emissive_factor[2] > 0.0f;
-            const uint32_t per = emissive ? 6u : 3u;
+        } else if (PHASE == P_DIRECT) {  // atomic injection: shade and fold in place
+            if (!ok || item_discarded(A, mat)) continue;
             raster_tile(rs, local, 8, [&](int, int, const float* b, float) {
-                if (PHASE == P_COUNT) {
-                    n += per;
-                    return;
-                }
                 InjRecord upd[6];
-                const int k = inject_fragment(A, w, mat, lvl, b, upd);
-                if (PHASE == P_DIRECT) {
-                    for (int i = 0; i < k; ++i) rgba8_avg_atomic(A.atlas + upd[i].key, upd[i].r, upd[i].g, upd[i].b, 1.0f, err);
-                } else {
-                    for (uint32_t i = 0; i < per; ++i)
-                        recs[base + n + i] = (int)i < k ? upd[i] : InjRecord{A.invalid_key, 0.f, 0.f, 0.f};
-                }
-                n += per;
+                const int k = inject_fragment(A, mat, lvl, interp3(b, w.p), interp3(b, w.n), upd);
+                for (int i = 0; i < k; ++i) rgba8_avg_atomic(A.atlas + upd[i].key, upd[i].r, upd[i].g, upd[i].b, 1.0f, err);
             });
-        } else {  // K_SVO
-            if (mat.occlusion_texture > -1 && texture_1x1(A.s, mat.occlusion_texture).x < 0.1f) continue;
-            raster_tile(rs, local, 8, [&](int, int, const float* b, float) {
-                if (PHASE == P_WRITE) {
-                    bool valid;
-                    uint2 v;
-                    svo_fragment(A, w, mat, pos, b, &valid, &v);
-                    const uint64_t slot = (uint64_t)base + n;
-                    if (valid && (int64_t)slot < A.frag_capacity) reinterpret_cast<uint2*>(A.frags)[slot] = v;
-                }
-                n += 1;
-            });
+        } else {
+            // Injection: every covered sample owns 3 face records (6 for emissive
+            // materials); SVO: one fragment-list slot.  Occlusion-discarded
+            // items own nothing (the reference discards before its counter).
+            const bool live = ok && !item_discarded(A, mat);
+            const uint32_t per = KIND == K_INJECT ? inject_per_fragment(mat) : 1u;
+            uint32_t n = 0;
+            if (PHASE == P_COUNT) {
+                if (live) raster_tile(rs, local, 8, [&](int, int, const float*, float) { ++n; });
+                counts[g] = make_uint2(n, n * per);
+            } else if (live) {
+                const uint2 base = offs[g];
+                const uint32_t meta = (uint32_t)lvl | (min(w.material, (uint32_t)max(A.s.material_count - 1, 0)) << 3);
+                raster_tile(rs, local, 8, [&](int, int, const float* b, float) {
+                    const float3 p = KIND == K_INJECT ? interp3(b, w.p) : interp3(b, pos);
+                    const float3 nn = interp3(b, w.n);
+                    FragDesc d;
+                    d.p = make_float4(p.x, p.y, p.z, __uint_as_float(base.y + n * per));
+                    d.n = make_float4(nn.x, nn.y, nn.z, __uint_as_float(meta));
+                    frags[base.x + n] = d;
+                    ++n;
+                });
+            }
         }
-        if (PHASE == P_COUNT) counts[g] = n;
     }
 }
 
-// Sequential per-texel fold of the stably sorted injection records.
-__global__ void k_inject_fold(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ order,
-                              const InjRecord* __restrict__ recs, uint32_t n, uint32_t invalid_key,
-                              uint32_t* __restrict__ atlas) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t key = keys[i];
-        if (key == invalid_key || (i > 0 && keys[i - 1] == key)) continue;
+// Injection shading, one thread per covered sample: writes its face records
+// (texel key, traversal position, colour) at the scanned record offset; the
+// records that the fragment shader does not produce get a key that sorts
+// past every texel.
+__global__ void __launch_bounds__(256) k_inject_shade(const __grid_constant__ RasterArgs A, const FragDesc* __restrict__ frags,
+                                                      uint32_t nfrag, uint32_t* __restrict__ keys,
+                                                      uint32_t* __restrict__ order, float4* __restrict__ rgb) {
+    for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < nfrag; f += gridDim.x * blockDim.x) {
+        const FragDesc d = frags[f];
+        const uint32_t rec = __float_as_uint(d.p.w), meta = __float_as_uint(d.n.w);
+        const vct_gltf_shade_material mat = material_of(A.s, meta >> 3);
+        InjRecord upd[6];
+        const int k = inject_fragment(A, mat, (int)(meta & 7u), make_float3(d.p.x, d.p.y, d.p.z),
+                                      make_float3(d.n.x, d.n.y, d.n.z), upd);
+        const uint32_t per = inject_per_fragment(mat);
+        for (uint32_t i = 0; i < per; ++i) {
+            const bool v = (int)i < k;
+            keys[rec + i] = v ? upd[i].key : A.invalid_key;
+            order[rec + i] = rec + i;
+            rgb[rec + i] = v ? make_float4(upd[i].r, upd[i].g, upd[i].b, 0.0f) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    }
+}
+
+// SVO fragment shading, one thread per covered sample: writes the packed
+// (position, colour) pair into its slot; light-discarded slots stay zero.
+__global__ void __launch_bounds__(256) k_svo_shade(const __grid_constant__ RasterArgs A, const FragDesc* __restrict__ frags,
+                                                   uint32_t nfrag) {
+    for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < nfrag; f += gridDim.x * blockDim.x) {
+        const FragDesc d = frags[f];
+        const uint32_t slot = __float_as_uint(d.p.w), meta = __float_as_uint(d.n.w);
+        const vct_gltf_shade_material mat = material_of(A.s, meta >> 3);
+        bool valid = false;
+        uint2 v;
+        svo_fragment(A, mat, make_float3(d.p.x, d.p.y, d.p.z), make_float3(d.n.x, d.n.y, d.n.z), &valid, &v);
+        if (valid && (int64_t)slot < A.frag_capacity) reinterpret_cast<uint2*>(A.frags)[slot] = v;
+    }
+}
+
+// Boundaries of the texel runs in the sorted record keys over positions
+// [0, n]: every position whose key differs from its predecessor, plus 0 and
+// n, so run h is [heads[h], heads[h + 1]).  The invalid-key run is skipped by
+// the fold.
+struct RunHead {
+    const uint32_t* keys;
+    uint32_t n;
+    __device__ bool operator()(uint32_t i) const { return i == 0 || i == n || keys[i - 1] != keys[i]; }
+};
+
+struct SumU2 {
+    __host__ __device__ uint2 operator()(uint2 a, uint2 b) const { return make_uint2(a.x + b.x, a.y + b.y); }
+};
+
+// Sequential per-texel fold of the stably sorted injection records, one
+// thread per texel run.
+//
+// Only the tail of a long run matters.  Every injection record has alpha 1,
+// so a step maps the stored alpha byte a to (a + 1) & 0xff whatever the colour
+// (the store truncates the float sum a + 1 and keeps its low byte): alpha is
+// a step counter mod 256.  A step whose input has alpha 0 computes
+// rgb * 0 + v over 0 + 1, i.e. exactly the record's own value with alpha 1,
+// which is also what it computes from an empty (zero) texel.  So if k* is
+// the last step of the run whose input alpha is 0, the result equals the fold
+// of records k*.. from zero, and a run costs at most 256 serial steps however
+// many records land on its texel (fragments clamped onto region borders pile
+// hundreds of thousands onto single texels).
+__global__ void __launch_bounds__(256) k_inject_fold(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ order,
+                                                     const float4* __restrict__ rgb, const uint32_t* __restrict__ heads,
+                                                     const uint32_t* __restrict__ nheads, uint32_t invalid_key,
+                                                     uint32_t* __restrict__ atlas) {
+    const uint32_t nruns = *nheads - 1u;
+    for (uint32_t h = blockIdx.x * blockDim.x + threadIdx.x; h < nruns; h += gridDim.x * blockDim.x) {
+        const uint32_t s = heads[h], e = heads[h + 1];
+        const uint32_t key = keys[s];
+        if (key == invalid_key) continue;
         uint32_t cell = atlas[key];
-        uint32_t j = i;
-        // the fold is a serial chain per texel; fetch four records ahead of it
-        for (;;) {
-            InjRecord r4[4];
-            bool in[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const uint32_t jj = j + u;
-                in[u] = jj < n && keys[jj] == key;
-                if (in[u]) r4[u] = recs[order[jj]];
-            }
+        const uint32_t len = e - s;
+        const uint32_t k0 = (256u - (cell >> 24)) & 255u;  // first step whose input alpha is 0
+        uint32_t j = s;
+        if (k0 < len) {
+            j = s + k0 + ((len - 1u - k0) & ~255u);  // the last such step
+            cell = 0u;
+        }
+        // the fold is a serial chain; fetch four records ahead of it
+        for (; j < e; j += 4) {
+            float4 r4[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u)
-                if (in[u]) cell = rgba8_avg_fold(cell, r4[u].r, r4[u].g, r4[u].b, 1.0f);
-            if (!in[3]) break;
-            j += 4;
+                if (j + u < e) r4[u] = rgb[order[j + u]];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (j + u < e) cell = rgba8_avg_fold(cell, r4[u].x, r4[u].y, r4[u].z, 1.0f);
         }
         atlas[key] = cell;
     }
 }
 
-__global__ void k_iota(uint32_t* v, uint32_t n) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[i] = i;
-}
-__global__ void k_rec_keys(const InjRecord* r, uint32_t* k, uint32_t n) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) k[i] = r[i].key;
-}
 __global__ void k_fill_f32(float* p, int64_t n, float v) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = v;
 }
@@ -701,6 +790,46 @@ static int plan_tiles(RasterArgs& A, vct_workspace_s* ws, size_t& off, uint32_t*
     VCT_CUDA_TRY(cub::DeviceScan::InclusiveSum(tmp, scan_bytes, counts, *tile_end, (int)n, st));
     VCT_CUDA_TRY(cudaMemcpyAsync(total, *tile_end + (n - 1), 4, cudaMemcpyDeviceToHost, st));
     VCT_CUDA_TRY(cudaStreamSynchronize(st));
+    return VCT_OK;
+}
+
+// Returned (positive) when the workspace had to grow: buffers carved before
+// the growth moved, so the caller restarts its pass from the top.
+constexpr int kWorkspaceGrew = 1;
+
+// Coverage count + exclusive scan of (covered samples, records) per tile for
+// the injection and the SVO pass.  On VCT_OK *offs (in the workspace, `off`
+// advanced past it) holds each tile's first descriptor / record and *nfrag /
+// *nrec the totals (host).
+template <int KIND>
+static int count_tiles(RasterArgs& A, vct_workspace_s* ws, size_t& off, const uint32_t* tile_end, uint32_t total,
+                       uint2** offs, uint32_t* nfrag, uint32_t* nrec, cudaStream_t st) {
+    size_t scan_bytes = 0;
+    VCT_CUDA_TRY(cub::DeviceScan::ExclusiveScan(nullptr, scan_bytes, (uint2*)nullptr, (uint2*)nullptr, SumU2{},
+                                                make_uint2(0u, 0u), (int)total));
+    const size_t need = off + a256(8 * (size_t)total) * 2 + a256(scan_bytes) + 256;
+    if (ws->bytes < need) {
+        int rc = workspace_reserve(ws, need);
+        return rc != VCT_OK ? rc : kWorkspaceGrew;
+    }
+    char* base = (char*)ws->ptr + off;
+    uint2* counts = (uint2*)base;
+    *offs = (uint2*)(base + a256(8 * (size_t)total));
+    void* tmp = base + 2 * a256(8 * (size_t)total);
+    off += 2 * a256(8 * (size_t)total) + a256(scan_bytes);
+    k_raster_tiles<KIND, P_COUNT><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, counts, nullptr, nullptr, nullptr);
+    VCT_LAUNCH_CHECK();
+    VCT_CUDA_TRY(cub::DeviceScan::ExclusiveScan(tmp, scan_bytes, counts, *offs, SumU2{}, make_uint2(0u, 0u), (int)total, st));
+    uint2 last[2];
+    VCT_CUDA_TRY(cudaMemcpyAsync(&last[0], *offs + (total - 1), 8, cudaMemcpyDeviceToHost, st));
+    VCT_CUDA_TRY(cudaMemcpyAsync(&last[1], counts + (total - 1), 8, cudaMemcpyDeviceToHost, st));
+    VCT_CUDA_TRY(cudaStreamSynchronize(st));
+    const uint64_t f = (uint64_t)last[0].x + last[1].x, r = (uint64_t)last[0].y + last[1].y;
+    // the per-tile sums are 32-bit: a wrapped total shows as fewer records than fragments
+    if (f >= (1ull << 31) || r >= (1ull << 31) || r < f)
+        return fail(VCT_E_OVERFLOW, "rasteriser: more than 2^31 covered samples or records in one pass");
+    *nfrag = (uint32_t)f;
+    *nrec = (uint32_t)r;
     return VCT_OK;
 }
 
@@ -898,59 +1027,49 @@ extern "C" int vct_inject_radiance(const vct_scene* scene, const vct_clipmap_reg
         if (herr) return fail(VCT_E_TIMEOUT, "vct_inject_radiance: a CAS loop gave up after 2^20 retries");
         return VCT_OK;
     }
-    // deterministic: count -> scan -> write records -> stable sort by texel -> fold
-    size_t scan_bytes = 0;
-    VCT_CUDA_TRY(cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, (uint32_t*)nullptr, (uint32_t*)nullptr, (int)total));
-    const size_t head = off;
-    size_t need = head + a256(4 * (size_t)total) * 2 + a256(scan_bytes) + 256;
-    // keep tile_end valid across a possible growth: grow first, then recount
-    if (ws->bytes < need) {
-        rc = workspace_reserve(ws, need);
-        if (rc != VCT_OK) return rc;
-        rc = plan_tiles(A, ws, off, &tile_end, &total, st);
-        if (rc != VCT_OK) return rc;
-    }
-    char* base = (char*)ws->ptr;
-    uint32_t* counts = (uint32_t*)(base + head);
-    uint32_t* offs = (uint32_t*)(base + head + a256(4 * (size_t)total));
-    void* tmp = base + head + 2 * a256(4 * (size_t)total);
-    k_raster_tiles<K_INJECT, P_COUNT><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, counts, nullptr, nullptr, nullptr);
-    VCT_LAUNCH_CHECK();
-    VCT_CUDA_TRY(cub::DeviceScan::ExclusiveSum(tmp, scan_bytes, counts, offs, (int)total, st));
-    uint32_t last[2];
-    VCT_CUDA_TRY(cudaMemcpyAsync(&last[0], offs + (total - 1), 4, cudaMemcpyDeviceToHost, st));
-    VCT_CUDA_TRY(cudaMemcpyAsync(&last[1], counts + (total - 1), 4, cudaMemcpyDeviceToHost, st));
-    VCT_CUDA_TRY(cudaStreamSynchronize(st));
-    const uint64_t nrec64 = (uint64_t)last[0] + last[1];
-    if (nrec64 == 0) return VCT_OK;
-    if (nrec64 >= (1ull << 31)) return fail(VCT_E_OVERFLOW, "vct_inject_radiance: more than 2^31 face updates");
-    const uint32_t nrec = (uint32_t)nrec64;
-    size_t sort_bytes = 0;
+    // deterministic: count -> scan -> emit covered samples -> shade into records
+    // -> stable sort by texel -> fold each texel's run in traversal order
+    uint2* offs;
+    uint32_t nfrag, nrec;
+    rc = count_tiles<K_INJECT>(A, ws, off, tile_end, total, &offs, &nfrag, &nrec, st);
+    if (rc == kWorkspaceGrew)
+        return vct_inject_radiance(scene, regions, R, shadow, light, light_shadow, atlas, level_mask, mode, ws, stream);
+    if (rc != VCT_OK) return rc;
+    if (nfrag == 0) return VCT_OK;
+    const int key_bits = 32 - __builtin_clz((unsigned)A.invalid_key);
+    size_t sort_bytes = 0, select_bytes = 0;
     VCT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(nullptr, sort_bytes, (uint32_t*)nullptr, (uint32_t*)nullptr,
-                                                 (uint32_t*)nullptr, (uint32_t*)nullptr, (int)nrec, 0, 32));
-    const size_t rec_off = head + a256(4 * (size_t)total) * 2 + a256(scan_bytes);
-    need = rec_off + a256(sizeof(InjRecord) * nrec) + 4 * a256(4 * (size_t)nrec) + a256(sort_bytes) + 256;
+                                                 (uint32_t*)nullptr, (uint32_t*)nullptr, (int)nrec, 0, key_bits));
+    VCT_CUDA_TRY(cub::DeviceSelect::If(nullptr, select_bytes, thrust::counting_iterator<uint32_t>(0u), (uint32_t*)nullptr,
+                                       (uint32_t*)nullptr, (int64_t)nrec + 1, RunHead{nullptr, nrec}));
+    const size_t r4 = a256(4 * (size_t)nrec + 4);
+    const size_t need = off + a256(sizeof(FragDesc) * (size_t)nfrag) + a256(16 * (size_t)nrec) + 5 * r4 + 256 +
+                        a256(sort_bytes > select_bytes ? sort_bytes : select_bytes);
     if (ws->bytes < need) {
-        // grow and redo the counting passes (their buffers move with the arena)
         rc = workspace_reserve(ws, need);
         if (rc != VCT_OK) return rc;
         return vct_inject_radiance(scene, regions, R, shadow, light, light_shadow, atlas, level_mask, mode, ws, stream);
     }
-    base = (char*)ws->ptr;
-    InjRecord* recs = (InjRecord*)(base + rec_off);
-    uint32_t* kin = (uint32_t*)(base + rec_off + a256(sizeof(InjRecord) * nrec));
-    uint32_t* kout = kin + a256(4 * (size_t)nrec) / 4;
-    uint32_t* vin = kout + a256(4 * (size_t)nrec) / 4;
-    uint32_t* vout = vin + a256(4 * (size_t)nrec) / 4;
-    void* stmp = (char*)(vout + a256(4 * (size_t)nrec) / 4);
-    k_raster_tiles<K_INJECT, P_WRITE><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, nullptr, offs, recs, nullptr);
+    char* p = (char*)ws->ptr + off;
+    FragDesc* fr = (FragDesc*)p;
+    p += a256(sizeof(FragDesc) * (size_t)nfrag);
+    float4* rgb = (float4*)p;
+    p += a256(16 * (size_t)nrec);
+    uint32_t* kin = (uint32_t*)p;
+    uint32_t* kout = (uint32_t*)(p + r4);
+    uint32_t* vin = (uint32_t*)(p + 2 * r4);
+    uint32_t* vout = (uint32_t*)(p + 3 * r4);
+    uint32_t* heads = (uint32_t*)(p + 4 * r4);
+    uint32_t* nheads = (uint32_t*)(p + 5 * r4);
+    void* stmp = p + 5 * r4 + 256;
+    k_raster_tiles<K_INJECT, P_WRITE><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, nullptr, offs, fr, nullptr);
     VCT_LAUNCH_CHECK();
-    k_rec_keys<<<grid_of(nrec, 256), 256, 0, st>>>(recs, kin, nrec);
-    k_iota<<<grid_of(nrec, 256), 256, 0, st>>>(vin, nrec);
+    k_inject_shade<<<grid_of(nfrag, 256), 256, 0, st>>>(A, fr, nfrag, kin, vin, rgb);
     VCT_LAUNCH_CHECK();
-    const int key_bits = 32 - __builtin_clz((unsigned)A.invalid_key);
     VCT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(stmp, sort_bytes, kin, kout, vin, vout, (int)nrec, 0, key_bits, st));
-    k_inject_fold<<<grid_of(nrec, 256), 256, 0, st>>>(kout, vout, recs, nrec, A.invalid_key, atlas);
+    VCT_CUDA_TRY(cub::DeviceSelect::If(stmp, select_bytes, thrust::counting_iterator<uint32_t>(0u), heads, nheads,
+                                       (int64_t)nrec + 1, RunHead{kout, nrec}, st));
+    k_inject_fold<<<grid_of(nrec, 256), 256, 0, st>>>(kout, vout, rgb, heads, nheads, A.invalid_key, atlas);
     VCT_LAUNCH_CHECK();
     return VCT_OK;
 }
@@ -994,33 +1113,30 @@ extern "C" int vct_svo_fragments(const vct_scene* scene, int32_t octree_level, c
     rc = plan_tiles(A, ws, off, &tile_end, &total, st);
     if (rc != VCT_OK) return rc;
     if (total == 0) return VCT_OK;
-    size_t scan_bytes = 0;
-    VCT_CUDA_TRY(cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, (uint32_t*)nullptr, (uint32_t*)nullptr, (int)total));
-    const size_t need = off + a256(4 * (size_t)total) * 2 + a256(scan_bytes) + 256;
+    // count pass (SparseVoxelizer::preVoxelize), host readback of the count
+    uint2* offs;
+    uint32_t nfrag, nslot;
+    rc = count_tiles<K_SVO>(A, ws, off, tile_end, total, &offs, &nfrag, &nslot, st);
+    if (rc == kWorkspaceGrew)
+        return vct_svo_fragments(scene, octree_level, bb_min, bb_max, shadow, light, light_shadow, frags, capacity,
+                                 count, ws, stream);
+    if (rc != VCT_OK) return rc;
+    *count = (int64_t)nslot;
+    if (capacity == 0 || nfrag == 0) return VCT_OK;  // count-only call
+    if (*count > capacity) return fail(VCT_E_OVERFLOW, "vct_svo_fragments: fragment list capacity too small");
+    const size_t need = off + a256(sizeof(FragDesc) * (size_t)nfrag) + 256;
     if (ws->bytes < need) {
         rc = workspace_reserve(ws, need);
         if (rc != VCT_OK) return rc;
         return vct_svo_fragments(scene, octree_level, bb_min, bb_max, shadow, light, light_shadow, frags, capacity,
                                  count, ws, stream);
     }
-    char* base = (char*)ws->ptr;
-    uint32_t* counts = (uint32_t*)(base + off);
-    uint32_t* offs = (uint32_t*)(base + off + a256(4 * (size_t)total));
-    void* tmp = base + off + 2 * a256(4 * (size_t)total);
-    // count pass (SparseVoxelizer::preVoxelize), host readback of the count
-    k_raster_tiles<K_SVO, P_COUNT><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, counts, nullptr, nullptr, nullptr);
-    VCT_LAUNCH_CHECK();
-    VCT_CUDA_TRY(cub::DeviceScan::ExclusiveSum(tmp, scan_bytes, counts, offs, (int)total, st));
-    uint32_t last[2];
-    VCT_CUDA_TRY(cudaMemcpyAsync(&last[0], offs + (total - 1), 4, cudaMemcpyDeviceToHost, st));
-    VCT_CUDA_TRY(cudaMemcpyAsync(&last[1], counts + (total - 1), 4, cudaMemcpyDeviceToHost, st));
-    VCT_CUDA_TRY(cudaStreamSynchronize(st));
-    *count = (int64_t)last[0] + last[1];
-    if (capacity == 0) return VCT_OK;  // count-only call
-    if (*count > capacity) return fail(VCT_E_OVERFLOW, "vct_svo_fragments: fragment list capacity too small");
+    FragDesc* fr = (FragDesc*)((char*)ws->ptr + off);
     // write pass (SparseVoxelizer::cmdVoxelize); discarded slots stay zero
     VCT_CUDA_TRY(cudaMemsetAsync(frags, 0, sizeof(uint32_t) * 2 * (size_t)*count, st));
-    k_raster_tiles<K_SVO, P_WRITE><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, nullptr, offs, nullptr, nullptr);
+    k_raster_tiles<K_SVO, P_WRITE><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, nullptr, offs, fr, nullptr);
+    VCT_LAUNCH_CHECK();
+    k_svo_shade<<<grid_of(nfrag, 256), 256, 0, st>>>(A, fr, nfrag);
     VCT_LAUNCH_CHECK();
     return VCT_OK;
 }

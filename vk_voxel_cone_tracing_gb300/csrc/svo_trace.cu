@@ -50,8 +50,7 @@ __device__ inline float4 sample_svo(const SvoScene& S, const vct_cone_tracing_de
         fp[2] -= cz * resolution;
     } while (cur != 0u && resolution > target);
     const uint32_t v = __ldg(&S.pool[idx].y);
-    return make_float4((float)(v & 0xffu) / 255.0f, (float)((v >> 8) & 0xffu) / 255.0f,
-                       (float)((v >> 16) & 0xffu) / 255.0f, (float)(v >> 24) / 255.0f);
+    return unpack_rgba8(v);
 }
 
 __device__ float4 svo_trace_cone(const SvoScene& S, const vct_cone_tracing_desc& d, float3 start, float3 dir,
