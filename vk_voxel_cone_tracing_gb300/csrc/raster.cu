@@ -12,10 +12,11 @@
 // float(e_i) * (1 / float(area)), the fragment shader at every covered sample.
 //
 // Work decomposition: one item per (triangle, clip level); each item's
-// bounding box is cut into 8x8-pixel tiles; one thread walks one tile (pixels
-// row-major, samples in index order).  Items' tile counts are prefix-summed
-// and the tile kernel finds its item by binary search, so no per-tile list is
-// materialised.  Order-dependent passes (RGBA8 running averages, the SVO
+// bounding box is cut into 8x8-pixel tiles (pixels row-major, samples in index
+// order).  Items' tile counts are prefix-summed and a warp sets up 32 tiles
+// (found by binary search, so no per-tile list is materialised) and then
+// walks their pixels as one flattened list, a pixel per lane (k_cover).
+// Order-dependent passes (RGBA8 running averages, the SVO
 // fragment list) use a coverage count pass + prefix sum + an emit pass that
 // writes one compact descriptor per covered sample in traversal order (item,
 // tile, pixel, sample); a shading kernel then runs one thread per covered
@@ -283,29 +284,6 @@ __device__ inline float3 interp3(const float b[3], const float3 v[3]) {
                        (b[0] * v[0].z + b[1] * v[1].z) + b[2] * v[2].z);
 }
 
-// Walk tile `t` of a set-up triangle in the pinned order.
-template <class F>
-__device__ inline void raster_tile(const RSetup& r, uint32_t t, int nsamples, F&& frag) {
-    const int tw = ((r.px1 - r.px0) >> 3) + 1;
-    const int tx = r.px0 + 8 * (int)(t % (uint32_t)tw), ty = r.py0 + 8 * (int)(t / (uint32_t)tw);
-    const int xe = min(tx + 7, r.px1), ye = min(ty + 7, r.py1);
-    for (int py = ty; py <= ye; ++py)
-        for (int px = tx; px <= xe; ++px)
-            for (int s = 0; s < nsamples; ++s) {
-                long long sx, sy;
-                if (nsamples == 1) {
-                    sx = (long long)px * 256 + 128;
-                    sy = (long long)py * 256 + 128;
-                } else {
-                    sx = (long long)px * 256 + c_sample_loc8[s][0];
-                    sy = (long long)py * 256 + c_sample_loc8[s][1];
-                }
-                float b[3];
-                float z;
-                if (raster_test(r, sx, sy, b, z)) frag(px, py, b, z);
-            }
-}
-
 // ------------------------------------------------------------ pass params
 enum Kind { K_OPACITY = 0, K_INJECT = 1, K_SHADOW = 2, K_SVO = 3 };
 enum Phase { P_DIRECT = 0, P_COUNT = 1, P_WRITE = 2 };
@@ -334,9 +312,13 @@ struct RasterArgs {
     uint32_t invalid_key;  // injection record key that sorts past every texel
 };
 
+// Items are numbered triangle-major (item = tri * nlevels + level index) and
+// stay below 2^31, so 32-bit arithmetic suffices.
 __device__ inline void item_of(const RasterArgs& A, int64_t item, int64_t& tri, int& lvl) {
-    tri = item / A.nlevels;
-    lvl = A.levels[item % A.nlevels];
+    const uint32_t it = (uint32_t)item, nl = (uint32_t)A.nlevels;
+    const uint32_t t = nl == 1u ? it : it / nl;
+    tri = t;
+    lvl = A.levels[it - t * nl];
 }
 
 // Clip-space vertices of item (tri, level) for the pass.
@@ -380,7 +362,7 @@ __device__ inline int3 clip_image_coords(const vct_voxelization_desc& d, float3 
     for (int a = 0; a < 3; ++a) {
         float q = p[a] / d.clip_max_extent;
         float f = q - floorf(q);
-        ic[a] = ((int)(f * (float)R)) % R;
+        ic[a] = ((int)(f * (float)R)) & (R - 1);  // f >= 0 and R a power of two: the value % R
     }
     return make_int3(ic[0] + 1, ic[1] + 1 + (R + 2) * (int)d.clip_level, ic[2] + 1);
 }
@@ -521,6 +503,20 @@ __device__ inline int svo_fragment(const RasterArgs& A, const vct_gltf_shade_mat
 }
 
 // ---------------------------------------------------------------- kernels
+struct TilePlan {
+    const uint32_t* tile_end;   // inclusive prefix of the items' tile counts
+    const uint32_t* tile_item;  // item of every tile
+    uint32_t total;             // tiles
+};
+
+// Item of every tile: item i owns tiles [tile_end[i-1], tile_end[i]).
+__global__ void k_tile_items(const uint32_t* __restrict__ tile_end, int64_t items, uint32_t* __restrict__ tile_item) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < items; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t b = i > 0 ? tile_end[i - 1] : 0u, e = tile_end[i];
+        for (uint32_t g = b; g < e; ++g) tile_item[g] = (uint32_t)i;
+    }
+}
+
 __global__ void k_item_tiles(const __grid_constant__ RasterArgs A, uint32_t* __restrict__ tiles) {
     for (int64_t item = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; item < A.items;
          item += (int64_t)gridDim.x * blockDim.x) {
@@ -558,83 +554,339 @@ __device__ inline uint32_t inject_per_fragment(const vct_gltf_shade_material& ma
     return emissive ? 6u : 3u;
 }
 
-// Tile kernels.  A thread takes one 8x8 pixel tile of one (triangle, level)
-// item, found by binary search over the inclusive tile sums.  P_DIRECT writes
-// the pass's output directly (opacity, shadow depth, atomic injection);
-// P_COUNT counts covered samples and their records per tile (injection, SVO);
-// P_WRITE emits the FragDesc of each covered sample at its scanned position.
-template <int KIND, int PHASE>
-__global__ void __launch_bounds__(128) k_raster_tiles(const __grid_constant__ RasterArgs A, const uint32_t* __restrict__ tile_end,
-                                                      uint2* __restrict__ counts, const uint2* __restrict__ offs,
-                                                      FragDesc* __restrict__ frags, int* __restrict__ err) {
-    const uint32_t total = A.items > 0 ? tile_end[A.items - 1] : 0u;
-    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
-        int64_t lo = 0, hi = A.items - 1;  // first item with tile_end > g
-        while (lo < hi) {
-            const int64_t mid = (lo + hi) >> 1;
-            if (tile_end[mid] > g) hi = mid;
-            else lo = mid + 1;
-        }
-        const int64_t item = lo;
-        const uint32_t local = g - (item > 0 ? tile_end[item - 1] : 0u);
-        int64_t tri;
-        int lvl;
-        item_of(A, item, tri, lvl);
-        const WTri w = world_triangle(A.s, tri);
-        RSetup rs;
-        float3 pos[3];
-        const bool ok = item_setup(A, w, lvl, rs, pos);
-        const vct_gltf_shade_material mat = material_of(A.s, w.material);
-        if (KIND == K_OPACITY) {
-            if (!ok) continue;
-            const vct_voxelization_desc& d = A.vd[lvl];
-            const AtlasDims AD(A.R);
-            raster_tile(rs, local, 8, [&](int, int, const float* b, float) {
-                const float3 wp = interp3(b, w.p);
-                if (wp.x < d.region_min_corner[0] || wp.y < d.region_min_corner[1] || wp.z < d.region_min_corner[2] ||
-                    wp.x > d.region_max_corner[0] || wp.y > d.region_max_corner[1] || wp.z > d.region_max_corner[2])
-                    return;
-                if (item_discarded(A, mat)) return;
-                const int3 ic = clip_image_coords(d, wp);
-                for (int f = 0; f < 6; ++f) A.atlas[AD.index(ic.x + (A.R + 2) * f, ic.y, ic.z)] = 0xFFFFFFFFu;
-            });
-        } else if (KIND == K_SHADOW) {
-            if (!ok) continue;
-            raster_tile(rs, local, 1, [&](int px, int py, const float*, float z) {
-                atomicMin(reinterpret_cast<unsigned int*>(A.depth) + (int64_t)py * A.W + px, __float_as_uint(z));
-            });
-        } else if (PHASE == P_DIRECT) {  // atomic injection: shade and fold in place
-            if (!ok || item_discarded(A, mat)) continue;
-            raster_tile(rs, local, 8, [&](int, int, const float* b, float) {
-                InjRecord upd[6];
-                const int k = inject_fragment(A, mat, lvl, interp3(b, w.p), interp3(b, w.n), upd);
-                for (int i = 0; i < k; ++i) rgba8_avg_atomic(A.atlas + upd[i].key, upd[i].r, upd[i].g, upd[i].b, 1.0f, err);
-            });
-        } else {
-            // Injection: every covered sample owns 3 face records (6 for emissive
-            // materials); SVO: one fragment-list slot.  Occlusion-discarded
-            // items own nothing (the reference discards before its counter).
-            const bool live = ok && !item_discarded(A, mat);
-            const uint32_t per = KIND == K_INJECT ? inject_per_fragment(mat) : 1u;
-            uint32_t n = 0;
-            if (PHASE == P_COUNT) {
-                if (live) raster_tile(rs, local, 8, [&](int, int, const float*, float) { ++n; });
-                counts[g] = make_uint2(n, n * per);
-            } else if (live) {
-                const uint2 base = offs[g];
-                const uint32_t meta = (uint32_t)lvl | (min(w.material, (uint32_t)max(A.s.material_count - 1, 0)) << 3);
-                raster_tile(rs, local, 8, [&](int, int, const float* b, float) {
-                    const float3 p = KIND == K_INJECT ? interp3(b, w.p) : interp3(b, pos);
-                    const float3 nn = interp3(b, w.n);
-                    FragDesc d;
-                    d.p = make_float4(p.x, p.y, p.z, __uint_as_float(base.y + n * per));
-                    d.n = make_float4(nn.x, nn.y, nn.z, __uint_as_float(meta));
-                    frags[base.x + n] = d;
-                    ++n;
-                });
-            }
+// 8x MSAA standard sample positions in 1/256 pixel (the c_sample_loc8 table
+// as constant expressions, so unrolled sample loops fold them).
+__host__ __device__ constexpr int sample_x(int s) {
+    return s == 0 ? 144 : s == 1 ? 112 : s == 2 ? 208 : s == 3 ? 80 : s == 4 ? 48 : s == 5 ? 16 : s == 6 ? 176 : 240;
+}
+__host__ __device__ constexpr int sample_y(int s) {
+    return s == 0 ? 80 : s == 1 ? 176 : s == 2 ? 144 : s == 3 ? 48 : s == 4 ? 208 : s == 5 ? 112 : s == 6 ? 240 : 16;
+}
+
+// The set-up triangle of one tile in the form the per-pixel tests use.  Edge
+// i runs from vertex a = (i+1)%3 to c = (i+2)%3 and
+//   e_i(x, y) = dX_i * (y - Y_a) - dY_i * (x - X_a)        (1/256-pixel units),
+// raster_test's edge function.  The tile keeps E_i = e_i at its corner
+// (tx * 256, ty * 256); a sample at offset (ox, oy) from that corner has
+// e_i = E_i + dX_i * oy - dY_i * ox, the same int64 value (equal modulo 2^64
+// even where a product wrapped).
+//   small: every |dX_i|, |dY_i| < 2^17.  A sample of the tile is then within
+//          Mt_i = (|dX_i| + |dY_i|) * 2032 < 2^29 of E_i (offsets < 7 * 256 +
+//          240), so an edge with E_i > Mt_i passes every sample of the tile,
+//          E_i < -Mt_i empties the tile, and the others run in 32 bits;
+//   zsafe: every vertex depth lies in [0, 1 - 2^-20].  The interpolated depth
+//          of a covered sample is then inside the [0, 1] clip: its weights
+//          are >= 0 and sum to at most (1 + 2^-24)^3 (area = sum of e_i, three
+//          roundings each) and the five roundings of the dot product add at
+//          most a factor (1 + 2^-24)^3, so z <= (1 + 2^-24)^6 (1 - 2^-20) < 1.
+struct TileRegs {
+    long long E[3];     // e_i at the tile corner
+    int dX[3], dY[3];   // small tiles: the edge deltas
+    float z[3], inv_area;
+    uint32_t flags;     // bits 0-2: edge i owns its ties; 3: vertices 1 and 2 swapped;
+                        // 4: small; 5: zsafe; 6-8: edge i passes every sample of the tile
+};
+
+// Per-tile state that the lanes of one warp share: one slot per lane's tile.
+struct TileSlot {
+    TileRegs t;                // the set-up triangle, ready for the per-pixel tests
+    long long dXl[3], dYl[3];  // the edge deltas in 64 bits (tiles that are not small)
+    int tx, ty, tw;            // tile origin and clipped width in pixels
+    uint32_t tw_magic;         // ceil(2^32 / tw) (tw > 1): n / tw = umulhi(n, tw_magic) for n < 64
+    uint32_t px_end;           // inclusive prefix of the warp's tile pixel counts
+    uint32_t done;             // covered samples of this tile met in earlier rounds
+    uint32_t base_f, base_r, per, meta;
+    float3 p[3], n[3];         // interpolation sources (position, normal)
+};
+
+// Fills the slot's test state for tile (tx, ty); returns false if an edge
+// rejects every sample of the tile.
+__device__ inline bool tile_regs(const RSetup& rs, int tx, int ty, TileSlot& T) {
+    TileRegs& t = T.t;
+    bool small = true;
+    long long Mt[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const int a = (i + 1) % 3, c = (i + 2) % 3;
+        const long long dX = rs.X[c] - rs.X[a], dY = rs.Y[c] - rs.Y[a];
+        T.dXl[i] = dX;
+        T.dYl[i] = dY;
+        t.E[i] = dX * ((long long)ty * 256 - rs.Y[a]) - dY * ((long long)tx * 256 - rs.X[a]);
+        const bool si = dX > -(1LL << 17) && dX < (1LL << 17) && dY > -(1LL << 17) && dY < (1LL << 17);
+        small = small && si;
+        t.dX[i] = (int)dX;  // meaningful only when small
+        t.dY[i] = (int)dY;
+        Mt[i] = si ? (llabs(dX) + llabs(dY)) * 2032 : 0;
+        t.z[i] = rs.z[i];
+    }
+    uint32_t flags = (uint32_t)rs.owned | (rs.swapped ? 8u : 0u);
+    if (small) {
+        flags |= 16u;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            if (t.E[i] < -Mt[i]) return false;
+            if (t.E[i] > Mt[i]) flags |= 64u << i;
         }
     }
+    const float zhi = 0.99999904632568359375f;  // 1 - 2^-20
+    if (rs.z[0] >= 0.0f && rs.z[1] >= 0.0f && rs.z[2] >= 0.0f && rs.z[0] <= zhi && rs.z[1] <= zhi && rs.z[2] <= zhi)
+        flags |= 32u;
+    t.flags = flags;
+    t.inv_area = rs.inv_area;
+    return true;
+}
+
+// Barycentrics and depth of the sample at offset (ox, oy) from the tile
+// corner -- raster_test's arithmetic.
+__device__ inline void sample_bz(const TileRegs& t, const TileSlot& T, int ox, int oy, float b[3], float& z) {
+    float bo[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const long long e = (t.flags & 16u) ? t.E[i] + (long long)(t.dX[i] * oy - t.dY[i] * ox)
+                                            : t.E[i] + (T.dXl[i] * oy - T.dYl[i] * ox);
+        bo[i] = (float)e * t.inv_area;
+    }
+    z = (bo[0] * t.z[0] + bo[1] * t.z[1]) + bo[2] * t.z[2];
+    b[0] = bo[0];
+    b[1] = (t.flags & 8u) ? bo[2] : bo[1];
+    b[2] = (t.flags & 8u) ? bo[1] : bo[2];
+}
+
+// Coverage mask of the NS samples of the pixel at offset (ox0, oy0) from the
+// tile corner (bit s: sample s covered and inside the depth clip).
+template <int NS>
+__device__ inline uint32_t cover_pixel(const TileRegs& t, const TileSlot& T, int ox0, int oy0) {
+    uint32_t mask = 0;
+    if (t.flags & 16u) {
+        int base[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) base[i] = (int)t.E[i] + (t.dX[i] * oy0 - t.dY[i] * ox0);
+#pragma unroll
+        for (int s = 0; s < NS; ++s) {
+            const int ox = NS == 1 ? 128 : sample_x(s), oy = NS == 1 ? 128 : sample_y(s);
+            bool cov = true;
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                if (!((t.flags >> (6 + i)) & 1u)) {
+                    const int e = base[i] + (t.dX[i] * oy - t.dY[i] * ox);
+                    cov = cov && (e > 0 || (e == 0 && ((t.flags >> i) & 1u)));
+                }
+            }
+            if (cov && !(t.flags & 32u)) {
+                float b[3], z;
+                sample_bz(t, T, ox0 + ox, oy0 + oy, b, z);
+                cov = z >= 0.0f && z <= 1.0f;
+            }
+            mask |= (uint32_t)cov << s;
+        }
+    } else {
+#pragma unroll 1
+        for (int s = 0; s < NS; ++s) {
+            const int ox = ox0 + (NS == 1 ? 128 : c_sample_loc8[s][0]), oy = oy0 + (NS == 1 ? 128 : c_sample_loc8[s][1]);
+            bool cov = true;
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                const long long e = t.E[i] + (T.dXl[i] * oy - T.dYl[i] * ox);
+                cov = cov && (e > 0 || (e == 0 && ((t.flags >> i) & 1u)));
+            }
+            if (cov) {
+                float b[3], z;
+                sample_bz(t, T, ox, oy, b, z);
+                cov = z >= 0.0f && z <= 1.0f;
+            }
+            mask |= (uint32_t)cov << s;
+        }
+    }
+    return mask;
+}
+
+// Coverage kernels.  A warp takes 32 consecutive 8x8 tiles of (triangle,
+// level) items -- one per lane -- sets each up once into shared memory, then
+// flattens the (tile, pixel) pairs of all 32 tiles and walks them 32 at a
+// time, one pixel (all of its samples) per lane, so every lane does the same
+// work however unequal the tiles are.  Pixel q of the flattened list belongs
+// to the first tile whose inclusive pixel sum exceeds q; within a tile pixels
+// are row-major, so the list is in traversal order (item, tile, pixel, sample).
+//   P_DIRECT writes the pass's output (opacity, shadow depth, atomic injection);
+//   P_COUNT counts covered samples and their records per tile;
+//   P_WRITE emits one FragDesc per covered sample at its rank within the tile
+//   (earlier rounds' count + a warp scan over the lanes of the same tile).
+// A tile's item comes from the tile plan's tile -> item array.
+template <int KIND, int PHASE>
+__global__ void __launch_bounds__(128) k_cover(const __grid_constant__ RasterArgs A, const TilePlan plan,
+                                               uint2* __restrict__ counts, const uint2* __restrict__ offs,
+                                               FragDesc* __restrict__ frags, int* __restrict__ err) {
+    constexpr int NS = KIND == K_SHADOW ? 1 : 8;
+    constexpr bool RANKED = PHASE != P_DIRECT;
+    constexpr unsigned FULL = 0xffffffffu;
+    __shared__ TileSlot slots[4][32];
+    const int lane = threadIdx.x & 31;
+    TileSlot* S = slots[threadIdx.x >> 5];
+    const uint32_t* __restrict__ tile_end = plan.tile_end;
+    const uint32_t total = plan.total;
+    const uint32_t nchunks = (total + 31u) >> 5;
+    for (uint32_t ch = blockIdx.x * 4u + (threadIdx.x >> 5); ch < nchunks; ch += gridDim.x * 4u) {
+        const uint32_t g = ch * 32u + lane;
+        uint32_t npx = 0;
+        if (g < total) {
+            const int64_t item = plan.tile_item[g];
+            const uint32_t local = g - (item > 0 ? tile_end[item - 1] : 0u);
+            int64_t tri;
+            int lvl;
+            item_of(A, item, tri, lvl);
+            const WTri w = world_triangle(A.s, tri);
+            RSetup rs;
+            float3 pos[3];
+            bool live = item_setup(A, w, lvl, rs, pos);
+            const uint32_t mi = min(w.material, (uint32_t)max(A.s.material_count - 1, 0));
+            uint32_t per = 1u;
+            if (KIND != K_SHADOW) {
+                const vct_gltf_shade_material mat = material_of(A.s, mi);
+                live = live && !item_discarded(A, mat);
+                if (KIND == K_INJECT) per = inject_per_fragment(mat);
+            }
+            TileSlot& T = S[lane];
+            T.per = per;
+            if (live) {
+                const int tcols = ((rs.px1 - rs.px0) >> 3) + 1;
+                const int tx = rs.px0 + 8 * (int)(local % (uint32_t)tcols), ty = rs.py0 + 8 * (int)(local / (uint32_t)tcols);
+                const int tw = min(tx + 7, rs.px1) - tx + 1, th = min(ty + 7, rs.py1) - ty + 1;
+                npx = tile_regs(rs, tx, ty, T) ? (uint32_t)(tw * th) : 0u;
+                T.tx = tx;
+                T.ty = ty;
+                T.tw = tw;
+                T.tw_magic = tw > 1 ? (uint32_t)(0xffffffffu / (uint32_t)tw) + 1u : 0u;
+                T.meta = (uint32_t)lvl | (mi << 3);
+                if (KIND != K_SHADOW) {
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        T.p[k] = KIND == K_SVO ? pos[k] : w.p[k];
+                        T.n[k] = w.n[k];
+                    }
+                }
+                if (PHASE == P_WRITE) {
+                    const uint2 b = offs[g];
+                    T.base_f = b.x;
+                    T.base_r = b.y;
+                }
+            }
+        }
+        // ---- flattened pixel list of the warp's tiles
+        uint32_t incl = npx;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t v = __shfl_up_sync(FULL, incl, d);
+            if (lane >= d) incl += v;
+        }
+        S[lane].px_end = incl;
+        S[lane].done = 0u;
+        const uint32_t P = __shfl_sync(FULL, incl, 31);
+        __syncwarp();
+        TileRegs t;
+        int cj = -1;
+        for (uint32_t q0 = 0; q0 < P; q0 += 32u) {
+            const uint32_t q = q0 + lane;
+            const bool act = q < P;
+            int j = 0;
+            uint32_t start = 0, mask = 0;
+            int px = 0, py = 0, ox0 = 0, oy0 = 0;
+            if (act) {
+                int lo = 0, hi = 31;
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (S[mid].px_end > q) hi = mid;
+                    else lo = mid + 1;
+                }
+                j = lo;
+                start = j > 0 ? S[j - 1].px_end : 0u;
+                if (j != cj) {
+                    t = S[j].t;
+                    cj = j;
+                }
+                const uint32_t lp = q - start, tw = (uint32_t)S[j].tw;
+                const uint32_t row = tw > 1u ? __umulhi(lp, S[j].tw_magic) : lp;
+                ox0 = (int)(lp - row * tw) * 256;
+                oy0 = (int)row * 256;
+                px = S[j].tx + (ox0 >> 8);
+                py = S[j].ty + (oy0 >> 8);
+                mask = cover_pixel<NS>(t, S[j], ox0, oy0);
+                if (PHASE == P_DIRECT && mask) {
+                    const TileSlot& T = S[j];
+                    const int lvl = (int)(T.meta & 7u);
+                    for (uint32_t m = mask; m; m &= m - 1u) {
+                        const int s = __ffs(m) - 1;
+                        float b[3], z;
+                        sample_bz(t, T, ox0 + (NS == 1 ? 128 : c_sample_loc8[s][0]),
+                                  oy0 + (NS == 1 ? 128 : c_sample_loc8[s][1]), b, z);
+                        if (KIND == K_SHADOW) {
+                            atomicMin(reinterpret_cast<unsigned int*>(A.depth) + (int64_t)py * A.W + px, __float_as_uint(z));
+                        } else if (KIND == K_OPACITY) {
+                            const vct_voxelization_desc& d = A.vd[lvl];
+                            const float3 wp = interp3(b, T.p);
+                            if (wp.x < d.region_min_corner[0] || wp.y < d.region_min_corner[1] ||
+                                wp.z < d.region_min_corner[2] || wp.x > d.region_max_corner[0] ||
+                                wp.y > d.region_max_corner[1] || wp.z > d.region_max_corner[2])
+                                continue;
+                            const AtlasDims AD(A.R);
+                            const int3 ic = clip_image_coords(d, wp);
+                            for (int f = 0; f < 6; ++f) A.atlas[AD.index(ic.x + (A.R + 2) * f, ic.y, ic.z)] = 0xFFFFFFFFu;
+                        } else if (KIND == K_INJECT) {
+                            const vct_gltf_shade_material mat = material_of(A.s, T.meta >> 3);
+                            InjRecord upd[6];
+                            const int k = inject_fragment(A, mat, lvl, interp3(b, T.p), interp3(b, T.n), upd);
+                            for (int i = 0; i < k; ++i)
+                                rgba8_avg_atomic(A.atlas + upd[i].key, upd[i].r, upd[i].g, upd[i].b, 1.0f, err);
+                        }
+                    }
+                }
+            }
+            if (RANKED) {
+                const uint32_t c = __popc(mask);
+                uint32_t ci = c;
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+                    const uint32_t v = __shfl_up_sync(FULL, ci, d);
+                    if (lane >= d) ci += v;
+                }
+                const uint32_t cx = ci - c;
+                const int first = (act && start > q0) ? (int)(start - q0) : 0;  // first lane of my tile this round
+                const uint32_t cx_first = __shfl_sync(FULL, cx, first);
+                const uint32_t rank = act ? S[j].done + (cx - cx_first) : 0u;
+                const bool last = act && (lane == 31 || q + 1u == P || q + 1u == S[j].px_end);
+                __syncwarp();
+                if (last) S[j].done += ci - cx_first;
+                __syncwarp();
+                if (PHASE == P_WRITE && mask) {
+                    const TileSlot& T = S[j];
+                    uint32_t k = rank;
+                    for (uint32_t m = mask; m; m &= m - 1u) {
+                        const int s = __ffs(m) - 1;
+                        float b[3], z;
+                        sample_bz(t, T, ox0 + c_sample_loc8[s][0], oy0 + c_sample_loc8[s][1], b, z);
+                        const float3 p = interp3(b, T.p);
+                        const float3 nn = interp3(b, T.n);
+                        FragDesc d;
+                        d.p = make_float4(p.x, p.y, p.z, __uint_as_float(T.base_r + k * T.per));
+                        d.n = make_float4(nn.x, nn.y, nn.z, __uint_as_float(T.meta));
+                        frags[T.base_f + k] = d;
+                        ++k;
+                    }
+                }
+            }
+        }
+        __syncwarp();
+        if (PHASE == P_COUNT && g < total) counts[g] = make_uint2(S[lane].done, S[lane].done * S[lane].per);
+        __syncwarp();
+    }
+}
+
+template <int KIND, int PHASE>
+static void launch_cover(const RasterArgs& A, const TilePlan& plan, uint2* counts, const uint2* offs, FragDesc* frags,
+                         int* err, cudaStream_t st) {
+    const uint32_t nchunks = (plan.total + 31u) >> 5;
+    int blocks = (int)((nchunks + 3u) >> 2);
+    blocks = blocks < 1 ? 1 : (blocks > 152 * 16 ? 152 * 16 : blocks);
+    k_cover<KIND, PHASE><<<blocks, 128, 0, st>>>(A, plan, counts, offs, frags, err);
 }
 
 // Injection shading, one thread per covered sample: writes its face records
@@ -770,10 +1022,10 @@ static int check_scene(const vct_scene* s) {
     return VCT_OK;
 }
 
-// Tile counting + prefix sum shared by every pass.  On return tile_end (in the
-// workspace) holds inclusive sums; *total receives the tile count (host).
-static int plan_tiles(RasterArgs& A, vct_workspace_s* ws, size_t& off, uint32_t** tile_end, uint32_t* total,
-                      cudaStream_t st) {
+// Tile plan shared by every pass: inclusive tile sums per item and the item
+// of every tile, in the workspace from offset 0; `off` is advanced past them.
+static int plan_tiles(RasterArgs& A, vct_workspace_s* ws, size_t& off, TilePlan* plan, cudaStream_t st) {
+    VCT_CHECK_ARG(A.items < (1LL << 31), "rasteriser: more than 2^31 (triangle, level) items");
     const size_t n = (size_t)A.items;
     size_t scan_bytes = 0;
     VCT_CUDA_TRY(cub::DeviceScan::InclusiveSum(nullptr, scan_bytes, (uint32_t*)nullptr, (uint32_t*)nullptr, (int)n));
@@ -782,14 +1034,29 @@ static int plan_tiles(RasterArgs& A, vct_workspace_s* ws, size_t& off, uint32_t*
     if (rc != VCT_OK) return rc;
     char* base = (char*)ws->ptr;
     uint32_t* counts = (uint32_t*)base;
-    *tile_end = (uint32_t*)(base + a256(4 * n));
+    uint32_t* tile_end = (uint32_t*)(base + a256(4 * n));
     void* tmp = base + 2 * a256(4 * n);
     off = 2 * a256(4 * n) + a256(scan_bytes);
     k_item_tiles<<<grid_of(n, 128), 128, 0, st>>>(A, counts);
     VCT_LAUNCH_CHECK();
-    VCT_CUDA_TRY(cub::DeviceScan::InclusiveSum(tmp, scan_bytes, counts, *tile_end, (int)n, st));
-    VCT_CUDA_TRY(cudaMemcpyAsync(total, *tile_end + (n - 1), 4, cudaMemcpyDeviceToHost, st));
+    VCT_CUDA_TRY(cub::DeviceScan::InclusiveSum(tmp, scan_bytes, counts, tile_end, (int)n, st));
+    uint32_t total = 0;
+    VCT_CUDA_TRY(cudaMemcpyAsync(&total, tile_end + (n - 1), 4, cudaMemcpyDeviceToHost, st));
     VCT_CUDA_TRY(cudaStreamSynchronize(st));
+    if (ws->bytes < off + a256(4 * (size_t)total) + 256) {
+        rc = workspace_reserve(ws, off + a256(4 * (size_t)total) + 256);
+        if (rc != VCT_OK) return rc;
+        return plan_tiles(A, ws, off, plan, st);  // the arena moved: plan again
+    }
+    uint32_t* tile_item = (uint32_t*)(base + off);
+    off += a256(4 * (size_t)total);
+    if (total) {
+        k_tile_items<<<grid_of(n, 256), 256, 0, st>>>(tile_end, A.items, tile_item);
+        VCT_LAUNCH_CHECK();
+    }
+    plan->tile_end = tile_end;
+    plan->tile_item = tile_item;
+    plan->total = total;
     return VCT_OK;
 }
 
@@ -802,8 +1069,9 @@ constexpr int kWorkspaceGrew = 1;
 // advanced past it) holds each tile's first descriptor / record and *nfrag /
 // *nrec the totals (host).
 template <int KIND>
-static int count_tiles(RasterArgs& A, vct_workspace_s* ws, size_t& off, const uint32_t* tile_end, uint32_t total,
-                       uint2** offs, uint32_t* nfrag, uint32_t* nrec, cudaStream_t st) {
+static int count_tiles(RasterArgs& A, vct_workspace_s* ws, size_t& off, const TilePlan& plan, uint2** offs,
+                       uint32_t* nfrag, uint32_t* nrec, cudaStream_t st) {
+    const uint32_t total = plan.total;
     size_t scan_bytes = 0;
     VCT_CUDA_TRY(cub::DeviceScan::ExclusiveScan(nullptr, scan_bytes, (uint2*)nullptr, (uint2*)nullptr, SumU2{},
                                                 make_uint2(0u, 0u), (int)total));
@@ -817,7 +1085,7 @@ static int count_tiles(RasterArgs& A, vct_workspace_s* ws, size_t& off, const ui
     *offs = (uint2*)(base + a256(8 * (size_t)total));
     void* tmp = base + 2 * a256(8 * (size_t)total);
     off += 2 * a256(8 * (size_t)total) + a256(scan_bytes);
-    k_raster_tiles<KIND, P_COUNT><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, counts, nullptr, nullptr, nullptr);
+    launch_cover<KIND, P_COUNT>(A, plan, counts, nullptr, nullptr, nullptr, st);
     VCT_LAUNCH_CHECK();
     VCT_CUDA_TRY(cub::DeviceScan::ExclusiveScan(tmp, scan_bytes, counts, *offs, SumU2{}, make_uint2(0u, 0u), (int)total, st));
     uint2 last[2];
@@ -943,11 +1211,10 @@ extern "C" int vct_voxelize_opacity(const vct_scene* scene, const vct_clipmap_re
     A.atlas = atlas;
     cudaStream_t st = as_stream(stream);
     size_t off;
-    uint32_t* tile_end;
-    uint32_t total;
-    rc = plan_tiles(A, ws, off, &tile_end, &total, st);
+    TilePlan plan;
+    rc = plan_tiles(A, ws, off, &plan, st);
     if (rc != VCT_OK) return rc;
-    if (total) k_raster_tiles<K_OPACITY, P_DIRECT><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, nullptr, nullptr, nullptr, nullptr);
+    if (plan.total) launch_cover<K_OPACITY, P_DIRECT>(A, plan, nullptr, nullptr, nullptr, nullptr, st);
     VCT_LAUNCH_CHECK();
     return VCT_OK;
 }
@@ -975,11 +1242,10 @@ extern "C" int vct_shadow_depth(const vct_scene* scene, const vct_directional_li
     A.items = scene->triangle_count;
     A.depth = depth;
     size_t off;
-    uint32_t* tile_end;
-    uint32_t total;
-    rc = plan_tiles(A, ws, off, &tile_end, &total, st);
+    TilePlan plan;
+    rc = plan_tiles(A, ws, off, &plan, st);
     if (rc != VCT_OK) return rc;
-    if (total) k_raster_tiles<K_SHADOW, P_DIRECT><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, nullptr, nullptr, nullptr, nullptr);
+    if (plan.total) launch_cover<K_SHADOW, P_DIRECT>(A, plan, nullptr, nullptr, nullptr, nullptr, st);
     VCT_LAUNCH_CHECK();
     return VCT_OK;
 }
@@ -1011,15 +1277,14 @@ extern "C" int vct_inject_radiance(const vct_scene* scene, const vct_clipmap_reg
     A.atlas = atlas;
     cudaStream_t st = as_stream(stream);
     size_t off;
-    uint32_t* tile_end;
-    uint32_t total;
-    rc = plan_tiles(A, ws, off, &tile_end, &total, st);
+    TilePlan plan;
+    rc = plan_tiles(A, ws, off, &plan, st);
     if (rc != VCT_OK) return rc;
-    if (total == 0) return VCT_OK;
+    if (plan.total == 0) return VCT_OK;
     if (mode == VCT_INJECT_ATOMIC) {
         int* err = (int*)((char*)ws->ptr + off);
         VCT_CUDA_TRY(cudaMemsetAsync(err, 0, 4, st));
-        k_raster_tiles<K_INJECT, P_DIRECT><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, nullptr, nullptr, nullptr, err);
+        launch_cover<K_INJECT, P_DIRECT>(A, plan, nullptr, nullptr, nullptr, err, st);
         VCT_LAUNCH_CHECK();
         int herr = 0;
         VCT_CUDA_TRY(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st));
@@ -1031,7 +1296,7 @@ extern "C" int vct_inject_radiance(const vct_scene* scene, const vct_clipmap_reg
     // -> stable sort by texel -> fold each texel's run in traversal order
     uint2* offs;
     uint32_t nfrag, nrec;
-    rc = count_tiles<K_INJECT>(A, ws, off, tile_end, total, &offs, &nfrag, &nrec, st);
+    rc = count_tiles<K_INJECT>(A, ws, off, plan, &offs, &nfrag, &nrec, st);
     if (rc == kWorkspaceGrew)
         return vct_inject_radiance(scene, regions, R, shadow, light, light_shadow, atlas, level_mask, mode, ws, stream);
     if (rc != VCT_OK) return rc;
@@ -1062,7 +1327,7 @@ extern "C" int vct_inject_radiance(const vct_scene* scene, const vct_clipmap_reg
     uint32_t* heads = (uint32_t*)(p + 4 * r4);
     uint32_t* nheads = (uint32_t*)(p + 5 * r4);
     void* stmp = p + 5 * r4 + 256;
-    k_raster_tiles<K_INJECT, P_WRITE><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, nullptr, offs, fr, nullptr);
+    launch_cover<K_INJECT, P_WRITE>(A, plan, nullptr, offs, fr, nullptr, st);
     VCT_LAUNCH_CHECK();
     k_inject_shade<<<grid_of(nfrag, 256), 256, 0, st>>>(A, fr, nfrag, kin, vin, rgb);
     VCT_LAUNCH_CHECK();
@@ -1108,15 +1373,14 @@ extern "C" int vct_svo_fragments(const vct_scene* scene, int32_t octree_level, c
     A.frag_capacity = capacity;
     cudaStream_t st = as_stream(stream);
     size_t off;
-    uint32_t* tile_end;
-    uint32_t total;
-    rc = plan_tiles(A, ws, off, &tile_end, &total, st);
+    TilePlan plan;
+    rc = plan_tiles(A, ws, off, &plan, st);
     if (rc != VCT_OK) return rc;
-    if (total == 0) return VCT_OK;
+    if (plan.total == 0) return VCT_OK;
     // count pass (SparseVoxelizer::preVoxelize), host readback of the count
     uint2* offs;
     uint32_t nfrag, nslot;
-    rc = count_tiles<K_SVO>(A, ws, off, tile_end, total, &offs, &nfrag, &nslot, st);
+    rc = count_tiles<K_SVO>(A, ws, off, plan, &offs, &nfrag, &nslot, st);
     if (rc == kWorkspaceGrew)
         return vct_svo_fragments(scene, octree_level, bb_min, bb_max, shadow, light, light_shadow, frags, capacity,
                                  count, ws, stream);
@@ -1134,7 +1398,7 @@ extern "C" int vct_svo_fragments(const vct_scene* scene, int32_t octree_level, c
     FragDesc* fr = (FragDesc*)((char*)ws->ptr + off);
     // write pass (SparseVoxelizer::cmdVoxelize); discarded slots stay zero
     VCT_CUDA_TRY(cudaMemsetAsync(frags, 0, sizeof(uint32_t) * 2 * (size_t)*count, st));
-    k_raster_tiles<K_SVO, P_WRITE><<<grid_of(total, 128, 152 * 64), 128, 0, st>>>(A, tile_end, nullptr, offs, fr, nullptr);
+    launch_cover<K_SVO, P_WRITE>(A, plan, nullptr, offs, fr, nullptr, st);
     VCT_LAUNCH_CHECK();
     k_svo_shade<<<grid_of(nfrag, 256), 256, 0, st>>>(A, fr, nfrag);
     VCT_LAUNCH_CHECK();
