@@ -152,7 +152,7 @@ __global__ void k_morton_keys(const vct_surface_sample* __restrict__ s, int64_t 
 
 constexpr int kWarpsPerBlock = 8;
 
-__global__ void __launch_bounds__(256) k_trace_diffuse(FastArgs A, const uint32_t* __restrict__ order,
+__global__ void __launch_bounds__(256) k_trace_diffuse(const __grid_constant__ FastArgs A, const uint32_t* __restrict__ order,
                                                        uint32_t* __restrict__ spec_key,
                                                        unsigned int* __restrict__ spec_count) {
     __shared__ float4 s_start[kWarpsPerBlock][32];
@@ -262,14 +262,54 @@ __global__ void __launch_bounds__(256) k_trace_diffuse(FastArgs A, const uint32_
     }
 }
 
-// One cone marched by a whole warp: lane j takes step k0 + j of each chunk of
-// 32.  The step schedule (step, diameter, segment length) depends only on the
-// step index, not on the samples, so every lane runs the scalar recurrence of
-// traceCone for the chunk (identical SIMT work, exact schedule) and keeps its
-// own step.  The front-to-back composite result += (1 - result.a) * src is
-// the associative "over" operator and 1 - occlusion is the product of
-// (1 - x_k): both are warp scans.  The march stops at the first step whose
-// occlusion reaches 1 or whose distance reaches maxDistance, like the loop.
+// One step of a cone: the sample's contribution (rgb * corr, opacity) and
+// its transmittance factor 1 - opacity / (1 + (step + vs) * decay).
+struct ConeStep {
+    float r, g, b, a, t;
+};
+
+__device__ __forceinline__ ConeStep cone_step(cudaTextureObject_t tex, const FastConsts& C, float3 start, float3 dir,
+                                              float fox, float foy, float foz, float3 wt, float start_level, float st,
+                                              float dm, float sg) {
+    const float3 pos = f3(fmaf(dir.x, st, start.x), fmaf(dir.y, st, start.y), fmaf(dir.z, st, start.z));
+    const float dx = C.cx - pos.x, dy = C.cy - pos.y, dz = C.cz - pos.z;
+    const float dist = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+    const float min_level = ceilf(log2f(dist * C.inv_min_radius));
+    float cl = log2f(dm * C.inv_uvs);
+    cl = fminf(fmaxf(fmaxf(start_level, cl), min_level), (float)(kClipLevels - 1));
+    const float flo = floorf(cl);
+    const int lo = (int)flo;
+    const float fr = cl - flo;
+    float4 smp = sample_level(tex, C, pos, lo, fox, foy, foz, wt);
+    if (fr > 0.0f) {
+        const float4 h = sample_level(tex, C, pos, lo + 1, fox, foy, foz, wt);
+        smp = make_float4(fmaf(h.x - smp.x, fr, smp.x), fmaf(h.y - smp.y, fr, smp.y), fmaf(h.z - smp.z, fr, smp.z),
+                          fmaf(h.w - smp.w, fr, smp.w));
+    }
+    const float vs = C.uvs * exp2f(cl);
+    const float corr = __fdividef(sg, vs);
+    const float opacity = __saturatef(1.0f - exp2f(corr * __log2f(1.0f - smp.w)));
+    return ConeStep{smp.x * corr, smp.y * corr, smp.z * corr, opacity,
+                    1.0f - __fdividef(opacity, fmaf(st + vs, C.decay, 1.0f))};
+}
+
+// `p` followed by `q` under front-to-back compositing: rgb and alpha by the
+// "over" operator, transmittance by product.
+__device__ __forceinline__ ConeStep over(const ConeStep& p, const ConeStep& q) {
+    const float k = 1.0f - p.a;
+    return ConeStep{fmaf(k, q.r, p.r), fmaf(k, q.g, p.g), fmaf(k, q.b, p.b), fmaf(k, q.a, p.a), p.t * q.t};
+}
+
+// One cone marched by a whole warp, 64 steps per round: lane j takes steps
+// 2j and 2j + 1 of the round.  The step schedule (step, diameter, segment
+// length) depends only on the step index, not on the samples, and has a
+// closed form (below), so every lane finds its own steps directly.  The
+// front-to-back composite result += (1 - result.a) * src is the associative
+// "over" operator and 1 - occlusion is the product of (1 - x_k): each lane
+// composes its two steps, a warp scan composes the lanes.  The march stops at
+// the first step whose occlusion reaches 1 or whose distance reaches
+// maxDistance, like the loop: the lane holding that step re-applies its own
+// steps from the state before it.
 __device__ __forceinline__ float4 trace_cone_warp(cudaTextureObject_t tex, const FastConsts& C, float3 start,
                                                   float3 dir, float coef, float start_level, float step_factor,
                                                   unsigned long long& steps) {
@@ -282,90 +322,84 @@ __device__ __forceinline__ float4 trace_cone_warp(cudaTextureObject_t tex, const
     const float foy = dir.y > 0.0f ? 2.0f / 6.0f : 3.0f / 6.0f;
     const float foz = dir.z > 0.0f ? 4.0f / 6.0f : 5.0f / 6.0f;
     const float3 wt = f3(dir.x * dir.x, dir.y * dir.y, dir.z * dir.z);
-    // carried state: composite (C, A), transmittance T, schedule (st, dm, sg)
-    float cr = 0.f, cg = 0.f, cb = 0.f, ca = 0.f, ct = 1.0f;
-    float st = 0.0f, dm = uvs, sg = vs0;
+    const ConeStep id{0.f, 0.f, 0.f, 0.f, 1.0f};
+    ConeStep carried = id;
+    float st = 0.0f, dm = uvs, sg = vs0;  // schedule at the round's first step
+    // The step schedule st += max(st * coef, uvs) * step_factor in closed form:
+    // linear steps of u = uvs * step_factor while st * coef <= uvs, then
+    // geometric growth by r = 1 + coef * step_factor.  From a round's start
+    // st_0, with K = the number of linear steps left,
+    //   st_j = st_0 + j u (j <= K),   st_j = (st_0 + K u) r^(j - K) (j >= K).
+    const float u = uvs * step_factor, lr = __log2f(fmaf(coef, step_factor, 1.0f)), T = uvs / coef;
     unsigned long long it = 0;
     for (;;) {
-        float my_st = 0.f, my_dm = 0.f, my_sg = 0.f;
-#pragma unroll 8
-        for (int j = 0; j < 32; ++j) {
-            if (j == lane) {
-                my_st = st;
-                my_dm = dm;
-                my_sg = sg;
-            }
-            const float nst = fmaf(fmaxf(dm, uvs), step_factor, st);
-            sg = nst - st;
-            st = nst;
-            dm = st * coef;
+        const float K = st <= T ? floorf((T - st) / u) + 1.0f : 0.0f;
+        const float sK = fmaf(K, u, st);
+        auto st_at = [&](float jf) { return jf <= K ? fmaf(jf, u, st) : sK * exp2f((jf - K) * lr); };
+        const float j0 = (float)(2 * lane);
+        const float s0 = st_at(j0), s1 = st_at(j0 + 1.0f);
+        const float dm0 = lane == 0 ? dm : s0 * coef, sg0 = lane == 0 ? sg : s0 - st_at(j0 - 1.0f);
+        const bool v0 = s0 < kMaxTraceDistance, v1 = s1 < kMaxTraceDistance;
+        ConeStep a = id, b = id;
+        if (v0) a = cone_step(tex, C, start, dir, fox, foy, foz, wt, start_level, s0, dm0, sg0);
+        if (v1) b = cone_step(tex, C, start, dir, fox, foy, foz, wt, start_level, s1, s1 * coef, s1 - s0);
+        {  // the schedule at the next round's first step
+            const float s63 = st_at(63.0f), s64 = st_at(64.0f);
+            st = s64;
+            sg = s64 - s63;
+            dm = s64 * coef;
         }
-        const bool valid = my_st < kMaxTraceDistance;
-        float sr = 0.f, sgc = 0.f, sbc = 0.f, sa = 0.f, tx = 1.0f;
-        if (valid) {
-            const float3 pos = f3(fmaf(dir.x, my_st, start.x), fmaf(dir.y, my_st, start.y), fmaf(dir.z, my_st, start.z));
-            const float dx = C.cx - pos.x, dy = C.cy - pos.y, dz = C.cz - pos.z;
-            const float dist = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
-            const float min_level = ceilf(log2f(dist * C.inv_min_radius));
-            float cl = log2f(my_dm * C.inv_uvs);
-            cl = fminf(fmaxf(fmaxf(start_level, cl), min_level), (float)(kClipLevels - 1));
-            const float flo = floorf(cl);
-            const int lo = (int)flo;
-            const float fr = cl - flo;
-            float4 smp = sample_level(tex, C, pos, lo, fox, foy, foz, wt);
-            if (fr > 0.0f) {
-                const float4 h = sample_level(tex, C, pos, lo + 1, fox, foy, foz, wt);
-                smp = make_float4(fmaf(h.x - smp.x, fr, smp.x), fmaf(h.y - smp.y, fr, smp.y),
-                                  fmaf(h.z - smp.z, fr, smp.z), fmaf(h.w - smp.w, fr, smp.w));
-            }
-            const float vs = uvs * exp2f(cl);
-            const float corr = __fdividef(my_sg, vs);
-            const float opacity = __saturatef(1.0f - exp2f(corr * __log2f(1.0f - smp.w)));
-            sr = smp.x * corr;
-            sgc = smp.y * corr;
-            sbc = smp.z * corr;
-            sa = opacity;
-            tx = 1.0f - __fdividef(opacity, fmaf(my_st + vs, C.decay, 1.0f));
-        }
-        // inclusive warp scans: over-composite of (rgb, a) and product of transmittance
+        // inclusive warp scan of the lanes' two-step composites
+        ConeStep x = over(a, b);
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const float pr = __shfl_up_sync(0xffffffffu, sr, o), pg = __shfl_up_sync(0xffffffffu, sgc, o);
-            const float pb = __shfl_up_sync(0xffffffffu, sbc, o), pa = __shfl_up_sync(0xffffffffu, sa, o);
-            const float pt = __shfl_up_sync(0xffffffffu, tx, o);
-            if (lane >= o) {
-                const float k = 1.0f - pa;
-                sr = fmaf(k, sr, pr);
-                sgc = fmaf(k, sgc, pg);
-                sbc = fmaf(k, sbc, pb);
-                sa = fmaf(k, sa, pa);
-                tx = tx * pt;
-            }
+            ConeStep p;
+            p.r = __shfl_up_sync(0xffffffffu, x.r, o);
+            p.g = __shfl_up_sync(0xffffffffu, x.g, o);
+            p.b = __shfl_up_sync(0xffffffffu, x.b, o);
+            p.a = __shfl_up_sync(0xffffffffu, x.a, o);
+            p.t = __shfl_up_sync(0xffffffffu, x.t, o);
+            if (lane >= o) x = over(p, x);
         }
-        // combine with the carried state
-        const float k = 1.0f - ca;
-        const float tr = fmaf(k, sr, cr), tg = fmaf(k, sgc, cg), tb = fmaf(k, sbc, cb), ta = fmaf(k, sa, ca);
-        const float tt = ct * tx;
-        // executed lanes: valid ones up to (and including) the first whose occlusion reaches 1
-        const unsigned vmask = __ballot_sync(0xffffffffu, valid);
-        const unsigned omask = __ballot_sync(0xffffffffu, valid && (1.0f - tt) >= 1.0f);
-        int last = 31 - __clz(vmask);  // vmask is a prefix of lanes (the step grows)
-        if (omask) last = min(last, __ffs(omask) - 1);
-        if (vmask == 0u) break;
-        cr = __shfl_sync(0xffffffffu, tr, last);
-        cg = __shfl_sync(0xffffffffu, tg, last);
-        cb = __shfl_sync(0xffffffffu, tb, last);
-        ca = __shfl_sync(0xffffffffu, ta, last);
-        ct = __shfl_sync(0xffffffffu, tt, last);
-        it += (unsigned long long)(last + 1);
-        if (last < 31 || omask) break;
+        // the state before this lane's steps, and after each of them
+        ConeStep before;
+        before.r = __shfl_up_sync(0xffffffffu, x.r, 1);
+        before.g = __shfl_up_sync(0xffffffffu, x.g, 1);
+        before.b = __shfl_up_sync(0xffffffffu, x.b, 1);
+        before.a = __shfl_up_sync(0xffffffffu, x.a, 1);
+        before.t = __shfl_up_sync(0xffffffffu, x.t, 1);
+        before = lane == 0 ? carried : over(carried, before);
+        const ConeStep after0 = over(before, a), after1 = over(after0, b);
+        const bool t0 = v0 && (1.0f - after0.t) >= 1.0f, t1 = v1 && (1.0f - after1.t) >= 1.0f;
+        const unsigned tmask = __ballot_sync(0xffffffffu, t0 || t1);
+        const unsigned vmask = __ballot_sync(0xffffffffu, v0);  // a prefix of lanes (the step grows)
+        if (tmask) {  // occlusion reached 1: stop after the first such step
+            const int L = __ffs(tmask) - 1;
+            const bool first = __shfl_sync(0xffffffffu, t0, L);
+            const ConeStep f = first ? after0 : after1;
+            carried.r = __shfl_sync(0xffffffffu, f.r, L);
+            carried.g = __shfl_sync(0xffffffffu, f.g, L);
+            carried.b = __shfl_sync(0xffffffffu, f.b, L);
+            carried.t = __shfl_sync(0xffffffffu, f.t, L);
+            it += (unsigned long long)(2 * L + (first ? 1 : 2));
+            break;
+        }
+        const unsigned v1mask = __ballot_sync(0xffffffffu, v1);
+        // invalid steps are the identity: the round's total is lane 31's prefix
+        carried.r = __shfl_sync(0xffffffffu, after1.r, 31);
+        carried.g = __shfl_sync(0xffffffffu, after1.g, 31);
+        carried.b = __shfl_sync(0xffffffffu, after1.b, 31);
+        carried.a = __shfl_sync(0xffffffffu, after1.a, 31);
+        carried.t = __shfl_sync(0xffffffffu, after1.t, 31);
+        it += (unsigned long long)(__popc(vmask) + __popc(v1mask));
+        if (v1mask != 0xffffffffu) break;  // maxDistance reached within the round
     }
     if (lane == 0) steps += it;
-    return make_float4(cr, cg, cb, ct);
+    return make_float4(carried.r, carried.g, carried.b, carried.t);
 }
 
 // One warp per specular cone of the list (the list is kept in Morton order).
-__global__ void __launch_bounds__(256) k_trace_specular_warp(FastArgs A, const uint32_t* __restrict__ list,
+__global__ void __launch_bounds__(256, 4) k_trace_specular_warp(const __grid_constant__ FastArgs A, const uint32_t* __restrict__ list,
                                                              const unsigned int* __restrict__ spec_count) {
     const TraceParams& P = A.P;
     const FastConsts& C = A.C;
