@@ -278,6 +278,8 @@ def run_ours(args, world, rank, local):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
     ms = float(t.item()) / args.steps
     value = cone_samples * world / (ms * 1e-3)
+    # the trace's speed of light: the same fetches per cone sample with nothing else (vct_gather_probe)
+    gather_peak = clipmap.gather_probe(desc, tex) if tex is not None else None
 
     # voxelise + shadow + inject + mips of one frame, and the SVO build at 256^3
     for _ in range(2):
@@ -359,6 +361,13 @@ def run_ours(args, world, rank, local):
                          "frac": achieved / peak, "traffic": traffic,
                          "note": f"{bpcs} B of algorithmic texel reads per cone sample over the {peak_kind} HBM "
                                  "copy peak; the taps are served mostly from L1/TEX and L2"},
+            "gather_roofline": None if gather_peak is None else {
+                "bound": "l1tex/l2 gather", "achieved": cone_samples / (statistics.mean(per) * 1e-3),
+                "peak": gather_peak, "unit": "cone samples/s",
+                "frac": cone_samples / (statistics.mean(per) * 1e-3) / gather_peak,
+                "note": "peak = vct_gather_probe: the texture fetches of one cone sample (3 faces x 2 levels, "
+                        "trilinear) per step of warp-coherent synthetic cones, measured on this GPU with the same "
+                        "texture; achieved = the whole trace step (sort, diffuse and specular kernels, texture refresh)"},
             "cpu_baseline": cpu,
             "e2e": {"value": cone_samples * world / (e2e_ms * 1e-3), "unit": "cone samples/s",
                     "h2d_bytes_per_step": int(samples.numel() * 4),

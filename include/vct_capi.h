@@ -247,6 +247,15 @@ int vct_downsample(uint32_t* atlas, const vct_downsample_desc* desc, int32_t mod
 int vct_downsample_all(uint32_t* atlas, const vct_clipmap_region regions_host[6],
                        int32_t clipmap_resolution, int32_t mode, void* stream);
 
+/* vct_copy_alpha(radiance, opacity, level l) followed by
+ * vct_downsample(radiance, desc, VCT_DOWNSAMPLE_RADIANCE) for the same level
+ * l >= 1 (RadianceInjectionPass's CopyAlpha then DownSampler::cmdDownSampleRadiance,
+ * RadianceInjectionPass.cpp:134-159), fused into one pass over the level; the
+ * result is bit-identical to the two calls in sequence.  No single-pass
+ * counterpart in the reference. */
+int vct_copy_alpha_downsample(uint32_t* radiance_atlas, const uint32_t* opacity_atlas,
+                              const vct_downsample_desc* desc, void* stream);
+
 /* BorderWrapper::cmdWrappingOpacityBorder (VFS/RenderPass/Clipmap/BorderWrapper.cpp:123-151,
  * borderWrapping.comp): copy toroidal neighbours into border texels. */
 int vct_wrap_border(uint32_t* atlas, const vct_border_wrapping_desc* desc, void* stream);
@@ -303,6 +312,17 @@ int vct_cone_trace_fast(const vct_cone_tracing_desc* desc, const vct_cam_matrix*
                         const vct_surface_sample* samples, int64_t sample_count,
                         float* diffuse_out, float* specular_out, unsigned long long* cone_steps,
                         void* scratch, size_t scratch_bytes, void* stream);
+
+/* Calibration probe for the trace's roofline; no counterpart in the
+ * reference.  Times (CUDA events on `stream`, after one warm-up launch) a
+ * kernel that marches `cones` synthetic cones of `steps_per_cone` steps, one
+ * warp per cone with consecutive steps on consecutive lanes, and performs at
+ * every step exactly the texture fetches of one cone sample (three face taps
+ * at two adjacent levels) and nothing else.  *samples_per_second receives
+ * the measured cone-sample rate: the gather speed of light that
+ * vct_cone_trace_fast's rate is compared with.  Synchronises `stream`. */
+int vct_gather_probe(const vct_cone_tracing_desc* desc, vct_texture radiance, int64_t cones, int32_t steps_per_cone,
+                     double* samples_per_second, void* stream);
 
 /* ------------------------------------------------ scene and raster passes */
 

@@ -110,3 +110,29 @@ def test_cone_trace_exact_matches_oracle(cuda, oracle, R, n):
         assert rel < 1e-2, rel
     gsteps = int(steps.item())
     assert abs(gsteps - steps32) <= max(8, 0.002 * steps32), (gsteps, steps32)
+
+
+@pytest.mark.parametrize("R", [16, 32, 64])
+@pytest.mark.parametrize("cam", [(0.0, 0.0, 0.0), (3.7, -1.2, 6.4), (-9.3, 4.1, -2.2)])
+def test_fused_copy_alpha_downsample_equals_the_two_passes(cuda, oracle, R, cam):
+    """vct_copy_alpha_downsample (levels 1..5) after vct_copy_alpha (level 0)
+    gives the atlas of copy-alpha on every level then the radiance mips, bit
+    for bit (the frame's order), including regions that wrap toroidally."""
+    torch = cuda
+    from vk_voxel_cone_tracing_gb300 import clipmap
+    from vk_voxel_cone_tracing_gb300.scene import random_atlas
+    rad = random_atlas(R, seed=R + 7, fill=0.4)
+    opa = random_atlas(R, seed=R + 8, fill=0.6)
+    regions = oracle.clip_regions(cam, R)
+    want = rad.copy()
+    for level in range(6):
+        oracle.copy_alpha(want, opa, R, level)
+    for level in range(1, 6):
+        oracle.downsample(want, R, regions[level - 1, 0:3], level, 1)
+    dev, dopa = _to_dev(torch, rad), _to_dev(torch, opa)
+    clipmap.cmd_copy_alpha(dev, dopa, R, 0)
+    for level in range(1, 6):
+        clipmap.cmd_copy_alpha_downsample(dev, dopa, R, tuple(int(v) for v in regions[level - 1, 0:3]), level)
+    torch.cuda.synchronize()
+    got = _from_dev(dev)
+    assert np.array_equal(got, want), f"{np.count_nonzero(got != want)} texels differ"

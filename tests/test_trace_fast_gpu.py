@@ -163,3 +163,21 @@ def test_fp16_form_trace_matches_fp64(cuda, oracle):
     assert _rel(d[:, :3], d64[:, :3]) < TOL_FP64
     assert _rel(s[:, :3], s64[:, :3]) < TOL_FP64
     tex.close()
+
+
+def test_gather_probe_reports_a_finite_rate_and_checks_arguments(cuda, oracle):
+    """The roofline probe (no reference counterpart) runs the fetch pattern of
+    one cone sample per step and reports a positive rate; bad arguments are
+    rejected before any launch."""
+    torch = cuda
+    import ctypes as C
+    from vk_voxel_cone_tracing_gb300 import capi, clipmap
+    R = 32
+    regions, desc, atlas, _ = _setup(oracle, R, 16, seed=9)
+    tex = clipmap.RadianceTexture(R).update(_dev(torch, atlas))
+    rate = clipmap.gather_probe(desc, tex, cones=2048, steps_per_cone=64)
+    assert np.isfinite(rate) and rate > 1e6
+    out = C.c_double(0.0)
+    rc = capi.lib().vct_gather_probe(capi.ref(desc), tex.handle, 0, 64, C.byref(out), None)
+    assert rc == capi.VCT_E_BAD_ARG
+    tex.close()

@@ -142,6 +142,7 @@ _SIGS: dict[str, tuple] = {
     "vct_clear_region": (C.c_int, [P, P, P]),
     "vct_copy_alpha": (C.c_int, [P, P, P, P]),
     "vct_downsample": (C.c_int, [P, P, C.c_int32, P]),
+    "vct_copy_alpha_downsample": (C.c_int, [P, P, P, P]),
     "vct_downsample_all": (C.c_int, [P, P, C.c_int32, C.c_int32, P]),
     "vct_wrap_border": (C.c_int, [P, P, P]),
     "vct_cone_trace": (C.c_int, [P, P, P, C.c_int32, P, P, P, P, C.c_int64, P, P, P, P]),
@@ -152,6 +153,7 @@ _SIGS: dict[str, tuple] = {
     "vct_downsample_rgba16f": (C.c_int, [P, P, C.c_int32, P]),
     "vct_cone_trace_fast_scratch_bytes": (C.c_int64, [C.c_int64]),
     "vct_cone_trace_fast": (C.c_int, [P, P, P, P, P, P, P, C.c_int64, P, P, P, P, C.c_size_t, P]),
+    "vct_gather_probe": (C.c_int, [P, P, C.c_int64, C.c_int32, P, P]),
     "vct_workspace_create": (C.c_int, [C.c_size_t, C.POINTER(C.c_void_p)]),
     "vct_workspace_destroy": (C.c_int, [P]),
     "vct_workspace_bytes": (C.c_int64, [P]),

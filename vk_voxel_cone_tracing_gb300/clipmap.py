@@ -64,6 +64,13 @@ def cmd_downsample(atlas: torch.Tensor, R: int, prev_region_min, level: int, mod
     capi.call("vct_downsample", _ptr(atlas), capi.ref(d), mode, _stream())
 
 
+def cmd_copy_alpha_downsample(radiance: torch.Tensor, opacity: torch.Tensor, R: int, prev_region_min, level: int,
+                              band: int = capi.DOWNSAMPLE_REGION_SIZE) -> None:
+    """vct_copy_alpha (level) + vct_downsample (radiance, level) fused into one pass."""
+    d = capi.DownSampleDesc(capi.i3(*prev_region_min), level, R, band)
+    capi.call("vct_copy_alpha_downsample", _ptr(radiance), _ptr(opacity), capi.ref(d), _stream())
+
+
 def cmd_downsample_all(atlas: torch.Tensor, R: int, regions, mode: int) -> None:
     capi.call("vct_downsample_all", _ptr(atlas), C.cast(regions, C.c_void_p), R, mode, _stream())
 
@@ -204,3 +211,10 @@ def cone_trace_fast(desc: capi.ConeTracingDesc, eye, tex: RadianceTexture, sampl
               capi.ref(sd), _ptr(samples), n, _ptr(diffuse), _ptr(specular), _ptr(steps), C.c_void_p(base),
               avail, _stream())
     return diffuse, specular
+
+
+def gather_probe(desc: capi.ConeTracingDesc, tex: RadianceTexture, cones: int = 152 * 1024, steps_per_cone: int = 64) -> float:
+    """Measured cone-sample rate of the pure fetch pattern (vct_gather_probe): the trace's speed of light."""
+    rate = C.c_double(0.0)
+    capi.call("vct_gather_probe", capi.ref(desc), tex.handle, cones, steps_per_cone, C.byref(rate), _stream())
+    return rate.value

@@ -14,15 +14,15 @@ namespace vct {
 // 6 face copies are 6 strided stores.
 __global__ void k_clear_region(uint32_t* __restrict__ atlas, AtlasDims A, int3 rmin, uint3 ext, int level,
                                int faces) {
-    const int64_t n = (int64_t)ext.x * ext.y * ext.z;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
-        int gx = (int)(t % ext.x);
-        int64_t r = t / ext.x;
-        int gy = (int)(r % ext.y);
-        int gz = (int)(r / ext.y);
-        int px = (gx + rmin.x) % A.R + 1;
-        int py = (gy + rmin.y) % A.R + 1 + level * A.rb;
-        int pz = (gz + rmin.z) % A.R + 1;
+    // extents <= R <= 1024 and corners in [0, 2^30]: 32-bit arithmetic; R is
+    // a power of two, so the (non-negative) % R is a mask
+    const uint32_t n = ext.x * ext.y * ext.z, m = (uint32_t)A.R - 1u;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const uint32_t gx = t % ext.x, r = t / ext.x;
+        const uint32_t gy = r % ext.y, gz = r / ext.y;
+        const int px = (int)((gx + (uint32_t)rmin.x) & m) + 1;
+        const int py = (int)((gy + (uint32_t)rmin.y) & m) + 1 + level * A.rb;
+        const int pz = (int)((gz + (uint32_t)rmin.z) & m) + 1;
         for (int f = 0; f < faces; ++f) atlas[A.index(px + A.rb * f, py, pz)] = 0u;
     }
 }
@@ -43,26 +43,40 @@ __global__ void k_copy_alpha(uint32_t* __restrict__ dst, const uint32_t* __restr
 }
 
 // ---------------------------------------------------------------- border
-// borderWrapping.comp:14-37: invocations over ((R+2)>>3)*8 per axis; the
-// ones with a zero coordinate copy the toroidal neighbour into the border
-// for every clip level and face.
-__global__ void k_wrap_border(uint32_t* __restrict__ atlas, AtlasDims A, int rwb, int faces, int regions, int n) {
-    const int64_t total = (int64_t)n * n * n;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-        int x = (int)(t % n);
-        int64_t r = t / n;
-        int y = (int)(r % n);
-        int z = (int)(r / n);
-        if (x >= rwb || y >= rwb || z >= rwb) continue;
-        if (x < A.R + 1 && y < A.R + 1 && z < A.R + 1 && x > 0 && y > 0 && z > 0) continue;
-        const int m = A.R - 1;
-        int rx = ((x + A.R - 1) & m) + 1, ry = ((y + A.R - 1) & m) + 1, rz = ((z + A.R - 1) & m) + 1;
-        int wy = y;
-        for (int i = 0; i < regions; ++i) {
-            for (int j = 0; j < faces; ++j) atlas[A.index(x + rwb * j, wy, z)] = atlas[A.index(rx + rwb * j, ry, rz)];
-            ry += rwb;
-            wy += rwb;
+// borderWrapping.comp:14-37: the dispatch covers ((R+2)>>3)*8 = R
+// invocations per axis (R a power of two >= 8), and an invocation whose
+// position has a zero coordinate copies its toroidal interior neighbour into
+// that border texel, for every clip level and face; the R+1 side is never
+// reached.  One thread per (level, face, position of [0,R)^3 with a zero
+// coordinate): the z = 0 plane, then the y = 0 rows, then the x = 0 column,
+// x fastest where it varies.  Sources are interior texels, never written here.
+__global__ void k_wrap_border(uint32_t* __restrict__ atlas, AtlasDims A, int faces, int regions) {
+    // R <= 1024: (3R^2 - 3R + 1) * 36 < 2^27
+    const uint32_t R = (uint32_t)A.R, lg = 31u - __clz(A.R);
+    const uint32_t zf = R * R, yr = R * (R - 1u), shell = zf + yr + (R - 1u) * (R - 1u);
+    const uint32_t total = shell * (uint32_t)faces * (uint32_t)regions;
+    const int m = A.R - 1, W = A.R + 2;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        uint32_t s = t % shell;
+        const uint32_t fl = t / shell;
+        const int j = (int)(fl % (uint32_t)faces), i = (int)(fl / (uint32_t)faces);
+        int x, y, z;
+        if (s < zf) {
+            z = 0;
+            x = (int)(s & (R - 1u));
+            y = (int)(s >> lg);
+        } else if ((s -= zf) < yr) {
+            y = 0;
+            x = (int)(s & (R - 1u));
+            z = 1 + (int)(s >> lg);
+        } else {
+            s -= yr;
+            x = 0;
+            y = 1 + (int)(s % (R - 1u));
+            z = 1 + (int)(s / (R - 1u));
         }
+        const int rx = ((x + A.R - 1) & m) + 1, ry = ((y + A.R - 1) & m) + 1, rz = ((z + A.R - 1) & m) + 1;
+        atlas[A.index(x + W * j, y + W * i, z)] = atlas[A.index(rx + W * j, ry + W * i, rz)];
     }
 }
 
@@ -158,6 +172,87 @@ __global__ void k_downsample(uint32_t* __restrict__ atlas, AtlasDims A, int3 pmi
     }
 }
 
+// copyAlphaImage.comp then radianceDownSample.comp for one level l >= 1, in
+// one pass over the level's R^3 interior (x fastest), all faces: every texel
+// takes the opacity atlas's alpha, and the texels the downsample writes --
+// the (R/2)^3 block from the previous region's corner / 2 on, toroidally --
+// then blend the 2x2x2 composite of level l-1 with that updated texel exactly
+// as k_downsample<1> does.  Same result as the two passes in sequence.
+__global__ void k_alpha_downsample(uint32_t* __restrict__ rad, const uint32_t* __restrict__ opa, AtlasDims A,
+                                   int3 pmin, int level, int band, int lg) {
+    const int half = A.R >> 1;
+    const uint32_t n = 1u << (3 * lg), m = (1u << lg) - 1u;
+    const int pm[3] = {pmin.x, pmin.y, pmin.z};
+    const float inv = 1.0f / __fadd_rn((float)band, 1.0f);
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int w[3] = {(int)(t & m), (int)((t >> lg) & m), (int)(t >> (2 * lg))};
+        int cur[3], ps[3];
+        bool target = true;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const int g = (w[a] - (pm[a] >> 1)) & (A.R - 1);  // this texel's downsample thread, if g < R/2
+            target = target && g < half;
+            cur[a] = (pm[a] >> 1) + g;
+            ps[a] = ds_wrap(cur[a] << 1, A.R) + 1;
+        }
+        ps[1] += A.rb * (level - 1);
+        float lerp = 0.0f;
+        if (target) {  // lerpFactor (opacityDownSample.comp:55-64)
+            float dist[3];
+            bool any_ge = false;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                float center = __fadd_rn((float)(pm[a] >> 1), (float)(half >> 1));
+                dist[a] = __fsub_rn(fabsf(__fsub_rn(__fadd_rn((float)cur[a], 0.5f), center)), 0.5f);
+                any_ge |= dist[a] >= (float)((half >> 1) - band);
+            }
+            if (any_ge) {
+                lerp = __fadd_rn(__fsub_rn(fmaxf(dist[0], fmaxf(dist[1], dist[2])), (float)((half >> 1) - band)), 1.0f);
+                lerp = __fmul_rn(lerp, inv);
+            }
+        }
+        // all six faces' texels and alphas first (independent loads in flight)
+        const int64_t w0 = A.index(w[0] + 1, w[1] + 1 + A.rb * level, w[2] + 1);
+        uint32_t own6[6];
+#pragma unroll
+        for (int f = 0; f < 6; ++f)
+            own6[f] = (rad[w0 + A.rb * f] & 0x00ffffffu) | (__ldg(opa + w0 + A.rb * f) & 0xff000000u);
+        if (!target) {
+#pragma unroll
+            for (int f = 0; f < 6; ++f) rad[w0 + A.rb * f] = own6[f];
+            continue;
+        }
+#pragma unroll
+        for (int f = 0; f < 6; ++f) {
+            const int64_t wi = w0 + A.rb * f;
+            const uint32_t own_raw = own6[f];
+            uint32_t raw[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+                raw[i] = rad[A.index(ps[0] + (i & 1) + A.rb * f, ps[1] + ((i >> 1) & 1), ps[2] + ((i >> 2) & 1))];
+            float s[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const uint32_t r0 = raw[c_pairs[f][k][0]], r1 = raw[c_pairs[f][k][1]];
+                const float tt = __fsub_rn(1.0f, unorm8_load(r0, 3));
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    const float a0 = unorm8_load(r0, c);
+                    const float b = __fmul_rn(tt, unorm8_load(r1, c));
+                    s[c] = (k == 0) ? __fadd_rn(a0, b) : __fadd_rn(__fadd_rn(s[c], a0), b);
+                }
+            }
+            uint32_t out = 0;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const float res = __fmul_rn(s[c], 0.25f);
+                out |= unorm8_store(mix_rn(res, unorm8_load(own_raw, c), lerp)) << (8 * c);
+            }
+            rad[wi] = out;
+        }
+    }
+}
+
 static int grid_for(int64_t n, int block) {
     int64_t g = (n + block - 1) / block;
     if (g > 152 * 64) g = 152 * 64;
@@ -175,7 +270,8 @@ extern "C" int vct_clear_region(uint32_t* atlas, const vct_image_cleaning_desc* 
     VCT_CHECK_ARG(d->clip_level >= 0 && d->clip_level < VCT_CLIP_LEVEL_COUNT, "vct_clear_region: clip level out of range");
     VCT_CHECK_ARG(d->face_count <= VCT_FACE_COUNT, "vct_clear_region: face count > 6");
     for (int a = 0; a < 3; ++a) {
-        VCT_CHECK_ARG(d->region_min_corner[a] >= 0, "vct_clear_region: region min corner must be non-negative (wrap it first)");
+        VCT_CHECK_ARG(d->region_min_corner[a] >= 0 && d->region_min_corner[a] <= (1 << 30),
+                      "vct_clear_region: region min corner must be in [0, 2^30] (wrap it first)");
         VCT_CHECK_ARG(d->clip_max_extent[a] <= (uint32_t)d->clipmap_resolution, "vct_clear_region: extent > resolution");
     }
     AtlasDims A(d->clipmap_resolution);
@@ -212,10 +308,11 @@ extern "C" int vct_wrap_border(uint32_t* atlas, const vct_border_wrapping_desc* 
     VCT_CHECK_ARG(d->face_count <= VCT_FACE_COUNT && d->clip_region_count <= VCT_CLIP_LEVEL_COUNT,
                   "vct_wrap_border: face/region count out of range");
     AtlasDims A((int)d->clipmap_resolution);
-    const int n = ((A.R + 2) >> 3) * 8;
-    const int64_t total = (int64_t)n * n * n;
-    k_wrap_border<<<grid_for(total, 256), 256, 0, as_stream(stream)>>>(atlas, A, A.R + (int)d->clip_border_width,
-                                                                       (int)d->face_count, (int)d->clip_region_count, n);
+    if (d->face_count == 0 || d->clip_region_count == 0) return VCT_OK;
+    const int64_t shell = 3 * (int64_t)A.R * A.R - 3 * (int64_t)A.R + 1;  // ((R+2)>>3)*8 == R here
+    const int64_t total = shell * d->face_count * d->clip_region_count;
+    k_wrap_border<<<grid_for(total, 256), 256, 0, as_stream(stream)>>>(atlas, A, (int)d->face_count,
+                                                                       (int)d->clip_region_count);
     VCT_LAUNCH_CHECK();
     return VCT_OK;
 }
@@ -236,6 +333,26 @@ extern "C" int vct_downsample(uint32_t* atlas, const vct_downsample_desc* d, int
         k_downsample<0><<<grid_for(n, 128), 128, 0, as_stream(stream)>>>(atlas, A, pm, d->clip_level, d->downsample_region_size, lgh);
     else
         k_downsample<1><<<grid_for(n, 128), 128, 0, as_stream(stream)>>>(atlas, A, pm, d->clip_level, d->downsample_region_size, lgh);
+    VCT_LAUNCH_CHECK();
+    return VCT_OK;
+}
+
+extern "C" int vct_copy_alpha_downsample(uint32_t* radiance, const uint32_t* opacity, const vct_downsample_desc* d,
+                                         void* stream) {
+    VCT_CHECK_ARG(radiance && opacity && d, "vct_copy_alpha_downsample: null argument");
+    VCT_CHECK_ARG(radiance != opacity, "vct_copy_alpha_downsample: radiance and opacity atlases must differ");
+    VCT_CHECK_ARG(valid_resolution(d->clipmap_resolution),
+                  "vct_copy_alpha_downsample: resolution must be a power of two in [8,1024]");
+    VCT_CHECK_ARG(d->clip_level >= 1 && d->clip_level < VCT_CLIP_LEVEL_COUNT,
+                  "vct_copy_alpha_downsample: clip level must be 1..5");
+    VCT_CHECK_ARG(d->downsample_region_size >= 0 && d->downsample_region_size <= 4096,
+                  "vct_copy_alpha_downsample: downsample band out of range");
+    AtlasDims A(d->clipmap_resolution);
+    const int64_t n = (int64_t)A.R * A.R * A.R;
+    int3 pm = make_int3(d->prev_region_min_corner[0], d->prev_region_min_corner[1], d->prev_region_min_corner[2]);
+    const int lg = 31 - __builtin_clz((unsigned)A.R);
+    k_alpha_downsample<<<grid_for(n, 128), 128, 0, as_stream(stream)>>>(radiance, opacity, A, pm, d->clip_level,
+                                                                        d->downsample_region_size, lg);
     VCT_LAUNCH_CHECK();
     return VCT_OK;
 }

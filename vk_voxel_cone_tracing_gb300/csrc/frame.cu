@@ -7,6 +7,7 @@
 //   RSMPass                directional-light depth map
 //   RadianceInjectionPass  for each level due this frame (frame % 2^level == 0):
 //                          clear, inject; then copy-alpha and radiance mips
+//                          (levels 1..5: vct_copy_alpha_downsample, one pass)
 //
 // Host-side orchestration only: every step is one of the C-ABI passes, run
 // on the caller's stream.
@@ -54,9 +55,13 @@ extern "C" int vct_clipmap_frame(const vct_scene* scene, const vct_frame_desc* f
     if ((rc = vct_inject_radiance(scene, regions, R, &sm, &f->light, &f->light_shadow, radiance, due, f->inject_mode,
                                   ws, stream)) != VCT_OK)
         return rc;
-    for (int l = 0; l < 6; ++l) {
-        if (!((due >> l) & 1u)) continue;
-        vct_copy_alpha_desc ca = {l, R, VCT_FACE_COUNT};
+    // copy-alpha of every due level, then the radiance mips 1..5 of the due
+    // levels; a due level's predecessor is always due (frame % 2^l == 0), so
+    // level 0 takes the plain copy and levels 1..5 the fused copy + mip pass,
+    // each after its predecessor is final -- the same result as all copies
+    // first and the mips after.
+    if (due & 1u) {
+        vct_copy_alpha_desc ca = {0, R, VCT_FACE_COUNT};
         if ((rc = vct_copy_alpha(radiance, opacity, &ca, stream)) != VCT_OK) return rc;
     }
     for (int l = 1; l < 6; ++l) {
@@ -66,7 +71,7 @@ extern "C" int vct_clipmap_frame(const vct_scene* scene, const vct_frame_desc* f
         d.clip_level = l;
         d.clipmap_resolution = R;
         d.downsample_region_size = VCT_DOWNSAMPLE_REGION_SIZE;
-        if ((rc = vct_downsample(radiance, &d, VCT_DOWNSAMPLE_RADIANCE, stream)) != VCT_OK) return rc;
+        if ((rc = vct_copy_alpha_downsample(radiance, opacity, &d, stream)) != VCT_OK) return rc;
     }
     return VCT_OK;
 }

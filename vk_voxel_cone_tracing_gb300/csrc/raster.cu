@@ -509,11 +509,25 @@ struct TilePlan {
     uint32_t total;             // tiles
 };
 
-// Item of every tile: item i owns tiles [tile_end[i-1], tile_end[i]).
+// Item of every tile: item i owns tiles [tile_end[i-1], tile_end[i]).  A warp
+// takes 32 items; a lane writes its own item's tiles when there are at most
+// eight, and the warp writes the larger items' together, so an item with
+// thousands of tiles (a floor quad in a 2048^2 shadow map) is spread over the
+// lanes.
 __global__ void k_tile_items(const uint32_t* __restrict__ tile_end, int64_t items, uint32_t* __restrict__ tile_item) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < items; i += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t b = i > 0 ? tile_end[i - 1] : 0u, e = tile_end[i];
-        for (uint32_t g = b; g < e; ++g) tile_item[g] = (uint32_t)i;
+    const int lane = threadIdx.x & 31;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t base = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; base < items; base += nwarps * 32) {
+        const int64_t i = base + lane;
+        const uint32_t e_i = i < items ? tile_end[i] : 0u;
+        const uint32_t b_i = i < items ? (i > 0 ? tile_end[i - 1] : 0u) : 0u;
+        if (e_i - b_i <= 8u)
+            for (uint32_t g = b_i; g < e_i; ++g) tile_item[g] = (uint32_t)i;
+        for (unsigned big = __ballot_sync(0xffffffffu, e_i - b_i > 8u); big; big &= big - 1u) {
+            const int j = __ffs(big) - 1;
+            const uint32_t b = __shfl_sync(0xffffffffu, b_i, j), e = __shfl_sync(0xffffffffu, e_i, j);
+            for (uint32_t g = b + (uint32_t)lane; g < e; g += 32u) tile_item[g] = (uint32_t)(base + j);
+        }
     }
 }
 

@@ -300,16 +300,18 @@ __device__ __forceinline__ ConeStep over(const ConeStep& p, const ConeStep& q) {
     return ConeStep{fmaf(k, q.r, p.r), fmaf(k, q.g, p.g), fmaf(k, q.b, p.b), fmaf(k, q.a, p.a), p.t * q.t};
 }
 
-// One cone marched by a whole warp, 64 steps per round: lane j takes steps
-// 2j and 2j + 1 of the round.  The step schedule (step, diameter, segment
-// length) depends only on the step index, not on the samples, and has a
-// closed form (below), so every lane finds its own steps directly.  The
+// One cone marched by a whole warp, 32 * S steps per round: lane j takes
+// steps S j .. S j + S - 1 of the round.  The step schedule (step, diameter,
+// segment length) depends only on the step index, not on the samples, and
+// has a closed form (below), so every lane finds its own steps directly.  The
 // front-to-back composite result += (1 - result.a) * src is the associative
 // "over" operator and 1 - occlusion is the product of (1 - x_k): each lane
-// composes its two steps, a warp scan composes the lanes.  The march stops at
+// composes its S steps, a warp scan composes the lanes.  The march stops at
 // the first step whose occlusion reaches 1 or whose distance reaches
-// maxDistance, like the loop: the lane holding that step re-applies its own
-// steps from the state before it.
+// maxDistance, like the loop.  Transmittance only falls, so the first lane
+// whose composite reaches occlusion 1 holds that step; it marches its steps
+// again from the state before them to stop exactly there (once per cone).
+template <int S>
 __device__ __forceinline__ float4 trace_cone_warp(cudaTextureObject_t tex, const FastConsts& C, float3 start,
                                                   float3 dir, float coef, float start_level, float step_factor,
                                                   unsigned long long& steps) {
@@ -336,21 +338,26 @@ __device__ __forceinline__ float4 trace_cone_warp(cudaTextureObject_t tex, const
         const float K = st <= T ? floorf((T - st) / u) + 1.0f : 0.0f;
         const float sK = fmaf(K, u, st);
         auto st_at = [&](float jf) { return jf <= K ? fmaf(jf, u, st) : sK * exp2f((jf - K) * lr); };
-        const float j0 = (float)(2 * lane);
-        const float s0 = st_at(j0), s1 = st_at(j0 + 1.0f);
-        const float dm0 = lane == 0 ? dm : s0 * coef, sg0 = lane == 0 ? sg : s0 - st_at(j0 - 1.0f);
-        const bool v0 = s0 < kMaxTraceDistance, v1 = s1 < kMaxTraceDistance;
-        ConeStep a = id, b = id;
-        if (v0) a = cone_step(tex, C, start, dir, fox, foy, foz, wt, start_level, s0, dm0, sg0);
-        if (v1) b = cone_step(tex, C, start, dir, fox, foy, foz, wt, start_level, s1, s1 * coef, s1 - s0);
-        {  // the schedule at the next round's first step
-            const float s63 = st_at(63.0f), s64 = st_at(64.0f);
-            st = s64;
-            sg = s64 - s63;
-            dm = s64 * coef;
+        const float j0 = (float)(S * lane);
+        // march this lane's steps: composite, count of valid steps
+        ConeStep x = id;
+        int nvalid = 0;
+        {
+            float prev = lane == 0 ? 0.0f : st_at(j0 - 1.0f);
+#pragma unroll
+            for (int k = 0; k < S; ++k) {
+                const float sk = st_at(j0 + (float)k);
+                if (sk < kMaxTraceDistance) {
+                    const bool first = lane == 0 && k == 0;
+                    x = over(x, cone_step(tex, C, start, dir, fox, foy, foz, wt, start_level, sk,
+                                          first ? dm : sk * coef, first ? sg : sk - prev));
+                    ++nvalid;
+                }
+                prev = sk;
+            }
         }
-        // inclusive warp scan of the lanes' two-step composites
-        ConeStep x = over(a, b);
+        const float s_last = st_at(32.0f * S - 1.0f), s_next = st_at(32.0f * S);
+        // inclusive warp scan of the lanes' composites
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             ConeStep p;
@@ -361,42 +368,59 @@ __device__ __forceinline__ float4 trace_cone_warp(cudaTextureObject_t tex, const
             p.t = __shfl_up_sync(0xffffffffu, x.t, o);
             if (lane >= o) x = over(p, x);
         }
-        // the state before this lane's steps, and after each of them
-        ConeStep before;
-        before.r = __shfl_up_sync(0xffffffffu, x.r, 1);
-        before.g = __shfl_up_sync(0xffffffffu, x.g, 1);
-        before.b = __shfl_up_sync(0xffffffffu, x.b, 1);
-        before.a = __shfl_up_sync(0xffffffffu, x.a, 1);
-        before.t = __shfl_up_sync(0xffffffffu, x.t, 1);
-        before = lane == 0 ? carried : over(carried, before);
-        const ConeStep after0 = over(before, a), after1 = over(after0, b);
-        const bool t0 = v0 && (1.0f - after0.t) >= 1.0f, t1 = v1 && (1.0f - after1.t) >= 1.0f;
-        const unsigned tmask = __ballot_sync(0xffffffffu, t0 || t1);
-        const unsigned vmask = __ballot_sync(0xffffffffu, v0);  // a prefix of lanes (the step grows)
-        if (tmask) {  // occlusion reached 1: stop after the first such step
+        const ConeStep after = over(carried, x);
+        const unsigned tmask = __ballot_sync(0xffffffffu, nvalid > 0 && (1.0f - after.t) >= 1.0f);
+        if (tmask) {  // occlusion reaches 1 within lane L's steps: stop after that step
             const int L = __ffs(tmask) - 1;
-            const bool first = __shfl_sync(0xffffffffu, t0, L);
-            const ConeStep f = first ? after0 : after1;
-            carried.r = __shfl_sync(0xffffffffu, f.r, L);
-            carried.g = __shfl_sync(0xffffffffu, f.g, L);
-            carried.b = __shfl_sync(0xffffffffu, f.b, L);
-            carried.t = __shfl_sync(0xffffffffu, f.t, L);
-            it += (unsigned long long)(2 * L + (first ? 1 : 2));
+            ConeStep before;
+            before.r = __shfl_up_sync(0xffffffffu, x.r, 1);
+            before.g = __shfl_up_sync(0xffffffffu, x.g, 1);
+            before.b = __shfl_up_sync(0xffffffffu, x.b, 1);
+            before.a = __shfl_up_sync(0xffffffffu, x.a, 1);
+            before.t = __shfl_up_sync(0xffffffffu, x.t, 1);
+            int done = 0;
+            if (lane == L) {
+                ConeStep y = lane == 0 ? carried : over(carried, before);
+                float prev = lane == 0 ? 0.0f : st_at(j0 - 1.0f);
+                for (int k = 0; k < S; ++k) {
+                    const float sk = st_at(j0 + (float)k);
+                    const bool first = lane == 0 && k == 0;
+                    y = over(y, cone_step(tex, C, start, dir, fox, foy, foz, wt, start_level, sk,
+                                          first ? dm : sk * coef, first ? sg : sk - prev));
+                    prev = sk;
+                    done = k + 1;
+                    if ((1.0f - y.t) >= 1.0f) break;
+                }
+                carried = y;
+            }
+            carried.r = __shfl_sync(0xffffffffu, carried.r, L);
+            carried.g = __shfl_sync(0xffffffffu, carried.g, L);
+            carried.b = __shfl_sync(0xffffffffu, carried.b, L);
+            carried.t = __shfl_sync(0xffffffffu, carried.t, L);
+            it += (unsigned long long)(S * L + __shfl_sync(0xffffffffu, done, L));
             break;
         }
-        const unsigned v1mask = __ballot_sync(0xffffffffu, v1);
         // invalid steps are the identity: the round's total is lane 31's prefix
-        carried.r = __shfl_sync(0xffffffffu, after1.r, 31);
-        carried.g = __shfl_sync(0xffffffffu, after1.g, 31);
-        carried.b = __shfl_sync(0xffffffffu, after1.b, 31);
-        carried.a = __shfl_sync(0xffffffffu, after1.a, 31);
-        carried.t = __shfl_sync(0xffffffffu, after1.t, 31);
-        it += (unsigned long long)(__popc(vmask) + __popc(v1mask));
-        if (v1mask != 0xffffffffu) break;  // maxDistance reached within the round
+        carried.r = __shfl_sync(0xffffffffu, after.r, 31);
+        carried.g = __shfl_sync(0xffffffffu, after.g, 31);
+        carried.b = __shfl_sync(0xffffffffu, after.b, 31);
+        carried.a = __shfl_sync(0xffffffffu, after.a, 31);
+        carried.t = __shfl_sync(0xffffffffu, after.t, 31);
+        int nv = nvalid;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) nv += __shfl_xor_sync(0xffffffffu, nv, o);
+        it += (unsigned long long)nv;
+        if (nv < 32 * S) break;  // maxDistance reached within the round
+        st = s_next;
+        sg = s_next - s_last;
+        dm = s_next * coef;
     }
     if (lane == 0) steps += it;
     return make_float4(carried.r, carried.g, carried.b, carried.t);
 }
+
+// Consecutive steps of one specular cone per lane.
+constexpr int kSpecStepsPerLane = 2;
 
 // One warp per specular cone of the list (the list is kept in Morton order).
 __global__ void __launch_bounds__(256, 4) k_trace_specular_warp(const __grid_constant__ FastArgs A, const uint32_t* __restrict__ list,
@@ -416,7 +440,7 @@ __global__ void __launch_bounds__(256, 4) k_trace_specular_warp(const __grid_con
         const float3 sdir = reflect3(f3(-g.view.x, -g.view.y, -g.view.z), g.normal);
         const float ap = fmaxf(g.roughness, kMinSpecularAperture);
         const float coef = 2.0f * tanf(ap * 0.5f);
-        const float4 r = trace_cone_warp(A.tex, C, start, sdir, coef, min_level, C.uvs, steps);
+        const float4 r = trace_cone_warp<kSpecStepsPerLane>(A.tex, C, start, sdir, coef, min_level, C.uvs, steps);
         if (lane == 0) {
             const float isi = P.d.indirect_specular_intensity;
             reinterpret_cast<float4*>(A.sout)[idx] =
@@ -428,6 +452,58 @@ __global__ void __launch_bounds__(256, 4) k_trace_specular_warp(const __grid_con
         for (int o = 16; o > 0; o >>= 1) steps += __shfl_xor_sync(0xffffffffu, steps, o);
         if (lane == 0 && steps) atomicAdd(A.steps, steps);
     }
+}
+
+// ------------------------------------------------------------- gather probe
+// The trace's speed of light: one warp per synthetic cone, consecutive steps
+// on consecutive lanes half a level-0 voxel apart (the specular kernel's
+// access pattern), and at every step exactly the fetches a cone sample needs
+// -- three face taps at two adjacent levels through sample_level -- with no
+// compositing, lighting or scans.  Cones start within two level-0 voxels of
+// the volume centre with hashed directions and cycle through the level
+// pairs, so the taps are served by L1/TEX: the rate is the texture pipe's,
+// an upper bound for the trace (which always does at least three of the six
+// fetches and all of its other work on top).
+__device__ __forceinline__ uint32_t probe_hash(uint32_t x) {
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+
+__global__ void __launch_bounds__(256) k_gather_probe(const __grid_constant__ FastArgs A, int64_t cones, int steps,
+                                                      float* __restrict__ out) {
+    const FastConsts& C = A.C;
+    const int lane = threadIdx.x & 31;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const float ext0 = 2.0f * C.uvs;
+    float acc = 0.0f;
+    for (int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < cones; c += nwarps) {
+        const uint32_t h0 = probe_hash((uint32_t)c * 3u + 1u), h1 = probe_hash((uint32_t)c * 3u + 2u),
+                       h2 = probe_hash((uint32_t)c * 3u + 3u);
+        const float3 start = f3(C.cx + ((float)(h0 & 0xffffu) * (1.0f / 65536.0f) - 0.5f) * ext0,
+                                C.cy + ((float)(h0 >> 16) * (1.0f / 65536.0f) - 0.5f) * ext0,
+                                C.cz + ((float)(h1 & 0xffffu) * (1.0f / 65536.0f) - 0.5f) * ext0);
+        float3 dir = f3((float)(h1 >> 16) - 32768.0f, (float)(h2 & 0xffffu) - 32768.0f, (float)(h2 >> 16) - 32768.0f);
+        const float inv = rsqrtf(fmaxf(dot3(dir, dir), 1.0f));
+        dir = f3(dir.x * inv, dir.y * inv, dir.z * inv);
+        const int lo = (int)(c % (kClipLevels - 1));
+        const float fox = dir.x > 0.0f ? 0.0f : 1.0f / 6.0f;
+        const float foy = dir.y > 0.0f ? 2.0f / 6.0f : 3.0f / 6.0f;
+        const float foz = dir.z > 0.0f ? 4.0f / 6.0f : 5.0f / 6.0f;
+        const float3 wt = f3(dir.x * dir.x, dir.y * dir.y, dir.z * dir.z);
+        const float step = 0.5f * C.uvs;
+        for (int k = lane; k < steps; k += 32) {
+            const float d = step * (float)k;
+            const float3 pos = f3(fmaf(dir.x, d, start.x), fmaf(dir.y, d, start.y), fmaf(dir.z, d, start.z));
+            const float4 a = sample_level(A.tex, C, pos, lo, fox, foy, foz, wt);
+            const float4 b = sample_level(A.tex, C, pos, lo + 1, fox, foy, foz, wt);
+            acc += (a.x + a.w) + (b.y + b.w);
+        }
+    }
+    out[(int64_t)blockIdx.x * blockDim.x + threadIdx.x] = acc;
 }
 
 // ------------------------------------------------------------- scratch layout
@@ -565,4 +641,43 @@ extern "C" int vct_cone_trace_fast(const vct_cone_tracing_desc* desc, const vct_
         VCT_LAUNCH_CHECK();
     }
     return VCT_OK;
+}
+
+extern "C" int vct_gather_probe(const vct_cone_tracing_desc* desc, vct_texture_s* radiance, int64_t cones,
+                                int32_t steps_per_cone, double* samples_per_second, void* stream) {
+    VCT_CHECK_ARG(desc && radiance && samples_per_second, "vct_gather_probe: null argument");
+    VCT_CHECK_ARG(cones > 0 && cones <= (1LL << 30) && steps_per_cone > 0 && steps_per_cone <= (1 << 20),
+                  "vct_gather_probe: cone or step count out of range");
+    VCT_CHECK_ARG((float)texture_resolution(radiance) == desc->volume_dimension,
+                  "vct_gather_probe: volume dimension differs from the texture's clipmap resolution");
+    FastArgs A;
+    memset(&A, 0, sizeof(A));
+    fill_fast_consts(A.C, *desc);
+    A.tex = texture_object(radiance);
+    cudaStream_t st = as_stream(stream);
+    const int block = 256, grid = 152 * 8;
+    float* out = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int rc = VCT_OK;
+    float ms = 0.0f;
+    cudaError_t err = cudaMalloc(&out, sizeof(float) * (size_t)grid * block);
+    if (err == cudaSuccess) err = cudaEventCreate(&e0);
+    if (err == cudaSuccess) err = cudaEventCreate(&e1);
+    if (err == cudaSuccess) {
+        k_gather_probe<<<grid, block, 0, st>>>(A, cones, steps_per_cone, out);  // warm-up
+        err = cudaEventRecord(e0, st);
+    }
+    if (err == cudaSuccess) {
+        k_gather_probe<<<grid, block, 0, st>>>(A, cones, steps_per_cone, out);
+        err = cudaGetLastError();
+    }
+    if (err == cudaSuccess) err = cudaEventRecord(e1, st);
+    if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+    if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+    if (err != cudaSuccess) rc = cuda_fail(err, "vct_gather_probe");
+    else *samples_per_second = (double)cones * (double)steps_per_cone / ((double)ms * 1e-3);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (out) cudaFree(out);
+    return rc;
 }
