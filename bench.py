@@ -280,6 +280,8 @@ def run_ours(args, world, rank, local):
     value = cone_samples * world / (ms * 1e-3)
     # the trace's speed of light: the same fetches per cone sample with nothing else (vct_gather_probe)
     gather_peak = clipmap.gather_probe(desc, tex) if tex is not None else None
+    # the clipmap -> texture array copy inside each trace step, on its own
+    refresh_ms = statistics.median(events_ms(stream, lambda: tex.update(tex_src), 5)[0]) if tex is not None else None
 
     # voxelise + shadow + inject + mips of one frame, and the SVO build at 256^3
     for _ in range(2):
@@ -354,6 +356,7 @@ def run_ours(args, world, rank, local):
                                    "1920x1080 G-buffer samples, 16 diffuse + 1 specular cone + VXAO",
                        "form": args.form, "R": R, "samples_per_step": n, "cone_samples_per_step": cone_samples,
                        "l2": "inputs larger than L2 (2.47 GB clipmap)",
+                       "texture_refresh_ms": refresh_ms,
                        "voxelize_inject_mip_ms": frame_ms, "svo_ms": svo_ms, "svo_level": SVO_LEVEL,
                        "svo_fragments": int(frags.shape[0]), "svo_nodes": int(nodes.value),
                        "voxelize_svo_mip_ms": frame_ms + svo_ms},
