@@ -234,8 +234,14 @@ def run_ours(args, world, rank, local):
     lsd = passes.light_shadow_desc(light_origin(), LIGHT_DIR)
     stream = torch.cuda.current_stream()
 
+    # the RGBA8 texture form samples a texture that the frame keeps equal to the radiance atlas (the frame's
+    # copy-alpha and mip passes store each texel into it too); the FP16 form refreshes its own texture
+    tex = clipmap.RadianceTexture(R, capi.TEX_RGBA8 if args.form != "fp16" else capi.TEX_RGBA16F) \
+        if args.form in ("tex", "fp16") else None
+    frame_tex = tex if args.form == "tex" else None
+
     def frame():
-        return passes.clipmap_frame(ds, CAMERA, R, opacity, radiance, shadow, light, lsd, ws)
+        return passes.clipmap_frame(ds, CAMERA, R, opacity, radiance, shadow, light, lsd, ws, texture=frame_tex)
 
     regs = frame()
     torch.cuda.synchronize()
@@ -247,12 +253,11 @@ def run_ours(args, world, rank, local):
     dout = torch.empty((n, 4), dtype=torch.float32, device=dev)
     sout = torch.empty((n, 4), dtype=torch.float32, device=dev)
     steps_ctr = torch.zeros(1, dtype=torch.int64, device=dev)
-    tex, tex_src, scratch = None, radiance, None
-    if args.form in ("tex", "fp16"):
+    tex_src, scratch = radiance, None
+    if tex is not None:
         if args.form == "fp16":
             tex_src = clipmap.to_rgba16f(radiance, R)
             clipmap.cmd_downsample_rgba16f_all(tex_src, R, regs, 1)
-        tex = clipmap.RadianceTexture(R, capi.TEX_RGBA8 if args.form == "tex" else capi.TEX_RGBA16F)
         scratch = clipmap.fast_scratch(n, dev)
 
     def trace(inp, counter=None):
@@ -260,7 +265,8 @@ def run_ours(args, world, rank, local):
             clipmap.cone_trace(desc, EYE, radiance, R, inp, light=light, shadow=shadow, shadow_desc=lsd,
                                diffuse=dout, specular=sout, steps=counter)
         else:
-            tex.update(tex_src)  # the texture copy of the clipmap is refreshed every step
+            if frame_tex is None:
+                tex.update(tex_src)  # FP16 form: its texture is refreshed from the FP16 atlas every step
             clipmap.cone_trace_fast(desc, EYE, tex, inp, light=light, shadow=shadow, shadow_desc=lsd, diffuse=dout,
                                     specular=sout, steps=counter, scratch=scratch)
 
@@ -280,8 +286,10 @@ def run_ours(args, world, rank, local):
     value = cone_samples * world / (ms * 1e-3)
     # the trace's speed of light: the same fetches per cone sample with nothing else (vct_gather_probe)
     gather_peak = clipmap.gather_probe(desc, tex) if tex is not None else None
-    # the clipmap -> texture array copy inside each trace step, on its own
+    # what a full clipmap -> texture array copy (vct_texture_update) costs; the RGBA8 form needs none per step
     refresh_ms = statistics.median(events_ms(stream, lambda: tex.update(tex_src), 5)[0]) if tex is not None else None
+    if frame_tex is not None:
+        frame()  # the measurement above overwrote the texture with the same atlas; keep the frame's state
 
     # voxelise + shadow + inject + mips of one frame, and the SVO build at 256^3
     for _ in range(2):
@@ -344,9 +352,10 @@ def run_ours(args, world, rank, local):
             cpu = {"value": rate, "unit": "cone samples/s", "cores": cores, "kind": "port",
                    "sample": f"first {ncpu} of {n} samples ({st} cone samples, {dt:.1f} s) traced by the FP32 C++ "
                              "restatement on the same clipmap"}
-        # kernels launched per trace step: texture copy (memcpy), Morton keys, 2 cub radix sorts
-        # (histogram + scan + 4 onesweep passes for 30 bits, 2 for 9 bits), diffuse, specular
-        launches = 1 if tex is None else 12
+        # kernels launched per trace step: Morton keys, cub radix sort of 30 bits (histogram, exclusive sum,
+        # 4 onesweep passes), specular keys, cub radix pass on 1 bit (histogram, exclusive sum, onesweep),
+        # diffuse, specular (the texture refresh is a memcpy, not a kernel)
+        launches = 1 if tex is None else 13
         line = {
             "metric": METRIC, "value": value, "unit": "cone samples/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -356,7 +365,9 @@ def run_ours(args, world, rank, local):
                                    "1920x1080 G-buffer samples, 16 diffuse + 1 specular cone + VXAO",
                        "form": args.form, "R": R, "samples_per_step": n, "cone_samples_per_step": cone_samples,
                        "l2": "inputs larger than L2 (2.47 GB clipmap)",
-                       "texture_refresh_ms": refresh_ms,
+                       "texture_full_copy_ms": refresh_ms,
+                       "texture": "kept current by the frame's copy-alpha and mip passes" if frame_tex is not None
+                       else ("refreshed by a full copy every trace step" if tex is not None else "none (linear atlas)"),
                        "voxelize_inject_mip_ms": frame_ms, "svo_ms": svo_ms, "svo_level": SVO_LEVEL,
                        "svo_fragments": int(frags.shape[0]), "svo_nodes": int(nodes.value),
                        "voxelize_svo_mip_ms": frame_ms + svo_ms},
@@ -370,7 +381,8 @@ def run_ours(args, world, rank, local):
                 "frac": cone_samples / (statistics.mean(per) * 1e-3) / gather_peak,
                 "note": "peak = vct_gather_probe: the texture fetches of one cone sample (3 faces x 2 levels, "
                         "trilinear) per step of warp-coherent synthetic cones, measured on this GPU with the same "
-                        "texture; achieved = the whole trace step (sort, diffuse and specular kernels, texture refresh)"},
+                        "texture; achieved = the whole trace step (Morton sort, specular partition, diffuse and "
+                        "specular kernels)"},
             "cpu_baseline": cpu,
             "e2e": {"value": cone_samples * world / (e2e_ms * 1e-3), "unit": "cone samples/s",
                     "h2d_bytes_per_step": int(samples.numel() * 4),

@@ -223,6 +223,8 @@ int vct_clip_regions(const float camera_pos_host[3], int32_t clipmap_resolution,
 
 /* ------------------------------------------------------- clipmap passes */
 
+struct vct_texture_s; /* the radiance texture handle (see vct_texture_create) */
+
 /* ClipmapCleaner::cmdClear{Opacity,Radiance}ClipRegion
  * (VFS/RenderPass/Clipmap/ClipmapCleaner.cpp:93-133, clipmapCleaning.comp):
  * zero `face_count` faces of a toroidal region of one level. */
@@ -251,10 +253,11 @@ int vct_downsample_all(uint32_t* atlas, const vct_clipmap_region regions_host[6]
  * vct_downsample(radiance, desc, VCT_DOWNSAMPLE_RADIANCE) for the same level
  * l >= 1 (RadianceInjectionPass's CopyAlpha then DownSampler::cmdDownSampleRadiance,
  * RadianceInjectionPass.cpp:134-159), fused into one pass over the level; the
- * result is bit-identical to the two calls in sequence.  No single-pass
- * counterpart in the reference. */
+ * result is bit-identical to the two calls in sequence.  `mirror` (may be
+ * NULL): an RGBA8 texture of the same resolution that receives every texel
+ * the pass writes.  No single-pass counterpart in the reference. */
 int vct_copy_alpha_downsample(uint32_t* radiance_atlas, const uint32_t* opacity_atlas,
-                              const vct_downsample_desc* desc, void* stream);
+                              const vct_downsample_desc* desc, struct vct_texture_s* mirror, void* stream);
 
 /* BorderWrapper::cmdWrappingOpacityBorder (VFS/RenderPass/Clipmap/BorderWrapper.cpp:123-151,
  * borderWrapping.comp): copy toroidal neighbours into border texels. */
@@ -280,13 +283,18 @@ int vct_cone_trace(const vct_cone_tracing_desc* desc, const vct_cam_matrix* cam,
 /* A hardware-filtered copy of a radiance atlas: a 3D CUDA array with
  * normalized coordinates, WRAP addressing and linear filtering (the
  * reference's VoxelSampler, VFS/RenderPass/Clipmap/Voxelizer.cpp:279).
- * vct_texture_create allocates the array (W x H x D texels of 4 or 8 B);
- * vct_texture_update copies a linear atlas of the texture's format into it. */
+ * vct_texture_create allocates the array (W x H x D texels of 4 or 8 B) and
+ * zeroes it (synchronises the device); vct_texture_update copies a linear
+ * atlas of the texture's format into it; vct_texture_read copies it back
+ * into a linear atlas.  An RGBA8 texture can also be kept current without
+ * copies: the frame (vct_frame_desc.radiance_texture) and
+ * vct_copy_alpha_downsample write every texel they produce into it too. */
 typedef struct vct_texture_s* vct_texture;
 #define VCT_TEX_RGBA8 0
 #define VCT_TEX_RGBA16F 1
 int vct_texture_create(int32_t clipmap_resolution, int32_t format, vct_texture* out);
 int vct_texture_update(vct_texture tex, const void* atlas, void* stream);
+int vct_texture_read(const struct vct_texture_s* tex, void* atlas, void* stream);
 int vct_texture_destroy(vct_texture tex);
 
 /* FP16-storage form of the radiance clipmap (4 halves per texel, same
@@ -452,7 +460,7 @@ int vct_svo_cone_trace(const vct_cone_tracing_desc* desc, const vct_cam_matrix* 
  * drives): camera position (clip regions), clipmap resolution, frame index
  * (radiance levels are refreshed every 2^level frames), injection mode,
  * directional light with its shadow projection, shadow-map size (0 = no
- * shadow pass: visibility 1). */
+ * shadow pass: visibility 1), and the radiance texture to keep current. */
 typedef struct vct_frame_desc {
     float camera_pos[3];
     int32_t clipmap_resolution;
@@ -462,6 +470,9 @@ typedef struct vct_frame_desc {
     int32_t shadow_height;
     vct_directional_light_desc light;
     vct_directional_light_shadow_desc light_shadow;
+    struct vct_texture_s* radiance_texture; /* may be NULL: an RGBA8 texture of the same resolution that
+                                               receives every radiance texel the frame's copy-alpha and
+                                               mip passes write (the texture the fast trace samples) */
 } vct_frame_desc;
 
 /* Application::run's pre-pass sequence (VFS/Application.cpp:142-201):

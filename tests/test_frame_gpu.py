@@ -72,3 +72,38 @@ def test_clipmap_frame_bit_exact(cuda, oracle, R):
         rel = np.linalg.norm(got - want) / max(np.linalg.norm(want), 1e-12)
         assert rel < 1e-2, rel
     tex.close()
+
+
+def test_frame_keeps_the_radiance_texture_equal_to_the_atlas(cuda):
+    """With vct_frame_desc.radiance_texture set, the frame's copy-alpha and mip
+    passes also store their texels into the texture: after a full frame and
+    after a frame that refreshes level 0 only (frame_index 1), the texture read
+    back equals the radiance atlas on every texel, borders included."""
+    torch = cuda
+    from vk_voxel_cone_tracing_gb300 import clipmap, passes
+    from vk_voxel_cone_tracing_gb300.scene import room_scene
+    R = 32
+    scene = room_scene(seed=2, n_random=2000)
+    ds = passes.DeviceScene(scene)
+    ws = passes.Workspace()
+    op, rad = clipmap.new_atlas(R), clipmap.new_atlas(R)
+    sh = torch.empty((256, 256), dtype=torch.float32, device="cuda")
+    tex = clipmap.RadianceTexture(R)
+    back = clipmap.new_atlas(R)
+    for frame_index, cam in ((0, CAM), (1, (CAM[0] + 0.7, CAM[1], CAM[2] - 0.4))):
+        passes.clipmap_frame(ds, cam, R, op, rad, sh, passes.light_desc(LIGHT_DIR),
+                             passes.light_shadow_desc(_origin(), LIGHT_DIR), ws, frame_index=frame_index,
+                             texture=tex)
+        tex.read(back)
+        torch.cuda.synchronize()
+        a = rad.cpu().numpy().view(np.uint32)
+        b = back.cpu().numpy().view(np.uint32)
+        assert np.count_nonzero(a) > 1000
+        assert np.array_equal(a, b), f"frame {frame_index}: {np.count_nonzero(a != b)} texels differ"
+    # a texture of another resolution is refused before any work
+    other = clipmap.RadianceTexture(16)
+    with pytest.raises(RuntimeError, match="radiance texture"):
+        passes.clipmap_frame(ds, CAM, R, op, rad, sh, passes.light_desc(LIGHT_DIR),
+                             passes.light_shadow_desc(_origin(), LIGHT_DIR), ws, texture=other)
+    tex.close()
+    other.close()

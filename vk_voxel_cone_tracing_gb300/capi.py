@@ -119,7 +119,8 @@ class Scene(C.Structure):
 class FrameDesc(C.Structure):
     _fields_ = [("camera_pos", f3), ("clipmap_resolution", C.c_int32), ("frame_index", C.c_int32),
                 ("inject_mode", C.c_int32), ("shadow_width", C.c_int32), ("shadow_height", C.c_int32),
-                ("light", DirectionalLightDesc), ("light_shadow", DirectionalLightShadowDesc)]
+                ("light", DirectionalLightDesc), ("light_shadow", DirectionalLightShadowDesc),
+                ("radiance_texture", C.c_void_p)]
 
 
 class ShadowMap(C.Structure):
@@ -142,12 +143,13 @@ _SIGS: dict[str, tuple] = {
     "vct_clear_region": (C.c_int, [P, P, P]),
     "vct_copy_alpha": (C.c_int, [P, P, P, P]),
     "vct_downsample": (C.c_int, [P, P, C.c_int32, P]),
-    "vct_copy_alpha_downsample": (C.c_int, [P, P, P, P]),
+    "vct_copy_alpha_downsample": (C.c_int, [P, P, P, P, P]),
     "vct_downsample_all": (C.c_int, [P, P, C.c_int32, C.c_int32, P]),
     "vct_wrap_border": (C.c_int, [P, P, P]),
     "vct_cone_trace": (C.c_int, [P, P, P, C.c_int32, P, P, P, P, C.c_int64, P, P, P, P]),
     "vct_texture_create": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     "vct_texture_update": (C.c_int, [P, P, P]),
+    "vct_texture_read": (C.c_int, [P, P, P]),
     "vct_texture_destroy": (C.c_int, [P]),
     "vct_atlas_rgba8_to_rgba16f": (C.c_int, [P, P, C.c_int32, P]),
     "vct_downsample_rgba16f": (C.c_int, [P, P, C.c_int32, P]),

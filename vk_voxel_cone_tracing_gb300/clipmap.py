@@ -65,10 +65,12 @@ def cmd_downsample(atlas: torch.Tensor, R: int, prev_region_min, level: int, mod
 
 
 def cmd_copy_alpha_downsample(radiance: torch.Tensor, opacity: torch.Tensor, R: int, prev_region_min, level: int,
-                              band: int = capi.DOWNSAMPLE_REGION_SIZE) -> None:
-    """vct_copy_alpha (level) + vct_downsample (radiance, level) fused into one pass."""
+                              band: int = capi.DOWNSAMPLE_REGION_SIZE, mirror=None) -> None:
+    """vct_copy_alpha (level) + vct_downsample (radiance, level) fused into one pass; `mirror` (a
+    RadianceTexture) receives every texel written."""
     d = capi.DownSampleDesc(capi.i3(*prev_region_min), level, R, band)
-    capi.call("vct_copy_alpha_downsample", _ptr(radiance), _ptr(opacity), capi.ref(d), _stream())
+    capi.call("vct_copy_alpha_downsample", _ptr(radiance), _ptr(opacity), capi.ref(d),
+              mirror.handle if mirror is not None else None, _stream())
 
 
 def cmd_downsample_all(atlas: torch.Tensor, R: int, regions, mode: int) -> None:
@@ -137,6 +139,11 @@ class RadianceTexture:
     def update(self, atlas: torch.Tensor) -> "RadianceTexture":
         capi.call("vct_texture_update", self.handle, _ptr(atlas), _stream())
         return self
+
+    def read(self, out: torch.Tensor) -> torch.Tensor:
+        """Copy the texture back into a linear atlas of its format."""
+        capi.call("vct_texture_read", self.handle, _ptr(out), _stream())
+        return out
 
     def close(self) -> None:
         if self.handle:

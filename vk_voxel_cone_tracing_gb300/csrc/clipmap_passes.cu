@@ -31,14 +31,17 @@ __global__ void k_clear_region(uint32_t* __restrict__ atlas, AtlasDims A, int3 r
 // copyAlphaImage.comp:16-30: dst.a = src.a over the R^3 interior, all faces.
 // Thread per texel of one face row (x fastest) -> coalesced 4-byte RMW.
 // blockIdx.y = face; R is a power of two, so the (x, y, z) split is shifts.
+// `mirror` (0 = none): a texture array's surface that receives the same texels.
 __global__ void k_copy_alpha(uint32_t* __restrict__ dst, const uint32_t* __restrict__ src, AtlasDims A, int level,
-                             int lg) {
+                             int lg, cudaSurfaceObject_t mirror) {
     const int f = blockIdx.y;
     const uint32_t n = 1u << (3 * lg), m = (1u << lg) - 1u;
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        const int x = (int)(t & m), y = (int)((t >> lg) & m), z = (int)(t >> (2 * lg));
-        const int64_t i = A.index(x + 1 + A.rb * f, y + 1 + level * A.rb, z + 1);
-        dst[i] = (dst[i] & 0x00ffffffu) | (__ldg(src + i) & 0xff000000u);
+        const int x = (int)(t & m) + 1 + A.rb * f, y = (int)((t >> lg) & m) + 1 + level * A.rb, z = (int)(t >> (2 * lg)) + 1;
+        const int64_t i = A.index(x, y, z);
+        const uint32_t v = (dst[i] & 0x00ffffffu) | (__ldg(src + i) & 0xff000000u);
+        dst[i] = v;
+        if (mirror) surf3Dwrite(v, mirror, x * 4, y, z);
     }
 }
 
@@ -179,7 +182,7 @@ __global__ void k_downsample(uint32_t* __restrict__ atlas, AtlasDims A, int3 pmi
 // then blend the 2x2x2 composite of level l-1 with that updated texel exactly
 // as k_downsample<1> does.  Same result as the two passes in sequence.
 __global__ void k_alpha_downsample(uint32_t* __restrict__ rad, const uint32_t* __restrict__ opa, AtlasDims A,
-                                   int3 pmin, int level, int band, int lg) {
+                                   int3 pmin, int level, int band, int lg, cudaSurfaceObject_t mirror) {
     const int half = A.R >> 1;
     const uint32_t n = 1u << (3 * lg), m = (1u << lg) - 1u;
     const int pm[3] = {pmin.x, pmin.y, pmin.z};
@@ -217,9 +220,13 @@ __global__ void k_alpha_downsample(uint32_t* __restrict__ rad, const uint32_t* _
 #pragma unroll
         for (int f = 0; f < 6; ++f)
             own6[f] = (rad[w0 + A.rb * f] & 0x00ffffffu) | (__ldg(opa + w0 + A.rb * f) & 0xff000000u);
+        const int my = w[1] + 1 + A.rb * level, mz = w[2] + 1;
         if (!target) {
 #pragma unroll
-            for (int f = 0; f < 6; ++f) rad[w0 + A.rb * f] = own6[f];
+            for (int f = 0; f < 6; ++f) {
+                rad[w0 + A.rb * f] = own6[f];
+                if (mirror) surf3Dwrite(own6[f], mirror, (w[0] + 1 + A.rb * f) * 4, my, mz);
+            }
             continue;
         }
 #pragma unroll
@@ -249,6 +256,7 @@ __global__ void k_alpha_downsample(uint32_t* __restrict__ rad, const uint32_t* _
                 out |= unorm8_store(mix_rn(res, unorm8_load(own_raw, c), lerp)) << (8 * c);
             }
             rad[wi] = out;
+            if (mirror) surf3Dwrite(out, mirror, (w[0] + 1 + A.rb * f) * 4, my, mz);
         }
     }
 }
@@ -285,7 +293,10 @@ extern "C" int vct_clear_region(uint32_t* atlas, const vct_image_cleaning_desc* 
     return VCT_OK;
 }
 
-extern "C" int vct_copy_alpha(uint32_t* dst, const uint32_t* src, const vct_copy_alpha_desc* d, void* stream) {
+namespace vct {
+
+int copy_alpha_pass(uint32_t* dst, const uint32_t* src, const vct_copy_alpha_desc* d, cudaSurfaceObject_t mirror,
+                    cudaStream_t st) {
     VCT_CHECK_ARG(dst && src && d, "vct_copy_alpha: null argument");
     VCT_CHECK_ARG(valid_resolution(d->clipmap_resolution), "vct_copy_alpha: resolution must be a power of two in [8,1024]");
     VCT_CHECK_ARG(d->clip_level >= 0 && d->clip_level < VCT_CLIP_LEVEL_COUNT, "vct_copy_alpha: clip level out of range");
@@ -296,9 +307,55 @@ extern "C" int vct_copy_alpha(uint32_t* dst, const uint32_t* src, const vct_copy
     const int lg = 31 - __builtin_clz((unsigned)A.R);
     const int64_t n = (int64_t)A.R * A.R * A.R;
     dim3 grid((unsigned)grid_for(n, 256), (unsigned)d->face_count);
-    k_copy_alpha<<<grid, 256, 0, as_stream(stream)>>>(dst, src, A, d->clip_level, lg);
+    k_copy_alpha<<<grid, 256, 0, st>>>(dst, src, A, d->clip_level, lg, mirror);
     VCT_LAUNCH_CHECK();
     return VCT_OK;
+}
+
+int copy_alpha_downsample_pass(uint32_t* radiance, const uint32_t* opacity, const vct_downsample_desc* d,
+                               cudaSurfaceObject_t mirror, cudaStream_t st) {
+    VCT_CHECK_ARG(radiance && opacity && d, "vct_copy_alpha_downsample: null argument");
+    VCT_CHECK_ARG(radiance != opacity, "vct_copy_alpha_downsample: radiance and opacity atlases must differ");
+    VCT_CHECK_ARG(valid_resolution(d->clipmap_resolution),
+                  "vct_copy_alpha_downsample: resolution must be a power of two in [8,1024]");
+    VCT_CHECK_ARG(d->clip_level >= 1 && d->clip_level < VCT_CLIP_LEVEL_COUNT,
+                  "vct_copy_alpha_downsample: clip level must be 1..5");
+    VCT_CHECK_ARG(d->downsample_region_size >= 0 && d->downsample_region_size <= 4096,
+                  "vct_copy_alpha_downsample: downsample band out of range");
+    AtlasDims A(d->clipmap_resolution);
+    const int64_t n = (int64_t)A.R * A.R * A.R;
+    int3 pm = make_int3(d->prev_region_min_corner[0], d->prev_region_min_corner[1], d->prev_region_min_corner[2]);
+    const int lg = 31 - __builtin_clz((unsigned)A.R);
+    k_alpha_downsample<<<grid_for(n, 128), 128, 0, st>>>(radiance, opacity, A, pm, d->clip_level,
+                                                        d->downsample_region_size, lg, mirror);
+    VCT_LAUNCH_CHECK();
+    return VCT_OK;
+}
+
+// The mirror texture must be an RGBA8 texture of the same resolution.
+static int mirror_surface(vct_texture_s* t, int R, const char* who, cudaSurfaceObject_t* out) {
+    *out = 0;
+    if (!t) return VCT_OK;
+    if (texture_format(t) != VCT_TEX_RGBA8 || texture_resolution(t) != R)
+        return fail(VCT_E_BAD_ARG, who);
+    *out = texture_surface(t);
+    return VCT_OK;
+}
+
+}  // namespace vct
+
+extern "C" int vct_copy_alpha(uint32_t* dst, const uint32_t* src, const vct_copy_alpha_desc* d, void* stream) {
+    return copy_alpha_pass(dst, src, d, 0, as_stream(stream));
+}
+
+extern "C" int vct_copy_alpha_downsample(uint32_t* radiance, const uint32_t* opacity, const vct_downsample_desc* d,
+                                         vct_texture_s* mirror, void* stream) {
+    VCT_CHECK_ARG(d, "vct_copy_alpha_downsample: null argument");
+    cudaSurfaceObject_t surf = 0;
+    int rc = mirror_surface(mirror, d->clipmap_resolution,
+                            "vct_copy_alpha_downsample: the mirror must be an RGBA8 texture of the same resolution", &surf);
+    if (rc != VCT_OK) return rc;
+    return copy_alpha_downsample_pass(radiance, opacity, d, surf, as_stream(stream));
 }
 
 extern "C" int vct_wrap_border(uint32_t* atlas, const vct_border_wrapping_desc* d, void* stream) {
@@ -333,26 +390,6 @@ extern "C" int vct_downsample(uint32_t* atlas, const vct_downsample_desc* d, int
         k_downsample<0><<<grid_for(n, 128), 128, 0, as_stream(stream)>>>(atlas, A, pm, d->clip_level, d->downsample_region_size, lgh);
     else
         k_downsample<1><<<grid_for(n, 128), 128, 0, as_stream(stream)>>>(atlas, A, pm, d->clip_level, d->downsample_region_size, lgh);
-    VCT_LAUNCH_CHECK();
-    return VCT_OK;
-}
-
-extern "C" int vct_copy_alpha_downsample(uint32_t* radiance, const uint32_t* opacity, const vct_downsample_desc* d,
-                                         void* stream) {
-    VCT_CHECK_ARG(radiance && opacity && d, "vct_copy_alpha_downsample: null argument");
-    VCT_CHECK_ARG(radiance != opacity, "vct_copy_alpha_downsample: radiance and opacity atlases must differ");
-    VCT_CHECK_ARG(valid_resolution(d->clipmap_resolution),
-                  "vct_copy_alpha_downsample: resolution must be a power of two in [8,1024]");
-    VCT_CHECK_ARG(d->clip_level >= 1 && d->clip_level < VCT_CLIP_LEVEL_COUNT,
-                  "vct_copy_alpha_downsample: clip level must be 1..5");
-    VCT_CHECK_ARG(d->downsample_region_size >= 0 && d->downsample_region_size <= 4096,
-                  "vct_copy_alpha_downsample: downsample band out of range");
-    AtlasDims A(d->clipmap_resolution);
-    const int64_t n = (int64_t)A.R * A.R * A.R;
-    int3 pm = make_int3(d->prev_region_min_corner[0], d->prev_region_min_corner[1], d->prev_region_min_corner[2]);
-    const int lg = 31 - __builtin_clz((unsigned)A.R);
-    k_alpha_downsample<<<grid_for(n, 128), 128, 0, as_stream(stream)>>>(radiance, opacity, A, pm, d->clip_level,
-                                                                        d->downsample_region_size, lg);
     VCT_LAUNCH_CHECK();
     return VCT_OK;
 }

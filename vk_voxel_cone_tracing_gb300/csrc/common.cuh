@@ -19,6 +19,20 @@ namespace vct {
 // Grow `ws` to at least `bytes` (synchronises the device before freeing).
 int workspace_reserve(vct_workspace_s* ws, size_t bytes);
 
+// Radiance texture accessors (textures.cu).
+cudaTextureObject_t texture_object(const vct_texture_s* t);
+cudaSurfaceObject_t texture_surface(const vct_texture_s* t);
+int texture_resolution(const vct_texture_s* t);
+int texture_format(const vct_texture_s* t);
+
+// Copy-alpha of one level, and copy-alpha + radiance mip of one level >= 1,
+// optionally mirroring every texel they write into a texture array's surface
+// (clipmap_passes.cu).
+int copy_alpha_pass(uint32_t* dst, const uint32_t* src, const vct_copy_alpha_desc* d, cudaSurfaceObject_t mirror,
+                    cudaStream_t st);
+int copy_alpha_downsample_pass(uint32_t* radiance, const uint32_t* opacity, const vct_downsample_desc* d,
+                               cudaSurfaceObject_t mirror, cudaStream_t st);
+
 // ---------------------------------------------------------------- errors
 void set_error(const std::string& msg);
 int fail(int code, const std::string& msg);

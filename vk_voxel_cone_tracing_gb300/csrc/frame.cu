@@ -9,8 +9,8 @@
 //                          clear, inject; then copy-alpha and radiance mips
 //                          (levels 1..5: vct_copy_alpha_downsample, one pass)
 //
-// Host-side orchestration only: every step is one of the C-ABI passes, run
-// on the caller's stream.
+// Host-side orchestration only: every step is one of the C-ABI passes (or
+// its internal form with a texture mirror), run on the caller's stream.
 #include "common.cuh"
 
 extern "C" int vct_clipmap_frame(const vct_scene* scene, const vct_frame_desc* f, uint32_t* opacity,
@@ -19,6 +19,9 @@ extern "C" int vct_clipmap_frame(const vct_scene* scene, const vct_frame_desc* f
     VCT_CHECK_ARG(scene && f && opacity && radiance && ws, "vct_clipmap_frame: null argument");
     VCT_CHECK_ARG(!f->shadow_width || shadow_depth, "vct_clipmap_frame: shadow map size given without a buffer");
     const int R = f->clipmap_resolution;
+    VCT_CHECK_ARG(!f->radiance_texture || (vct::texture_format(f->radiance_texture) == VCT_TEX_RGBA8 &&
+                                           vct::texture_resolution(f->radiance_texture) == R),
+                  "vct_clipmap_frame: the radiance texture must be RGBA8 of the clipmap resolution");
     vct_clipmap_region regions[6];
     int rc = vct_clip_regions(f->camera_pos, R, VCT_VOXEL_EXTENT_L0, regions);
     if (rc != VCT_OK) return rc;
@@ -60,9 +63,15 @@ extern "C" int vct_clipmap_frame(const vct_scene* scene, const vct_frame_desc* f
     // level 0 takes the plain copy and levels 1..5 the fused copy + mip pass,
     // each after its predecessor is final -- the same result as all copies
     // first and the mips after.
+    // Both passes also store their texels into the radiance texture when one
+    // is given: together they rewrite every interior texel of every due
+    // level, and radiance borders are never written, so the texture stays
+    // equal to the atlas without a copy.
+    const cudaSurfaceObject_t mirror = f->radiance_texture ? vct::texture_surface(f->radiance_texture) : 0;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (due & 1u) {
         vct_copy_alpha_desc ca = {0, R, VCT_FACE_COUNT};
-        if ((rc = vct_copy_alpha(radiance, opacity, &ca, stream)) != VCT_OK) return rc;
+        if ((rc = vct::copy_alpha_pass(radiance, opacity, &ca, mirror, st)) != VCT_OK) return rc;
     }
     for (int l = 1; l < 6; ++l) {
         if (!((due >> l) & 1u)) continue;
@@ -71,7 +80,7 @@ extern "C" int vct_clipmap_frame(const vct_scene* scene, const vct_frame_desc* f
         d.clip_level = l;
         d.clipmap_resolution = R;
         d.downsample_region_size = VCT_DOWNSAMPLE_REGION_SIZE;
-        if ((rc = vct_copy_alpha_downsample(radiance, opacity, &d, stream)) != VCT_OK) return rc;
+        if ((rc = vct::copy_alpha_downsample_pass(radiance, opacity, &d, mirror, st)) != VCT_OK) return rc;
     }
     return VCT_OK;
 }

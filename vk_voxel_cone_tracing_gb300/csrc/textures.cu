@@ -15,13 +15,27 @@ struct vct_texture_s {
     int format = 0;
     cudaArray_t array = nullptr;
     cudaTextureObject_t tex = 0;
+    cudaSurfaceObject_t surf = 0;  // the same array for direct texel stores
 };
 
 namespace vct {
 
 cudaTextureObject_t texture_object(const vct_texture_s* t) { return t->tex; }
+cudaSurfaceObject_t texture_surface(const vct_texture_s* t) { return t->surf; }
 int texture_resolution(const vct_texture_s* t) { return t->R; }
 int texture_format(const vct_texture_s* t) { return t->format; }
+
+// Zero every texel of a texture array through its surface (4- or 8-byte texels).
+__global__ void k_surface_zero(cudaSurfaceObject_t s, int W, int H, int D, int texel_bytes) {
+    const int64_t n = (int64_t)W * H * D;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int x = (int)(i % W);
+        const int64_t r = i / W;
+        const int y = (int)(r % H), z = (int)(r / H);
+        if (texel_bytes == 4) surf3Dwrite(0u, s, x * 4, y, z);
+        else surf3Dwrite(make_uint2(0u, 0u), s, x * 8, y, z);
+    }
+}
 
 __device__ __forceinline__ uint16_t h_bits(float x) { return __half_as_ushort(__float2half_rn(x)); }
 __device__ __forceinline__ float h_val(uint16_t b) { return __half2float(__ushort_as_half(b)); }
@@ -134,7 +148,7 @@ extern "C" int vct_texture_create(int32_t R, int32_t format, vct_texture_s** out
     t->R = R;
     t->format = format;
     cudaChannelFormatDesc ch = format == 0 ? cudaCreateChannelDesc<uchar4>() : cudaCreateChannelDescHalf4();
-    cudaError_t e = cudaMalloc3DArray(&t->array, &ch, make_cudaExtent(A.W, A.H, A.D));
+    cudaError_t e = cudaMalloc3DArray(&t->array, &ch, make_cudaExtent(A.W, A.H, A.D), cudaArraySurfaceLoadStore);
     if (e != cudaSuccess) {
         delete t;
         return cuda_fail(e, "cudaMalloc3DArray (radiance texture)");
@@ -148,10 +162,18 @@ extern "C" int vct_texture_create(int32_t R, int32_t format, vct_texture_s** out
     td.readMode = format == 0 ? cudaReadModeNormalizedFloat : cudaReadModeElementType;
     td.normalizedCoords = 1;
     e = cudaCreateTextureObject(&t->tex, &rd, &td, nullptr);
+    if (e == cudaSuccess) e = cudaCreateSurfaceObject(&t->surf, &rd);
+    if (e == cudaSuccess) {  // a defined starting content: all zero, like a fresh atlas
+        k_surface_zero<<<grid_for16(A.texels(), 256), 256>>>(t->surf, A.W, A.H, A.D, format == 0 ? 4 : 8);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    }
     if (e != cudaSuccess) {
+        if (t->surf) cudaDestroySurfaceObject(t->surf);
+        if (t->tex) cudaDestroyTextureObject(t->tex);
         cudaFreeArray(t->array);
         delete t;
-        return cuda_fail(e, "cudaCreateTextureObject (radiance texture)");
+        return cuda_fail(e, "vct_texture_create (texture/surface object or zero fill)");
     }
     *out = t;
     return VCT_OK;
@@ -170,8 +192,22 @@ extern "C" int vct_texture_update(vct_texture_s* t, const void* atlas, void* str
     return VCT_OK;
 }
 
+extern "C" int vct_texture_read(const vct_texture_s* t, void* atlas, void* stream) {
+    VCT_CHECK_ARG(t && atlas, "vct_texture_read: null argument");
+    AtlasDims A(t->R);
+    const size_t texel = t->format == 0 ? 4 : 8;
+    cudaMemcpy3DParms p = {};
+    p.srcArray = t->array;
+    p.dstPtr = make_cudaPitchedPtr(atlas, A.W * texel, A.W, A.H);
+    p.extent = make_cudaExtent(A.W, A.H, A.D);
+    p.kind = cudaMemcpyDeviceToDevice;
+    VCT_CUDA_TRY(cudaMemcpy3DAsync(&p, as_stream(stream)));
+    return VCT_OK;
+}
+
 extern "C" int vct_texture_destroy(vct_texture_s* t) {
     if (!t) return VCT_OK;
+    if (t->surf) cudaDestroySurfaceObject(t->surf);
     cudaError_t e1 = cudaDestroyTextureObject(t->tex);
     cudaError_t e2 = cudaFreeArray(t->array);
     delete t;

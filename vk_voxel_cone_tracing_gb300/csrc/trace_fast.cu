@@ -150,11 +150,31 @@ __global__ void k_morton_keys(const vct_surface_sample* __restrict__ s, int64_t 
     }
 }
 
+// Specular classification of the Morton-ordered samples (the shader traces
+// a specular cone where depth != 1 and the sample has a specular colour and
+// metalness): key 0 for specular samples, 256 otherwise, and their count.
+// One radix pass on bit 8 then lists the specular samples in Morton order.
+__global__ void k_spec_keys(const __grid_constant__ FastArgs A, const uint32_t* __restrict__ order,
+                            uint32_t* __restrict__ spec_key, unsigned int* __restrict__ spec_count) {
+    const int lane = threadIdx.x & 31;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + threadIdx.x - lane; base < A.n;
+         base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t pos = base + lane;
+        bool spec = false;
+        if (pos < A.n && A.C.need_specular) {
+            const float4* p = reinterpret_cast<const float4*>(A.samples + __ldg(order + pos));
+            const float4 a = __ldg(p + 0), d = __ldg(p + 3);
+            spec = a.w != 1.0f && (d.x > 1e-6f || d.y > 1e-6f || d.z > 1e-6f) && d.w > 1e-6f;
+        }
+        if (pos < A.n) spec_key[pos] = spec ? 0u : 256u;
+        const unsigned bal = __ballot_sync(0xffffffffu, spec);
+        if (lane == 0 && bal) atomicAdd(spec_count, (unsigned)__popc(bal));
+    }
+}
+
 constexpr int kWarpsPerBlock = 8;
 
-__global__ void __launch_bounds__(256) k_trace_diffuse(const __grid_constant__ FastArgs A, const uint32_t* __restrict__ order,
-                                                       uint32_t* __restrict__ spec_key,
-                                                       unsigned int* __restrict__ spec_count) {
+__global__ void __launch_bounds__(256) k_trace_diffuse(const __grid_constant__ FastArgs A, const uint32_t* __restrict__ order) {
     __shared__ float4 s_start[kWarpsPerBlock][32];
     __shared__ float4 s_norm[kWarpsPerBlock][32];
     __shared__ int s_incl[kWarpsPerBlock][32];
@@ -252,9 +272,6 @@ __global__ void __launch_bounds__(256) k_trace_diffuse(const __grid_constant__ F
             reinterpret_cast<float4*>(A.dout)[idx] = dd[0];
             if (!spec) reinterpret_cast<float4*>(A.sout)[idx] = dd[1];
         }
-        if (pos < A.n) spec_key[pos] = spec ? 0u : 256u;
-        const unsigned bal = __ballot_sync(0xffffffffu, spec);
-        if (lane == 0 && bal) atomicAdd(spec_count, (unsigned)__popc(bal));
     }
     if (A.steps) {
         for (int o = 16; o > 0; o >>= 1) steps += __shfl_xor_sync(0xffffffffu, steps, o);
@@ -628,18 +645,24 @@ extern "C" int vct_cone_trace_fast(const vct_cone_tracing_desc* desc, const vct_
     VCT_CUDA_TRY(cudaMemsetAsync(S.spec_count, 0, sizeof(unsigned int), st));
     int64_t gd = (n + 255) / 256;
     const int grid_d = (int)(gd > 152 * 8 ? 152 * 8 : gd);
-    k_trace_diffuse<<<grid_d, 256, 0, st>>>(A, S.order, S.spec_key, S.spec_count);
-    VCT_LAUNCH_CHECK();
-    if (A.C.need_specular) {
-        tb = S.temp_bytes;
-        // stable partition (one radix pass on bit 8): specular samples first, Morton order kept
-        VCT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(S.temp, tb, S.spec_key, S.spec_key_out, S.order, S.spec_list,
-                                                     (int)n, 8, 9, st));
-        int64_t gw = (n * 32 + 255) / 256;
-        const int grid_s = (int)(gw > 152 * 64 ? 152 * 64 : gw);
-        k_trace_specular_warp<<<grid_s, 256, 0, st>>>(A, S.spec_list, S.spec_count);
+    if (!A.C.need_specular) {
+        k_trace_diffuse<<<grid_d, 256, 0, st>>>(A, S.order);
         VCT_LAUNCH_CHECK();
+        return VCT_OK;
     }
+    const int grid_k = (int)(gd > 152 * 16 ? 152 * 16 : gd);
+    k_spec_keys<<<grid_k, 256, 0, st>>>(A, S.order, S.spec_key, S.spec_count);
+    VCT_LAUNCH_CHECK();
+    tb = S.temp_bytes;
+    // stable partition (one radix pass on bit 8): specular samples first, Morton order kept
+    VCT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(S.temp, tb, S.spec_key, S.spec_key_out, S.order, S.spec_list, (int)n,
+                                                 8, 9, st));
+    int64_t gw = (n * 32 + 255) / 256;
+    const int grid_s = (int)(gw > 152 * 64 ? 152 * 64 : gw);
+    k_trace_diffuse<<<grid_d, 256, 0, st>>>(A, S.order);
+    VCT_LAUNCH_CHECK();
+    k_trace_specular_warp<<<grid_s, 256, 0, st>>>(A, S.spec_list, S.spec_count);
+    VCT_LAUNCH_CHECK();
     return VCT_OK;
 }
 

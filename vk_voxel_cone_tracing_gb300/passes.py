@@ -169,8 +169,9 @@ def svo_cone_trace(desc: capi.ConeTracingDesc, eye, pool: torch.Tensor, node_cou
 def clipmap_frame(dscene: DeviceScene, camera_pos, R: int, opacity: torch.Tensor, radiance: torch.Tensor,
                   shadow: torch.Tensor | None, light: capi.DirectionalLightDesc,
                   light_shadow: capi.DirectionalLightShadowDesc, ws: Workspace, frame_index: int = 0,
-                  inject_mode: int = capi.INJECT_DETERMINISTIC):
-    """vct_clipmap_frame: voxelise, mips, border, shadow depth, inject, copy alpha, radiance mips."""
+                  inject_mode: int = capi.INJECT_DETERMINISTIC, texture=None):
+    """vct_clipmap_frame: voxelise, mips, border, shadow depth, inject, copy alpha, radiance mips; `texture`
+    (an RGBA8 RadianceTexture of resolution R) is kept equal to the radiance atlas's written texels."""
     f = capi.FrameDesc()
     f.camera_pos = capi.f3(*camera_pos)
     f.clipmap_resolution = R
@@ -180,6 +181,7 @@ def clipmap_frame(dscene: DeviceScene, camera_pos, R: int, opacity: torch.Tensor
     f.shadow_height = shadow.shape[0] if shadow is not None else 0
     f.light = light
     f.light_shadow = light_shadow
+    f.radiance_texture = texture.handle if texture is not None else None
     regs = (capi.ClipmapRegion * 6)()
     capi.call("vct_clipmap_frame", capi.ref(dscene.desc), capi.ref(f), _ptr(opacity), _ptr(radiance),
               _ptr(shadow), C.cast(regs, C.c_void_p), ws.handle, _stream())
