@@ -34,7 +34,7 @@ int fill_trace_params(TraceParams& P, const vct_cone_tracing_desc* desc, const v
                       const vct_directional_light_shadow_desc* light_shadow);
 
 struct FastConsts {
-    float uvs, inv_uvs, min_radius, inv_min_radius, decay, start_off;
+    float uvs, inv_uvs, min_radius, inv_min_radius, inv_min_radius2, decay, start_off;
     float coef_diffuse, sf_diffuse, aperture_diffuse;
     float cx, cy, cz;
     float inv_ext[kClipLevels];
@@ -54,6 +54,15 @@ struct FastArgs {
     float* __restrict__ sout;
     unsigned long long* steps;
 };
+
+// 2^x by the hardware approximation (PTX ex2.approx: about 2 ulp, flushes
+// subnormal results): the per-step level size and opacity correction of the
+// texture form, whose error bar (8-bit texture filter weights) dominates.
+__device__ __forceinline__ float ex2_approx(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
 
 __device__ __forceinline__ float4 fma4(float4 a, float s, float4 b) {
     return make_float4(fmaf(a.x, s, b.x), fmaf(a.y, s, b.y), fmaf(a.z, s, b.z), fmaf(a.w, s, b.w));
@@ -96,9 +105,9 @@ __device__ __forceinline__ float4 trace_cone_fast(cudaTextureObject_t tex, const
         ++it;
         const float3 pos = f3(fmaf(dir.x, step, start.x), fmaf(dir.y, step, start.y), fmaf(dir.z, step, start.z));
         const float dx = C.cx - pos.x, dy = C.cy - pos.y, dz = C.cz - pos.z;
-        const float dist = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
-        const float min_level = ceilf(log2f(dist * C.inv_min_radius));
-        float cl = log2f(diameter * C.inv_uvs);
+        // ceil(log2(dist / r)) as ceil(log2(dist^2 / r^2) / 2): no square root
+        const float min_level = ceilf(0.5f * __log2f(fmaf(dx, dx, fmaf(dy, dy, dz * dz)) * C.inv_min_radius2));
+        float cl = __log2f(diameter * C.inv_uvs);
         cl = fminf(fmaxf(fmaxf(start_level, cl), min_level), (float)(kClipLevels - 1));
         const float flo = floorf(cl);
         const int lo = (int)flo;
@@ -109,9 +118,9 @@ __device__ __forceinline__ float4 trace_cone_fast(cudaTextureObject_t tex, const
             s = make_float4(fmaf(h.x - s.x, fr, s.x), fmaf(h.y - s.y, fr, s.y), fmaf(h.z - s.z, fr, s.z),
                             fmaf(h.w - s.w, fr, s.w));
         }
-        vs = uvs * exp2f(cl);
+        vs = uvs * ex2_approx(cl);
         const float corr = __fdividef(seg, vs);
-        const float opacity = __saturatef(1.0f - exp2f(corr * __log2f(1.0f - s.w)));
+        const float opacity = __saturatef(1.0f - ex2_approx(corr * __log2f(1.0f - s.w)));
         const float k = __saturatef(1.0f - result.w);
         result = make_float4(fmaf(k * s.x, corr, result.x), fmaf(k * s.y, corr, result.y),
                              fmaf(k * s.z, corr, result.z), fmaf(k, opacity, result.w));
@@ -290,9 +299,9 @@ __device__ __forceinline__ ConeStep cone_step(cudaTextureObject_t tex, const Fas
                                               float dm, float sg) {
     const float3 pos = f3(fmaf(dir.x, st, start.x), fmaf(dir.y, st, start.y), fmaf(dir.z, st, start.z));
     const float dx = C.cx - pos.x, dy = C.cy - pos.y, dz = C.cz - pos.z;
-    const float dist = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
-    const float min_level = ceilf(log2f(dist * C.inv_min_radius));
-    float cl = log2f(dm * C.inv_uvs);
+    // ceil(log2(dist / r)) as ceil(log2(dist^2 / r^2) / 2): no square root
+    const float min_level = ceilf(0.5f * __log2f(fmaf(dx, dx, fmaf(dy, dy, dz * dz)) * C.inv_min_radius2));
+    float cl = __log2f(dm * C.inv_uvs);
     cl = fminf(fmaxf(fmaxf(start_level, cl), min_level), (float)(kClipLevels - 1));
     const float flo = floorf(cl);
     const int lo = (int)flo;
@@ -303,9 +312,9 @@ __device__ __forceinline__ ConeStep cone_step(cudaTextureObject_t tex, const Fas
         smp = make_float4(fmaf(h.x - smp.x, fr, smp.x), fmaf(h.y - smp.y, fr, smp.y), fmaf(h.z - smp.z, fr, smp.z),
                           fmaf(h.w - smp.w, fr, smp.w));
     }
-    const float vs = C.uvs * exp2f(cl);
+    const float vs = C.uvs * ex2_approx(cl);
     const float corr = __fdividef(sg, vs);
-    const float opacity = __saturatef(1.0f - exp2f(corr * __log2f(1.0f - smp.w)));
+    const float opacity = __saturatef(1.0f - ex2_approx(corr * __log2f(1.0f - smp.w)));
     return ConeStep{smp.x * corr, smp.y * corr, smp.z * corr, opacity,
                     1.0f - __fdividef(opacity, fmaf(st + vs, C.decay, 1.0f))};
 }
@@ -354,7 +363,7 @@ __device__ __forceinline__ float4 trace_cone_warp(cudaTextureObject_t tex, const
     for (;;) {
         const float K = st <= T ? floorf((T - st) / u) + 1.0f : 0.0f;
         const float sK = fmaf(K, u, st);
-        auto st_at = [&](float jf) { return jf <= K ? fmaf(jf, u, st) : sK * exp2f((jf - K) * lr); };
+        auto st_at = [&](float jf) { return jf <= K ? fmaf(jf, u, st) : sK * ex2_approx((jf - K) * lr); };
         const float j0 = (float)(S * lane);
         // march this lane's steps: composite, count of valid steps
         ConeStep x = id;
@@ -569,6 +578,7 @@ static void fill_fast_consts(FastConsts& C, const vct_cone_tracing_desc& d) {
     C.inv_uvs = 1.0f / d.voxel_size;
     C.min_radius = d.voxel_size * d.volume_dimension * 0.5f;
     C.inv_min_radius = 1.0f / C.min_radius;
+    C.inv_min_radius2 = C.inv_min_radius * C.inv_min_radius;
     C.decay = d.occlusion_decay;
     C.start_off = d.trace_start_offset;
     const bool c32 = d.enable_32_cones != 0;
