@@ -33,6 +33,13 @@ int copy_alpha_pass(uint32_t* dst, const uint32_t* src, const vct_copy_alpha_des
 int copy_alpha_downsample_pass(uint32_t* radiance, const uint32_t* opacity, const vct_downsample_desc* d,
                                cudaSurfaceObject_t mirror, cudaStream_t st);
 
+// The frame's rasterised passes with the deterministic injection, up to the
+// fold (raster.cu): opacity clear + voxelisation + mips + border, shadow
+// depth, clear of the due radiance levels and the injection.
+int frame_raster_passes(const vct_scene* scene, const vct_frame_desc* f, const vct_clipmap_region regions[6],
+                        uint32_t due, uint32_t* opacity, uint32_t* radiance, float* shadow_depth, vct_workspace_s* ws,
+                        cudaStream_t st);
+
 // ---------------------------------------------------------------- errors
 void set_error(const std::string& msg);
 int fail(int code, const std::string& msg);

@@ -18,6 +18,8 @@ extern "C" int vct_clipmap_frame(const vct_scene* scene, const vct_frame_desc* f
                                  vct_workspace_s* ws, void* stream) {
     VCT_CHECK_ARG(scene && f && opacity && radiance && ws, "vct_clipmap_frame: null argument");
     VCT_CHECK_ARG(!f->shadow_width || shadow_depth, "vct_clipmap_frame: shadow map size given without a buffer");
+    VCT_CHECK_ARG(f->inject_mode == VCT_INJECT_DETERMINISTIC || f->inject_mode == VCT_INJECT_ATOMIC,
+                  "vct_clipmap_frame: bad injection mode");
     const int R = f->clipmap_resolution;
     VCT_CHECK_ARG(!f->radiance_texture || (vct::texture_format(f->radiance_texture) == VCT_TEX_RGBA8 &&
                                            vct::texture_resolution(f->radiance_texture) == R),
@@ -28,36 +30,44 @@ extern "C" int vct_clipmap_frame(const vct_scene* scene, const vct_frame_desc* f
     if (regions_out)
         for (int l = 0; l < 6; ++l) regions_out[l] = regions[l];
 
-    // VoxelizationPass (full revoxelisation every frame, VoxelizationPass.cpp:79-125)
-    if ((rc = vct_clear_atlas(opacity, R, stream)) != VCT_OK) return rc;
-    if ((rc = vct_voxelize_opacity(scene, regions, R, opacity, 0x3Fu, ws, stream)) != VCT_OK) return rc;
-    if ((rc = vct_downsample_all(opacity, regions, R, VCT_DOWNSAMPLE_OPACITY, stream)) != VCT_OK) return rc;
-    vct_border_wrapping_desc bw = {(uint32_t)R, VCT_VOXEL_BORDER, VCT_FACE_COUNT, VCT_CLIP_LEVEL_COUNT};
-    if ((rc = vct_wrap_border(opacity, &bw, stream)) != VCT_OK) return rc;
-
-    // RSMPass: the depth map the injection's visibility samples
-    vct_shadow_map sm = {nullptr, 0, 0};
-    if (f->shadow_width > 0) {
-        if ((rc = vct_shadow_depth(scene, &f->light_shadow, shadow_depth, f->shadow_width, f->shadow_height, ws,
-                                   stream)) != VCT_OK)
-            return rc;
-        sm.depth = shadow_depth;
-        sm.width = f->shadow_width;
-        sm.height = f->shadow_height;
-    }
-
-    // RadianceInjectionPass (RadianceInjectionPass.cpp:64-159), level cadence 2^level frames
-    uint32_t due = 0;
+    uint32_t due = 0;  // radiance levels refreshed this frame: cadence 2^level frames
     for (int l = 0; l < 6; ++l)
         if (f->frame_index % (1 << l) == 0) due |= 1u << l;
-    for (int l = 0; l < 6; ++l) {
-        if (!((due >> l) & 1u)) continue;
-        vct_image_cleaning_desc c = {{0, 0, 0}, l, {(uint32_t)R, (uint32_t)R, (uint32_t)R}, R, VCT_FACE_COUNT};
-        if ((rc = vct_clear_region(radiance, &c, stream)) != VCT_OK) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+
+    if (f->inject_mode == VCT_INJECT_DETERMINISTIC) {
+        // VoxelizationPass, RSMPass and RadianceInjectionPass up to the fold,
+        // with the opacity voxelisation and the injection's coverage count
+        // sharing one coverage pass (same results as the passes below)
+        if ((rc = vct::frame_raster_passes(scene, f, regions, due, opacity, radiance, shadow_depth, ws, st)) != VCT_OK)
+            return rc;
+    } else {
+        // VoxelizationPass (full revoxelisation every frame, VoxelizationPass.cpp:79-125)
+        if ((rc = vct_clear_atlas(opacity, R, stream)) != VCT_OK) return rc;
+        if ((rc = vct_voxelize_opacity(scene, regions, R, opacity, 0x3Fu, ws, stream)) != VCT_OK) return rc;
+        if ((rc = vct_downsample_all(opacity, regions, R, VCT_DOWNSAMPLE_OPACITY, stream)) != VCT_OK) return rc;
+        vct_border_wrapping_desc bw = {(uint32_t)R, VCT_VOXEL_BORDER, VCT_FACE_COUNT, VCT_CLIP_LEVEL_COUNT};
+        if ((rc = vct_wrap_border(opacity, &bw, stream)) != VCT_OK) return rc;
+        // RSMPass: the depth map the injection's visibility samples
+        vct_shadow_map sm = {nullptr, 0, 0};
+        if (f->shadow_width > 0) {
+            if ((rc = vct_shadow_depth(scene, &f->light_shadow, shadow_depth, f->shadow_width, f->shadow_height, ws,
+                                       stream)) != VCT_OK)
+                return rc;
+            sm.depth = shadow_depth;
+            sm.width = f->shadow_width;
+            sm.height = f->shadow_height;
+        }
+        // RadianceInjectionPass (RadianceInjectionPass.cpp:64-159)
+        for (int l = 0; l < 6; ++l) {
+            if (!((due >> l) & 1u)) continue;
+            vct_image_cleaning_desc c = {{0, 0, 0}, l, {(uint32_t)R, (uint32_t)R, (uint32_t)R}, R, VCT_FACE_COUNT};
+            if ((rc = vct_clear_region(radiance, &c, stream)) != VCT_OK) return rc;
+        }
+        if ((rc = vct_inject_radiance(scene, regions, R, &sm, &f->light, &f->light_shadow, radiance, due,
+                                      f->inject_mode, ws, stream)) != VCT_OK)
+            return rc;
     }
-    if ((rc = vct_inject_radiance(scene, regions, R, &sm, &f->light, &f->light_shadow, radiance, due, f->inject_mode,
-                                  ws, stream)) != VCT_OK)
-        return rc;
     // copy-alpha of every due level, then the radiance mips 1..5 of the due
     // levels; a due level's predecessor is always due (frame % 2^l == 0), so
     // level 0 takes the plain copy and levels 1..5 the fused copy + mip pass,
@@ -68,7 +78,6 @@ extern "C" int vct_clipmap_frame(const vct_scene* scene, const vct_frame_desc* f
     // level, and radiance borders are never written, so the texture stays
     // equal to the atlas without a copy.
     const cudaSurfaceObject_t mirror = f->radiance_texture ? vct::texture_surface(f->radiance_texture) : 0;
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (due & 1u) {
         vct_copy_alpha_desc ca = {0, R, VCT_FACE_COUNT};
         if ((rc = vct::copy_alpha_pass(radiance, opacity, &ca, mirror, st)) != VCT_OK) return rc;

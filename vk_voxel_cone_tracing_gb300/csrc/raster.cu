@@ -285,7 +285,9 @@ __device__ inline float3 interp3(const float b[3], const float3 v[3]) {
 }
 
 // ------------------------------------------------------------ pass params
-enum Kind { K_OPACITY = 0, K_INJECT = 1, K_SHADOW = 2, K_SVO = 3 };
+// K_OPA_COUNT: the opacity voxelisation and the injection's coverage count in
+// one pass (the frame's items are the same for both).
+enum Kind { K_OPACITY = 0, K_INJECT = 1, K_SHADOW = 2, K_SVO = 3, K_OPA_COUNT = 4 };
 enum Phase { P_DIRECT = 0, P_COUNT = 1, P_WRITE = 2 };
 
 struct RasterArgs {
@@ -310,6 +312,7 @@ struct RasterArgs {
     int64_t frag_capacity;
     int64_t items;
     uint32_t invalid_key;  // injection record key that sorts past every texel
+    uint32_t count_levels; // injection: the clip levels (bit l) whose samples are counted and emitted
 };
 
 // Items are numbered triangle-major (item = tri * nlevels + level index) and
@@ -757,7 +760,8 @@ __global__ void __launch_bounds__(128) k_cover(const __grid_constant__ RasterArg
             if (KIND != K_SHADOW) {
                 const vct_gltf_shade_material mat = material_of(A.s, mi);
                 live = live && !item_discarded(A, mat);
-                if (KIND == K_INJECT) per = inject_per_fragment(mat);
+                if (KIND == K_INJECT || KIND == K_OPA_COUNT) per = inject_per_fragment(mat);
+                if (KIND == K_INJECT) live = live && ((A.count_levels >> lvl) & 1u);
             }
             TileSlot& T = S[lane];
             T.per = per;
@@ -824,7 +828,7 @@ __global__ void __launch_bounds__(128) k_cover(const __grid_constant__ RasterArg
                 px = S[j].tx + (ox0 >> 8);
                 py = S[j].ty + (oy0 >> 8);
                 mask = cover_pixel<NS>(t, S[j], ox0, oy0);
-                if (PHASE == P_DIRECT && mask) {
+                if ((PHASE == P_DIRECT || KIND == K_OPA_COUNT) && mask) {
                     const TileSlot& T = S[j];
                     const int lvl = (int)(T.meta & 7u);
                     for (uint32_t m = mask; m; m &= m - 1u) {
@@ -834,7 +838,7 @@ __global__ void __launch_bounds__(128) k_cover(const __grid_constant__ RasterArg
                                   oy0 + (NS == 1 ? 128 : c_sample_loc8[s][1]), b, z);
                         if (KIND == K_SHADOW) {
                             atomicMin(reinterpret_cast<unsigned int*>(A.depth) + (int64_t)py * A.W + px, __float_as_uint(z));
-                        } else if (KIND == K_OPACITY) {
+                        } else if (KIND == K_OPACITY || KIND == K_OPA_COUNT) {
                             const vct_voxelization_desc& d = A.vd[lvl];
                             const float3 wp = interp3(b, T.p);
                             if (wp.x < d.region_min_corner[0] || wp.y < d.region_min_corner[1] ||
@@ -855,6 +859,7 @@ __global__ void __launch_bounds__(128) k_cover(const __grid_constant__ RasterArg
                 }
             }
             if (RANKED) {
+                if (KIND == K_OPA_COUNT && act && !((A.count_levels >> (S[j].meta & 7u)) & 1u)) mask = 0u;
                 const uint32_t c = __popc(mask);
                 uint32_t ci = c;
 #pragma unroll
@@ -1115,6 +1120,84 @@ static int count_tiles(RasterArgs& A, vct_workspace_s* ws, size_t& off, const Ti
     return VCT_OK;
 }
 
+// The deterministic injection after its coverage count: the emitted sample
+// descriptors and the record arrays, carved from the workspace.
+struct InjectState {
+    TilePlan plan;
+    uint32_t nfrag = 0, nrec = 0;
+    FragDesc* fr = nullptr;
+    float4* rgb = nullptr;
+    uint32_t *kin = nullptr, *kout = nullptr, *vin = nullptr, *vout = nullptr, *heads = nullptr, *nheads = nullptr;
+    void* stmp = nullptr;
+    size_t sort_bytes = 0, select_bytes = 0;
+    int key_bits = 0;
+};
+
+// Plan the tiles of `C`'s items, count covered samples and records per tile
+// with the KIND kernel (K_INJECT; or K_OPA_COUNT, which also writes `C`'s
+// opacity atlas), scan, read the totals back, reserve and carve everything
+// the rest of the injection needs, and emit the descriptors with `I` (the
+// injection's args over the same items).  Returns kWorkspaceGrew when the
+// workspace moved: the caller restarts (every step here is idempotent).
+template <int KIND>
+static int inject_prepare(RasterArgs& C, RasterArgs& I, vct_workspace_s* ws, cudaStream_t st, InjectState* S) {
+    size_t off;
+    int rc = plan_tiles(C, ws, off, &S->plan, st);
+    if (rc != VCT_OK) return rc;
+    S->nfrag = S->nrec = 0;
+    if (S->plan.total == 0) return VCT_OK;
+    uint2* offs;
+    rc = count_tiles<KIND>(C, ws, off, S->plan, &offs, &S->nfrag, &S->nrec, st);
+    if (rc != VCT_OK) return rc;  // including kWorkspaceGrew
+    if (S->nfrag == 0) return VCT_OK;
+    const uint32_t nfrag = S->nfrag, nrec = S->nrec;
+    S->key_bits = 32 - __builtin_clz((unsigned)I.invalid_key);
+    VCT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(nullptr, S->sort_bytes, (uint32_t*)nullptr, (uint32_t*)nullptr,
+                                                 (uint32_t*)nullptr, (uint32_t*)nullptr, (int)nrec, 0, S->key_bits));
+    VCT_CUDA_TRY(cub::DeviceSelect::If(nullptr, S->select_bytes, thrust::counting_iterator<uint32_t>(0u),
+                                       (uint32_t*)nullptr, (uint32_t*)nullptr, (int64_t)nrec + 1,
+                                       RunHead{nullptr, nrec}));
+    const size_t r4 = a256(4 * (size_t)nrec + 4);
+    const size_t need = off + a256(sizeof(FragDesc) * (size_t)nfrag) + a256(16 * (size_t)nrec) + 5 * r4 + 256 +
+                        a256(S->sort_bytes > S->select_bytes ? S->sort_bytes : S->select_bytes);
+    if (ws->bytes < need) {
+        rc = workspace_reserve(ws, need);
+        return rc != VCT_OK ? rc : kWorkspaceGrew;
+    }
+    char* p = (char*)ws->ptr + off;
+    S->fr = (FragDesc*)p;
+    p += a256(sizeof(FragDesc) * (size_t)nfrag);
+    S->rgb = (float4*)p;
+    p += a256(16 * (size_t)nrec);
+    S->kin = (uint32_t*)p;
+    S->kout = (uint32_t*)(p + r4);
+    S->vin = (uint32_t*)(p + 2 * r4);
+    S->vout = (uint32_t*)(p + 3 * r4);
+    S->heads = (uint32_t*)(p + 4 * r4);
+    S->nheads = (uint32_t*)(p + 5 * r4);
+    S->stmp = p + 5 * r4 + 256;
+    launch_cover<K_INJECT, P_WRITE>(I, S->plan, nullptr, offs, S->fr, nullptr, st);
+    VCT_LAUNCH_CHECK();
+    return VCT_OK;
+}
+
+// Shade the emitted samples into face records (needs the light and shadow
+// map in `I`), sort them stably by texel and fold every texel's run.
+static int inject_finish(const RasterArgs& I, const InjectState& S, cudaStream_t st) {
+    if (S.nfrag == 0) return VCT_OK;
+    const uint32_t nfrag = S.nfrag, nrec = S.nrec;
+    k_inject_shade<<<grid_of(nfrag, 256), 256, 0, st>>>(I, S.fr, nfrag, S.kin, S.vin, S.rgb);
+    VCT_LAUNCH_CHECK();
+    size_t tb = S.sort_bytes;
+    VCT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(S.stmp, tb, S.kin, S.kout, S.vin, S.vout, (int)nrec, 0, S.key_bits, st));
+    tb = S.select_bytes;
+    VCT_CUDA_TRY(cub::DeviceSelect::If(S.stmp, tb, thrust::counting_iterator<uint32_t>(0u), S.heads, S.nheads,
+                                       (int64_t)nrec + 1, RunHead{S.kout, nrec}, st));
+    k_inject_fold<<<grid_of(nrec, 256), 256, 0, st>>>(S.kout, S.vout, S.rgb, S.heads, S.nheads, I.invalid_key, I.atlas);
+    VCT_LAUNCH_CHECK();
+    return VCT_OK;
+}
+
 static void fill_clipmap_levels(RasterArgs& A, const vct_clipmap_region* regions, int R, uint32_t level_mask) {
     A.nlevels = 0;
     for (int l = 0; l < 6; ++l) {
@@ -1289,13 +1372,14 @@ extern "C" int vct_inject_radiance(const vct_scene* scene, const vct_clipmap_reg
     if (rc != VCT_OK) return rc;
     A.items = scene->triangle_count * A.nlevels;
     A.atlas = atlas;
+    A.count_levels = 0x3Fu;  // every level of the item list
     cudaStream_t st = as_stream(stream);
-    size_t off;
-    TilePlan plan;
-    rc = plan_tiles(A, ws, off, &plan, st);
-    if (rc != VCT_OK) return rc;
-    if (plan.total == 0) return VCT_OK;
     if (mode == VCT_INJECT_ATOMIC) {
+        size_t off;
+        TilePlan plan;
+        rc = plan_tiles(A, ws, off, &plan, st);
+        if (rc != VCT_OK) return rc;
+        if (plan.total == 0) return VCT_OK;
         int* err = (int*)((char*)ws->ptr + off);
         VCT_CUDA_TRY(cudaMemsetAsync(err, 0, 4, st));
         launch_cover<K_INJECT, P_DIRECT>(A, plan, nullptr, nullptr, nullptr, err, st);
@@ -1308,50 +1392,80 @@ extern "C" int vct_inject_radiance(const vct_scene* scene, const vct_clipmap_reg
     }
     // deterministic: count -> scan -> emit covered samples -> shade into records
     // -> stable sort by texel -> fold each texel's run in traversal order
-    uint2* offs;
-    uint32_t nfrag, nrec;
-    rc = count_tiles<K_INJECT>(A, ws, off, plan, &offs, &nfrag, &nrec, st);
+    InjectState S;
+    rc = inject_prepare<K_INJECT>(A, A, ws, st, &S);
     if (rc == kWorkspaceGrew)
         return vct_inject_radiance(scene, regions, R, shadow, light, light_shadow, atlas, level_mask, mode, ws, stream);
     if (rc != VCT_OK) return rc;
-    if (nfrag == 0) return VCT_OK;
-    const int key_bits = 32 - __builtin_clz((unsigned)A.invalid_key);
-    size_t sort_bytes = 0, select_bytes = 0;
-    VCT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(nullptr, sort_bytes, (uint32_t*)nullptr, (uint32_t*)nullptr,
-                                                 (uint32_t*)nullptr, (uint32_t*)nullptr, (int)nrec, 0, key_bits));
-    VCT_CUDA_TRY(cub::DeviceSelect::If(nullptr, select_bytes, thrust::counting_iterator<uint32_t>(0u), (uint32_t*)nullptr,
-                                       (uint32_t*)nullptr, (int64_t)nrec + 1, RunHead{nullptr, nrec}));
-    const size_t r4 = a256(4 * (size_t)nrec + 4);
-    const size_t need = off + a256(sizeof(FragDesc) * (size_t)nfrag) + a256(16 * (size_t)nrec) + 5 * r4 + 256 +
-                        a256(sort_bytes > select_bytes ? sort_bytes : select_bytes);
-    if (ws->bytes < need) {
-        rc = workspace_reserve(ws, need);
-        if (rc != VCT_OK) return rc;
-        return vct_inject_radiance(scene, regions, R, shadow, light, light_shadow, atlas, level_mask, mode, ws, stream);
+    return inject_finish(A, S, st);
+}
+
+namespace vct {
+
+// The rasterised part of a frame with the deterministic injection
+// (Application::run's VoxelizationPass, RSMPass and RadianceInjectionPass up to
+// the fold).  The opacity voxelisation and the injection's coverage count
+// share one tile plan and one coverage pass -- their items (every triangle at
+// every level, the same projections and viewport) are the same -- so the
+// order is: clear opacity, shadow depth (it does not depend on the atlases),
+// opacity + count + emit, opacity mips, border, clear of the due radiance
+// levels, then shading, sort and fold.  The results equal the passes run one
+// by one in the reference's order.
+int frame_raster_passes(const vct_scene* scene, const vct_frame_desc* f, const vct_clipmap_region regions[6],
+                        uint32_t due, uint32_t* opacity, uint32_t* radiance, float* shadow_depth, vct_workspace_s* ws,
+                        cudaStream_t st) {
+    const int R = f->clipmap_resolution;
+    void* stream = st;
+    int rc;
+    if ((rc = vct_clear_atlas(opacity, R, stream)) != VCT_OK) return rc;
+    vct_shadow_map sm = {nullptr, 0, 0};
+    if (f->shadow_width > 0) {
+        if ((rc = vct_shadow_depth(scene, &f->light_shadow, shadow_depth, f->shadow_width, f->shadow_height, ws,
+                                   stream)) != VCT_OK)
+            return rc;
+        sm.depth = shadow_depth;
+        sm.width = f->shadow_width;
+        sm.height = f->shadow_height;
     }
-    char* p = (char*)ws->ptr + off;
-    FragDesc* fr = (FragDesc*)p;
-    p += a256(sizeof(FragDesc) * (size_t)nfrag);
-    float4* rgb = (float4*)p;
-    p += a256(16 * (size_t)nrec);
-    uint32_t* kin = (uint32_t*)p;
-    uint32_t* kout = (uint32_t*)(p + r4);
-    uint32_t* vin = (uint32_t*)(p + 2 * r4);
-    uint32_t* vout = (uint32_t*)(p + 3 * r4);
-    uint32_t* heads = (uint32_t*)(p + 4 * r4);
-    uint32_t* nheads = (uint32_t*)(p + 5 * r4);
-    void* stmp = p + 5 * r4 + 256;
-    launch_cover<K_INJECT, P_WRITE>(A, plan, nullptr, offs, fr, nullptr, st);
-    VCT_LAUNCH_CHECK();
-    k_inject_shade<<<grid_of(nfrag, 256), 256, 0, st>>>(A, fr, nfrag, kin, vin, rgb);
-    VCT_LAUNCH_CHECK();
-    VCT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(stmp, sort_bytes, kin, kout, vin, vout, (int)nrec, 0, key_bits, st));
-    VCT_CUDA_TRY(cub::DeviceSelect::If(stmp, select_bytes, thrust::counting_iterator<uint32_t>(0u), heads, nheads,
-                                       (int64_t)nrec + 1, RunHead{kout, nrec}, st));
-    k_inject_fold<<<grid_of(nrec, 256), 256, 0, st>>>(kout, vout, rgb, heads, nheads, A.invalid_key, atlas);
-    VCT_LAUNCH_CHECK();
+    if ((rc = check_scene(scene)) != VCT_OK) return rc;
+    InjectState S;
+    RasterArgs I;
+    memset(&I, 0, sizeof(I));
+    if (scene->triangle_count > 0) {
+        RasterArgs C;  // the opacity pass over all six levels, counting the due levels' samples
+        memset(&C, 0, sizeof(C));
+        C.s = *scene;
+        C.kind = K_OPA_COUNT;
+        C.R = R;
+        C.W = C.H = R + 2;
+        fill_clipmap_levels(C, regions, R, 0x3Fu);
+        C.items = scene->triangle_count * C.nlevels;
+        C.atlas = opacity;
+        C.count_levels = due;
+        I = C;  // the injection's args over the same items
+        I.kind = K_INJECT;
+        I.atlas = radiance;
+        I.invalid_key = 0xffffffffu >> __builtin_clz((uint32_t)AtlasDims(R).texels());
+        if ((rc = fill_light(I, &sm, &f->light, &f->light_shadow)) != VCT_OK) return rc;
+        for (;;) {
+            rc = inject_prepare<K_OPA_COUNT>(C, I, ws, st, &S);
+            if (rc != kWorkspaceGrew) break;
+        }
+        if (rc != VCT_OK) return rc;
+    }
+    if ((rc = vct_downsample_all(opacity, regions, R, VCT_DOWNSAMPLE_OPACITY, stream)) != VCT_OK) return rc;
+    vct_border_wrapping_desc bw = {(uint32_t)R, VCT_VOXEL_BORDER, VCT_FACE_COUNT, VCT_CLIP_LEVEL_COUNT};
+    if ((rc = vct_wrap_border(opacity, &bw, stream)) != VCT_OK) return rc;
+    for (int l = 0; l < 6; ++l) {
+        if (!((due >> l) & 1u)) continue;
+        vct_image_cleaning_desc c = {{0, 0, 0}, l, {(uint32_t)R, (uint32_t)R, (uint32_t)R}, R, VCT_FACE_COUNT};
+        if ((rc = vct_clear_region(radiance, &c, stream)) != VCT_OK) return rc;
+    }
+    if (scene->triangle_count > 0) return inject_finish(I, S, st);
     return VCT_OK;
 }
+
+}  // namespace vct
 
 extern "C" int vct_svo_fragments(const vct_scene* scene, int32_t octree_level, const float bb_min[3],
                                  const float bb_max[3], const vct_shadow_map* shadow,
