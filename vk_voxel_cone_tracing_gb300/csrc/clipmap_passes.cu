@@ -32,14 +32,24 @@ __global__ void k_clear_region(uint32_t* __restrict__ atlas, AtlasDims A, int3 r
 // Thread per texel of one face row (x fastest) -> coalesced 4-byte RMW.
 // blockIdx.y = face; R is a power of two, so the (x, y, z) split is shifts.
 // `mirror` (0 = none): a texture array's surface that receives the same texels.
+// `touched` (may be null): texels whose bit is clear read as zero rgb.
+// (Both words are loaded unconditionally and selected, so the loads of a
+// thread's texels stay independent and in flight together.)
+__device__ __forceinline__ uint32_t rgb_of(const uint32_t* __restrict__ atlas, const uint32_t* __restrict__ touched,
+                                           int64_t i) {
+    const uint32_t r = atlas[i];
+    const uint32_t w = touched ? __ldg(touched + (i >> 5)) : 0xffffffffu;
+    return ((w >> (i & 31)) & 1u) ? (r & 0x00ffffffu) : 0u;
+}
+
 __global__ void k_copy_alpha(uint32_t* __restrict__ dst, const uint32_t* __restrict__ src, AtlasDims A, int level,
-                             int lg, cudaSurfaceObject_t mirror) {
+                             int lg, cudaSurfaceObject_t mirror, const uint32_t* __restrict__ touched) {
     const int f = blockIdx.y;
     const uint32_t n = 1u << (3 * lg), m = (1u << lg) - 1u;
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         const int x = (int)(t & m) + 1 + A.rb * f, y = (int)((t >> lg) & m) + 1 + level * A.rb, z = (int)(t >> (2 * lg)) + 1;
         const int64_t i = A.index(x, y, z);
-        const uint32_t v = (dst[i] & 0x00ffffffu) | (__ldg(src + i) & 0xff000000u);
+        const uint32_t v = rgb_of(dst, touched, i) | (__ldg(src + i) & 0xff000000u);
         dst[i] = v;
         if (mirror) surf3Dwrite(v, mirror, x * 4, y, z);
     }
@@ -182,7 +192,8 @@ __global__ void k_downsample(uint32_t* __restrict__ atlas, AtlasDims A, int3 pmi
 // then blend the 2x2x2 composite of level l-1 with that updated texel exactly
 // as k_downsample<1> does.  Same result as the two passes in sequence.
 __global__ void k_alpha_downsample(uint32_t* __restrict__ rad, const uint32_t* __restrict__ opa, AtlasDims A,
-                                   int3 pmin, int level, int band, int lg, cudaSurfaceObject_t mirror) {
+                                   int3 pmin, int level, int band, int lg, cudaSurfaceObject_t mirror,
+                                   const uint32_t* __restrict__ touched) {
     const int half = A.R >> 1;
     const uint32_t n = 1u << (3 * lg), m = (1u << lg) - 1u;
     const int pm[3] = {pmin.x, pmin.y, pmin.z};
@@ -219,7 +230,7 @@ __global__ void k_alpha_downsample(uint32_t* __restrict__ rad, const uint32_t* _
         uint32_t own6[6];
 #pragma unroll
         for (int f = 0; f < 6; ++f)
-            own6[f] = (rad[w0 + A.rb * f] & 0x00ffffffu) | (__ldg(opa + w0 + A.rb * f) & 0xff000000u);
+            own6[f] = rgb_of(rad, touched, w0 + A.rb * f) | (__ldg(opa + w0 + A.rb * f) & 0xff000000u);
         const int my = w[1] + 1 + A.rb * level, mz = w[2] + 1;
         if (!target) {
 #pragma unroll
@@ -296,7 +307,7 @@ extern "C" int vct_clear_region(uint32_t* atlas, const vct_image_cleaning_desc* 
 namespace vct {
 
 int copy_alpha_pass(uint32_t* dst, const uint32_t* src, const vct_copy_alpha_desc* d, cudaSurfaceObject_t mirror,
-                    cudaStream_t st) {
+                    const uint32_t* touched, cudaStream_t st) {
     VCT_CHECK_ARG(dst && src && d, "vct_copy_alpha: null argument");
     VCT_CHECK_ARG(valid_resolution(d->clipmap_resolution), "vct_copy_alpha: resolution must be a power of two in [8,1024]");
     VCT_CHECK_ARG(d->clip_level >= 0 && d->clip_level < VCT_CLIP_LEVEL_COUNT, "vct_copy_alpha: clip level out of range");
@@ -307,13 +318,13 @@ int copy_alpha_pass(uint32_t* dst, const uint32_t* src, const vct_copy_alpha_des
     const int lg = 31 - __builtin_clz((unsigned)A.R);
     const int64_t n = (int64_t)A.R * A.R * A.R;
     dim3 grid((unsigned)grid_for(n, 256), (unsigned)d->face_count);
-    k_copy_alpha<<<grid, 256, 0, st>>>(dst, src, A, d->clip_level, lg, mirror);
+    k_copy_alpha<<<grid, 256, 0, st>>>(dst, src, A, d->clip_level, lg, mirror, touched);
     VCT_LAUNCH_CHECK();
     return VCT_OK;
 }
 
 int copy_alpha_downsample_pass(uint32_t* radiance, const uint32_t* opacity, const vct_downsample_desc* d,
-                               cudaSurfaceObject_t mirror, cudaStream_t st) {
+                               cudaSurfaceObject_t mirror, const uint32_t* touched, cudaStream_t st) {
     VCT_CHECK_ARG(radiance && opacity && d, "vct_copy_alpha_downsample: null argument");
     VCT_CHECK_ARG(radiance != opacity, "vct_copy_alpha_downsample: radiance and opacity atlases must differ");
     VCT_CHECK_ARG(valid_resolution(d->clipmap_resolution),
@@ -327,7 +338,7 @@ int copy_alpha_downsample_pass(uint32_t* radiance, const uint32_t* opacity, cons
     int3 pm = make_int3(d->prev_region_min_corner[0], d->prev_region_min_corner[1], d->prev_region_min_corner[2]);
     const int lg = 31 - __builtin_clz((unsigned)A.R);
     k_alpha_downsample<<<grid_for(n, 128), 128, 0, st>>>(radiance, opacity, A, pm, d->clip_level,
-                                                        d->downsample_region_size, lg, mirror);
+                                                        d->downsample_region_size, lg, mirror, touched);
     VCT_LAUNCH_CHECK();
     return VCT_OK;
 }
@@ -345,7 +356,7 @@ static int mirror_surface(vct_texture_s* t, int R, const char* who, cudaSurfaceO
 }  // namespace vct
 
 extern "C" int vct_copy_alpha(uint32_t* dst, const uint32_t* src, const vct_copy_alpha_desc* d, void* stream) {
-    return copy_alpha_pass(dst, src, d, 0, as_stream(stream));
+    return copy_alpha_pass(dst, src, d, 0, nullptr, as_stream(stream));
 }
 
 extern "C" int vct_copy_alpha_downsample(uint32_t* radiance, const uint32_t* opacity, const vct_downsample_desc* d,
@@ -355,7 +366,7 @@ extern "C" int vct_copy_alpha_downsample(uint32_t* radiance, const uint32_t* opa
     int rc = mirror_surface(mirror, d->clipmap_resolution,
                             "vct_copy_alpha_downsample: the mirror must be an RGBA8 texture of the same resolution", &surf);
     if (rc != VCT_OK) return rc;
-    return copy_alpha_downsample_pass(radiance, opacity, d, surf, as_stream(stream));
+    return copy_alpha_downsample_pass(radiance, opacity, d, surf, nullptr, as_stream(stream));
 }
 
 extern "C" int vct_wrap_border(uint32_t* atlas, const vct_border_wrapping_desc* d, void* stream) {

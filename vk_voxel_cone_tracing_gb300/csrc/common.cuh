@@ -8,10 +8,14 @@
 
 #include "../../include/vct_capi.h"
 
-// Device scratch arena of the raster / SVO passes (vct_workspace).
+// Device scratch arena of the raster / SVO passes (vct_workspace), and a
+// second buffer that outlives a pass within one frame (the frame's
+// touched-texel bitmap).
 struct vct_workspace_s {
     void* ptr = nullptr;
     size_t bytes = 0;
+    void* aux = nullptr;
+    size_t aux_bytes = 0;
 };
 
 namespace vct {
@@ -28,17 +32,24 @@ int texture_format(const vct_texture_s* t);
 // Copy-alpha of one level, and copy-alpha + radiance mip of one level >= 1,
 // optionally mirroring every texel they write into a texture array's surface
 // (clipmap_passes.cu).
+// `touched` (may be null): a bitmap over the atlas's texel indices; a texel
+// whose bit is clear is read as zero rgb (the frame's radiance clear folded
+// into these passes).
 int copy_alpha_pass(uint32_t* dst, const uint32_t* src, const vct_copy_alpha_desc* d, cudaSurfaceObject_t mirror,
-                    cudaStream_t st);
+                    const uint32_t* touched, cudaStream_t st);
 int copy_alpha_downsample_pass(uint32_t* radiance, const uint32_t* opacity, const vct_downsample_desc* d,
-                               cudaSurfaceObject_t mirror, cudaStream_t st);
+                               cudaSurfaceObject_t mirror, const uint32_t* touched, cudaStream_t st);
 
 // The frame's rasterised passes with the deterministic injection, up to the
 // fold (raster.cu): opacity clear + voxelisation + mips + border, shadow
 // depth, clear of the due radiance levels and the injection.
+// The radiance levels due are not cleared: the fold starts their texels from
+// zero and marks each texel it writes in *touched (a bitmap over the atlas's
+// texel indices, in the workspace's second buffer), and the copy-alpha / mip
+// passes read unmarked texels as zero rgb -- the cleared result.
 int frame_raster_passes(const vct_scene* scene, const vct_frame_desc* f, const vct_clipmap_region regions[6],
                         uint32_t due, uint32_t* opacity, uint32_t* radiance, float* shadow_depth, vct_workspace_s* ws,
-                        cudaStream_t st);
+                        const uint32_t** touched, cudaStream_t st);
 
 // ---------------------------------------------------------------- errors
 void set_error(const std::string& msg);

@@ -35,11 +35,13 @@ extern "C" int vct_clipmap_frame(const vct_scene* scene, const vct_frame_desc* f
         if (f->frame_index % (1 << l) == 0) due |= 1u << l;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
 
+    const uint32_t* touched = nullptr;  // deterministic mode: the due levels' clear happens in the passes below
     if (f->inject_mode == VCT_INJECT_DETERMINISTIC) {
         // VoxelizationPass, RSMPass and RadianceInjectionPass up to the fold,
         // with the opacity voxelisation and the injection's coverage count
         // sharing one coverage pass (same results as the passes below)
-        if ((rc = vct::frame_raster_passes(scene, f, regions, due, opacity, radiance, shadow_depth, ws, st)) != VCT_OK)
+        if ((rc = vct::frame_raster_passes(scene, f, regions, due, opacity, radiance, shadow_depth, ws, &touched,
+                                           st)) != VCT_OK)
             return rc;
     } else {
         // VoxelizationPass (full revoxelisation every frame, VoxelizationPass.cpp:79-125)
@@ -80,7 +82,7 @@ extern "C" int vct_clipmap_frame(const vct_scene* scene, const vct_frame_desc* f
     const cudaSurfaceObject_t mirror = f->radiance_texture ? vct::texture_surface(f->radiance_texture) : 0;
     if (due & 1u) {
         vct_copy_alpha_desc ca = {0, R, VCT_FACE_COUNT};
-        if ((rc = vct::copy_alpha_pass(radiance, opacity, &ca, mirror, st)) != VCT_OK) return rc;
+        if ((rc = vct::copy_alpha_pass(radiance, opacity, &ca, mirror, touched, st)) != VCT_OK) return rc;
     }
     for (int l = 1; l < 6; ++l) {
         if (!((due >> l) & 1u)) continue;
@@ -89,7 +91,7 @@ extern "C" int vct_clipmap_frame(const vct_scene* scene, const vct_frame_desc* f
         d.clip_level = l;
         d.clipmap_resolution = R;
         d.downsample_region_size = VCT_DOWNSAMPLE_REGION_SIZE;
-        if ((rc = vct::copy_alpha_downsample_pass(radiance, opacity, &d, mirror, st)) != VCT_OK) return rc;
+        if ((rc = vct::copy_alpha_downsample_pass(radiance, opacity, &d, mirror, touched, st)) != VCT_OK) return rc;
     }
     return VCT_OK;
 }

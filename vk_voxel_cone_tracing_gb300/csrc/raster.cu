@@ -974,16 +974,20 @@ struct SumU2 {
 // of records k*.. from zero, and a run costs at most 256 serial steps however
 // many records land on its texel (fragments clamped onto region borders pile
 // hundreds of thousands onto single texels).
+// `touched` (the frame's path, may be null): the texels start from zero (their
+// level is being refreshed) and each one written is marked in the bitmap.
 __global__ void __launch_bounds__(256) k_inject_fold(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ order,
                                                      const float4* __restrict__ rgb, const uint32_t* __restrict__ heads,
                                                      const uint32_t* __restrict__ nheads, uint32_t invalid_key,
-                                                     uint32_t* __restrict__ atlas) {
+                                                     uint32_t* __restrict__ atlas, uint32_t* __restrict__ touched) {
     const uint32_t nruns = *nheads - 1u;
     for (uint32_t h = blockIdx.x * blockDim.x + threadIdx.x; h < nruns; h += gridDim.x * blockDim.x) {
         const uint32_t s = heads[h], e = heads[h + 1];
         const uint32_t key = keys[s];
         if (key == invalid_key) continue;
-        uint32_t cell = atlas[key];
+        uint32_t cell = 0u;
+        if (touched) atomicOr(touched + (key >> 5), 1u << (key & 31u));
+        else cell = atlas[key];
         const uint32_t len = e - s;
         const uint32_t k0 = (256u - (cell >> 24)) & 255u;  // first step whose input alpha is 0
         uint32_t j = s;
@@ -1183,7 +1187,7 @@ static int inject_prepare(RasterArgs& C, RasterArgs& I, vct_workspace_s* ws, cud
 
 // Shade the emitted samples into face records (needs the light and shadow
 // map in `I`), sort them stably by texel and fold every texel's run.
-static int inject_finish(const RasterArgs& I, const InjectState& S, cudaStream_t st) {
+static int inject_finish(const RasterArgs& I, const InjectState& S, uint32_t* touched, cudaStream_t st) {
     if (S.nfrag == 0) return VCT_OK;
     const uint32_t nfrag = S.nfrag, nrec = S.nrec;
     k_inject_shade<<<grid_of(nfrag, 256), 256, 0, st>>>(I, S.fr, nfrag, S.kin, S.vin, S.rgb);
@@ -1193,7 +1197,8 @@ static int inject_finish(const RasterArgs& I, const InjectState& S, cudaStream_t
     tb = S.select_bytes;
     VCT_CUDA_TRY(cub::DeviceSelect::If(S.stmp, tb, thrust::counting_iterator<uint32_t>(0u), S.heads, S.nheads,
                                        (int64_t)nrec + 1, RunHead{S.kout, nrec}, st));
-    k_inject_fold<<<grid_of(nrec, 256), 256, 0, st>>>(S.kout, S.vout, S.rgb, S.heads, S.nheads, I.invalid_key, I.atlas);
+    k_inject_fold<<<grid_of(nrec, 256), 256, 0, st>>>(S.kout, S.vout, S.rgb, S.heads, S.nheads, I.invalid_key, I.atlas,
+                                                      touched);
     VCT_LAUNCH_CHECK();
     return VCT_OK;
 }
@@ -1249,6 +1254,10 @@ extern "C" int vct_workspace_create(size_t initial_bytes, vct_workspace_s** out)
 extern "C" int vct_workspace_destroy(vct_workspace_s* w) {
     if (!w) return VCT_OK;
     cudaError_t e = w->ptr ? cudaFree(w->ptr) : cudaSuccess;
+    if (w->aux) {
+        cudaError_t e2 = cudaFree(w->aux);
+        if (e == cudaSuccess) e = e2;
+    }
     delete w;
     if (e != cudaSuccess) return cuda_fail(e, "cudaFree (workspace)");
     return VCT_OK;
@@ -1397,7 +1406,7 @@ extern "C" int vct_inject_radiance(const vct_scene* scene, const vct_clipmap_reg
     if (rc == kWorkspaceGrew)
         return vct_inject_radiance(scene, regions, R, shadow, light, light_shadow, atlas, level_mask, mode, ws, stream);
     if (rc != VCT_OK) return rc;
-    return inject_finish(A, S, st);
+    return inject_finish(A, S, nullptr, st);
 }
 
 namespace vct {
@@ -1413,10 +1422,25 @@ namespace vct {
 // by one in the reference's order.
 int frame_raster_passes(const vct_scene* scene, const vct_frame_desc* f, const vct_clipmap_region regions[6],
                         uint32_t due, uint32_t* opacity, uint32_t* radiance, float* shadow_depth, vct_workspace_s* ws,
-                        cudaStream_t st) {
+                        const uint32_t** touched_out, cudaStream_t st) {
     const int R = f->clipmap_resolution;
     void* stream = st;
     int rc;
+    // the touched-texel bitmap, one bit per atlas texel, cleared every frame
+    const size_t bm_bytes = a256(((size_t)AtlasDims(R).texels() + 31) / 32 * 4);
+    if (ws->aux_bytes < bm_bytes) {
+        if (ws->aux) {
+            VCT_CUDA_TRY(cudaDeviceSynchronize());
+            VCT_CUDA_TRY(cudaFree(ws->aux));
+            ws->aux = nullptr;
+            ws->aux_bytes = 0;
+        }
+        VCT_CUDA_TRY(cudaMalloc(&ws->aux, bm_bytes));
+        ws->aux_bytes = bm_bytes;
+    }
+    uint32_t* touched = (uint32_t*)ws->aux;
+    VCT_CUDA_TRY(cudaMemsetAsync(touched, 0, bm_bytes, st));
+    *touched_out = touched;
     if ((rc = vct_clear_atlas(opacity, R, stream)) != VCT_OK) return rc;
     vct_shadow_map sm = {nullptr, 0, 0};
     if (f->shadow_width > 0) {
@@ -1456,12 +1480,9 @@ int frame_raster_passes(const vct_scene* scene, const vct_frame_desc* f, const v
     if ((rc = vct_downsample_all(opacity, regions, R, VCT_DOWNSAMPLE_OPACITY, stream)) != VCT_OK) return rc;
     vct_border_wrapping_desc bw = {(uint32_t)R, VCT_VOXEL_BORDER, VCT_FACE_COUNT, VCT_CLIP_LEVEL_COUNT};
     if ((rc = vct_wrap_border(opacity, &bw, stream)) != VCT_OK) return rc;
-    for (int l = 0; l < 6; ++l) {
-        if (!((due >> l) & 1u)) continue;
-        vct_image_cleaning_desc c = {{0, 0, 0}, l, {(uint32_t)R, (uint32_t)R, (uint32_t)R}, R, VCT_FACE_COUNT};
-        if ((rc = vct_clear_region(radiance, &c, stream)) != VCT_OK) return rc;
-    }
-    if (scene->triangle_count > 0) return inject_finish(I, S, st);
+    // the due radiance levels' clear is folded into the fold (texels start from
+    // zero) and the copy-alpha / mip passes (unmarked texels read as zero rgb)
+    if (scene->triangle_count > 0) return inject_finish(I, S, touched, st);
     return VCT_OK;
 }
 
