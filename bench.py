@@ -301,8 +301,10 @@ def run_ours(args, world, rank, local):
     import ctypes as C
     nodes = C.c_int64(0)
 
-    def svo():
-        f = passes.svo_fragments(ds, SVO_LEVEL, shadow, light, lsd, ws)
+    svo_buf = torch.empty((int(frags.shape[0] * 1.25) + 1024, 2), dtype=torch.int32, device=dev)
+
+    def svo():  # one fragment-list call per build: the buffer is sized from the first frame's count
+        f = passes.svo_fragments(ds, SVO_LEVEL, shadow, light, lsd, ws, out=svo_buf)
         capi.call("vct_svo_build", f.data_ptr(), f.shape[0], SVO_LEVEL, pool.data_ptr(), pool_cap,
                   capi.SVO_DETERMINISTIC, C.byref(nodes), ws.handle, C.c_void_p(stream.cuda_stream))
 

@@ -109,3 +109,21 @@ def test_svo_cone_trace_matches_oracle(cuda, oracle, setup):
     for got, want in ((d[:, :3], d64[:, :3]), (s[:, :3], s64[:, :3])):
         assert np.linalg.norm(got - want) / max(np.linalg.norm(want), 1e-12) < 1e-2
     assert abs(int(steps.item()) - st32) <= max(8, 0.002 * st32)
+
+
+def test_fragment_list_into_a_given_buffer(cuda, setup):
+    """svo_fragments(out=...) writes the list in one call when the buffer is
+    large enough, and repeats into a new buffer when it is too small; both
+    equal the two-step (count, then write) list bit for bit."""
+    torch = cuda
+    from vk_voxel_cone_tracing_gb300 import passes
+    scene, ds, ws, origin, sd_o, shadow = setup
+    sh = torch.from_numpy(shadow).cuda()
+    light, sd = passes.light_desc(LIGHT_DIR), passes.light_shadow_desc(origin, LIGHT_DIR)
+    want = passes.svo_fragments(ds, 6, sh, light, sd, ws).cpu().numpy()
+    big = torch.full((want.shape[0] + 100, 2), -1, dtype=torch.int32, device="cuda")
+    got = passes.svo_fragments(ds, 6, sh, light, sd, ws, out=big)
+    assert got.data_ptr() == big.data_ptr() and np.array_equal(got.cpu().numpy(), want)
+    small = torch.empty((want.shape[0] // 2, 2), dtype=torch.int32, device="cuda")
+    got2 = passes.svo_fragments(ds, 6, sh, light, sd, ws, out=small)
+    assert np.array_equal(got2.cpu().numpy(), want)

@@ -14,6 +14,7 @@
 // without the shader's per-fragment redundancy.
 // Compiled with -fmad=false.
 #include <cub/cub.cuh>
+#include <thrust/iterator/counting_iterator.h>
 
 #include "common.cuh"
 
@@ -136,13 +137,35 @@ __global__ void k_leaf_keys(const uint32_t* __restrict__ cursor, int64_t F, uint
     }
 }
 
-__global__ void k_leaf_fold(uint2* pool, const uint2* __restrict__ frags, const uint32_t* __restrict__ keys,
-                            const uint32_t* __restrict__ order, int64_t F) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < F; i += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t key = keys[i];
-        if (key == 0xffffffffu || (i > 0 && keys[i - 1] == key)) continue;
+// Boundaries of the leaf runs in the sorted keys over positions [0, n]: every
+// position whose key differs from its predecessor, plus 0 and n.
+struct LeafRunHead {
+    const uint32_t* keys;
+    uint32_t n;
+    __device__ bool operator()(uint32_t i) const { return i == 0 || i == n || keys[i - 1] != keys[i]; }
+};
+
+// Sequential fold of each leaf's fragments in fragment order (the stable sort
+// keeps it), one thread per leaf run.
+__global__ void __launch_bounds__(256) k_leaf_fold(uint2* pool, const uint2* __restrict__ frags,
+                                                   const uint32_t* __restrict__ keys, const uint32_t* __restrict__ order,
+                                                   const uint32_t* __restrict__ heads,
+                                                   const uint32_t* __restrict__ nheads) {
+    const uint32_t nruns = *nheads - 1u;
+    for (uint32_t h = blockIdx.x * blockDim.x + threadIdx.x; h < nruns; h += gridDim.x * blockDim.x) {
+        const uint32_t s = heads[h], e = heads[h + 1];
+        const uint32_t key = keys[s];
         uint32_t cell = pool[key].y;
-        for (int64_t j = i; j < F && keys[j] == key; ++j) cell = avg_fold(cell, frags[order[j]].y & 0xfffffffu);
+        // the fold is a serial chain; fetch four fragments ahead of it
+        for (uint32_t j = s; j < e; j += 4) {
+            uint32_t v4[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (j + u < e) v4[u] = __ldg(&frags[order[j + u]].y) & 0xfffffffu;
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (j + u < e) cell = avg_fold(cell, v4[u]);
+        }
         pool[key].y = cell;
     }
 }
@@ -252,13 +275,16 @@ extern "C" int vct_svo_build(const uint32_t* fragments, int64_t F, int32_t L, ui
     const uint2* frags = reinterpret_cast<const uint2*>(fragments);
     const uint32_t res = 1u << L;
     // workspace: flags, ranks (window sized: <= capacity), scan temp, counter, leaf sort buffers
-    size_t scan_bytes = 0, sort_bytes = 0;
+    size_t scan_bytes = 0, sort_bytes = 0, select_bytes = 0;
     VCT_CUDA_TRY(cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, (uint32_t*)nullptr, (uint32_t*)nullptr, (int)capacity));
     const int64_t Fs = F > 0 ? F : 1;
     VCT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(nullptr, sort_bytes, (uint32_t*)nullptr, (uint32_t*)nullptr,
                                                  (uint32_t*)nullptr, (uint32_t*)nullptr, (int)Fs, 0, 32));
-    const size_t cap_arr = a256s(4 * (size_t)capacity), f_arr = a256s(4 * (size_t)Fs);
-    const size_t need = 2 * cap_arr + a256s(scan_bytes) + 256 + 5 * f_arr + a256s(sort_bytes);
+    VCT_CUDA_TRY(cub::DeviceSelect::If(nullptr, select_bytes, thrust::counting_iterator<uint32_t>(0u), (uint32_t*)nullptr,
+                                       (uint32_t*)nullptr, (int64_t)Fs + 1, LeafRunHead{nullptr, (uint32_t)Fs}));
+    if (select_bytes > sort_bytes) sort_bytes = select_bytes;
+    const size_t cap_arr = a256s(4 * (size_t)capacity), f_arr = a256s(4 * (size_t)Fs + 4);
+    const size_t need = 2 * cap_arr + a256s(scan_bytes) + 256 + 6 * f_arr + 256 + a256s(sort_bytes);
     int rc = workspace_reserve(ws, need);
     if (rc != VCT_OK) return rc;
     char* b = (char*)ws->ptr;
@@ -272,7 +298,9 @@ extern "C" int vct_svo_build(const uint32_t* fragments, int64_t F, int32_t L, ui
     uint32_t* vin = (uint32_t*)(fb + 2 * f_arr);
     uint32_t* vout = (uint32_t*)(fb + 3 * f_arr);
     uint32_t* cursor = (uint32_t*)(fb + 4 * f_arr);
-    void* stmp = fb + 5 * f_arr;
+    uint32_t* heads = (uint32_t*)(fb + 5 * f_arr);
+    uint32_t* nheads = (uint32_t*)(fb + 6 * f_arr);
+    void* stmp = fb + 6 * f_arr + 256;
 
     uint64_t begin = 0, num = 8, count = 0;
     uint64_t wbegin[12], wnum[12];
@@ -312,9 +340,14 @@ extern "C" int vct_svo_build(const uint32_t* fragments, int64_t F, int32_t L, ui
         if (mode == VCT_SVO_DETERMINISTIC) {
             k_leaf_keys<<<grid_n(F), 256, 0, st>>>(cursor, F, kin, vin);
             VCT_LAUNCH_CHECK();
+            // leaf indices are node indices < node_count: sort only those bits
+            const int key_bits = 32 - __builtin_clz((unsigned)(*node_count - 1));
             size_t tb = sort_bytes;
-            VCT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(stmp, tb, kin, kout, vin, vout, (int)F, 0, 32, st));
-            k_leaf_fold<<<grid_n(F), 256, 0, st>>>(pool, frags, kout, vout, F);
+            VCT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(stmp, tb, kin, kout, vin, vout, (int)F, 0, key_bits, st));
+            tb = sort_bytes;
+            VCT_CUDA_TRY(cub::DeviceSelect::If(stmp, tb, thrust::counting_iterator<uint32_t>(0u), heads, nheads,
+                                               (int64_t)F + 1, LeafRunHead{kout, (uint32_t)F}, st));
+            k_leaf_fold<<<grid_n(F), 256, 0, st>>>(pool, frags, kout, vout, heads, nheads);
             VCT_LAUNCH_CHECK();
         } else {
             int* err = (int*)flags;

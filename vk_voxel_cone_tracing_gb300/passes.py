@@ -106,18 +106,34 @@ def inject_radiance(dscene: DeviceScene, regions, R: int, depth: torch.Tensor | 
 
 
 def svo_fragments(dscene: DeviceScene, level: int, depth: torch.Tensor | None, light: capi.DirectionalLightDesc,
-                  sd: capi.DirectionalLightShadowDesc, ws: Workspace, bb_min=None, bb_max=None):
-    """Count pass + write pass; returns an (F, 2) int32 tensor of packed fragments."""
+                  sd: capi.DirectionalLightShadowDesc, ws: Workspace, bb_min=None, bb_max=None,
+                  out: torch.Tensor | None = None):
+    """The SVO fragment list as an (F, 2) int32 tensor (a view of `out` when it is large enough).
+
+    Without `out` this is the reference's two-step shape: a count-only call, then the write into a buffer
+    of that size.  With `out` (for instance the previous frame's list) it is one call; when `out` is too
+    small the call reports the count and is repeated into a new buffer."""
     bmin = (C.c_float * 3)(*(dscene.bb_min if bb_min is None else bb_min))
     bmax = (C.c_float * 3)(*(dscene.bb_max if bb_max is None else bb_max))
     sm = _shadow_map(depth)
     count = C.c_int64(0)
-    capi.call("vct_svo_fragments", capi.ref(dscene.desc), level, C.cast(bmin, C.c_void_p), C.cast(bmax, C.c_void_p),
-              capi.ref(sm), capi.ref(light), capi.ref(sd), None, 0, C.byref(count), ws.handle, _stream())
+
+    def run(buf, cap):
+        return capi.lib().vct_svo_fragments(capi.ref(dscene.desc), level, C.cast(bmin, C.c_void_p),
+                                            C.cast(bmax, C.c_void_p), capi.ref(sm), capi.ref(light), capi.ref(sd),
+                                            _ptr(buf) if buf is not None else None, cap, C.byref(count),
+                                            ws.handle, _stream())
+
+    if out is not None and out.shape[0] > 0:
+        rc = run(out, out.shape[0])
+        if rc == capi.VCT_OK:
+            return out[:count.value]
+        if rc != capi.VCT_E_OVERFLOW:
+            capi.check("vct_svo_fragments", rc)
+    else:
+        capi.check("vct_svo_fragments", run(None, 0))
     frags = torch.empty((max(count.value, 1), 2), dtype=torch.int32, device=dscene.positions.device)
-    capi.call("vct_svo_fragments", capi.ref(dscene.desc), level, C.cast(bmin, C.c_void_p), C.cast(bmax, C.c_void_p),
-              capi.ref(sm), capi.ref(light), capi.ref(sd), _ptr(frags), count.value, C.byref(count), ws.handle,
-              _stream())
+    capi.check("vct_svo_fragments", run(frags, count.value))
     return frags[:count.value]
 
 
