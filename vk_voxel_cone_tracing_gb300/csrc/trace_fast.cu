@@ -186,8 +186,8 @@ constexpr int kWarpsPerBlock = 8;
 __global__ void __launch_bounds__(256) k_trace_diffuse(const __grid_constant__ FastArgs A, const uint32_t* __restrict__ order) {
     __shared__ float4 s_start[kWarpsPerBlock][32];
     __shared__ float4 s_norm[kWarpsPerBlock][32];
-    __shared__ int s_incl[kWarpsPerBlock][32];
-    __shared__ uint32_t s_mask[kWarpsPerBlock][32];
+    __shared__ int s_cincl[kWarpsPerBlock][32];     // inclusive prefix of the pairs per cone
+    __shared__ uint32_t s_cmask[kWarpsPerBlock][32];  // samples (lanes) that trace each cone
     __shared__ float4 s_res[kWarpsPerBlock][32];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const TraceParams& P = A.P;
@@ -218,38 +218,48 @@ __global__ void __launch_bounds__(256) k_trace_diffuse(const __grid_constant__ F
                     if (!(dot3(g.normal, dir) < 0.0f)) mask |= 1u << c;
                 }
         }
-        const int cnt = __popc(mask);
-        int incl = cnt;
+        // Deal the (sample, cone) pairs cone-major: lane k of a round takes the
+        // k-th pair of the list ordered by cone, then by sample, so neighbouring
+        // lanes march the same direction from neighbouring (Morton-ordered)
+        // samples and share texels.  Cone c's pairs are the lanes of cmask[c].
+        uint32_t my_cmask = 0;
+        for (int c = 0; c < C.ncones; ++c) {
+            const uint32_t cm = __ballot_sync(0xffffffffu, (mask >> c) & 1u);
+            if (lane == c) my_cmask = cm;
+        }
+        int cincl = __popc(my_cmask);
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const int t = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += t;
+            const int t = __shfl_up_sync(0xffffffffu, cincl, o);
+            if (lane >= o) cincl += t;
         }
-        const int total = __shfl_sync(0xffffffffu, incl, 31);
-        const int excl = incl - cnt;
+        const int total = __shfl_sync(0xffffffffu, cincl, 31);
         s_start[w][lane] = make_float4(start.x, start.y, start.z, min_level);
         s_norm[w][lane] = valid ? make_float4(g.normal.x, g.normal.y, g.normal.z, 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
-        s_incl[w][lane] = incl;
-        s_mask[w][lane] = mask;
+        s_cincl[w][lane] = cincl;
+        s_cmask[w][lane] = my_cmask;
         __syncwarp();
         float4 acc = make_float4(0.f, 0.f, 0.f, 1.f);
+        const uint32_t below = (1u << lane) - 1u;
+        uint32_t pending = mask;  // this lane's cones not yet added, added in cone order
         for (int r0 = 0; r0 < total; r0 += 32) {
             const int k = r0 + lane;
             float4 res = make_float4(0.f, 0.f, 0.f, 0.f);
             if (k < total) {
-                int lo = 0, hi = 31;  // first lane with incl > k
+                int lo = 0, hi = 31;  // the cone whose inclusive prefix first exceeds k
                 while (lo < hi) {
                     const int mid = (lo + hi) >> 1;
-                    if (s_incl[w][mid] > k) hi = mid;
+                    if (s_cincl[w][mid] > k) hi = mid;
                     else lo = mid + 1;
                 }
-                const uint32_t m = s_mask[w][lo];
-                const int j = k - (s_incl[w][lo] - __popc(m));
-                const int cone = (int)__fns(m, 0, j + 1);
+                const int cone = lo;
+                const uint32_t cm = s_cmask[w][cone];
+                const int j = k - (s_cincl[w][cone] - __popc(cm));
+                const int sl = (int)__fns(cm, 0, j + 1);  // the sample's lane
                 const float3 dir = c32 ? f3(c_dirs32[cone][0], c_dirs32[cone][1], c_dirs32[cone][2])
                                        : f3(c_dirs16[cone][0], c_dirs16[cone][1], c_dirs16[cone][2]);
-                const float4 st = s_start[w][lo];
-                const float4 nn = s_norm[w][lo];
+                const float4 st = s_start[w][sl];
+                const float4 nn = s_norm[w][sl];
                 const float cos_t = nn.x * dir.x + nn.y * dir.y + nn.z * dir.z;
                 const float4 r =
                     trace_cone_fast(A.tex, C, f3(st.x, st.y, st.z), dir, C.coef_diffuse, st.w, C.sf_diffuse, steps);
@@ -257,10 +267,16 @@ __global__ void __launch_bounds__(256) k_trace_diffuse(const __grid_constant__ F
             }
             s_res[w][lane] = res;
             __syncwarp();
-            const int a = max(excl, r0), b = min(incl, r0 + 32);
-            for (int q = a; q < b; ++q) {
-                const float4 v = s_res[w][q - r0];
+            // this lane's pairs in this round, lowest cone first: a pair's index
+            // grows with its cone, so the sum runs in cone order (the shader's)
+            while (pending) {
+                const int c = __ffs(pending) - 1;
+                const uint32_t cm = s_cmask[w][c];
+                const int pidx = s_cincl[w][c] - __popc(cm) + __popc(cm & below);
+                if (pidx >= r0 + 32) break;
+                const float4 v = s_res[w][pidx - r0];
                 acc = make_float4(acc.x + v.x, acc.y + v.y, acc.z + v.z, acc.w + v.w);
+                pending &= pending - 1u;
             }
             __syncwarp();
         }
