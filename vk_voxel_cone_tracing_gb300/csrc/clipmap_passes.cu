@@ -191,7 +191,7 @@ __global__ void k_downsample(uint32_t* __restrict__ atlas, AtlasDims A, int3 pmi
 // the (R/2)^3 block from the previous region's corner / 2 on, toroidally --
 // then blend the 2x2x2 composite of level l-1 with that updated texel exactly
 // as k_downsample<1> does.  Same result as the two passes in sequence.
-__global__ void k_alpha_downsample(uint32_t* __restrict__ rad, const uint32_t* __restrict__ opa, AtlasDims A,
+__global__ void __launch_bounds__(128, 8) k_alpha_downsample(uint32_t* __restrict__ rad, const uint32_t* __restrict__ opa, AtlasDims A,
                                    int3 pmin, int level, int band, int lg, cudaSurfaceObject_t mirror,
                                    const uint32_t* __restrict__ touched) {
     const int half = A.R >> 1;
@@ -240,8 +240,8 @@ __global__ void k_alpha_downsample(uint32_t* __restrict__ rad, const uint32_t* _
             }
             continue;
         }
-#pragma unroll
-        for (int f = 0; f < 6; ++f) {
+#pragma unroll 1
+        for (int f = 0; f < 6; ++f) {  // the composite path: one face at a time keeps 8 blocks per SM resident
             const int64_t wi = w0 + A.rb * f;
             const uint32_t own_raw = own6[f];
             uint32_t raw[8];
