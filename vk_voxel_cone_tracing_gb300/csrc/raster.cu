@@ -730,7 +730,7 @@ __device__ inline uint32_t cover_pixel(const TileRegs& t, const TileSlot& T, int
 //   (earlier rounds' count + a warp scan over the lanes of the same tile).
 // A tile's item comes from the tile plan's tile -> item array.
 template <int KIND, int PHASE>
-__global__ void __launch_bounds__(128) k_cover(const __grid_constant__ RasterArgs A, const TilePlan plan,
+__global__ void __launch_bounds__(128, 6) k_cover(const __grid_constant__ RasterArgs A, const TilePlan plan,
                                                uint2* __restrict__ counts, const uint2* __restrict__ offs,
                                                FragDesc* __restrict__ frags, int* __restrict__ err) {
     constexpr int NS = KIND == K_SHADOW ? 1 : 8;
