@@ -260,25 +260,6 @@ __device__ inline uint32_t tiles_of(const RSetup& r) {
     return (uint32_t)(((r.px1 - r.px0) >> 3) + 1) * (uint32_t)(((r.py1 - r.py0) >> 3) + 1);
 }
 
-__device__ inline bool raster_test(const RSetup& r, long long sx, long long sy, float b[3], float& z) {
-    long long e[3];
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        const int a = (i + 1) % 3, c = (i + 2) % 3;
-        e[i] = (r.X[c] - r.X[a]) * (sy - r.Y[a]) - (r.Y[c] - r.Y[a]) * (sx - r.X[a]);
-        if (e[i] < 0 || (e[i] == 0 && !((r.owned >> i) & 1))) return false;
-    }
-    float bo[3];
-#pragma unroll
-    for (int i = 0; i < 3; ++i) bo[i] = (float)e[i] * r.inv_area;
-    z = (bo[0] * r.z[0] + bo[1] * r.z[1]) + bo[2] * r.z[2];
-    if (!(z >= 0.0f && z <= 1.0f)) return false;
-    b[0] = bo[0];
-    b[1] = r.swapped ? bo[2] : bo[1];
-    b[2] = r.swapped ? bo[1] : bo[2];
-    return true;
-}
-
 __device__ inline float3 interp3(const float b[3], const float3 v[3]) {
     return make_float3((b[0] * v[0].x + b[1] * v[1].x) + b[2] * v[2].x, (b[0] * v[0].y + b[1] * v[1].y) + b[2] * v[2].y,
                        (b[0] * v[0].z + b[1] * v[1].z) + b[2] * v[2].z);
@@ -583,7 +564,10 @@ __host__ __device__ constexpr int sample_y(int s) {
 // The set-up triangle of one tile in the form the per-pixel tests use.  Edge
 // i runs from vertex a = (i+1)%3 to c = (i+2)%3 and
 //   e_i(x, y) = dX_i * (y - Y_a) - dY_i * (x - X_a)        (1/256-pixel units),
-// raster_test's edge function.  The tile keeps E_i = e_i at its corner
+// the pinned edge function: a sample is covered when every e_i > 0, or
+// e_i == 0 on an edge that owns its ties, and its interpolated depth
+// (b0 z0 + b1 z1) + b2 z2 with b_i = float(e_i) * inv_area lies in [0, 1].
+// The tile keeps E_i = e_i at its corner
 // (tx * 256, ty * 256); a sample at offset (ox, oy) from that corner has
 // e_i = E_i + dX_i * oy - dY_i * ox, the same int64 value (equal modulo 2^64
 // even where a product wrapped).
@@ -654,7 +638,7 @@ __device__ inline bool tile_regs(const RSetup& rs, int tx, int ty, TileSlot& T) 
 }
 
 // Barycentrics and depth of the sample at offset (ox, oy) from the tile
-// corner -- raster_test's arithmetic.
+// corner: the pinned FP32 barycentrics and depth.
 __device__ inline void sample_bz(const TileRegs& t, const TileSlot& T, int ox, int oy, float b[3], float& z) {
     float bo[3];
 #pragma unroll
@@ -802,6 +786,39 @@ __global__ void __launch_bounds__(128, 6) k_cover(const __grid_constant__ Raster
         __syncwarp();
         TileRegs t;
         int cj = -1;
+        if (KIND == K_SHADOW) {
+            // one centre sample per pixel: each lane takes four consecutive
+            // pixels of the list per round, so the tile search and slot reload
+            // are shared by four depth tests
+            for (uint32_t q0 = (uint32_t)lane * 4u; q0 < P; q0 += 128u) {
+                int lo = 0, hi = 31;
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (S[mid].px_end > q0) hi = mid;
+                    else lo = mid + 1;
+                }
+                int j = lo;
+                for (uint32_t q = q0; q < q0 + 4u && q < P; ++q) {
+                    while (S[j].px_end <= q) ++j;  // the next pixel's tile (at most 3 steps)
+                    if (j != cj) {
+                        t = S[j].t;
+                        cj = j;
+                    }
+                    const uint32_t start = j > 0 ? S[j - 1].px_end : 0u;
+                    const uint32_t lp = q - start, tw = (uint32_t)S[j].tw;
+                    const uint32_t row = tw > 1u ? __umulhi(lp, S[j].tw_magic) : lp;
+                    const int ox0 = (int)(lp - row * tw) * 256, oy0 = (int)row * 256;
+                    if (cover_pixel<1>(t, S[j], ox0, oy0)) {
+                        float b[3], z;
+                        sample_bz(t, S[j], ox0 + 128, oy0 + 128, b, z);
+                        const int px = S[j].tx + (ox0 >> 8), py = S[j].ty + (oy0 >> 8);
+                        atomicMin(reinterpret_cast<unsigned int*>(A.depth) + (int64_t)py * A.W + px, __float_as_uint(z));
+                    }
+                }
+            }
+            __syncwarp();
+            continue;
+        }
         for (uint32_t q0 = 0; q0 < P; q0 += 32u) {
             const uint32_t q = q0 + lane;
             const bool act = q < P;
