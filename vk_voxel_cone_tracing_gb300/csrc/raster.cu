@@ -711,7 +711,8 @@ __device__ inline uint32_t cover_pixel(const TileRegs& t, const TileSlot& T, int
 //   P_DIRECT writes the pass's output (opacity, shadow depth, atomic injection);
 //   P_COUNT counts covered samples and their records per tile;
 //   P_WRITE emits one FragDesc per covered sample at its rank within the tile
-//   (earlier rounds' count + a warp scan over the lanes of the same tile).
+//   (earlier rounds' count + a warp scan over the lanes of the same tile),
+//   skipping the tiles whose count (`counts`, from P_COUNT) is zero.
 // A tile's item comes from the tile plan's tile -> item array.
 template <int KIND, int PHASE>
 __global__ void __launch_bounds__(128, 6) k_cover(const __grid_constant__ RasterArgs A, const TilePlan plan,
@@ -729,7 +730,8 @@ __global__ void __launch_bounds__(128, 6) k_cover(const __grid_constant__ Raster
     for (uint32_t ch = blockIdx.x * 4u + (threadIdx.x >> 5); ch < nchunks; ch += gridDim.x * 4u) {
         const uint32_t g = ch * 32u + lane;
         uint32_t npx = 0;
-        if (g < total) {
+        // the emit phase skips tiles whose count pass found no covered sample
+        if (g < total && !(PHASE == P_WRITE && counts[g].x == 0u)) {
             const int64_t item = plan.tile_item[g];
             const uint32_t local = g - (item > 0 ? tile_end[item - 1] : 0u);
             int64_t tri;
@@ -1105,12 +1107,12 @@ static int plan_tiles(RasterArgs& A, vct_workspace_s* ws, size_t& off, TilePlan*
 constexpr int kWorkspaceGrew = 1;
 
 // Coverage count + exclusive scan of (covered samples, records) per tile for
-// the injection and the SVO pass.  On VCT_OK *offs (in the workspace, `off`
-// advanced past it) holds each tile's first descriptor / record and *nfrag /
-// *nrec the totals (host).
+// the injection and the SVO pass.  On VCT_OK *counts_out and *offs (in the
+// workspace, `off` advanced past them) hold each tile's counts and its first
+// descriptor / record, and *nfrag / *nrec the totals (host).
 template <int KIND>
-static int count_tiles(RasterArgs& A, vct_workspace_s* ws, size_t& off, const TilePlan& plan, uint2** offs,
-                       uint32_t* nfrag, uint32_t* nrec, cudaStream_t st) {
+static int count_tiles(RasterArgs& A, vct_workspace_s* ws, size_t& off, const TilePlan& plan, uint2** counts_out,
+                       uint2** offs, uint32_t* nfrag, uint32_t* nrec, cudaStream_t st) {
     const uint32_t total = plan.total;
     size_t scan_bytes = 0;
     VCT_CUDA_TRY(cub::DeviceScan::ExclusiveScan(nullptr, scan_bytes, (uint2*)nullptr, (uint2*)nullptr, SumU2{},
@@ -1122,6 +1124,7 @@ static int count_tiles(RasterArgs& A, vct_workspace_s* ws, size_t& off, const Ti
     }
     char* base = (char*)ws->ptr + off;
     uint2* counts = (uint2*)base;
+    *counts_out = counts;
     *offs = (uint2*)(base + a256(8 * (size_t)total));
     void* tmp = base + 2 * a256(8 * (size_t)total);
     off += 2 * a256(8 * (size_t)total) + a256(scan_bytes);
@@ -1167,8 +1170,8 @@ static int inject_prepare(RasterArgs& C, RasterArgs& I, vct_workspace_s* ws, cud
     if (rc != VCT_OK) return rc;
     S->nfrag = S->nrec = 0;
     if (S->plan.total == 0) return VCT_OK;
-    uint2* offs;
-    rc = count_tiles<KIND>(C, ws, off, S->plan, &offs, &S->nfrag, &S->nrec, st);
+    uint2 *counts, *offs;
+    rc = count_tiles<KIND>(C, ws, off, S->plan, &counts, &offs, &S->nfrag, &S->nrec, st);
     if (rc != VCT_OK) return rc;  // including kWorkspaceGrew
     if (S->nfrag == 0) return VCT_OK;
     const uint32_t nfrag = S->nfrag, nrec = S->nrec;
@@ -1197,7 +1200,7 @@ static int inject_prepare(RasterArgs& C, RasterArgs& I, vct_workspace_s* ws, cud
     S->heads = (uint32_t*)(p + 4 * r4);
     S->nheads = (uint32_t*)(p + 5 * r4);
     S->stmp = p + 5 * r4 + 256;
-    launch_cover<K_INJECT, P_WRITE>(I, S->plan, nullptr, offs, S->fr, nullptr, st);
+    launch_cover<K_INJECT, P_WRITE>(I, S->plan, counts, offs, S->fr, nullptr, st);
     VCT_LAUNCH_CHECK();
     return VCT_OK;
 }
@@ -1544,9 +1547,9 @@ extern "C" int vct_svo_fragments(const vct_scene* scene, int32_t octree_level, c
     if (rc != VCT_OK) return rc;
     if (plan.total == 0) return VCT_OK;
     // count pass (SparseVoxelizer::preVoxelize), host readback of the count
-    uint2* offs;
+    uint2 *counts, *offs;
     uint32_t nfrag, nslot;
-    rc = count_tiles<K_SVO>(A, ws, off, plan, &offs, &nfrag, &nslot, st);
+    rc = count_tiles<K_SVO>(A, ws, off, plan, &counts, &offs, &nfrag, &nslot, st);
     if (rc == kWorkspaceGrew)
         return vct_svo_fragments(scene, octree_level, bb_min, bb_max, shadow, light, light_shadow, frags, capacity,
                                  count, ws, stream);
@@ -1564,7 +1567,7 @@ extern "C" int vct_svo_fragments(const vct_scene* scene, int32_t octree_level, c
     FragDesc* fr = (FragDesc*)((char*)ws->ptr + off);
     // write pass (SparseVoxelizer::cmdVoxelize); discarded slots stay zero
     VCT_CUDA_TRY(cudaMemsetAsync(frags, 0, sizeof(uint32_t) * 2 * (size_t)*count, st));
-    launch_cover<K_SVO, P_WRITE>(A, plan, nullptr, offs, fr, nullptr, st);
+    launch_cover<K_SVO, P_WRITE>(A, plan, counts, offs, fr, nullptr, st);
     VCT_LAUNCH_CHECK();
     k_svo_shade<<<grid_of(nfrag, 256), 256, 0, st>>>(A, fr, nfrag);
     VCT_LAUNCH_CHECK();
