@@ -850,6 +850,7 @@ __global__ void __launch_bounds__(128, 6) k_cover(const __grid_constant__ Raster
                 if ((PHASE == P_DIRECT || KIND == K_OPA_COUNT) && mask) {
                     const TileSlot& T = S[j];
                     const int lvl = (int)(T.meta & 7u);
+                    int3 last_ic = make_int3(-1, -1, -1);  // opacity: the previous sample's voxel (stores are idempotent)
                     for (uint32_t m = mask; m; m &= m - 1u) {
                         const int s = __ffs(m) - 1;
                         float b[3], z;
@@ -866,6 +867,8 @@ __global__ void __launch_bounds__(128, 6) k_cover(const __grid_constant__ Raster
                                 continue;
                             const AtlasDims AD(A.R);
                             const int3 ic = clip_image_coords(d, wp);
+                            if (ic.x == last_ic.x && ic.y == last_ic.y && ic.z == last_ic.z) continue;
+                            last_ic = ic;
                             for (int f = 0; f < 6; ++f) A.atlas[AD.index(ic.x + (A.R + 2) * f, ic.y, ic.z)] = 0xFFFFFFFFu;
                         } else if (KIND == K_INJECT) {
                             const vct_gltf_shade_material mat = material_of(A.s, T.meta >> 3);
