@@ -374,6 +374,12 @@ int vct_voxelization_desc_for(const vct_clipmap_region regions_host[6], int32_t 
  * +-16 orthographic projection of a directional light. */
 int vct_directional_light_shadow(const float origin_host[3], const float direction_host[3], float z_near,
                                  float z_far, vct_directional_light_shadow_desc* out_host);
+/* Camera::updateCamera (VFS/Camera.cpp:110-117): view = lookAtLH(position,
+ * position + direction, up), proj = perspectiveLH_ZO(radians(fovy), aspect,
+ * 0.01, 5000), and the CamMatrix block {proj * view, inverse(view) *
+ * inverse(proj), position} (glm's cofactor inverse, FP32). */
+int vct_camera_matrix(const float position_host[3], const float direction_host[3], const float up_host[3],
+                      float fovy_degrees, float aspect, vct_cam_matrix* out_host);
 
 /* vkCmdClearColorImage of a whole atlas to 0 (VoxelizationPass.cpp:104-125). */
 int vct_clear_atlas(uint32_t* atlas, int32_t clipmap_resolution, void* stream);
@@ -403,6 +409,18 @@ int vct_inject_radiance(const vct_scene* scene, const vct_clipmap_region regions
                         const vct_shadow_map* shadow, const vct_directional_light_desc* light,
                         const vct_directional_light_shadow_desc* light_shadow, uint32_t* radiance_atlas,
                         uint32_t level_mask, int32_t mode, vct_workspace ws, void* stream);
+
+/* GBufferPass::onUpdate + gBufferPass.{vert,frag} (VFS/RenderPass/GBufferPass.cpp:80-160,
+ * 329; depth test LESS against a 1.0 clear, no culling) feeding the
+ * cone-tracing pass: rasterise the scene with the camera's view-projection
+ * at one centre sample per pixel (triangles clipped to the near plane),
+ * resolve each pixel's closest fragment (ties: the earlier triangle) into a
+ * vct_surface_sample with the attachments' formats applied, and the world
+ * position rebuilt from the depth as worldPosFromDepth does.  Writes
+ * width * height records (row-major, row 0 = NDC y -1); pixels no triangle
+ * covers get depth 1.  `out` is a device pointer, 16-byte aligned. */
+int vct_gbuffer(const vct_scene* scene, const vct_cam_matrix* cam_host, int32_t width, int32_t height,
+                vct_surface_sample* out, vct_workspace ws, void* stream);
 
 /* SparseVoxelizer::preVoxelize + cmdVoxelize (VFS/RenderPass/Octree/SparseVoxelizer.cpp:248-326)
  * with voxelizer.{vert,geom,frag}: count pass, host readback of the count

@@ -19,7 +19,7 @@ HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 LIB = BUILD / "libvct_oracle.so"
 SOURCES = ["vct_oracle.cpp"]
-HEADERS = ["oracle_common.hpp", "clipmap_oracle.hpp", "raster_oracle.hpp", "svo_oracle.hpp"]
+HEADERS = ["oracle_common.hpp", "clipmap_oracle.hpp", "raster_oracle.hpp", "svo_oracle.hpp", "gbuffer_oracle.hpp"]
 
 P = C.c_void_p
 
@@ -70,6 +70,9 @@ def lib():
         L.vcto_light_shadow_desc.argtypes = [P, P, C.c_float, C.c_float, P]
         L.vcto_voxelize_opacity.argtypes = [P, C.c_int, P, P, C.c_int]
         L.vcto_shadow_depth.argtypes = [P, P, P, C.c_int, C.c_int]
+        L.vcto_camera_matrix.argtypes = [P, P, P, C.c_float, C.c_float, P]
+        L.vcto_inverse4.argtypes = [P, P]
+        L.vcto_gbuffer.argtypes = [P, P, C.c_int, C.c_int, P]
         L.vcto_inject_radiance.argtypes = [P, C.c_int, P, P, C.c_int, C.c_int, P, P, P, C.c_int]
         L.vcto_svo_fragments.restype = C.c_int64
         L.vcto_svo_fragments.argtypes = [P, C.c_int, P, P, P, C.c_int, C.c_int, P, P, P, C.c_int64]
@@ -248,6 +251,29 @@ def shadow_depth(scene, shadow_desc_bytes: bytes, W: int, H: int) -> np.ndarray:
     sv = scene_view(scene)
     lib().vcto_shadow_depth(C.byref(sv), _p(sd), _p(depth), W, H)
     return depth
+
+
+def camera_matrix(position, direction, up=(0.0, 1.0, 0.0), fovy_degrees=60.0, aspect=16.0 / 9.0) -> np.ndarray:
+    """Camera::updateCamera's CamMatrix block as 36 float32 (view_proj, view_proj_inv, eye, padding)."""
+    out = np.zeros(36, np.float32)
+    v = [np.asarray(x, np.float32) for x in (position, direction, up)]
+    lib().vcto_camera_matrix(_p(v[0]), _p(v[1]), _p(v[2]), fovy_degrees, aspect, _p(out))
+    return out
+
+
+def inverse4(m: np.ndarray) -> np.ndarray:
+    """glm::inverse of a column-major 4x4 (16 float32)."""
+    out = np.zeros(16, np.float32)
+    lib().vcto_inverse4(_p(np.ascontiguousarray(m, np.float32)), _p(out))
+    return out
+
+
+def gbuffer(scene, cam: np.ndarray, W: int, H: int) -> np.ndarray:
+    """GBufferPass at one centre sample per pixel: (H * W, 20) float32 vct_surface_sample rows."""
+    out = np.zeros((W * H, 20), np.float32)
+    sv = scene_view(scene)
+    lib().vcto_gbuffer(C.byref(sv), _p(np.ascontiguousarray(cam, np.float32)), W, H, _p(out))
+    return out
 
 
 def inject_radiance(scene, R: int, regions: np.ndarray, shadow: np.ndarray | None, shadow_desc_bytes: bytes,

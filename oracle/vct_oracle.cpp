@@ -1,11 +1,12 @@
 // vct_oracle.cpp -- TEST INFRASTRUCTURE ONLY.
 //
 // C entry points over the CPU restatement (clipmap_oracle.hpp, svo_oracle.hpp,
-// raster_oracle.hpp) for the Python test harness and bench.py's CPU-baseline
+// raster_oracle.hpp, gbuffer_oracle.hpp) for the Python test harness and bench.py's CPU-baseline
 // leg (ctypes).  The CUDA product library never links or calls this file.
 #include <omp.h>
 
 #include "clipmap_oracle.hpp"
+#include "gbuffer_oracle.hpp"
 #include "raster_oracle.hpp"
 #include "svo_oracle.hpp"
 
@@ -145,6 +146,19 @@ void vcto_voxelize_opacity(const SceneView* s, int R, const Region regions[6], u
 }
 void vcto_shadow_depth(const SceneView* s, const ShadowDesc* sd, float* depth, int W, int H) {
     shadow_depth(*s, *sd, depth, W, H);
+}
+void vcto_camera_matrix(const float pos[3], const float dir[3], const float up[3], float fovy_deg, float aspect,
+                        CamMatrix* out) {
+    *out = camera_matrix(pos, dir, up, fovy_deg, aspect);
+}
+void vcto_inverse4(const float m[16], float out[16]) {
+    Mat4 a;
+    std::memcpy(a.m, m, 64);
+    const Mat4 r = inverse4(a);
+    std::memcpy(out, r.m, 64);
+}
+void vcto_gbuffer(const SceneView* s, const CamMatrix* cam, int W, int H, SurfaceSample* out) {
+    gbuffer(*s, *cam, W, H, out);
 }
 void vcto_inject_radiance(const SceneView* s, int R, const Region regions[6], const float* shadow, int sw, int sh,
                           const ShadowDesc* sd, const LightDesc* light, uint32_t* radiance, int level_mask) {

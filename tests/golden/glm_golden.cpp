@@ -4,8 +4,9 @@
 // math of the path: VoxelizationPass::createVoxelClipmap/calculateChangeDelta
 // (VFS/RenderPass/Clipmap/VoxelizationPass.cpp:335-357, 438-448) fed by
 // Application::updateClipRegionBoundingBox (VFS/Application.cpp:116-128),
-// Voxelizer::setViewProjection (VFS/RenderPass/Clipmap/Voxelizer.cpp:394-423)
-// and DirectionalLight::setTransform (VFS/DirectionalLight.cpp:21-47).  The
+// Voxelizer::setViewProjection (VFS/RenderPass/Clipmap/Voxelizer.cpp:394-423),
+// DirectionalLight::setTransform (VFS/DirectionalLight.cpp:21-47) and
+// Camera::updateCamera (VFS/Camera.cpp:110-117).  The
 // calls below are written here from those functions' arguments; nothing of
 // the reference is compiled.  Prints JSON with every float as its bit pattern.
 #define GLM_FORCE_SIZE_T_LENGTH
@@ -99,6 +100,34 @@ int main() {
         print_mat(view);
         std::printf(",\"proj\":");
         print_mat(proj);
+        std::printf("}");
+    }
+    // Camera::updateCamera (VFS/Camera.cpp:110-117)
+    std::printf("],\"cameras\":[");
+    const float cams2[][11] = {{0.f, 2.f, -5.f, 0.f, 0.f, 1.f, 0.f, 1.f, 0.f, 60.f, 1.7777778f},
+                               {1.3f, 2.7f, -5.1f, 0.3f, -0.2f, 0.93f, 0.f, 1.f, 0.f, 60.f, 1.5f},
+                               {-4.f, 1.5f, 3.f, 0.8f, 0.1f, -0.59f, 0.f, 1.f, 0.f, 45.f, 1.0f},
+                               {0.37f, 6.1f, 0.2f, 0.05f, -0.99f, 0.1f, 0.f, 1.f, 0.f, 75.f, 1.25f}};
+    first = true;
+    for (auto& c : cams2) {
+        const glm::vec3 pos(c[0], c[1], c[2]), dir(c[3], c[4], c[5]), up(c[6], c[7], c[8]);
+        const glm::mat4 view = glm::lookAt(pos, pos + dir, up);
+        const glm::mat4 proj = glm::perspective(glm::radians(c[9]), c[10], 0.01f, 5000.0f);
+        std::printf("%s{\"in\":[", first ? "" : ",");
+        first = false;
+        for (int i = 0; i < 11; ++i) std::printf("%u%s", bits(c[i]), i == 10 ? "" : ",");
+        std::printf("],\"view_proj\":");
+        print_mat(proj * view);
+        std::printf(",\"view_proj_inv\":");
+        print_mat(glm::inverse(view) * glm::inverse(proj));
+        std::printf(",\"view\":");
+        print_mat(view);
+        std::printf(",\"proj\":");
+        print_mat(proj);
+        std::printf(",\"view_inv\":");
+        print_mat(glm::inverse(view));
+        std::printf(",\"proj_inv\":");
+        print_mat(glm::inverse(proj));
         std::printf("}");
     }
     std::printf("]}\n");

@@ -12,7 +12,8 @@ tree, which does not travel with the tests):
    VFS/pch.h:33-35) and records, for a set of cameras / resolutions / lights:
      * the clip regions of VoxelizationPass::createVoxelClipmap,
      * the three view-projection matrices of Voxelizer::setViewProjection,
-     * the view / projection of DirectionalLight::setTransform.
+     * the view / projection of DirectionalLight::setTransform,
+     * the CamMatrix block of Camera::updateCamera (glm::perspective, glm::inverse).
 2. Parses the fixed cone tables and trace constants out of
    VFS/Shaders/voxelConeTracing.frag.
 Writes glm_host_math.json and cone_tables.json next to this script.

@@ -68,3 +68,28 @@ def test_cone_tables_match_shader():
         assert lit.replace(" ", "") in src.replace(" ", ""), lit
         assert lit.replace(" ", "") in cu.replace(" ", ""), lit
     assert t["MAX_TRACE_DISTANCE"] == 30.0 and t["MIN_TRACE_STEP_FACTOR"] == 0.2
+
+
+def _cam_inputs(rec):
+    v = _f(rec["in"])
+    return v[0:3], v[3:6], v[6:9], float(v[9]), float(v[10])
+
+
+def test_camera_matrix_bit_exact(oracle, host_math):
+    """Camera::updateCamera: perspective, lookAt and glm::inverse against glm itself."""
+    assert len(host_math["cameras"]) == 4
+    for rec in host_math["cameras"]:
+        pos, d, up, fovy, aspect = _cam_inputs(rec)
+        cam = oracle.camera_matrix(pos, d, up, fovy, aspect)
+        assert np.array_equal(cam[0:16].view(np.uint32), np.array(rec["view_proj"], np.uint32))
+        assert np.array_equal(cam[16:32].view(np.uint32), np.array(rec["view_proj_inv"], np.uint32))
+        assert np.array_equal(cam[32:35], pos)
+
+
+def test_inverse4_bit_exact(oracle, host_math):
+    """glm::inverse restated: the view and projection inverses, entry by entry."""
+    for rec in host_math["cameras"]:
+        for m, inv in (("view", "view_inv"), ("proj", "proj_inv")):
+            src = np.array(rec[m], np.uint32).view(np.float32)
+            got = oracle.inverse4(src)
+            assert np.array_equal(got.view(np.uint32), np.array(rec[inv], np.uint32)), m

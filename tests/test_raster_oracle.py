@@ -77,6 +77,19 @@ def test_library_host_matrices_match_glm_golden(vct_lib):
         assert np.array_equal(np.frombuffer(bytes(sd.proj), np.uint32), np.array(rec["proj"], np.uint32))
 
 
+def test_library_camera_matrix_matches_glm_golden(vct_lib):
+    g = json.loads((GOLDEN / "glm_host_math.json").read_text())
+    from vk_voxel_cone_tracing_gb300.passes import camera_matrix
+    for rec in g["cameras"]:
+        v = np.array(rec["in"], np.uint32).view(np.float32)
+        cam = camera_matrix(v[0:3].tolist(), v[3:6].tolist(), v[6:9].tolist(), float(v[9]), float(v[10]))
+        assert np.array_equal(np.frombuffer(bytes(cam.view_proj), np.uint32), np.array(rec["view_proj"], np.uint32))
+        assert np.array_equal(np.frombuffer(bytes(cam.view_proj_inv), np.uint32),
+                              np.array(rec["view_proj_inv"], np.uint32))
+    with pytest.raises(capi.VctError):
+        camera_matrix((0, 0, 0), (0, 0, 1), aspect=0.0)
+
+
 def test_library_voxelization_desc_matches_oracle(vct_lib, oracle):
     from vk_voxel_cone_tracing_gb300.clipmap import clip_regions
     for cam, R in (((0.0, 0.0, 0.0), 128), ((1.3, 2.7, -5.1), 256)):

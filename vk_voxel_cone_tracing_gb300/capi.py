@@ -162,6 +162,8 @@ _SIGS: dict[str, tuple] = {
     "vct_voxelization_view_proj": (C.c_int, [P, P]),
     "vct_voxelization_desc_for": (C.c_int, [P, C.c_int32, C.c_int32, P]),
     "vct_directional_light_shadow": (C.c_int, [P, P, C.c_float, C.c_float, P]),
+    "vct_camera_matrix": (C.c_int, [P, P, P, C.c_float, C.c_float, P]),
+    "vct_gbuffer": (C.c_int, [P, P, C.c_int32, C.c_int32, P, P, P]),
     "vct_clear_atlas": (C.c_int, [P, C.c_int32, P]),
     "vct_voxelize_opacity": (C.c_int, [P, P, C.c_int32, P, C.c_uint32, P, P]),
     "vct_shadow_depth": (C.c_int, [P, P, P, C.c_int32, C.c_int32, P, P]),

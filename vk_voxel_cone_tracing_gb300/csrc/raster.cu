@@ -101,6 +101,55 @@ __host__ inline M4 ortho_lh_zo(float l, float r, float b, float t, float n, floa
     return R;
 }
 
+// glm::perspectiveLH_ZO (column-major): fovy in radians.
+__host__ inline M4 perspective_lh_zo(float fovy, float aspect, float n, float f) {
+    const float th = tanf(fovy / 2.0f);
+    M4 R = {};
+    R.m[0] = 1.0f / (aspect * th);
+    R.m[5] = 1.0f / th;
+    R.m[10] = f / (f - n);
+    R.m[11] = 1.0f;
+    R.m[14] = -(f * n) / (f - n);
+    return R;
+}
+
+// General 4x4 inverse by cofactors, in glm::inverse's evaluation order
+// (glm 0.9.9 detail/func_matrix.inl, compute_inverse<4, 4>): the 2x2 minors
+// of columns 2-3 (and 1-3, 1-2) taken over row pairs, each adjugate entry as
+// (a * m0 - b * m1) + c * m2 with its checkerboard sign, then a scale by
+// 1 / det where det = (c0 + c1) + (c2 + c3) over column 0's products with the
+// adjugate's row 0.  M[c * 4 + r] is column c, row r.
+__host__ inline M4 inverse4(const float* M) {
+    auto e = [&](int c, int r) { return M[c * 4 + r]; };
+    // F[f][j]: the 2x2 minor of rows fr[f] and columns cp[j] (glm's Fac0..Fac5)
+    const int cp[4][2] = {{2, 3}, {2, 3}, {1, 3}, {1, 2}};
+    const int fr[6][2] = {{2, 3}, {1, 3}, {1, 2}, {0, 3}, {0, 2}, {0, 1}};
+    float F[6][4];
+    for (int f = 0; f < 6; ++f)
+        for (int j = 0; j < 4; ++j) {
+            const int a = cp[j][0], b = cp[j][1], r0 = fr[f][0], r1 = fr[f][1];
+            F[f][j] = e(a, r0) * e(b, r1) - e(b, r0) * e(a, r1);
+        }
+    float V[4][4];  // V[r][j] = element (column 1 for j == 0 else column 0, row r)
+    for (int r = 0; r < 4; ++r)
+        for (int j = 0; j < 4; ++j) V[r][j] = e(j == 0 ? 1 : 0, r);
+    // adjugate column k = (V_p * F_q - V_s * F_t) + V_u * F_v, {p, q, s, t, u, v} = tab[k]
+    const int tab[4][6] = {{1, 0, 2, 1, 3, 2}, {0, 0, 2, 3, 3, 4}, {0, 1, 1, 3, 3, 5}, {0, 2, 1, 4, 2, 5}};
+    M4 I;
+    for (int k = 0; k < 4; ++k)
+        for (int j = 0; j < 4; ++j) {
+            const float sgn = ((k + j) & 1) ? -1.0f : 1.0f;
+            const float v = (V[tab[k][0]][j] * F[tab[k][1]][j] - V[tab[k][2]][j] * F[tab[k][3]][j]) +
+                            V[tab[k][4]][j] * F[tab[k][5]][j];
+            I.m[k * 4 + j] = v * sgn;
+        }
+    const float d0 = e(0, 0) * I.m[0], d1 = e(0, 1) * I.m[4], d2 = e(0, 2) * I.m[8], d3 = e(0, 3) * I.m[12];
+    const float det = (d0 + d1) + (d2 + d3);
+    const float inv = 1.0f / det;
+    for (int i = 0; i < 16; ++i) I.m[i] = I.m[i] * inv;
+    return I;
+}
+
 // Voxelizer::setViewProjection over the extended region (min - 1, extent + 2).
 __host__ void voxel_view_proj(const vct_clipmap_region& r, float out[48]) {
     const float vs = r.voxel_size;
@@ -268,7 +317,8 @@ __device__ inline float3 interp3(const float b[3], const float3 v[3]) {
 // ------------------------------------------------------------ pass params
 // K_OPA_COUNT: the opacity voxelisation and the injection's coverage count in
 // one pass (the frame's items are the same for both).
-enum Kind { K_OPACITY = 0, K_INJECT = 1, K_SHADOW = 2, K_SVO = 3, K_OPA_COUNT = 4 };
+// K_GBUFFER: the camera's visibility pass (closest fragment per pixel centre).
+enum Kind { K_OPACITY = 0, K_INJECT = 1, K_SHADOW = 2, K_SVO = 3, K_OPA_COUNT = 4, K_GBUFFER = 5 };
 enum Phase { P_DIRECT = 0, P_COUNT = 1, P_WRITE = 2 };
 
 struct RasterArgs {
@@ -294,6 +344,7 @@ struct RasterArgs {
     int64_t items;
     uint32_t invalid_key;  // injection record key that sorts past every texel
     uint32_t count_levels; // injection: the clip levels (bit l) whose samples are counted and emitted
+    unsigned long long* vis;  // G-buffer: per pixel (depth bits << 32 | triangle * 8 + sub-triangle), min wins
 };
 
 // Items are numbered triangle-major (item = tri * nlevels + level index) and
@@ -305,12 +356,109 @@ __device__ inline void item_of(const RasterArgs& A, int64_t item, int64_t& tri, 
     lvl = A.levels[it - t * nl];
 }
 
+// ---------------------------------------------------------- camera clipping
+// The G-buffer pass draws with a perspective camera, so a triangle is clipped
+// in homogeneous space before the divide: against the near plane z >= 0 (the
+// zero-to-one depth range; it also keeps w >= zNear > 0) and a guard band
+// |x|, |y| <= 16 w, which bounds the snapped screen coordinates so the 64-bit
+// edge functions cannot overflow (pixels outside the viewport are never
+// tested, so the band changes no coverage).  Sutherland-Hodgman over the five
+// planes leaves at most 8 vertices; the polygon is fanned from its first
+// vertex into at most 6 sub-triangles.  Every vertex carries its barycentric
+// coordinates in the original triangle, so attributes interpolate
+// perspective-correctly across sub-triangles.  FP32, no contraction; the
+// oracle restates the same steps.
+struct ClipVert {
+    float x, y, z, w;  // clip coordinates
+    float l[3];        // barycentric coordinates in the original triangle
+};
+
+constexpr float kGuardBand = 16.0f;
+
+__host__ __device__ inline float clip_dist(const ClipVert& v, int plane) {
+    switch (plane) {
+        case 0: return v.z;
+        case 1: return v.x + kGuardBand * v.w;
+        case 2: return kGuardBand * v.w - v.x;
+        case 3: return v.y + kGuardBand * v.w;
+        default: return kGuardBand * v.w - v.y;
+    }
+}
+
+// Clips triangle c[3] (clip coordinates) into poly[]; returns the vertex count (0 or 3..8).
+__host__ __device__ inline int clip_triangle(const float4 c[3], ClipVert poly[8]) {
+    ClipVert a[8], b[8];
+    int n = 3;
+    for (int k = 0; k < 3; ++k) {
+        a[k].x = c[k].x;
+        a[k].y = c[k].y;
+        a[k].z = c[k].z;
+        a[k].w = c[k].w;
+        a[k].l[0] = k == 0 ? 1.0f : 0.0f;
+        a[k].l[1] = k == 1 ? 1.0f : 0.0f;
+        a[k].l[2] = k == 2 ? 1.0f : 0.0f;
+    }
+    ClipVert* src = a;
+    ClipVert* dst = b;
+    for (int plane = 0; plane < 5; ++plane) {
+        bool all_in = true;
+        for (int k = 0; k < n; ++k) all_in = all_in && clip_dist(src[k], plane) >= 0.0f;
+        if (all_in) continue;
+        int m = 0;
+        for (int k = 0; k < n; ++k) {
+            const ClipVert& p = src[k];
+            const ClipVert& q = src[(k + 1) % n];
+            const float dp = clip_dist(p, plane), dq = clip_dist(q, plane);
+            if (dp >= 0.0f) dst[m++] = p;
+            if ((dp >= 0.0f) != (dq >= 0.0f)) {
+                const float t = dp / (dp - dq);
+                ClipVert r;
+                r.x = p.x + t * (q.x - p.x);
+                r.y = p.y + t * (q.y - p.y);
+                r.z = p.z + t * (q.z - p.z);
+                r.w = p.w + t * (q.w - p.w);
+                for (int i = 0; i < 3; ++i) r.l[i] = p.l[i] + t * (q.l[i] - p.l[i]);
+                dst[m++] = r;
+            }
+        }
+        n = m;
+        ClipVert* t = src;
+        src = dst;
+        dst = t;
+        if (n < 3) return 0;
+    }
+    for (int k = 0; k < n; ++k) poly[k] = src[k];
+    return n;
+}
+
+// Sub-triangle `sub` of the clipped triangle (fan from vertex 0), or false.
+__host__ __device__ inline bool clip_sub_triangle(const float4 c[3], int sub, ClipVert v[3]) {
+    ClipVert poly[8];
+    const int n = clip_triangle(c, poly);
+    if (sub + 2 >= n) return false;
+    v[0] = poly[0];
+    v[1] = poly[sub + 1];
+    v[2] = poly[sub + 2];
+    return true;
+}
+
 // Clip-space vertices of item (tri, level) for the pass.
 __device__ inline bool item_setup(const RasterArgs& A, const WTri& w, int lvl, RSetup& rs, float3 pos[3]) {
     float4 c[3];
     if (A.kind == K_SHADOW) {
 #pragma unroll
         for (int k = 0; k < 3; ++k) c[k] = mat_vec4(A.pv, w.p[k].x, w.p[k].y, w.p[k].z, 1.0f);
+    } else if (A.kind == K_GBUFFER) {  // `lvl` is the sub-triangle of the clipped triangle
+        float4 h[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) h[k] = mat_vec4(A.pv, w.p[k].x, w.p[k].y, w.p[k].z, 1.0f);
+        ClipVert v[3];
+        if (!clip_sub_triangle(h, lvl, v)) {
+            rs.ok = false;
+            return false;
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) c[k] = make_float4(v[k].x / v[k].w, v[k].y / v[k].w, v[k].z / v[k].w, 1.0f);
     } else if (A.kind == K_SVO) {
         float3 q[3];
 #pragma unroll
@@ -547,6 +695,22 @@ __device__ inline bool item_discarded(const RasterArgs& A, const vct_gltf_shade_
     return mat.occlusion_texture > -1 && texture_1x1(A.s, mat.occlusion_texture).x < 0.1f;
 }
 
+// gBufferPass.frag:103-106: alpha-tested materials discard below the cutoff
+// (1x1 textures make the base colour's alpha per material).
+__device__ inline float4 gbuffer_base_color(const RasterArgs& A, const vct_gltf_shade_material& mat) {
+    float4 c = make_float4(mat.pbr_base_color_factor[0], mat.pbr_base_color_factor[1], mat.pbr_base_color_factor[2],
+                           mat.pbr_base_color_factor[3]);
+    if (mat.pbr_base_color_texture > -1) {
+        const float4 t = texture_1x1(A.s, mat.pbr_base_color_texture);
+        c = make_float4(c.x * t.x, c.y * t.y, c.z * t.z, c.w * t.w);
+    }
+    return c;
+}
+
+__device__ inline bool gbuffer_discarded(const RasterArgs& A, const vct_gltf_shade_material& mat) {
+    return mat.alpha_mode > 0 && gbuffer_base_color(A, mat).w < mat.alpha_cutoff;
+}
+
 __device__ inline uint32_t inject_per_fragment(const vct_gltf_shade_material& mat) {
     const bool emissive = mat.emissive_factor[0] > 0.0f || mat.emissive_factor[1] > 0.0f || mat.emissive_factor[2] > 0.0f;
     return emissive ? 6u : 3u;
@@ -597,6 +761,7 @@ struct TileSlot {
     uint32_t px_end;           // inclusive prefix of the warp's tile pixel counts
     uint32_t done;             // covered samples of this tile met in earlier rounds
     uint32_t base_f, base_r, per, meta;
+    uint32_t item;             // the tile's (triangle, level or sub-triangle) item
     float3 p[3], n[3];         // interpolation sources (position, normal)
 };
 
@@ -718,7 +883,7 @@ template <int KIND, int PHASE>
 __global__ void __launch_bounds__(128, 6) k_cover(const __grid_constant__ RasterArgs A, const TilePlan plan,
                                                uint2* __restrict__ counts, const uint2* __restrict__ offs,
                                                FragDesc* __restrict__ frags, int* __restrict__ err) {
-    constexpr int NS = KIND == K_SHADOW ? 1 : 8;
+    constexpr int NS = (KIND == K_SHADOW || KIND == K_GBUFFER) ? 1 : 8;
     constexpr bool RANKED = PHASE != P_DIRECT;
     constexpr unsigned FULL = 0xffffffffu;
     __shared__ TileSlot slots[4][32];
@@ -743,7 +908,8 @@ __global__ void __launch_bounds__(128, 6) k_cover(const __grid_constant__ Raster
             bool live = item_setup(A, w, lvl, rs, pos);
             const uint32_t mi = min(w.material, (uint32_t)max(A.s.material_count - 1, 0));
             uint32_t per = 1u;
-            if (KIND != K_SHADOW) {
+            if (KIND == K_GBUFFER) live = live && !gbuffer_discarded(A, material_of(A.s, mi));
+            if (KIND != K_SHADOW && KIND != K_GBUFFER) {
                 const vct_gltf_shade_material mat = material_of(A.s, mi);
                 live = live && !item_discarded(A, mat);
                 if (KIND == K_INJECT || KIND == K_OPA_COUNT) per = inject_per_fragment(mat);
@@ -761,7 +927,8 @@ __global__ void __launch_bounds__(128, 6) k_cover(const __grid_constant__ Raster
                 T.tw = tw;
                 T.tw_magic = tw > 1 ? (uint32_t)(0xffffffffu / (uint32_t)tw) + 1u : 0u;
                 T.meta = (uint32_t)lvl | (mi << 3);
-                if (KIND != K_SHADOW) {
+                T.item = (uint32_t)item;
+                if (KIND != K_SHADOW && KIND != K_GBUFFER) {
 #pragma unroll
                     for (int k = 0; k < 3; ++k) {
                         T.p[k] = KIND == K_SVO ? pos[k] : w.p[k];
@@ -788,7 +955,7 @@ __global__ void __launch_bounds__(128, 6) k_cover(const __grid_constant__ Raster
         __syncwarp();
         TileRegs t;
         int cj = -1;
-        if (KIND == K_SHADOW) {
+        if (KIND == K_SHADOW || KIND == K_GBUFFER) {
             // one centre sample per pixel: each lane takes four consecutive
             // pixels of the list per round, so the tile search and slot reload
             // are shared by four depth tests
@@ -814,7 +981,14 @@ __global__ void __launch_bounds__(128, 6) k_cover(const __grid_constant__ Raster
                         float b[3], z;
                         sample_bz(t, S[j], ox0 + 128, oy0 + 128, b, z);
                         const int px = S[j].tx + (ox0 >> 8), py = S[j].ty + (oy0 >> 8);
-                        atomicMin(reinterpret_cast<unsigned int*>(A.depth) + (int64_t)py * A.W + px, __float_as_uint(z));
+                        if (KIND == K_SHADOW) {
+                            atomicMin(reinterpret_cast<unsigned int*>(A.depth) + (int64_t)py * A.W + px,
+                                      __float_as_uint(z));
+                        } else if (z < 1.0f) {  // depth test LESS against the cleared 1.0
+                            // z >= 0 here; -0 is keyed as +0 so the bit order is the numeric order
+                            atomicMin(A.vis + (int64_t)py * A.W + px,
+                                      ((unsigned long long)(__float_as_uint(z) & 0x7fffffffu) << 32) | S[j].item);
+                        }
                     }
                 }
             }
@@ -982,6 +1156,103 @@ struct RunHead {
 struct SumU2 {
     __host__ __device__ uint2 operator()(uint2 a, uint2 b) const { return make_uint2(a.x + b.x, a.y + b.y); }
 };
+
+// gBufferPass.frag at each pixel's closest fragment, written as the
+// vct_surface_sample the trace reads: the sub-triangle the visibility pass
+// kept is set up again, its FP32 barycentrics at the pixel centre are made
+// perspective-correct (b_k / w_k, normalised) and mapped to the original
+// triangle's, the world normal and the material give the attachments' values,
+// which are stored through their formats (diffuse / specular RGBA8 UNORM,
+// normal / emission RGBA16F), and the world position is rebuilt from the depth
+// as worldPosFromDepth does (voxelConeTracing.frag:305-311).  Pixels with no
+// fragment keep depth 1 (the trace leaves them untouched).
+__device__ inline float u8_texel(float x) { return unorm8_decode(unorm8_store(x)); }
+__device__ inline float f16_texel(float x) { return __half2float(__float2half_rn(x)); }
+
+__global__ void __launch_bounds__(256) k_gbuffer_resolve(const __grid_constant__ RasterArgs A, const M4 vp_inv,
+                                                         vct_surface_sample* __restrict__ out) {
+    const int64_t npx = (int64_t)A.W * A.H;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npx; i += (int64_t)gridDim.x * blockDim.x) {
+        const unsigned long long key = A.vis[i];
+        const int px = (int)(i % A.W), py = (int)(i / A.W);
+        // the attachments' clear values: colour (0, 0, 0, 1), depth 1
+        float depth = 1.0f;
+        float4 r1 = make_float4(0.f, 0.f, 0.f, 1.0f), r2 = r1, r3 = r1, r4 = r1;
+        if (key != ~0ull) {
+            depth = __uint_as_float((uint32_t)(key >> 32));
+            const uint32_t item = (uint32_t)key;
+            const int64_t tri = item / 6u;
+            const int sub = (int)(item % 6u);
+            const WTri w = world_triangle(A.s, tri);
+            float4 h[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) h[k] = mat_vec4(A.pv, w.p[k].x, w.p[k].y, w.p[k].z, 1.0f);
+            ClipVert v[3];
+            clip_sub_triangle(h, sub, v);  // the visibility pass drew this sub-triangle
+            float4 c[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) c[k] = make_float4(v[k].x / v[k].w, v[k].y / v[k].w, v[k].z / v[k].w, 1.0f);
+            const RSetup rs = raster_setup(c, A.W, A.H);
+            const long long sx = (long long)px * 256 + 128, sy = (long long)py * 256 + 128;
+            float bo[3];
+#pragma unroll
+            for (int e = 0; e < 3; ++e) {
+                const int a = (e + 1) % 3, cc = (e + 2) % 3;
+                const long long ev = (rs.X[cc] - rs.X[a]) * (sy - rs.Y[a]) - (rs.Y[cc] - rs.Y[a]) * (sx - rs.X[a]);
+                bo[e] = (float)ev * rs.inv_area;
+            }
+            const float b[3] = {bo[0], rs.swapped ? bo[2] : bo[1], rs.swapped ? bo[1] : bo[2]};
+            // perspective-correct weights of the sub-triangle's vertices, then
+            // of the original triangle's
+            float q[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) q[k] = b[k] / v[k].w;
+            const float qs = (q[0] + q[1]) + q[2];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) q[k] = q[k] / qs;
+            float lam[3];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) lam[j] = (q[0] * v[0].l[j] + q[1] * v[1].l[j]) + q[2] * v[2].l[j];
+            const float3 nrm = normalize3h(interp3(lam, w.n));
+            // gBufferPass.frag:64-121 with 1x1 textures (no tangents: the
+            // normal texture is not applied)
+            const vct_gltf_shade_material mat = material_of(A.s, w.material);
+            float rough = mat.pbr_roughness_factor, metal = mat.pbr_metallic_factor;
+            if (mat.pbr_metallic_roughness_texture > -1) {
+                const float4 mr = texture_1x1(A.s, mat.pbr_metallic_roughness_texture);
+                rough = rough * mr.y;
+                metal = metal * mr.z;
+            } else {
+                rough = fminf(fmaxf(rough, 0.04f), 1.0f);
+                metal = fminf(fmaxf(metal, 0.0f), 1.0f);
+            }
+            const float4 base = gbuffer_base_color(A, mat);
+            const float dk = 1.0f - metal;
+            const float3 diff = make_float3(base.x * 0.96f * dk, base.y * 0.96f * dk, base.z * 0.96f * dk);
+            const float3 spec = make_float3(mix_rn(0.04f, base.x, metal), mix_rn(0.04f, base.y, metal),
+                                            mix_rn(0.04f, base.z, metal));
+            float3 em = make_float3(mat.emissive_factor[0], mat.emissive_factor[1], mat.emissive_factor[2]);
+            if (mat.emissive_texture > -1) {
+                const float4 t = texture_1x1(A.s, mat.emissive_texture);
+                em = make_float3(em.x * powf(t.x, 2.2f), em.y * powf(t.y, 2.2f), em.z * powf(t.z, 2.2f));
+            }
+            r1 = make_float4(f16_texel(nrm.x * 0.5f + 0.5f), f16_texel(nrm.y * 0.5f + 0.5f), f16_texel(nrm.z * 0.5f + 0.5f),
+                             1.0f);
+            r2 = make_float4(u8_texel(diff.x), u8_texel(diff.y), u8_texel(diff.z), u8_texel(rough));
+            r3 = make_float4(u8_texel(spec.x), u8_texel(spec.y), u8_texel(spec.z), u8_texel(metal));
+            r4 = make_float4(f16_texel(em.x), f16_texel(em.y), f16_texel(em.z), 1.0f);
+        }
+        // worldPosFromDepth (voxelConeTracing.frag:305-311) at the pixel centre
+        const float u = ((float)px + 0.5f) / (float)A.W, vv = ((float)py + 0.5f) / (float)A.H;
+        const float4 wp = mat_vec4(vp_inv.m, u * 2.0f - 1.0f, vv * 2.0f - 1.0f, depth, 1.0f);
+        float4* o = reinterpret_cast<float4*>(out + i);
+        o[0] = make_float4(wp.x / wp.w, wp.y / wp.w, wp.z / wp.w, depth);
+        o[1] = r1;
+        o[2] = r2;
+        o[3] = r3;
+        o[4] = r4;
+    }
+}
 
 // Sequential per-texel fold of the stably sorted injection records, one
 // thread per texel run.
@@ -1301,6 +1572,27 @@ extern "C" int vct_voxelization_desc_for(const vct_clipmap_region regions[6], in
     return VCT_OK;
 }
 
+extern "C" int vct_camera_matrix(const float position[3], const float direction[3], const float up[3],
+                                 float fovy_degrees, float aspect, vct_cam_matrix* out) {
+    VCT_CHECK_ARG(position && direction && up && out, "vct_camera_matrix: null argument");
+    VCT_CHECK_ARG(aspect > 0.0f && fovy_degrees > 0.0f && fovy_degrees < 180.0f, "vct_camera_matrix: bad fovy or aspect");
+    const float3 eye = make_float3(position[0], position[1], position[2]);
+    const M4 view = look_at_lh(eye, make_float3(eye.x + direction[0], eye.y + direction[1], eye.z + direction[2]),
+                               make_float3(up[0], up[1], up[2]));
+    const float fovy = fovy_degrees * (float)0.01745329251994329576923690768489;  // glm::radians
+    const M4 proj = perspective_lh_zo(fovy, aspect, 0.01f, 5000.0f);
+    const M4 vp = mat_mul4(proj.m, view.m);
+    const M4 vinv = inverse4(view.m), pinv = inverse4(proj.m);
+    const M4 vpi = mat_mul4(vinv.m, pinv.m);
+    memcpy(out->view_proj, vp.m, 64);
+    memcpy(out->view_proj_inv, vpi.m, 64);
+    out->eye_pos[0] = position[0];
+    out->eye_pos[1] = position[1];
+    out->eye_pos[2] = position[2];
+    out->padding = 0;
+    return VCT_OK;
+}
+
 extern "C" int vct_directional_light_shadow(const float origin[3], const float direction[3], float z_near, float z_far,
                                             vct_directional_light_shadow_desc* out) {
     VCT_CHECK_ARG(origin && direction && out, "vct_directional_light_shadow: null argument");
@@ -1430,6 +1722,50 @@ extern "C" int vct_inject_radiance(const vct_scene* scene, const vct_clipmap_reg
         return vct_inject_radiance(scene, regions, R, shadow, light, light_shadow, atlas, level_mask, mode, ws, stream);
     if (rc != VCT_OK) return rc;
     return inject_finish(A, S, nullptr, st);
+}
+
+extern "C" int vct_gbuffer(const vct_scene* scene, const vct_cam_matrix* cam, int32_t width, int32_t height,
+                           vct_surface_sample* out, vct_workspace_s* ws, void* stream) {
+    int rc = check_scene(scene);
+    if (rc != VCT_OK) return rc;
+    VCT_CHECK_ARG(cam && out && ws, "vct_gbuffer: null argument");
+    VCT_CHECK_ARG(width > 0 && height > 0 && width <= 16384 && height <= 16384, "vct_gbuffer: bad image size");
+    VCT_CHECK_ARG(((uintptr_t)out & 15) == 0, "vct_gbuffer: the output must be 16-byte aligned");
+    VCT_CHECK_ARG(scene->triangle_count < (1LL << 28), "vct_gbuffer: more than 2^28 triangles");
+    RasterArgs A;
+    memset(&A, 0, sizeof(A));
+    A.s = *scene;
+    A.kind = K_GBUFFER;
+    A.W = width;
+    A.H = height;
+    A.nlevels = 6;  // up to six sub-triangles per clipped triangle
+    for (int l = 0; l < 6; ++l) A.levels[l] = l;
+    memcpy(A.pv, cam->view_proj, 64);
+    A.items = scene->triangle_count * 6;
+    cudaStream_t st = as_stream(stream);
+    const int64_t npx = (int64_t)width * height;
+    size_t off = 0;
+    TilePlan plan;
+    plan.total = 0;
+    if (scene->triangle_count > 0) {
+        rc = plan_tiles(A, ws, off, &plan, st);
+        if (rc != VCT_OK) return rc;
+    }
+    const size_t need = off + a256(8 * (size_t)npx);
+    if (ws->bytes < need) {
+        rc = workspace_reserve(ws, need);
+        if (rc != VCT_OK) return rc;
+        return vct_gbuffer(scene, cam, width, height, out, ws, stream);  // the plan moved with the arena
+    }
+    A.vis = (unsigned long long*)((char*)ws->ptr + off);
+    M4 vp_inv;
+    memcpy(vp_inv.m, cam->view_proj_inv, 64);
+    VCT_CUDA_TRY(cudaMemsetAsync(A.vis, 0xff, 8 * (size_t)npx, st));
+    if (plan.total) launch_cover<K_GBUFFER, P_DIRECT>(A, plan, nullptr, nullptr, nullptr, nullptr, st);
+    VCT_LAUNCH_CHECK();
+    k_gbuffer_resolve<<<grid_of(npx, 256), 256, 0, st>>>(A, vp_inv, out);
+    VCT_LAUNCH_CHECK();
+    return VCT_OK;
 }
 
 namespace vct {

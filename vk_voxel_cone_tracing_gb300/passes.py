@@ -76,6 +76,27 @@ def light_shadow_desc(origin, direction, z_near=0.1, z_far=30.0) -> capi.Directi
     return out
 
 
+def camera_matrix(position, direction, up=(0.0, 1.0, 0.0), fovy_degrees=60.0, aspect=16.0 / 9.0) -> capi.CamMatrix:
+    """Camera::updateCamera's CamMatrix block (view-projection, its inverse, eye)."""
+    out = capi.CamMatrix()
+    vecs = [(C.c_float * 3)(*v) for v in (position, direction, up)]
+    capi.call("vct_camera_matrix", *[C.cast(v, C.c_void_p) for v in vecs], fovy_degrees, aspect, capi.ref(out))
+    return out
+
+
+def gbuffer(dscene: DeviceScene, cam: capi.CamMatrix, width: int, height: int, ws: Workspace,
+            out: torch.Tensor | None = None) -> torch.Tensor:
+    """GBufferPass: the camera's per-pixel surface records, an (height * width, 20) float32 tensor
+    (vct_surface_sample rows, row-major pixels; depth 1 where nothing was drawn)."""
+    n = width * height
+    if out is None:
+        out = torch.empty((n, 20), dtype=torch.float32, device=dscene.positions.device)
+    if out.shape != (n, 20) or out.dtype != torch.float32 or not out.is_contiguous():
+        raise ValueError("gbuffer: out must be a contiguous (width * height, 20) float32 tensor")
+    capi.call("vct_gbuffer", capi.ref(dscene.desc), capi.ref(cam), width, height, _ptr(out), ws.handle, _stream())
+    return out
+
+
 def clear_atlas(atlas: torch.Tensor, R: int) -> None:
     capi.call("vct_clear_atlas", _ptr(atlas), R, _stream())
 
