@@ -422,6 +422,40 @@ int vct_inject_radiance(const vct_scene* scene, const vct_clipmap_region regions
 int vct_gbuffer(const vct_scene* scene, const vct_cam_matrix* cam_host, int32_t width, int32_t height,
                 vct_surface_sample* out, vct_workspace ws, void* stream);
 
+/* ------------------------------------------- specular filter + present */
+
+/* SpecularFilterPass push constants (VFS/Shaders/specularFilter.frag:18-24)
+ * and their defaults (VFS/RenderPass/SpecularFilterPass.h:48-51): gamma 2.2,
+ * exposure 0.1, tone map off, filter 1 = the Gaussian blur.  filter_method 0
+ * (and any value but 1) selects the bilateral filter.  (The reference's GUI
+ * labels the two methods the other way round.) */
+typedef struct vct_specular_filter_desc {
+    float tonemap_gamma;
+    float tonemap_exposure;
+    int32_t tonemap_enable;
+    int32_t filter_method;
+} vct_specular_filter_desc;
+#define VCT_FILTER_BILATERAL 0
+#define VCT_FILTER_GAUSSIAN 1
+
+/* SpecularFilterPass::onUpdate + specularFilter.frag: out = diffuse +
+ * filter(specular) (rgb; alpha = diffuse's), Uncharted2 tone map when
+ * enabled.  Images are RGBA32F, row-major width x height float4, device
+ * pointers, 16-byte aligned (the cone trace's diffuse / specular outputs over
+ * the G-buffer's pixels, pre-filled with the pass's clear (0, 0, 0, 1) where
+ * the trace discards).  `out` must not alias `specular`.  The Gaussian blur's
+ * taps are all within 0.01 texel, so it runs as one 3 x 3 stencil; the
+ * stencil is returned by vct_specular_filter_stencil (9 floats, row-major
+ * dy = -1..1, dx = -1..1, already divided by the shader's 241). */
+int vct_specular_filter(const vct_specular_filter_desc* desc_host, const float* diffuse_rgba,
+                        const float* specular_rgba, int32_t width, int32_t height, float* out_rgba, void* stream);
+int vct_specular_filter_stencil(float out_host[9]);
+
+/* FinalPass into the B8G8R8A8_SRGB swapchain (VFS/SwapChain.cpp:400-412,
+ * finalPass.frag), headless: clamp to [0, 1], sRGB-encode rgb, store UNORM8
+ * (round half up); one uint32 per pixel with bytes B, G, R, A. */
+int vct_present_srgb8(const float* rgba, int32_t width, int32_t height, uint32_t* out_bgra8, void* stream);
+
 /* SparseVoxelizer::preVoxelize + cmdVoxelize (VFS/RenderPass/Octree/SparseVoxelizer.cpp:248-326)
  * with voxelizer.{vert,geom,frag}: count pass, host readback of the count
  * into *count_host, write pass of packed uint2 fragments in traversal order.
@@ -539,6 +573,7 @@ VCT_STATIC_ASSERT(sizeof(vct_cone_tracing_desc) == 52, "VoxelConeTracingDesc is 
 VCT_STATIC_ASSERT(sizeof(vct_cam_matrix) == 144, "CamMatrix is 144 B");
 VCT_STATIC_ASSERT(sizeof(vct_directional_light_desc) == 32, "DirectionalLightDesc is 32 B");
 VCT_STATIC_ASSERT(sizeof(vct_directional_light_shadow_desc) == 136, "DirectionalLightShadowDesc is 136 B");
+VCT_STATIC_ASSERT(sizeof(vct_specular_filter_desc) == 16, "SpecularFilterPassDesc is 16 B");
 VCT_STATIC_ASSERT(sizeof(vct_gltf_shade_material) == 80, "GltfShadeMaterial is 80 B");
 VCT_STATIC_ASSERT(sizeof(vct_surface_sample) == 80, "surface sample is 80 B");
 

@@ -19,7 +19,8 @@ HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 LIB = BUILD / "libvct_oracle.so"
 SOURCES = ["vct_oracle.cpp"]
-HEADERS = ["oracle_common.hpp", "clipmap_oracle.hpp", "raster_oracle.hpp", "svo_oracle.hpp", "gbuffer_oracle.hpp"]
+HEADERS = ["oracle_common.hpp", "clipmap_oracle.hpp", "raster_oracle.hpp", "svo_oracle.hpp", "gbuffer_oracle.hpp",
+           "composite_oracle.hpp"]
 
 P = C.c_void_p
 
@@ -73,6 +74,9 @@ def lib():
         L.vcto_camera_matrix.argtypes = [P, P, P, C.c_float, C.c_float, P]
         L.vcto_inverse4.argtypes = [P, P]
         L.vcto_gbuffer.argtypes = [P, P, C.c_int, C.c_int, P]
+        L.vcto_gaussian_stencil.argtypes = [P]
+        L.vcto_specular_filter.argtypes = [P, P, P, C.c_int, C.c_int, P]
+        L.vcto_present_srgb8.argtypes = [P, C.c_int64, P]
         L.vcto_inject_radiance.argtypes = [P, C.c_int, P, P, C.c_int, C.c_int, P, P, P, C.c_int]
         L.vcto_svo_fragments.restype = C.c_int64
         L.vcto_svo_fragments.argtypes = [P, C.c_int, P, P, P, C.c_int, C.c_int, P, P, P, C.c_int64]
@@ -273,6 +277,33 @@ def gbuffer(scene, cam: np.ndarray, W: int, H: int) -> np.ndarray:
     out = np.zeros((W * H, 20), np.float32)
     sv = scene_view(scene)
     lib().vcto_gbuffer(C.byref(sv), _p(np.ascontiguousarray(cam, np.float32)), W, H, _p(out))
+    return out
+
+
+def gaussian_stencil() -> np.ndarray:
+    """The Gaussian blur's 3 x 3 stencil (row-major dy, dx = -1..1), divided by 241."""
+    w = np.zeros(9, np.float32)
+    lib().vcto_gaussian_stencil(_p(w))
+    return w
+
+
+def specular_filter(diffuse: np.ndarray, specular: np.ndarray, gamma=2.2, exposure=0.1, tonemap=0,
+                    method=1) -> np.ndarray:
+    """specularFilter.frag over (H, W, 4) float32 images -> (H, W, 4) float32."""
+    H, W = diffuse.shape[:2]
+    fd = np.array([gamma, exposure], np.float32).tobytes() + np.array([tonemap, method], np.int32).tobytes()
+    fd = np.frombuffer(fd, np.uint8).copy()
+    out = np.zeros((H, W, 4), np.float32)
+    lib().vcto_specular_filter(_p(fd), _p(np.ascontiguousarray(diffuse, np.float32)),
+                               _p(np.ascontiguousarray(specular, np.float32)), W, H, _p(out))
+    return out
+
+
+def present_srgb8(rgba: np.ndarray) -> np.ndarray:
+    """FinalPass into B8G8R8A8_SRGB: uint32 per pixel (bytes B, G, R, A)."""
+    rgba = np.ascontiguousarray(rgba, np.float32)
+    out = np.zeros(rgba.shape[:-1], np.uint32)
+    lib().vcto_present_srgb8(_p(rgba), out.size, _p(out))
     return out
 
 

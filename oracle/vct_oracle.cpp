@@ -1,11 +1,12 @@
 // vct_oracle.cpp -- TEST INFRASTRUCTURE ONLY.
 //
 // C entry points over the CPU restatement (clipmap_oracle.hpp, svo_oracle.hpp,
-// raster_oracle.hpp, gbuffer_oracle.hpp) for the Python test harness and bench.py's CPU-baseline
+// raster_oracle.hpp, gbuffer_oracle.hpp, composite_oracle.hpp) for the Python test harness and bench.py's CPU-baseline
 // leg (ctypes).  The CUDA product library never links or calls this file.
 #include <omp.h>
 
 #include "clipmap_oracle.hpp"
+#include "composite_oracle.hpp"
 #include "gbuffer_oracle.hpp"
 #include "raster_oracle.hpp"
 #include "svo_oracle.hpp"
@@ -160,6 +161,12 @@ void vcto_inverse4(const float m[16], float out[16]) {
 void vcto_gbuffer(const SceneView* s, const CamMatrix* cam, int W, int H, SurfaceSample* out) {
     gbuffer(*s, *cam, W, H, out);
 }
+void vcto_gaussian_stencil(float w[9]) { gaussian_stencil(w); }
+void vcto_specular_filter(const FilterDesc* fd, const float* diffuse, const float* specular, int W, int H,
+                          float* out) {
+    specular_filter(*fd, diffuse, specular, W, H, out);
+}
+void vcto_present_srgb8(const float* rgba, int64_t n, uint32_t* out) { present_srgb8(rgba, n, out); }
 void vcto_inject_radiance(const SceneView* s, int R, const Region regions[6], const float* shadow, int sw, int sh,
                           const ShadowDesc* sd, const LightDesc* light, uint32_t* radiance, int level_mask) {
     inject_radiance(*s, R, regions, shadow, sw, sh, *sd, *light, radiance, level_mask);

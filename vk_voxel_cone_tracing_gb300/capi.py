@@ -30,6 +30,9 @@ DOWNSAMPLE_RADIANCE = 1
 
 MODE_GI_OUTPUT = 8
 
+FILTER_BILATERAL = 0
+FILTER_GAUSSIAN = 1
+
 INJECT_DETERMINISTIC = 0
 INJECT_ATOMIC = 1
 
@@ -108,6 +111,11 @@ class GltfShadeMaterial(C.Structure):
                 ("padding", C.c_int32)]
 
 
+class SpecularFilterDesc(C.Structure):
+    _fields_ = [("tonemap_gamma", C.c_float), ("tonemap_exposure", C.c_float), ("tonemap_enable", C.c_int32),
+                ("filter_method", C.c_int32)]
+
+
 class Scene(C.Structure):
     _fields_ = [("positions", C.c_void_p), ("normals", C.c_void_p), ("indices", C.c_void_p),
                 ("vertex_count", C.c_int64), ("triangle_count", C.c_int64), ("triangle_material", C.c_void_p),
@@ -130,7 +138,7 @@ class ShadowMap(C.Structure):
 STRUCT_SIZES = {
     ClipmapRegion: 28, VoxelizationDesc: 64, DownSampleDesc: 24, ImageCleaningDesc: 36, CopyAlphaDesc: 12,
     BorderWrappingDesc: 16, ConeTracingDesc: 52, CamMatrix: 144, DirectionalLightDesc: 32,
-    DirectionalLightShadowDesc: 136, GltfShadeMaterial: 80, Scene: 104,
+    DirectionalLightShadowDesc: 136, GltfShadeMaterial: 80, Scene: 104, SpecularFilterDesc: 16,
 }
 
 # Every entry point of include/vct_capi.h: name -> (restype, argtypes).
@@ -164,6 +172,9 @@ _SIGS: dict[str, tuple] = {
     "vct_directional_light_shadow": (C.c_int, [P, P, C.c_float, C.c_float, P]),
     "vct_camera_matrix": (C.c_int, [P, P, P, C.c_float, C.c_float, P]),
     "vct_gbuffer": (C.c_int, [P, P, C.c_int32, C.c_int32, P, P, P]),
+    "vct_specular_filter": (C.c_int, [P, P, P, C.c_int32, C.c_int32, P, P]),
+    "vct_specular_filter_stencil": (C.c_int, [P]),
+    "vct_present_srgb8": (C.c_int, [P, C.c_int32, C.c_int32, P, P]),
     "vct_clear_atlas": (C.c_int, [P, C.c_int32, P]),
     "vct_voxelize_opacity": (C.c_int, [P, P, C.c_int32, P, C.c_uint32, P, P]),
     "vct_shadow_depth": (C.c_int, [P, P, P, C.c_int32, C.c_int32, P, P]),
