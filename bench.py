@@ -43,6 +43,7 @@ R_DEFAULT = 256
 N_SAMPLES = 1920 * 1080
 SVO_LEVEL = 8
 CAMERA = (0.0, 5.0, 0.0)
+VIEW_DIR = (0.6, -0.2, 0.77)
 EYE = (0.0, 5.0, -12.0)
 LIGHT_DIR = (0.3, -1.0, 0.2)
 SHADOW_RES = 2048
@@ -313,6 +314,64 @@ def run_ours(args, world, rank, local):
     frame_ms = statistics.median(frame_per)
     svo_ms = statistics.median(svo_per)
 
+    # the camera's view: G-buffer at 1920x1080 for a camera in the hall, the trace over its pixels, the
+    # specular filter and the sRGB present -- the passes of a rendered frame after the clipmap frame
+    from vk_voxel_cone_tracing_gb300 import render
+    GW, GH = 1920, 1080
+    cam = passes.camera_matrix(CAMERA, VIEW_DIR, (0.0, 1.0, 0.0), 60.0, GW / GH)
+    gb = torch.empty((GW * GH, 20), dtype=torch.float32, device=dev)
+    cd = torch.empty((GW * GH, 4), dtype=torch.float32, device=dev)
+    cs = torch.empty((GW * GH, 4), dtype=torch.float32, device=dev)
+    img = torch.empty((GW * GH, 4), dtype=torch.float32, device=dev)
+    srgb = torch.empty((GH, GW), dtype=torch.int32, device=dev)
+    clear = torch.tensor([0.0, 0.0, 0.0, 1.0], device=dev)
+    fdesc = render.filter_desc()
+    bdesc = render.filter_desc(method=capi.FILTER_BILATERAL)
+    cam_scratch = clipmap.fast_scratch(GW * GH, dev) if tex is not None else None
+
+    def cam_trace():
+        cd.copy_(clear.expand_as(cd))
+        cs.copy_(clear.expand_as(cs))
+        if tex is None:
+            clipmap.cone_trace(desc, CAMERA, radiance, R, gb, light=light, shadow=shadow, shadow_desc=lsd,
+                               diffuse=cd, specular=cs)
+        else:
+            clipmap.cone_trace_fast(desc, CAMERA, tex, gb, light=light, shadow=shadow, shadow_desc=lsd,
+                                    diffuse=cd, specular=cs, scratch=cam_scratch)
+
+    stages = {
+        "gbuffer": lambda: passes.gbuffer(ds, cam, GW, GH, ws, out=gb),
+        "trace": cam_trace,
+        "filter_gaussian": lambda: render.specular_filter(cd, cs, GW, GH, fdesc, out=img),
+        "filter_bilateral": lambda: render.specular_filter(cd, cs, GW, GH, bdesc, out=img),
+        "present": lambda: render.present_srgb8(img, GW, GH, out=srgb),
+    }
+    cam_ms = {}
+    for name, fn in stages.items():
+        for _ in range(2):
+            fn()
+        cam_ms[name] = statistics.median(events_ms(stream, fn, max(3, args.steps))[0])
+    cam_steps = torch.zeros(1, dtype=torch.int64, device=dev)
+    if tex is None:
+        clipmap.cone_trace(desc, CAMERA, radiance, R, gb, light=light, shadow=shadow, shadow_desc=lsd,
+                           diffuse=cd, specular=cs, steps=cam_steps)
+    else:
+        clipmap.cone_trace_fast(desc, CAMERA, tex, gb, light=light, shadow=shadow, shadow_desc=lsd, diffuse=cd,
+                                specular=cs, steps=cam_steps, scratch=cam_scratch)
+    covered = int((gb[:, 3] < 1.0).sum().item())
+
+    def rendered_frame():
+        frame()
+        stages["gbuffer"]()
+        cam_trace()
+        stages["filter_gaussian"]()
+        stages["present"]()
+
+    for _ in range(2):
+        rendered_frame()
+    rendered_ms = statistics.median(events_ms(stream, rendered_frame, max(3, args.steps))[0])
+    filter_bytes = GW * GH * 48  # diffuse + specular texel read, output written (RGBA32F)
+
     # end to end: host G-buffer -> device, frame, trace, outputs -> host
     h_samples = samples.cpu().pin_memory()
     h_d = torch.empty(dout.shape, dtype=torch.float32).pin_memory()
@@ -381,7 +440,16 @@ def run_ours(args, world, rank, local):
                        else ("refreshed by a full copy every trace step" if tex is not None else "none (linear atlas)"),
                        "voxelize_inject_mip_ms": frame_ms, "svo_ms": svo_ms, "svo_level": SVO_LEVEL,
                        "svo_fragments": int(frags.shape[0]), "svo_nodes": int(nodes.value),
-                       "voxelize_svo_mip_ms": frame_ms + svo_ms},
+                       "voxelize_svo_mip_ms": frame_ms + svo_ms,
+                       "camera_view": {
+                           "resolution": [GW, GH], "camera": list(CAMERA), "direction": list(VIEW_DIR),
+                           "covered_pixels": covered, "cone_samples": int(cam_steps.item()),
+                           "stage_ms": cam_ms,
+                           "trace_cone_samples_per_s": int(cam_steps.item()) / (cam_ms["trace"] * 1e-3),
+                           "filter_gaussian_gbs": filter_bytes / (cam_ms["filter_gaussian"] * 1e-3) / 1e9,
+                           "rendered_frame_ms": rendered_ms,
+                           "rendered_frame": "clipmap frame + G-buffer + trace + Gaussian specular filter + "
+                                             "sRGB present, all on the device"}},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "note": f"{bpcs} B of algorithmic texel reads per cone sample over the {peak_kind} HBM "

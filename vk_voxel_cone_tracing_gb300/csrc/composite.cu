@@ -18,8 +18,9 @@
 //     a quirk kept as is).  The stencil is accumulated in double on the host
 //     (directions d from the shader's FP32 loop, cos / sin in double) and
 //     rounded to FP32 once;
-//   * the bilateral filter's weights follow normpdf3 / KERNEL in FP32; its
-//     exp is the device's expf (within 2 ulp of the exact value).
+//   * the bilateral filter's weights follow normpdf3 / KERNEL in FP32 up to a
+//     few ulp: the range term is one ex2 per tap and the constant factors
+//     are folded into a 15 x 15 table.
 // Everything else is FP32 without contraction (this unit is built with
 // -fmad=false) in the shader's evaluation order.
 #include <math.h>
@@ -34,13 +35,16 @@ constexpr int kBX = 32, kBY = 8, kHalo = 7;
 struct FilterParams {
     float gamma, exposure;
     int tonemap, method;
-    float stencil[9];  // Gaussian: [(dy + 1) * 3 + (dx + 1)], divided by 241
+    float stencil[9];        // Gaussian: [(dy + 1) * 3 + (dx + 1)], divided by 241
+    float bilateral_exp2;    // -0.5 / sigma^2 * log2(e)
+    float bw[225];           // bilateral weights without the range term, [i][j] = [x offset + 7][y offset + 7]
 };
 
-// filter.glsl KERNEL[15]: normpdf(x, 10) at x = -7..7, as the shader lists it.
-__constant__ float c_kernel15[15] = {0.031225216f, 0.033322271f, 0.035206333f, 0.036826804f, 0.038138565f,
-                                     0.039104044f, 0.039695028f, 0.039894000f, 0.039695028f, 0.039104044f,
-                                     0.038138565f, 0.036826804f, 0.035206333f, 0.033322271f, 0.031225216f};
+__device__ __forceinline__ float ex2_approx(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
 
 // tonemapping.glsl Uncharted2Tonemap for one channel.
 __device__ inline float uncharted2(float c) {
@@ -102,21 +106,23 @@ __global__ void __launch_bounds__(256) k_composite_bilateral(const float4* __res
     const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
     if (x >= W || y >= H) return;
     const float3 cc = tile[threadIdx.y + kHalo][threadIdx.x + kHalo];
-    const float sigma = 10.0f;
-    const float bZ = 1.0f / (0.39894f * expf(-0.5f * 0.0f * 0.0f / (sigma * sigma)) / sigma);  // 1 / normpdf(0, sigma)
+    // factor = normpdf3(s - c, 10) * bZ * KERNEL[7+j] * KERNEL[7+i] as exp2(dd * c_e) * c_w[i][j]:
+    // the constant part of normpdf3 times bZ times the two KERNEL entries is folded into c_w
+    // (host-computed in the shader's order), the exp becomes one ex2 of dd * (-0.5 / sigma^2) * log2(e).
+    // Within a few ulp of the shader's factor; the sums use fused multiply-adds.
     float Z = 0.0f;
     float3 acc = make_float3(0.0f, 0.0f, 0.0f);
-    for (int i = -kHalo; i <= kHalo; ++i) {
-        const float ki = c_kernel15[kHalo + i];
-#pragma unroll 5
-        for (int j = -kHalo; j <= kHalo; ++j) {
-            const float3 s = tile[threadIdx.y + kHalo + j][threadIdx.x + kHalo + i];
+    const float ce = P.bilateral_exp2;
+#pragma unroll 1
+    for (int i = 0; i < 2 * kHalo + 1; ++i) {
+#pragma unroll
+        for (int j = 0; j < 2 * kHalo + 1; ++j) {
+            const float3 s = tile[threadIdx.y + j][threadIdx.x + i];
             const float vx = s.x - cc.x, vy = s.y - cc.y, vz = s.z - cc.z;
-            const float dd = (vx * vx + vy * vy) + vz * vz;
-            const float pdf = 0.39894f * expf(-0.5f * dd / (sigma * sigma)) / sigma;  // normpdf3
-            const float f = pdf * bZ * c_kernel15[kHalo + j] * ki;
-            Z = Z + f;
-            acc = make_float3(acc.x + f * s.x, acc.y + f * s.y, acc.z + f * s.z);
+            const float dd = __fmaf_rn(vz, vz, __fmaf_rn(vy, vy, __fmul_rn(vx, vx)));
+            const float f = __fmul_rn(ex2_approx(__fmul_rn(dd, ce)), P.bw[i * (2 * kHalo + 1) + j]);
+            Z = __fadd_rn(Z, f);
+            acc = make_float3(__fmaf_rn(f, s.x, acc.x), __fmaf_rn(f, s.y, acc.y), __fmaf_rn(f, s.z, acc.z));
         }
     }
     const int64_t idx = (int64_t)y * W + x;
@@ -163,6 +169,18 @@ void gaussian_stencil(float out[9]) {
         for (int c = 0; c < 3; ++c) out[r * 3 + c] = (float)(S[r][c] / norm);
 }
 
+// normpdf's constant factor times bZ times KERNEL[7+j] * KERNEL[7+i], in the shader's order
+// (filter.glsl KERNEL[15] = normpdf(x, 10) at x = -7..7, as the shader lists it).
+void bilateral_weights(float w[225]) {
+    static const float K[15] = {0.031225216f, 0.033322271f, 0.035206333f, 0.036826804f, 0.038138565f,
+                                0.039104044f, 0.039695028f, 0.039894000f, 0.039695028f, 0.039104044f,
+                                0.038138565f, 0.036826804f, 0.035206333f, 0.033322271f, 0.031225216f};
+    const float sigma = 10.0f;
+    const float bz = 1.0f / (0.39894f * 1.0f / sigma);  // 1 / normpdf(0, sigma)
+    for (int i = 0; i < 15; ++i)
+        for (int j = 0; j < 15; ++j) w[i * 15 + j] = 0.39894f / sigma * bz * K[j] * K[i];
+}
+
 int grid1(int64_t n) {
     const int64_t g = (n + 255) / 256;
     return (int)(g < 1 ? 1 : (g > 152 * 16 ? 152 * 16 : g));
@@ -193,6 +211,8 @@ extern "C" int vct_specular_filter(const vct_specular_filter_desc* desc, const f
     P.tonemap = desc->tonemap_enable;
     P.method = desc->filter_method;
     gaussian_stencil(P.stencil);
+    P.bilateral_exp2 = (float)(-0.5 / 100.0 * 1.4426950408889634);
+    bilateral_weights(P.bw);
     const dim3 block(kBX, kBY), grid((width + kBX - 1) / kBX, (height + kBY - 1) / kBY);
     cudaStream_t st = as_stream(stream);
     const float4* d = reinterpret_cast<const float4*>(diffuse_rgba);
