@@ -456,6 +456,14 @@ int vct_specular_filter_stencil(float out_host[9]);
  * (round half up); one uint32 per pixel with bytes B, G, R, A. */
 int vct_present_srgb8(const float* rgba, int32_t width, int32_t height, uint32_t* out_bgra8, void* stream);
 
+/* ------------------------------------------------------------ scene ingest */
+
+/* Reverses the scanline filters of an inflated PNG image (filter byte + row
+ * per scanline; None / Sub / Up / Average / Paeth, ISO/IEC 15948 section 9)
+ * into `out_host` (rows x row_bytes).  bpp = bytes per pixel (at least 1).
+ * Host memory; used by the glTF loader for the scene's images. */
+int vct_png_unfilter(const uint8_t* filtered_host, int64_t row_bytes, int64_t rows, int32_t bpp, uint8_t* out_host);
+
 /* SparseVoxelizer::preVoxelize + cmdVoxelize (VFS/RenderPass/Octree/SparseVoxelizer.cpp:248-326)
  * with voxelizer.{vert,geom,frag}: count pass, host readback of the count
  * into *count_host, write pass of packed uint2 fragments in traversal order.

@@ -211,8 +211,12 @@ def scene_view(scene):
     keep = [np.ascontiguousarray(scene.positions, np.float32), np.ascontiguousarray(scene.normals, np.float32),
             np.ascontiguousarray(scene.indices, np.uint32), np.ascontiguousarray(scene.tri_material, np.uint32),
             np.ascontiguousarray(scene.materials), np.ascontiguousarray(scene.textures, np.uint32)]
+    nm, ti, ninst = None, None, 0
+    if getattr(scene, "node_matrices", None) is not None:
+        keep += [np.ascontiguousarray(scene.node_matrices, np.float32), np.ascontiguousarray(scene.tri_instance, np.uint32)]
+        nm, ti, ninst = _p(keep[6]), _p(keep[7]), keep[6].shape[0]
     sv = SceneView(_p(keep[0]), _p(keep[1]), _p(keep[2]), keep[0].shape[0], keep[2].shape[0], _p(keep[3]),
-                   _p(keep[4]), keep[4].shape[0], _p(keep[5]), keep[5].shape[0], None, None, 0)
+                   _p(keep[4]), keep[4].shape[0], _p(keep[5]), keep[5].shape[0], nm, ti, ninst)
     sv._keep = keep
     return sv
 

@@ -227,14 +227,17 @@ struct WorldTri {
 
 inline WorldTri world_triangle(const SceneView& s, int64_t t) {
     WorldTri w;
-    const uint32_t inst = s.triangle_instance ? s.triangle_instance[t] : 0u;
+    // instance and vertex indices clamped to the arrays, as the CUDA path does
+    const uint32_t inst =
+        s.triangle_instance ? std::min<uint32_t>(s.triangle_instance[t], (uint32_t)std::max(s.instance_count - 1, 0)) : 0u;
+    const uint32_t vmax = (uint32_t)std::max<int64_t>(s.vertex_count - 1, 0);
     Mat4 model = mat_identity(), it = mat_identity();
     if (s.node_matrices) {
         std::memcpy(model.m, s.node_matrices + 32 * (int64_t)inst, 64);
         std::memcpy(it.m, s.node_matrices + 32 * (int64_t)inst + 16, 64);
     }
     for (int k = 0; k < 3; ++k) {
-        const uint32_t vi = s.indices[3 * t + k];
+        const uint32_t vi = std::min(s.indices[3 * t + k], vmax);
         const float* p = s.positions + 3 * (int64_t)vi;
         const float* n = s.normals + 3 * (int64_t)vi;
         if (s.node_matrices) {

@@ -5,8 +5,9 @@
 // (VFS/RenderPass/Clipmap/VoxelizationPass.cpp:335-357, 438-448) fed by
 // Application::updateClipRegionBoundingBox (VFS/Application.cpp:116-128),
 // Voxelizer::setViewProjection (VFS/RenderPass/Clipmap/Voxelizer.cpp:394-423),
-// DirectionalLight::setTransform (VFS/DirectionalLight.cpp:21-47) and
-// Camera::updateCamera (VFS/Camera.cpp:110-117).  The
+// DirectionalLight::setTransform (VFS/DirectionalLight.cpp:21-47),
+// Camera::updateCamera (VFS/Camera.cpp:110-117) and the glTF node matrices
+// (VFS/Util/GLTFLoader.cpp:399-431, VFS/GLTFScene.cpp:398-412).  The
 // calls below are written here from those functions' arguments; nothing of
 // the reference is compiled.  Prints JSON with every float as its bit pattern.
 #define GLM_FORCE_SIZE_T_LENGTH
@@ -17,6 +18,7 @@
 #include <cstring>
 #include <glm/glm.hpp>
 #include <glm/gtc/matrix_transform.hpp>
+#include <glm/gtc/quaternion.hpp>
 
 static uint32_t bits(float f) {
     uint32_t u;
@@ -129,6 +131,32 @@ int main() {
         std::printf(",\"proj_inv\":");
         print_mat(glm::inverse(proj));
         std::printf("}");
+    }
+    // GLTFLoader::processNode / GetLocalMatrix (VFS/Util/GLTFLoader.cpp:399-431,511-517) and
+    // GLTFScene::uploadMatrixBuffer (VFS/GLTFScene.cpp:398-412): a chain of three nodes
+    std::printf("],\"nodes\":[");
+    // translation xyz, rotation quaternion xyzw (glTF order), scale xyz
+    const float trs[][10] = {{1.5f, -2.0f, 0.25f, 0.0f, 0.38268343f, 0.0f, 0.92387953f, 2.0f, 2.0f, 2.0f},
+                             {0.0f, 3.0f, -1.0f, 0.1f, 0.2f, 0.3f, 0.9273618f, 1.0f, 0.5f, 1.5f},
+                             {-4.0f, 0.5f, 7.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.75f, 0.75f, 0.75f}};
+    glm::mat4 parent(1.0f);
+    first = true;
+    for (auto& n : trs) {
+        const glm::quat q(n[6], n[3], n[4], n[5]);  // glm::quat(w, x, y, z)
+        const glm::mat4 local = glm::translate(glm::mat4(1.0f), glm::vec3(n[0], n[1], n[2])) * glm::mat4_cast(q) *
+                                glm::scale(glm::mat4(1.0f), glm::vec3(n[7], n[8], n[9])) * glm::mat4(1.0f);
+        const glm::mat4 world = parent * local;
+        std::printf("%s{\"trs\":[", first ? "" : ",");
+        first = false;
+        for (int i = 0; i < 10; ++i) std::printf("%u%s", bits(n[i]), i == 9 ? "" : ",");
+        std::printf("],\"local\":");
+        print_mat(local);
+        std::printf(",\"world\":");
+        print_mat(world);
+        std::printf(",\"it_world\":");
+        print_mat(glm::transpose(glm::inverse(world)));
+        std::printf("}");
+        parent = world;
     }
     std::printf("]}\n");
     return 0;

@@ -13,7 +13,9 @@ tree, which does not travel with the tests):
      * the clip regions of VoxelizationPass::createVoxelClipmap,
      * the three view-projection matrices of Voxelizer::setViewProjection,
      * the view / projection of DirectionalLight::setTransform,
-     * the CamMatrix block of Camera::updateCamera (glm::perspective, glm::inverse).
+     * the CamMatrix block of Camera::updateCamera (glm::perspective, glm::inverse),
+     * the node matrices of the glTF loader (translate * mat4_cast(quat) * scale, parent chains,
+       transpose(inverse(world))).
 2. Parses the fixed cone tables and trace constants out of
    VFS/Shaders/voxelConeTracing.frag.
 Writes glm_host_math.json and cone_tables.json next to this script.

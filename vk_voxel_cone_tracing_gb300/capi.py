@@ -175,6 +175,7 @@ _SIGS: dict[str, tuple] = {
     "vct_specular_filter": (C.c_int, [P, P, P, C.c_int32, C.c_int32, P, P]),
     "vct_specular_filter_stencil": (C.c_int, [P]),
     "vct_present_srgb8": (C.c_int, [P, C.c_int32, C.c_int32, P, P]),
+    "vct_png_unfilter": (C.c_int, [P, C.c_int64, C.c_int64, C.c_int32, P]),
     "vct_clear_atlas": (C.c_int, [P, C.c_int32, P]),
     "vct_voxelize_opacity": (C.c_int, [P, P, C.c_int32, P, C.c_uint32, P, P]),
     "vct_shadow_depth": (C.c_int, [P, P, P, C.c_int32, C.c_int32, P, P]),

@@ -199,11 +199,14 @@ struct WTri {
 
 __device__ inline WTri world_triangle(const vct_scene& s, int64_t t) {
     WTri w;
-    const uint32_t inst = s.triangle_instance ? __ldg(s.triangle_instance + t) : 0u;
+    // instance and vertex indices are clamped to the scene's arrays (a bad
+    // index reads the last entry instead of out of bounds)
+    const uint32_t inst = s.triangle_instance ? min(__ldg(s.triangle_instance + t), (uint32_t)max(s.instance_count - 1, 0)) : 0u;
     const float* model = s.node_matrices ? s.node_matrices + 32 * (int64_t)inst : nullptr;
+    const uint32_t vmax = (uint32_t)max(s.vertex_count - 1, (int64_t)0);
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        const uint32_t vi = __ldg(s.indices + 3 * t + k);
+        const uint32_t vi = min(__ldg(s.indices + 3 * t + k), vmax);
         const float* p = s.positions + 3 * (int64_t)vi;
         const float* n = s.normals + 3 * (int64_t)vi;
         float px = __ldg(p), py = __ldg(p + 1), pz = __ldg(p + 2);
@@ -1335,6 +1338,7 @@ static int check_scene(const vct_scene* s) {
     VCT_CHECK_ARG(s->positions && s->normals && s->indices, "scene positions / normals / indices are required");
     VCT_CHECK_ARG(s->materials && s->material_count > 0, "scene needs at least one material");
     VCT_CHECK_ARG(!s->node_matrices || s->instance_count > 0, "node matrices given without an instance count");
+    VCT_CHECK_ARG(s->vertex_count > 0 && s->vertex_count <= (1LL << 32), "scene vertex count out of range");
     return VCT_OK;
 }
 

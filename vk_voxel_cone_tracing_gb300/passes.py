@@ -14,6 +14,7 @@ import torch
 
 from . import capi
 from .clipmap import _ptr, _stream
+from .scene import world_positions
 
 
 class Workspace:
@@ -50,11 +51,17 @@ class DeviceScene:
         self.tri_material = torch.from_numpy(np.ascontiguousarray(scene.tri_material, np.uint32).view(np.int32)).to(device)
         self.materials = torch.from_numpy(np.ascontiguousarray(scene.materials).view(np.uint8)).to(device)
         self.textures = torch.from_numpy(np.ascontiguousarray(scene.textures, np.uint32).view(np.int32)).to(device)
+        nm, ti, ninst = None, None, 0
+        if getattr(scene, "node_matrices", None) is not None:
+            self.node_matrices = torch.from_numpy(np.ascontiguousarray(scene.node_matrices, np.float32)).to(device)
+            self.tri_instance = torch.from_numpy(
+                np.ascontiguousarray(scene.tri_instance, np.uint32).view(np.int32)).to(device)
+            nm, ti, ninst = self.node_matrices.data_ptr(), self.tri_instance.data_ptr(), scene.node_matrices.shape[0]
         self.desc = capi.Scene(self.positions.data_ptr(), self.normals.data_ptr(), self.indices.data_ptr(),
                                scene.positions.shape[0], scene.indices.shape[0], self.tri_material.data_ptr(),
                                self.materials.data_ptr(), scene.materials.shape[0], self.textures.data_ptr(),
-                               scene.textures.shape[0], None, None, 0)
-        p = scene.positions
+                               scene.textures.shape[0], nm, ti, ninst)
+        p = world_positions(scene)
         self.bb_min = p.min(0).astype(np.float32)
         self.bb_max = p.max(0).astype(np.float32)
 

@@ -48,12 +48,14 @@ assert MATERIAL_DTYPE.itemsize == 80
 
 @dataclass
 class Scene:
-    positions: np.ndarray   # (V, 3) f32, world space
+    positions: np.ndarray   # (V, 3) f32, object space (world space without node matrices)
     normals: np.ndarray     # (V, 3) f32
-    indices: np.ndarray     # (T, 3) u32
+    indices: np.ndarray     # (T, 3) u32, into the whole vertex arrays
     tri_material: np.ndarray  # (T,) u32
     materials: np.ndarray   # (M,) MATERIAL_DTYPE
-    textures: np.ndarray    # (M,) u32 RGBA8 1x1 base-colour texels
+    textures: np.ndarray    # (X,) u32 RGBA8 1x1 texels, indexed by the materials' texture ids
+    node_matrices: np.ndarray | None = None  # (N, 32) f32: NodeMatrix {model, itModel}, column-major
+    tri_instance: np.ndarray | None = None   # (T,) u32: the NodeMatrix of each triangle
 
     @property
     def triangle_count(self) -> int:
@@ -61,6 +63,20 @@ class Scene:
 
     def triangles(self) -> np.ndarray:
         return self.positions[self.indices]  # (T, 3, 3)
+
+
+def world_positions(scene: Scene) -> np.ndarray:
+    """World-space corners of every triangle, (3T, 3) f32: NodeMatrix.model * (p, 1) in glm's
+    mat4 * vec4 order ((c0 x + c1 y) + (c2 z + c3 w)); the object positions without node matrices."""
+    if scene.node_matrices is None:
+        return np.asarray(scene.positions, np.float32)
+    idx = np.asarray(scene.indices, np.int64).reshape(-1)
+    inst = np.minimum(np.repeat(np.asarray(scene.tri_instance, np.int64), 3), scene.node_matrices.shape[0] - 1)
+    m = np.asarray(scene.node_matrices, np.float32)[inst, :16]
+    p = np.asarray(scene.positions, np.float32)[idx]
+    x, y, z = p[:, 0:1], p[:, 1:2], p[:, 2:3]
+    r = (m[:, 0:4] * x + m[:, 4:8] * y) + (m[:, 8:12] * z + m[:, 12:16])
+    return r[:, :3].astype(np.float32)
 
 
 def _rgba8(rng, n):
