@@ -221,6 +221,16 @@ int64_t vct_atlas_texels(int32_t clipmap_resolution);
 int vct_clip_regions(const float camera_pos_host[3], int32_t clipmap_resolution,
                      int32_t voxel_extent_l0, vct_clipmap_region regions_host[6]);
 
+/* VoxelizationPass::fillRevoxelizationRegions + calculateChangeDelta
+ * (VFS/RenderPass/Clipmap/VoxelizationPass.cpp:438-494), the toroidal mode
+ * the reference leaves switched off (:79-92): moves each persistent region
+ * (in/out) by the camera-snapped delta of its own corner and lists the newly
+ * covered slabs (at most 3 per level, or the whole region when a delta
+ * reaches the extent) with their levels.  Host only. */
+int vct_update_clip_regions(vct_clipmap_region regions_inout_host[6], const float camera_pos_host[3], int32_t R,
+                            int32_t extent_l0, vct_clipmap_region slabs_out_host[18], int32_t slab_level_out_host[18],
+                            int32_t* slab_count_host);
+
 /* ------------------------------------------------------- clipmap passes */
 
 struct vct_texture_s; /* the radiance texture handle (see vct_texture_create) */
@@ -464,6 +474,17 @@ int vct_present_srgb8(const float* rgba, int32_t width, int32_t height, uint32_t
  * Host memory; used by the glTF loader for the scene's images. */
 int vct_png_unfilter(const uint8_t* filtered_host, int64_t row_bytes, int64_t rows, int32_t bpp, uint8_t* out_host);
 
+/* The toroidal half of VoxelizationPass (VoxelizationPass.cpp:127-141,
+ * 190-212): clear each slab at its corner wrapped into the level
+ * (ClipmapCleaner), then voxelise, for every level with slabs, the fragments
+ * that fall inside them -- with the level's full-region projection, so a
+ * voxel comes out as the full pass at `regions` would make it.  A slab that
+ * covers the whole region revoxelises its level in full.  Slabs and levels
+ * as vct_update_clip_regions lists them (host arrays). */
+int vct_voxelize_opacity_slabs(const vct_scene* scene, const vct_clipmap_region regions_host[6], int32_t R,
+                               uint32_t* opacity_atlas, const vct_clipmap_region* slabs_host,
+                               const int32_t* slab_levels_host, int32_t slab_count, vct_workspace ws, void* stream);
+
 /* SparseVoxelizer::preVoxelize + cmdVoxelize (VFS/RenderPass/Octree/SparseVoxelizer.cpp:248-326)
  * with voxelizer.{vert,geom,frag}: count pass, host readback of the count
  * into *count_host, write pass of packed uint2 fragments in traversal order.
@@ -533,7 +554,22 @@ typedef struct vct_frame_desc {
     struct vct_texture_s* radiance_texture; /* may be NULL: an RGBA8 texture of the same resolution that
                                                receives every radiance texel the frame's copy-alpha and
                                                mip passes write (the texture the fast trace samples) */
+    int32_t revoxelization;                 /* VCT_REVOX_FULL (the reference as shipped) or VCT_REVOX_TOROIDAL */
+    int32_t reserved;
+    vct_clipmap_region* regions_state;      /* host, 6 regions: FULL writes the frame's regions here (may be
+                                               NULL); TOROIDAL reads the previous frame's regions, moves them
+                                               (vct_update_clip_regions) and writes them back (required) */
 } vct_frame_desc;
+
+/* Opacity revoxelisation of a frame.  FULL: clear the atlas and voxelise
+ * every level at regions placed from the camera (VoxelizationPass.cpp:79-92,
+ * _fullRevoxelization stays true).  TOROIDAL: the regions persist; only the
+ * slabs the camera move uncovers are cleared and voxelised, and only the
+ * levels that moved get new opacity mips (the reference's switched-off path,
+ * VoxelizationPass.cpp:93-141, 167-178, 450-494).  The opacity atlas must
+ * hold the previous frame's voxels of `regions_state`. */
+#define VCT_REVOX_FULL 0
+#define VCT_REVOX_TOROIDAL 1
 
 /* Application::run's pre-pass sequence (VFS/Application.cpp:142-201):
  * VoxelizationPass (clear, voxelise all levels, opacity mips, border wrap),

@@ -7,6 +7,8 @@
 // the RGBA8 results are a deterministic function of the inputs.
 #pragma once
 
+#include <cstdlib>
+
 #include "oracle_common.hpp"
 
 namespace vcto {
@@ -42,6 +44,44 @@ inline void clip_regions(const float cam[3], int R, int extent_l0, Region out[6]
             r.min_corner[a] += d;
         }
     }
+}
+
+// VoxelizationPass::fillRevoxelizationRegions + calculateChangeDelta
+// (VoxelizationPass.cpp:438-494): move persistent regions by the snapped
+// delta of their own corner; list the uncovered slabs (whole region when a
+// delta reaches the extent).  Returns the slab count.
+inline int update_clip_regions(Region regions[6], const float cam[3], int R, int extent_l0, Region slabs[18],
+                               int32_t levels[18]) {
+    static const int kMinChange[6] = {2, 2, 2, 2, 2, 1};
+    int n = 0;
+    for (int l = 0; l < 6; ++l) {
+        Region& r = regions[l];
+        const float half_size = (float)((extent_l0 >> 1) * (1 << l));
+        const float min_change = r.voxel_size * (float)kMinChange[l];
+        int32_t d[3];
+        for (int a = 0; a < 3; ++a) {
+            const float bb_min = cam[a] - half_size;
+            const float delta_w = bb_min - (float)r.min_corner[a] * r.voxel_size;
+            d[a] = (int32_t)std::trunc(delta_w / min_change) * kMinChange[l];
+            r.min_corner[a] += d[a];
+        }
+        if (std::abs(d[0]) >= (int)r.extent[0] || std::abs(d[1]) >= (int)r.extent[1] ||
+            std::abs(d[2]) >= (int)r.extent[2]) {
+            slabs[n] = r;
+            levels[n++] = l;
+            continue;
+        }
+        for (int a = 0; a < 3; ++a) {
+            if (std::abs(d[a]) < kMinChange[l]) continue;
+            Region sl = r;
+            sl.extent[a] = (uint32_t)std::abs(d[a]);
+            if (d[a] > 0) sl.min_corner[a] = r.min_corner[a] + (int32_t)r.extent[a] - (int32_t)sl.extent[a];
+            slabs[n] = sl;
+            levels[n++] = l;
+        }
+    }
+    (void)R;
+    return n;
 }
 
 // ------------------------------------------------------------------ clear

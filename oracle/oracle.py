@@ -74,6 +74,9 @@ def lib():
         L.vcto_camera_matrix.argtypes = [P, P, P, C.c_float, C.c_float, P]
         L.vcto_inverse4.argtypes = [P, P]
         L.vcto_gbuffer.argtypes = [P, P, C.c_int, C.c_int, P]
+        L.vcto_update_clip_regions.restype = C.c_int
+        L.vcto_update_clip_regions.argtypes = [P, P, C.c_int, C.c_int, P, P]
+        L.vcto_voxelize_opacity_slabs.argtypes = [P, C.c_int, P, P, P, P, C.c_int]
         L.vcto_gaussian_stencil.argtypes = [P]
         L.vcto_specular_filter.argtypes = [P, P, P, C.c_int, C.c_int, P]
         L.vcto_present_srgb8.argtypes = [P, C.c_int64, P]
@@ -259,6 +262,25 @@ def shadow_depth(scene, shadow_desc_bytes: bytes, W: int, H: int) -> np.ndarray:
     sv = scene_view(scene)
     lib().vcto_shadow_depth(C.byref(sv), _p(sd), _p(depth), W, H)
     return depth
+
+
+def update_clip_regions(regions: np.ndarray, cam, R: int, extent_l0: int = 16):
+    """Toroidal region update: moves `regions` ((6, 7) int32 records, in place) and returns the slabs
+    ((n, 7) records) and their levels."""
+    assert regions.dtype == np.int32 and regions.flags["C_CONTIGUOUS"]
+    slabs = np.zeros((18, 7), np.int32)
+    levels = np.zeros(18, np.int32)
+    c = np.asarray(cam, np.float32)
+    n = lib().vcto_update_clip_regions(_p(regions), _p(c), R, extent_l0, _p(slabs), _p(levels))
+    return slabs[:n].copy(), levels[:n].copy()
+
+
+def voxelize_opacity_slabs(scene, R: int, regions: np.ndarray, atlas: np.ndarray, slabs: np.ndarray,
+                           levels: np.ndarray) -> None:
+    sv = scene_view(scene)
+    lib().vcto_voxelize_opacity_slabs(C.byref(sv), R, _p(_regions_arg(regions)), _p(atlas),
+                                      _p(np.ascontiguousarray(slabs, np.int32)),
+                                      _p(np.ascontiguousarray(levels, np.int32)), len(levels))
 
 
 def camera_matrix(position, direction, up=(0.0, 1.0, 0.0), fovy_degrees=60.0, aspect=16.0 / 9.0) -> np.ndarray:

@@ -418,8 +418,22 @@ inline int clip_vertices(const WorldTri& w, const Mat4 vp[3], V4<float> c[3]) {
     return axis;
 }
 
+// Fragment filter of the toroidal update: per level, keep everything
+// (unrestricted) or only the union of the level's slabs (per axis an interval
+// [lo, hi], empty when lo > hi).
+struct SlabFilter {
+    uint32_t restricted = 0;
+    float lo[6][3], hi[6][3];
+    bool keeps(int level, V3<float> p) const {
+        if (!((restricted >> level) & 1u)) return true;
+        return (p.x >= lo[level][0] && p.x <= hi[level][0]) || (p.y >= lo[level][1] && p.y <= hi[level][1]) ||
+               (p.z >= lo[level][2] && p.z <= hi[level][2]);
+    }
+};
+
 // VoxelizationPass::onUpdate + msaaVoxelizer.* over the levels in `level_mask`.
-inline void voxelize_opacity(const SceneView& s, int R, const Region regions[6], uint32_t* atlas, int level_mask) {
+inline void voxelize_opacity(const SceneView& s, int R, const Region regions[6], uint32_t* atlas, int level_mask,
+                             const SlabFilter* filter = nullptr) {
     Atlas A(R);
     for (int64_t t = 0; t < s.triangle_count; ++t) {
         WorldTri w = world_triangle(s, t);
@@ -438,12 +452,49 @@ inline void voxelize_opacity(const SceneView& s, int R, const Region regions[6],
                 if (wp.x < d.region_min[0] || wp.y < d.region_min[1] || wp.z < d.region_min[2] ||
                     wp.x > d.region_max[0] || wp.y > d.region_max[1] || wp.z > d.region_max[2])
                     return;
+                if (filter && !filter->keeps(level, wp)) return;
                 if (mat.occlusion_texture > -1 && texture_1x1(s, mat.occlusion_texture).x < 0.1f) return;
                 I3 ic = clip_image_coords(d, wp);
                 for (int f = 0; f < 6; ++f) atlas[A.index(ic.x + (R + 2) * f, ic.y, ic.z)] = 0xFFFFFFFFu;
             });
         }
     }
+}
+
+// The toroidal update of the opacity atlas (VoxelizationPass.cpp:127-141,
+// 190-212 with fillRevoxelizationRegions' slabs): clear each slab at its
+// wrapped corner, then voxelise the levels with slabs keeping only the
+// fragments inside them; a slab spanning the whole region keeps the whole
+// level.  Slab bounds as Voxelizer::cmdVoxelize would set them for the slab.
+inline void voxelize_opacity_slabs(const SceneView& s, int R, const Region regions[6], uint32_t* atlas,
+                                   const Region* slabs, const int32_t* levels, int n) {
+    SlabFilter F;
+    uint32_t changed = 0, full = 0;
+    for (int l = 0; l < 6; ++l)
+        for (int a = 0; a < 3; ++a) {
+            F.lo[l][a] = 3.0e38f;
+            F.hi[l][a] = -3.0e38f;
+        }
+    for (int i = 0; i < n; ++i) {
+        const Region& sl = slabs[i];
+        const int l = levels[i];
+        changed |= 1u << l;
+        int thin = -1;
+        for (int a = 0; a < 3; ++a)
+            if (sl.extent[a] != (uint32_t)R) thin = a;
+        if (thin < 0) {
+            full |= 1u << l;
+        } else {
+            const float vs = sl.voxel_size;
+            F.lo[l][thin] = std::min(F.lo[l][thin], (float)sl.min_corner[thin] * vs - 1e-6f);
+            F.hi[l][thin] = std::max(F.hi[l][thin], (float)(sl.min_corner[thin] + (int32_t)sl.extent[thin]) * vs + 1e-6f);
+        }
+        int32_t mn[3];
+        for (int a = 0; a < 3; ++a) mn[a] = ((sl.min_corner[a] % R) + R) % R;
+        clear_region(atlas, R, mn, sl.extent, l, 6);
+    }
+    F.restricted = 0x3Fu & ~full;
+    voxelize_opacity(s, R, regions, atlas, (int)changed, &F);
 }
 
 // RSM pass depth (reflectiveShadowPass.vert:40-50): gl_Position =

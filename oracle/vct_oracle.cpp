@@ -167,6 +167,14 @@ void vcto_specular_filter(const FilterDesc* fd, const float* diffuse, const floa
     specular_filter(*fd, diffuse, specular, W, H, out);
 }
 void vcto_present_srgb8(const float* rgba, int64_t n, uint32_t* out) { present_srgb8(rgba, n, out); }
+int vcto_update_clip_regions(Region regions[6], const float cam[3], int R, int extent_l0, Region slabs[18],
+                             int32_t levels[18]) {
+    return update_clip_regions(regions, cam, R, extent_l0, slabs, levels);
+}
+void vcto_voxelize_opacity_slabs(const SceneView* s, int R, const Region regions[6], uint32_t* atlas,
+                                 const Region* slabs, const int32_t* levels, int n) {
+    voxelize_opacity_slabs(*s, R, regions, atlas, slabs, levels, n);
+}
 void vcto_inject_radiance(const SceneView* s, int R, const Region regions[6], const float* shadow, int sw, int sh,
                           const ShadowDesc* sd, const LightDesc* light, uint32_t* radiance, int level_mask) {
     inject_radiance(*s, R, regions, shadow, sw, sh, *sd, *light, radiance, level_mask);

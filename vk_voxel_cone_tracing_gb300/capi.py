@@ -36,6 +36,9 @@ FILTER_GAUSSIAN = 1
 INJECT_DETERMINISTIC = 0
 INJECT_ATOMIC = 1
 
+REVOX_FULL = 0
+REVOX_TOROIDAL = 1
+
 SVO_DETERMINISTIC = 0
 SVO_ATOMIC = 1
 
@@ -128,7 +131,8 @@ class FrameDesc(C.Structure):
     _fields_ = [("camera_pos", f3), ("clipmap_resolution", C.c_int32), ("frame_index", C.c_int32),
                 ("inject_mode", C.c_int32), ("shadow_width", C.c_int32), ("shadow_height", C.c_int32),
                 ("light", DirectionalLightDesc), ("light_shadow", DirectionalLightShadowDesc),
-                ("radiance_texture", C.c_void_p)]
+                ("radiance_texture", C.c_void_p), ("revoxelization", C.c_int32), ("reserved", C.c_int32),
+                ("regions_state", C.c_void_p)]
 
 
 class ShadowMap(C.Structure):
@@ -148,6 +152,8 @@ _SIGS: dict[str, tuple] = {
     "vct_version": (C.c_char_p, []),
     "vct_atlas_texels": (C.c_int64, [C.c_int32]),
     "vct_clip_regions": (C.c_int, [P, C.c_int32, C.c_int32, P]),
+    "vct_update_clip_regions": (C.c_int, [P, P, C.c_int32, C.c_int32, P, P, P]),
+    "vct_voxelize_opacity_slabs": (C.c_int, [P, P, C.c_int32, P, P, P, C.c_int32, P, P]),
     "vct_clear_region": (C.c_int, [P, P, P]),
     "vct_copy_alpha": (C.c_int, [P, P, P, P]),
     "vct_downsample": (C.c_int, [P, P, C.c_int32, P]),

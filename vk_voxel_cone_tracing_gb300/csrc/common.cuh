@@ -47,8 +47,12 @@ int copy_alpha_downsample_pass(uint32_t* radiance, const uint32_t* opacity, cons
 // zero and marks each texel it writes in *touched (a bitmap over the atlas's
 // texel indices, in the workspace's second buffer), and the copy-alpha / mip
 // passes read unmarked texels as zero rgb -- the cleared result.
+// With nslabs >= 0 the opacity atlas is updated toroidally: only the listed
+// slabs are cleared and revoxelised (levels with a whole-region slab in
+// full), and only the revoxelised levels' opacity mips are rebuilt.
 int frame_raster_passes(const vct_scene* scene, const vct_frame_desc* f, const vct_clipmap_region regions[6],
-                        uint32_t due, uint32_t* opacity, uint32_t* radiance, float* shadow_depth, vct_workspace_s* ws,
+                        uint32_t due, const vct_clipmap_region* slabs, const int32_t* slab_levels, int nslabs,
+                        uint32_t* opacity, uint32_t* radiance, float* shadow_depth, vct_workspace_s* ws,
                         const uint32_t** touched, cudaStream_t st);
 
 // ---------------------------------------------------------------- errors

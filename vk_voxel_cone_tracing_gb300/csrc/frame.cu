@@ -3,7 +3,9 @@
 // Application::buildClipmapMethodPasses, :406-522):
 //
 //   VoxelizationPass       clear opacity, voxelise every level, opacity
-//                          mips 1..5, opacity border wrap
+//                          mips 1..5, opacity border wrap (or, in the
+//                          toroidal mode, clear + voxelise the slabs the
+//                          camera move uncovered and redo the moved levels' mips)
 //   RSMPass                directional-light depth map
 //   RadianceInjectionPass  for each level due this frame (frame % 2^level == 0):
 //                          clear, inject; then copy-alpha and radiance mips
@@ -24,9 +26,24 @@ extern "C" int vct_clipmap_frame(const vct_scene* scene, const vct_frame_desc* f
     VCT_CHECK_ARG(!f->radiance_texture || (vct::texture_format(f->radiance_texture) == VCT_TEX_RGBA8 &&
                                            vct::texture_resolution(f->radiance_texture) == R),
                   "vct_clipmap_frame: the radiance texture must be RGBA8 of the clipmap resolution");
+    VCT_CHECK_ARG(f->revoxelization == VCT_REVOX_FULL || f->revoxelization == VCT_REVOX_TOROIDAL,
+                  "vct_clipmap_frame: bad revoxelization mode");
+    const bool toroidal = f->revoxelization == VCT_REVOX_TOROIDAL;
+    VCT_CHECK_ARG(!toroidal || f->regions_state, "vct_clipmap_frame: the toroidal mode needs regions_state");
     vct_clipmap_region regions[6];
-    int rc = vct_clip_regions(f->camera_pos, R, VCT_VOXEL_EXTENT_L0, regions);
+    vct_clipmap_region slabs[18];
+    int32_t slab_levels[18];
+    int32_t nslabs = -1;  // full revoxelisation
+    int rc;
+    if (toroidal) {
+        for (int l = 0; l < 6; ++l) regions[l] = f->regions_state[l];
+        rc = vct_update_clip_regions(regions, f->camera_pos, R, VCT_VOXEL_EXTENT_L0, slabs, slab_levels, &nslabs);
+    } else {
+        rc = vct_clip_regions(f->camera_pos, R, VCT_VOXEL_EXTENT_L0, regions);
+    }
     if (rc != VCT_OK) return rc;
+    if (f->regions_state)
+        for (int l = 0; l < 6; ++l) f->regions_state[l] = regions[l];
     if (regions_out)
         for (int l = 0; l < 6; ++l) regions_out[l] = regions[l];
 
@@ -40,14 +57,32 @@ extern "C" int vct_clipmap_frame(const vct_scene* scene, const vct_frame_desc* f
         // VoxelizationPass, RSMPass and RadianceInjectionPass up to the fold,
         // with the opacity voxelisation and the injection's coverage count
         // sharing one coverage pass (same results as the passes below)
-        if ((rc = vct::frame_raster_passes(scene, f, regions, due, opacity, radiance, shadow_depth, ws, &touched,
-                                           st)) != VCT_OK)
+        if ((rc = vct::frame_raster_passes(scene, f, regions, due, slabs, slab_levels, nslabs, opacity, radiance,
+                                           shadow_depth, ws, &touched, st)) != VCT_OK)
             return rc;
     } else {
-        // VoxelizationPass (full revoxelisation every frame, VoxelizationPass.cpp:79-125)
-        if ((rc = vct_clear_atlas(opacity, R, stream)) != VCT_OK) return rc;
-        if ((rc = vct_voxelize_opacity(scene, regions, R, opacity, 0x3Fu, ws, stream)) != VCT_OK) return rc;
-        if ((rc = vct_downsample_all(opacity, regions, R, VCT_DOWNSAMPLE_OPACITY, stream)) != VCT_OK) return rc;
+        if (!toroidal) {
+            // VoxelizationPass (full revoxelisation every frame, VoxelizationPass.cpp:79-125)
+            if ((rc = vct_clear_atlas(opacity, R, stream)) != VCT_OK) return rc;
+            if ((rc = vct_voxelize_opacity(scene, regions, R, opacity, 0x3Fu, ws, stream)) != VCT_OK) return rc;
+            if ((rc = vct_downsample_all(opacity, regions, R, VCT_DOWNSAMPLE_OPACITY, stream)) != VCT_OK) return rc;
+        } else {
+            // the toroidal path: slabs cleared and voxelised, mips of the levels that moved
+            if ((rc = vct_voxelize_opacity_slabs(scene, regions, R, opacity, slabs, slab_levels, nslabs, ws,
+                                                 stream)) != VCT_OK)
+                return rc;
+            uint32_t moved = 0;
+            for (int i = 0; i < nslabs; ++i) moved |= 1u << slab_levels[i];
+            for (int l = 1; l < 6; ++l) {
+                if (!((moved >> l) & 1u)) continue;
+                vct_downsample_desc d;
+                for (int a = 0; a < 3; ++a) d.prev_region_min_corner[a] = regions[l - 1].min_corner[a];
+                d.clip_level = l;
+                d.clipmap_resolution = R;
+                d.downsample_region_size = VCT_DOWNSAMPLE_REGION_SIZE;
+                if ((rc = vct_downsample(opacity, &d, VCT_DOWNSAMPLE_OPACITY, stream)) != VCT_OK) return rc;
+            }
+        }
         vct_border_wrapping_desc bw = {(uint32_t)R, VCT_VOXEL_BORDER, VCT_FACE_COUNT, VCT_CLIP_LEVEL_COUNT};
         if ((rc = vct_wrap_border(opacity, &bw, stream)) != VCT_OK) return rc;
         // RSMPass: the depth map the injection's visibility samples

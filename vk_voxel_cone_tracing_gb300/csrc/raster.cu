@@ -347,8 +347,39 @@ struct RasterArgs {
     int64_t items;
     uint32_t invalid_key;  // injection record key that sorts past every texel
     uint32_t count_levels; // injection: the clip levels (bit l) whose samples are counted and emitted
-    unsigned long long* vis;  // G-buffer: per pixel (depth bits << 32 | triangle * 8 + sub-triangle), min wins
+    unsigned long long* vis;  // G-buffer: per pixel (depth bits << 32 | triangle * 6 + sub-triangle), min wins
+    // toroidal revoxelisation: levels whose bit is set keep only the opacity
+    // fragments inside the union of their slabs (axis a: slab_lo[l][a] <=
+    // p.a <= slab_hi[l][a]; an empty interval has lo > hi)
+    uint32_t slab_levels;
+    float slab_lo[6][3], slab_hi[6][3];
 };
+
+// A fragment at world position p of a slab-restricted level is kept when it
+// lies inside one of the level's slabs.
+__device__ inline bool in_slabs(const RasterArgs& A, int lvl, float3 p) {
+    const float* lo = A.slab_lo[lvl];
+    const float* hi = A.slab_hi[lvl];
+    return (p.x >= lo[0] && p.x <= hi[0]) || (p.y >= lo[1] && p.y <= hi[1]) || (p.z >= lo[2] && p.z <= hi[2]);
+}
+
+// Conservative triangle cull for a slab-restricted level: false when no
+// interpolated point of the triangle can fall inside a slab (the margin
+// covers the rounding of the FP32 barycentric interpolation).
+__device__ inline bool tri_meets_slabs(const RasterArgs& A, int lvl, const float3 p[3]) {
+    const float mn[3] = {fminf(fminf(p[0].x, p[1].x), p[2].x), fminf(fminf(p[0].y, p[1].y), p[2].y),
+                         fminf(fminf(p[0].z, p[1].z), p[2].z)};
+    const float mx[3] = {fmaxf(fmaxf(p[0].x, p[1].x), p[2].x), fmaxf(fmaxf(p[0].y, p[1].y), p[2].y),
+                         fmaxf(fmaxf(p[0].z, p[1].z), p[2].z)};
+    bool hit = false;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float lo = A.slab_lo[lvl][a], hi = A.slab_hi[lvl][a];
+        const float m = 1e-5f * (fabsf(mn[a]) + fabsf(mx[a])) + 1e-6f;
+        hit = hit || (lo <= hi && mx[a] + m >= lo && mn[a] - m <= hi);
+    }
+    return hit;
+}
 
 // Items are numbered triangle-major (item = tri * nlevels + level index) and
 // stay below 2^31, so 32-bit arithmetic suffices.
@@ -478,6 +509,16 @@ __device__ inline bool item_setup(const RasterArgs& A, const WTri& w, int lvl, R
             c[k] = make_float4(a, b, 1.0f, 1.0f);
         }
     } else {
+        // toroidal revoxelisation: a level restricted to its slabs skips the
+        // triangles that cannot reach them, unless the fused pass also counts
+        // the level's injection samples
+        if ((A.slab_levels >> lvl) & 1u) {
+            const bool counted = A.kind == K_OPA_COUNT && ((A.count_levels >> lvl) & 1u);
+            if ((A.kind == K_OPACITY || A.kind == K_OPA_COUNT) && !counted && !tri_meets_slabs(A, lvl, w.p)) {
+                rs.ok = false;
+                return false;
+            }
+        }
         const int axis = dominant_axis(w.p);
         const float* M = A.vp[lvl][axis];
 #pragma unroll
@@ -1042,6 +1083,7 @@ __global__ void __launch_bounds__(128, 6) k_cover(const __grid_constant__ Raster
                                 wp.z < d.region_min_corner[2] || wp.x > d.region_max_corner[0] ||
                                 wp.y > d.region_max_corner[1] || wp.z > d.region_max_corner[2])
                                 continue;
+                            if (((A.slab_levels >> lvl) & 1u) && !in_slabs(A, lvl, wp)) continue;
                             const AtlasDims AD(A.R);
                             const int3 ic = clip_image_coords(d, wp);
                             if (ic.x == last_ic.x && ic.y == last_ic.y && ic.z == last_ic.z) continue;
@@ -1618,6 +1660,114 @@ extern "C" int vct_clear_atlas(uint32_t* atlas, int32_t R, void* stream) {
     return VCT_OK;
 }
 
+namespace vct {
+
+// The opacity pass's restriction for a toroidal update from its slab list
+// (vct_update_clip_regions' output): a level with a whole-region slab is
+// voxelised in full; every other level keeps only the fragments inside its
+// slabs, each slab bounded like the region Voxelizer::cmdVoxelize would be
+// given for it (min * voxel size - 1e-6, max * voxel size + 1e-6; the other
+// two axes span the level's region, whose bounds the pass already applies).
+struct SlabPlan {
+    uint32_t restricted = 0;  // levels limited to their slabs
+    uint32_t changed = 0;     // levels with at least one slab (cleared, voxelised, mipped)
+    float lo[6][3], hi[6][3];
+};
+
+int slab_plan(const vct_clipmap_region regions[6], int R, const vct_clipmap_region* slabs, const int32_t* levels,
+              int n, SlabPlan* P) {
+    VCT_CHECK_ARG(n >= 0 && n <= 18 && (n == 0 || (slabs && levels)), "toroidal update: bad slab list");
+    uint32_t full = 0;
+    for (int l = 0; l < 6; ++l)
+        for (int a = 0; a < 3; ++a) {
+            P->lo[l][a] = 3.0e38f;
+            P->hi[l][a] = -3.0e38f;
+        }
+    for (int i = 0; i < n; ++i) {
+        const int l = levels[i];
+        VCT_CHECK_ARG(l >= 0 && l < 6, "toroidal update: slab level out of range");
+        const vct_clipmap_region& sr = slabs[i];
+        const vct_clipmap_region& r = regions[l];
+        VCT_CHECK_ARG(sr.voxel_size == r.voxel_size, "toroidal update: slab voxel size differs from its level's");
+        int thin = -1, nthin = 0;
+        for (int a = 0; a < 3; ++a) {
+            VCT_CHECK_ARG(sr.extent[a] >= 1 && sr.extent[a] <= (uint32_t)R, "toroidal update: bad slab extent");
+            if (sr.extent[a] != (uint32_t)R) {
+                thin = a;
+                ++nthin;
+            }
+        }
+        VCT_CHECK_ARG(nthin <= 1, "toroidal update: a slab is thin along one axis at most");
+        P->changed |= 1u << l;
+        if (nthin == 0) {
+            full |= 1u << l;
+            continue;
+        }
+        const float vs = sr.voxel_size;
+        P->lo[l][thin] = fminf(P->lo[l][thin], (float)sr.min_corner[thin] * vs - 1e-6f);
+        P->hi[l][thin] = fmaxf(P->hi[l][thin], (float)(sr.min_corner[thin] + (int32_t)sr.extent[thin]) * vs + 1e-6f);
+    }
+    P->restricted = 0x3Fu & ~full;
+    return VCT_OK;
+}
+
+// ClipmapCleaner::cmdClearOpacityClipRegion of every slab, at its corner
+// wrapped into the level ((min % extent + extent) % extent,
+// VoxelizationPass.cpp:127-141).
+int clear_slabs(uint32_t* atlas, int R, const vct_clipmap_region* slabs, const int32_t* levels, int n, void* stream) {
+    for (int i = 0; i < n; ++i) {
+        vct_image_cleaning_desc c;
+        for (int a = 0; a < 3; ++a) {
+            c.region_min_corner[a] = ((slabs[i].min_corner[a] % R) + R) % R;
+            c.clip_max_extent[a] = slabs[i].extent[a];
+        }
+        c.clip_level = levels[i];
+        c.clipmap_resolution = R;
+        c.face_count = VCT_FACE_COUNT;
+        int rc = vct_clear_region(atlas, &c, stream);
+        if (rc != VCT_OK) return rc;
+    }
+    return VCT_OK;
+}
+
+void apply_slabs(RasterArgs& A, const SlabPlan& P) {
+    A.slab_levels = P.restricted;
+    memcpy(A.slab_lo, P.lo, sizeof(P.lo));
+    memcpy(A.slab_hi, P.hi, sizeof(P.hi));
+}
+
+}  // namespace vct
+
+extern "C" int vct_voxelize_opacity_slabs(const vct_scene* scene, const vct_clipmap_region regions[6], int32_t R,
+                                          uint32_t* atlas, const vct_clipmap_region* slabs, const int32_t* slab_levels,
+                                          int32_t slab_count, vct_workspace_s* ws, void* stream) {
+    int rc = check_scene(scene);
+    if (rc != VCT_OK) return rc;
+    VCT_CHECK_ARG(regions && atlas && ws && valid_resolution(R), "vct_voxelize_opacity_slabs: bad argument");
+    SlabPlan P;
+    if ((rc = slab_plan(regions, R, slabs, slab_levels, slab_count, &P)) != VCT_OK) return rc;
+    if ((rc = clear_slabs(atlas, R, slabs, slab_levels, slab_count, stream)) != VCT_OK) return rc;
+    if (scene->triangle_count == 0 || P.changed == 0) return VCT_OK;
+    RasterArgs A;
+    memset(&A, 0, sizeof(A));
+    A.s = *scene;
+    A.kind = K_OPACITY;
+    A.R = R;
+    A.W = A.H = R + 2;
+    fill_clipmap_levels(A, regions, R, P.changed);
+    apply_slabs(A, P);
+    A.items = scene->triangle_count * A.nlevels;
+    A.atlas = atlas;
+    cudaStream_t st = as_stream(stream);
+    size_t off;
+    TilePlan plan;
+    rc = plan_tiles(A, ws, off, &plan, st);
+    if (rc != VCT_OK) return rc;
+    if (plan.total) launch_cover<K_OPACITY, P_DIRECT>(A, plan, nullptr, nullptr, nullptr, nullptr, st);
+    VCT_LAUNCH_CHECK();
+    return VCT_OK;
+}
+
 extern "C" int vct_voxelize_opacity(const vct_scene* scene, const vct_clipmap_region regions[6], int32_t R,
                                     uint32_t* atlas, uint32_t level_mask, vct_workspace_s* ws, void* stream) {
     int rc = check_scene(scene);
@@ -1784,11 +1934,15 @@ namespace vct {
 // levels, then shading, sort and fold.  The results equal the passes run one
 // by one in the reference's order.
 int frame_raster_passes(const vct_scene* scene, const vct_frame_desc* f, const vct_clipmap_region regions[6],
-                        uint32_t due, uint32_t* opacity, uint32_t* radiance, float* shadow_depth, vct_workspace_s* ws,
+                        uint32_t due, const vct_clipmap_region* slabs, const int32_t* slab_levels, int nslabs,
+                        uint32_t* opacity, uint32_t* radiance, float* shadow_depth, vct_workspace_s* ws,
                         const uint32_t** touched_out, cudaStream_t st) {
     const int R = f->clipmap_resolution;
     void* stream = st;
     int rc;
+    const bool toroidal = nslabs >= 0;
+    SlabPlan P;
+    if (toroidal && (rc = slab_plan(regions, R, slabs, slab_levels, nslabs, &P)) != VCT_OK) return rc;
     // the touched-texel bitmap, one bit per atlas texel, cleared every frame
     const size_t bm_bytes = a256(((size_t)AtlasDims(R).texels() + 31) / 32 * 4);
     if (ws->aux_bytes < bm_bytes) {
@@ -1804,7 +1958,9 @@ int frame_raster_passes(const vct_scene* scene, const vct_frame_desc* f, const v
     uint32_t* touched = (uint32_t*)ws->aux;
     VCT_CUDA_TRY(cudaMemsetAsync(touched, 0, bm_bytes, st));
     *touched_out = touched;
-    if ((rc = vct_clear_atlas(opacity, R, stream)) != VCT_OK) return rc;
+    if (toroidal) rc = clear_slabs(opacity, R, slabs, slab_levels, nslabs, stream);
+    else rc = vct_clear_atlas(opacity, R, stream);
+    if (rc != VCT_OK) return rc;
     vct_shadow_map sm = {nullptr, 0, 0};
     if (f->shadow_width > 0) {
         if ((rc = vct_shadow_depth(scene, &f->light_shadow, shadow_depth, f->shadow_width, f->shadow_height, ws,
@@ -1826,6 +1982,7 @@ int frame_raster_passes(const vct_scene* scene, const vct_frame_desc* f, const v
         C.R = R;
         C.W = C.H = R + 2;
         fill_clipmap_levels(C, regions, R, 0x3Fu);
+        if (toroidal) apply_slabs(C, P);
         C.items = scene->triangle_count * C.nlevels;
         C.atlas = opacity;
         C.count_levels = due;
@@ -1840,7 +1997,20 @@ int frame_raster_passes(const vct_scene* scene, const vct_frame_desc* f, const v
         }
         if (rc != VCT_OK) return rc;
     }
-    if ((rc = vct_downsample_all(opacity, regions, R, VCT_DOWNSAMPLE_OPACITY, stream)) != VCT_OK) return rc;
+    if (!toroidal) {
+        if ((rc = vct_downsample_all(opacity, regions, R, VCT_DOWNSAMPLE_OPACITY, stream)) != VCT_OK) return rc;
+    } else {
+        // VoxelizationPass::onEndRenderPass: the mips of the levels that were revoxelised
+        for (int l = 1; l < 6; ++l) {
+            if (!((P.changed >> l) & 1u)) continue;
+            vct_downsample_desc d;
+            for (int a = 0; a < 3; ++a) d.prev_region_min_corner[a] = regions[l - 1].min_corner[a];
+            d.clip_level = l;
+            d.clipmap_resolution = R;
+            d.downsample_region_size = VCT_DOWNSAMPLE_REGION_SIZE;
+            if ((rc = vct_downsample(opacity, &d, VCT_DOWNSAMPLE_OPACITY, stream)) != VCT_OK) return rc;
+        }
+    }
     vct_border_wrapping_desc bw = {(uint32_t)R, VCT_VOXEL_BORDER, VCT_FACE_COUNT, VCT_CLIP_LEVEL_COUNT};
     if ((rc = vct_wrap_border(opacity, &bw, stream)) != VCT_OK) return rc;
     // the due radiance levels' clear is folded into the fold (texels start from

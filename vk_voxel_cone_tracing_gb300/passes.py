@@ -213,9 +213,12 @@ def svo_cone_trace(desc: capi.ConeTracingDesc, eye, pool: torch.Tensor, node_cou
 def clipmap_frame(dscene: DeviceScene, camera_pos, R: int, opacity: torch.Tensor, radiance: torch.Tensor,
                   shadow: torch.Tensor | None, light: capi.DirectionalLightDesc,
                   light_shadow: capi.DirectionalLightShadowDesc, ws: Workspace, frame_index: int = 0,
-                  inject_mode: int = capi.INJECT_DETERMINISTIC, texture=None):
+                  inject_mode: int = capi.INJECT_DETERMINISTIC, texture=None, revoxelization: int = capi.REVOX_FULL,
+                  regions_state=None):
     """vct_clipmap_frame: voxelise, mips, border, shadow depth, inject, copy alpha, radiance mips; `texture`
-    (an RGBA8 RadianceTexture of resolution R) is kept equal to the radiance atlas's written texels."""
+    (an RGBA8 RadianceTexture of resolution R) is kept equal to the radiance atlas's written texels.
+    `regions_state` ((ClipmapRegion * 6), kept by the caller) persists the regions between frames: a FULL
+    frame writes them, a TOROIDAL frame moves them and revoxelises only the uncovered slabs."""
     f = capi.FrameDesc()
     f.camera_pos = capi.f3(*camera_pos)
     f.clipmap_resolution = R
@@ -226,7 +229,29 @@ def clipmap_frame(dscene: DeviceScene, camera_pos, R: int, opacity: torch.Tensor
     f.light = light
     f.light_shadow = light_shadow
     f.radiance_texture = texture.handle if texture is not None else None
+    f.revoxelization = revoxelization
+    f.regions_state = C.cast(regions_state, C.c_void_p) if regions_state is not None else None
     regs = (capi.ClipmapRegion * 6)()
     capi.call("vct_clipmap_frame", capi.ref(dscene.desc), capi.ref(f), _ptr(opacity), _ptr(radiance),
               _ptr(shadow), C.cast(regs, C.c_void_p), ws.handle, _stream())
     return regs
+
+
+def update_clip_regions(regions, camera_pos, R: int, extent_l0: int = capi.VOXEL_EXTENT_L0):
+    """vct_update_clip_regions: moves `regions` ((ClipmapRegion * 6), in place) toward the camera and returns
+    the uncovered slabs as (ClipmapRegion * n, [level per slab])."""
+    slabs = (capi.ClipmapRegion * 18)()
+    levels = (C.c_int32 * 18)()
+    n = C.c_int32(0)
+    cam = (C.c_float * 3)(*camera_pos)
+    capi.call("vct_update_clip_regions", C.cast(regions, C.c_void_p), C.cast(cam, C.c_void_p), R, extent_l0,
+              C.cast(slabs, C.c_void_p), C.cast(levels, C.c_void_p), C.byref(n))
+    return slabs, list(levels[:n.value])
+
+
+def voxelize_opacity_slabs(dscene: DeviceScene, regions, R: int, atlas: torch.Tensor, slabs, levels,
+                           ws: Workspace) -> None:
+    """vct_voxelize_opacity_slabs: clear and revoxelise the listed slabs (toroidal update)."""
+    lv = (C.c_int32 * max(1, len(levels)))(*levels)
+    capi.call("vct_voxelize_opacity_slabs", capi.ref(dscene.desc), C.cast(regions, C.c_void_p), R, _ptr(atlas),
+              C.cast(slabs, C.c_void_p), C.cast(lv, C.c_void_p), len(levels), ws.handle, _stream())
