@@ -535,6 +535,94 @@ int vct_svo_cone_trace(const vct_cone_tracing_desc* desc, const vct_cam_matrix* 
                        const vct_surface_sample* samples, int64_t sample_count, float* diffuse_out,
                        float* specular_out, unsigned long long* cone_steps, void* stream);
 
+/* -------------------------------------------------- instances and batches */
+
+/* An atlas in the reference's layout ((R+2)*6 x (R+2)*6 x (R+2) texels),
+ * zeroed: RGBA8 (4 B per texel, VCT_TEX_RGBA8) or the packed FP16 form
+ * (8 B, VCT_TEX_RGBA16F). */
+int vct_atlas_alloc(int32_t R, int32_t format, void** out);
+int vct_atlas_free(void* atlas);
+
+/* One headless instance of the clipmap method: what Application::initialize
+ * and buildClipmapMethodPasses create once (VFS/Application.cpp:406-522) --
+ * opacity and radiance atlases, the light's depth map, the radiance texture,
+ * the raster workspace, the trace scratch -- and the state the passes keep
+ * between frames (frame index of the radiance cadence, clip regions). */
+typedef struct vct_config {
+    int32_t clipmap_resolution; /* R: power of two in [8, 1024] (the reference's DEFAULT_VOXEL_RESOLUTION) */
+    int32_t shadow_width;       /* light depth map size; 0 x 0 = no shadow pass (visibility 1) */
+    int32_t shadow_height;
+    int32_t reserved;
+    size_t workspace_bytes;     /* initial raster workspace (grows on demand) */
+} vct_config;
+
+typedef struct vct_context_s* vct_context;
+
+typedef struct vct_context_buffers {
+    uint32_t* opacity;                    /* RGBA8 atlases, device */
+    uint32_t* radiance;
+    float* shadow_depth;                  /* NULL without a shadow pass */
+    struct vct_texture_s* radiance_texture;
+    struct vct_workspace_s* workspace;
+    vct_clipmap_region regions[6];        /* of the last frame */
+    int32_t frame_index;                  /* of the next frame */
+    int32_t reserved;
+} vct_context_buffers;
+
+int vct_create(const vct_config* cfg_host, vct_context* out);
+int vct_destroy(vct_context ctx); /* synchronises the device */
+int vct_context_buffers_get(const struct vct_context_s* ctx, vct_context_buffers* out_host);
+/* Forget the frame history: the next frame is frame 0 (every radiance level
+ * due) with a full revoxelisation.  The atlases keep their contents. */
+int vct_context_reset(vct_context ctx);
+
+/* Application::run's pre-passes on the instance (vct_clipmap_frame with its
+ * buffers, deterministic injection, the radiance texture kept current); the
+ * frame index advances by one per call.  revoxelization: VCT_REVOX_FULL or
+ * VCT_REVOX_TOROIDAL (the first frame of an instance is always full). */
+int vct_context_frame(vct_context ctx, const vct_scene* scene, const float camera_pos_host[3],
+                      const vct_directional_light_desc* light_host,
+                      const vct_directional_light_shadow_desc* light_shadow_host, int32_t revoxelization,
+                      void* stream);
+
+/* VoxelConeTracingPass::onUpdate on the instance: the fast trace of
+ * `samples` against its radiance texture and depth map; volume_center,
+ * voxel_size and volume_dimension of `desc` are replaced by the ones the
+ * pass derives from the last frame's level-0 region
+ * (VoxelConeTracingPass.cpp:86-102).  The trace scratch grows on demand. */
+int vct_context_trace(vct_context ctx, const vct_cone_tracing_desc* desc_host, const vct_cam_matrix* cam_host,
+                      const vct_directional_light_desc* light_host,
+                      const vct_directional_light_shadow_desc* light_shadow_host,
+                      const vct_surface_sample* samples, int64_t sample_count, float* diffuse_out,
+                      float* specular_out, unsigned long long* cone_steps, void* stream);
+
+/* One independent unit of a batch: a frame of `scene` on `context` and the
+ * trace of `samples` (sample_count 0: frame only). */
+typedef struct vct_batch_job {
+    vct_context context;
+    const vct_scene* scene;
+    float camera_pos[3];
+    int32_t revoxelization;
+    int32_t reset;              /* nonzero: vct_context_reset first (an independent single-frame job) */
+    int32_t reserved;
+    vct_directional_light_desc light;
+    vct_directional_light_shadow_desc light_shadow;
+    const vct_cone_tracing_desc* trace_desc;
+    const vct_cam_matrix* cam;
+    const vct_surface_sample* samples;
+    int64_t sample_count;
+    float* diffuse_out;
+    float* specular_out;
+    unsigned long long* cone_steps;
+} vct_batch_job;
+
+/* Runs every job (frame + trace) on `streams` host threads, each with its
+ * own CUDA stream, so that one job's host-side waits overlap the others' GPU
+ * work; returns when all are done.  The contexts are dealt round-robin to the
+ * threads in order of first appearance; the jobs of one context run in list
+ * order on its thread. */
+int vct_batch_submit(const vct_batch_job* jobs_host, int32_t job_count, int32_t streams);
+
 /* ------------------------------------------------------------ one frame */
 
 /* Per-frame inputs of the clipmap method (Application::run and the passes it
@@ -618,6 +706,9 @@ VCT_STATIC_ASSERT(sizeof(vct_cam_matrix) == 144, "CamMatrix is 144 B");
 VCT_STATIC_ASSERT(sizeof(vct_directional_light_desc) == 32, "DirectionalLightDesc is 32 B");
 VCT_STATIC_ASSERT(sizeof(vct_directional_light_shadow_desc) == 136, "DirectionalLightShadowDesc is 136 B");
 VCT_STATIC_ASSERT(sizeof(vct_specular_filter_desc) == 16, "SpecularFilterPassDesc is 16 B");
+VCT_STATIC_ASSERT(sizeof(vct_config) == 24, "vct_config is 24 B");
+VCT_STATIC_ASSERT(sizeof(vct_context_buffers) == 216, "vct_context_buffers is 216 B");
+VCT_STATIC_ASSERT(sizeof(vct_batch_job) == 264, "vct_batch_job is 264 B");
 VCT_STATIC_ASSERT(sizeof(vct_gltf_shade_material) == 80, "GltfShadeMaterial is 80 B");
 VCT_STATIC_ASSERT(sizeof(vct_surface_sample) == 80, "surface sample is 80 B");
 

@@ -139,10 +139,30 @@ class ShadowMap(C.Structure):
     _fields_ = [("depth", C.c_void_p), ("width", C.c_int32), ("height", C.c_int32)]
 
 
+class Config(C.Structure):
+    _fields_ = [("clipmap_resolution", C.c_int32), ("shadow_width", C.c_int32), ("shadow_height", C.c_int32),
+                ("reserved", C.c_int32), ("workspace_bytes", C.c_size_t)]
+
+
+class ContextBuffers(C.Structure):
+    _fields_ = [("opacity", C.c_void_p), ("radiance", C.c_void_p), ("shadow_depth", C.c_void_p),
+                ("radiance_texture", C.c_void_p), ("workspace", C.c_void_p), ("regions", ClipmapRegion * 6),
+                ("frame_index", C.c_int32), ("reserved", C.c_int32)]
+
+
+class BatchJob(C.Structure):
+    _fields_ = [("context", C.c_void_p), ("scene", C.c_void_p), ("camera_pos", f3), ("revoxelization", C.c_int32),
+                ("reset", C.c_int32), ("reserved", C.c_int32), ("light", DirectionalLightDesc),
+                ("light_shadow", DirectionalLightShadowDesc), ("trace_desc", C.c_void_p), ("cam", C.c_void_p),
+                ("samples", C.c_void_p), ("sample_count", C.c_int64), ("diffuse_out", C.c_void_p),
+                ("specular_out", C.c_void_p), ("cone_steps", C.c_void_p)]
+
+
 STRUCT_SIZES = {
     ClipmapRegion: 28, VoxelizationDesc: 64, DownSampleDesc: 24, ImageCleaningDesc: 36, CopyAlphaDesc: 12,
     BorderWrappingDesc: 16, ConeTracingDesc: 52, CamMatrix: 144, DirectionalLightDesc: 32,
-    DirectionalLightShadowDesc: 136, GltfShadeMaterial: 80, Scene: 104, SpecularFilterDesc: 16,
+    DirectionalLightShadowDesc: 136, GltfShadeMaterial: 80, Scene: 104, SpecularFilterDesc: 16, Config: 24,
+    ContextBuffers: 216, BatchJob: 264,
 }
 
 # Every entry point of include/vct_capi.h: name -> (restype, argtypes).
@@ -182,6 +202,15 @@ _SIGS: dict[str, tuple] = {
     "vct_specular_filter_stencil": (C.c_int, [P]),
     "vct_present_srgb8": (C.c_int, [P, C.c_int32, C.c_int32, P, P]),
     "vct_png_unfilter": (C.c_int, [P, C.c_int64, C.c_int64, C.c_int32, P]),
+    "vct_atlas_alloc": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
+    "vct_atlas_free": (C.c_int, [P]),
+    "vct_create": (C.c_int, [P, C.POINTER(C.c_void_p)]),
+    "vct_destroy": (C.c_int, [P]),
+    "vct_context_buffers_get": (C.c_int, [P, P]),
+    "vct_context_reset": (C.c_int, [P]),
+    "vct_context_frame": (C.c_int, [P, P, P, P, P, C.c_int32, P]),
+    "vct_context_trace": (C.c_int, [P, P, P, P, P, P, C.c_int64, P, P, P, P]),
+    "vct_batch_submit": (C.c_int, [P, C.c_int32, C.c_int32]),
     "vct_clear_atlas": (C.c_int, [P, C.c_int32, P]),
     "vct_voxelize_opacity": (C.c_int, [P, P, C.c_int32, P, C.c_uint32, P, P]),
     "vct_shadow_depth": (C.c_int, [P, P, P, C.c_int32, C.c_int32, P, P]),
