@@ -288,6 +288,30 @@ int vct_cone_trace(const vct_cone_tracing_desc* desc, const vct_cam_matrix* cam,
                    float* diffuse_out, float* specular_out,
                    unsigned long long* cone_steps, void* stream);
 
+/* ------------------------------------------------ differentiable form */
+
+/* The FP32 trace over a float RGBA atlas (16 B per texel, the reference's
+ * layout; the FP16 form widened): the same march and epilogue as
+ * vct_cone_trace with the texels read as floats.  The forward of
+ * vct_cone_trace_backward. */
+int vct_cone_trace_f32(const vct_cone_tracing_desc* desc, const vct_cam_matrix* cam, const float* atlas4, int32_t R,
+                       const vct_shadow_map* shadow, const vct_directional_light_desc* light,
+                       const vct_directional_light_shadow_desc* light_shadow,
+                       const vct_surface_sample* samples, int64_t sample_count, float* diffuse_out,
+                       float* specular_out, unsigned long long* cone_steps, void* stream);
+
+/* The adjoint of vct_cone_trace_f32 with respect to the atlas: adds
+ * dL/d(texel) to grad_atlas4 (same layout, float RGBA; not cleared here)
+ * given dL/d(diffuse_out) and dL/d(specular_out) (sample_count x 4 floats
+ * each).  The number of march steps (the occlusion stop) and the clamps are
+ * held at their forward values.  Synchronises `stream`; VCT_E_OVERFLOW if a
+ * cone marches more than 8192 steps. */
+int vct_cone_trace_backward(const vct_cone_tracing_desc* desc, const vct_cam_matrix* cam, const float* atlas4,
+                            int32_t R, const vct_shadow_map* shadow, const vct_directional_light_desc* light,
+                            const vct_directional_light_shadow_desc* light_shadow,
+                            const vct_surface_sample* samples, int64_t sample_count, const float* grad_diffuse,
+                            const float* grad_specular, float* grad_atlas4, void* stream);
+
 /* ------------------------------------------- texture-sampled (fast) form */
 
 /* A hardware-filtered copy of a radiance atlas: a 3D CUDA array with

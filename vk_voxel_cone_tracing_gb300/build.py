@@ -28,7 +28,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
           "-Xptxas", "-O3",
           "--expt-relaxed-constexpr", "-I", str(INCLUDE)]
 # Units that mirror FP32 shader arithmetic op for op.
-NO_FMA = {"clipmap_passes.cu", "trace_exact.cu", "raster.cu", "svo.cu", "svo_trace.cu", "composite.cu"}
+NO_FMA = {"clipmap_passes.cu", "trace_exact.cu", "raster.cu", "svo.cu", "svo_trace.cu", "composite.cu", "trace_grad.cu"}
 
 
 def nvcc() -> str:

@@ -1,0 +1,316 @@
+// trace_grad.cu -- the adjoint of the FP32 cone trace over a float atlas
+// (vct_cone_trace_f32): given dL/d(diffuse out) and dL/d(specular out) per
+// sample, accumulate dL/d(texel) into a float RGBA atlas of the same layout.
+//
+// One thread per (sample, cone): the diffuse cones and the specular cone of
+// voxelConeTracing.frag:143-293.  The march's step schedule, levels, tap
+// positions, opacity corrections and occlusion decay depend on geometry
+// only; the number of steps depends on the volume through the occlusion
+// stop and is held fixed (the derivative of a piecewise-smooth function away
+// from its switches; likewise the clamps of opacity and of 1 - alpha).
+//
+// The cone state runs forward as
+//     k_i   = clamp(1 - A_i, 0, 1)                 (A: accumulated alpha)
+//     op_i  = clamp(1 - (1 - s_i.a)^c_i, 0, 1)     (c: opacity correction)
+//     C    += k_i c_i s_i.rgb,   A += k_i op_i
+//     O    += (1 - O) op_i / (1 + (t_i + vs_i) decay)
+// and the adjoint runs it backward (gC constant along the march):
+//     g(s_i.rgb) = gC k_i c_i
+//     g(op_i)    = gA k_i + gO (1 - O_i) / (1 + (t_i + vs_i) decay)
+//     g(s_i.a)   = g(op_i) c_i (1 - s_i.a)^(c_i - 1)      (inside the clamp)
+//     gA        += -(gC . s_i.rgb c_i + gA op_i)           (inside the clamp of k)
+//     gO        *= 1 - op_i / (1 + (t_i + vs_i) decay)
+// The backward needs A_i and O_i step by step in reverse: the forward pass
+// keeps a checkpoint of the march state every 32 steps, and each 32-step
+// segment is recomputed from its checkpoint before it is walked backward
+// (O(steps) work, a few KB of local memory per thread).  s_i is recomputed
+// from the atlas; g(s_i) is split over the two levels (1 - fr, fr), the three
+// faces (the direction weights) and the eight texels of each trilinear tap
+// (the products of the lerp fractions) and added to the gradient atlas with
+// float4 atomics.  Same FP32 expressions as the forward kernel (this unit is
+// built with -fmad=false like it), so the recomputed states are the forward's.
+#include "trace_exact.cuh"
+
+namespace vct {
+
+int fill_trace_params(TraceParams& P, const vct_cone_tracing_desc* desc, const vct_cam_matrix* cam,
+                      const vct_shadow_map* shadow, const vct_directional_light_desc* light,
+                      const vct_directional_light_shadow_desc* light_shadow);
+
+namespace {
+
+constexpr int kSegSteps = 32;
+constexpr int kMaxSegments = 256;  // 8192 steps per cone: the specular cone at R = 1024 takes ~7.1k
+
+struct MarchState {
+    float step, seg, diameter, alpha, occ;
+};
+
+struct Cone {
+    float3 start, dir, fo, wt, center;
+    float uvs, coef, start_level, step_factor, min_radius;
+};
+
+__device__ __forceinline__ void add4(float4* p, float4 v) {
+    if (v.x != 0.0f || v.y != 0.0f || v.z != 0.0f || v.w != 0.0f) atomicAdd(p, v);
+}
+
+// Adjoint of texture3d: the eight texels' shares of g.
+__device__ __forceinline__ void texture3d_grad(float4* __restrict__ G, const AtlasDims& A, float ux, float uy, float uz,
+                                               float4 g) {
+    float u = ux * (float)A.W - 0.5f, v = uy * (float)A.H - 0.5f, w = uz * (float)A.D - 0.5f;
+    float fu = floorf(u), fv = floorf(v), fw = floorf(w);
+    float a = u - fu, b = v - fv, c = w - fw;
+    int i0 = wrap_rep((int)fu, A.W), i1 = wrap_rep((int)fu + 1, A.W);
+    int j0 = wrap_rep((int)fv, A.H), j1 = wrap_rep((int)fv + 1, A.H);
+    int k0 = wrap_rep((int)fw, A.D), k1 = wrap_rep((int)fw + 1, A.D);
+    const float wi[2] = {1.0f - a, a}, wj[2] = {1.0f - b, b}, wk[2] = {1.0f - c, c};
+    const int ii[2] = {i0, i1}, jj[2] = {j0, j1}, kk[2] = {k0, k1};
+#pragma unroll
+    for (int z = 0; z < 2; ++z)
+#pragma unroll
+        for (int y = 0; y < 2; ++y)
+#pragma unroll
+            for (int x = 0; x < 2; ++x) {
+                const float wt = wi[x] * wj[y] * wk[z];
+                add4(G + A.index(ii[x], jj[y], kk[z]), make_float4(g.x * wt, g.y * wt, g.z * wt, g.w * wt));
+            }
+}
+
+// Adjoint of sample_clipmap: the three face taps' shares.
+__device__ __forceinline__ void sample_clipmap_grad(float4* __restrict__ G, const AtlasDims& A,
+                                                    const vct_cone_tracing_desc& d, float3 p, int level, float3 fo,
+                                                    float3 wt, float4 g) {
+    float vs = d.voxel_size * exp2f((float)level);
+    float extent = vs * d.volume_dimension;
+    float dim = d.volume_dimension;
+    float sx = (fractf(p.x / extent) * dim + 1.0f) / (dim + 2.0f);
+    float sy = (fractf(p.y / extent) * dim + 1.0f) / (dim + 2.0f);
+    float sz = (fractf(p.z / extent) * dim + 1.0f) / (dim + 2.0f);
+    sy = sy + (float)level;
+    sy = sy / (float)kClipLevels;
+    sx = sx / (float)kFaces;
+    texture3d_grad(G, A, sx + fo.x, sy, sz, make_float4(g.x * wt.x, g.y * wt.x, g.z * wt.x, g.w * wt.x));
+    texture3d_grad(G, A, sx + fo.y, sy, sz, make_float4(g.x * wt.y, g.y * wt.y, g.z * wt.y, g.w * wt.y));
+    texture3d_grad(G, A, sx + fo.z, sy, sz, make_float4(g.x * wt.z, g.y * wt.z, g.z * wt.z, g.w * wt.z));
+}
+
+// The volume-independent part of one step of trace_cone at state m.
+struct StepGeo {
+    float3 pos;
+    int lower, upper;
+    float fr, vs, correction;
+};
+
+__device__ __forceinline__ StepGeo step_geo(const Cone& K, const MarchState& m) {
+    StepGeo s;
+    s.pos = K.start + K.dir * m.step;
+    float dist = sqrtf(dot3(K.center - s.pos, K.center - s.pos));
+    float min_level = ceilf(log2f(dist / K.min_radius));
+    float cur_level = log2f(m.diameter / K.uvs);
+    cur_level = fminf(fmaxf(fmaxf(K.start_level, cur_level), min_level), (float)(kClipLevels - 1));
+    s.lower = (int)floorf(cur_level);
+    s.upper = (int)ceilf(cur_level);
+    s.fr = fractf(cur_level);
+    s.vs = K.uvs * exp2f(cur_level);
+    s.correction = m.seg / s.vs;
+    return s;
+}
+
+// One step of trace_cone (same expressions): advances m (alpha, occlusion,
+// schedule) and returns the step's sample.
+__device__ __forceinline__ float4 march_step(const F4Atlas& T, const vct_cone_tracing_desc& d, const Cone& K,
+                                             MarchState& m, const StepGeo& s) {
+    float4 lo = sample_clipmap(T, d, s.pos, s.lower, K.fo, K.wt);
+    float4 hi = sample_clipmap(T, d, s.pos, s.upper, K.fo, K.wt);
+    float4 smp = make_float4(lo.x * (1.0f - s.fr) + hi.x * s.fr, lo.y * (1.0f - s.fr) + hi.y * s.fr,
+                             lo.z * (1.0f - s.fr) + hi.z * s.fr, lo.w * (1.0f - s.fr) + hi.w * s.fr);
+    float opacity = clampf(1.0f - powf(1.0f - smp.w, s.correction), 0.0f, 1.0f);
+    float k = clampf(1.0f - m.alpha, 0.0f, 1.0f);
+    m.alpha = m.alpha + k * opacity;
+    m.occ = m.occ + (1.0f - m.occ) * opacity / (1.0f + (m.step + s.vs) * d.occlusion_decay);
+    float prev = m.step;
+    m.step = m.step + fmaxf(m.diameter, K.uvs) * K.step_factor;
+    m.seg = m.step - prev;
+    m.diameter = m.step * K.coef;
+    return smp;
+}
+
+// The adjoint of one cone: gC (rgb) and gO (d/d occlusion) at the end of the march.
+__device__ void cone_backward(const F4Atlas& T, float4* __restrict__ G, const vct_cone_tracing_desc& d, const Cone& K,
+                              float3 gC, float gO, float max_dist, int* __restrict__ err) {
+    MarchState ckpt[kMaxSegments];
+    MarchState m;
+    m.step = 0.0f;
+    m.diameter = fmaxf(0.0f * K.coef, K.uvs);
+    m.seg = K.uvs * exp2f(K.start_level);
+    m.alpha = 0.0f;
+    m.occ = 0.0f;
+    int n = 0;
+    while (m.step < max_dist && m.occ < 1.0f) {
+        if ((n % kSegSteps) == 0) {
+            if (n / kSegSteps >= kMaxSegments) {
+                atomicOr(err, 1);
+                return;
+            }
+            ckpt[n / kSegSteps] = m;
+        }
+        march_step(T, d, K, m, step_geo(K, m));
+        ++n;
+    }
+    float gA = 0.0f;
+    MarchState seg[kSegSteps];
+    for (int sidx = (n - 1) / kSegSteps; sidx >= 0 && n > 0; --sidx) {
+        const int first = sidx * kSegSteps, last = min(n, first + kSegSteps);
+        MarchState r = ckpt[sidx];
+        for (int i = first; i < last; ++i) {
+            seg[i - first] = r;
+            march_step(T, d, K, r, step_geo(K, r));
+        }
+        for (int i = last - 1; i >= first; --i) {
+            const MarchState& mi = seg[i - first];
+            const StepGeo s = step_geo(K, mi);
+            float4 lo = sample_clipmap(T, d, s.pos, s.lower, K.fo, K.wt);
+            float4 hi = sample_clipmap(T, d, s.pos, s.upper, K.fo, K.wt);
+            float4 smp = make_float4(lo.x * (1.0f - s.fr) + hi.x * s.fr, lo.y * (1.0f - s.fr) + hi.y * s.fr,
+                                     lo.z * (1.0f - s.fr) + hi.z * s.fr, lo.w * (1.0f - s.fr) + hi.w * s.fr);
+            const float c = s.correction;
+            const float base = 1.0f - smp.w;
+            const float op_raw = 1.0f - powf(base, c);
+            const float op = clampf(op_raw, 0.0f, 1.0f);
+            const float dop = (op_raw > 0.0f && op_raw < 1.0f && base > 0.0f) ? c * powf(base, c - 1.0f) : 0.0f;
+            const float k_raw = 1.0f - mi.alpha;
+            const float k = clampf(k_raw, 0.0f, 1.0f);
+            const float qd = 1.0f + (mi.step + s.vs) * d.occlusion_decay;
+            float4 gs;
+            gs.x = gC.x * k * c;
+            gs.y = gC.y * k * c;
+            gs.z = gC.z * k * c;
+            const float gop = gA * k + gO * (1.0f - mi.occ) / qd;
+            gs.w = gop * dop;
+            if (k_raw > 0.0f && k_raw < 1.0f) gA = gA - ((gC.x * smp.x + gC.y * smp.y + gC.z * smp.z) * c + gA * op);
+            gO = gO * (1.0f - op / qd);
+            // s = lo (1 - fr) + hi fr
+            const float4 glo = make_float4(gs.x * (1.0f - s.fr), gs.y * (1.0f - s.fr), gs.z * (1.0f - s.fr),
+                                           gs.w * (1.0f - s.fr));
+            const float4 ghi = make_float4(gs.x * s.fr, gs.y * s.fr, gs.z * s.fr, gs.w * s.fr);
+            sample_clipmap_grad(G, T.A, d, s.pos, s.lower, K.fo, K.wt, glo);
+            sample_clipmap_grad(G, T.A, d, s.pos, s.upper, K.fo, K.wt, ghi);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128) k_cone_trace_backward(TraceParams P, F4Atlas T,
+                                                             const vct_surface_sample* __restrict__ samples, int64_t n,
+                                                             const float4* __restrict__ gd, const float4* __restrict__ gs,
+                                                             float4* __restrict__ G, int* __restrict__ err) {
+    const vct_cone_tracing_desc& d = P.d;
+    const bool c32 = d.enable_32_cones != 0;
+    const int nc = c32 ? 32 : 16;
+    const int slots = nc + 1;
+    const uint32_t mode = d.rendering_mode;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * slots;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t / slots;
+        const int slot = (int)(t - i * slots);
+        GSample g = load_sample(samples + i, P.eye);
+        if (g.depth == 1.0f) continue;
+        float min_level = calc_min_level(d, g.wp);
+        float vs = d.voxel_size * exp2f(min_level);
+        Cone K;
+        K.start = g.wp + g.normal * (vs * d.trace_start_offset);
+        K.uvs = d.voxel_size;
+        K.center = f3(d.volume_center[0], d.volume_center[1], d.volume_center[2]);
+        K.min_radius = K.uvs * d.volume_dimension * 0.5f;
+        K.start_level = min_level;
+        float3 gC;
+        float gO;
+        float aperture;
+        const float4 GD = gd[i], GS = gs[i];
+        if (slot < nc) {
+            K.dir = c32 ? f3(c_dirs32[slot][0], c_dirs32[slot][1], c_dirs32[slot][2])
+                        : f3(c_dirs16[slot][0], c_dirs16[slot][1], c_dirs16[slot][2]);
+            const float cos_t = dot3(g.normal, K.dir);
+            if (cos_t < 0.0f) continue;
+            // dL/d(indirect): D.rgb = direct * ind.w + ind.rgb (modes 5 and the default), direct * ind.w (4),
+            // ind.w (7); the others do not read the volume
+            float3 g_ind = f3(0.f, 0.f, 0.f);
+            float g_ao = 0.0f;
+            const bool rgb_mode = mode == 5 || mode >= 8;
+            if (rgb_mode) g_ind = f3(GD.x, GD.y, GD.z);
+            if (rgb_mode || mode == 4) {
+                const float3 direct = direct_term(P, g);
+                g_ao = GD.x * direct.x + GD.y * direct.y + GD.z * direct.z;
+            } else if (mode == 7) {
+                g_ao = GD.x + GD.y + GD.z;
+            }
+            const float w = cos_t / (float)nc;
+            gC = f3(g_ind.x * w * (g.diffuse_color.x * d.indirect_diffuse_intensity),
+                    g_ind.y * w * (g.diffuse_color.y * d.indirect_diffuse_intensity),
+                    g_ind.z * w * (g.diffuse_color.z * d.indirect_diffuse_intensity));
+            gO = -(g_ao * w * d.ambient_occlusion_factor);  // the cone returns 1 - occlusion
+            aperture = c32 ? kAperture32 : kAperture16;
+            K.step_factor = fmaxf(kMinTraceStepFactor, d.min_trace_step_factor);
+        } else {
+            if (!has_specular_cone(g) || !(mode == 6 || mode >= 8)) continue;
+            K.dir = reflect3(f3(-g.view.x, -g.view.y, -g.view.z), g.normal);
+            const float isi = d.indirect_specular_intensity;
+            gC = f3(GS.x * g.specular_color.x * isi, GS.y * g.specular_color.y * isi, GS.z * g.specular_color.z * isi);
+            gO = 0.0f;
+            aperture = fmaxf(g.roughness, kMinSpecularAperture);
+            K.step_factor = d.voxel_size;
+        }
+        if (gC.x == 0.0f && gC.y == 0.0f && gC.z == 0.0f && gO == 0.0f) continue;
+        K.coef = 2.0f * tanf(aperture * 0.5f);
+        K.start = K.start + K.dir * (K.uvs * exp2f(K.start_level) * d.trace_start_offset * 0.5f);
+        K.fo = f3(K.dir.x > 0.0f ? 0.0f : 1.0f / 6.0f, K.dir.y > 0.0f ? 2.0f / 6.0f : 3.0f / 6.0f,
+                  K.dir.z > 0.0f ? 4.0f / 6.0f : 5.0f / 6.0f);
+        K.wt = f3(K.dir.x * K.dir.x, K.dir.y * K.dir.y, K.dir.z * K.dir.z);
+        cone_backward(T, G, d, K, gC, gO, kMaxTraceDistance, err);
+    }
+}
+
+}  // namespace
+}  // namespace vct
+
+using namespace vct;
+
+extern "C" int vct_cone_trace_backward(const vct_cone_tracing_desc* desc, const vct_cam_matrix* cam,
+                                       const float* atlas4, int32_t R, const vct_shadow_map* shadow,
+                                       const vct_directional_light_desc* light,
+                                       const vct_directional_light_shadow_desc* light_shadow,
+                                       const vct_surface_sample* samples, int64_t n, const float* grad_diffuse,
+                                       const float* grad_specular, float* grad_atlas4, void* stream) {
+    VCT_CHECK_ARG(atlas4 && grad_atlas4 && valid_resolution(R), "vct_cone_trace_backward: bad atlas / resolution");
+    VCT_CHECK_ARG((((uintptr_t)atlas4 | (uintptr_t)grad_atlas4) & 15) == 0,
+                  "vct_cone_trace_backward: atlases must be 16-byte aligned");
+    VCT_CHECK_ARG(n >= 0, "vct_cone_trace_backward: negative sample count");
+    if (n == 0) return VCT_OK;
+    VCT_CHECK_ARG(samples && grad_diffuse && grad_specular, "vct_cone_trace_backward: null sample or gradient buffer");
+    VCT_CHECK_ARG((((uintptr_t)samples | (uintptr_t)grad_diffuse | (uintptr_t)grad_specular) & 15) == 0,
+                  "vct_cone_trace_backward: sample / gradient buffers must be 16-byte aligned");
+    TraceParams P;
+    int rc = fill_trace_params(P, desc, cam, shadow, light, light_shadow);
+    if (rc != VCT_OK) return rc;
+    cudaStream_t st = as_stream(stream);
+    int* err = nullptr;
+    VCT_CUDA_TRY(cudaMallocAsync(&err, sizeof(int), st));
+    VCT_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), st));
+    F4Atlas T{reinterpret_cast<const float4*>(atlas4), AtlasDims(R)};
+    const int slots = (desc->enable_32_cones ? 32 : 16) + 1;
+    int64_t blocks = (n * slots + 127) / 128;
+    if (blocks > 152 * 32) blocks = 152 * 32;
+    k_cone_trace_backward<<<(int)blocks, 128, 0, st>>>(P, T, samples, n, reinterpret_cast<const float4*>(grad_diffuse),
+                                                        reinterpret_cast<const float4*>(grad_specular),
+                                                        reinterpret_cast<float4*>(grad_atlas4), err);
+    cudaError_t le = cudaGetLastError();
+    int h_err = 0;
+    cudaError_t ce = cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaError_t se = cudaStreamSynchronize(st);
+    cudaFreeAsync(err, st);
+    if (le != cudaSuccess) return cuda_fail(le, "k_cone_trace_backward");
+    if (ce != cudaSuccess) return cuda_fail(ce, "vct_cone_trace_backward readback");
+    if (se != cudaSuccess) return cuda_fail(se, "vct_cone_trace_backward");
+    if (h_err) return fail(VCT_E_OVERFLOW, "vct_cone_trace_backward: a cone marched more than 8192 steps");
+    return VCT_OK;
+}

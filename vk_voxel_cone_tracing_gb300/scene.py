@@ -299,6 +299,26 @@ def atlas_shape(R: int) -> tuple[int, int, int]:
     return (R + 2, (R + 2) * 6, (R + 2) * 6)
 
 
+def smooth_volume(R: int, seed: int = 5, max_alpha: float = 0.3, waves: int = 6) -> np.ndarray:
+    """A float RGBA atlas (reference layout, (D, H, W, 4) float32) of smooth noise: each channel a sum of
+    random low-frequency waves over the texel grid, rgb in [0, 1], alpha in [0, max_alpha] (the
+    differentiable form's test volume; below 1 alpha never saturates the march)."""
+    rng = np.random.default_rng(seed)
+    D, H, W = atlas_shape(R)
+    z, y, x = np.meshgrid(np.arange(D, dtype=np.float32), np.arange(H, dtype=np.float32),
+                          np.arange(W, dtype=np.float32), indexing="ij")
+    out = np.empty((D, H, W, 4), np.float32)
+    for c in range(4):
+        acc = np.zeros((D, H, W), np.float32)
+        for _ in range(waves):
+            k = rng.uniform(0.02, 0.12, 3).astype(np.float32) * 2 * np.pi
+            ph = np.float32(rng.uniform(0, 2 * np.pi))
+            acc += np.sin(k[0] * x + k[1] * y + k[2] * z + ph).astype(np.float32)
+        v = 0.5 + 0.5 * acc / waves
+        out[..., c] = v * (max_alpha if c == 3 else 1.0)
+    return out
+
+
 def random_atlas(R: int, seed: int = 3, fill: float = 0.15) -> np.ndarray:
     """Sparse random RGBA8 atlas (uint32 words, reference layout): `fill` of the texels are occupied."""
     rng = np.random.default_rng(seed)
