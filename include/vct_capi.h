@@ -312,6 +312,15 @@ int vct_cone_trace_backward(const vct_cone_tracing_desc* desc, const vct_cam_mat
                             const vct_surface_sample* samples, int64_t sample_count, const float* grad_diffuse,
                             const float* grad_specular, float* grad_atlas4, void* stream);
 
+/* DownSampler::cmdDownSampleRadiance / Opacity of one level on a float RGBA
+ * atlas (no 8-bit store; the RGBA8 pass's arithmetic otherwise), and its
+ * adjoint: grad_atlas4 enters holding dL/d(atlas after the level's pass) and
+ * leaves holding dL/d(atlas before it); atlas4 holds the forward's final
+ * values.  Run the adjoint from level 5 down to 1 to reach level 0. */
+int vct_downsample_f32(float* atlas4, const vct_downsample_desc* desc, int32_t mode, void* stream);
+int vct_downsample_backward(const float* atlas4, float* grad_atlas4, const vct_downsample_desc* desc, int32_t mode,
+                            void* stream);
+
 /* ------------------------------------------- texture-sampled (fast) form */
 
 /* A hardware-filtered copy of a radiance atlas: a 3D CUDA array with

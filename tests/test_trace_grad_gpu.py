@@ -95,3 +95,71 @@ def test_backward_matches_finite_differences(cuda, oracle, mode):
         if abs(fd - g) > 2e-2 * max(abs(fd), abs(g)) + 1e-5:
             bad.append((int(k), g, fd))
     assert not bad, bad[:6]
+
+
+def _ds_desc(regions, level, R):
+    from vk_voxel_cone_tracing_gb300 import capi
+    d = capi.DownSampleDesc()
+    d.prev_region_min_corner = capi.i3(*[int(x) for x in regions[level - 1, 0:3]])
+    d.clip_level = level
+    d.clipmap_resolution = R
+    d.downsample_region_size = capi.DOWNSAMPLE_REGION_SIZE
+    return d
+
+
+@pytest.mark.parametrize("mode", [1, 0])
+def test_downsample_f32_and_its_adjoint(cuda, oracle, mode):
+    """The float mips against the oracle's, and the adjoint of the five-level chain against central
+    differences of the oracle's chain (each scalar enters the chain linearly, so the difference quotient
+    is exact up to rounding)."""
+    torch = cuda
+    import ctypes as C
+    from vk_voxel_cone_tracing_gb300 import capi
+    from vk_voxel_cone_tracing_gb300.scene import smooth_volume
+    R = 16
+    regions = oracle.clip_regions((0.7, -0.3, 1.9), R)
+    vol = smooth_volume(R, seed=11, max_alpha=0.9)
+
+    def chain_oracle(v):
+        v = v.copy()
+        for level in range(1, 6):
+            oracle.downsample_f4(v, R, regions[level - 1, 0:3], level, mode)
+        return v
+
+    want = chain_oracle(vol)
+    a = torch.from_numpy(vol.reshape(-1)).cuda()
+    for level in range(1, 6):
+        capi.call("vct_downsample_f32", C.c_void_p(a.data_ptr()), capi.ref(_ds_desc(regions, level, R)), mode, None)
+    torch.cuda.synchronize()
+    got = a.cpu().numpy().reshape(vol.shape)
+    assert np.allclose(got, want, rtol=1e-6, atol=1e-7)
+    # adjoint of L = sum(W * chain(V))
+    rng = np.random.default_rng(mode)
+    W = rng.normal(size=vol.shape).astype(np.float32)
+    G = torch.from_numpy(W.reshape(-1).copy()).cuda()
+    for level in range(5, 0, -1):
+        capi.call("vct_downsample_backward", C.c_void_p(a.data_ptr()), C.c_void_p(G.data_ptr()),
+                  capi.ref(_ds_desc(regions, level, R)), mode, None)
+    torch.cuda.synchronize()
+    grad = G.cpu().numpy().reshape(vol.shape)
+    # entries of level 0 (which feed the whole chain) and of the mipped levels
+    D, H, W_ = vol.shape[:3]
+    picks = []
+    for level in (0, 1, 2, 4):
+        for _ in range(8):
+            z = rng.integers(1, R + 1)
+            y = rng.integers(1, R + 1) + level * (R + 2)
+            x = rng.integers(1, R + 1) + (R + 2) * rng.integers(0, 6)
+            picks.append((z, y, x, rng.integers(0, 4)))
+    eps = np.float32(1e-2)
+    bad = []
+    for z, y, x, c in picks:
+        vp, vm = vol.copy(), vol.copy()
+        vp[z, y, x, c] += eps
+        vm[z, y, x, c] -= eps
+        h = float(vp[z, y, x, c]) - float(vm[z, y, x, c])
+        fd = float(((chain_oracle(vp) - chain_oracle(vm)).astype(np.float64) * W).sum()) / h
+        g = float(grad[z, y, x, c])
+        if abs(fd - g) > 1e-3 * max(abs(fd), abs(g)) + 2e-5:
+            bad.append(((z, y, x, c), g, fd))
+    assert not bad, bad[:6]

@@ -183,6 +183,8 @@ _SIGS: dict[str, tuple] = {
     "vct_cone_trace": (C.c_int, [P, P, P, C.c_int32, P, P, P, P, C.c_int64, P, P, P, P]),
     "vct_cone_trace_f32": (C.c_int, [P, P, P, C.c_int32, P, P, P, P, C.c_int64, P, P, P, P]),
     "vct_cone_trace_backward": (C.c_int, [P, P, P, C.c_int32, P, P, P, P, C.c_int64, P, P, P, P]),
+    "vct_downsample_f32": (C.c_int, [P, P, C.c_int32, P]),
+    "vct_downsample_backward": (C.c_int, [P, P, P, C.c_int32, P]),
     "vct_texture_create": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     "vct_texture_update": (C.c_int, [P, P, P]),
     "vct_texture_read": (C.c_int, [P, P, P]),

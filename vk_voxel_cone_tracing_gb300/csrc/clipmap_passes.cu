@@ -385,6 +385,200 @@ extern "C" int vct_wrap_border(uint32_t* atlas, const vct_border_wrapping_desc* 
     return VCT_OK;
 }
 
+// ----------------------------------------------- differentiable (float) mips
+// The same level downsample on float RGBA texels (no 8-bit store), and its
+// adjoint.  One output voxel g of level l per thread: its write position,
+// the corner of its 2x2x2 child block in level l-1 and the band's lerp
+// factor, as k_downsample computes them.
+struct DsSite {
+    int wpos[3], ps[3];
+    float lerp;
+};
+
+__device__ __forceinline__ DsSite ds_site(const AtlasDims& A, int3 pmin, int level, int band, int lgh, uint32_t t) {
+    const int half = A.R >> 1;
+    const uint32_t m = (1u << lgh) - 1u;
+    const int g[3] = {(int)(t & m), (int)((t >> lgh) & m), (int)(t >> (2 * lgh))};
+    const int pm[3] = {pmin.x, pmin.y, pmin.z};
+    DsSite s;
+    float dist[3];
+    bool any_ge = false;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const int cur = (pm[a] >> 1) + g[a];
+        s.wpos[a] = ds_wrap(cur, A.R) + 1;
+        s.ps[a] = ds_wrap(cur << 1, A.R) + 1;
+        const float center = __fadd_rn((float)(pm[a] >> 1), (float)(half >> 1));
+        dist[a] = __fsub_rn(fabsf(__fsub_rn(__fadd_rn((float)cur, 0.5f), center)), 0.5f);
+        any_ge |= dist[a] >= (float)((half >> 1) - band);
+    }
+    s.wpos[1] += A.rb * level;
+    s.ps[1] += A.rb * (level - 1);
+    s.lerp = 0.0f;
+    if (any_ge) {
+        const float inv = 1.0f / __fadd_rn((float)band, 1.0f);
+        s.lerp = __fmul_rn(__fadd_rn(__fsub_rn(fmaxf(dist[0], fmaxf(dist[1], dist[2])), (float)((half >> 1) - band)), 1.0f), inv);
+    }
+    return s;
+}
+
+__device__ __forceinline__ int64_t ds_child(const AtlasDims& A, const DsSite& s, int f, int i) {
+    return A.index(s.ps[0] + (i & 1) + A.rb * f, s.ps[1] + ((i >> 1) & 1), s.ps[2] + ((i >> 2) & 1));
+}
+
+template <int MODE>
+__global__ void k_downsample_f32(float4* __restrict__ atlas, AtlasDims A, int3 pmin, int level, int band, int lgh) {
+    const uint32_t n = 1u << (3 * lgh);
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const DsSite st = ds_site(A, pmin, level, band, lgh, t);
+        for (int f = 0; f < 6; ++f) {
+            float4 v[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) v[i] = atlas[ds_child(A, st, f, i)];
+            const int64_t wi = A.index(st.wpos[0] + A.rb * f, st.wpos[1], st.wpos[2]);
+            const float4 own = atlas[wi];
+            if (MODE == 0) {
+                float s = 0.0f;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const float a0 = v[c_pairs[f][k][0]].w, a1 = v[c_pairs[f][k][1]].w;
+                    const float tt = __fmul_rn(__fsub_rn(1.0f, a0), a1);
+                    s = (k == 0) ? __fadd_rn(a0, tt) : __fadd_rn(__fadd_rn(s, a0), tt);
+                }
+                const float a = mix_rn(__fmul_rn(s, 0.25f), own.x, st.lerp);
+                atlas[wi] = make_float4(own.x, a, own.z, a);
+            } else {
+                float s[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const float4 a0 = v[c_pairs[f][k][0]], a1 = v[c_pairs[f][k][1]];
+                    const float tt = __fsub_rn(1.0f, a0.w);
+                    const float av[4] = {a0.x, a0.y, a0.z, a0.w}, bv[4] = {a1.x, a1.y, a1.z, a1.w};
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) {
+                        const float b = __fmul_rn(tt, bv[c]);
+                        s[c] = (k == 0) ? __fadd_rn(av[c], b) : __fadd_rn(__fadd_rn(s[c], av[c]), b);
+                    }
+                }
+                atlas[wi] = make_float4(mix_rn(__fmul_rn(s[0], 0.25f), own.x, st.lerp),
+                                        mix_rn(__fmul_rn(s[1], 0.25f), own.y, st.lerp),
+                                        mix_rn(__fmul_rn(s[2], 0.25f), own.z, st.lerp),
+                                        mix_rn(__fmul_rn(s[3], 0.25f), own.w, st.lerp));
+            }
+        }
+    }
+}
+
+// The adjoint of k_downsample_f32 for one level: G holds dL/d(atlas after
+// the pass) and leaves with dL/d(atlas before it).  A written texel's
+// gradient becomes its share through the blend (lerp; opacity: only x and
+// the blended alpha's lerp share, y and w are overwritten); its child block
+// gains the composite's shares: d/d a0 = 1 per channel and -sum_c g_c a1_c
+// on a0's alpha, d/d a1 = (1 - a0.w) (opacity: 1 - a1 and 1 - a0 on the
+// alphas).  Each (voxel, face) owns its written texel and its child block,
+// so no two threads touch the same gradient.  `atlas` holds the forward's
+// final values (a level's children are final before the level is mipped).
+template <int MODE>
+__global__ void k_downsample_backward(const float4* __restrict__ atlas, float4* __restrict__ G, AtlasDims A, int3 pmin,
+                                      int level, int band, int lgh) {
+    const uint32_t n = 1u << (3 * lgh);
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const DsSite st = ds_site(A, pmin, level, band, lgh, t);
+        for (int f = 0; f < 6; ++f) {
+            float4 v[8], gc[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                v[i] = atlas[ds_child(A, st, f, i)];
+                gc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+            const int64_t wi = A.index(st.wpos[0] + A.rb * f, st.wpos[1], st.wpos[2]);
+            const float4 go = G[wi];
+            if (MODE == 0) {
+                const float ga = go.y + go.w;
+                G[wi] = make_float4(go.x + ga * st.lerp, 0.0f, go.z, 0.0f);
+                const float gs = ga * (1.0f - st.lerp) * 0.25f;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const int i0 = c_pairs[f][k][0], i1 = c_pairs[f][k][1];
+                    gc[i0].w += gs * (1.0f - v[i1].w);
+                    gc[i1].w += gs * (1.0f - v[i0].w);
+                }
+            } else {
+                G[wi] = make_float4(go.x * st.lerp, go.y * st.lerp, go.z * st.lerp, go.w * st.lerp);
+                const float w = (1.0f - st.lerp) * 0.25f;
+                const float4 gs = make_float4(go.x * w, go.y * w, go.z * w, go.w * w);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const int i0 = c_pairs[f][k][0], i1 = c_pairs[f][k][1];
+                    const float tt = 1.0f - v[i0].w;
+                    gc[i0].x += gs.x;
+                    gc[i0].y += gs.y;
+                    gc[i0].z += gs.z;
+                    gc[i0].w += gs.w - (gs.x * v[i1].x + gs.y * v[i1].y + gs.z * v[i1].z + gs.w * v[i1].w);
+                    gc[i1].x += gs.x * tt;
+                    gc[i1].y += gs.y * tt;
+                    gc[i1].z += gs.z * tt;
+                    gc[i1].w += gs.w * tt;
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const int64_t ci = ds_child(A, st, f, i);
+                float4 g = G[ci];
+                G[ci] = make_float4(g.x + gc[i].x, g.y + gc[i].y, g.z + gc[i].z, g.w + gc[i].w);
+            }
+        }
+    }
+}
+
+static int check_ds_desc(const vct_downsample_desc* d, int32_t mode, const char* who) {
+    VCT_CHECK_ARG(d, who);
+    VCT_CHECK_ARG(valid_resolution(d->clipmap_resolution), "downsample: resolution must be a power of two in [8,1024]");
+    VCT_CHECK_ARG(d->clip_level >= 1 && d->clip_level < VCT_CLIP_LEVEL_COUNT, "downsample: clip level must be 1..5");
+    VCT_CHECK_ARG(mode == VCT_DOWNSAMPLE_OPACITY || mode == VCT_DOWNSAMPLE_RADIANCE, "downsample: bad mode");
+    VCT_CHECK_ARG(d->downsample_region_size >= 0 && d->downsample_region_size <= 4096, "downsample: band out of range");
+    return VCT_OK;
+}
+
+extern "C" int vct_downsample_f32(float* atlas4, const vct_downsample_desc* d, int32_t mode, void* stream) {
+    VCT_CHECK_ARG(atlas4 && ((uintptr_t)atlas4 & 15) == 0, "vct_downsample_f32: null or unaligned atlas");
+    int rc = check_ds_desc(d, mode, "vct_downsample_f32: null desc");
+    if (rc != VCT_OK) return rc;
+    AtlasDims A(d->clipmap_resolution);
+    const int half = A.R >> 1;
+    const int64_t n = (int64_t)half * half * half;
+    const int3 pm = make_int3(d->prev_region_min_corner[0], d->prev_region_min_corner[1], d->prev_region_min_corner[2]);
+    const int lgh = 31 - __builtin_clz((unsigned)half);
+    float4* a = reinterpret_cast<float4*>(atlas4);
+    if (mode == VCT_DOWNSAMPLE_OPACITY)
+        k_downsample_f32<0><<<grid_for(n, 128), 128, 0, as_stream(stream)>>>(a, A, pm, d->clip_level, d->downsample_region_size, lgh);
+    else
+        k_downsample_f32<1><<<grid_for(n, 128), 128, 0, as_stream(stream)>>>(a, A, pm, d->clip_level, d->downsample_region_size, lgh);
+    VCT_LAUNCH_CHECK();
+    return VCT_OK;
+}
+
+extern "C" int vct_downsample_backward(const float* atlas4, float* grad4, const vct_downsample_desc* d, int32_t mode,
+                                       void* stream) {
+    VCT_CHECK_ARG(atlas4 && grad4 && (((uintptr_t)atlas4 | (uintptr_t)grad4) & 15) == 0 && atlas4 != grad4,
+                  "vct_downsample_backward: null, unaligned or aliased atlases");
+    int rc = check_ds_desc(d, mode, "vct_downsample_backward: null desc");
+    if (rc != VCT_OK) return rc;
+    AtlasDims A(d->clipmap_resolution);
+    const int half = A.R >> 1;
+    const int64_t n = (int64_t)half * half * half;
+    const int3 pm = make_int3(d->prev_region_min_corner[0], d->prev_region_min_corner[1], d->prev_region_min_corner[2]);
+    const int lgh = 31 - __builtin_clz((unsigned)half);
+    const float4* a = reinterpret_cast<const float4*>(atlas4);
+    float4* g = reinterpret_cast<float4*>(grad4);
+    if (mode == VCT_DOWNSAMPLE_OPACITY)
+        k_downsample_backward<0><<<grid_for(n, 128), 128, 0, as_stream(stream)>>>(a, g, A, pm, d->clip_level, d->downsample_region_size, lgh);
+    else
+        k_downsample_backward<1><<<grid_for(n, 128), 128, 0, as_stream(stream)>>>(a, g, A, pm, d->clip_level, d->downsample_region_size, lgh);
+    VCT_LAUNCH_CHECK();
+    return VCT_OK;
+}
+
 extern "C" int vct_downsample(uint32_t* atlas, const vct_downsample_desc* d, int32_t mode, void* stream) {
     VCT_CHECK_ARG(atlas && d, "vct_downsample: null argument");
     VCT_CHECK_ARG(valid_resolution(d->clipmap_resolution), "vct_downsample: resolution must be a power of two in [8,1024]");
