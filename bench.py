@@ -393,6 +393,7 @@ def run_ours(args, world, rank, local):
     filter_bytes = GW * GH * 48  # diffuse + specular texel read, output written (RGBA32F)
 
     batch = batched_scenes(dev) if not args.no_batch and world == 1 else None
+    diff = differentiable_volume(dev) if not args.no_batch and world == 1 else None
 
     # end to end: host G-buffer -> device, frame, trace, outputs -> host
     h_samples = samples.cpu().pin_memory()
@@ -464,6 +465,7 @@ def run_ours(args, world, rank, local):
                        "svo_fragments": int(frags.shape[0]), "svo_nodes": int(nodes.value),
                        "voxelize_svo_mip_ms": frame_ms + svo_ms,
                        "batched_scenes": batch,
+                       "differentiable": diff,
                        "moving_camera_frame_ms": walk_ms,
                        "moving_camera": "32 frames (the whole radiance cadence) along a path of 0.06 per frame; "
                                         "mean frame time, full revoxelisation vs the toroidal update",
@@ -560,6 +562,71 @@ def batched_scenes(dev, streams: int = 4, n_scenes: int = 64, seed: int = 4):
                     "samples; host wall clock, the submission synchronises"}
 
 
+def differentiable_volume(dev, R: int = 128, views: int = 16, res: int = 512, seed: int = 5):
+    """Configuration 5: a hidden float RGBA clipmap (R = 128, smooth noise, alpha <= 0.3) seen through
+    `views` x res^2 G-buffer samples: one forward trace of the float atlas (vct_cone_trace_f32), its adjoint
+    (vct_cone_trace_backward, dL/d atlas for a unit upstream gradient on every output), and the five-level
+    float mip chain with its adjoint.  CUDA events on the stream; the adjoint synchronises."""
+    import ctypes as C
+    import torch
+    from vk_voxel_cone_tracing_gb300 import capi, clipmap
+    from vk_voxel_cone_tracing_gb300.scene import default_trace_desc, random_samples, smooth_volume
+    regs = clipmap.clip_regions((0.0, 0.0, 0.0), R)
+    regions = clipmap.regions_to_numpy(regs)
+    vol = smooth_volume(R, seed=seed, xp=torch, device=dev).reshape(-1)
+    n = views * res * res
+    smp = clipmap.samples_to_device(random_samples(n, (0.0, 0.0, 0.0), 6.0, seed=seed, specular_fraction=0.5), dev)
+    desc = clipmap.trace_desc(**default_trace_desc(regions, R))
+    cam = clipmap.cam_matrix((0.0, 2.0, -9.0))
+    light = capi.DirectionalLightDesc(capi.f3(*LIGHT_DIR), 1.0, capi.f3(1, 1, 1), 0)
+    dout = torch.empty((n, 4), dtype=torch.float32, device=dev)
+    sout = torch.empty_like(dout)
+    gd = torch.ones_like(dout)
+    gs = torch.ones_like(dout)
+    G = torch.zeros_like(vol)
+    steps = torch.zeros(1, dtype=torch.int64, device=dev)
+    st = torch.cuda.current_stream()
+    p = lambda t: C.c_void_p(t.data_ptr())
+
+    def fwd(counter=None):
+        capi.call("vct_cone_trace_f32", capi.ref(desc), capi.ref(cam), p(vol), R, None, capi.ref(light), None, p(smp), n,
+                  p(dout), p(sout), p(counter) if counter is not None else None, C.c_void_p(st.cuda_stream))
+
+    def bwd():
+        capi.call("vct_cone_trace_backward", capi.ref(desc), capi.ref(cam), p(vol), R, None, capi.ref(light), None,
+                  p(smp), n, p(gd), p(gs), p(G), C.c_void_p(st.cuda_stream))
+
+    fwd(steps)
+    torch.cuda.synchronize()
+    cone_samples = int(steps.item())
+    fwd_ms = statistics.median(events_ms(st, fwd, 3)[0])
+    bwd()
+    bwd_ms = statistics.median(events_ms(st, bwd, 2)[0])
+
+    def ds_desc(level):
+        d = capi.DownSampleDesc()
+        d.prev_region_min_corner = capi.i3(*[int(x) for x in regions[level - 1, 0:3]])
+        d.clip_level, d.clipmap_resolution, d.downsample_region_size = level, R, capi.DOWNSAMPLE_REGION_SIZE
+        return d
+
+    def mips():
+        for level in range(1, 6):
+            capi.call("vct_downsample_f32", p(vol), capi.ref(ds_desc(level)), 1, C.c_void_p(st.cuda_stream))
+
+    def mips_bwd():
+        for level in range(5, 0, -1):
+            capi.call("vct_downsample_backward", p(vol), p(G), capi.ref(ds_desc(level)), 1, C.c_void_p(st.cuda_stream))
+
+    mips()
+    mips_ms = statistics.median(events_ms(st, mips, 3)[0])
+    mips_bwd_ms = statistics.median(events_ms(st, mips_bwd, 3)[0])
+    return {"R": R, "views": views, "resolution": res, "samples": n, "cone_samples": cone_samples,
+            "forward_ms": fwd_ms, "backward_ms": bwd_ms, "forward_cone_samples_per_s": cone_samples / (fwd_ms * 1e-3),
+            "mips_ms": mips_ms, "mips_backward_ms": mips_bwd_ms,
+            "note": "float RGBA atlas (16 B per texel, 1.27 GB at R = 128), software trilinear; the adjoint "
+                    "recomputes each cone from 32-step checkpoints and scatters float4 atomics"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -571,7 +638,8 @@ def main():
     ap.add_argument("--R", type=int, default=R_DEFAULT)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--no-batch", action="store_true", help="skip the batched multi-scene measurement")
+    ap.add_argument("--no-batch", action="store_true",
+                    help="skip the batched multi-scene and the differentiable-form measurements")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":

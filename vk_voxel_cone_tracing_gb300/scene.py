@@ -299,23 +299,32 @@ def atlas_shape(R: int) -> tuple[int, int, int]:
     return (R + 2, (R + 2) * 6, (R + 2) * 6)
 
 
-def smooth_volume(R: int, seed: int = 5, max_alpha: float = 0.3, waves: int = 6) -> np.ndarray:
-    """A float RGBA atlas (reference layout, (D, H, W, 4) float32) of smooth noise: each channel a sum of
-    random low-frequency waves over the texel grid, rgb in [0, 1], alpha in [0, max_alpha] (the
-    differentiable form's test volume; below 1 alpha never saturates the march)."""
+def smooth_volume(R: int, seed: int = 5, max_alpha: float = 0.3, waves: int = 6, xp=np, device=None):
+    """A float RGBA atlas (reference layout, (D, H, W, 4) float32) of smooth noise: each channel the mean
+    of `waves` separable products sin(kx x + a) sin(ky y + b) sin(kz z + c) over the texel grid mapped to
+    rgb in [0, 1] and alpha in [0, max_alpha] (the differentiable form's volume; alpha below 1 never
+    saturates the march).  `xp` = numpy, or torch with `device` to build it on the GPU."""
     rng = np.random.default_rng(seed)
     D, H, W = atlas_shape(R)
-    z, y, x = np.meshgrid(np.arange(D, dtype=np.float32), np.arange(H, dtype=np.float32),
-                          np.arange(W, dtype=np.float32), indexing="ij")
-    out = np.empty((D, H, W, 4), np.float32)
+
+    def axis(n):
+        return xp.arange(n, dtype=xp.float32) if device is None else xp.arange(n, dtype=xp.float32, device=device)
+
+    x, y, z = axis(W), axis(H), axis(D)
+    if device is None:
+        out = np.empty((D, H, W, 4), np.float32)
+    else:
+        out = xp.empty((D, H, W, 4), dtype=xp.float32, device=device)
     for c in range(4):
-        acc = np.zeros((D, H, W), np.float32)
+        acc = None
         for _ in range(waves):
-            k = rng.uniform(0.02, 0.12, 3).astype(np.float32) * 2 * np.pi
-            ph = np.float32(rng.uniform(0, 2 * np.pi))
-            acc += np.sin(k[0] * x + k[1] * y + k[2] * z + ph).astype(np.float32)
-        v = 0.5 + 0.5 * acc / waves
-        out[..., c] = v * (max_alpha if c == 3 else 1.0)
+            k = rng.uniform(0.02, 0.12, 3) * 2 * np.pi
+            ph = rng.uniform(0, 2 * np.pi, 3)
+            term = (xp.sin(z * float(k[2]) + float(ph[2]))[:, None, None] *
+                    xp.sin(y * float(k[1]) + float(ph[1]))[None, :, None] *
+                    xp.sin(x * float(k[0]) + float(ph[0]))[None, None, :])
+            acc = term if acc is None else acc + term
+        out[..., c] = (acc / waves * 0.5 + 0.5) * (max_alpha if c == 3 else 1.0)
     return out
 
 
