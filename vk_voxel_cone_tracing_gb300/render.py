@@ -83,6 +83,7 @@ class Renderer:
         self.scratch = clipmap.fast_scratch(n, device)
         self.clear = torch.tensor([0.0, 0.0, 0.0, 1.0], dtype=torch.float32, device=device)
         self.regions = None
+        self.regions_state = (capi.ClipmapRegion * 6)()  # persists between frames (toroidal mode)
         self.camera = None
 
     def light_shadow(self, center) -> capi.DirectionalLightShadowDesc:
@@ -92,11 +93,13 @@ class Renderer:
         return passes.light_shadow_desc(tuple(origin.tolist()), self.light_dir)
 
     def render(self, position, direction, up=(0.0, 1.0, 0.0), frame_index: int = 0,
-               desc: capi.SpecularFilterDesc | None = None) -> torch.Tensor:
-        """One frame from camera `position` looking along `direction`; returns the RGBA32F output image."""
+               desc: capi.SpecularFilterDesc | None = None, revoxelization: int = capi.REVOX_FULL) -> torch.Tensor:
+        """One frame from camera `position` looking along `direction`; returns the RGBA32F output image.
+        `revoxelization` VCT_REVOX_TOROIDAL updates the opacity atlas from the previous frame's regions."""
         lsd = self.light_shadow(position)
         self.regions = passes.clipmap_frame(self.ds, position, self.R, self.opacity, self.radiance, self.shadow,
-                                            self.light, lsd, self.ws, frame_index=frame_index, texture=self.tex)
+                                            self.light, lsd, self.ws, frame_index=frame_index, texture=self.tex,
+                                            revoxelization=revoxelization, regions_state=self.regions_state)
         self.camera = passes.camera_matrix(position, direction, up, self.fovy, self.width / self.height)
         passes.gbuffer(self.ds, self.camera, self.width, self.height, self.ws, out=self.samples)
         # the cone-tracing pass's attachments clear to (0, 0, 0, 1); the trace leaves sky pixels untouched
@@ -112,3 +115,47 @@ class Renderer:
     def close(self) -> None:
         self.tex.close()
         self.ws.close()
+
+
+def main(argv=None) -> None:
+    """Render frames of a scene to PPM images: python -m vk_voxel_cone_tracing_gb300.render --out frame.ppm"""
+    import argparse
+    import time
+
+    from .scene import hall_scene, room_scene
+    ap = argparse.ArgumentParser(description=main.__doc__)
+    ap.add_argument("--scene", default="hall", help="hall, room, or a .gltf / .glb path")
+    ap.add_argument("--R", type=int, default=256)
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
+    ap.add_argument("--frames", type=int, default=1, help="frames along a short camera path")
+    ap.add_argument("--toroidal", action="store_true", help="toroidal revoxelisation after the first frame")
+    ap.add_argument("--position", type=float, nargs=3, default=(0.0, 5.0, 0.0))
+    ap.add_argument("--direction", type=float, nargs=3, default=(0.6, -0.2, 0.77))
+    ap.add_argument("--out", default="frame.ppm", help="image of the last frame (binary PPM)")
+    a = ap.parse_args(argv)
+    if a.scene == "hall":
+        sc = hall_scene()
+    elif a.scene == "room":
+        sc = room_scene()
+    else:
+        from .gltf import load_gltf
+        sc = load_gltf(a.scene).scene
+    r = Renderer(sc, R=a.R, width=a.width, height=a.height)
+    from . import capi
+    times = []
+    for k in range(a.frames):
+        pos = (a.position[0] + 0.05 * k, a.position[1], a.position[2] + 0.03 * k)
+        t0 = time.perf_counter()
+        r.render(pos, a.direction, frame_index=k,
+                 revoxelization=capi.REVOX_TOROIDAL if (a.toroidal and k > 0) else capi.REVOX_FULL)
+        torch.cuda.synchronize()
+        times.append((time.perf_counter() - t0) * 1e3)
+    write_ppm(a.out, r.image.cpu().numpy())
+    print(f"{sc.triangle_count} triangles, R={a.R}, {a.width}x{a.height}: frame ms " +
+          " ".join(f"{t:.2f}" for t in times) + f" -> {a.out}")
+    r.close()
+
+
+if __name__ == "__main__":
+    main()
