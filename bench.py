@@ -241,8 +241,9 @@ def run_ours(args, world, rank, local):
         if args.form in ("tex", "fp16") else None
     frame_tex = tex if args.form == "tex" else None
 
-    def frame():
-        return passes.clipmap_frame(ds, CAMERA, R, opacity, radiance, shadow, light, lsd, ws, texture=frame_tex)
+    def frame(frame_index: int = 0):
+        return passes.clipmap_frame(ds, CAMERA, R, opacity, radiance, shadow, light, lsd, ws, texture=frame_tex,
+                                    frame_index=frame_index)
 
     regs = frame()
     torch.cuda.synchronize()
@@ -404,14 +405,19 @@ def run_ours(args, world, rank, local):
     copy_stream = torch.cuda.Stream(device=dev)
     uploaded = torch.cuda.Event()
 
+    frame_counter = [0]
+
     def e2e_step():
-        # the G-buffer upload overlaps the frame (which does not read it); it waits for the previous
-        # step's work so d_in is not overwritten under a running trace, and the trace waits for it
+        # one frame of the reference's loop: full opacity revoxelisation, radiance level l refreshed every
+        # 2^l frames (the frame index advances per step), then the trace.  The G-buffer upload overlaps
+        # the frame (which does not read it); it waits for the previous step's work so d_in is not
+        # overwritten under a running trace, and the trace waits for it
         copy_stream.wait_stream(stream)
         with torch.cuda.stream(copy_stream):
             d_in.copy_(h_samples, non_blocking=True)
             uploaded.record(copy_stream)
-        frame()
+        frame(frame_counter[0])
+        frame_counter[0] += 1
         stream.wait_event(uploaded)
         trace(d_in)
         h_d.copy_(dout, non_blocking=True)
@@ -494,8 +500,11 @@ def run_ours(args, world, rank, local):
             "e2e": {"value": cone_samples * world / (e2e_ms * 1e-3), "unit": "cone samples/s",
                     "h2d_bytes_per_step": int(samples.numel() * 4),
                     "d2h_bytes_per_step": int((dout.numel() + sout.numel()) * 4),
-                    "step": "G-buffer upload (overlapping the frame) + voxelise/shadow/inject/mips + trace + "
-                            "output readback"},
+                    "step": "G-buffer upload (overlapping the frame) + one frame of the reference's loop "
+                            "(full opacity revoxelisation, shadow, radiance levels due at the frame index: level "
+                            "l every 2^l frames) + trace + output readback",
+                    "frames": f"frame indices {args.warmup}..{args.warmup + args.steps - 1} timed after "
+                              f"{args.warmup} warm-up frames"},
             "gpu_launches": args.steps * launches,
             "clocks": clocks.summary(),
         }
