@@ -77,3 +77,42 @@ def test_bad_arguments_rejected_without_gpu(vct_lib):
     # an empty trace is a no-op, not an error
     assert vct_lib.vct_cone_trace(None, None, C.c_void_p(16), 128, None, None, None, None, 0, None, None, None,
                                   None) == capi.VCT_OK
+
+
+def test_new_entry_points_reject_bad_arguments(vct_lib):
+    """The entry points of the G-buffer, filter, toroidal, instance, batch and gradient paths validate their
+    arguments on the host before any device work (these calls need no GPU)."""
+    P = C.c_void_p
+    bad = [
+        ("vct_gbuffer", (None, None, 16, 16, None, None, None)),
+        ("vct_specular_filter", (None, None, None, 16, 16, None, None)),
+        ("vct_present_srgb8", (P(16), 0, 16, P(16), None)),
+        ("vct_cone_trace_f32", (None, None, P(16), 48, None, None, None, None, 0, None, None, None, None)),
+        ("vct_cone_trace_backward", (None, None, P(16), 48, None, None, None, None, 0, None, None, P(16), None)),
+        ("vct_downsample_f32", (P(16), None, 1, None)),
+        ("vct_downsample_backward", (P(16), P(16), None, 1, None)),
+        ("vct_batch_submit", (None, 1, 4)),
+        ("vct_atlas_alloc", (48, capi.TEX_RGBA8, C.byref(C.c_void_p()))),
+        ("vct_create", (None, C.byref(C.c_void_p()))),
+        ("vct_context_frame", (None, None, None, None, None, 0, None)),
+        ("vct_voxelize_opacity_slabs", (None, None, 32, None, None, None, 0, None, None)),
+        ("vct_update_clip_regions", (None, None, 32, 16, None, None, None)),
+    ]
+    for name, args in bad:
+        with pytest.raises(capi.VctError):
+            capi.call(name, *args)
+    # the batch's stream count is checked first
+    with pytest.raises(capi.VctError, match="streams"):
+        capi.call("vct_batch_submit", None, 0, 0)
+    # a direction parallel to up has no camera frame
+    out = capi.CamMatrix()
+    v = lambda *x: C.cast((C.c_float * 3)(*x), C.c_void_p)
+    with pytest.raises(capi.VctError, match="parallel"):
+        capi.call("vct_camera_matrix", v(0, 0, 0), v(0, 2, 0), v(0, 1, 0), 60.0, 1.0, capi.ref(out))
+
+
+def test_png_unfilter_rejects_an_unknown_filter(vct_lib):
+    raw = np.array([7, 1, 2, 3], np.uint8)  # filter type 7
+    out = np.zeros(3, np.uint8)
+    with pytest.raises(capi.VctError, match="filter"):
+        capi.call("vct_png_unfilter", raw.ctypes.data_as(C.c_void_p), 3, 1, 1, out.ctypes.data_as(C.c_void_p))

@@ -1622,6 +1622,9 @@ extern "C" int vct_camera_matrix(const float position[3], const float direction[
                                  float fovy_degrees, float aspect, vct_cam_matrix* out) {
     VCT_CHECK_ARG(position && direction && up && out, "vct_camera_matrix: null argument");
     VCT_CHECK_ARG(aspect > 0.0f && fovy_degrees > 0.0f && fovy_degrees < 180.0f, "vct_camera_matrix: bad fovy or aspect");
+    const float dd = direction[0] * direction[0] + direction[1] * direction[1] + direction[2] * direction[2];
+    const float3 side = cross3h(make_float3(up[0], up[1], up[2]), make_float3(direction[0], direction[1], direction[2]));
+    VCT_CHECK_ARG(dd > 0.0f && dot3h(side, side) > 0.0f, "vct_camera_matrix: zero direction or direction parallel to up");
     const float3 eye = make_float3(position[0], position[1], position[2]);
     const M4 view = look_at_lh(eye, make_float3(eye.x + direction[0], eye.y + direction[1], eye.z + direction[2]),
                                make_float3(up[0], up[1], up[2]));

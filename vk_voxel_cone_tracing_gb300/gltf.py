@@ -320,6 +320,8 @@ def load_gltf(path) -> Gltf:
         for prim in mesh.get("primitives", []):
             if prim.get("mode", 4) != 4:
                 continue
+            if "KHR_draco_mesh_compression" in prim.get("extensions", {}):
+                raise ValueError(f"{path}: Draco-compressed meshes are not supported")
             pos = d.accessor(prim["attributes"]["POSITION"]).astype(np.float32)
             if "indices" in prim:
                 idx = d.accessor(prim["indices"]).reshape(-1).astype(np.uint32)
