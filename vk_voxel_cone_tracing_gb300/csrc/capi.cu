@@ -17,6 +17,10 @@ int fail(int code, const std::string& msg) {
 }
 int cuda_fail(cudaError_t e, const char* what) {
     g_last_error = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+    // a failed call that leaves the context usable (an allocation the device cannot satisfy, a bad
+    // argument) also sets the runtime's last-error state: clear it so that the next launch check does
+    // not report it again; a sticky error stays and is reported by every later call
+    cudaGetLastError();
     return VCT_E_CUDA;
 }
 

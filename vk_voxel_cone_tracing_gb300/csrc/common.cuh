@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
 #include <string>
@@ -72,6 +73,15 @@ int cuda_fail(cudaError_t e, const char* what);
 #define VCT_LAUNCH_CHECK() VCT_CUDA_TRY(cudaGetLastError())
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// An NVTX range over a pass's host-side submission (visible to profilers that
+// attach an NVTX tool; a few nanoseconds otherwise).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // ------------------------------------------------------------- geometry
 // The reference atlas: width (R+2)*6, height (R+2)*6, depth R+2.

@@ -200,6 +200,7 @@ extern "C" int vct_specular_filter_stencil(float out_host[9]) {
 extern "C" int vct_specular_filter(const vct_specular_filter_desc* desc, const float* diffuse_rgba,
                                    const float* specular_rgba, int32_t width, int32_t height, float* out_rgba,
                                    void* stream) {
+    vct::NvtxRange nvtx_range("vct_specular_filter");
     VCT_CHECK_ARG(desc && diffuse_rgba && specular_rgba && out_rgba, "vct_specular_filter: null argument");
     VCT_CHECK_ARG(width > 0 && height > 0 && width <= 32768 && height <= 32768, "vct_specular_filter: bad image size");
     VCT_CHECK_ARG(out_rgba != specular_rgba, "vct_specular_filter: the output must not alias the specular image");

@@ -193,6 +193,7 @@ extern "C" int vct_context_trace(vct_context_s* c, const vct_cone_tracing_desc* 
 }
 
 extern "C" int vct_batch_submit(const vct_batch_job* jobs, int32_t job_count, int32_t streams) {
+    vct::NvtxRange nvtx_range("vct_batch_submit");
     VCT_CHECK_ARG(job_count >= 0 && (job_count == 0 || jobs), "vct_batch_submit: bad job list");
     VCT_CHECK_ARG(streams >= 1 && streams <= 64, "vct_batch_submit: streams must be 1..64");
     for (int i = 0; i < job_count; ++i)

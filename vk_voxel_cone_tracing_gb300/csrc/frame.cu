@@ -18,6 +18,7 @@
 extern "C" int vct_clipmap_frame(const vct_scene* scene, const vct_frame_desc* f, uint32_t* opacity,
                                  uint32_t* radiance, float* shadow_depth, vct_clipmap_region regions_out[6],
                                  vct_workspace_s* ws, void* stream) {
+    vct::NvtxRange range("vct_clipmap_frame");
     VCT_CHECK_ARG(scene && f && opacity && radiance && ws, "vct_clipmap_frame: null argument");
     VCT_CHECK_ARG(!f->shadow_width || shadow_depth, "vct_clipmap_frame: shadow map size given without a buffer");
     VCT_CHECK_ARG(f->inject_mode == VCT_INJECT_DETERMINISTIC || f->inject_mode == VCT_INJECT_ATOMIC,

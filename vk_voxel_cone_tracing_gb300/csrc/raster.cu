@@ -1773,6 +1773,7 @@ extern "C" int vct_voxelize_opacity_slabs(const vct_scene* scene, const vct_clip
 
 extern "C" int vct_voxelize_opacity(const vct_scene* scene, const vct_clipmap_region regions[6], int32_t R,
                                     uint32_t* atlas, uint32_t level_mask, vct_workspace_s* ws, void* stream) {
+    vct::NvtxRange nvtx_range("vct_voxelize_opacity");
     int rc = check_scene(scene);
     if (rc != VCT_OK) return rc;
     VCT_CHECK_ARG(regions && atlas && ws && valid_resolution(R), "vct_voxelize_opacity: bad argument");
@@ -1799,6 +1800,7 @@ extern "C" int vct_voxelize_opacity(const vct_scene* scene, const vct_clipmap_re
 
 extern "C" int vct_shadow_depth(const vct_scene* scene, const vct_directional_light_shadow_desc* sd, float* depth,
                                 int32_t W, int32_t H, vct_workspace_s* ws, void* stream) {
+    vct::NvtxRange nvtx_range("vct_shadow_depth");
     int rc = check_scene(scene);
     if (rc != VCT_OK) return rc;
     VCT_CHECK_ARG(sd && depth && ws && W > 0 && H > 0 && W <= 32768 && H <= 32768, "vct_shadow_depth: bad argument");
@@ -1832,6 +1834,7 @@ extern "C" int vct_inject_radiance(const vct_scene* scene, const vct_clipmap_reg
                                    const vct_shadow_map* shadow, const vct_directional_light_desc* light,
                                    const vct_directional_light_shadow_desc* light_shadow, uint32_t* atlas,
                                    uint32_t level_mask, int32_t mode, vct_workspace_s* ws, void* stream) {
+    vct::NvtxRange nvtx_range("vct_inject_radiance");
     int rc = check_scene(scene);
     if (rc != VCT_OK) return rc;
     VCT_CHECK_ARG(regions && atlas && ws && valid_resolution(R), "vct_inject_radiance: bad argument");
@@ -1883,6 +1886,7 @@ extern "C" int vct_inject_radiance(const vct_scene* scene, const vct_clipmap_reg
 
 extern "C" int vct_gbuffer(const vct_scene* scene, const vct_cam_matrix* cam, int32_t width, int32_t height,
                            vct_surface_sample* out, vct_workspace_s* ws, void* stream) {
+    vct::NvtxRange nvtx_range("vct_gbuffer");
     int rc = check_scene(scene);
     if (rc != VCT_OK) return rc;
     VCT_CHECK_ARG(cam && out && ws, "vct_gbuffer: null argument");
@@ -2029,6 +2033,7 @@ extern "C" int vct_svo_fragments(const vct_scene* scene, int32_t octree_level, c
                                  const vct_directional_light_desc* light,
                                  const vct_directional_light_shadow_desc* light_shadow, uint32_t* frags,
                                  int64_t capacity, int64_t* count, vct_workspace_s* ws, void* stream) {
+    vct::NvtxRange nvtx_range("vct_svo_fragments");
     int rc = check_scene(scene);
     if (rc != VCT_OK) return rc;
     VCT_CHECK_ARG(count && bb_min && bb_max && ws, "vct_svo_fragments: null argument");

@@ -263,6 +263,7 @@ extern "C" int64_t vct_svo_pool_capacity(int64_t F) {
 
 extern "C" int vct_svo_build(const uint32_t* fragments, int64_t F, int32_t L, uint32_t* pool_u32, int64_t capacity,
                              int32_t mode, int64_t* node_count, vct_workspace_s* ws, void* stream) {
+    vct::NvtxRange nvtx_range("vct_svo_build");
     VCT_CHECK_ARG(node_count && ws, "vct_svo_build: null argument");
     VCT_CHECK_ARG(L >= 1 && L <= 11, "vct_svo_build: octree level must be 1..11");
     VCT_CHECK_ARG(F >= 0 && F < (1LL << 31), "vct_svo_build: fragment count out of range");

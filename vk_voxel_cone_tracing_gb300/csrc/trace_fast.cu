@@ -637,6 +637,7 @@ extern "C" int vct_cone_trace_fast(const vct_cone_tracing_desc* desc, const vct_
                                    const vct_surface_sample* samples, int64_t n, float* dout, float* sout,
                                    unsigned long long* cone_steps, void* scratch, size_t scratch_bytes,
                                    void* stream) {
+    vct::NvtxRange nvtx_range("vct_cone_trace_fast");
     VCT_CHECK_ARG(radiance, "vct_cone_trace_fast: null radiance texture");
     VCT_CHECK_ARG(n >= 0 && n <= 0x7fffffffLL, "vct_cone_trace_fast: sample count out of range");
     if (n == 0) return VCT_OK;

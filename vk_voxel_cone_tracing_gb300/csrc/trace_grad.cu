@@ -281,6 +281,7 @@ extern "C" int vct_cone_trace_backward(const vct_cone_tracing_desc* desc, const 
                                        const vct_directional_light_shadow_desc* light_shadow,
                                        const vct_surface_sample* samples, int64_t n, const float* grad_diffuse,
                                        const float* grad_specular, float* grad_atlas4, void* stream) {
+    vct::NvtxRange nvtx_range("vct_cone_trace_backward");
     VCT_CHECK_ARG(atlas4 && grad_atlas4 && valid_resolution(R), "vct_cone_trace_backward: bad atlas / resolution");
     VCT_CHECK_ARG((((uintptr_t)atlas4 | (uintptr_t)grad_atlas4) & 15) == 0,
                   "vct_cone_trace_backward: atlases must be 16-byte aligned");

@@ -70,7 +70,8 @@ def world_positions(scene: Scene) -> np.ndarray:
     mat4 * vec4 order ((c0 x + c1 y) + (c2 z + c3 w)); the object positions without node matrices."""
     if scene.node_matrices is None:
         return np.asarray(scene.positions, np.float32)
-    idx = np.asarray(scene.indices, np.int64).reshape(-1)
+    # indices past the arrays read the last entry, as on the device
+    idx = np.minimum(np.asarray(scene.indices, np.int64).reshape(-1), scene.positions.shape[0] - 1)
     inst = np.minimum(np.repeat(np.asarray(scene.tri_instance, np.int64), 3), scene.node_matrices.shape[0] - 1)
     m = np.asarray(scene.node_matrices, np.float32)[inst, :16]
     p = np.asarray(scene.positions, np.float32)[idx]
