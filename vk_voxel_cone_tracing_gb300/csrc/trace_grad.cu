@@ -2,7 +2,7 @@
 // (vct_cone_trace_f32): given dL/d(diffuse out) and dL/d(specular out) per
 // sample, accumulate dL/d(texel) into a float RGBA atlas of the same layout.
 //
-// One thread per (sample, cone): the diffuse cones and the specular cone of
+// One thread per (cone, sample), cone-major: the diffuse cones and the specular cone of
 // voxelConeTracing.frag:143-293.  The march's step schedule, levels, tap
 // positions, opacity corrections and occlusion decay depend on geometry
 // only; the number of steps depends on the volume through the occlusion
@@ -211,8 +211,10 @@ __global__ void __launch_bounds__(128) k_cone_trace_backward(TraceParams P, F4At
     const uint32_t mode = d.rendering_mode;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * slots;
          t += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = t / slots;
-        const int slot = (int)(t - i * slots);
+        // cone-major: a warp's lanes march the same cone of consecutive samples (the same aperture and
+        // step schedule, so the lanes stay in step)
+        const int slot = (int)(t / n);
+        const int64_t i = t - (int64_t)slot * n;
         GSample g = load_sample(samples + i, P.eye);
         if (g.depth == 1.0f) continue;
         float min_level = calc_min_level(d, g.wp);
