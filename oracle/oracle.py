@@ -5,6 +5,14 @@ The oracle is a C++ restatement of the reference's shader arithmetic
 and bench.py's CPU-baseline leg import this module; the CUDA product path
 never does.  ``build()`` compiles the oracle with g++ (-ffp-contract=off so
 no multiply-add is fused, -fopenmp for the timed CPU baseline).
+
+Parity pinning: the host math (clip regions, the voxeliser / light / camera /
+glTF-node matrices with glm::inverse) is pinned bit for bit against the
+reference's vendored glm, and the cone tables and trace constants against its
+shader source (tests/golden).  The shader arithmetic itself is a restatement:
+its parity with the GLSL is unpinned, because the reference's passes need
+Vulkan, which is unavailable on this machine, and the reference ships no tests or
+fixtures.
 """
 from __future__ import annotations
 
