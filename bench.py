@@ -314,6 +314,17 @@ def run_ours(args, world, rank, local):
     svo_per, _ = events_ms(stream, svo, max(3, args.steps))
     frame_ms = statistics.median(frame_per)
     svo_ms = statistics.median(svo_per)
+    # the SVO cone trace (voxelConeTracing_Octree.frag) over the first 262144 samples of the octree just built,
+    # with the scene's bounding box (the reference's hard-coded Sponza box does not fit the hall scene)
+    svo_n = min(n, 262144)
+    svo_steps = torch.zeros(1, dtype=torch.int64, device=dev)
+    svo_trace = lambda counter=None: passes.svo_cone_trace(desc, EYE, pool, int(nodes.value), samples[:svo_n],
+                                                          bb_min=ds.bb_min, bb_max=ds.bb_max, light=light,
+                                                          shadow=shadow, shadow_desc=lsd, steps=counter)
+    svo_trace(svo_steps)
+    torch.cuda.synchronize()
+    svo_trace_ms = statistics.median(events_ms(stream, svo_trace, 3)[0])
+    svo_trace_rate = int(svo_steps.item()) / (svo_trace_ms * 1e-3)
 
     # a moving camera over the 32-frame radiance cadence (level l refreshed every 2^l frames): the mean
     # frame time with full revoxelisation every frame (the reference as shipped) and with the toroidal
@@ -469,6 +480,7 @@ def run_ours(args, world, rank, local):
                        else ("refreshed by a full copy every trace step" if tex is not None else "none (linear atlas)"),
                        "voxelize_inject_mip_ms": frame_ms, "svo_ms": svo_ms, "svo_level": SVO_LEVEL,
                        "svo_fragments": int(frags.shape[0]), "svo_nodes": int(nodes.value),
+                       "svo_trace": {"samples": svo_n, "ms": svo_trace_ms, "cone_samples_per_s": svo_trace_rate},
                        "voxelize_svo_mip_ms": frame_ms + svo_ms,
                        "batched_scenes": batch,
                        "differentiable": diff,
