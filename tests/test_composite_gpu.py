@@ -105,3 +105,13 @@ def test_renderer_frame(cuda, oracle):
     assert np.isfinite(want).all()
     assert img[..., :3].mean() > 5 and img[..., :3].std() > 2  # lit, with structure
     r.close()
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_random_sizes_gaussian_bit_exact(cuda, oracle, seed):
+    rng = np.random.default_rng(seed)
+    H, W = int(rng.integers(1, 90)), int(rng.integers(1, 130))
+    d, s = _img(rng, H, W, hdr=float(rng.uniform(0.5, 20))), _img(rng, H, W, hdr=float(rng.uniform(0.5, 20)))
+    got = _gpu_filter(cuda, d, s, method=1)
+    want = oracle.specular_filter(d, s, method=1)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))

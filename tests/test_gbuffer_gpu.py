@@ -110,3 +110,20 @@ def test_empty_and_bad_arguments(cuda, oracle, ws):
         passes.gbuffer(ds, cam, 0, 32, ws)
     with pytest.raises(ValueError):
         passes.gbuffer(ds, cam, 32, 32, ws, out=torch.empty((10, 20), device="cuda"))
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_random_cameras_bit_exact(cuda, oracle, ws, seed):
+    """Random cameras in and around the room (random field of view, aspect and odd image sizes): every
+    record equal to the oracle's."""
+    from vk_voxel_cone_tracing_gb300.scene import room_scene
+    rng = np.random.default_rng(100 + seed)
+    sc = room_scene(seed=seed % 3, n_random=1500)
+    W, H = int(rng.integers(40, 200)), int(rng.integers(30, 150))
+    pos = rng.uniform([-14, -3, -9], [14, 12, 9]).astype(np.float32)
+    d = rng.normal(size=3).astype(np.float32)
+    d[1] *= 0.4
+    cam = oracle.camera_matrix(tuple(pos.tolist()), tuple(d.tolist()), fovy_degrees=float(rng.uniform(30, 100)),
+                               aspect=float(W) / H)
+    want = oracle.gbuffer(sc, cam, W, H)
+    _compare(_run(cuda, sc, cam, W, H, ws), want)

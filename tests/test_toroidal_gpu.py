@@ -101,3 +101,31 @@ def test_toroidal_frames_bit_exact(cuda, oracle):
     # the toroidal mode without its region state is refused
     with pytest.raises(capi.VctError):
         passes.clipmap_frame(ds, PATH[0], R, op, rad, sh, light, lsd, ws, revoxelization=capi.REVOX_TOROIDAL)
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_random_walk_slabs_bit_exact(cuda, oracle, seed):
+    """A random camera walk (small steps, a few jumps past level extents) through the slab pass."""
+    torch = cuda
+    from vk_voxel_cone_tracing_gb300 import clipmap, passes
+    from vk_voxel_cone_tracing_gb300.scene import room_scene
+    R = 32
+    rng = np.random.default_rng(seed)
+    sc = room_scene(seed=seed, n_random=2000)
+    ds, ws = passes.DeviceScene(sc), passes.Workspace()
+    cam = np.float32([0.3, 2.0, -0.5])
+    regs = clipmap.clip_regions(tuple(cam.tolist()), R)
+    o_regs = oracle.clip_regions(cam, R).astype(np.int32).copy()
+    atlas = clipmap.new_atlas(R)
+    passes.voxelize_opacity(ds, regs, R, atlas, ws)
+    want = oracle.voxelize_opacity(sc, R, o_regs)
+    for k in range(8):
+        step = rng.normal(0, 0.8, 3) if k % 4 else rng.normal(0, 12.0, 3)
+        cam = (cam + step).astype(np.float32)
+        slabs, levels = passes.update_clip_regions(regs, cam.tolist(), R)
+        o_slabs, o_levels = oracle.update_clip_regions(o_regs, cam, R)
+        passes.voxelize_opacity_slabs(ds, regs, R, atlas, slabs, levels, ws)
+        oracle.voxelize_opacity_slabs(sc, R, o_regs, want, o_slabs, o_levels)
+    torch.cuda.synchronize()
+    got = atlas.cpu().numpy().view(np.uint32)
+    assert np.array_equal(got, want), f"{np.count_nonzero(got != want)} texels differ"
