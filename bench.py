@@ -123,6 +123,20 @@ def dist_setup():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
+def aggregate(units: float, ms: float, world: int, device="cpu") -> tuple[float, float]:
+    """The whole job's units (summed over the ranks) and the slowest rank's time (max over the ranks), over
+    the job's process group (NCCL on the GPUs; any backend works); one rank returns its own values."""
+    if world == 1:
+        return float(units), float(ms)
+    import torch
+    import torch.distributed as dist
+    u = torch.tensor([float(units)], dtype=torch.float64, device=device)
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(u.item()), float(t.item())
+
+
 def make_inputs(n_samples: int, sample_seed: int):
     from vk_voxel_cone_tracing_gb300.scene import hall_scene, surface_samples
     scene = hall_scene(seed=SCENE_SEED)
@@ -281,11 +295,9 @@ def run_ours(args, world, rank, local):
         dist.barrier()
     with Clocks(local) as clocks:
         per, total_ms = events_ms(stream, lambda: trace(samples), args.steps)
-    t = torch.tensor([total_ms], device=dev)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms = float(t.item()) / args.steps
-    value = cone_samples * world / (ms * 1e-3)
+    total_cone_samples, total_ms = aggregate(cone_samples, total_ms, world, dev)
+    ms = total_ms / args.steps
+    value = total_cone_samples / (ms * 1e-3)
     # the trace's speed of light: the same fetches per cone sample with nothing else (vct_gather_probe)
     gather_peak = clipmap.gather_probe(desc, tex) if tex is not None else None
     # what a full clipmap -> texture array copy (vct_texture_update) costs; the RGBA8 form needs none per step
@@ -437,10 +449,8 @@ def run_ours(args, world, rank, local):
     for _ in range(max(1, args.warmup)):
         e2e_step()
     _, e2e_total = events_ms(stream, e2e_step, args.steps)
-    te = torch.tensor([e2e_total / args.steps], device=dev)
-    if world > 1:
-        dist.all_reduce(te, op=dist.ReduceOp.MAX)
-    e2e_ms = float(te.item())
+    _, e2e_total = aggregate(cone_samples, e2e_total, world, dev)
+    e2e_ms = e2e_total / args.steps
 
     if rank == 0:
         peak, peak_kind = measured_peaks()
@@ -509,7 +519,7 @@ def run_ours(args, world, rank, local):
                         "texture; achieved = the whole trace step (Morton sort, specular partition, diffuse and "
                         "specular kernels)"},
             "cpu_baseline": cpu,
-            "e2e": {"value": cone_samples * world / (e2e_ms * 1e-3), "unit": "cone samples/s",
+            "e2e": {"value": total_cone_samples / (e2e_ms * 1e-3), "unit": "cone samples/s",
                     "h2d_bytes_per_step": int(samples.numel() * 4),
                     "d2h_bytes_per_step": int((dout.numel() + sout.numel()) * 4),
                     "step": "G-buffer upload (overlapping the frame) + one frame of the reference's loop "
