@@ -418,6 +418,7 @@ def run_ours(args, world, rank, local):
 
     batch = batched_scenes(dev) if not args.no_batch and world == 1 else None
     diff = differentiable_volume(dev) if not args.no_batch and world == 1 else None
+    svo_large = large_svo(dev, max(3, args.steps)) if not args.no_batch and world == 1 else None
 
     # end to end: host G-buffer -> device, frame, trace, outputs -> host
     h_samples = samples.cpu().pin_memory()
@@ -494,6 +495,7 @@ def run_ours(args, world, rank, local):
                        "voxelize_svo_mip_ms": frame_ms + svo_ms,
                        "batched_scenes": batch,
                        "differentiable": diff,
+                       "svo_large": svo_large,
                        "moving_camera_frame_ms": walk_ms,
                        "moving_camera": "32 frames (the whole radiance cadence) along a path of 0.06 per frame; "
                                         "mean frame time, full revoxelisation vs the toroidal update",
@@ -593,6 +595,80 @@ def batched_scenes(dev, streams: int = 4, n_scenes: int = 64, seed: int = 4):
                     "samples; host wall clock, the submission synchronises"}
 
 
+def large_svo(dev, reps: int, level: int = 9, n_samples: int = 4 << 20, seed: int = 3):
+    """Configuration 3: the sparse-voxel-octree chain at 512^3 (level 9) over the 4M-triangle terrain scene
+    (gradient-noise terrain + 10k boxes): the fragment list (vct_svo_fragments), the octree build
+    (vct_svo_build: subdivision, leaf fold, mips) and the octree cone trace (vct_svo_cone_trace) of
+    `n_samples` area-uniform surface samples with 16 diffuse cones + the specular cone.  CUDA events on the
+    stream, median of `reps`."""
+    import ctypes as C
+
+    import torch
+    from vk_voxel_cone_tracing_gb300 import capi, clipmap, passes
+    from vk_voxel_cone_tracing_gb300.scene import default_trace_desc, surface_samples, terrain_scene
+    stream = torch.cuda.current_stream()
+    sc = terrain_scene(seed=seed)
+    ds = passes.DeviceScene(sc, dev)
+    ws = passes.Workspace()
+    light = passes.light_desc(LIGHT_DIR)
+    d = np.asarray(LIGHT_DIR, np.float64)
+    d /= np.linalg.norm(d)
+    lsd = passes.light_shadow_desc(tuple((np.array([0.0, 1.5, 0.0]) - 15.0 * d).astype(np.float32).tolist()),
+                                   LIGHT_DIR)
+    shadow = torch.empty((SHADOW_RES, SHADOW_RES), dtype=torch.float32, device=dev)
+    passes.shadow_depth(ds, lsd, shadow, ws)
+    frags = passes.svo_fragments(ds, level, shadow, light, lsd, ws)
+    F = int(frags.shape[0])
+    buf = torch.empty((int(F * 1.25) + 1024, 2), dtype=torch.int32, device=dev)
+    pool_cap = passes.svo_pool_capacity(F)
+    pool = torch.empty((pool_cap, 2), dtype=torch.int32, device=dev)
+    nodes = C.c_int64(0)
+    del frags
+    holder = [None]
+
+    def fragments():
+        holder[0] = passes.svo_fragments(ds, level, shadow, light, lsd, ws, out=buf)
+
+    def build():
+        f = holder[0]
+        capi.call("vct_svo_build", f.data_ptr(), f.shape[0], level, pool.data_ptr(), pool_cap,
+                  capi.SVO_DETERMINISTIC, C.byref(nodes), ws.handle, C.c_void_p(stream.cuda_stream))
+
+    for _ in range(2):
+        fragments()
+        build()
+    frag_ms = statistics.median(events_ms(stream, fragments, reps)[0])
+    build_ms = statistics.median(events_ms(stream, build, reps)[0])
+    # octree trace: volume dimension 2^level over the scene's own box (the reference hard-codes Sponza's)
+    regions = clipmap.regions_to_numpy(clipmap.clip_regions((0.0, 3.0, 0.0), 1 << level))
+    kw = default_trace_desc(regions, 1 << level)
+    desc = clipmap.trace_desc(**kw)
+    samples = clipmap.samples_to_device(surface_samples(sc, n_samples, seed=seed), dev)
+    steps = torch.zeros(1, dtype=torch.int64, device=dev)
+    eye = (0.0, 6.0, -20.0)
+    bmin, bmax = tuple(ds.bb_min.tolist()), tuple(ds.bb_max.tolist())
+
+    def trace(counter=None):
+        passes.svo_cone_trace(desc, eye, pool, int(nodes.value), samples, bb_min=bmin, bb_max=bmax, light=light,
+                              shadow=shadow, shadow_desc=lsd, steps=counter)
+
+    trace(steps)
+    torch.cuda.synchronize()
+    cone_samples = int(steps.item())
+    trace_ms = statistics.median(events_ms(stream, trace, reps)[0])
+    # algorithmic bytes of the build: the fragment (8 B) + every node on its root-to-leaf path (8 B per
+    # level, summed over the L flag passes: 8 L (L + 1) / 2) + the leaf read-modify-write (8 B)
+    build_bytes = F * (8 + 8 * level * (level + 1) // 2 + 8)
+    return {"scene": f"terrain ({sc.triangle_count} fp32 triangles: gradient-noise heightfield + 10000 boxes)",
+            "level": level, "resolution": 1 << level, "fragments": F, "nodes": int(nodes.value),
+            "pool_capacity_nodes": pool_cap, "fragments_ms": frag_ms, "build_ms": build_ms,
+            "fragments_build_ms": frag_ms + build_ms,
+            "build_algorithmic_gbs": build_bytes / (build_ms * 1e-3) / 1e9,
+            "trace": {"samples": n_samples, "cone_samples": cone_samples, "ms": trace_ms,
+                      "cone_samples_per_s": cone_samples / (trace_ms * 1e-3)},
+            "note": "deterministic build (scan allocation, fragment-order leaf fold); CUDA events, median"}
+
+
 def differentiable_volume(dev, R: int = 128, views: int = 16, res: int = 512, seed: int = 5):
     """Configuration 5: a hidden float RGBA clipmap (R = 128, smooth noise, alpha <= 0.3) seen through
     `views` x res^2 G-buffer samples: one forward trace of the float atlas (vct_cone_trace_f32), its adjoint
@@ -670,7 +746,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true",
-                    help="skip the batched multi-scene and the differentiable-form measurements")
+                    help="skip the batched multi-scene, differentiable-form and large-SVO measurements")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":

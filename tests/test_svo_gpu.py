@@ -127,3 +127,44 @@ def test_fragment_list_into_a_given_buffer(cuda, setup):
     small = torch.empty((want.shape[0] // 2, 2), dtype=torch.int32, device="cuda")
     got2 = passes.svo_fragments(ds, 6, sh, light, sd, ws, out=small)
     assert np.array_equal(got2.cpu().numpy(), want)
+
+
+def test_terrain_level9_chain_bit_exact(cuda, oracle):
+    """The large-octree workload's scene (gradient-noise terrain + boxes) at its level 9 (512^3), reduced to
+    about 40k triangles: the fragment list and the deterministic build equal the oracle's word for word, and
+    the octree trace over the built pool follows the oracle's FP32 mirror."""
+    torch = cuda
+    from vk_voxel_cone_tracing_gb300 import capi, clipmap, passes
+    from vk_voxel_cone_tracing_gb300.scene import default_trace_desc, surface_samples, terrain_scene
+    scene = terrain_scene(seed=3, target=40000, boxes=250)
+    ds, ws = passes.DeviceScene(scene), passes.Workspace()
+    d = np.array(LIGHT_DIR, np.float64)
+    d /= np.linalg.norm(d)
+    origin = tuple((np.array([0.0, 1.5, 0.0]) - 15.0 * d).astype(np.float32).tolist())
+    sd_o = oracle.light_shadow_desc(origin, LIGHT_DIR)
+    shadow = oracle.shadow_depth(scene, sd_o, 512, 512)
+    level = 9
+    want_f, F = oracle.svo_fragments(scene, level, ds.bb_min, ds.bb_max, shadow, sd_o)
+    frags = passes.svo_fragments(ds, level, torch.from_numpy(shadow).cuda(), passes.light_desc(LIGHT_DIR),
+                                 passes.light_shadow_desc(origin, LIGHT_DIR), ws)
+    torch.cuda.synchronize()
+    assert F > 500000 and frags.shape[0] == F
+    assert np.array_equal(frags.cpu().numpy().view(np.uint32), want_f)
+    want, n_want = oracle.svo_build(want_f, level)
+    pool, n = passes.svo_build(frags, level, ws, mode=capi.SVO_DETERMINISTIC)
+    torch.cuda.synchronize()
+    assert n == n_want
+    assert np.array_equal(pool[:n].cpu().numpy().view(np.uint32), want)
+    # the trace over the octree: the scene's own box, volume dimension 512
+    regions = oracle.clip_regions((0.0, 3.0, 0.0), 512)
+    desc = clipmap.trace_desc(**default_trace_desc(regions, 512))
+    samples = surface_samples(scene, 1024, seed=3)
+    eye = (0.0, 6.0, -20.0)
+    bmin, bmax = tuple(ds.bb_min.tolist()), tuple(ds.bb_max.tolist())
+    d32, s32, st32 = oracle.svo_trace(32, bytes(desc), eye, want, samples, bmin, bmax)
+    dg, sg = passes.svo_cone_trace(desc, eye, pool, n, clipmap.samples_to_device(samples), bmin, bmax)
+    torch.cuda.synchronize()
+    for got, ref in ((dg.cpu().numpy().astype(np.float64), d32), (sg.cpu().numpy().astype(np.float64), s32)):
+        err = np.abs(got - ref).max(1) / np.maximum(np.abs(ref).max(1), 1e-3)
+        assert np.mean(err < 1e-4) > 0.99, np.sort(err)[-8:]
+    assert np.abs(d32[:, :3]).sum() > 0

@@ -8,6 +8,8 @@ benchmark configurations use procedural scenes instead:
   uniform-random RGBA8 albedo per triangle (about 34k triangles).
 * ``hall_scene`` -- configuration 2: instanced columns, arches and random
   clutter, about 1M triangles.
+* ``terrain_scene`` -- configuration 3 (the large octree): a gradient-noise
+  heightfield plus 10k boxes, about 4M triangles (58M SVO fragments at 512^3).
 
 Geometry comes out as separate fp32 position / normal streams and uint32
 indices (the reference binds one vertex stream per attribute,
@@ -231,6 +233,91 @@ def hall_scene(seed: int = 2, target: int = 1_000_000) -> Scene:
     used = sum(p.shape[0] for p in parts)
     parts.append(_random_triangles(rng, max(0, target - used), [-28, -0.5, -28], [28, 18, 28]))
     return _pack(np.concatenate(parts, 0), rng)
+
+
+# Eight unit gradients for the 2D gradient noise below.
+_GRAD2 = np.array([[1, 0], [-1, 0], [0, 1], [0, -1], [1, 1], [-1, 1], [1, -1], [-1, -1]], np.float64)
+_GRAD2[4:] *= np.sqrt(0.5)
+
+
+def gradient_noise2(x, y, perm: np.ndarray) -> np.ndarray:
+    """Perlin's gradient noise in 2D (K. Perlin, "Improving Noise", SIGGRAPH 2002): each lattice point takes
+    one of eight unit gradients through the hash perm[perm[i] + j] of a doubled 256-entry permutation, the
+    four corner ramps are blended with the quintic fade 6t^5 - 15t^4 + 10t^3.  Values lie in [-1, 1]."""
+    x = np.asarray(x, np.float64)
+    y = np.asarray(y, np.float64)
+    x0, y0 = np.floor(x), np.floor(y)
+    fx, fy = x - x0, y - y0
+    i, j = x0.astype(np.int64) & 255, y0.astype(np.int64) & 255
+
+    def ramp(di, dj):
+        g = _GRAD2[perm[perm[i + di] + j + dj] & 7]
+        return g[..., 0] * (fx - di) + g[..., 1] * (fy - dj)
+
+    def fade(t):
+        return t * t * t * (t * (t * 6.0 - 15.0) + 10.0)
+
+    u, v = fade(fx), fade(fy)
+    a = ramp(0, 0) + u * (ramp(1, 0) - ramp(0, 0))
+    b = ramp(0, 1) + u * (ramp(1, 1) - ramp(0, 1))
+    return a + v * (b - a)
+
+
+def _box_triangles(lo: np.ndarray, hi: np.ndarray) -> np.ndarray:
+    """Closed axis-aligned boxes, 12 outward-wound triangles each: (N, 12, 3, 3).  Corner c has the
+    coordinates (hi if bit k of c else lo) on axis k."""
+    quads = [(1, 3, 7, 5), (0, 4, 6, 2), (2, 6, 7, 3), (0, 1, 5, 4), (4, 5, 7, 6), (0, 2, 3, 1)]  # +x -x +y -y +z -z
+    corners = np.stack([np.where(np.array([(c >> k) & 1 for k in range(3)], bool)[None], hi, lo)
+                        for c in range(8)], 1)  # (N, 8, 3)
+    tri = np.array([t for a, b, c, d in quads for t in ((a, b, c), (a, c, d))])  # (12, 3)
+    return corners[:, tri]
+
+
+def terrain_height(x, z, perm: np.ndarray, amplitude: float = 2.5, frequency: float = 0.11,
+                   octaves: int = 5) -> np.ndarray:
+    """Fractal sum of gradient noise: amplitude * sum_o 0.5^o noise(frequency 2^o (x, z))."""
+    h = np.zeros(np.broadcast(np.asarray(x), np.asarray(z)).shape)
+    for o in range(octaves):
+        f = frequency * (2.0 ** o)
+        h += (0.5 ** o) * gradient_noise2(np.asarray(x) * f, np.asarray(z) * f, perm)
+    return amplitude * h
+
+
+def terrain_scene(seed: int = 3, target: int = 4_000_000, boxes: int = 10_000, half: float = 15.0,
+                  palette: int = 4096) -> Scene:
+    """Configuration 3: a gradient-noise terrain over [-half, half]^2 (a regular grid, two up-facing triangles
+    per cell) plus `boxes` closed boxes standing on it (footprint U(0.2, 0.9)^2, height U(0.2, 1.5)), about
+    `target` triangles in all.  Albedo from a palette of `palette` RGBA8 texels, one entry per triangle."""
+    rng = np.random.default_rng(seed)
+    perm = rng.permutation(256)
+    perm = np.concatenate([perm, perm])
+    cells = max(1, int(np.sqrt(max(target - 12 * boxes, 2) / 2.0)))
+    g = np.linspace(-half, half, cells + 1)
+    gx, gz = np.meshgrid(g, g, indexing="xy")
+    gy = terrain_height(gx, gz, perm)
+    v = np.stack([gx, gy, gz], -1)  # (cells+1, cells+1, 3), v[j, i] at (g[i], g[j])
+    v00, v10, v01, v11 = v[:-1, :-1], v[:-1, 1:], v[1:, :-1], v[1:, 1:]
+    # (v00, v01, v10) turns +y up: cross(v01 - v00, v10 - v00) = (0, dx dz, 0) on a flat cell
+    terrain = np.stack([np.stack([v00, v01, v10], -2), np.stack([v10, v01, v11], -2)], -3).reshape(-1, 3, 3)
+    parts = [terrain]
+    if boxes:
+        foot = rng.uniform(0.2, 0.9, size=(boxes, 2))
+        tall = rng.uniform(0.2, 1.5, size=boxes)
+        cx = rng.uniform(-half + 1.5, half - 1.5, boxes)
+        cz = rng.uniform(-half + 1.5, half - 1.5, boxes)
+        base = terrain_height(cx, cz, perm) - 0.2
+        lo = np.stack([cx - 0.5 * foot[:, 0], base, cz - 0.5 * foot[:, 1]], 1)
+        hi = np.stack([cx + 0.5 * foot[:, 0], base + tall, cz + 0.5 * foot[:, 1]], 1)
+        parts.append(_box_triangles(lo, hi).reshape(-1, 3, 3))
+    tris = np.concatenate(parts, 0).astype(np.float32)
+    T = tris.shape[0]
+    n = np.cross(tris[:, 1] - tris[:, 0], tris[:, 2] - tris[:, 0])
+    ln = np.linalg.norm(n, axis=1, keepdims=True)
+    n = np.where(ln > 0, n / np.maximum(ln, 1e-30), np.array([0, 1, 0], np.float32)).astype(np.float32)
+    textures = _rgba8(rng, palette)
+    tri_mat = rng.integers(0, palette, size=T, dtype=np.uint32)
+    return Scene(tris.reshape(-1, 3).copy(), np.repeat(n, 3, axis=0), np.arange(3 * T, dtype=np.uint32).reshape(T, 3),
+                 tri_mat, _materials_for(textures), textures)
 
 
 def _f16(x):
