@@ -321,6 +321,28 @@ int vct_downsample_f32(float* atlas4, const vct_downsample_desc* desc, int32_t m
 int vct_downsample_backward(const float* atlas4, float* grad_atlas4, const vct_downsample_desc* desc, int32_t mode,
                             void* stream);
 
+/* Inverse radiance fitting (build-only; the reference renders forward only).
+ * vct_sq_error: the squared error of `n` float4 outputs against targets,
+ * grad4 = 2 (out - target) scale and *loss (one device double) = scale *
+ * sum (out - target)^2, reduced in a fixed order (deterministic).
+ * vct_adam_step: one Adam step (Kingma & Ba, ICLR 2015) over n floats of a
+ * float RGBA volume with bias correction at `step` (1-based):
+ *   m = b1 m + (1 - b1) g,  v = b2 v + (1 - b2) g^2,
+ *   p = clamp(p - lr (m c1) / (sqrt(v c2) + eps)),  c1 = 1/(1 - b1^t), c2 = 1/(1 - b2^t),
+ * each operation rounded once (no fused multiply-add), RGB clamped to
+ * [rgb_lo, rgb_hi] and A to [alpha_lo, alpha_hi]; zero_grad != 0 clears g.
+ * n is a multiple of 4; all buffers 16-byte aligned. */
+typedef struct vct_adam_desc {
+    float lr, beta1, beta2, eps;
+    int32_t step, zero_grad;
+    float rgb_lo, rgb_hi, alpha_lo, alpha_hi;
+} vct_adam_desc;
+
+int vct_sq_error(const float* out4, const float* target4, int64_t n, float scale, float* grad4, double* loss,
+                 void* stream);
+int vct_adam_step(float* param, float* grad, float* m, float* v, int64_t n, const vct_adam_desc* desc,
+                  void* stream);
+
 /* ------------------------------------------- texture-sampled (fast) form */
 
 /* A hardware-filtered copy of a radiance atlas: a 3D CUDA array with
@@ -740,6 +762,7 @@ VCT_STATIC_ASSERT(sizeof(vct_directional_light_desc) == 32, "DirectionalLightDes
 VCT_STATIC_ASSERT(sizeof(vct_directional_light_shadow_desc) == 136, "DirectionalLightShadowDesc is 136 B");
 VCT_STATIC_ASSERT(sizeof(vct_specular_filter_desc) == 16, "SpecularFilterPassDesc is 16 B");
 VCT_STATIC_ASSERT(sizeof(vct_config) == 24, "vct_config is 24 B");
+VCT_STATIC_ASSERT(sizeof(vct_adam_desc) == 40, "vct_adam_desc is 40 B");
 VCT_STATIC_ASSERT(sizeof(vct_context_buffers) == 216, "vct_context_buffers is 216 B");
 VCT_STATIC_ASSERT(sizeof(vct_batch_job) == 264, "vct_batch_job is 264 B");
 VCT_STATIC_ASSERT(sizeof(vct_gltf_shade_material) == 80, "GltfShadeMaterial is 80 B");

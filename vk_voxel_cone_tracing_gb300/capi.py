@@ -119,6 +119,12 @@ class SpecularFilterDesc(C.Structure):
                 ("filter_method", C.c_int32)]
 
 
+class AdamDesc(C.Structure):
+    _fields_ = [("lr", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("eps", C.c_float),
+                ("step", C.c_int32), ("zero_grad", C.c_int32), ("rgb_lo", C.c_float), ("rgb_hi", C.c_float),
+                ("alpha_lo", C.c_float), ("alpha_hi", C.c_float)]
+
+
 class Scene(C.Structure):
     _fields_ = [("positions", C.c_void_p), ("normals", C.c_void_p), ("indices", C.c_void_p),
                 ("vertex_count", C.c_int64), ("triangle_count", C.c_int64), ("triangle_material", C.c_void_p),
@@ -162,7 +168,7 @@ STRUCT_SIZES = {
     ClipmapRegion: 28, VoxelizationDesc: 64, DownSampleDesc: 24, ImageCleaningDesc: 36, CopyAlphaDesc: 12,
     BorderWrappingDesc: 16, ConeTracingDesc: 52, CamMatrix: 144, DirectionalLightDesc: 32,
     DirectionalLightShadowDesc: 136, GltfShadeMaterial: 80, Scene: 104, SpecularFilterDesc: 16, Config: 24,
-    ContextBuffers: 216, BatchJob: 264,
+    ContextBuffers: 216, BatchJob: 264, AdamDesc: 40,
 }
 
 # Every entry point of include/vct_capi.h: name -> (restype, argtypes).
@@ -185,6 +191,8 @@ _SIGS: dict[str, tuple] = {
     "vct_cone_trace_backward": (C.c_int, [P, P, P, C.c_int32, P, P, P, P, C.c_int64, P, P, P, P]),
     "vct_downsample_f32": (C.c_int, [P, P, C.c_int32, P]),
     "vct_downsample_backward": (C.c_int, [P, P, P, C.c_int32, P]),
+    "vct_sq_error": (C.c_int, [P, P, C.c_int64, C.c_float, P, P, P]),
+    "vct_adam_step": (C.c_int, [P, P, P, P, C.c_int64, P, P]),
     "vct_texture_create": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     "vct_texture_update": (C.c_int, [P, P, P]),
     "vct_texture_read": (C.c_int, [P, P, P]),

@@ -317,3 +317,142 @@ extern "C" int vct_cone_trace_backward(const vct_cone_tracing_desc* desc, const 
     if (h_err) return fail(VCT_E_OVERFLOW, "vct_cone_trace_backward: a cone marched more than 8192 steps");
     return VCT_OK;
 }
+
+// ------------------------------------------------------ inverse fitting ops
+namespace vct {
+namespace {
+
+constexpr int kSqErrBlocks = 152 * 4;
+constexpr int kSqErrThreads = 256;
+
+// Squared error and its gradient; one double partial sum per block, each
+// thread summing its grid-stride elements in index order, the block in a
+// fixed tree order: the result does not depend on scheduling.
+__global__ void __launch_bounds__(kSqErrThreads) k_sq_error(const float4* __restrict__ out,
+                                                            const float4* __restrict__ target, int64_t n, float scale,
+                                                            float4* __restrict__ grad, double* __restrict__ partial) {
+    __shared__ double red[kSqErrThreads / 32];
+    const float two_scale = 2.0f * scale;
+    double acc = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float4 o = out[i], t = target[i];
+        const float dx = o.x - t.x, dy = o.y - t.y, dz = o.z - t.z, dw = o.w - t.w;
+        if (grad) grad[i] = make_float4(two_scale * dx, two_scale * dy, two_scale * dz, two_scale * dw);
+        acc += ((double)dx * dx + (double)dy * dy) + ((double)dz * dz + (double)dw * dw);
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < kSqErrThreads / 32; ++w) s += red[w];
+        partial[blockIdx.x] = s;
+    }
+}
+
+__global__ void k_sq_error_fold(const double* __restrict__ partial, int blocks, double scale,
+                                double* __restrict__ loss) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        double s = 0.0;
+        for (int b = 0; b < blocks; ++b) s += partial[b];
+        *loss = s * scale;
+    }
+}
+
+struct AdamArgs {
+    float lr, b1, omb1, b2, omb2, eps, c1, c2;
+    float lo[4], hi[4];
+    int zero_grad;
+};
+
+// One rounding per operation (the file is compiled without contraction), so
+// a float32 host restatement in the same order reproduces every bit.
+__device__ __forceinline__ float adam1(float& p, float g, float& m, float& v, const AdamArgs& a, int c) {
+    m = a.b1 * m + a.omb1 * g;
+    v = a.b2 * v + (a.omb2 * g) * g;
+    const float mh = m * a.c1, vh = v * a.c2;
+    const float upd = (a.lr * mh) / (__fsqrt_rn(vh) + a.eps);
+    p = fminf(fmaxf(p - upd, a.lo[c]), a.hi[c]);
+    return p;
+}
+
+__global__ void __launch_bounds__(256) k_adam(float4* __restrict__ p, float4* __restrict__ g, float4* __restrict__ m,
+                                              float4* __restrict__ v, int64_t n4, const AdamArgs a) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (int64_t)gridDim.x * blockDim.x) {
+        float4 P = p[i], G = g[i], M = m[i], V = v[i];
+        adam1(P.x, G.x, M.x, V.x, a, 0);
+        adam1(P.y, G.y, M.y, V.y, a, 1);
+        adam1(P.z, G.z, M.z, V.z, a, 2);
+        adam1(P.w, G.w, M.w, V.w, a, 3);
+        p[i] = P;
+        m[i] = M;
+        v[i] = V;
+        if (a.zero_grad) g[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
+}  // namespace
+}  // namespace vct
+
+extern "C" int vct_sq_error(const float* out4, const float* target4, int64_t n, float scale, float* grad4,
+                            double* loss, void* stream) {
+    vct::NvtxRange nvtx_range("vct_sq_error");
+    VCT_CHECK_ARG(n >= 0 && loss, "vct_sq_error: bad size or null loss");
+    VCT_CHECK_ARG(n == 0 || (out4 && target4), "vct_sq_error: null output / target");
+    VCT_CHECK_ARG((((uintptr_t)out4 | (uintptr_t)target4 | (uintptr_t)grad4) & 15) == 0,
+                  "vct_sq_error: buffers must be 16-byte aligned");
+    cudaStream_t st = as_stream(stream);
+    double* partial = nullptr;
+    VCT_CUDA_TRY(cudaMallocAsync(&partial, sizeof(double) * kSqErrBlocks, st));
+    int64_t blocks = (n + kSqErrThreads - 1) / kSqErrThreads;
+    blocks = blocks < 1 ? 1 : (blocks > kSqErrBlocks ? kSqErrBlocks : blocks);
+    k_sq_error<<<(int)blocks, kSqErrThreads, 0, st>>>(reinterpret_cast<const float4*>(out4),
+                                                      reinterpret_cast<const float4*>(target4), n, scale,
+                                                      reinterpret_cast<float4*>(grad4), partial);
+    cudaError_t le = cudaGetLastError();
+    if (le == cudaSuccess) {
+        k_sq_error_fold<<<1, 32, 0, st>>>(partial, (int)blocks, (double)scale, loss);
+        le = cudaGetLastError();
+    }
+    cudaFreeAsync(partial, st);
+    if (le != cudaSuccess) return cuda_fail(le, "k_sq_error");
+    return VCT_OK;
+}
+
+extern "C" int vct_adam_step(float* param, float* grad, float* m, float* v, int64_t n, const vct_adam_desc* desc,
+                             void* stream) {
+    vct::NvtxRange nvtx_range("vct_adam_step");
+    VCT_CHECK_ARG(desc && n >= 0 && (n & 3) == 0, "vct_adam_step: null descriptor or n not a multiple of 4");
+    VCT_CHECK_ARG(desc->step >= 1, "vct_adam_step: step counts from 1");
+    VCT_CHECK_ARG(desc->beta1 >= 0.0f && desc->beta1 < 1.0f && desc->beta2 >= 0.0f && desc->beta2 < 1.0f &&
+                      desc->eps > 0.0f,
+                  "vct_adam_step: betas must lie in [0, 1) and eps be positive");
+    if (n == 0) return VCT_OK;
+    VCT_CHECK_ARG(param && grad && m && v, "vct_adam_step: null buffer");
+    VCT_CHECK_ARG((((uintptr_t)param | (uintptr_t)grad | (uintptr_t)m | (uintptr_t)v) & 15) == 0,
+                  "vct_adam_step: buffers must be 16-byte aligned");
+    AdamArgs a;
+    a.lr = desc->lr;
+    a.b1 = desc->beta1;
+    a.omb1 = 1.0f - desc->beta1;
+    a.b2 = desc->beta2;
+    a.omb2 = 1.0f - desc->beta2;
+    a.eps = desc->eps;
+    a.c1 = (float)(1.0 / (1.0 - pow((double)desc->beta1, (double)desc->step)));
+    a.c2 = (float)(1.0 / (1.0 - pow((double)desc->beta2, (double)desc->step)));
+    for (int c = 0; c < 3; ++c) {
+        a.lo[c] = desc->rgb_lo;
+        a.hi[c] = desc->rgb_hi;
+    }
+    a.lo[3] = desc->alpha_lo;
+    a.hi[3] = desc->alpha_hi;
+    a.zero_grad = desc->zero_grad;
+    cudaStream_t st = as_stream(stream);
+    const int64_t n4 = n / 4;
+    int64_t blocks = (n4 + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    k_adam<<<(int)blocks, 256, 0, st>>>(reinterpret_cast<float4*>(param), reinterpret_cast<float4*>(grad),
+                                        reinterpret_cast<float4*>(m), reinterpret_cast<float4*>(v), n4, a);
+    VCT_LAUNCH_CHECK();
+    return VCT_OK;
+}
