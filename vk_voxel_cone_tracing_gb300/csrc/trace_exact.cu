@@ -7,6 +7,8 @@
 // Compiled with -fmad=false so no multiply-add is fused.
 #include <cstring>
 
+#include <cub/cub.cuh>
+
 #include "trace_exact.cuh"
 
 namespace vct {
@@ -14,10 +16,12 @@ namespace vct {
 template <class Atlas>
 __global__ void __launch_bounds__(128) k_cone_trace_exact(TraceParams P, Atlas T,
                                                           const vct_surface_sample* __restrict__ samples, int64_t n,
+                                                          const uint32_t* __restrict__ order,
                                                           float* __restrict__ dout, float* __restrict__ sout,
                                                           unsigned long long* __restrict__ step_counter) {
     unsigned long long steps = 0;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = order ? (int64_t)__ldg(order + t) : t;
         GSample g = load_sample(samples + i, P.eye);
         if (g.depth == 1.0f) continue;
         const vct_cone_tracing_desc& d = P.d;
@@ -60,6 +64,56 @@ __global__ void __launch_bounds__(128) k_cone_trace_exact(TraceParams P, Atlas T
     }
 }
 
+__device__ __forceinline__ uint32_t spread_bits10(uint32_t v) {
+    v &= 0x3ffu;
+    v = (v | (v << 16)) & 0x030000FFu;
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+__global__ void k_sample_keys(const vct_surface_sample* __restrict__ s, int64_t n, float cx, float cy, float cz,
+                              float q, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float* p = s[i].position;
+        const int x = min(max(__float2int_rd((p[0] - cx) * q) + 512, 0), 1023);
+        const int y = min(max(__float2int_rd((p[1] - cy) * q) + 512, 0), 1023);
+        const int z = min(max(__float2int_rd((p[2] - cz) * q) + 512, 0), 1023);
+        keys[i] = spread_bits10(x) | (spread_bits10(y) << 1) | (spread_bits10(z) << 2);
+        vals[i] = (uint32_t)i;
+    }
+}
+
+int sample_morton_order(const vct_surface_sample* samples, int64_t n, const vct_cone_tracing_desc& d,
+                        SampleOrder* out, cudaStream_t st) {
+    out->order = nullptr;
+    out->block = nullptr;
+    if (n <= 1 || n >= (1LL << 31)) return VCT_OK;
+    size_t temp = 0;
+    VCT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(nullptr, temp, (uint32_t*)nullptr, (uint32_t*)nullptr,
+                                                 (uint32_t*)nullptr, (uint32_t*)nullptr, (int)n, 0, 30, st));
+    const size_t arr = (4 * (size_t)n + 255) & ~(size_t)255;
+    char* b = nullptr;
+    VCT_CUDA_TRY(cudaMallocAsync((void**)&b, 4 * arr + temp, st));
+    uint32_t *keys = (uint32_t*)b, *keys_out = (uint32_t*)(b + arr), *vals = (uint32_t*)(b + 2 * arr),
+             *order = (uint32_t*)(b + 3 * arr);
+    int64_t g = (n + 255) / 256;
+    k_sample_keys<<<(int)(g > 152 * 32 ? 152 * 32 : g), 256, 0, st>>>(samples, n, d.volume_center[0],
+                                                                        d.volume_center[1], d.volume_center[2],
+                                                                        0.5f / d.voxel_size, keys, vals);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess)
+        e = cub::DeviceRadixSort::SortPairs(b + 4 * arr, temp, keys, keys_out, vals, order, (int)n, 0, 30, st);
+    if (e != cudaSuccess) {
+        cudaFreeAsync(b, st);
+        return cuda_fail(e, "sample_morton_order");
+    }
+    out->order = order;
+    out->block = b;
+    return VCT_OK;
+}
+
 }  // namespace vct
 
 using namespace vct;
@@ -88,6 +142,22 @@ int fill_trace_params(TraceParams& P, const vct_cone_tracing_desc* desc, const v
     }
     return VCT_OK;
 }
+
+// One thread per sample, the samples walked in Morton order.
+template <class Atlas>
+static int launch_exact(const TraceParams& P, const Atlas& T, const vct_surface_sample* samples, int64_t n,
+                        float* dout, float* sout, unsigned long long* cone_steps, cudaStream_t st) {
+    SampleOrder so;
+    int rc = sample_morton_order(samples, n, P.d, &so, st);
+    if (rc != VCT_OK) return rc;
+    int64_t blocks = (n + 127) / 128;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    k_cone_trace_exact<<<(int)blocks, 128, 0, st>>>(P, T, samples, n, so.order, dout, sout, cone_steps);
+    cudaError_t e = cudaGetLastError();
+    if (so.block) cudaFreeAsync(so.block, st);
+    if (e != cudaSuccess) return cuda_fail(e, "k_cone_trace_exact");
+    return VCT_OK;
+}
 }  // namespace vct
 
 extern "C" int vct_cone_trace(const vct_cone_tracing_desc* desc, const vct_cam_matrix* cam,
@@ -106,11 +176,7 @@ extern "C" int vct_cone_trace(const vct_cone_tracing_desc* desc, const vct_cam_m
     int rc = fill_trace_params(P, desc, cam, shadow, light, light_shadow);
     if (rc != VCT_OK) return rc;
     ExactAtlas T{radiance_atlas, AtlasDims(R)};
-    int64_t blocks = (n + 127) / 128;
-    if (blocks > 152 * 16) blocks = 152 * 16;
-    k_cone_trace_exact<<<(int)blocks, 128, 0, as_stream(stream)>>>(P, T, samples, n, dout, sout, cone_steps);
-    VCT_LAUNCH_CHECK();
-    return VCT_OK;
+    return launch_exact(P, T, samples, n, dout, sout, cone_steps, as_stream(stream));
 }
 
 extern "C" int vct_cone_trace_f32(const vct_cone_tracing_desc* desc, const vct_cam_matrix* cam, const float* atlas4,
@@ -129,9 +195,5 @@ extern "C" int vct_cone_trace_f32(const vct_cone_tracing_desc* desc, const vct_c
     int rc = fill_trace_params(P, desc, cam, shadow, light, light_shadow);
     if (rc != VCT_OK) return rc;
     F4Atlas T{reinterpret_cast<const float4*>(atlas4), AtlasDims(R)};
-    int64_t blocks = (n + 127) / 128;
-    if (blocks > 152 * 16) blocks = 152 * 16;
-    k_cone_trace_exact<<<(int)blocks, 128, 0, as_stream(stream)>>>(P, T, samples, n, dout, sout, cone_steps);
-    VCT_LAUNCH_CHECK();
-    return VCT_OK;
+    return launch_exact(P, T, samples, n, dout, sout, cone_steps, as_stream(stream));
 }

@@ -202,6 +202,7 @@ __device__ void cone_backward(const F4Atlas& T, float4* __restrict__ G, const vc
 
 __global__ void __launch_bounds__(128) k_cone_trace_backward(TraceParams P, F4Atlas T,
                                                              const vct_surface_sample* __restrict__ samples, int64_t n,
+                                                             const uint32_t* __restrict__ order,
                                                              const float4* __restrict__ gd, const float4* __restrict__ gs,
                                                              float4* __restrict__ G, int* __restrict__ err) {
     const vct_cone_tracing_desc& d = P.d;
@@ -211,10 +212,11 @@ __global__ void __launch_bounds__(128) k_cone_trace_backward(TraceParams P, F4At
     const uint32_t mode = d.rendering_mode;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * slots;
          t += (int64_t)gridDim.x * blockDim.x) {
-        // cone-major: a warp's lanes march the same cone of consecutive samples (the same aperture and
-        // step schedule, so the lanes stay in step)
+        // cone-major: a warp's lanes march the same cone of consecutive samples in Morton order (the same
+        // direction from neighbouring points: the lanes stay in step and share texels)
         const int slot = (int)(t / n);
-        const int64_t i = t - (int64_t)slot * n;
+        const int64_t u = t - (int64_t)slot * n;
+        const int64_t i = order ? (int64_t)__ldg(order + u) : u;
         GSample g = load_sample(samples + i, P.eye);
         if (g.depth == 1.0f) continue;
         float min_level = calc_min_level(d, g.wp);
@@ -303,7 +305,14 @@ extern "C" int vct_cone_trace_backward(const vct_cone_tracing_desc* desc, const 
     const int slots = (desc->enable_32_cones ? 32 : 16) + 1;
     int64_t blocks = (n * slots + 127) / 128;
     if (blocks > 152 * 32) blocks = 152 * 32;
-    k_cone_trace_backward<<<(int)blocks, 128, 0, st>>>(P, T, samples, n, reinterpret_cast<const float4*>(grad_diffuse),
+    SampleOrder so;
+    rc = sample_morton_order(samples, n, P.d, &so, st);
+    if (rc != VCT_OK) {
+        cudaFreeAsync(err, st);
+        return rc;
+    }
+    k_cone_trace_backward<<<(int)blocks, 128, 0, st>>>(P, T, samples, n, so.order,
+                                                        reinterpret_cast<const float4*>(grad_diffuse),
                                                         reinterpret_cast<const float4*>(grad_specular),
                                                         reinterpret_cast<float4*>(grad_atlas4), err);
     cudaError_t le = cudaGetLastError();
@@ -311,6 +320,7 @@ extern "C" int vct_cone_trace_backward(const vct_cone_tracing_desc* desc, const 
     cudaError_t ce = cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, st);
     cudaError_t se = cudaStreamSynchronize(st);
     cudaFreeAsync(err, st);
+    if (so.block) cudaFreeAsync(so.block, st);
     if (le != cudaSuccess) return cuda_fail(le, "k_cone_trace_backward");
     if (ce != cudaSuccess) return cuda_fail(ce, "vct_cone_trace_backward readback");
     if (se != cudaSuccess) return cuda_fail(se, "vct_cone_trace_backward");
