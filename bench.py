@@ -732,19 +732,22 @@ def differentiable_volume(dev, R: int = 128, views: int = 16, res: int = 512, se
     # = mips + trace + squared error + trace adjoint + mip adjoint + Adam (host clock: the adjoint synchronises)
     from vk_voxel_cone_tracing_gb300 import fit
     del G
-    f = fit.RadianceFit(R, regions, desc, cam, light, smp, lr=0.02)
-    f.set_targets(*f.render(vol))
-    losses, iter_ms = [], []
-    for _ in range(fit_iterations):
-        t0 = time.perf_counter()
-        losses.append(f.step())
-        iter_ms.append((time.perf_counter() - t0) * 1e3)
-    losses.append(f.loss())
+    fit_result = None
+    if fit_iterations > 0:
+        f = fit.RadianceFit(R, regions, desc, cam, light, smp, lr=0.02)
+        f.set_targets(*f.render(vol))
+        losses, iter_ms = [], []
+        for _ in range(fit_iterations):
+            t0 = time.perf_counter()
+            losses.append(f.step())
+            iter_ms.append((time.perf_counter() - t0) * 1e3)
+        losses.append(f.loss())
+        fit_result = {"iterations": fit_iterations, "iteration_ms": statistics.median(iter_ms), "loss": losses,
+                      "optimiser": "Adam (lr 0.02, betas 0.9 / 0.999), from zero"}
     return {"R": R, "views": views, "resolution": res, "samples": n, "cone_samples": cone_samples,
             "forward_ms": fwd_ms, "backward_ms": bwd_ms, "forward_cone_samples_per_s": cone_samples / (fwd_ms * 1e-3),
             "mips_ms": mips_ms, "mips_backward_ms": mips_bwd_ms,
-            "fit": {"iterations": fit_iterations, "iteration_ms": statistics.median(iter_ms), "loss": losses,
-                    "optimiser": "Adam (lr 0.02, betas 0.9 / 0.999), from zero"},
+            "fit": fit_result,
             "note": "float RGBA atlas (16 B per texel, 1.27 GB at R = 128), software trilinear; the adjoint "
                     "recomputes each cone from 32-step checkpoints and scatters float4 atomics"}
 
