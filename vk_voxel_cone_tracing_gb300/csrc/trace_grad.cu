@@ -77,7 +77,9 @@ __device__ __forceinline__ void texture3d_grad(float4* __restrict__ G, const Atl
             }
 }
 
-// Adjoint of sample_clipmap: the three face taps' shares.
+// Adjoint of sample_clipmap: the three face taps' shares (one copy of the
+// tap code, looped: the kernel is instruction-fetch bound when it is inlined
+// six times per step).
 __device__ __forceinline__ void sample_clipmap_grad(float4* __restrict__ G, const AtlasDims& A,
                                                     const vct_cone_tracing_desc& d, float3 p, int level, float3 fo,
                                                     float3 wt, float4 g) {
@@ -90,9 +92,12 @@ __device__ __forceinline__ void sample_clipmap_grad(float4* __restrict__ G, cons
     sy = sy + (float)level;
     sy = sy / (float)kClipLevels;
     sx = sx / (float)kFaces;
-    texture3d_grad(G, A, sx + fo.x, sy, sz, make_float4(g.x * wt.x, g.y * wt.x, g.z * wt.x, g.w * wt.x));
-    texture3d_grad(G, A, sx + fo.y, sy, sz, make_float4(g.x * wt.y, g.y * wt.y, g.z * wt.y, g.w * wt.y));
-    texture3d_grad(G, A, sx + fo.z, sy, sz, make_float4(g.x * wt.z, g.y * wt.z, g.z * wt.z, g.w * wt.z));
+#pragma unroll 1
+    for (int f = 0; f < 3; ++f) {
+        const float off = f == 0 ? fo.x : (f == 1 ? fo.y : fo.z);
+        const float w = f == 0 ? wt.x : (f == 1 ? wt.y : wt.z);
+        texture3d_grad(G, A, sx + off, sy, sz, make_float4(g.x * w, g.y * w, g.z * w, g.w * w));
+    }
 }
 
 // The volume-independent part of one step of trace_cone at state m.
@@ -136,9 +141,17 @@ __device__ __forceinline__ float4 march_step(const F4Atlas& T, const vct_cone_tr
     return smp;
 }
 
-// The adjoint of one cone: gC (rgb) and gO (d/d occlusion) at the end of the march.
+// The adjoint of one cone per lane: gC (rgb) and gO (d/d occlusion) at the
+// end of the march.  The warp's lanes run in lock step: every loop runs to
+// the warp's longest march and a lane sits out the steps its cone does not
+// have (or all of them when `active` is false), so a warp walks one step
+// index at a time -- no divergent loop control, and with cone-major Morton-
+// ordered lanes the taps of a step land on neighbouring texels.  The forward
+// recompute of a segment keeps each step's filtered sample, so the reverse
+// walk reads no texels.
 __device__ void cone_backward(const F4Atlas& T, float4* __restrict__ G, const vct_cone_tracing_desc& d, const Cone& K,
-                              float3 gC, float gO, float max_dist, int* __restrict__ err) {
+                              float3 gC, float gO, bool active, float max_dist, int* __restrict__ err) {
+    constexpr unsigned kFull = 0xffffffffu;
     MarchState ckpt[kMaxSegments];
     MarchState m;
     m.step = 0.0f;
@@ -147,33 +160,39 @@ __device__ void cone_backward(const F4Atlas& T, float4* __restrict__ G, const vc
     m.alpha = 0.0f;
     m.occ = 0.0f;
     int n = 0;
-    while (m.step < max_dist && m.occ < 1.0f) {
-        if ((n % kSegSteps) == 0) {
-            if (n / kSegSteps >= kMaxSegments) {
-                atomicOr(err, 1);
-                return;
-            }
-            ckpt[n / kSegSteps] = m;
+    bool running = active && m.step < max_dist && m.occ < 1.0f;
+    for (int j = 0; __any_sync(kFull, running); ++j) {
+        if ((j % kSegSteps) == 0 && j / kSegSteps >= kMaxSegments) {  // j is warp-uniform
+            if (running) atomicOr(err, 1);
+            return;
         }
-        march_step(T, d, K, m, step_geo(K, m));
-        ++n;
+        if (running) {
+            if ((j % kSegSteps) == 0) ckpt[j / kSegSteps] = m;
+            march_step(T, d, K, m, step_geo(K, m));
+            ++n;
+            running = m.step < max_dist && m.occ < 1.0f;
+        }
     }
+    const int nmax = __reduce_max_sync(kFull, n);
     float gA = 0.0f;
     MarchState seg[kSegSteps];
-    for (int sidx = (n - 1) / kSegSteps; sidx >= 0 && n > 0; --sidx) {
-        const int first = sidx * kSegSteps, last = min(n, first + kSegSteps);
-        MarchState r = ckpt[sidx];
+    float4 seg_smp[kSegSteps];
+    for (int sidx = (nmax - 1) / kSegSteps; nmax > 0 && sidx >= 0; --sidx) {
+        const int first = sidx * kSegSteps, last = min(nmax, first + kSegSteps);
+        const int mine = min(n, first + kSegSteps);  // this lane's steps of the segment: first .. mine - 1
+        MarchState r;
+        if (first < n) r = ckpt[sidx];
         for (int i = first; i < last; ++i) {
-            seg[i - first] = r;
-            march_step(T, d, K, r, step_geo(K, r));
+            if (i < mine) {
+                seg[i - first] = r;
+                seg_smp[i - first] = march_step(T, d, K, r, step_geo(K, r));
+            }
         }
         for (int i = last - 1; i >= first; --i) {
+            if (i >= mine) continue;
             const MarchState& mi = seg[i - first];
             const StepGeo s = step_geo(K, mi);
-            float4 lo = sample_clipmap(T, d, s.pos, s.lower, K.fo, K.wt);
-            float4 hi = sample_clipmap(T, d, s.pos, s.upper, K.fo, K.wt);
-            float4 smp = make_float4(lo.x * (1.0f - s.fr) + hi.x * s.fr, lo.y * (1.0f - s.fr) + hi.y * s.fr,
-                                     lo.z * (1.0f - s.fr) + hi.z * s.fr, lo.w * (1.0f - s.fr) + hi.w * s.fr);
+            const float4 smp = seg_smp[i - first];
             const float c = s.correction;
             const float base = 1.0f - smp.w;
             const float op_raw = 1.0f - powf(base, c);
@@ -190,12 +209,14 @@ __device__ void cone_backward(const F4Atlas& T, float4* __restrict__ G, const vc
             gs.w = gop * dop;
             if (k_raw > 0.0f && k_raw < 1.0f) gA = gA - ((gC.x * smp.x + gC.y * smp.y + gC.z * smp.z) * c + gA * op);
             gO = gO * (1.0f - op / qd);
-            // s = lo (1 - fr) + hi fr
-            const float4 glo = make_float4(gs.x * (1.0f - s.fr), gs.y * (1.0f - s.fr), gs.z * (1.0f - s.fr),
-                                           gs.w * (1.0f - s.fr));
-            const float4 ghi = make_float4(gs.x * s.fr, gs.y * s.fr, gs.z * s.fr, gs.w * s.fr);
-            sample_clipmap_grad(G, T.A, d, s.pos, s.lower, K.fo, K.wt, glo);
-            sample_clipmap_grad(G, T.A, d, s.pos, s.upper, K.fo, K.wt, ghi);
+            // s = lo (1 - fr) + hi fr: the lower level's share, then the upper's (zero when fr = 0)
+#pragma unroll 1
+            for (int lv = 0; lv < 2; ++lv) {
+                const float f = lv ? s.fr : 1.0f - s.fr;
+                if (f == 0.0f) continue;
+                sample_clipmap_grad(G, T.A, d, s.pos, lv ? s.upper : s.lower, K.fo, K.wt,
+                                    make_float4(gs.x * f, gs.y * f, gs.z * f, gs.w * f));
+            }
         }
     }
 }
@@ -210,15 +231,20 @@ __global__ void __launch_bounds__(128) k_cone_trace_backward(TraceParams P, F4At
     const int nc = c32 ? 32 : 16;
     const int slots = nc + 1;
     const uint32_t mode = d.rendering_mode;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * slots;
-         t += (int64_t)gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int64_t total = n * slots;
+    // warp-uniform trip count: a warp's lanes enter cone_backward together
+    for (int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x - lane; t0 < total;
+         t0 += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t t = t0 + lane;
+        bool active = t < total;
         // cone-major: a warp's lanes march the same cone of consecutive samples in Morton order (the same
         // direction from neighbouring points: the lanes stay in step and share texels)
-        const int slot = (int)(t / n);
-        const int64_t u = t - (int64_t)slot * n;
+        const int slot = active ? (int)(t / n) : 0;
+        const int64_t u = active ? t - (int64_t)slot * n : 0;
         const int64_t i = order ? (int64_t)__ldg(order + u) : u;
         GSample g = load_sample(samples + i, P.eye);
-        if (g.depth == 1.0f) continue;
+        active = active && g.depth != 1.0f;
         float min_level = calc_min_level(d, g.wp);
         float vs = d.voxel_size * exp2f(min_level);
         Cone K;
@@ -227,22 +253,22 @@ __global__ void __launch_bounds__(128) k_cone_trace_backward(TraceParams P, F4At
         K.center = f3(d.volume_center[0], d.volume_center[1], d.volume_center[2]);
         K.min_radius = K.uvs * d.volume_dimension * 0.5f;
         K.start_level = min_level;
-        float3 gC;
-        float gO;
+        float3 gC = f3(0.f, 0.f, 0.f);
+        float gO = 0.0f;
         float aperture;
         const float4 GD = gd[i], GS = gs[i];
         if (slot < nc) {
             K.dir = c32 ? f3(c_dirs32[slot][0], c_dirs32[slot][1], c_dirs32[slot][2])
                         : f3(c_dirs16[slot][0], c_dirs16[slot][1], c_dirs16[slot][2]);
             const float cos_t = dot3(g.normal, K.dir);
-            if (cos_t < 0.0f) continue;
+            active = active && cos_t >= 0.0f;
             // dL/d(indirect): D.rgb = direct * ind.w + ind.rgb (modes 5 and the default), direct * ind.w (4),
             // ind.w (7); the others do not read the volume
             float3 g_ind = f3(0.f, 0.f, 0.f);
             float g_ao = 0.0f;
             const bool rgb_mode = mode == 5 || mode >= 8;
             if (rgb_mode) g_ind = f3(GD.x, GD.y, GD.z);
-            if (rgb_mode || mode == 4) {
+            if (active && (rgb_mode || mode == 4)) {
                 const float3 direct = direct_term(P, g);
                 g_ao = GD.x * direct.x + GD.y * direct.y + GD.z * direct.z;
             } else if (mode == 7) {
@@ -256,7 +282,7 @@ __global__ void __launch_bounds__(128) k_cone_trace_backward(TraceParams P, F4At
             aperture = c32 ? kAperture32 : kAperture16;
             K.step_factor = fmaxf(kMinTraceStepFactor, d.min_trace_step_factor);
         } else {
-            if (!has_specular_cone(g) || !(mode == 6 || mode >= 8)) continue;
+            active = active && has_specular_cone(g) && (mode == 6 || mode >= 8);
             K.dir = reflect3(f3(-g.view.x, -g.view.y, -g.view.z), g.normal);
             const float isi = d.indirect_specular_intensity;
             gC = f3(GS.x * g.specular_color.x * isi, GS.y * g.specular_color.y * isi, GS.z * g.specular_color.z * isi);
@@ -264,13 +290,13 @@ __global__ void __launch_bounds__(128) k_cone_trace_backward(TraceParams P, F4At
             aperture = fmaxf(g.roughness, kMinSpecularAperture);
             K.step_factor = d.voxel_size;
         }
-        if (gC.x == 0.0f && gC.y == 0.0f && gC.z == 0.0f && gO == 0.0f) continue;
+        active = active && !(gC.x == 0.0f && gC.y == 0.0f && gC.z == 0.0f && gO == 0.0f);
         K.coef = 2.0f * tanf(aperture * 0.5f);
         K.start = K.start + K.dir * (K.uvs * exp2f(K.start_level) * d.trace_start_offset * 0.5f);
         K.fo = f3(K.dir.x > 0.0f ? 0.0f : 1.0f / 6.0f, K.dir.y > 0.0f ? 2.0f / 6.0f : 3.0f / 6.0f,
                   K.dir.z > 0.0f ? 4.0f / 6.0f : 5.0f / 6.0f);
         K.wt = f3(K.dir.x * K.dir.x, K.dir.y * K.dir.y, K.dir.z * K.dir.z);
-        cone_backward(T, G, d, K, gC, gO, kMaxTraceDistance, err);
+        cone_backward(T, G, d, K, gC, gO, active, kMaxTraceDistance, err);
     }
 }
 
