@@ -73,19 +73,36 @@ __device__ __forceinline__ uint32_t spread_bits10(uint32_t v) {
     return v;
 }
 
+// Key = normal class (6 bits: the octahedral map of the normal on an 8 x 8
+// grid) above a 24-bit Morton code of the position (8 bits per axis, cells of
+// two level-0 voxels).  Samples with similar normals skip the same diffuse
+// cones (cos < 0), so a warp's lanes agree on which cones to march; within a
+// class, neighbouring points share texels.
 __global__ void k_sample_keys(const vct_surface_sample* __restrict__ s, int64_t n, float cx, float cy, float cz,
                               float q, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const float* p = s[i].position;
-        const int x = min(max(__float2int_rd((p[0] - cx) * q) + 512, 0), 1023);
-        const int y = min(max(__float2int_rd((p[1] - cy) * q) + 512, 0), 1023);
-        const int z = min(max(__float2int_rd((p[2] - cz) * q) + 512, 0), 1023);
-        keys[i] = spread_bits10(x) | (spread_bits10(y) << 1) | (spread_bits10(z) << 2);
+        const int x = min(max(__float2int_rd((p[0] - cx) * q) + 128, 0), 255);
+        const int y = min(max(__float2int_rd((p[1] - cy) * q) + 128, 0), 255);
+        const int z = min(max(__float2int_rd((p[2] - cz) * q) + 128, 0), 255);
+        const float* t = s[i].normal_texel;
+        const float nx = t[0] * 2.0f - 1.0f, ny = t[1] * 2.0f - 1.0f, nz = t[2] * 2.0f - 1.0f;
+        const float l1 = fabsf(nx) + fabsf(ny) + fabsf(nz);
+        float ox = l1 > 0.0f ? nx / l1 : 0.0f, oy = l1 > 0.0f ? ny / l1 : 0.0f;
+        if (nz < 0.0f) {
+            const float ax = (1.0f - fabsf(oy)) * (ox >= 0.0f ? 1.0f : -1.0f);
+            const float ay = (1.0f - fabsf(ox)) * (oy >= 0.0f ? 1.0f : -1.0f);
+            ox = ax;
+            oy = ay;
+        }
+        const int cu = min(max((int)((ox * 0.5f + 0.5f) * 8.0f), 0), 7);
+        const int cv = min(max((int)((oy * 0.5f + 0.5f) * 8.0f), 0), 7);
+        keys[i] = ((uint32_t)(cv * 8 + cu) << 24) | spread_bits10(x) | (spread_bits10(y) << 1) | (spread_bits10(z) << 2);
         vals[i] = (uint32_t)i;
     }
 }
 
-int sample_morton_order(const vct_surface_sample* samples, int64_t n, const vct_cone_tracing_desc& d,
+int sample_coherent_order(const vct_surface_sample* samples, int64_t n, const vct_cone_tracing_desc& d,
                         SampleOrder* out, cudaStream_t st) {
     out->order = nullptr;
     out->block = nullptr;
@@ -107,7 +124,7 @@ int sample_morton_order(const vct_surface_sample* samples, int64_t n, const vct_
         e = cub::DeviceRadixSort::SortPairs(b + 4 * arr, temp, keys, keys_out, vals, order, (int)n, 0, 30, st);
     if (e != cudaSuccess) {
         cudaFreeAsync(b, st);
-        return cuda_fail(e, "sample_morton_order");
+        return cuda_fail(e, "sample_coherent_order");
     }
     out->order = order;
     out->block = b;
@@ -143,12 +160,12 @@ int fill_trace_params(TraceParams& P, const vct_cone_tracing_desc* desc, const v
     return VCT_OK;
 }
 
-// One thread per sample, the samples walked in Morton order.
+// One thread per sample, the samples walked in the coherent order (normal class, then Morton).
 template <class Atlas>
 static int launch_exact(const TraceParams& P, const Atlas& T, const vct_surface_sample* samples, int64_t n,
                         float* dout, float* sout, unsigned long long* cone_steps, cudaStream_t st) {
     SampleOrder so;
-    int rc = sample_morton_order(samples, n, P.d, &so, st);
+    int rc = sample_coherent_order(samples, n, P.d, &so, st);
     if (rc != VCT_OK) return rc;
     int64_t blocks = (n + 127) / 128;
     if (blocks > 152 * 16) blocks = 152 * 16;

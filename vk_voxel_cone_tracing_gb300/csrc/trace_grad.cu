@@ -238,7 +238,7 @@ __global__ void __launch_bounds__(128) k_cone_trace_backward(TraceParams P, F4At
          t0 += (int64_t)gridDim.x * blockDim.x) {
         const int64_t t = t0 + lane;
         bool active = t < total;
-        // cone-major: a warp's lanes march the same cone of consecutive samples in Morton order (the same
+        // cone-major: a warp's lanes march the same cone of consecutive samples in the coherent order (the same
         // direction from neighbouring points: the lanes stay in step and share texels)
         const int slot = active ? (int)(t / n) : 0;
         const int64_t u = active ? t - (int64_t)slot * n : 0;
@@ -332,7 +332,7 @@ extern "C" int vct_cone_trace_backward(const vct_cone_tracing_desc* desc, const 
     int64_t blocks = (n * slots + 127) / 128;
     if (blocks > 152 * 32) blocks = 152 * 32;
     SampleOrder so;
-    rc = sample_morton_order(samples, n, P.d, &so, st);
+    rc = sample_coherent_order(samples, n, P.d, &so, st);
     if (rc != VCT_OK) {
         cudaFreeAsync(err, st);
         return rc;
