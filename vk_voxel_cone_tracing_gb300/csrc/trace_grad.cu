@@ -145,11 +145,10 @@ __device__ __forceinline__ float4 march_step(const F4Atlas& T, const vct_cone_tr
 // end of the march.  The warp's lanes run in lock step: every loop runs to
 // the warp's longest march and a lane sits out the steps its cone does not
 // have (or all of them when `active` is false), so a warp walks one step
-// index at a time -- no divergent loop control, and with cone-major lanes in
-// the coherent sample order the taps of a step land on neighbouring texels.
-// The forward pass and the recompute of a segment keep each step's state and
-// filtered sample, so the reverse walk reads no texels and the last segment
-// is never recomputed.
+// index at a time -- no divergent loop control, and with cone-major Morton-
+// ordered lanes the taps of a step land on neighbouring texels.  The forward
+// recompute of a segment keeps each step's filtered sample, so the reverse
+// walk reads no texels.
 __device__ void cone_backward(const F4Atlas& T, float4* __restrict__ G, const vct_cone_tracing_desc& d, const Cone& K,
                               float3 gC, float gO, bool active, float max_dist, int* __restrict__ err) {
     constexpr unsigned kFull = 0xffffffffu;
@@ -162,10 +161,6 @@ __device__ void cone_backward(const F4Atlas& T, float4* __restrict__ G, const vc
     m.occ = 0.0f;
     int n = 0;
     bool running = active && m.step < max_dist && m.occ < 1.0f;
-    // the forward pass keeps every step of the segment it is in, so the last
-    // segment (the only one of most diffuse cones) needs no recompute
-    MarchState seg[kSegSteps];
-    float4 seg_smp[kSegSteps];
     for (int j = 0; __any_sync(kFull, running); ++j) {
         if ((j % kSegSteps) == 0 && j / kSegSteps >= kMaxSegments) {  // j is warp-uniform
             if (running) atomicOr(err, 1);
@@ -173,23 +168,22 @@ __device__ void cone_backward(const F4Atlas& T, float4* __restrict__ G, const vc
         }
         if (running) {
             if ((j % kSegSteps) == 0) ckpt[j / kSegSteps] = m;
-            seg[j % kSegSteps] = m;
-            seg_smp[j % kSegSteps] = march_step(T, d, K, m, step_geo(K, m));
+            march_step(T, d, K, m, step_geo(K, m));
             ++n;
             running = m.step < max_dist && m.occ < 1.0f;
         }
     }
     const int nmax = __reduce_max_sync(kFull, n);
-    const int kept = n > 0 ? (n - 1) / kSegSteps : -1;  // the segment the forward pass left in seg[]
     float gA = 0.0f;
+    MarchState seg[kSegSteps];
+    float4 seg_smp[kSegSteps];
     for (int sidx = (nmax - 1) / kSegSteps; nmax > 0 && sidx >= 0; --sidx) {
         const int first = sidx * kSegSteps, last = min(nmax, first + kSegSteps);
         const int mine = min(n, first + kSegSteps);  // this lane's steps of the segment: first .. mine - 1
-        const bool redo = sidx < kept;
         MarchState r;
-        if (redo) r = ckpt[sidx];
+        if (first < n) r = ckpt[sidx];
         for (int i = first; i < last; ++i) {
-            if (redo && i < mine) {
+            if (i < mine) {
                 seg[i - first] = r;
                 seg_smp[i - first] = march_step(T, d, K, r, step_geo(K, r));
             }
