@@ -669,7 +669,7 @@ def large_svo(dev, reps: int, level: int = 9, n_samples: int = 4 << 20, seed: in
             "note": "deterministic build (scan allocation, fragment-order leaf fold); CUDA events, median"}
 
 
-def differentiable_volume(dev, R: int = 128, views: int = 16, res: int = 512, seed: int = 5, fit_iterations: int = 3):
+def differentiable_volume(dev, R: int = 128, views: int = 16, res: int = 512, seed: int = 5, fit_iterations: int = 8):
     """Configuration 5: a hidden float RGBA clipmap (R = 128, smooth noise, alpha <= 0.3) seen through
     `views` x res^2 G-buffer samples: one forward trace of the float atlas (vct_cone_trace_f32), its adjoint
     (vct_cone_trace_backward, dL/d atlas for a unit upstream gradient on every output), and the five-level
@@ -734,7 +734,7 @@ def differentiable_volume(dev, R: int = 128, views: int = 16, res: int = 512, se
     del G
     fit_result = None
     if fit_iterations > 0:
-        f = fit.RadianceFit(R, regions, desc, cam, light, smp, lr=0.02)
+        f = fit.RadianceFit(R, regions, desc, cam, light, smp, lr=0.005)
         f.set_targets(*f.render(vol))
         losses, iter_ms = [], []
         for _ in range(fit_iterations):
@@ -743,7 +743,7 @@ def differentiable_volume(dev, R: int = 128, views: int = 16, res: int = 512, se
             iter_ms.append((time.perf_counter() - t0) * 1e3)
         losses.append(f.loss())
         fit_result = {"iterations": fit_iterations, "iteration_ms": statistics.median(iter_ms), "loss": losses,
-                      "optimiser": "Adam (lr 0.02, betas 0.9 / 0.999), from zero"}
+                      "optimiser": "Adam (lr 0.005, betas 0.9 / 0.999), from zero"}
     return {"R": R, "views": views, "resolution": res, "samples": n, "cone_samples": cone_samples,
             "forward_ms": fwd_ms, "backward_ms": bwd_ms, "forward_cone_samples_per_s": cone_samples / (fwd_ms * 1e-3),
             "mips_ms": mips_ms, "mips_backward_ms": mips_bwd_ms,
