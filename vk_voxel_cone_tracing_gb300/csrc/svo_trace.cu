@@ -93,11 +93,13 @@ __device__ float4 svo_trace_cone(const SvoScene& S, const vct_cone_tracing_desc&
 }
 
 __global__ void __launch_bounds__(128) k_svo_trace(TraceParams P, SvoScene S, const vct_surface_sample* __restrict__ samples,
-                                                   int64_t n, float* __restrict__ dout, float* __restrict__ sout,
+                                                   int64_t n, const uint32_t* __restrict__ order,
+                                                   float* __restrict__ dout, float* __restrict__ sout,
                                                    unsigned long long* __restrict__ step_counter) {
     unsigned long long steps = 0;
     const vct_cone_tracing_desc& d = P.d;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = order ? (int64_t)__ldg(order + t) : t;
         GSample g = load_sample(samples + i, P.eye);
         if (g.depth == 1.0f) continue;
         const float min_level = calc_min_level(d, g.wp);
@@ -206,9 +208,16 @@ extern "C" int vct_svo_cone_trace(const vct_cone_tracing_desc* desc, const vct_c
         S.bmin[a] = bb_min[a];
         S.bmax[a] = bb_max[a];
     }
+    // the samples walked in the coherent order (normal class, then Morton), as the clipmap trace does
+    cudaStream_t st = as_stream(stream);
+    SampleOrder so;
+    rc = sample_coherent_order(samples, n, P.d, &so, st);
+    if (rc != VCT_OK) return rc;
     int64_t blocks = (n + 127) / 128;
     if (blocks > 152 * 16) blocks = 152 * 16;
-    k_svo_trace<<<(int)blocks, 128, 0, as_stream(stream)>>>(P, S, samples, n, dout, sout, cone_steps);
-    VCT_LAUNCH_CHECK();
+    k_svo_trace<<<(int)blocks, 128, 0, st>>>(P, S, samples, n, so.order, dout, sout, cone_steps);
+    cudaError_t e = cudaGetLastError();
+    if (so.block) cudaFreeAsync(so.block, st);
+    if (e != cudaSuccess) return cuda_fail(e, "k_svo_trace");
     return VCT_OK;
 }

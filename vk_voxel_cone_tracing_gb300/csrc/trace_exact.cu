@@ -74,17 +74,18 @@ __device__ __forceinline__ uint32_t spread_bits10(uint32_t v) {
 }
 
 // Key = normal class (6 bits: the octahedral map of the normal on an 8 x 8
-// grid) above a 24-bit Morton code of the position (8 bits per axis, cells of
-// two level-0 voxels).  Samples with similar normals skip the same diffuse
-// cones (cos < 0), so a warp's lanes agree on which cones to march; within a
-// class, neighbouring points share texels.
+// grid) above a 30-bit Morton code of the position (10 bits per axis, cells
+// of two level-0 voxels: +-1024 voxels around the centre).  Samples with
+// similar normals skip the same diffuse cones (cos < 0), so a warp's lanes
+// agree on which cones to march; within a class, neighbouring points share
+// texels.
 __global__ void k_sample_keys(const vct_surface_sample* __restrict__ s, int64_t n, float cx, float cy, float cz,
-                              float q, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+                              float q, unsigned long long* __restrict__ keys, uint32_t* __restrict__ vals) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const float* p = s[i].position;
-        const int x = min(max(__float2int_rd((p[0] - cx) * q) + 128, 0), 255);
-        const int y = min(max(__float2int_rd((p[1] - cy) * q) + 128, 0), 255);
-        const int z = min(max(__float2int_rd((p[2] - cz) * q) + 128, 0), 255);
+        const int x = min(max(__float2int_rd((p[0] - cx) * q) + 512, 0), 1023);
+        const int y = min(max(__float2int_rd((p[1] - cy) * q) + 512, 0), 1023);
+        const int z = min(max(__float2int_rd((p[2] - cz) * q) + 512, 0), 1023);
         const float* t = s[i].normal_texel;
         const float nx = t[0] * 2.0f - 1.0f, ny = t[1] * 2.0f - 1.0f, nz = t[2] * 2.0f - 1.0f;
         const float l1 = fabsf(nx) + fabsf(ny) + fabsf(nz);
@@ -97,31 +98,34 @@ __global__ void k_sample_keys(const vct_surface_sample* __restrict__ s, int64_t 
         }
         const int cu = min(max((int)((ox * 0.5f + 0.5f) * 8.0f), 0), 7);
         const int cv = min(max((int)((oy * 0.5f + 0.5f) * 8.0f), 0), 7);
-        keys[i] = ((uint32_t)(cv * 8 + cu) << 24) | spread_bits10(x) | (spread_bits10(y) << 1) | (spread_bits10(z) << 2);
+        keys[i] = ((unsigned long long)(cv * 8 + cu) << 30) |
+                  (spread_bits10(x) | (spread_bits10(y) << 1) | (spread_bits10(z) << 2));
         vals[i] = (uint32_t)i;
     }
 }
 
 int sample_coherent_order(const vct_surface_sample* samples, int64_t n, const vct_cone_tracing_desc& d,
-                        SampleOrder* out, cudaStream_t st) {
+                          SampleOrder* out, cudaStream_t st) {
     out->order = nullptr;
     out->block = nullptr;
     if (n <= 1 || n >= (1LL << 31)) return VCT_OK;
     size_t temp = 0;
-    VCT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(nullptr, temp, (uint32_t*)nullptr, (uint32_t*)nullptr,
-                                                 (uint32_t*)nullptr, (uint32_t*)nullptr, (int)n, 0, 30, st));
-    const size_t arr = (4 * (size_t)n + 255) & ~(size_t)255;
+    VCT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(nullptr, temp, (unsigned long long*)nullptr,
+                                                 (unsigned long long*)nullptr, (uint32_t*)nullptr, (uint32_t*)nullptr,
+                                                 (int)n, 0, 36, st));
+    const size_t arr4 = (4 * (size_t)n + 255) & ~(size_t)255, arr8 = (8 * (size_t)n + 255) & ~(size_t)255;
     char* b = nullptr;
-    VCT_CUDA_TRY(cudaMallocAsync((void**)&b, 4 * arr + temp, st));
-    uint32_t *keys = (uint32_t*)b, *keys_out = (uint32_t*)(b + arr), *vals = (uint32_t*)(b + 2 * arr),
-             *order = (uint32_t*)(b + 3 * arr);
+    VCT_CUDA_TRY(cudaMallocAsync((void**)&b, 2 * arr8 + 2 * arr4 + temp, st));
+    unsigned long long *keys = (unsigned long long*)b, *keys_out = (unsigned long long*)(b + arr8);
+    uint32_t *vals = (uint32_t*)(b + 2 * arr8), *order = (uint32_t*)(b + 2 * arr8 + arr4);
     int64_t g = (n + 255) / 256;
     k_sample_keys<<<(int)(g > 152 * 32 ? 152 * 32 : g), 256, 0, st>>>(samples, n, d.volume_center[0],
                                                                         d.volume_center[1], d.volume_center[2],
                                                                         0.5f / d.voxel_size, keys, vals);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess)
-        e = cub::DeviceRadixSort::SortPairs(b + 4 * arr, temp, keys, keys_out, vals, order, (int)n, 0, 30, st);
+        e = cub::DeviceRadixSort::SortPairs(b + 2 * arr8 + 2 * arr4, temp, keys, keys_out, vals, order, (int)n, 0, 36,
+                                            st);
     if (e != cudaSuccess) {
         cudaFreeAsync(b, st);
         return cuda_fail(e, "sample_coherent_order");

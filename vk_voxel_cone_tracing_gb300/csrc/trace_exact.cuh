@@ -10,23 +10,6 @@
 
 namespace vct {
 
-// A coherent processing order of G-buffer samples: radix-sorted by normal
-// class (6 bits, octahedral 8 x 8) and then by the Morton code of the
-// position on a grid of two level-0 voxels per cell around the volume centre
-// (8 bits per axis).  Per-sample results do not depend on the processing
-// order, so the per-thread kernels walk this permutation: a warp's lanes skip
-// the same diffuse cones and their texel fetches (and the adjoint's gradient
-// atomics) land on neighbouring cache lines.  Allocates its buffers
-// stream-ordered: `*block` is freed with cudaFreeAsync after the last kernel
-// that reads `*order`.  For n >= 2^31 it returns VCT_OK with *order = nullptr
-// (identity order).
-struct SampleOrder {
-    uint32_t* order = nullptr;
-    void* block = nullptr;
-};
-int sample_coherent_order(const vct_surface_sample* samples, int64_t n, const vct_cone_tracing_desc& d,
-                        SampleOrder* out, cudaStream_t st);
-
 struct ExactAtlas {
     const uint32_t* __restrict__ p;
     AtlasDims A;
