@@ -7,7 +7,12 @@
  * stream (`stream` is a cudaStream_t passed as void*, NULL = legacy default
  * stream).  All buffer pointers are DEVICE pointers unless the parameter name
  * ends in `_host`.  Nothing is allocated behind the caller's back except where
- * a function says so (texture objects, `vct_texture_*`).
+ * a function says so: texture objects (`vct_texture_*`), and stream-ordered
+ * scratch (cudaMallocAsync on the call's stream, freed on it with
+ * cudaFreeAsync before the call returns) in the per-sample traces
+ * (vct_cone_trace, vct_cone_trace_f32, vct_cone_trace_backward,
+ * vct_svo_cone_trace: the samples' processing order) and vct_sq_error.
+ * vct_cone_trace_fast_noalloc allocates nothing at all.
  *
  * Parameter structs keep the reference's byte layouts (std140 / push-constant
  * layouts of the GLSL blocks); the static asserts at the end of this header
@@ -279,7 +284,10 @@ int vct_wrap_border(uint32_t* atlas, const vct_border_wrapping_desc* desc, void*
  * sample) like the pass's two attachments.  `cone_steps` (optional, may be
  * NULL) receives += the number of traceCone loop iterations executed.
  * Exact form: FP32 arithmetic, trilinear weights in FP32 (no 8-bit filter
- * weights), reads the linear atlas. */
+ * weights), reads the linear atlas.  One thread per sample; the samples are
+ * walked in a coherent order (normal class, then Morton code of the
+ * position; stream-ordered scratch of 24 B per sample), which changes no
+ * output. */
 int vct_cone_trace(const vct_cone_tracing_desc* desc, const vct_cam_matrix* cam,
                    const uint32_t* radiance_atlas, int32_t clipmap_resolution,
                    const vct_shadow_map* shadow, const vct_directional_light_desc* light,
