@@ -249,15 +249,21 @@ def run_ours(args, world, rank, local):
     lsd = passes.light_shadow_desc(light_origin(), LIGHT_DIR)
     stream = torch.cuda.current_stream()
 
-    # the RGBA8 texture form samples a texture that the frame keeps equal to the radiance atlas (the frame's
-    # copy-alpha and mip passes store each texel into it too); the FP16 form refreshes its own texture
+    # the texture forms sample a texture the frame keeps equal to the atlas they trace: the RGBA8 form's
+    # through the frame's copy-alpha and mip passes, the FP16 form's through its conversion and FP16 mip
+    # passes (each texel those passes write is stored into the texture too)
     tex = clipmap.RadianceTexture(R, capi.TEX_RGBA8 if args.form != "fp16" else capi.TEX_RGBA16F) \
         if args.form in ("tex", "fp16") else None
     frame_tex = tex if args.form == "tex" else None
+    atlas16 = clipmap.new_atlas_rgba16f(R, dev) if args.form == "fp16" else None
 
     def frame(frame_index: int = 0):
-        return passes.clipmap_frame(ds, CAMERA, R, opacity, radiance, shadow, light, lsd, ws, texture=frame_tex,
+        regs = passes.clipmap_frame(ds, CAMERA, R, opacity, radiance, shadow, light, lsd, ws, texture=frame_tex,
                                     frame_index=frame_index)
+        if atlas16 is not None:  # FP16 form: RGBA16F radiance with FP16 mips, mirrored into its texture
+            clipmap.to_rgba16f(radiance, R, out=atlas16, mirror=tex)
+            clipmap.cmd_downsample_rgba16f_all(atlas16, R, regs, 1, mirror=tex)
+        return regs
 
     regs = frame()
     torch.cuda.synchronize()
@@ -269,11 +275,8 @@ def run_ours(args, world, rank, local):
     dout = torch.empty((n, 4), dtype=torch.float32, device=dev)
     sout = torch.empty((n, 4), dtype=torch.float32, device=dev)
     steps_ctr = torch.zeros(1, dtype=torch.int64, device=dev)
-    tex_src, scratch = radiance, None
+    tex_src, scratch = (atlas16 if atlas16 is not None else radiance), None
     if tex is not None:
-        if args.form == "fp16":
-            tex_src = clipmap.to_rgba16f(radiance, R)
-            clipmap.cmd_downsample_rgba16f_all(tex_src, R, regs, 1)
         scratch = clipmap.fast_scratch(n, dev)
 
     def trace(inp, counter=None):
@@ -281,8 +284,6 @@ def run_ours(args, world, rank, local):
             clipmap.cone_trace(desc, EYE, radiance, R, inp, light=light, shadow=shadow, shadow_desc=lsd,
                                diffuse=dout, specular=sout, steps=counter)
         else:
-            if frame_tex is None:
-                tex.update(tex_src)  # FP16 form: its texture is refreshed from the FP16 atlas every step
             clipmap.cone_trace_fast(desc, EYE, tex, inp, light=light, shadow=shadow, shadow_desc=lsd, diffuse=dout,
                                     specular=sout, steps=counter, scratch=scratch)
 
@@ -300,9 +301,9 @@ def run_ours(args, world, rank, local):
     value = total_cone_samples / (ms * 1e-3)
     # the trace's speed of light: the same fetches per cone sample with nothing else (vct_gather_probe)
     gather_peak = clipmap.gather_probe(desc, tex) if tex is not None else None
-    # what a full clipmap -> texture array copy (vct_texture_update) costs; the RGBA8 form needs none per step
+    # what a full clipmap -> texture array copy (vct_texture_update) costs; the texture forms need none per step
     refresh_ms = statistics.median(events_ms(stream, lambda: tex.update(tex_src), 5)[0]) if tex is not None else None
-    if frame_tex is not None:
+    if tex is not None:
         frame()  # the measurement above overwrote the texture with the same atlas; keep the frame's state
 
     # voxelise + shadow + inject + mips of one frame, and the SVO build at 256^3
@@ -488,7 +489,8 @@ def run_ours(args, world, rank, local):
                        "l2": "inputs larger than L2 (2.47 GB clipmap)",
                        "texture_full_copy_ms": refresh_ms,
                        "texture": "kept current by the frame's copy-alpha and mip passes" if frame_tex is not None
-                       else ("refreshed by a full copy every trace step" if tex is not None else "none (linear atlas)"),
+                       else ("kept current by the frame's FP16 conversion and FP16 mip passes" if tex is not None
+                             else "none (linear atlas)"),
                        "voxelize_inject_mip_ms": frame_ms, "svo_ms": svo_ms, "svo_level": SVO_LEVEL,
                        "svo_fragments": int(frags.shape[0]), "svo_nodes": int(nodes.value),
                        "svo_trace": {"samples": svo_n, "ms": svo_trace_ms, "cone_samples_per_s": svo_trace_rate},

@@ -373,9 +373,14 @@ int vct_texture_destroy(vct_texture tex);
 /* FP16-storage form of the radiance clipmap (4 halves per texel, same
  * layout): conversion of an RGBA8 atlas, and the anisotropic downsample of
  * radianceDownSample.comp / opacityDownSample.comp with FP32 arithmetic and
- * RGBA16F storage (no 8-bit quantisation of the mips). */
-int vct_atlas_rgba8_to_rgba16f(const uint32_t* src, uint16_t* dst, int32_t clipmap_resolution, void* stream);
-int vct_downsample_rgba16f(uint16_t* atlas, const vct_downsample_desc* desc, int32_t mode, void* stream);
+ * RGBA16F storage (no 8-bit quantisation of the mips).  `mirror` (may be
+ * NULL) is an RGBA16F texture of the same resolution: every texel written is
+ * stored into it too, so a conversion followed by the level mips leaves it
+ * equal to the FP16 atlas without a vct_texture_update. */
+int vct_atlas_rgba8_to_rgba16f(const uint32_t* src, uint16_t* dst, int32_t clipmap_resolution,
+                               struct vct_texture_s* mirror, void* stream);
+int vct_downsample_rgba16f(uint16_t* atlas, const vct_downsample_desc* desc, int32_t mode,
+                           struct vct_texture_s* mirror, void* stream);
 
 /* Bytes of caller-provided scratch vct_cone_trace_fast needs for
  * `sample_count` samples (-1 if the count is out of range). */

@@ -165,6 +165,33 @@ def test_fp16_form_trace_matches_fp64(cuda, oracle):
     tex.close()
 
 
+def test_fp16_passes_keep_their_texture_current(cuda, oracle):
+    """The FP16 conversion and mips with a mirror texture leave the texture equal to the FP16 atlas, texel for
+    texel, with no vct_texture_update (a texture refreshed by a copy is the reference); a mirror of the wrong
+    format or resolution is refused."""
+    torch = cuda
+    from vk_voxel_cone_tracing_gb300 import capi, clipmap
+    from vk_voxel_cone_tracing_gb300.scene import random_atlas
+    R = 32
+    atlas = _dev(torch, random_atlas(R, seed=5, fill=0.3))
+    creg = clipmap.clip_regions((0.7, 0.2, -1.1), R)
+    mirrored = clipmap.RadianceTexture(R, capi.TEX_RGBA16F)
+    a16 = clipmap.to_rgba16f(atlas, R, mirror=mirrored)
+    clipmap.cmd_downsample_rgba16f_all(a16, R, creg, 1, mirror=mirrored)
+    back = mirrored.read(torch.empty_like(a16))
+    copied = clipmap.RadianceTexture(R, capi.TEX_RGBA16F).update(a16)
+    back2 = copied.read(torch.empty_like(a16))
+    torch.cuda.synchronize()
+    assert torch.equal(back, a16) and torch.equal(back2, a16)
+    assert (a16 != 0).any()
+    with pytest.raises(capi.VctError):
+        clipmap.to_rgba16f(atlas, R, out=a16, mirror=clipmap.RadianceTexture(R, capi.TEX_RGBA8))
+    with pytest.raises(capi.VctError):
+        clipmap.cmd_downsample_rgba16f(a16, R, (0, 0, 0), 1, 1, mirror=clipmap.RadianceTexture(16, capi.TEX_RGBA16F))
+    mirrored.close()
+    copied.close()
+
+
 def test_gather_probe_reports_a_finite_rate_and_checks_arguments(cuda, oracle):
     """The roofline probe (no reference counterpart) runs the fetch pattern of
     one cone sample per step and reports a positive rate; bad arguments are

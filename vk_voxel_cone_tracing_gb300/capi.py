@@ -197,8 +197,8 @@ _SIGS: dict[str, tuple] = {
     "vct_texture_update": (C.c_int, [P, P, P]),
     "vct_texture_read": (C.c_int, [P, P, P]),
     "vct_texture_destroy": (C.c_int, [P]),
-    "vct_atlas_rgba8_to_rgba16f": (C.c_int, [P, P, C.c_int32, P]),
-    "vct_downsample_rgba16f": (C.c_int, [P, P, C.c_int32, P]),
+    "vct_atlas_rgba8_to_rgba16f": (C.c_int, [P, P, C.c_int32, P, P]),
+    "vct_downsample_rgba16f": (C.c_int, [P, P, C.c_int32, P, P]),
     "vct_cone_trace_fast_scratch_bytes": (C.c_int64, [C.c_int64]),
     "vct_cone_trace_fast": (C.c_int, [P, P, P, P, P, P, P, C.c_int64, P, P, P, P, C.c_size_t, P]),
     "vct_gather_probe": (C.c_int, [P, P, C.c_int64, C.c_int32, P, P]),

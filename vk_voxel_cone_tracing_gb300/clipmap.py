@@ -163,22 +163,29 @@ def new_atlas_rgba16f(R: int, device="cuda") -> torch.Tensor:
     return torch.zeros((d, h, w * 4), dtype=torch.int16, device=device)
 
 
-def to_rgba16f(atlas: torch.Tensor, R: int, out: torch.Tensor | None = None) -> torch.Tensor:
+def _mirror(tex: "RadianceTexture | None"):
+    return None if tex is None else tex.handle
+
+
+def to_rgba16f(atlas: torch.Tensor, R: int, out: torch.Tensor | None = None,
+               mirror: "RadianceTexture | None" = None) -> torch.Tensor:
+    """The RGBA8 atlas as RGBA16F; `mirror` (an RGBA16F RadianceTexture) receives every texel too."""
     out = new_atlas_rgba16f(R, atlas.device) if out is None else out
-    capi.call("vct_atlas_rgba8_to_rgba16f", _ptr(atlas), _ptr(out), R, _stream())
+    capi.call("vct_atlas_rgba8_to_rgba16f", _ptr(atlas), _ptr(out), R, _mirror(mirror), _stream())
     return out
 
 
 def cmd_downsample_rgba16f(atlas16: torch.Tensor, R: int, prev_region_min, level: int, mode: int,
-                           band: int = capi.DOWNSAMPLE_REGION_SIZE) -> None:
+                           band: int = capi.DOWNSAMPLE_REGION_SIZE, mirror: "RadianceTexture | None" = None) -> None:
     d = capi.DownSampleDesc(capi.i3(*prev_region_min), level, R, band)
-    capi.call("vct_downsample_rgba16f", _ptr(atlas16), capi.ref(d), mode, _stream())
+    capi.call("vct_downsample_rgba16f", _ptr(atlas16), capi.ref(d), mode, _mirror(mirror), _stream())
 
 
-def cmd_downsample_rgba16f_all(atlas16: torch.Tensor, R: int, regions, mode: int) -> None:
+def cmd_downsample_rgba16f_all(atlas16: torch.Tensor, R: int, regions, mode: int,
+                               mirror: "RadianceTexture | None" = None) -> None:
     for level in range(1, 6):
         prev = regions[level - 1].min_corner
-        cmd_downsample_rgba16f(atlas16, R, (prev[0], prev[1], prev[2]), level, mode)
+        cmd_downsample_rgba16f(atlas16, R, (prev[0], prev[1], prev[2]), level, mode, mirror=mirror)
 
 
 def fast_scratch(n: int, device="cuda") -> torch.Tensor:

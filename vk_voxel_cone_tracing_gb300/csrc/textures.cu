@@ -40,13 +40,20 @@ __global__ void k_surface_zero(cudaSurfaceObject_t s, int W, int H, int D, int t
 __device__ __forceinline__ uint16_t h_bits(float x) { return __half_as_ushort(__float2half_rn(x)); }
 __device__ __forceinline__ float h_val(uint16_t b) { return __half2float(__ushort_as_half(b)); }
 
-__global__ void k_rgba8_to_rgba16f(const uint32_t* __restrict__ src, uint2* __restrict__ dst, int64_t n) {
+// `mirror` (0 = none): an RGBA16F texture array of the same atlas; every
+// texel written is stored into it as well, so it needs no copy afterwards.
+__global__ void k_rgba8_to_rgba16f(const uint32_t* __restrict__ src, uint2* __restrict__ dst, int64_t n, int W, int H,
+                                   cudaSurfaceObject_t mirror) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         float4 c = unpack_rgba8(__ldg(src + i));
         uint2 o;
         o.x = (uint32_t)h_bits(c.x) | ((uint32_t)h_bits(c.y) << 16);
         o.y = (uint32_t)h_bits(c.z) | ((uint32_t)h_bits(c.w) << 16);
         dst[i] = o;
+        if (mirror) {
+            const int64_t r = i / W;
+            surf3Dwrite(o, mirror, (int)(i - r * W) * 8, (int)(r % H), (int)(r / H));
+        }
     }
 }
 
@@ -60,17 +67,19 @@ __device__ __forceinline__ float4 load_h4(const uint2* p, int64_t i) {
     uint2 v = p[i];
     return make_float4(h_val(v.x & 0xffff), h_val(v.x >> 16), h_val(v.y & 0xffff), h_val(v.y >> 16));
 }
-__device__ __forceinline__ void store_h4(uint2* p, int64_t i, float4 c) {
+__device__ __forceinline__ uint2 store_h4(uint2* p, int64_t i, float4 c) {
     uint2 o;
     o.x = (uint32_t)h_bits(c.x) | ((uint32_t)h_bits(c.y) << 16);
     o.y = (uint32_t)h_bits(c.z) | ((uint32_t)h_bits(c.w) << 16);
     p[i] = o;
+    return o;
 }
 
 // Same composite and band blend as the RGBA8 downsample (opacityDownSample.comp /
 // radianceDownSample.comp), FP32 arithmetic, RGBA16F storage.
 template <int MODE>
-__global__ void k_downsample_f16(uint2* __restrict__ atlas, AtlasDims A, int3 pmin, int level, int band) {
+__global__ void k_downsample_f16(uint2* __restrict__ atlas, AtlasDims A, int3 pmin, int level, int band,
+                                 cudaSurfaceObject_t mirror) {
     const int half = A.R >> 1;
     const int64_t n = (int64_t)half * half * half;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
@@ -119,11 +128,13 @@ __global__ void k_downsample_f16(uint2* __restrict__ atlas, AtlasDims A, int3 pm
                 float a = s.w * 0.25f * (1.0f - lerp) + own.x * lerp;
                 own.w = a;
                 own.y = a;
-                store_h4(atlas, wi, own);
+                const uint2 o = store_h4(atlas, wi, own);
+                if (mirror) surf3Dwrite(o, mirror, (wpos[0] + A.rb * f) * 8, wpos[1], wpos[2]);
             } else {
                 float4 o = make_float4(s.x * 0.25f * (1.0f - lerp) + own.x * lerp, s.y * 0.25f * (1.0f - lerp) + own.y * lerp,
                                        s.z * 0.25f * (1.0f - lerp) + own.z * lerp, s.w * 0.25f * (1.0f - lerp) + own.w * lerp);
-                store_h4(atlas, wi, o);
+                const uint2 b = store_h4(atlas, wi, o);
+                if (mirror) surf3Dwrite(b, mirror, (wpos[0] + A.rb * f) * 8, wpos[1], wpos[2]);
             }
         }
     }
@@ -216,16 +227,32 @@ extern "C" int vct_texture_destroy(vct_texture_s* t) {
     return VCT_OK;
 }
 
-extern "C" int vct_atlas_rgba8_to_rgba16f(const uint32_t* src, uint16_t* dst, int32_t R, void* stream) {
+static int fp16_mirror(const vct_texture_s* mirror, int R, const char* fn, cudaSurfaceObject_t* out) {
+    *out = 0;
+    if (!mirror) return VCT_OK;
+    if (mirror->format != VCT_TEX_RGBA16F || mirror->R != R || !mirror->surf)
+        return fail(VCT_E_BAD_ARG, std::string(fn) + ": the mirror must be an RGBA16F texture of the same resolution");
+    *out = mirror->surf;
+    return VCT_OK;
+}
+
+extern "C" int vct_atlas_rgba8_to_rgba16f(const uint32_t* src, uint16_t* dst, int32_t R, vct_texture_s* mirror,
+                                          void* stream) {
     VCT_CHECK_ARG(src && dst && valid_resolution(R), "vct_atlas_rgba8_to_rgba16f: bad argument");
     VCT_CHECK_ARG(((uintptr_t)dst & 7) == 0, "vct_atlas_rgba8_to_rgba16f: destination must be 8-byte aligned");
-    const int64_t n = AtlasDims(R).texels();
-    k_rgba8_to_rgba16f<<<grid_for16(n, 256), 256, 0, as_stream(stream)>>>(src, reinterpret_cast<uint2*>(dst), n);
+    cudaSurfaceObject_t surf;
+    int rc = fp16_mirror(mirror, R, "vct_atlas_rgba8_to_rgba16f", &surf);
+    if (rc != VCT_OK) return rc;
+    AtlasDims A(R);
+    const int64_t n = A.texels();
+    k_rgba8_to_rgba16f<<<grid_for16(n, 256), 256, 0, as_stream(stream)>>>(src, reinterpret_cast<uint2*>(dst), n, A.W,
+                                                                           A.H, surf);
     VCT_LAUNCH_CHECK();
     return VCT_OK;
 }
 
-extern "C" int vct_downsample_rgba16f(uint16_t* atlas, const vct_downsample_desc* d, int32_t mode, void* stream) {
+extern "C" int vct_downsample_rgba16f(uint16_t* atlas, const vct_downsample_desc* d, int32_t mode,
+                                      vct_texture_s* mirror, void* stream) {
     VCT_CHECK_ARG(atlas && d, "vct_downsample_rgba16f: null argument");
     VCT_CHECK_ARG(((uintptr_t)atlas & 7) == 0, "vct_downsample_rgba16f: atlas must be 8-byte aligned");
     VCT_CHECK_ARG(valid_resolution(d->clipmap_resolution), "vct_downsample_rgba16f: bad resolution");
@@ -237,10 +264,15 @@ extern "C" int vct_downsample_rgba16f(uint16_t* atlas, const vct_downsample_desc
     const int64_t n = (int64_t)half * half * half;
     int3 pm = make_int3(d->prev_region_min_corner[0], d->prev_region_min_corner[1], d->prev_region_min_corner[2]);
     uint2* a = reinterpret_cast<uint2*>(atlas);
+    cudaSurfaceObject_t surf;
+    int rc = fp16_mirror(mirror, A.R, "vct_downsample_rgba16f", &surf);
+    if (rc != VCT_OK) return rc;
     if (mode == 0)
-        k_downsample_f16<0><<<grid_for16(n, 128), 128, 0, as_stream(stream)>>>(a, A, pm, d->clip_level, d->downsample_region_size);
+        k_downsample_f16<0><<<grid_for16(n, 128), 128, 0, as_stream(stream)>>>(a, A, pm, d->clip_level,
+                                                                              d->downsample_region_size, surf);
     else
-        k_downsample_f16<1><<<grid_for16(n, 128), 128, 0, as_stream(stream)>>>(a, A, pm, d->clip_level, d->downsample_region_size);
+        k_downsample_f16<1><<<grid_for16(n, 128), 128, 0, as_stream(stream)>>>(a, A, pm, d->clip_level,
+                                                                              d->downsample_region_size, surf);
     VCT_LAUNCH_CHECK();
     return VCT_OK;
 }
