@@ -42,17 +42,21 @@ __device__ __forceinline__ float h_val(uint16_t b) { return __half2float(__ushor
 
 // `mirror` (0 = none): an RGBA16F texture array of the same atlas; every
 // texel written is stored into it as well, so it needs no copy afterwards.
-__global__ void k_rgba8_to_rgba16f(const uint32_t* __restrict__ src, uint2* __restrict__ dst, int64_t n, int W, int H,
+// One block per atlas row (y, z) at a time, the row's texels across the
+// threads: the surface coordinates cost no 64-bit division per texel.
+__global__ void k_rgba8_to_rgba16f(const uint32_t* __restrict__ src, uint2* __restrict__ dst, int W, int H, int D,
                                    cudaSurfaceObject_t mirror) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        float4 c = unpack_rgba8(__ldg(src + i));
-        uint2 o;
-        o.x = (uint32_t)h_bits(c.x) | ((uint32_t)h_bits(c.y) << 16);
-        o.y = (uint32_t)h_bits(c.z) | ((uint32_t)h_bits(c.w) << 16);
-        dst[i] = o;
-        if (mirror) {
-            const int64_t r = i / W;
-            surf3Dwrite(o, mirror, (int)(i - r * W) * 8, (int)(r % H), (int)(r / H));
+    const int rows = H * D;
+    for (int row = blockIdx.x; row < rows; row += gridDim.x) {
+        const int y = row % H, z = row / H;
+        const int64_t base = (int64_t)row * W;
+        for (int x = threadIdx.x; x < W; x += blockDim.x) {
+            float4 c = unpack_rgba8(__ldg(src + base + x));
+            uint2 o;
+            o.x = (uint32_t)h_bits(c.x) | ((uint32_t)h_bits(c.y) << 16);
+            o.y = (uint32_t)h_bits(c.z) | ((uint32_t)h_bits(c.w) << 16);
+            dst[base + x] = o;
+            if (mirror) surf3Dwrite(o, mirror, x * 8, y, z);
         }
     }
 }
@@ -244,9 +248,9 @@ extern "C" int vct_atlas_rgba8_to_rgba16f(const uint32_t* src, uint16_t* dst, in
     int rc = fp16_mirror(mirror, R, "vct_atlas_rgba8_to_rgba16f", &surf);
     if (rc != VCT_OK) return rc;
     AtlasDims A(R);
-    const int64_t n = A.texels();
-    k_rgba8_to_rgba16f<<<grid_for16(n, 256), 256, 0, as_stream(stream)>>>(src, reinterpret_cast<uint2*>(dst), n, A.W,
-                                                                           A.H, surf);
+    const int rows = A.H * A.D;
+    k_rgba8_to_rgba16f<<<rows < 152 * 64 ? rows : 152 * 64, 256, 0, as_stream(stream)>>>(
+        src, reinterpret_cast<uint2*>(dst), A.W, A.H, A.D, surf);
     VCT_LAUNCH_CHECK();
     return VCT_OK;
 }
