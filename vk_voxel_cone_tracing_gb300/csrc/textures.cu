@@ -42,22 +42,28 @@ __device__ __forceinline__ float h_val(uint16_t b) { return __half2float(__ushor
 
 // `mirror` (0 = none): an RGBA16F texture array of the same atlas; every
 // texel written is stored into it as well, so it needs no copy afterwards.
-// One block per atlas row (y, z) at a time, the row's texels across the
-// threads: the surface coordinates cost no 64-bit division per texel.
-__global__ void k_rgba8_to_rgba16f(const uint32_t* __restrict__ src, uint2* __restrict__ dst, int W, int H, int D,
-                                   cudaSurfaceObject_t mirror) {
-    const int rows = H * D;
-    for (int row = blockIdx.x; row < rows; row += gridDim.x) {
-        const int y = row % H, z = row / H;
-        const int64_t base = (int64_t)row * W;
-        for (int x = threadIdx.x; x < W; x += blockDim.x) {
-            float4 c = unpack_rgba8(__ldg(src + base + x));
-            uint2 o;
-            o.x = (uint32_t)h_bits(c.x) | ((uint32_t)h_bits(c.y) << 16);
-            o.y = (uint32_t)h_bits(c.z) | ((uint32_t)h_bits(c.w) << 16);
-            dst[base + x] = o;
-            if (mirror) surf3Dwrite(o, mirror, x * 8, y, z);
-        }
+// A block converts a 16 x 16 tile of one depth slice, each warp two
+// neighbouring rows of 16 texels: a 32-byte sector of the array's
+// block-linear layout holds two texels of two neighbouring rows, so every
+// sector a warp writes is written whole (row-by-row warps wrote half sectors
+// and paid a read-modify-write for each).
+__global__ void __launch_bounds__(256) k_rgba8_to_rgba16f(const uint32_t* __restrict__ src, uint2* __restrict__ dst,
+                                                          int W, int H, int D, cudaSurfaceObject_t mirror) {
+    const int tx = (W + 15) >> 4, ty = (H + 15) >> 4;
+    const int64_t tiles = (int64_t)tx * ty * D;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int64_t t = blockIdx.x; t < tiles; t += gridDim.x) {
+        const int z = (int)(t / ((int64_t)tx * ty));
+        const int r = (int)(t - (int64_t)z * tx * ty);
+        const int x = ((r % tx) << 4) + (lane & 15), y = ((r / tx) << 4) + 2 * warp + (lane >> 4);
+        if (x >= W || y >= H) continue;
+        const int64_t i = ((int64_t)z * H + y) * W + x;
+        float4 c = unpack_rgba8(__ldg(src + i));
+        uint2 o;
+        o.x = (uint32_t)h_bits(c.x) | ((uint32_t)h_bits(c.y) << 16);
+        o.y = (uint32_t)h_bits(c.z) | ((uint32_t)h_bits(c.w) << 16);
+        dst[i] = o;
+        if (mirror) surf3Dwrite(o, mirror, x * 8, y, z);
     }
 }
 
@@ -248,8 +254,8 @@ extern "C" int vct_atlas_rgba8_to_rgba16f(const uint32_t* src, uint16_t* dst, in
     int rc = fp16_mirror(mirror, R, "vct_atlas_rgba8_to_rgba16f", &surf);
     if (rc != VCT_OK) return rc;
     AtlasDims A(R);
-    const int rows = A.H * A.D;
-    k_rgba8_to_rgba16f<<<rows < 152 * 64 ? rows : 152 * 64, 256, 0, as_stream(stream)>>>(
+    const int64_t tiles = (int64_t)((A.W + 15) >> 4) * ((A.H + 15) >> 4) * A.D;
+    k_rgba8_to_rgba16f<<<(int)(tiles < 152 * 64 ? tiles : 152 * 64), 256, 0, as_stream(stream)>>>(
         src, reinterpret_cast<uint2*>(dst), A.W, A.H, A.D, surf);
     VCT_LAUNCH_CHECK();
     return VCT_OK;
