@@ -42,12 +42,33 @@ __device__ __forceinline__ uint32_t rgb_of(const uint32_t* __restrict__ atlas, c
     return ((w >> (i & 31)) & 1u) ? (r & 0x00ffffffu) : 0u;
 }
 
+// Texel order of the passes that also store into a texture: a warp takes 16
+// x-neighbours of two neighbouring rows, so each 32-byte sector of the
+// array's block-linear layout (16 B of two neighbouring rows) is written
+// whole -- row-by-row warps half-filled every sector and paid a DRAM
+// read-modify-write for each.  t -> (x, y, z) of a 2^lg cube, a bijection.
+__device__ __forceinline__ void cube_texel(uint32_t t, int lg, int& x, int& y, int& z) {
+    const uint32_t m = (1u << lg) - 1u;
+    if (lg >= 4) {
+        x = (int)((t & 15u) | (((t >> 5) & (m >> 4)) << 4));
+        y = (int)(((t >> 4) & 1u) | (((t >> (lg + 1)) & (m >> 1)) << 1));
+    } else {
+        x = (int)(t & m);
+        y = (int)((t >> lg) & m);
+    }
+    z = (int)(t >> (2 * lg));
+}
+
 __global__ void k_copy_alpha(uint32_t* __restrict__ dst, const uint32_t* __restrict__ src, AtlasDims A, int level,
                              int lg, cudaSurfaceObject_t mirror, const uint32_t* __restrict__ touched) {
     const int f = blockIdx.y;
-    const uint32_t n = 1u << (3 * lg), m = (1u << lg) - 1u;
+    const uint32_t n = 1u << (3 * lg);
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        const int x = (int)(t & m) + 1 + A.rb * f, y = (int)((t >> lg) & m) + 1 + level * A.rb, z = (int)(t >> (2 * lg)) + 1;
+        int x, y, z;
+        cube_texel(t, lg, x, y, z);
+        x += 1 + A.rb * f;
+        y += 1 + level * A.rb;
+        z += 1;
         const int64_t i = A.index(x, y, z);
         const uint32_t v = rgb_of(dst, touched, i) | (__ldg(src + i) & 0xff000000u);
         dst[i] = v;
@@ -195,11 +216,12 @@ __global__ void __launch_bounds__(128, 8) k_alpha_downsample(uint32_t* __restric
                                    int3 pmin, int level, int band, int lg, cudaSurfaceObject_t mirror,
                                    const uint32_t* __restrict__ touched) {
     const int half = A.R >> 1;
-    const uint32_t n = 1u << (3 * lg), m = (1u << lg) - 1u;
+    const uint32_t n = 1u << (3 * lg);
     const int pm[3] = {pmin.x, pmin.y, pmin.z};
     const float inv = 1.0f / __fadd_rn((float)band, 1.0f);
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        const int w[3] = {(int)(t & m), (int)((t >> lg) & m), (int)(t >> (2 * lg))};
+        int w[3];
+        cube_texel(t, lg, w[0], w[1], w[2]);
         int cur[3], ps[3];
         bool target = true;
 #pragma unroll
