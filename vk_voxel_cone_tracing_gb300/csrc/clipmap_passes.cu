@@ -45,8 +45,9 @@ __device__ __forceinline__ uint32_t rgb_of(const uint32_t* __restrict__ atlas, c
 // Texel order of the passes that also store into a texture: a warp takes 16
 // x-neighbours of two neighbouring rows, so each 32-byte sector of the
 // array's block-linear layout (16 B of two neighbouring rows) is written
-// whole -- row-by-row warps half-filled every sector and paid a DRAM
-// read-modify-write for each.  t -> (x, y, z) of a 2^lg cube, a bijection.
+// whole by one warp.  (On the 8-byte FP16 conversion, row-by-row warps cost
+// a DRAM read-modify-write per sector; with these 4-byte texels the frame
+// time is the same either way.)  t -> (x, y, z) of a 2^lg cube, a bijection.
 __device__ __forceinline__ void cube_texel(uint32_t t, int lg, int& x, int& y, int& z) {
     const uint32_t m = (1u << lg) - 1u;
     if (lg >= 4) {
