@@ -78,6 +78,9 @@ def lib():
         L.vcto_voxelization_desc.argtypes = [P, C.c_int, C.c_int, P]
         L.vcto_light_shadow_desc.argtypes = [P, P, C.c_float, C.c_float, P]
         L.vcto_voxelize_opacity.argtypes = [P, C.c_int, P, P, C.c_int]
+        L.vcto_voxelize_conservative.argtypes = [P, C.c_int, P, P, C.c_int]
+        L.vcto_cons_overlap.restype = C.c_int
+        L.vcto_cons_overlap.argtypes = [P, P, C.c_int, C.c_int, C.c_int, C.c_int]
         L.vcto_shadow_depth.argtypes = [P, P, P, C.c_int, C.c_int]
         L.vcto_camera_matrix.argtypes = [P, P, P, C.c_float, C.c_float, P]
         L.vcto_inverse4.argtypes = [P, P]
@@ -262,6 +265,25 @@ def voxelize_opacity(scene, R: int, regions: np.ndarray, level_mask: int = 0x3F,
     sv = scene_view(scene)
     lib().vcto_voxelize_opacity(C.byref(sv), R, _p(_regions_arg(regions)), _p(atlas), level_mask)
     return atlas
+
+
+def voxelize_conservative(scene, R: int, regions: np.ndarray, level_mask: int = 0x3F,
+                          atlas: np.ndarray | None = None) -> np.ndarray:
+    """The conservative voxelisation mode (triangle / box overlap, Schwarz & Seidel 2010) into an opacity
+    atlas: every voxel of each level's region that a triangle touches."""
+    if atlas is None:
+        atlas = np.zeros((R + 2, 6 * (R + 2), 6 * (R + 2)), np.uint32)
+    sv = scene_view(scene)
+    lib().vcto_voxelize_conservative(C.byref(sv), R, _p(_regions_arg(regions)), _p(atlas), level_mask)
+    return atlas
+
+
+def cons_overlap(tri, region_row, R: int, i: int, j: int, k: int) -> bool:
+    """One overlap decision of the conservative mode: triangle (3 x 3 world floats) against voxel (i, j, k)
+    of the region given as one clip_regions row."""
+    t = np.ascontiguousarray(tri, np.float32).reshape(9)
+    rg = np.ascontiguousarray(region_row, np.int32).reshape(7)
+    return bool(lib().vcto_cons_overlap(_p(t), _p(rg), R, i, j, k))
 
 
 def shadow_depth(scene, shadow_desc_bytes: bytes, W: int, H: int) -> np.ndarray:

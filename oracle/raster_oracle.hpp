@@ -461,6 +461,118 @@ inline void voxelize_opacity(const SceneView& s, int R, const Region regions[6],
     }
 }
 
+// -------------------------------------------------- conservative voxels
+// The conservative voxelisation mode (an extension beside the MSAA voxeliser
+// the reference runs): every voxel of a level's region that the triangle
+// touches, by the triangle / box overlap test of M. Schwarz and H.-P. Seidel,
+// "Fast parallel surface and solid voxelization on GPUs" (SIGGRAPH Asia 2010,
+// section 3.1): the box overlaps the triangle's plane (the plane's values at
+// the box's two critical corners differ in sign or vanish) and, in each of
+// the three axis projections, lies on the inner side of every edge line
+// shifted outward by the box's extent.  FP32 throughout, no contraction, in
+// the level's voxel units u = p * (1 / voxel_size) - min_corner, the voxel
+// (i, j, k) being the box [i, i+1] x [j, j+1] x [k, k+1]; the voxel is stored
+// (opacity 1.0 in all six faces) at its toroidal texel, as msaaVoxelizer.frag
+// stores.  Materials with an occlusion texture below 0.1 are skipped, as there.
+struct ConsTri {
+    float u[3][3];     // vertices in voxel units
+    float n[3];        // (u1 - u0) x (u2 - u0)
+    float d1, d2;      // plane offsets at the critical corners
+    float ne[3][3][2]; // [projection xy, yz, zx][edge][2] edge normals
+    float de[3][3];    // [projection][edge] offsets
+    int lo[3], hi[3];  // voxel bounds in [0, R)
+    bool ok;
+};
+
+inline float fmax0(float x) { return x > 0.0f ? x : 0.0f; }
+
+inline ConsTri cons_setup(const V3<float> p[3], const Region& rg, int R) {
+    ConsTri t;
+    const float inv = 1.0f / rg.voxel_size;
+    for (int k = 0; k < 3; ++k) {
+        const float w[3] = {p[k].x, p[k].y, p[k].z};
+        for (int a = 0; a < 3; ++a) t.u[k][a] = w[a] * inv - (float)rg.min_corner[a];
+    }
+    t.ok = true;
+    for (int a = 0; a < 3; ++a) {
+        const float mn = std::min(std::min(t.u[0][a], t.u[1][a]), t.u[2][a]);
+        const float mx = std::max(std::max(t.u[0][a], t.u[1][a]), t.u[2][a]);
+        const float fl = std::floor(mn), fh = std::floor(mx);
+        t.lo[a] = fl < 0.0f ? 0 : (fl > (float)(R - 1) ? R : (int)fl);
+        t.hi[a] = fh > (float)(R - 1) ? R - 1 : (fh < 0.0f ? -1 : (int)fh);
+        if (t.lo[a] > t.hi[a]) t.ok = false;
+    }
+    float e0[3], e1[3];
+    for (int a = 0; a < 3; ++a) {
+        e0[a] = t.u[1][a] - t.u[0][a];
+        e1[a] = t.u[2][a] - t.u[0][a];
+    }
+    t.n[0] = e0[1] * e1[2] - e0[2] * e1[1];
+    t.n[1] = e0[2] * e1[0] - e0[0] * e1[2];
+    t.n[2] = e0[0] * e1[1] - e0[1] * e1[0];
+    float c[3], c2[3];
+    for (int a = 0; a < 3; ++a) {
+        c[a] = t.n[a] > 0.0f ? 1.0f : 0.0f;
+        c2[a] = 1.0f - c[a];
+    }
+    t.d1 = t.n[0] * (c[0] - t.u[0][0]) + t.n[1] * (c[1] - t.u[0][1]) + t.n[2] * (c[2] - t.u[0][2]);
+    t.d2 = t.n[0] * (c2[0] - t.u[0][0]) + t.n[1] * (c2[1] - t.u[0][1]) + t.n[2] * (c2[2] - t.u[0][2]);
+    // projection q onto axes (a0, a1), oriented by the sign of the normal's third component
+    static const int kAx[3][3] = {{0, 1, 2}, {1, 2, 0}, {2, 0, 1}};
+    for (int q = 0; q < 3; ++q) {
+        const int a0 = kAx[q][0], a1 = kAx[q][1], a2 = kAx[q][2];
+        const float sg = t.n[a2] >= 0.0f ? 1.0f : -1.0f;
+        for (int e = 0; e < 3; ++e) {
+            const float* v0 = t.u[e];
+            const float* v1 = t.u[(e + 1) % 3];
+            const float n0 = -(v1[a1] - v0[a1]) * sg, n1 = (v1[a0] - v0[a0]) * sg;
+            t.ne[q][e][0] = n0;
+            t.ne[q][e][1] = n1;
+            t.de[q][e] = -(n0 * v0[a0] + n1 * v0[a1]) + fmax0(n0) + fmax0(n1);
+        }
+    }
+    return t;
+}
+
+// The three tests assume the box lies in the triangle's bounding box (the
+// loop visits only those boxes); the first line makes the decision standalone.
+inline bool cons_overlap(const ConsTri& t, int i, int j, int k) {
+    if (i < t.lo[0] || i > t.hi[0] || j < t.lo[1] || j > t.hi[1] || k < t.lo[2] || k > t.hi[2]) return false;
+    const float p[3] = {(float)i, (float)j, (float)k};
+    const float np = t.n[0] * p[0] + t.n[1] * p[1] + t.n[2] * p[2];
+    if ((np + t.d1) * (np + t.d2) > 0.0f) return false;
+    static const int kAx[3][2] = {{0, 1}, {1, 2}, {2, 0}};
+    for (int q = 0; q < 3; ++q)
+        for (int e = 0; e < 3; ++e)
+            if (t.ne[q][e][0] * p[kAx[q][0]] + t.ne[q][e][1] * p[kAx[q][1]] + t.de[q][e] < 0.0f) return false;
+    return true;
+}
+
+inline void voxelize_conservative(const SceneView& s, int R, const Region regions[6], uint32_t* atlas,
+                                  int level_mask) {
+    Atlas A(R);
+    for (int64_t t = 0; t < s.triangle_count; ++t) {
+        WorldTri w = world_triangle(s, t);
+        const Material& mat = s.materials[w.material];
+        if (mat.occlusion_texture > -1 && texture_1x1(s, mat.occlusion_texture).x < 0.1f) continue;
+        for (int level = 0; level < 6; ++level) {
+            if (!((level_mask >> level) & 1)) continue;
+            const Region& rg = regions[level];
+            const ConsTri ct = cons_setup(w.p, rg, R);
+            if (!ct.ok) continue;
+            for (int k = ct.lo[2]; k <= ct.hi[2]; ++k)
+                for (int j = ct.lo[1]; j <= ct.hi[1]; ++j)
+                    for (int i = ct.lo[0]; i <= ct.hi[0]; ++i) {
+                        if (!cons_overlap(ct, i, j, k)) continue;
+                        const int x = (((rg.min_corner[0] + i) % R) + R) % R + 1;
+                        const int y = (((rg.min_corner[1] + j) % R) + R) % R + 1 + (R + 2) * level;
+                        const int z = (((rg.min_corner[2] + k) % R) + R) % R + 1;
+                        for (int f = 0; f < 6; ++f) atlas[A.index(x + (R + 2) * f, y, z)] = 0xFFFFFFFFu;
+                    }
+        }
+    }
+}
+
 // The toroidal update of the opacity atlas (VoxelizationPass.cpp:127-141,
 // 190-212 with fillRevoxelizationRegions' slabs): clear each slab at its
 // wrapped corner, then voxelise the levels with slabs keeping only the

@@ -145,6 +145,16 @@ void vcto_light_shadow_desc(const float origin[3], const float direction[3], flo
 void vcto_voxelize_opacity(const SceneView* s, int R, const Region regions[6], uint32_t* atlas, int level_mask) {
     voxelize_opacity(*s, R, regions, atlas, level_mask);
 }
+void vcto_voxelize_conservative(const SceneView* s, int R, const Region regions[6], uint32_t* atlas, int level_mask) {
+    voxelize_conservative(*s, R, regions, atlas, level_mask);
+}
+// One triangle / box overlap decision (voxel units of `region`), for tests of the test.
+int vcto_cons_overlap(const float tri[9], const Region* region, int R, int i, int j, int k) {
+    V3<float> p[3];
+    for (int v = 0; v < 3; ++v) p[v] = V3<float>(tri[3 * v], tri[3 * v + 1], tri[3 * v + 2]);
+    const ConsTri t = cons_setup(p, *region, R);
+    return cons_overlap(t, i, j, k) ? 1 : 0;
+}
 void vcto_shadow_depth(const SceneView* s, const ShadowDesc* sd, float* depth, int W, int H) {
     shadow_depth(*s, *sd, depth, W, H);
 }
