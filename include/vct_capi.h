@@ -469,6 +469,17 @@ int vct_clear_atlas(uint32_t* atlas, int32_t clipmap_resolution, void* stream);
 int vct_voxelize_opacity(const vct_scene* scene, const vct_clipmap_region regions_host[6], int32_t clipmap_resolution,
                          uint32_t* opacity_atlas, uint32_t level_mask, vct_workspace ws, void* stream);
 
+/* Conservative voxelisation mode (build-only; the reference rasterises with
+ * MSAA): every voxel of each level's region in `level_mask` that a triangle
+ * touches -- the triangle / box overlap test of Schwarz & Seidel 2010 in the
+ * level's voxel units -- stored like vct_voxelize_opacity (1.0 into the 6
+ * face copies at the voxel's toroidal texel).  Does not clear.  Materials
+ * whose occlusion texel is below 0.1 are skipped, as msaaVoxelizer.frag
+ * discards them. */
+int vct_voxelize_opacity_conservative(const vct_scene* scene, const vct_clipmap_region regions_host[6],
+                                      int32_t clipmap_resolution, uint32_t* opacity_atlas, uint32_t level_mask,
+                                      void* stream);
+
 /* ReflectiveShadowMapPass depth (VFS/RenderPass/ReflectiveShadowMapPass.cpp,
  * reflectiveShadowPass.vert:40-50): clear to 1.0, rasterise with depth test
  * LESS into a width x height D32 map. */

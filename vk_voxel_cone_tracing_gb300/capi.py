@@ -225,6 +225,7 @@ _SIGS: dict[str, tuple] = {
     "vct_batch_submit": (C.c_int, [P, C.c_int32, C.c_int32]),
     "vct_clear_atlas": (C.c_int, [P, C.c_int32, P]),
     "vct_voxelize_opacity": (C.c_int, [P, P, C.c_int32, P, C.c_uint32, P, P]),
+    "vct_voxelize_opacity_conservative": (C.c_int, [P, P, C.c_int32, P, C.c_uint32, P]),
     "vct_shadow_depth": (C.c_int, [P, P, P, C.c_int32, C.c_int32, P, P]),
     "vct_inject_radiance": (C.c_int, [P, P, C.c_int32, P, P, P, P, C.c_uint32, C.c_int32, P, P]),
     "vct_svo_fragments": (C.c_int, [P, C.c_int32, P, P, P, P, P, P, C.c_int64, C.POINTER(C.c_int64), P, P]),

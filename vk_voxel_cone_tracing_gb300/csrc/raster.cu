@@ -1798,6 +1798,169 @@ extern "C" int vct_voxelize_opacity(const vct_scene* scene, const vct_clipmap_re
     return VCT_OK;
 }
 
+// ------------------------------------------------ conservative voxels
+// The conservative voxelisation mode: every voxel of a level's region that
+// the triangle touches, by the triangle / box overlap test of M. Schwarz and
+// H.-P. Seidel ("Fast parallel surface and solid voxelization on GPUs",
+// SIGGRAPH Asia 2010, section 3.1): the box overlaps the triangle's plane
+// (the plane's values at the box's two critical corners differ in sign or
+// vanish) and, in each axis projection, lies on the inner side of every edge
+// line shifted outward by the box's extent.  FP32 without contraction in the
+// level's voxel units u = p * (1 / voxel_size) - min_corner, the voxel
+// (i, j, k) being the box [i, i+1] x [j, j+1] x [k, k+1] -- the oracle's
+// arithmetic, so the voxel sets are equal bit for bit.
+namespace vct {
+namespace {
+
+struct ConsTri {
+    float u[3][3];
+    float n[3];
+    float d1, d2;
+    float ne[3][3][2];
+    float de[3][3];
+    int lo[3], hi[3];
+    bool ok;
+};
+
+__device__ __forceinline__ float fmax0(float x) { return x > 0.0f ? x : 0.0f; }
+
+__device__ inline ConsTri cons_setup(const float3 p[3], const vct_clipmap_region& rg, int R) {
+    ConsTri t;
+    const float inv = 1.0f / rg.voxel_size;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        t.u[k][0] = p[k].x * inv - (float)rg.min_corner[0];
+        t.u[k][1] = p[k].y * inv - (float)rg.min_corner[1];
+        t.u[k][2] = p[k].z * inv - (float)rg.min_corner[2];
+    }
+    t.ok = true;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float mn = fminf(fminf(t.u[0][a], t.u[1][a]), t.u[2][a]);
+        const float mx = fmaxf(fmaxf(t.u[0][a], t.u[1][a]), t.u[2][a]);
+        const float fl = floorf(mn), fh = floorf(mx);
+        t.lo[a] = fl < 0.0f ? 0 : (fl > (float)(R - 1) ? R : (int)fl);
+        t.hi[a] = fh > (float)(R - 1) ? R - 1 : (fh < 0.0f ? -1 : (int)fh);
+        if (t.lo[a] > t.hi[a]) t.ok = false;
+    }
+    float e0[3], e1[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        e0[a] = t.u[1][a] - t.u[0][a];
+        e1[a] = t.u[2][a] - t.u[0][a];
+    }
+    t.n[0] = e0[1] * e1[2] - e0[2] * e1[1];
+    t.n[1] = e0[2] * e1[0] - e0[0] * e1[2];
+    t.n[2] = e0[0] * e1[1] - e0[1] * e1[0];
+    float c[3], c2[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        c[a] = t.n[a] > 0.0f ? 1.0f : 0.0f;
+        c2[a] = 1.0f - c[a];
+    }
+    t.d1 = t.n[0] * (c[0] - t.u[0][0]) + t.n[1] * (c[1] - t.u[0][1]) + t.n[2] * (c[2] - t.u[0][2]);
+    t.d2 = t.n[0] * (c2[0] - t.u[0][0]) + t.n[1] * (c2[1] - t.u[0][1]) + t.n[2] * (c2[2] - t.u[0][2]);
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const int a0 = q, a1 = (q + 1) % 3, a2 = (q + 2) % 3;  // projections xy, yz, zx
+        const float sg = t.n[a2] >= 0.0f ? 1.0f : -1.0f;
+#pragma unroll
+        for (int e = 0; e < 3; ++e) {
+            const float* v0 = t.u[e];
+            const float* v1 = t.u[(e + 1) % 3];
+            const float n0 = -(v1[a1] - v0[a1]) * sg, n1 = (v1[a0] - v0[a0]) * sg;
+            t.ne[q][e][0] = n0;
+            t.ne[q][e][1] = n1;
+            t.de[q][e] = -(n0 * v0[a0] + n1 * v0[a1]) + fmax0(n0) + fmax0(n1);
+        }
+    }
+    return t;
+}
+
+__device__ inline bool cons_overlap(const ConsTri& t, int i, int j, int k) {
+    if (i < t.lo[0] || i > t.hi[0] || j < t.lo[1] || j > t.hi[1] || k < t.lo[2] || k > t.hi[2]) return false;
+    const float p[3] = {(float)i, (float)j, (float)k};
+    const float np = t.n[0] * p[0] + t.n[1] * p[1] + t.n[2] * p[2];
+    if ((np + t.d1) * (np + t.d2) > 0.0f) return false;
+#pragma unroll
+    for (int q = 0; q < 3; ++q)
+#pragma unroll
+        for (int e = 0; e < 3; ++e)
+            if (t.ne[q][e][0] * p[q] + t.ne[q][e][1] * p[(q + 1) % 3] + t.de[q][e] < 0.0f) return false;
+    return true;
+}
+
+struct ConsArgs {
+    vct_scene s;
+    vct_clipmap_region rg[6];
+    int levels[6];
+    int nlevels;
+    int R;
+    uint32_t* atlas;
+};
+
+// One warp per (triangle, level) item, the item's bounding-box voxels dealt
+// over the lanes (a large triangle's box has thousands of voxels, a small
+// one's a few).
+__global__ void __launch_bounds__(256) k_voxelize_conservative(const __grid_constant__ ConsArgs A, int64_t items) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int rb = A.R + 2;
+    const int64_t W = (int64_t)rb * 6, H = (int64_t)rb * 6;
+    for (int64_t it = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; it < items; it += nwarps) {
+        const int64_t tri = it / A.nlevels;
+        const int level = A.levels[it - tri * A.nlevels];
+        const WTri w = world_triangle(A.s, tri);
+        const vct_gltf_shade_material mat = material_of(A.s, w.material);
+        if (mat.occlusion_texture > -1 && texture_1x1(A.s, mat.occlusion_texture).x < 0.1f) continue;
+        const vct_clipmap_region& rg = A.rg[level];
+        const ConsTri t = cons_setup(w.p, rg, A.R);
+        if (!t.ok) continue;
+        const int nx = t.hi[0] - t.lo[0] + 1, ny = t.hi[1] - t.lo[1] + 1, nz = t.hi[2] - t.lo[2] + 1;
+        const int64_t nv = (int64_t)nx * ny * nz;
+        for (int64_t v = lane; v < nv; v += 32) {
+            const int64_t r = v / nx;
+            const int i = t.lo[0] + (int)(v - r * nx), j = t.lo[1] + (int)(r % ny), k = t.lo[2] + (int)(r / ny);
+            if (!cons_overlap(t, i, j, k)) continue;
+            const int x = (((rg.min_corner[0] + i) % A.R) + A.R) % A.R + 1;
+            const int y = (((rg.min_corner[1] + j) % A.R) + A.R) % A.R + 1 + rb * level;
+            const int z = (((rg.min_corner[2] + k) % A.R) + A.R) % A.R + 1;
+            const int64_t base = ((int64_t)z * H + y) * W + x;
+#pragma unroll
+            for (int f = 0; f < 6; ++f) A.atlas[base + (int64_t)rb * f] = 0xFFFFFFFFu;
+        }
+    }
+}
+
+}  // namespace
+}  // namespace vct
+
+extern "C" int vct_voxelize_opacity_conservative(const vct_scene* scene, const vct_clipmap_region regions[6],
+                                                 int32_t R, uint32_t* atlas, uint32_t level_mask, void* stream) {
+    vct::NvtxRange nvtx_range("vct_voxelize_opacity_conservative");
+    int rc = check_scene(scene);
+    if (rc != VCT_OK) return rc;
+    VCT_CHECK_ARG(regions && atlas && valid_resolution(R), "vct_voxelize_opacity_conservative: bad argument");
+    VCT_CHECK_ARG((level_mask & ~0x3Fu) == 0, "vct_voxelize_opacity_conservative: level mask has bits above level 5");
+    if (scene->triangle_count == 0 || level_mask == 0) return VCT_OK;
+    vct::ConsArgs A;
+    memset(&A, 0, sizeof(A));
+    A.s = *scene;
+    A.R = R;
+    A.atlas = atlas;
+    for (int l = 0; l < 6; ++l) {
+        A.rg[l] = regions[l];
+        VCT_CHECK_ARG(regions[l].voxel_size > 0.0f, "vct_voxelize_opacity_conservative: non-positive voxel size");
+        if ((level_mask >> l) & 1u) A.levels[A.nlevels++] = l;
+    }
+    const int64_t items = scene->triangle_count * (int64_t)A.nlevels;
+    int64_t blocks = (items * 32 + 255) / 256;
+    if (blocks > 152 * 64) blocks = 152 * 64;
+    vct::k_voxelize_conservative<<<(int)blocks, 256, 0, as_stream(stream)>>>(A, items);
+    VCT_LAUNCH_CHECK();
+    return VCT_OK;
+}
+
 extern "C" int vct_shadow_depth(const vct_scene* scene, const vct_directional_light_shadow_desc* sd, float* depth,
                                 int32_t W, int32_t H, vct_workspace_s* ws, void* stream) {
     vct::NvtxRange nvtx_range("vct_shadow_depth");

@@ -114,6 +114,14 @@ def voxelize_opacity(dscene: DeviceScene, regions, R: int, atlas: torch.Tensor, 
               level_mask, ws.handle, _stream())
 
 
+def voxelize_opacity_conservative(dscene: DeviceScene, regions, R: int, atlas: torch.Tensor,
+                                  level_mask: int = 0x3F) -> None:
+    """The conservative voxelisation mode: every voxel of each level's region a triangle touches (triangle /
+    box overlap, Schwarz & Seidel 2010), stored like voxelize_opacity."""
+    capi.call("vct_voxelize_opacity_conservative", capi.ref(dscene.desc), C.cast(regions, C.c_void_p), R,
+              _ptr(atlas), level_mask, _stream())
+
+
 def shadow_depth(dscene: DeviceScene, sd: capi.DirectionalLightShadowDesc, depth: torch.Tensor, ws: Workspace) -> None:
     H, W = depth.shape
     capi.call("vct_shadow_depth", capi.ref(dscene.desc), capi.ref(sd), _ptr(depth), W, H, ws.handle, _stream())
