@@ -326,6 +326,13 @@ def run_ours(args, world, rank, local):
     svo()
     svo_per, _ = events_ms(stream, svo, max(3, args.steps))
     frame_ms = statistics.median(frame_per)
+    # the conservative voxelisation mode over the same levels (into the opacity atlas; the frame after the
+    # moving-camera runs below restores it)
+    cons = lambda: passes.voxelize_opacity_conservative(ds, regs, R, opacity)
+    passes.clear_atlas(opacity, R)
+    cons()
+    cons_voxels = int((opacity != 0).sum().item()) // 6
+    cons_ms = statistics.median(events_ms(stream, cons, 3)[0])
     svo_ms = statistics.median(svo_per)
     # the SVO cone trace (voxelConeTracing_Octree.frag) over the first 262144 samples of the octree just built,
     # with the scene's bounding box (the reference's hard-coded Sponza box does not fit the hall scene)
@@ -492,6 +499,9 @@ def run_ours(args, world, rank, local):
                        else ("kept current by the frame's FP16 conversion and FP16 mip passes" if tex is not None
                              else "none (linear atlas)"),
                        "voxelize_inject_mip_ms": frame_ms, "svo_ms": svo_ms, "svo_level": SVO_LEVEL,
+                       "conservative_voxelize": {"ms": cons_ms, "voxels": cons_voxels,
+                                                 "note": "triangle/box overlap mode (Schwarz & Seidel 2010), "
+                                                         "6 levels of 256^3; voxels marked over all levels"},
                        "svo_fragments": int(frags.shape[0]), "svo_nodes": int(nodes.value),
                        "svo_trace": {"samples": svo_n, "ms": svo_trace_ms, "cone_samples_per_s": svo_trace_rate},
                        "voxelize_svo_mip_ms": frame_ms + svo_ms,
