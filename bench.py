@@ -523,7 +523,10 @@ def run_ours(args, world, rank, local):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "note": f"{bpcs} B of algorithmic texel reads per cone sample over the {peak_kind} HBM "
-                                 "copy peak; the taps are served mostly from L1/TEX and L2"},
+                                 "copy peak, per trace step (CUDA events around the step: Morton sort, specular "
+                                 "partition, diffuse and specular kernels; the specular kernel is about 71 % of it "
+                                 "in the ncu launch list); the taps are served mostly from L1/TEX and L2, so the "
+                                 "figure exceeds the HBM peak; traffic = ncu DRAM bytes of one step"},
             "gather_roofline": None if gather_peak is None else {
                 "bound": "l1tex/l2 gather", "achieved": cone_samples / (statistics.mean(per) * 1e-3),
                 "peak": gather_peak, "unit": "cone samples/s",
