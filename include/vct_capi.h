@@ -12,7 +12,10 @@
  * cudaFreeAsync before the call returns) in the per-sample traces
  * (vct_cone_trace, vct_cone_trace_f32, vct_cone_trace_backward,
  * vct_svo_cone_trace: the samples' processing order) and vct_sq_error.
- * vct_cone_trace_fast_noalloc allocates nothing at all.
+ * vct_gather_probe allocates and frees a small device buffer and two events.
+ * vct_cone_trace_fast_noalloc never calls cudaMalloc: its scratch is a static
+ * device array that the runtime commits when the array's module loads (see
+ * that function).
  *
  * Parameter structs keep the reference's byte layouts (std140 / push-constant
  * layouts of the GLSL blocks); the static asserts at the end of this header
@@ -406,7 +409,9 @@ int vct_cone_trace_fast(const vct_cone_tracing_desc* desc, const vct_cam_matrix*
  * every step exactly the texture fetches of one cone sample (three face taps
  * at two adjacent levels) and nothing else.  *samples_per_second receives
  * the measured cone-sample rate: the gather speed of light that
- * vct_cone_trace_fast's rate is compared with.  Synchronises `stream`. */
+ * vct_cone_trace_fast's rate is compared with.  Allocates and frees a small
+ * device buffer and creates and destroys two CUDA events; synchronises
+ * `stream`. */
 int vct_gather_probe(const vct_cone_tracing_desc* desc, vct_texture radiance, int64_t cones, int32_t steps_per_cone,
                      double* samples_per_second, void* stream);
 
@@ -754,10 +759,13 @@ int vct_clipmap_frame(const vct_scene* scene, const vct_frame_desc* frame, uint3
  * with its scratch in a static device array of VCT_NOALLOC_SCRATCH_BYTES that
  * the library holds on every GPU that loads it, for up to
  * VCT_NOALLOC_MAX_SAMPLES samples (larger counts are rejected with
- * VCT_E_BAD_ARG).  The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress); make it before any stream capture.  Calls
- * share the array: calls that overlap on the GPU race and must be serialised
- * by the caller. */
+ * VCT_E_BAD_ARG).  No call runs cudaMalloc, but the array must be resident:
+ * under lazy module loading (the CUDA runtime's default) the runtime commits
+ * its 48 MiB on a device at the first call there, so make one call on each
+ * device before the host reserves its device memory and before any stream
+ * capture.  Every call looks up the array's address on the current device
+ * (cudaGetSymbolAddress).  Calls share the array: calls that overlap on the
+ * GPU race and must be serialised by the caller. */
 #define VCT_NOALLOC_MAX_SAMPLES 1048576
 #define VCT_NOALLOC_SCRATCH_BYTES (48u << 20)
 int vct_cone_trace_fast_noalloc(const vct_cone_tracing_desc* desc, const vct_cam_matrix* cam, vct_texture radiance,

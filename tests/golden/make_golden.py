@@ -63,7 +63,10 @@ def cone_tables(ref: Path) -> dict:
 
 
 def main():
-    ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) > 1:
+        ref = Path(sys.argv[1])
+    else:  # the reference checkout named in the repository's benchmark spec
+        ref = Path(json.loads((HERE.parents[1] / "BASELINE.json").read_text())["reference_path"])
     host = build_and_run(ref)
     (HERE / "glm_host_math.json").write_text(json.dumps(host, separators=(",", ":")) + "\n")
     (HERE / "cone_tables.json").write_text(json.dumps(cone_tables(ref), indent=1) + "\n")

@@ -38,15 +38,20 @@ def test_noalloc_matches_fast_trace_on_two_calls(cuda, oracle):
     stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
     need = capi.lib().vct_cone_trace_fast_scratch_bytes(capi.NOALLOC_MAX_SAMPLES)
     assert 0 < need <= capi.NOALLOC_SCRATCH_BYTES
-    for seed, n in ((42, 3000), (43, 1200)):
+    for call, (seed, n) in enumerate(((42, 3000), (43, 1200))):
         samples = clipmap.samples_to_device(random_samples(n, (0, 0, 0), 6.0, seed=seed))
         want_d, want_s = clipmap.cone_trace_fast(desc, eye, tex, samples)
         got_d = torch.full((n, 4), -1.0, device="cuda")
         got_s = torch.full((n, 4), -1.0, device="cuda")
+        torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info()[0]
         capi.call("vct_cone_trace_fast_noalloc", capi.ref(desc), capi.ref(cam), tex.handle, capi.ref(sm),
                   capi.ref(light), capi.ref(sd), C.c_void_p(samples.data_ptr()), n, C.c_void_p(got_d.data_ptr()),
                   C.c_void_p(got_s.data_ptr()), None, stream)
         torch.cuda.synchronize()
+        if call > 0:
+            # the first call may commit the static array (lazy module loading); later calls take no device memory
+            assert torch.cuda.mem_get_info()[0] == free_before
         wd, ws = want_d.cpu().numpy(), want_s.cpu().numpy()
         gd, gs = got_d.cpu().numpy(), got_s.cpu().numpy()
         assert _rel(gd, wd) < TOL and _rel(gs, ws) < TOL

@@ -10,27 +10,30 @@
 // storage that vct_cone_trace_fast needs as scratch.
 //
 // This entry point keeps that scratch in a file-scope device array of
-// VCT_NOALLOC_SCRATCH_BYTES.  The array is part of the library's device
-// image: every GPU that loads the library holds it until the process exits.
-// Host code cannot use the array's name as a device address, so on the first
-// call on each device (with that device current) the address is looked up
-// with cudaGetSymbolAddress and cached; make that first call before any
-// stream capture.  All calls share the one array and it keeps the previous
-// call's contents: the tracer clears what must start at zero (its specular
-// counter) on every call, and calls whose GPU work overlaps -- on two streams,
-// or from two host threads -- race on the array and must be serialised by
-// the caller.
-#include <mutex>
-
+// VCT_NOALLOC_SCRATCH_BYTES.  The array is part of this translation unit's
+// device module.  Under lazy module loading (CUDA_MODULE_LOADING=LAZY, the
+// runtime's default) that module -- and with it the 48 MiB -- is committed on
+// a device the first time this entry point runs there; with eager loading it
+// is committed when the library's modules load.  Either way the device keeps
+// it until the process exits, and no call ever runs cudaMalloc.  A host that
+// reserves (nearly) all device memory for its own allocator must therefore
+// make one call on each device before it makes that reservation, and before
+// any stream capture.
+//
+// Host code cannot use the array's name as a device address, so every call
+// looks the address up with cudaGetSymbolAddress on the current device (a
+// table lookup once the module is loaded); nothing is cached across calls,
+// so a context torn down and re-created (cudaDeviceReset) gets the new
+// module's address.  All calls share the one array and it keeps the
+// previous call's contents: the tracer clears what must start at zero (its
+// specular counter) on every call, and calls whose GPU work overlaps -- on
+// two streams, or from two host threads -- race on the array and must be
+// serialised by the caller.
 #include "common.cuh"
 
 namespace {
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[VCT_NOALLOC_SCRATCH_BYTES];
-
-constexpr int kMaxDevices = 64;
-std::mutex g_noalloc_mutex;
-void* g_noalloc_ptr[kMaxDevices] = {};
 
 }  // namespace
 
@@ -44,23 +47,13 @@ extern "C" int vct_cone_trace_fast_noalloc(const vct_cone_tracing_desc* desc, co
     VCT_CHECK_ARG(sample_count >= 0 && sample_count <= VCT_NOALLOC_MAX_SAMPLES,
                   "vct_cone_trace_fast_noalloc: sample count exceeds VCT_NOALLOC_MAX_SAMPLES (1048576); "
                   "use vct_cone_trace_fast with caller-provided scratch");
-    int dev = 0;
-    VCT_CUDA_TRY(cudaGetDevice(&dev));
-    VCT_CHECK_ARG(dev >= 0 && dev < kMaxDevices, "vct_cone_trace_fast_noalloc: device ordinal out of range");
-    void* scratch = nullptr;
-    {
-        std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-        if (!g_noalloc_ptr[dev]) {
-            void* p = nullptr;
-            VCT_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-            g_noalloc_ptr[dev] = p;
-        }
-        scratch = g_noalloc_ptr[dev];
-    }
     const int64_t need = vct_cone_trace_fast_scratch_bytes(sample_count);
     if (need < 0 || need > (int64_t)VCT_NOALLOC_SCRATCH_BYTES)
         return vct::fail(VCT_E_BAD_ARG, "vct_cone_trace_fast_noalloc: the static scratch array is too small for "
                                         "this sample count");
+    // the address on the current device, looked up with that device current
+    void* scratch = nullptr;
+    VCT_CUDA_TRY(cudaGetSymbolAddress(&scratch, g_noalloc_scratch));
     return vct_cone_trace_fast(desc, cam, radiance, shadow, light, light_shadow, samples, sample_count, diffuse_out,
                                specular_out, cone_steps, scratch, (size_t)VCT_NOALLOC_SCRATCH_BYTES, stream);
 }
