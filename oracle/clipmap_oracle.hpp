@@ -243,13 +243,26 @@ inline void downsample(uint32_t* atlas, int R, const int prev_min[3], int level,
 
 
 // The same level downsample on float4 storage (no 8-bit quantisation),
-// arithmetic in T: the error reference of the FP16-storage mips.
-template <class T>
-inline void downsample_f4(float* atlas4, int R, const int prev_min[3], int level, int band, int mode) {
+// arithmetic in T: the error reference of the FP16-storage mips.  The texel
+// store is a parameter: F4Store rounds every written value to float (the
+// float atlas); the reference gradient instantiates it with a store of
+// ad::Var values (adjoint_oracle.hpp).
+struct F4Store {
+    float* atlas4;
+    static constexpr bool kParallel = true;
+    template <class T> V4<T> load(int64_t t) const {
+        const float* p = atlas4 + 4 * t;
+        return V4<T>(T(p[0]), T(p[1]), T(p[2]), T(p[3]));
+    }
+    template <class T> void put(int64_t t, int c, T v) { atlas4[4 * t + c] = (float)v; }
+};
+
+template <class T, class Store>
+inline void downsample_f4_on(Store& st, int R, const int prev_min[3], int level, int band, int mode) {
     Atlas A(R);
     const int half = R >> 1;
     const int rb = R + 2;
-#pragma omp parallel for collapse(2) schedule(static)
+#pragma omp parallel for collapse(2) schedule(static) if (Store::kParallel)
     for (int gz = 0; gz < half; ++gz)
         for (int gy = 0; gy < half; ++gy)
             for (int gx = 0; gx < half; ++gx) {
@@ -264,13 +277,11 @@ inline void downsample_f4(float* atlas4, int R, const int prev_min[3], int level
                 const T lerp = T(ds_lerp(cur, prev_min, R, band));
                 for (int f = 0; f < 6; ++f) {
                     V4<T> v[8];
-                    for (int i = 0; i < 8; ++i) {
-                        const float* p = atlas4 + 4 * A.index(pstart[0] + kOff[i][0] + 1 + rb * f,
-                                                              pstart[1] + kOff[i][1] + 1 + rb * (level - 1),
-                                                              pstart[2] + kOff[i][2] + 1);
-                        v[i] = V4<T>(T(p[0]), T(p[1]), T(p[2]), T(p[3]));
-                    }
-                    float* o = atlas4 + 4 * A.index(wpos[0] + rb * f, wpos[1], wpos[2]);
+                    for (int i = 0; i < 8; ++i)
+                        v[i] = st.template load<T>(A.index(pstart[0] + kOff[i][0] + 1 + rb * f,
+                                                           pstart[1] + kOff[i][1] + 1 + rb * (level - 1),
+                                                           pstart[2] + kOff[i][2] + 1));
+                    const int64_t o = A.index(wpos[0] + rb * f, wpos[1], wpos[2]);
                     V4<T> s(T(0));
                     for (int k = 0; k < 4; ++k) {
                         const V4<T>& a0 = v[kPairs[f][k][0]];
@@ -278,19 +289,25 @@ inline void downsample_f4(float* atlas4, int R, const int prev_min[3], int level
                         const T t = T(1) - a0.w;
                         s = V4<T>(s.x + a0.x + t * a1.x, s.y + a0.y + t * a1.y, s.z + a0.z + t * a1.z, s.w + a0.w + t * a1.w);
                     }
+                    const V4<T> own = st.template load<T>(o);
                     if (mode == 0) {
-                        T a = mixv(s.w * T(0.25), T(o[0]), lerp);
-                        o[3] = (float)a;
-                        o[1] = (float)a;
+                        T a = mixv(s.w * T(0.25), own.x, lerp);
+                        st.put(o, 3, a);
+                        st.put(o, 1, a);
                     } else {
-                        T own[4] = {T(o[0]), T(o[1]), T(o[2]), T(o[3])};
-                        o[0] = (float)mixv(s.x * T(0.25), own[0], lerp);
-                        o[1] = (float)mixv(s.y * T(0.25), own[1], lerp);
-                        o[2] = (float)mixv(s.z * T(0.25), own[2], lerp);
-                        o[3] = (float)mixv(s.w * T(0.25), own[3], lerp);
+                        st.put(o, 0, mixv(s.x * T(0.25), own.x, lerp));
+                        st.put(o, 1, mixv(s.y * T(0.25), own.y, lerp));
+                        st.put(o, 2, mixv(s.z * T(0.25), own.z, lerp));
+                        st.put(o, 3, mixv(s.w * T(0.25), own.w, lerp));
                     }
                 }
             }
+}
+
+template <class T>
+inline void downsample_f4(float* atlas4, int R, const int prev_min[3], int level, int band, int mode) {
+    F4Store st{atlas4};
+    downsample_f4_on<T>(st, R, prev_min, level, band, mode);
 }
 
 // ----------------------------------------------------------- texture fetch

@@ -27,7 +27,7 @@ HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 LIB = BUILD / "libvct_oracle.so"
 SOURCES = ["vct_oracle.cpp"]
-HEADERS = ["oracle_common.hpp", "clipmap_oracle.hpp", "raster_oracle.hpp", "svo_oracle.hpp", "gbuffer_oracle.hpp",
+HEADERS = ["ad_tape.hpp", "adjoint_oracle.hpp", "oracle_common.hpp", "clipmap_oracle.hpp", "raster_oracle.hpp", "svo_oracle.hpp", "gbuffer_oracle.hpp",
            "composite_oracle.hpp"]
 
 P = C.c_void_p
@@ -74,6 +74,9 @@ def lib():
         L.vcto_cone_trace_f4.argtypes = [P, P, P, C.c_int, P, C.c_int, C.c_int, P, P, P, C.c_int64, C.c_int64,
                                          P, P]
         L.vcto_downsample_f4.argtypes = [P, C.c_int, P, C.c_int, C.c_int, C.c_int]
+        L.vcto_cone_trace_grad_f4.argtypes = [P, P, P, C.c_int, P, C.c_int, C.c_int, P, P, P, C.c_int64, C.c_int64,
+                                              P, P, P]
+        L.vcto_downsample_chain_grad_f4.argtypes = [P, C.c_int, P, C.c_int, C.c_int, C.c_int, P]
         L.vcto_voxel_view_proj.argtypes = [P, P]
         L.vcto_voxelization_desc.argtypes = [P, C.c_int, C.c_int, P]
         L.vcto_light_shadow_desc.argtypes = [P, P, C.c_float, C.c_float, P]
@@ -208,6 +211,37 @@ def cone_trace_f4(desc_bytes: bytes, eye, atlas4: np.ndarray, R: int, samples: n
     steps = lib().vcto_cone_trace_f4(_p(desc), _p(eye), _p(atlas4), R, _p(shadow), sw, sh, _p(sd), _p(light),
                                      _p(samples), begin, end, _p(dout), _p(sout))
     return dout, sout, int(steps)
+
+
+def cone_trace_grad_f4(desc_bytes: bytes, eye, atlas4: np.ndarray, R: int, samples: np.ndarray,
+                       grad_diffuse: np.ndarray, grad_specular: np.ndarray, shadow: np.ndarray | None = None,
+                       shadow_desc_bytes: bytes | None = None, light_bytes: bytes | None = None) -> np.ndarray:
+    """FP64 reference gradient (reverse-mode AD of the restated trace) of
+    sum(grad_diffuse * diffuse + grad_specular * specular) with respect to the float atlas: an array of the
+    atlas's shape, float64."""
+    assert atlas4.dtype == np.float32 and atlas4.flags["C_CONTIGUOUS"]
+    n = samples.shape[0]
+    gd = np.ascontiguousarray(grad_diffuse, np.float32).reshape(n, 4)
+    gs = np.ascontiguousarray(grad_specular, np.float32).reshape(n, 4)
+    out = np.zeros(atlas4.shape, np.float64)
+    desc = np.frombuffer(desc_bytes, np.uint8).copy()
+    sd = np.frombuffer(shadow_desc_bytes or bytes(136), np.uint8).copy()
+    light = np.frombuffer(light_bytes or default_light_bytes(), np.uint8).copy()
+    sh, sw = (shadow.shape if shadow is not None else (0, 0))
+    lib().vcto_cone_trace_grad_f4(_p(desc), _p(np.asarray(eye, np.float32)), _p(atlas4), R, _p(shadow), sw, sh,
+                                  _p(sd), _p(light), _p(samples), 0, n, _p(gd), _p(gs), _p(out))
+    return out
+
+
+def downsample_chain_grad_f4(atlas4: np.ndarray, R: int, regions: np.ndarray, grad_out: np.ndarray, mode: int,
+                             first: int = 1, band: int = 10) -> np.ndarray:
+    """FP64 reference adjoint of the float mips, levels first..5: given dL/d(atlas after the chain), returns
+    dL/d(atlas before it) (float64, the atlas's shape)."""
+    assert atlas4.dtype == np.float32 and atlas4.flags["C_CONTIGUOUS"]
+    pm = np.ascontiguousarray(np.asarray(regions)[0:5, 0:3], np.int32).reshape(15)
+    G = np.ascontiguousarray(grad_out, np.float64).copy()
+    lib().vcto_downsample_chain_grad_f4(_p(atlas4), R, _p(pm), first, band, mode, _p(G))
+    return G
 
 
 # ------------------------------------------------------------ raster passes

@@ -17,6 +17,8 @@
 #include <cstring>
 #include <algorithm>
 
+#include "ad_tape.hpp"  // before the templates: its std:: overloads must be visible to them
+
 namespace vcto {
 
 template <class T> struct V2 { T x, y; };

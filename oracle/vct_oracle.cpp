@@ -1,10 +1,12 @@
 // vct_oracle.cpp -- TEST INFRASTRUCTURE ONLY.
 //
 // C entry points over the CPU restatement (clipmap_oracle.hpp, svo_oracle.hpp,
-// raster_oracle.hpp, gbuffer_oracle.hpp, composite_oracle.hpp) for the Python test harness and bench.py's CPU-baseline
+// raster_oracle.hpp, gbuffer_oracle.hpp, composite_oracle.hpp) and its FP64
+// reference gradients (adjoint_oracle.hpp) for the Python test harness and bench.py's CPU-baseline
 // leg (ctypes).  The CUDA product library never links or calls this file.
 #include <omp.h>
 
+#include "adjoint_oracle.hpp"
 #include "clipmap_oracle.hpp"
 #include "composite_oracle.hpp"
 #include "gbuffer_oracle.hpp"
@@ -103,6 +105,28 @@ uint64_t vcto_cone_trace_f4(const TraceDesc* desc, const float eye[3], const flo
         total += tr.steps;
     }
     return total;
+}
+
+// FP64 reference gradient of the float-atlas trace (adjoint_oracle.hpp):
+// grad (4 doubles per texel, zeroed here) = d/d(atlas4) of
+// sum_i gd_i . diffuse_i + gs_i . specular_i over samples [begin, end).
+void vcto_cone_trace_grad_f4(const TraceDesc* desc, const float eye[3], const float* atlas4, int R,
+                             const float* shadow, int sw, int sh, const ShadowDesc* sd, const LightDesc* light,
+                             const SurfaceSample* samples, int64_t begin, int64_t end, const float* gd,
+                             const float* gs, double* grad) {
+    const int64_t n = 4 * Atlas(R).texels();
+    for (int64_t k = 0; k < n; ++k) grad[k] = 0.0;
+    cone_trace_grad_f4(*desc, eye, atlas4, R, shadow, sw, sh, *sd, *light, samples, begin, end, gd, gs, grad);
+}
+
+// FP64 reference adjoint of the float mips, levels first..5 (adjoint_oracle.hpp):
+// G enters as dL/d(atlas after the chain) and leaves as dL/d(atlas before it).
+void vcto_downsample_chain_grad_f4(const float* atlas4, int R, const int prev_min[15], int first, int band, int mode,
+                                   double* G) {
+    int pm[5][3];
+    for (int l = 0; l < 5; ++l)
+        for (int a = 0; a < 3; ++a) pm[l][a] = prev_min[3 * l + a];
+    downsample_chain_grad_f4(atlas4, R, pm, first, band, mode, G);
 }
 
 // The benchmark's hash-random sparse atlas (same words as
