@@ -1,66 +1,107 @@
 // trace_exact.cu -- the plain FP32 drop-in of voxelConeTracing.frag.
 //
-// One thread per G-buffer sample, cones traced in the shader's order, the
-// radiance clipmap read from the reference's linear RGBA8 atlas with a
-// software trilinear filter (FP32 weights, REPEAT addressing) -- the same
-// arithmetic, in the same order, as the FP32 restatement of the shader.
-// Compiled with -fmad=false so no multiply-add is fused.
+// The radiance clipmap is read from the reference's linear RGBA8 atlas (or a
+// float RGBA atlas: the differentiable form) with a software trilinear
+// filter (FP32 weights, REPEAT addressing) -- the same arithmetic, in the
+// same order, as the FP32 restatement of the shader.  Compiled with
+// -fmad=false so no multiply-add is fused.  The work is laid out like the
+// texture form's: samples in a coherent order (normal class, then Morton),
+// the diffuse cones of 32 samples dealt to the lanes of a warp
+// (trace_deal.cuh), each cone marched by trace_cone; the specular cones one
+// per warp with 64 consecutive steps per round (trace_cone_warp_exact).  The
+// specular cone is traced wherever the shader traces it (every rendering
+// mode), the diffuse cones likewise.
 #include <cstring>
 
 #include <cub/cub.cuh>
 
+#include "trace_deal.cuh"
 #include "trace_exact.cuh"
 
 namespace vct {
 
+constexpr int kExactWarps = 4;  // warps per block of the diffuse kernel
+
 template <class Atlas>
-__global__ void __launch_bounds__(128) k_cone_trace_exact(TraceParams P, Atlas T,
-                                                          const vct_surface_sample* __restrict__ samples, int64_t n,
-                                                          const uint32_t* __restrict__ order,
-                                                          float* __restrict__ dout, float* __restrict__ sout,
-                                                          unsigned long long* __restrict__ step_counter) {
-    unsigned long long steps = 0;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = order ? (int64_t)__ldg(order + t) : t;
-        GSample g = load_sample(samples + i, P.eye);
-        if (g.depth == 1.0f) continue;
-        const vct_cone_tracing_desc& d = P.d;
-        float min_level = calc_min_level(d, g.wp);
-        float vs = d.voxel_size * exp2f(min_level);
-        float3 start = g.wp + g.normal * (vs * d.trace_start_offset);
-        float4 ind = make_float4(0.f, 0.f, 0.f, 1.f);
-        const bool c32 = d.enable_32_cones != 0;
-        const int nc = c32 ? 32 : 16;
-        const float aperture = c32 ? kAperture32 : kAperture16;
-        const float sf = fmaxf(kMinTraceStepFactor, d.min_trace_step_factor);
-        for (int c = 0; c < nc; ++c) {
-            float3 dir = c32 ? f3(c_dirs32[c][0], c_dirs32[c][1], c_dirs32[c][2])
-                             : f3(c_dirs16[c][0], c_dirs16[c][1], c_dirs16[c][2]);
-            float cos_t = dot3(g.normal, dir);
-            if (cos_t < 0.0f) continue;
-            float4 r = trace_cone(T, d, start, dir, aperture, kMaxTraceDistance, min_level, sf, steps);
-            ind = make_float4(ind.x + r.x * cos_t, ind.y + r.y * cos_t, ind.z + r.z * cos_t, ind.w + r.w * cos_t);
-        }
-        ind = make_float4(ind.x / (float)nc, ind.y / (float)nc, ind.z / (float)nc, ind.w / (float)nc);
-        ind.w = ind.w * d.ambient_occlusion_factor;
-        ind.x = ind.x * (g.diffuse_color.x * d.indirect_diffuse_intensity);
-        ind.y = ind.y * (g.diffuse_color.y * d.indirect_diffuse_intensity);
-        ind.z = ind.z * (g.diffuse_color.z * d.indirect_diffuse_intensity);
-        float3 ispec = f3(0.f, 0.f, 0.f);
-        if (has_specular_cone(g)) {
-            float3 sdir = reflect3(f3(-g.view.x, -g.view.y, -g.view.z), g.normal);
-            float4 r = trace_cone(T, d, start, sdir, fmaxf(g.roughness, kMinSpecularAperture), kMaxTraceDistance,
-                                  min_level, d.voxel_size, steps);
-            const float isi = d.indirect_specular_intensity;
-            ispec = f3(r.x * g.specular_color.x * isi, r.y * g.specular_color.y * isi, r.z * g.specular_color.z * isi);
-        }
-        float3 direct = direct_term(P, g);
-        write_outputs(P, g, min_level, ind, ispec, direct, dout + 4 * i, sout + 4 * i);
+struct ExactDiffuseMarch {
+    Atlas T;
+    const vct_cone_tracing_desc* d;
+    float aperture, step_factor;
+    __device__ __forceinline__ float4 operator()(float3 start, float3 dir, float start_level,
+                                                 unsigned long long& steps) const {
+        return trace_cone(T, *d, start, dir, aperture, kMaxTraceDistance, start_level, step_factor, steps);
     }
-    if (step_counter) {
-        // Warp-aggregated accumulation of the iteration count.
-        for (int o = 16; o > 0; o >>= 1) steps += __shfl_xor_sync(0xffffffffu, steps, o);
-        if ((threadIdx.x & 31) == 0 && steps) atomicAdd(step_counter, steps);
+};
+
+template <class Atlas>
+__global__ void __launch_bounds__(32 * kExactWarps) k_exact_diffuse(TraceParams P, Atlas T,
+                                                                    const vct_surface_sample* __restrict__ samples,
+                                                                    int64_t n, const uint32_t* __restrict__ order,
+                                                                    float* __restrict__ dout, float* __restrict__ sout,
+                                                                    unsigned long long* __restrict__ step_counter) {
+    const bool c32 = P.d.enable_32_cones != 0;
+    DealArgs D{&P, samples, n, order, 0u, (uint32_t)n, dout, sout, c32 ? 32 : 16, true, true};
+    const ExactDiffuseMarch<Atlas> march{T, &P.d, c32 ? kAperture32 : kAperture16,
+                                         fmaxf(kMinTraceStepFactor, P.d.min_trace_step_factor)};
+    unsigned long long steps = 0;
+    deal_diffuse<kExactWarps>(D, march, steps);
+    add_steps(step_counter, steps);
+}
+
+// One warp per specular cone of the list (kept in the coherent order).
+template <class Atlas>
+__global__ void __launch_bounds__(256) k_exact_specular(TraceParams P, Atlas T,
+                                                        const vct_surface_sample* __restrict__ samples,
+                                                        const uint32_t* __restrict__ list,
+                                                        const unsigned int* __restrict__ spec_count,
+                                                        float* __restrict__ sout,
+                                                        unsigned long long* __restrict__ step_counter) {
+    const vct_cone_tracing_desc& d = P.d;
+    const int lane = threadIdx.x & 31;
+    const int64_t m = *spec_count;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    unsigned long long steps = 0;
+    for (int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < m; c += nwarps) {
+        const uint32_t idx = __ldg(list + c);
+        const GSample g = load_sample(samples + idx, P.eye);
+        const float min_level = calc_min_level(d, g.wp);
+        const float vs = d.voxel_size * exp2f(min_level);
+        const float3 start = g.wp + g.normal * (vs * d.trace_start_offset);
+        const float3 sdir = reflect3(f3(-g.view.x, -g.view.y, -g.view.z), g.normal);
+        const ConeGeo K = make_cone(d, start, sdir, fmaxf(g.roughness, kMinSpecularAperture), min_level, d.voxel_size);
+        const float4 r = trace_cone_warp_exact(T, d, K, kMaxTraceDistance, steps);
+        if (lane == 0) {
+            const float isi = d.indirect_specular_intensity;
+            const uint32_t mode = d.rendering_mode;
+            float4 S = make_float4(0.f, 0.f, 0.f, 1.f);  // write_outputs' specular output
+            if (mode == 6 || mode >= 8)
+                S = make_float4(0.f + r.x * g.specular_color.x * isi, 0.f + r.y * g.specular_color.y * isi,
+                                0.f + r.z * g.specular_color.z * isi, 1.f);
+            reinterpret_cast<float4*>(sout)[idx] = S;
+        }
+    }
+    add_steps(step_counter, steps);
+}
+
+// Specular classification of the ordered samples (the shader traces a
+// specular cone where depth != 1 and the sample has a specular colour and
+// metalness): key 0 for specular samples, 256 otherwise, and their count.
+__global__ void k_exact_spec_keys(const vct_surface_sample* __restrict__ samples, int64_t n,
+                                  const uint32_t* __restrict__ order, uint32_t* __restrict__ spec_key,
+                                  unsigned int* __restrict__ spec_count) {
+    const int lane = threadIdx.x & 31;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + threadIdx.x - lane; base < n;
+         base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t pos = base + lane;
+        bool spec = false;
+        if (pos < n) {
+            const float4* q = reinterpret_cast<const float4*>(samples + __ldg(order + pos));
+            const float4 a = __ldg(q + 0), d = __ldg(q + 3);
+            spec = a.w != 1.0f && (d.x > 1e-6f || d.y > 1e-6f || d.z > 1e-6f) && d.w > 1e-6f;
+        }
+        if (pos < n) spec_key[pos] = spec ? 0u : 256u;
+        const unsigned bal = __ballot_sync(0xffffffffu, spec);
+        if (lane == 0 && bal) atomicAdd(spec_count, (unsigned)__popc(bal));
     }
 }
 
@@ -164,19 +205,70 @@ int fill_trace_params(TraceParams& P, const vct_cone_tracing_desc* desc, const v
     return VCT_OK;
 }
 
-// One thread per sample, the samples walked in the coherent order (normal class, then Morton).
+// The samples in the coherent order (normal class, then Morton), the
+// specular ones listed in that order, then the diffuse and specular kernels.
+// Scratch is stream-ordered (cudaMallocAsync, freed after the kernels).
+// Counts of 2^30 samples or more run in chunks (the orders are 32-bit).
 template <class Atlas>
 static int launch_exact(const TraceParams& P, const Atlas& T, const vct_surface_sample* samples, int64_t n,
                         float* dout, float* sout, unsigned long long* cone_steps, cudaStream_t st) {
-    SampleOrder so;
-    int rc = sample_coherent_order(samples, n, P.d, &so, st);
-    if (rc != VCT_OK) return rc;
-    int64_t blocks = (n + 127) / 128;
-    if (blocks > 152 * 16) blocks = 152 * 16;
-    k_cone_trace_exact<<<(int)blocks, 128, 0, st>>>(P, T, samples, n, so.order, dout, sout, cone_steps);
-    cudaError_t e = cudaGetLastError();
-    if (so.block) cudaFreeAsync(so.block, st);
-    if (e != cudaSuccess) return cuda_fail(e, "k_cone_trace_exact");
+    constexpr int64_t kChunk = 1LL << 30;
+    for (int64_t off = 0; off < n; off += kChunk) {
+        const int64_t m = n - off < kChunk ? n - off : kChunk;
+        const vct_surface_sample* smp = samples + off;
+        SampleOrder so;
+        int rc = sample_coherent_order(smp, m, P.d, &so, st);
+        if (rc != VCT_OK) return rc;
+        size_t temp = 0;
+        cudaError_t e = cub::DeviceRadixSort::SortPairs(nullptr, temp, (uint32_t*)nullptr, (uint32_t*)nullptr,
+                                                        (uint32_t*)nullptr, (uint32_t*)nullptr, (int)m, 8, 9, st);
+        const size_t arr4 = (4 * (size_t)m + 255) & ~(size_t)255;
+        char* b = nullptr;
+        if (e == cudaSuccess) e = cudaMallocAsync((void**)&b, 4 * arr4 + 256 + temp, st);
+        if (e != cudaSuccess) {
+            if (so.block) cudaFreeAsync(so.block, st);
+            return cuda_fail(e, "cone trace scratch");
+        }
+        uint32_t* identity = (uint32_t*)b;  // used when the coherent order is the identity (one sample)
+        uint32_t* spec_key = (uint32_t*)(b + arr4);
+        uint32_t* spec_key_out = (uint32_t*)(b + 2 * arr4);
+        uint32_t* spec_list = (uint32_t*)(b + 3 * arr4);
+        unsigned int* spec_count = (unsigned int*)(b + 4 * arr4);
+        void* sort_temp = b + 4 * arr4 + 256;
+        const uint32_t* order = so.order;
+        if (!order) {
+            // n == 1 (the coherent order is only built for n >= 2)
+            const uint32_t zero = 0;
+            e = cudaMemcpyAsync(identity, &zero, sizeof(zero), cudaMemcpyHostToDevice, st);
+            order = identity;
+        }
+        if (e == cudaSuccess) e = cudaMemsetAsync(spec_count, 0, sizeof(unsigned int), st);
+        const int64_t gb = (m + 255) / 256;
+        if (e == cudaSuccess) {
+            k_exact_spec_keys<<<(int)(gb > 152 * 16 ? 152 * 16 : gb), 256, 0, st>>>(smp, m, order, spec_key,
+                                                                                   spec_count);
+            e = cudaGetLastError();
+        }
+        // stable partition (one radix pass on bit 8): specular samples first, the order kept
+        if (e == cudaSuccess)
+            e = cub::DeviceRadixSort::SortPairs(sort_temp, temp, spec_key, spec_key_out, order, spec_list, (int)m, 8, 9,
+                                                st);
+        const int64_t gdw = (m + 32 * kExactWarps - 1) / (32 * kExactWarps);
+        if (e == cudaSuccess) {
+            k_exact_diffuse<<<(int)(gdw > 152 * 16 ? 152 * 16 : gdw), 32 * kExactWarps, 0, st>>>(
+                P, T, smp, m, order, dout + 4 * off, sout + 4 * off, cone_steps);
+            e = cudaGetLastError();
+        }
+        const int64_t gw = (m * 32 + 255) / 256;
+        if (e == cudaSuccess) {
+            k_exact_specular<<<(int)(gw > 152 * 32 ? 152 * 32 : gw), 256, 0, st>>>(P, T, smp, spec_list, spec_count,
+                                                                                  sout + 4 * off, cone_steps);
+            e = cudaGetLastError();
+        }
+        cudaFreeAsync(b, st);
+        if (so.block) cudaFreeAsync(so.block, st);
+        if (e != cudaSuccess) return cuda_fail(e, "exact cone trace");
+    }
     return VCT_OK;
 }
 }  // namespace vct

@@ -20,7 +20,7 @@
 // the caller; vct_cone_trace_fast_scratch_bytes() gives its size.
 #include <cub/cub.cuh>
 
-#include "trace_common.cuh"
+#include "trace_deal.cuh"
 
 struct vct_texture_s;
 
@@ -183,125 +183,23 @@ __global__ void k_spec_keys(const __grid_constant__ FastArgs A, const uint32_t* 
 
 constexpr int kWarpsPerBlock = 8;
 
+// The diffuse cones, dealt to the lanes of a warp (trace_deal.cuh), each
+// marched by trace_cone_fast.
+struct FastDiffuseMarch {
+    cudaTextureObject_t tex;
+    const FastConsts* C;
+    __device__ __forceinline__ float4 operator()(float3 start, float3 dir, float start_level,
+                                                 unsigned long long& steps) const {
+        return trace_cone_fast(tex, *C, start, dir, C->coef_diffuse, start_level, C->sf_diffuse, steps);
+    }
+};
+
 __global__ void __launch_bounds__(256) k_trace_diffuse(const __grid_constant__ FastArgs A, const uint32_t* __restrict__ order) {
-    __shared__ float4 s_start[kWarpsPerBlock][32];
-    __shared__ float4 s_norm[kWarpsPerBlock][32];
-    __shared__ int s_cincl[kWarpsPerBlock][32];     // inclusive prefix of the pairs per cone
-    __shared__ uint32_t s_cmask[kWarpsPerBlock][32];  // samples (lanes) that trace each cone
-    __shared__ float4 s_res[kWarpsPerBlock][32];
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const TraceParams& P = A.P;
-    const FastConsts& C = A.C;
-    const bool c32 = C.ncones == 32;
+    DealArgs D{&A.P, A.samples, A.n, order, 0u, (uint32_t)A.n, A.dout, A.sout, A.C.ncones, A.C.need_diffuse != 0,
+               A.C.need_specular != 0};
     unsigned long long steps = 0;
-    const int64_t nwarps = (int64_t)gridDim.x * kWarpsPerBlock;
-    for (int64_t base = ((int64_t)blockIdx.x * kWarpsPerBlock + w) * 32; base < A.n; base += nwarps * 32) {
-        const int64_t pos = base + lane;
-        bool valid = pos < A.n;
-        const uint32_t idx = valid ? __ldg(order + pos) : 0u;
-        GSample g;
-        float min_level = 0.0f;
-        float3 start = f3(0.f, 0.f, 0.f);
-        uint32_t mask = 0;
-        if (valid) {
-            g = load_sample(A.samples + idx, P.eye);
-            valid = g.depth != 1.0f;
-        }
-        if (valid) {
-            min_level = calc_min_level(P.d, g.wp);
-            const float vs = C.uvs * exp2f(min_level);
-            start = g.wp + g.normal * (vs * C.start_off);
-            if (C.need_diffuse)
-                for (int c = 0; c < C.ncones; ++c) {
-                    const float3 dir = c32 ? f3(c_dirs32[c][0], c_dirs32[c][1], c_dirs32[c][2])
-                                           : f3(c_dirs16[c][0], c_dirs16[c][1], c_dirs16[c][2]);
-                    if (!(dot3(g.normal, dir) < 0.0f)) mask |= 1u << c;
-                }
-        }
-        // Deal the (sample, cone) pairs cone-major: lane k of a round takes the
-        // k-th pair of the list ordered by cone, then by sample, so neighbouring
-        // lanes march the same direction from neighbouring (Morton-ordered)
-        // samples and share texels.  Cone c's pairs are the lanes of cmask[c].
-        uint32_t my_cmask = 0;
-        for (int c = 0; c < C.ncones; ++c) {
-            const uint32_t cm = __ballot_sync(0xffffffffu, (mask >> c) & 1u);
-            if (lane == c) my_cmask = cm;
-        }
-        int cincl = __popc(my_cmask);
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int t = __shfl_up_sync(0xffffffffu, cincl, o);
-            if (lane >= o) cincl += t;
-        }
-        const int total = __shfl_sync(0xffffffffu, cincl, 31);
-        s_start[w][lane] = make_float4(start.x, start.y, start.z, min_level);
-        s_norm[w][lane] = valid ? make_float4(g.normal.x, g.normal.y, g.normal.z, 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
-        s_cincl[w][lane] = cincl;
-        s_cmask[w][lane] = my_cmask;
-        __syncwarp();
-        float4 acc = make_float4(0.f, 0.f, 0.f, 1.f);
-        const uint32_t below = (1u << lane) - 1u;
-        uint32_t pending = mask;  // this lane's cones not yet added, added in cone order
-        for (int r0 = 0; r0 < total; r0 += 32) {
-            const int k = r0 + lane;
-            float4 res = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (k < total) {
-                int lo = 0, hi = 31;  // the cone whose inclusive prefix first exceeds k
-                while (lo < hi) {
-                    const int mid = (lo + hi) >> 1;
-                    if (s_cincl[w][mid] > k) hi = mid;
-                    else lo = mid + 1;
-                }
-                const int cone = lo;
-                const uint32_t cm = s_cmask[w][cone];
-                const int j = k - (s_cincl[w][cone] - __popc(cm));
-                const int sl = (int)__fns(cm, 0, j + 1);  // the sample's lane
-                const float3 dir = c32 ? f3(c_dirs32[cone][0], c_dirs32[cone][1], c_dirs32[cone][2])
-                                       : f3(c_dirs16[cone][0], c_dirs16[cone][1], c_dirs16[cone][2]);
-                const float4 st = s_start[w][sl];
-                const float4 nn = s_norm[w][sl];
-                const float cos_t = nn.x * dir.x + nn.y * dir.y + nn.z * dir.z;
-                const float4 r =
-                    trace_cone_fast(A.tex, C, f3(st.x, st.y, st.z), dir, C.coef_diffuse, st.w, C.sf_diffuse, steps);
-                res = make_float4(r.x * cos_t, r.y * cos_t, r.z * cos_t, r.w * cos_t);
-            }
-            s_res[w][lane] = res;
-            __syncwarp();
-            // this lane's pairs in this round, lowest cone first: a pair's index
-            // grows with its cone, so the sum runs in cone order (the shader's)
-            while (pending) {
-                const int c = __ffs(pending) - 1;
-                const uint32_t cm = s_cmask[w][c];
-                const int pidx = s_cincl[w][c] - __popc(cm) + __popc(cm & below);
-                if (pidx >= r0 + 32) break;
-                const float4 v = s_res[w][pidx - r0];
-                acc = make_float4(acc.x + v.x, acc.y + v.y, acc.z + v.z, acc.w + v.w);
-                pending &= pending - 1u;
-            }
-            __syncwarp();
-        }
-        bool spec = false;
-        if (valid) {
-            const vct_cone_tracing_desc& d = P.d;
-            const float inv_n = 1.0f / (float)C.ncones;
-            float4 ind = make_float4(acc.x * inv_n, acc.y * inv_n, acc.z * inv_n, acc.w * inv_n);
-            ind.w = ind.w * d.ambient_occlusion_factor;
-            ind.x = ind.x * (g.diffuse_color.x * d.indirect_diffuse_intensity);
-            ind.y = ind.y * (g.diffuse_color.y * d.indirect_diffuse_intensity);
-            ind.z = ind.z * (g.diffuse_color.z * d.indirect_diffuse_intensity);
-            const float3 direct = direct_term(P, g);
-            spec = C.need_specular && has_specular_cone(g);
-            float4 dd[2];
-            write_outputs(P, g, min_level, ind, f3(0.f, 0.f, 0.f), direct, reinterpret_cast<float*>(&dd[0]),
-                          reinterpret_cast<float*>(&dd[1]));
-            reinterpret_cast<float4*>(A.dout)[idx] = dd[0];
-            if (!spec) reinterpret_cast<float4*>(A.sout)[idx] = dd[1];
-        }
-    }
-    if (A.steps) {
-        for (int o = 16; o > 0; o >>= 1) steps += __shfl_xor_sync(0xffffffffu, steps, o);
-        if (lane == 0 && steps) atomicAdd(A.steps, steps);
-    }
+    deal_diffuse<kWarpsPerBlock>(D, FastDiffuseMarch{A.tex, &A.C}, steps);
+    add_steps(A.steps, steps);
 }
 
 // One step of a cone: the sample's contribution (rgb * corr, opacity) and
