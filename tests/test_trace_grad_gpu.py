@@ -1,9 +1,20 @@
 """The differentiable form on the GPU: the FP32 trace over a float atlas
-against the oracle's FP64 trace of the same atlas, and its adjoint
-(vct_cone_trace_backward) against central finite differences of the FP64
-oracle on a 32^3 clipmap with 256 samples (the survey's check for this
-configuration).  The test volume keeps alpha below 0.3, so no clamp and no
-occlusion stop switches under the perturbations."""
+against the oracle's FP64 trace of the same atlas, and the adjoints
+(vct_cone_trace_backward, vct_downsample_backward) against the oracle's FP64
+reference gradients -- reverse-mode differentiation of the restated trace
+and mips (oracle/adjoint_oracle.hpp), compared entry by entry -- and against
+central finite differences of the FP64 oracle on a 32^3 clipmap with 256
+samples (the survey's check for this configuration).  The test volume keeps
+alpha below 0.3, so no clamp and no occlusion stop switches under the
+perturbations.
+
+Bars: every gradient entry within 1e-4 of the largest entry's magnitude of
+the FP64 reference and relative L2 error below 1e-4; finite differences
+within 1e-4 relative (plus 1e-6 of the largest entry for the near-zero ones).
+Entries above 1 % of the largest are also held entry by entry: FP32 atomics
+sum each texel's shares in no fixed order, and an entry built from shares of
+both signs keeps their rounding, so the measured relative error of such
+entries reaches 2.5e-4 (relative L2 6e-6 overall); the bar there is 5e-4."""
 import numpy as np
 import pytest
 
@@ -51,6 +62,55 @@ def test_f32_forward_matches_fp64_oracle(cuda, oracle):
     assert np.abs(d64[:, :3]).sum() > 1.0 and np.abs(s64[:, :3]).sum() > 0.1
 
 
+TOL_REF = 1e-4  # against the FP64 reference gradient, relative to its largest entry / relative L2
+TOL_REF_ENTRY = 5e-4  # entries above 1 % of the largest, relative (FP32 atomic accumulation; measured 2.5e-4)
+TOL_FD = 1e-4   # against FP64 central differences, relative
+
+
+def _grad_stats(got, want):
+    scale = float(np.abs(want).max())
+    err = np.abs(got.astype(np.float64) - want)
+    big = np.abs(want) > 1e-2 * scale
+    return {"rel_l2": float(np.linalg.norm(err) / np.linalg.norm(want)), "max_err_over_max": float(err.max() / scale),
+            "max_rel_big": float((err[big] / np.abs(want[big])).max()), "entries": int(np.count_nonzero(want))}
+
+
+def _gpu_backward(torch, desc, samples, R, v, s, cam, light, wd, ws):
+    import ctypes as C
+    from vk_voxel_cone_tracing_gb300 import capi
+    n = samples.shape[0]
+    gd = torch.from_numpy(wd).cuda()
+    gs = torch.from_numpy(ws).cuda()
+    G = torch.zeros_like(v)
+    capi.call("vct_cone_trace_backward", capi.ref(desc), capi.ref(cam), C.c_void_p(v.data_ptr()), R, None,
+              capi.ref(light), None, C.c_void_p(s.data_ptr()), n, C.c_void_p(gd.data_ptr()),
+              C.c_void_p(gs.data_ptr()), C.c_void_p(G.data_ptr()), None)
+    torch.cuda.synchronize()
+    return G.cpu().numpy()
+
+
+@pytest.mark.parametrize("mode", [8, 7, 6])
+def test_backward_matches_fp64_reference_gradient(cuda, oracle, mode):
+    """Every entry of the GPU adjoint against reverse-mode differentiation of the FP64 oracle."""
+    torch = cuda
+    R = 32
+    vol, desc, samples = _setup(R, seed=3 + mode)
+    desc.rendering_mode = mode
+    n = samples.shape[0]
+    rng = np.random.default_rng(mode)
+    wd = rng.normal(size=(n, 4)).astype(np.float32)
+    ws = rng.normal(size=(n, 4)).astype(np.float32)
+    _, _, (v, s, cam, light) = _gpu_forward(torch, vol, desc, samples, R)
+    grad = _gpu_backward(torch, desc, samples, R, v, s, cam, light, wd, ws).reshape(vol.shape)
+    ref = oracle.cone_trace_grad_f4(bytes(desc), (0.0, 3.0, -3.0), vol, R, samples, wd, ws)
+    st = _grad_stats(grad, ref)
+    print("trace adjoint vs FP64 reference", mode, st)
+    assert st["entries"] > 10000
+    assert st["rel_l2"] < TOL_REF and st["max_err_over_max"] < TOL_REF and st["max_rel_big"] < TOL_REF_ENTRY, st
+    # untouched texels stay exactly zero
+    assert np.all(grad[ref == 0] == 0) or np.count_nonzero(grad[ref == 0]) < 1e-4 * ref.size
+
+
 @pytest.mark.parametrize("mode", [8, 7, 6])
 def test_backward_matches_finite_differences(cuda, oracle, mode):
     torch = cuda
@@ -64,15 +124,9 @@ def test_backward_matches_finite_differences(cuda, oracle, mode):
     wd = rng.normal(size=(n, 4)).astype(np.float32)
     ws = rng.normal(size=(n, 4)).astype(np.float32)
     _, _, (v, s, cam, light) = _gpu_forward(torch, vol, desc, samples, R)
-    gd = torch.from_numpy(wd).cuda()
-    gs = torch.from_numpy(ws).cuda()
-    G = torch.zeros_like(v)
-    capi.call("vct_cone_trace_backward", capi.ref(desc), capi.ref(cam), C.c_void_p(v.data_ptr()), R, None,
-              capi.ref(light), None, C.c_void_p(s.data_ptr()), n, C.c_void_p(gd.data_ptr()),
-              C.c_void_p(gs.data_ptr()), C.c_void_p(G.data_ptr()), None)
-    torch.cuda.synchronize()
-    grad = G.cpu().numpy().reshape(vol.shape)
+    grad = _gpu_backward(torch, desc, samples, R, v, s, cam, light, wd, ws).reshape(vol.shape)
     assert np.abs(grad).sum() > 0
+    scale = float(np.abs(grad).max())
 
     def loss(vv):
         d64, s64, _ = oracle.cone_trace_f4(bytes(desc), (0.0, 3.0, -3.0), vv, R, samples)
@@ -82,7 +136,7 @@ def test_backward_matches_finite_differences(cuda, oracle, mode):
     top = np.argsort(flat)[-24:]  # the largest entries, plus random touched ones
     touched = np.nonzero(flat)[0]
     pick = np.concatenate([top, rng.choice(touched, 12, replace=False)])
-    eps = np.float32(2e-3)
+    eps = np.float32(1e-3)
     bad = []
     for k in pick:
         vp, vm = vol.copy(), vol.copy()
@@ -92,7 +146,7 @@ def test_backward_matches_finite_differences(cuda, oracle, mode):
         hm = float(vol.reshape(-1)[k]) - float(vm.reshape(-1)[k])
         fd = (loss(vp) - loss(vm)) / (hp + hm)
         g = float(grad.reshape(-1)[k])
-        if abs(fd - g) > 2e-2 * max(abs(fd), abs(g)) + 1e-5:
+        if abs(fd - g) > TOL_FD * abs(fd) + 1e-6 * scale:
             bad.append((int(k), g, fd))
     assert not bad, bad[:6]
 
@@ -142,6 +196,11 @@ def test_downsample_f32_and_its_adjoint(cuda, oracle, mode):
                   capi.ref(_ds_desc(regions, level, R)), mode, None)
     torch.cuda.synchronize()
     grad = G.cpu().numpy().reshape(vol.shape)
+    # every entry against the FP64 reference adjoint of the chain
+    ref = oracle.downsample_chain_grad_f4(vol, R, regions, W, mode)
+    st = _grad_stats(grad, ref)
+    print("mip adjoint vs FP64 reference", mode, st)
+    assert st["rel_l2"] < TOL_REF and st["max_err_over_max"] < TOL_REF and st["max_rel_big"] < TOL_REF_ENTRY, st
     # entries of level 0 (which feed the whole chain) and of the mipped levels
     D, H, W_ = vol.shape[:3]
     picks = []
@@ -160,6 +219,6 @@ def test_downsample_f32_and_its_adjoint(cuda, oracle, mode):
         h = float(vp[z, y, x, c]) - float(vm[z, y, x, c])
         fd = float(((chain_oracle(vp) - chain_oracle(vm)).astype(np.float64) * W).sum()) / h
         g = float(grad[z, y, x, c])
-        if abs(fd - g) > 1e-3 * max(abs(fd), abs(g)) + 2e-5:
+        if abs(fd - g) > TOL_FD * abs(fd) + 1e-6 * float(np.abs(ref).max()):
             bad.append(((z, y, x, c), g, fd))
     assert not bad, bad[:6]

@@ -2,33 +2,39 @@
 // (vct_cone_trace_f32): given dL/d(diffuse out) and dL/d(specular out) per
 // sample, accumulate dL/d(texel) into a float RGBA atlas of the same layout.
 //
-// One thread per (cone, sample), cone-major: the diffuse cones and the specular cone of
-// voxelConeTracing.frag:143-293.  The march's step schedule, levels, tap
-// positions, opacity corrections and occlusion decay depend on geometry
-// only; the number of steps depends on the volume through the occlusion
-// stop and is held fixed (the derivative of a piecewise-smooth function away
-// from its switches; likewise the clamps of opacity and of 1 - alpha).
+// The march's step schedule, levels, tap positions, opacity corrections and
+// occlusion divisors depend on geometry only; the number of steps depends on
+// the volume through the occlusion stop and is held fixed (the derivative of
+// a piecewise-smooth function away from its switches).  The clamps of the
+// opacity and of 1 - alpha pass the derivative of their argument when it lies
+// in [0, 1], bounds included: from an empty texel (alpha 0) the opacity's
+// right derivative reaches it, which is the one inverse fitting needs.
 //
-// The cone state runs forward as
-//     k_i   = clamp(1 - A_i, 0, 1)                 (A: accumulated alpha)
-//     op_i  = clamp(1 - (1 - s_i.a)^c_i, 0, 1)     (c: opacity correction)
-//     C    += k_i c_i s_i.rgb,   A += k_i op_i
-//     O    += (1 - O) op_i / (1 + (t_i + vs_i) decay)
-// and the adjoint runs it backward (gC constant along the march):
-//     g(s_i.rgb) = gC k_i c_i
-//     g(op_i)    = gA k_i + gO (1 - O_i) / (1 + (t_i + vs_i) decay)
-//     g(s_i.a)   = g(op_i) c_i (1 - s_i.a)^(c_i - 1)      (inside the clamp)
-//     gA        += -(gC . s_i.rgb c_i + gA op_i)           (inside the clamp of k)
-//     gO        *= 1 - op_i / (1 + (t_i + vs_i) decay)
-// The backward needs A_i and O_i step by step in reverse: the forward pass
-// keeps a checkpoint of the march state every 32 steps, and each 32-step
-// segment is recomputed from its checkpoint before it is walked backward
-// (O(steps) work, a few KB of local memory per thread).  s_i is recomputed
-// from the atlas; g(s_i) is split over the two levels (1 - fr, fr), the three
-// faces (the direction weights) and the eight texels of each trilinear tap
-// (the products of the lerp fractions) and added to the gradient atlas with
-// float4 atomics.  Same FP32 expressions as the forward kernel (this unit is
-// built with -fmad=false like it), so the recomputed states are the forward's.
+// With T_i = prod_{m<i} (1 - op_m) (the weight clamp(1 - alpha) of step i),
+// U_i = prod_{m<i} (1 - op_m / q_m) (1 - occlusion before step i),
+// q_i = 1 + (t_i + vs_i) decay and c_i the opacity correction, the cone
+// returns C = sum_i T_i c_i s_i.rgb and O = 1 - U_n, so for L = gC . C + gO O
+//     dL/d(s_i.rgb) = gC T_i c_i
+//     dL/d(op_i)    = -T_i R_i + gO U_i V_i / q_i,
+//     R_i = sum_{j>i} prod_{i<m<j} (1 - op_m) c_j gC . s_j.rgb,
+//     V_i = prod_{j>i} (1 - op_j / q_j),
+//     dL/d(s_i.a)   = dL/d(op_i) c_i (1 - s_i.a)^(c_i - 1).
+// g(s_i) is split over the two levels (1 - fr, fr), the three faces (the
+// direction weights) and the eight texels of each trilinear tap (the products
+// of the lerp fractions) and added to the gradient atlas with float4 atomics.
+// Same FP32 expressions as the forward kernels (this unit is built with
+// -fmad=false like them), so the recomputed steps are the forward's.
+//
+// Diffuse cones: one lane per (cone, sample), cone-major, the warp's lanes in
+// lock step (all diffuse cones share one step schedule); a checkpoint of the
+// march state every 32 steps, each segment recomputed from its checkpoint and
+// walked backward with the recurrences above in sequential form.
+// Specular cones (57 to thousands of steps): one warp per cone, 64 steps per
+// round as in the forward kernel; a forward pass keeps the schedule and the
+// composite at each round's start in shared memory, and a reverse pass over
+// the rounds recomputes each round's steps, forms T_i, U_i by a warp scan
+// from the round's start and R_i, V_i by a reverse warp scan from the rounds
+// after it, and scatters.
 #include "trace_exact.cuh"
 
 namespace vct {
@@ -41,14 +47,11 @@ namespace {
 
 constexpr int kSegSteps = 32;
 constexpr int kMaxSegments = 256;  // 8192 steps per cone: the specular cone at R = 1024 takes ~7.1k
+constexpr int kMaxRounds = kMaxSegments * kSegSteps / (32 * kExactStepsPerLane);
+constexpr int kSpecWarps = 4;      // warps per block of the specular adjoint
 
 struct MarchState {
     float step, seg, diameter, alpha, occ;
-};
-
-struct Cone {
-    float3 start, dir, fo, wt, center;
-    float uvs, coef, start_level, step_factor, min_radius;
 };
 
 __device__ __forceinline__ void add4(float4* p, float4 v) {
@@ -100,65 +103,55 @@ __device__ __forceinline__ void sample_clipmap_grad(float4* __restrict__ G, cons
     }
 }
 
-// The volume-independent part of one step of trace_cone at state m.
-struct StepGeo {
-    float3 pos;
-    int lower, upper;
-    float fr, vs, correction;
-};
-
-__device__ __forceinline__ StepGeo step_geo(const Cone& K, const MarchState& m) {
-    StepGeo s;
-    s.pos = K.start + K.dir * m.step;
-    float dist = sqrtf(dot3(K.center - s.pos, K.center - s.pos));
-    float min_level = ceilf(log2f(dist / K.min_radius));
-    float cur_level = log2f(m.diameter / K.uvs);
-    cur_level = fminf(fmaxf(fmaxf(K.start_level, cur_level), min_level), (float)(kClipLevels - 1));
-    s.lower = (int)floorf(cur_level);
-    s.upper = (int)ceilf(cur_level);
-    s.fr = fractf(cur_level);
-    s.vs = K.uvs * exp2f(cur_level);
-    s.correction = m.seg / s.vs;
-    return s;
+// g(s) of one step spread over its levels, faces and texels.
+__device__ __forceinline__ void scatter_step(float4* __restrict__ G, const AtlasDims& A, const vct_cone_tracing_desc& d,
+                                             const ConeGeo& K, float3 pos, int lower, int upper, float fr, float4 gs) {
+    // s = lo (1 - fr) + hi fr: the lower level's share, then the upper's (zero when fr = 0)
+#pragma unroll 1
+    for (int lv = 0; lv < 2; ++lv) {
+        const float f = lv ? fr : 1.0f - fr;
+        if (f == 0.0f) continue;
+        sample_clipmap_grad(G, A, d, pos, lv ? upper : lower, K.fo, K.wt,
+                            make_float4(gs.x * f, gs.y * f, gs.z * f, gs.w * f));
+    }
 }
 
-// One step of trace_cone (same expressions): advances m (alpha, occlusion,
-// schedule) and returns the step's sample.
-__device__ __forceinline__ float4 march_step(const F4Atlas& T, const vct_cone_tracing_desc& d, const Cone& K,
-                                             MarchState& m, const StepGeo& s) {
-    float4 lo = sample_clipmap(T, d, s.pos, s.lower, K.fo, K.wt);
-    float4 hi = sample_clipmap(T, d, s.pos, s.upper, K.fo, K.wt);
-    float4 smp = make_float4(lo.x * (1.0f - s.fr) + hi.x * s.fr, lo.y * (1.0f - s.fr) + hi.y * s.fr,
-                             lo.z * (1.0f - s.fr) + hi.z * s.fr, lo.w * (1.0f - s.fr) + hi.w * s.fr);
-    float opacity = clampf(1.0f - powf(1.0f - smp.w, s.correction), 0.0f, 1.0f);
-    float k = clampf(1.0f - m.alpha, 0.0f, 1.0f);
-    m.alpha = m.alpha + k * opacity;
-    m.occ = m.occ + (1.0f - m.occ) * opacity / (1.0f + (m.step + s.vs) * d.occlusion_decay);
-    float prev = m.step;
-    m.step = m.step + fmaxf(m.diameter, K.uvs) * K.step_factor;
-    m.seg = m.step - prev;
-    m.diameter = m.step * K.coef;
-    return smp;
+// d(op)/d(s.a) for op = clamp(1 - (1 - s.a)^c, 0, 1), the bounds inside.
+__device__ __forceinline__ float opacity_slope(const StepDetail& e) {
+    const float base = 1.0f - e.smp.w;
+    return (e.op_raw >= 0.0f && e.op_raw <= 1.0f && base > 0.0f) ? e.correction * powf(base, e.correction - 1.0f)
+                                                                   : 0.0f;
 }
 
-// The adjoint of one cone per lane: gC (rgb) and gO (d/d occlusion) at the
-// end of the march.  The warp's lanes run in lock step: every loop runs to
-// the warp's longest march and a lane sits out the steps its cone does not
-// have (or all of them when `active` is false), so a warp walks one step
-// index at a time -- no divergent loop control, and with cone-major Morton-
-// ordered lanes the taps of a step land on neighbouring texels.  The forward
-// recompute of a segment keeps each step's filtered sample, so the reverse
-// walk reads no texels.
-__device__ void cone_backward(const F4Atlas& T, float4* __restrict__ G, const vct_cone_tracing_desc& d, const Cone& K,
-                              float3 gC, float gO, bool active, float max_dist, int* __restrict__ err) {
+// One step of trace_cone (same expressions) at march state m: advances m
+// (alpha, occlusion, schedule) and returns the step.
+__device__ __forceinline__ StepDetail march_step(const F4Atlas& T, const vct_cone_tracing_desc& d, const ConeGeo& K,
+                                                 MarchState& m) {
+    const Sched s{m.step, m.seg, m.diameter};
+    const StepDetail e = exact_step_detail(T, d, K, s);
+    const float k = clampf(1.0f - m.alpha, 0.0f, 1.0f);
+    m.alpha = m.alpha + k * e.op;
+    m.occ = m.occ + (1.0f - m.occ) * e.op / e.q;
+    Sched n = s;
+    sched_advance(n, K);
+    m.step = n.step;
+    m.seg = n.seg;
+    m.diameter = n.diameter;
+    return e;
+}
+
+// The adjoint of one diffuse cone per lane: gC (rgb) and gO (d/d occlusion)
+// at the end of the march.  The warp's lanes run in lock step: every loop
+// runs to the warp's longest march and a lane sits out the steps its cone
+// does not have (or all of them when `active` is false).  The forward
+// recompute of a segment keeps each step, so the reverse walk reads no texels.
+__device__ void cone_backward_lane(const F4Atlas& T, float4* __restrict__ G, const vct_cone_tracing_desc& d,
+                                   const ConeGeo& K, float3 gC, float gO, bool active, float max_dist,
+                                   int* __restrict__ err) {
     constexpr unsigned kFull = 0xffffffffu;
     MarchState ckpt[kMaxSegments];
-    MarchState m;
-    m.step = 0.0f;
-    m.diameter = fmaxf(0.0f * K.coef, K.uvs);
-    m.seg = K.uvs * exp2f(K.start_level);
-    m.alpha = 0.0f;
-    m.occ = 0.0f;
+    const Sched s0 = first_sched(K);
+    MarchState m{s0.step, s0.seg, s0.diameter, 0.0f, 0.0f};
     int n = 0;
     bool running = active && m.step < max_dist && m.occ < 1.0f;
     for (int j = 0; __any_sync(kFull, running); ++j) {
@@ -168,7 +161,7 @@ __device__ void cone_backward(const F4Atlas& T, float4* __restrict__ G, const vc
         }
         if (running) {
             if ((j % kSegSteps) == 0) ckpt[j / kSegSteps] = m;
-            march_step(T, d, K, m, step_geo(K, m));
+            march_step(T, d, K, m);
             ++n;
             running = m.step < max_dist && m.occ < 1.0f;
         }
@@ -176,7 +169,7 @@ __device__ void cone_backward(const F4Atlas& T, float4* __restrict__ G, const vc
     const int nmax = __reduce_max_sync(kFull, n);
     float gA = 0.0f;
     MarchState seg[kSegSteps];
-    float4 seg_smp[kSegSteps];
+    StepDetail seg_step[kSegSteps];
     for (int sidx = (nmax - 1) / kSegSteps; nmax > 0 && sidx >= 0; --sidx) {
         const int first = sidx * kSegSteps, last = min(nmax, first + kSegSteps);
         const int mine = min(n, first + kSegSteps);  // this lane's steps of the segment: first .. mine - 1
@@ -185,55 +178,221 @@ __device__ void cone_backward(const F4Atlas& T, float4* __restrict__ G, const vc
         for (int i = first; i < last; ++i) {
             if (i < mine) {
                 seg[i - first] = r;
-                seg_smp[i - first] = march_step(T, d, K, r, step_geo(K, r));
+                seg_step[i - first] = march_step(T, d, K, r);
             }
         }
         for (int i = last - 1; i >= first; --i) {
             if (i >= mine) continue;
             const MarchState& mi = seg[i - first];
-            const StepGeo s = step_geo(K, mi);
-            const float4 smp = seg_smp[i - first];
-            const float c = s.correction;
-            const float base = 1.0f - smp.w;
-            const float op_raw = 1.0f - powf(base, c);
-            const float op = clampf(op_raw, 0.0f, 1.0f);
-            const float dop = (op_raw > 0.0f && op_raw < 1.0f && base > 0.0f) ? c * powf(base, c - 1.0f) : 0.0f;
+            const StepDetail& e = seg_step[i - first];
+            const float c = e.correction;
             const float k_raw = 1.0f - mi.alpha;
             const float k = clampf(k_raw, 0.0f, 1.0f);
-            const float qd = 1.0f + (mi.step + s.vs) * d.occlusion_decay;
             float4 gs;
             gs.x = gC.x * k * c;
             gs.y = gC.y * k * c;
             gs.z = gC.z * k * c;
-            const float gop = gA * k + gO * (1.0f - mi.occ) / qd;
-            gs.w = gop * dop;
-            if (k_raw > 0.0f && k_raw < 1.0f) gA = gA - ((gC.x * smp.x + gC.y * smp.y + gC.z * smp.z) * c + gA * op);
-            gO = gO * (1.0f - op / qd);
-            // s = lo (1 - fr) + hi fr: the lower level's share, then the upper's (zero when fr = 0)
-#pragma unroll 1
-            for (int lv = 0; lv < 2; ++lv) {
-                const float f = lv ? s.fr : 1.0f - s.fr;
-                if (f == 0.0f) continue;
-                sample_clipmap_grad(G, T.A, d, s.pos, lv ? s.upper : s.lower, K.fo, K.wt,
-                                    make_float4(gs.x * f, gs.y * f, gs.z * f, gs.w * f));
-            }
+            const float gop = gA * k + gO * (1.0f - mi.occ) / e.q;
+            gs.w = gop * opacity_slope(e);
+            if (k_raw >= 0.0f && k_raw <= 1.0f)
+                gA = gA - ((gC.x * e.smp.x + gC.y * e.smp.y + gC.z * e.smp.z) * c + gA * e.op);
+            gO = gO * (1.0f - e.op / e.q);
+            scatter_step(G, T.A, d, K, e.pos, e.lower, e.upper, e.fr, gs);
         }
     }
 }
 
-__global__ void __launch_bounds__(128) k_cone_trace_backward(TraceParams P, F4Atlas T,
-                                                             const vct_surface_sample* __restrict__ samples, int64_t n,
-                                                             const uint32_t* __restrict__ order,
-                                                             const float4* __restrict__ gd, const float4* __restrict__ gs,
-                                                             float4* __restrict__ G, int* __restrict__ err) {
+// The suffix of a march from some step to its end: P = prod (1 - op),
+// R = sum_j prod_{m<j} (1 - op_m) c_j gC . s_j.rgb, V = prod (1 - op / q).
+struct Suffix {
+    float P, R, V;
+};
+
+// `a` followed by `b`.
+__device__ __forceinline__ Suffix then(const Suffix& a, const Suffix& b) {
+    return Suffix{a.P * b.P, a.R + a.P * b.R, a.V * b.V};
+}
+
+__device__ __forceinline__ Suffix step_suffix(const StepDetail& e, float3 gC) {
+    const float w = (gC.x * e.smp.x + gC.y * e.smp.y + gC.z * e.smp.z) * e.correction;
+    return Suffix{1.0f - e.op, w, 1.0f - e.op / e.q};
+}
+
+__device__ __forceinline__ Suffix shfl_suffix(const Suffix& s, int src) {
+    return Suffix{__shfl_sync(0xffffffffu, s.P, src), __shfl_sync(0xffffffffu, s.R, src),
+                  __shfl_sync(0xffffffffu, s.V, src)};
+}
+
+// The state at the first step of a round: the schedule and the composite of
+// the steps before it (its alpha a = 1 - T and its t = U).
+struct RoundStart {
+    float step, seg, diameter, a, t;
+};
+
+// The adjoint of one cone marched by the whole warp (steps over the lanes).
+// `rounds` is this warp's shared-memory array of kMaxRounds round starts.
+__device__ void cone_backward_warp(const F4Atlas& T, float4* __restrict__ G, const vct_cone_tracing_desc& d,
+                                   const ConeGeo& K, float3 gC, float gO, float max_dist,
+                                   RoundStart* __restrict__ rounds, int* __restrict__ err) {
+    constexpr int S = kExactStepsPerLane;
+    const int lane = threadIdx.x & 31;
+    const Composite id{0.0f, 0.0f, 0.0f, 0.0f, 1.0f};
+    // forward: the rounds' starts and the number of steps the loop takes
+    Composite carried = id;
+    Sched round0 = first_sched(K);
+    int nsteps = 0, nrounds = 0;
+    for (;;) {
+        if (nrounds == kMaxRounds) {
+            if (lane == 0) atomicOr(err, 1);
+            return;
+        }
+        if (lane == 0) rounds[nrounds] = RoundStart{round0.step, round0.seg, round0.diameter, carried.a, carried.t};
+        Sched s = round0;
+        for (int k = 0; k < S * lane; ++k) sched_advance(s, K);
+        const Sched mine = s;
+        Composite x = id;
+        int nvalid = 0;
+#pragma unroll
+        for (int k = 0; k < S; ++k) {
+            if (s.step < max_dist) {
+                x = over(x, as_composite(exact_step(T, d, K, s)));
+                ++nvalid;
+            }
+            sched_advance(s, K);
+        }
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const Composite p = shfl_composite(x, (lane - o) & 31);
+            if (lane >= o) x = over(p, x);
+        }
+        const Composite after = over(carried, x);
+        ++nrounds;
+        const unsigned tmask = __ballot_sync(0xffffffffu, nvalid > 0 && (1.0f - after.t) >= 1.0f);
+        if (tmask) {  // the loop stops within lane L's steps (the forward kernel's rule)
+            const int L = __ffs(tmask) - 1;
+            const Composite prior = shfl_composite(x, (lane - 1) & 31);
+            int done = 0;
+            if (lane == L) {
+                const Composite before = lane == 0 ? carried : over(carried, prior);
+                float occ = 1.0f - before.t;
+                Sched q = mine;
+                for (int k = 0; k < S && q.step < max_dist && occ < 1.0f; ++k) {
+                    const ExactStep e = exact_step(T, d, K, q);
+                    occ = occ + (1.0f - occ) * e.op / e.q;
+                    ++done;
+                    sched_advance(q, K);
+                }
+            }
+            nsteps += S * L + __shfl_sync(0xffffffffu, done, L);
+            break;
+        }
+        carried = shfl_composite(after, 31);
+        int nv = nvalid;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) nv += __shfl_xor_sync(0xffffffffu, nv, o);
+        nsteps += nv;
+        if (nv < 32 * S) break;
+        round0 = Sched{__shfl_sync(0xffffffffu, s.step, 31), __shfl_sync(0xffffffffu, s.seg, 31),
+                       __shfl_sync(0xffffffffu, s.diameter, 31)};
+    }
+    __syncwarp();
+    // reverse: rounds last to first, carrying the suffix of the rounds after
+    Suffix tail{1.0f, 0.0f, 1.0f};
+    for (int r = nrounds - 1; r >= 0; --r) {
+        const RoundStart rs = rounds[r];
+        Sched s{rs.step, rs.seg, rs.diameter};
+        for (int k = 0; k < S * lane; ++k) sched_advance(s, K);
+        const int first = r * 32 * S + S * lane;  // this lane's first step index
+        StepDetail e[S];
+        bool valid[S];
+        Composite x = id;
+        Suffix own{1.0f, 0.0f, 1.0f};
+#pragma unroll
+        for (int k = 0; k < S; ++k) {
+            valid[k] = first + k < nsteps;
+            if (valid[k]) {
+                e[k] = exact_step_detail(T, d, K, s);
+                x = over(x, Composite{e[k].smp.x * e[k].correction, e[k].smp.y * e[k].correction,
+                                      e[k].smp.z * e[k].correction, e[k].op, 1.0f - e[k].op / e[k].q});
+                own = then(own, step_suffix(e[k], gC));
+            }
+            sched_advance(s, K);
+        }
+        // exclusive prefix composite of the lanes before this one, from the round's start
+        Composite pre = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const Composite p = shfl_composite(pre, (lane - o) & 31);
+            if (lane >= o) pre = over(p, pre);
+        }
+        Composite before = shfl_composite(pre, (lane - 1) & 31);
+        const Composite start{0.0f, 0.0f, 0.0f, rs.a, rs.t};
+        before = lane == 0 ? start : over(start, before);
+        // inclusive suffix of the lanes from this one to the round's end, then the rounds after
+        Suffix suf = own;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const Suffix q = shfl_suffix(suf, (lane + o) & 31);
+            if (lane + o < 32) suf = then(suf, q);
+        }
+        Suffix after = shfl_suffix(suf, (lane + 1) & 31);
+        after = lane == 31 ? tail : then(after, tail);
+        const Suffix round_total = then(shfl_suffix(suf, 0), tail);
+        // this lane's steps, last first: the suffix after step k, the prefix before it
+        Suffix rest = after;
+#pragma unroll
+        for (int k = S - 1; k >= 0; --k) {
+            if (!valid[k]) continue;
+            Composite pk = before;
+            for (int j = 0; j < k; ++j)
+                if (valid[j]) pk = over(pk, Composite{0.0f, 0.0f, 0.0f, e[j].op, 1.0f - e[j].op / e[j].q});
+            const float Tk = clampf(1.0f - pk.a, 0.0f, 1.0f), Uk = pk.t;
+            const float c = e[k].correction;
+            const float gop = -Tk * rest.R + gO * Uk * rest.V / e[k].q;
+            const float4 gs = make_float4(gC.x * Tk * c, gC.y * Tk * c, gC.z * Tk * c, gop * opacity_slope(e[k]));
+            scatter_step(G, T.A, d, K, e[k].pos, e[k].lower, e[k].upper, e[k].fr, gs);
+            rest = then(step_suffix(e[k], gC), rest);
+        }
+        tail = round_total;
+    }
+}
+
+// dL/d(indirect) -> the diffuse cones' gC and gO; false when the mode does
+// not read the volume through the diffuse cones.
+__device__ __forceinline__ bool diffuse_seeds(const TraceParams& P, const GSample& g, float4 GD, float cos_t, int nc,
+                                              float3& gC, float& gO) {
+    const vct_cone_tracing_desc& d = P.d;
+    const uint32_t mode = d.rendering_mode;
+    // D.rgb = direct * ind.w + ind.rgb (modes 5 and the default), direct * ind.w (4), ind.w (7)
+    float3 g_ind = f3(0.f, 0.f, 0.f);
+    float g_ao = 0.0f;
+    const bool rgb_mode = mode == 5 || mode >= 8;
+    if (rgb_mode) g_ind = f3(GD.x, GD.y, GD.z);
+    if (rgb_mode || mode == 4) {
+        const float3 direct = direct_term(P, g);
+        g_ao = GD.x * direct.x + GD.y * direct.y + GD.z * direct.z;
+    } else if (mode == 7) {
+        g_ao = GD.x + GD.y + GD.z;
+    }
+    const float w = cos_t / (float)nc;
+    gC = f3(g_ind.x * w * (g.diffuse_color.x * d.indirect_diffuse_intensity),
+            g_ind.y * w * (g.diffuse_color.y * d.indirect_diffuse_intensity),
+            g_ind.z * w * (g.diffuse_color.z * d.indirect_diffuse_intensity));
+    gO = -(g_ao * w * d.ambient_occlusion_factor);  // the cone returns 1 - occlusion
+    return !(gC.x == 0.0f && gC.y == 0.0f && gC.z == 0.0f && gO == 0.0f);
+}
+
+__global__ void __launch_bounds__(128) k_cone_backward_diffuse(TraceParams P, F4Atlas T,
+                                                               const vct_surface_sample* __restrict__ samples,
+                                                               int64_t n, const uint32_t* __restrict__ order,
+                                                               const float4* __restrict__ gd, float4* __restrict__ G,
+                                                               int* __restrict__ err) {
     const vct_cone_tracing_desc& d = P.d;
     const bool c32 = d.enable_32_cones != 0;
     const int nc = c32 ? 32 : 16;
-    const int slots = nc + 1;
-    const uint32_t mode = d.rendering_mode;
     const int lane = threadIdx.x & 31;
-    const int64_t total = n * slots;
-    // warp-uniform trip count: a warp's lanes enter cone_backward together
+    const int64_t total = n * nc;
+    // warp-uniform trip count: a warp's lanes enter cone_backward_lane together
     for (int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x - lane; t0 < total;
          t0 += (int64_t)gridDim.x * blockDim.x) {
         const int64_t t = t0 + lane;
@@ -243,60 +402,51 @@ __global__ void __launch_bounds__(128) k_cone_trace_backward(TraceParams P, F4At
         const int slot = active ? (int)(t / n) : 0;
         const int64_t u = active ? t - (int64_t)slot * n : 0;
         const int64_t i = order ? (int64_t)__ldg(order + u) : u;
-        GSample g = load_sample(samples + i, P.eye);
+        const GSample g = load_sample(samples + i, P.eye);
         active = active && g.depth != 1.0f;
-        float min_level = calc_min_level(d, g.wp);
-        float vs = d.voxel_size * exp2f(min_level);
-        Cone K;
-        K.start = g.wp + g.normal * (vs * d.trace_start_offset);
-        K.uvs = d.voxel_size;
-        K.center = f3(d.volume_center[0], d.volume_center[1], d.volume_center[2]);
-        K.min_radius = K.uvs * d.volume_dimension * 0.5f;
-        K.start_level = min_level;
+        const float min_level = calc_min_level(d, g.wp);
+        const float vs = d.voxel_size * exp2f(min_level);
+        const float3 start = g.wp + g.normal * (vs * d.trace_start_offset);
+        const float3 dir = c32 ? f3(c_dirs32[slot][0], c_dirs32[slot][1], c_dirs32[slot][2])
+                               : f3(c_dirs16[slot][0], c_dirs16[slot][1], c_dirs16[slot][2]);
+        const float cos_t = dot3(g.normal, dir);
+        active = active && cos_t >= 0.0f;
         float3 gC = f3(0.f, 0.f, 0.f);
         float gO = 0.0f;
-        float aperture;
-        const float4 GD = gd[i], GS = gs[i];
-        if (slot < nc) {
-            K.dir = c32 ? f3(c_dirs32[slot][0], c_dirs32[slot][1], c_dirs32[slot][2])
-                        : f3(c_dirs16[slot][0], c_dirs16[slot][1], c_dirs16[slot][2]);
-            const float cos_t = dot3(g.normal, K.dir);
-            active = active && cos_t >= 0.0f;
-            // dL/d(indirect): D.rgb = direct * ind.w + ind.rgb (modes 5 and the default), direct * ind.w (4),
-            // ind.w (7); the others do not read the volume
-            float3 g_ind = f3(0.f, 0.f, 0.f);
-            float g_ao = 0.0f;
-            const bool rgb_mode = mode == 5 || mode >= 8;
-            if (rgb_mode) g_ind = f3(GD.x, GD.y, GD.z);
-            if (active && (rgb_mode || mode == 4)) {
-                const float3 direct = direct_term(P, g);
-                g_ao = GD.x * direct.x + GD.y * direct.y + GD.z * direct.z;
-            } else if (mode == 7) {
-                g_ao = GD.x + GD.y + GD.z;
-            }
-            const float w = cos_t / (float)nc;
-            gC = f3(g_ind.x * w * (g.diffuse_color.x * d.indirect_diffuse_intensity),
-                    g_ind.y * w * (g.diffuse_color.y * d.indirect_diffuse_intensity),
-                    g_ind.z * w * (g.diffuse_color.z * d.indirect_diffuse_intensity));
-            gO = -(g_ao * w * d.ambient_occlusion_factor);  // the cone returns 1 - occlusion
-            aperture = c32 ? kAperture32 : kAperture16;
-            K.step_factor = fmaxf(kMinTraceStepFactor, d.min_trace_step_factor);
-        } else {
-            active = active && has_specular_cone(g) && (mode == 6 || mode >= 8);
-            K.dir = reflect3(f3(-g.view.x, -g.view.y, -g.view.z), g.normal);
-            const float isi = d.indirect_specular_intensity;
-            gC = f3(GS.x * g.specular_color.x * isi, GS.y * g.specular_color.y * isi, GS.z * g.specular_color.z * isi);
-            gO = 0.0f;
-            aperture = fmaxf(g.roughness, kMinSpecularAperture);
-            K.step_factor = d.voxel_size;
-        }
-        active = active && !(gC.x == 0.0f && gC.y == 0.0f && gC.z == 0.0f && gO == 0.0f);
-        K.coef = 2.0f * tanf(aperture * 0.5f);
-        K.start = K.start + K.dir * (K.uvs * exp2f(K.start_level) * d.trace_start_offset * 0.5f);
-        K.fo = f3(K.dir.x > 0.0f ? 0.0f : 1.0f / 6.0f, K.dir.y > 0.0f ? 2.0f / 6.0f : 3.0f / 6.0f,
-                  K.dir.z > 0.0f ? 4.0f / 6.0f : 5.0f / 6.0f);
-        K.wt = f3(K.dir.x * K.dir.x, K.dir.y * K.dir.y, K.dir.z * K.dir.z);
-        cone_backward(T, G, d, K, gC, gO, active, kMaxTraceDistance, err);
+        active = active && diffuse_seeds(P, g, gd[i], cos_t, nc, gC, gO);
+        const ConeGeo K = make_cone(d, start, dir, c32 ? kAperture32 : kAperture16, min_level,
+                                    fmaxf(kMinTraceStepFactor, d.min_trace_step_factor));
+        cone_backward_lane(T, G, d, K, gC, gO, active, kMaxTraceDistance, err);
+    }
+}
+
+// One warp per sample in the coherent order; samples without a specular cone
+// (or a zero specular gradient) are skipped by the whole warp.
+__global__ void __launch_bounds__(32 * kSpecWarps) k_cone_backward_specular(
+    TraceParams P, F4Atlas T, const vct_surface_sample* __restrict__ samples, int64_t n,
+    const uint32_t* __restrict__ order, const float4* __restrict__ gsp, float4* __restrict__ G,
+    int* __restrict__ err) {
+    __shared__ RoundStart s_rounds[kSpecWarps][kMaxRounds];
+    const vct_cone_tracing_desc& d = P.d;
+    const int w = threadIdx.x >> 5;
+    const int64_t nwarps = (int64_t)gridDim.x * kSpecWarps;
+    if (!(d.rendering_mode == 6 || d.rendering_mode >= 8)) return;
+    for (int64_t u = (int64_t)blockIdx.x * kSpecWarps + w; u < n; u += nwarps) {
+        const int64_t i = order ? (int64_t)__ldg(order + u) : u;
+        const GSample g = load_sample(samples + i, P.eye);
+        if (g.depth == 1.0f || !has_specular_cone(g)) continue;
+        const float4 GS = gsp[i];
+        const float isi = d.indirect_specular_intensity;
+        const float3 gC = f3(GS.x * g.specular_color.x * isi, GS.y * g.specular_color.y * isi,
+                             GS.z * g.specular_color.z * isi);
+        if (gC.x == 0.0f && gC.y == 0.0f && gC.z == 0.0f) continue;
+        const float min_level = calc_min_level(d, g.wp);
+        const float vs = d.voxel_size * exp2f(min_level);
+        const float3 start = g.wp + g.normal * (vs * d.trace_start_offset);
+        const float3 sdir = reflect3(f3(-g.view.x, -g.view.y, -g.view.z), g.normal);
+        const ConeGeo K = make_cone(d, start, sdir, fmaxf(g.roughness, kMinSpecularAperture), min_level, d.voxel_size);
+        cone_backward_warp(T, G, d, K, gC, 0.0f, kMaxTraceDistance, s_rounds[w], err);
+        __syncwarp();
     }
 }
 
@@ -328,26 +478,32 @@ extern "C" int vct_cone_trace_backward(const vct_cone_tracing_desc* desc, const 
     VCT_CUDA_TRY(cudaMallocAsync(&err, sizeof(int), st));
     VCT_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), st));
     F4Atlas T{reinterpret_cast<const float4*>(atlas4), AtlasDims(R)};
-    const int slots = (desc->enable_32_cones ? 32 : 16) + 1;
-    int64_t blocks = (n * slots + 127) / 128;
+    const int nc = desc->enable_32_cones ? 32 : 16;
+    int64_t blocks = (n * nc + 127) / 128;
     if (blocks > 152 * 32) blocks = 152 * 32;
+    int64_t sblocks = (n + kSpecWarps - 1) / kSpecWarps;
+    if (sblocks > 152 * 16) sblocks = 152 * 16;
     SampleOrder so;
     rc = sample_coherent_order(samples, n, P.d, &so, st);
     if (rc != VCT_OK) {
         cudaFreeAsync(err, st);
         return rc;
     }
-    k_cone_trace_backward<<<(int)blocks, 128, 0, st>>>(P, T, samples, n, so.order,
-                                                        reinterpret_cast<const float4*>(grad_diffuse),
-                                                        reinterpret_cast<const float4*>(grad_specular),
-                                                        reinterpret_cast<float4*>(grad_atlas4), err);
+    float4* G = reinterpret_cast<float4*>(grad_atlas4);
+    k_cone_backward_diffuse<<<(int)blocks, 128, 0, st>>>(P, T, samples, n, so.order,
+                                                          reinterpret_cast<const float4*>(grad_diffuse), G, err);
     cudaError_t le = cudaGetLastError();
+    if (le == cudaSuccess) {
+        k_cone_backward_specular<<<(int)sblocks, 32 * kSpecWarps, 0, st>>>(
+            P, T, samples, n, so.order, reinterpret_cast<const float4*>(grad_specular), G, err);
+        le = cudaGetLastError();
+    }
     int h_err = 0;
     cudaError_t ce = cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, st);
     cudaError_t se = cudaStreamSynchronize(st);
     cudaFreeAsync(err, st);
     if (so.block) cudaFreeAsync(so.block, st);
-    if (le != cudaSuccess) return cuda_fail(le, "k_cone_trace_backward");
+    if (le != cudaSuccess) return cuda_fail(le, "vct_cone_trace_backward kernels");
     if (ce != cudaSuccess) return cuda_fail(ce, "vct_cone_trace_backward readback");
     if (se != cudaSuccess) return cuda_fail(se, "vct_cone_trace_backward");
     if (h_err) return fail(VCT_E_OVERFLOW, "vct_cone_trace_backward: a cone marched more than 8192 steps");
