@@ -424,6 +424,15 @@ def run_ours(args, world, rank, local):
     rendered_ms = statistics.median(events_ms(stream, rendered_frame, max(3, args.steps))[0])
     filter_bytes = GW * GH * 48  # diffuse + specular texel read, output written (RGBA32F)
 
+    forms = other_forms(dev, stream, R, regs, desc, radiance, samples, light, shadow, lsd, max(3, args.steps)) \
+        if args.form == "tex" and not args.no_batch and world == 1 else None
+    if forms is not None:
+        rate_tex = cone_samples / (ms * 1e-3)
+        forms["texture_rgba8"] = {"trace_ms": ms, "cone_samples_per_s": rate_tex}
+        forms["ratio_fp16_vs_exact_fp32"] = forms["texture_rgba16f"]["cone_samples_per_s"] / \
+            forms["exact_rgba8"]["cone_samples_per_s"]
+        forms["ratio_rgba8_texture_vs_exact_fp32"] = rate_tex / forms["exact_rgba8"]["cone_samples_per_s"]
+        frame()  # restore the RGBA8 texture the frame keeps (the FP16 section used its own)
     batch = batched_scenes(dev) if not args.no_batch and world == 1 else None
     diff = differentiable_volume(dev) if not args.no_batch and world == 1 else None
     svo_large = large_svo(dev, max(3, args.steps)) if not args.no_batch and world == 1 else None
@@ -505,6 +514,7 @@ def run_ours(args, world, rank, local):
                        "svo_fragments": int(frags.shape[0]), "svo_nodes": int(nodes.value),
                        "svo_trace": {"samples": svo_n, "ms": svo_trace_ms, "cone_samples_per_s": svo_trace_rate},
                        "voxelize_svo_mip_ms": frame_ms + svo_ms,
+                       "forms": forms,
                        "batched_scenes": batch,
                        "differentiable": diff,
                        "svo_large": svo_large,
@@ -552,6 +562,60 @@ def run_ours(args, world, rank, local):
         tex.close()
     if world > 1:
         dist.destroy_process_group()
+
+
+def other_forms(dev, stream, R, regs, desc, radiance, samples, light, shadow, lsd, reps):
+    """The two other forms of the trace on the benchmark's frame and samples: the FP16-storage form (the
+    frame's radiance converted to RGBA16F with FP16 mips, written into an RGBA16F texture as the passes run;
+    FP32 compositing) and the exact FP32 drop-in (software trilinear over the linear RGBA8 atlas, the
+    shader's arithmetic).  CUDA events on the launching stream, median over `reps`."""
+    import torch
+
+    from vk_voxel_cone_tracing_gb300 import capi, clipmap
+    n = samples.shape[0]
+    dout = torch.empty((n, 4), dtype=torch.float32, device=dev)
+    sout = torch.empty((n, 4), dtype=torch.float32, device=dev)
+    out = {}
+    tex16 = clipmap.RadianceTexture(R, capi.TEX_RGBA16F)
+    a16 = clipmap.new_atlas_rgba16f(R, dev)
+
+    def fp16_passes():
+        clipmap.to_rgba16f(radiance, R, out=a16, mirror=tex16)
+        clipmap.cmd_downsample_rgba16f_all(a16, R, regs, 1, mirror=tex16)
+
+    scratch = clipmap.fast_scratch(n, dev)
+
+    def fp16_trace(counter=None):
+        clipmap.cone_trace_fast(desc, EYE, tex16, samples, light=light, shadow=shadow, shadow_desc=lsd, diffuse=dout,
+                                specular=sout, steps=counter, scratch=scratch)
+
+    for _ in range(2):
+        fp16_passes()
+    passes_ms = statistics.median(events_ms(stream, fp16_passes, reps)[0])
+    ctr = torch.zeros(1, dtype=torch.int64, device=dev)
+    fp16_trace(ctr)
+    for _ in range(2):
+        fp16_trace()
+    t16 = statistics.median(events_ms(stream, fp16_trace, reps)[0])
+    c16 = int(ctr.item())
+    out["texture_rgba16f"] = {"trace_ms": t16, "cone_samples": c16, "cone_samples_per_s": c16 / (t16 * 1e-3),
+                              "conversion_and_fp16_mips_ms": passes_ms,
+                              "note": "radiance mips recomputed in FP16 from level 0, FP32 compositing"}
+    tex16.close()
+    del a16, scratch
+
+    def exact_trace(counter=None):
+        clipmap.cone_trace(desc, EYE, radiance, R, samples, light=light, shadow=shadow, shadow_desc=lsd,
+                           diffuse=dout, specular=sout, steps=counter)
+
+    ctr.zero_()
+    exact_trace(ctr)
+    exact_trace()
+    te = statistics.median(events_ms(stream, exact_trace, reps)[0])
+    ce = int(ctr.item())
+    out["exact_rgba8"] = {"trace_ms": te, "cone_samples": ce, "cone_samples_per_s": ce / (te * 1e-3),
+                          "note": "the plain FP32 drop-in: software trilinear over the linear RGBA8 atlas"}
+    return out
 
 
 def batched_scenes(dev, streams: int = 4, n_scenes: int = 64, seed: int = 4):
