@@ -493,7 +493,9 @@ struct ClipmapTracer {
             vs = uvs * std::exp2(cur_level);
             T correction = seg / vs;
             V3<T> radiance(s.x * correction, s.y * correction, s.z * correction);
-            T opacity = clampv(T(1) - std::pow(T(1) - s.w, correction), T(0), T(1));
+            // a filtered alpha that rounds above 1 would give pow a negative base (undefined in GLSL); the
+            // base is taken as 0 there (the sample is opaque), pinned the same way in every GPU form
+            T opacity = clampv(T(1) - std::pow(std::max(T(1) - s.w, T(0)), correction), T(0), T(1));
             T k = clampv(T(1) - result.w, T(0), T(1));
             result = V4<T>(result.x + k * radiance.x, result.y + k * radiance.y, result.z + k * radiance.z,
                            result.w + k * opacity);
@@ -567,7 +569,8 @@ struct SurfaceSample {
 // Writes diffuse/specular RGBA; returns false if the fragment is discarded.
 template <class T, class Fetch>
 inline bool trace_sample(ClipmapTracer<T, Fetch>& tr, const float eye[3], const float* shadow, int sw, int sh,
-                         const ShadowDesc& sd, const LightDesc& light, const SurfaceSample& s, T out_d[4], T out_s[4]) {
+                         const ShadowDesc& sd, const LightDesc& light, const SurfaceSample& s, T out_d[4], T out_s[4],
+                         float diffuse_aperture = 0.0f) {
     const TraceDesc& d = tr.d;
     if (T(s.depth) == T(1)) return false;
     V3<T> wp(T(s.position[0]), T(s.position[1]), T(s.position[2]));
@@ -588,7 +591,8 @@ inline bool trace_sample(ClipmapTracer<T, Fetch>& tr, const float eye[3], const 
     V4<T> indirect(T(0), T(0), T(0), T(1));
     const bool c32 = d.enable_32_cones != 0;
     const int n = c32 ? 32 : 16;
-    const T aperture = T(c32 ? kAperture32 : kAperture16);
+    // the shader's constant, or a configured aperture (vct_trace_options)
+    const T aperture = T(diffuse_aperture != 0.0f ? diffuse_aperture : (c32 ? kAperture32 : kAperture16));
     const T sf = std::max(T(kMinTraceStepFactor), T(d.min_trace_step_factor));
     for (int i = 0; i < n; ++i) {
         const float* dd = c32 ? kDirs32[i] : kDirs16[i];

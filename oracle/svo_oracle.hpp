@@ -200,7 +200,8 @@ struct SvoTracer {
             vs = uvs * std::exp2(cur_level);
             T correction = seg / vs;
             V3<T> radiance(s.x * correction, s.y * correction, s.z * correction);
-            T opacity = clampv(T(1) - std::pow(T(1) - s.w, correction), T(0), T(1));
+            // base of pow clamped at 0, as in the clipmap tracer
+            T opacity = clampv(T(1) - std::pow(std::max(T(1) - s.w, T(0)), correction), T(0), T(1));
             T k = clampv(T(1) - result.w, T(0), T(1));
             result = V4<T>(result.x + k * radiance.x, result.y + k * radiance.y, result.z + k * radiance.z,
                            result.w + k * opacity);

@@ -79,7 +79,8 @@ __device__ float4 svo_trace_cone(const SvoScene& S, const vct_cone_tracing_desc&
         vs = uvs * exp2f(cur_level);
         const float correction = seg / vs;
         const float rx = s.x * correction, ry = s.y * correction, rz = s.z * correction;
-        const float opacity = clampf(1.0f - powf(1.0f - s.w, correction), 0.0f, 1.0f);
+        // alpha rounded above 1 (a pow of a negative base, undefined in GLSL) is taken as 1
+        const float opacity = clampf(1.0f - powf(fmaxf(1.0f - s.w, 0.0f), correction), 0.0f, 1.0f);
         const float k = clampf(1.0f - result.w, 0.0f, 1.0f);
         result = make_float4(result.x + k * rx, result.y + k * ry, result.z + k * rz, result.w + k * opacity);
         occlusion = occlusion + (1.0f - occlusion) * opacity / (1.0f + (step + vs) * d.occlusion_decay);
