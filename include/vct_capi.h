@@ -402,6 +402,32 @@ int vct_cone_trace_fast(const vct_cone_tracing_desc* desc, const vct_cam_matrix*
                         float* diffuse_out, float* specular_out, unsigned long long* cone_steps,
                         void* scratch, size_t scratch_bytes, void* stream);
 
+/* Options of the _opt trace entry points; no counterpart in the reference,
+ * whose shader fixes its cone tables.  diffuse_aperture: the full cone angle,
+ * in radians, of every diffuse cone, in place of the shader's constant
+ * (0.872665 for the 16-cone set, 0.628319 for the 32-cone set,
+ * voxelConeTracing.frag:78-135); 0 keeps the constant, otherwise it must lie
+ * in (0, pi).  The cone directions stay the shader's.  reserved: zero. */
+typedef struct vct_trace_options {
+    float diffuse_aperture;
+    float reserved[3];
+} vct_trace_options;
+
+/* vct_cone_trace / vct_cone_trace_fast with options (NULL = none): the same
+ * passes, for workloads such as one of 16 fixed 30-degree cones
+ * (diffuse_aperture = 0.523599). */
+int vct_cone_trace_opt(const vct_cone_tracing_desc* desc, const vct_cam_matrix* cam, const uint32_t* radiance_atlas,
+                       int32_t R, const vct_shadow_map* shadow, const vct_directional_light_desc* light,
+                       const vct_directional_light_shadow_desc* light_shadow, const vct_surface_sample* samples,
+                       int64_t sample_count, float* diffuse_out, float* specular_out, unsigned long long* cone_steps,
+                       const vct_trace_options* options, void* stream);
+int vct_cone_trace_fast_opt(const vct_cone_tracing_desc* desc, const vct_cam_matrix* cam, vct_texture radiance,
+                            const vct_shadow_map* shadow, const vct_directional_light_desc* light,
+                            const vct_directional_light_shadow_desc* light_shadow,
+                            const vct_surface_sample* samples, int64_t sample_count, float* diffuse_out,
+                            float* specular_out, unsigned long long* cone_steps, const vct_trace_options* options,
+                            void* scratch, size_t scratch_bytes, void* stream);
+
 /* Calibration probe for the trace's roofline; no counterpart in the
  * reference.  Times (CUDA events on `stream`, after one warm-up launch) a
  * kernel that marches `cones` synthetic cones of `steps_per_cone` steps, one
@@ -799,5 +825,6 @@ VCT_STATIC_ASSERT(sizeof(vct_context_buffers) == 216, "vct_context_buffers is 21
 VCT_STATIC_ASSERT(sizeof(vct_batch_job) == 264, "vct_batch_job is 264 B");
 VCT_STATIC_ASSERT(sizeof(vct_gltf_shade_material) == 80, "GltfShadeMaterial is 80 B");
 VCT_STATIC_ASSERT(sizeof(vct_surface_sample) == 80, "surface sample is 80 B");
+VCT_STATIC_ASSERT(sizeof(vct_trace_options) == 16, "vct_trace_options is 16 B");
 
 #endif /* VCT_CAPI_H */

@@ -67,6 +67,9 @@ def lib():
         L.vcto_copy_alpha.argtypes = [P, P, C.c_int, C.c_int, C.c_int]
         L.vcto_wrap_border.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int]
         L.vcto_downsample.argtypes = [P, C.c_int, P, C.c_int, C.c_int, C.c_int]
+        L.vcto_cone_trace_opt.restype = C.c_uint64
+        L.vcto_cone_trace_opt.argtypes = [C.c_int, P, P, P, C.c_int, P, C.c_int, C.c_int, P, P, P, C.c_int64,
+                                          C.c_int64, P, P, P, C.c_float]
         L.vcto_cone_trace.restype = C.c_uint64
         L.vcto_cone_trace.argtypes = [C.c_int, P, P, P, C.c_int, P, C.c_int, C.c_int, P, P, P, C.c_int64,
                                       C.c_int64, P, P, P]
@@ -177,8 +180,10 @@ def default_light_bytes() -> bytes:
 
 def cone_trace(precision: int, desc_bytes: bytes, eye, atlas: np.ndarray, R: int, samples: np.ndarray,
                shadow: np.ndarray | None = None, shadow_desc_bytes: bytes | None = None,
-               light_bytes: bytes | None = None, begin: int = 0, end: int | None = None):
-    """Trace samples [begin, end) with the FP32 (precision=32) or FP64 (64) restatement.
+               light_bytes: bytes | None = None, begin: int = 0, end: int | None = None,
+               diffuse_aperture: float = 0.0):
+    """Trace samples [begin, end) with the FP32 (precision=32) or FP64 (64) restatement; a non-zero
+    `diffuse_aperture` (radians) replaces the shader's diffuse cone aperture.
 
     Returns (diffuse[n,4] f64, specular[n,4] f64, steps, written[n] u8)."""
     n = samples.shape[0]
@@ -191,8 +196,9 @@ def cone_trace(precision: int, desc_bytes: bytes, eye, atlas: np.ndarray, R: int
     light = np.frombuffer(light_bytes or default_light_bytes(), np.uint8).copy()
     eye = np.asarray(eye, np.float32)
     sh, sw = (shadow.shape if shadow is not None else (0, 0))
-    steps = lib().vcto_cone_trace(precision, _p(desc), _p(eye), _p(atlas), R, _p(shadow), sw, sh, _p(sd),
-                                  _p(light), _p(samples), begin, end, _p(dout), _p(sout), _p(written))
+    steps = lib().vcto_cone_trace_opt(precision, _p(desc), _p(eye), _p(atlas), R, _p(shadow), sw, sh, _p(sd),
+                                      _p(light), _p(samples), begin, end, _p(dout), _p(sout), _p(written),
+                                      float(diffuse_aperture))
     return dout, sout, int(steps), written
 
 

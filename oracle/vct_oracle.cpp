@@ -48,10 +48,10 @@ void vcto_downsample_f4(float* atlas4, int R, const int prev_min[3], int level, 
 // Cone trace over an RGBA8 atlas.  precision: 32 = FP32 mirror, 64 = FP64.
 // Samples [begin, end) are traced; outputs are 4 doubles per sample.
 // Returns the number of traceCone loop iterations executed.
-uint64_t vcto_cone_trace(int precision, const TraceDesc* desc, const float eye[3], const uint32_t* atlas, int R,
-                         const float* shadow, int sw, int sh, const ShadowDesc* sd, const LightDesc* light,
-                         const SurfaceSample* samples, int64_t begin, int64_t end, double* out_d, double* out_s,
-                         uint8_t* written) {
+uint64_t vcto_cone_trace_opt(int precision, const TraceDesc* desc, const float eye[3], const uint32_t* atlas, int R,
+                             const float* shadow, int sw, int sh, const ShadowDesc* sd, const LightDesc* light,
+                             const SurfaceSample* samples, int64_t begin, int64_t end, double* out_d, double* out_s,
+                             uint8_t* written, float diffuse_aperture) {
     Atlas A(R);
     uint64_t total = 0;
 #pragma omp parallel for schedule(dynamic, 64) reduction(+ : total)
@@ -61,7 +61,7 @@ uint64_t vcto_cone_trace(int precision, const TraceDesc* desc, const float eye[3
             Rgba8Fetch<double> f{atlas, A};
             ClipmapTracer<double, Rgba8Fetch<double>> tr{*desc, f, A};
             double d[4], s[4];
-            ok = trace_sample<double>(tr, eye, shadow, sw, sh, *sd, *light, samples[i], d, s);
+            ok = trace_sample<double>(tr, eye, shadow, sw, sh, *sd, *light, samples[i], d, s, diffuse_aperture);
             if (ok)
                 for (int c = 0; c < 4; ++c) {
                     out_d[4 * i + c] = d[c];
@@ -72,7 +72,7 @@ uint64_t vcto_cone_trace(int precision, const TraceDesc* desc, const float eye[3
             Rgba8Fetch<float> f{atlas, A};
             ClipmapTracer<float, Rgba8Fetch<float>> tr{*desc, f, A};
             float d[4], s[4];
-            ok = trace_sample<float>(tr, eye, shadow, sw, sh, *sd, *light, samples[i], d, s);
+            ok = trace_sample<float>(tr, eye, shadow, sw, sh, *sd, *light, samples[i], d, s, diffuse_aperture);
             if (ok)
                 for (int c = 0; c < 4; ++c) {
                     out_d[4 * i + c] = d[c];
@@ -83,6 +83,14 @@ uint64_t vcto_cone_trace(int precision, const TraceDesc* desc, const float eye[3
         if (written) written[i] = ok ? 1 : 0;
     }
     return total;
+}
+
+uint64_t vcto_cone_trace(int precision, const TraceDesc* desc, const float eye[3], const uint32_t* atlas, int R,
+                         const float* shadow, int sw, int sh, const ShadowDesc* sd, const LightDesc* light,
+                         const SurfaceSample* samples, int64_t begin, int64_t end, double* out_d, double* out_s,
+                         uint8_t* written) {
+    return vcto_cone_trace_opt(precision, desc, eye, atlas, R, shadow, sw, sh, sd, light, samples, begin, end, out_d,
+                               out_s, written, 0.0f);
 }
 
 // Cone trace over a float4 atlas (unquantised storage) in FP64: the error

@@ -23,6 +23,7 @@ output: indirect diffuse + direct RGB, ambient occlusion, specular RGB) are
 written as JSON to the path in $VCT_ERROR_REPORT when it is set.
 """
 import json
+import math
 import os
 
 import numpy as np
@@ -268,6 +269,7 @@ def test_benchmark_workload_hall_r256(cuda, oracle):
 
 def test_configuration_1_room_at_stated_size(cuda, oracle):
     torch = cuda
+    from vk_voxel_cone_tracing_gb300 import clipmap
     from vk_voxel_cone_tracing_gb300.scene import room_scene, surface_samples
     R, cam, eye = 128, (0.0, 4.0, 0.0), (0.0, 4.0, -4.5)
     scene = room_scene(seed=1)
@@ -277,6 +279,22 @@ def test_configuration_1_room_at_stated_size(cuda, oracle):
     rows = {"samples": 65536, "R": R, "triangles": scene.triangle_count}
     base = _trace_all_forms(torch, oracle, rows, R, f["regions"], f["rad_np"], f["rad"], f["tex"], f["sh_np"],
                             f["sh"], samples, eye, f["light"], f["lsd"], f["sd_bytes"], f["regs"])
+    # the configuration's own cone set: 16 fixed 30-degree cones (the shader's aperture constant is 50 degrees)
+    ap = math.radians(30.0)
+    want, got_t, got_e = {}, {}, {}
+    dev_s = clipmap.samples_to_device(samples)
+    for mode in (8, 7):
+        desc = _desc_mode(base, mode)
+        want[mode] = oracle.cone_trace(64, bytes(desc), eye, f["rad_np"], R, samples, shadow=f["sh_np"],
+                                       shadow_desc_bytes=f["sd_bytes"], diffuse_aperture=ap)[:2]
+        got_t[mode] = [t.cpu().numpy() for t in clipmap.cone_trace_fast(
+            desc, eye, f["tex"], dev_s, light=f["light"], shadow=f["sh"], shadow_desc=f["lsd"], diffuse_aperture=ap)]
+        got_e[mode] = [t.cpu().numpy() for t in clipmap.cone_trace(
+            desc, eye, f["rad"], R, dev_s, light=f["light"], shadow=f["sh"], shadow_desc=f["lsd"],
+            diffuse_aperture=ap)]
+    w30 = _outputs(want[8], want[7])
+    _check_form(rows, "texture_rgba8_30deg_cones", _outputs(got_t[8], got_t[7]), w30)
+    _check_form(rows, "exact_rgba8_30deg_cones", _outputs(got_e[8], got_e[7]), w30)
     f["tex"].close()
     _svo_chain(torch, oracle, rows, scene, f["ds"], f["ws"], 7, f["sh_np"], f["sh"], f["sd_bytes"], f["light"],
                f["lsd"], base, samples, eye)

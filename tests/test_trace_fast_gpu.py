@@ -208,3 +208,41 @@ def test_gather_probe_reports_a_finite_rate_and_checks_arguments(cuda, oracle):
     rc = capi.lib().vct_gather_probe(capi.ref(desc), tex.handle, 0, 64, C.byref(out), None)
     assert rc == capi.VCT_E_BAD_ARG
     tex.close()
+
+
+def test_diffuse_aperture_option_thirty_degree_cones(cuda, oracle):
+    """vct_cone_trace_opt / vct_cone_trace_fast_opt with 16 fixed 30-degree cones: the exact form follows the
+    oracle's FP32 mirror per sample, both forms stay within the FP64 bar; bad options are rejected."""
+    import ctypes as C
+    import math
+    torch = cuda
+    from vk_voxel_cone_tracing_gb300 import capi, clipmap
+    R = 32
+    regions, desc, atlas, samples = _setup(oracle, R, 2000, seed=31)
+    ap = math.radians(30.0)
+    eye = (0.5, 1.0, -4.0)
+    d32, s32, st32, _ = oracle.cone_trace(32, bytes(desc), eye, atlas, R, samples, diffuse_aperture=ap)
+    d64, s64, _, _ = oracle.cone_trace(64, bytes(desc), eye, atlas, R, samples, diffuse_aperture=ap)
+    da = _dev(torch, atlas)
+    dev_s = clipmap.samples_to_device(samples)
+    steps = torch.zeros(1, dtype=torch.int64, device="cuda")
+    de, se = clipmap.cone_trace(desc, eye, da, R, dev_s, steps=steps, diffuse_aperture=ap)
+    tex = clipmap.RadianceTexture(R).update(da)
+    df, sf = clipmap.cone_trace_fast(desc, eye, tex, dev_s, diffuse_aperture=ap)
+    torch.cuda.synchronize()
+    de = de.cpu().numpy().astype(np.float64)
+    err = np.abs(de - d32).max(1) / np.maximum(np.abs(d32).max(1), 1e-3)
+    assert np.mean(err < 1e-4) > 0.99, np.sort(err)[-8:]
+    assert abs(int(steps.item()) - st32) <= max(8, 0.002 * st32)
+    for got in (de, df.cpu().numpy().astype(np.float64)):
+        assert _rel(got[:, :3], d64[:, :3]) < TOL_FP64
+    bad = capi.TraceOptions(4.0)
+    out = torch.zeros((2000, 4), device="cuda")
+    cam = clipmap.cam_matrix(eye)
+    light = capi.DirectionalLightDesc(capi.f3(0.3, -1.0, 0.2), 1.0, capi.f3(1, 1, 1), 0)
+    rc = capi.lib().vct_cone_trace_opt(capi.ref(desc), capi.ref(cam), C.c_void_p(da.data_ptr()), R, None,
+                                       capi.ref(light), None, C.c_void_p(dev_s.data_ptr()), 2000,
+                                       C.c_void_p(out.data_ptr()), C.c_void_p(out.data_ptr()), None, capi.ref(bad),
+                                       None)
+    assert rc == capi.VCT_E_BAD_ARG
+    tex.close()

@@ -92,6 +92,11 @@ class ConeTracingDesc(C.Structure):
                 ("occlusion_decay", C.c_float), ("enable_32_cones", C.c_int32)]
 
 
+class TraceOptions(C.Structure):
+    """vct_trace_options: diffuse_aperture (radians, 0 = the shader's constant), reserved zeros."""
+    _fields_ = [("diffuse_aperture", C.c_float), ("reserved", C.c_float * 3)]
+
+
 class CamMatrix(C.Structure):
     _fields_ = [("view_proj", f16), ("view_proj_inv", f16), ("eye_pos", f3), ("padding", C.c_int32)]
 
@@ -168,7 +173,7 @@ STRUCT_SIZES = {
     ClipmapRegion: 28, VoxelizationDesc: 64, DownSampleDesc: 24, ImageCleaningDesc: 36, CopyAlphaDesc: 12,
     BorderWrappingDesc: 16, ConeTracingDesc: 52, CamMatrix: 144, DirectionalLightDesc: 32,
     DirectionalLightShadowDesc: 136, GltfShadeMaterial: 80, Scene: 104, SpecularFilterDesc: 16, Config: 24,
-    ContextBuffers: 216, BatchJob: 264, AdamDesc: 40,
+    ContextBuffers: 216, BatchJob: 264, AdamDesc: 40, TraceOptions: 16,
 }
 
 # Every entry point of include/vct_capi.h: name -> (restype, argtypes).
@@ -187,6 +192,7 @@ _SIGS: dict[str, tuple] = {
     "vct_downsample_all": (C.c_int, [P, P, C.c_int32, C.c_int32, P]),
     "vct_wrap_border": (C.c_int, [P, P, P]),
     "vct_cone_trace": (C.c_int, [P, P, P, C.c_int32, P, P, P, P, C.c_int64, P, P, P, P]),
+    "vct_cone_trace_opt": (C.c_int, [P, P, P, C.c_int32, P, P, P, P, C.c_int64, P, P, P, P, P]),
     "vct_cone_trace_f32": (C.c_int, [P, P, P, C.c_int32, P, P, P, P, C.c_int64, P, P, P, P]),
     "vct_cone_trace_backward": (C.c_int, [P, P, P, C.c_int32, P, P, P, P, C.c_int64, P, P, P, P]),
     "vct_downsample_f32": (C.c_int, [P, P, C.c_int32, P]),
@@ -201,6 +207,7 @@ _SIGS: dict[str, tuple] = {
     "vct_downsample_rgba16f": (C.c_int, [P, P, C.c_int32, P, P]),
     "vct_cone_trace_fast_scratch_bytes": (C.c_int64, [C.c_int64]),
     "vct_cone_trace_fast": (C.c_int, [P, P, P, P, P, P, P, C.c_int64, P, P, P, P, C.c_size_t, P]),
+    "vct_cone_trace_fast_opt": (C.c_int, [P, P, P, P, P, P, P, C.c_int64, P, P, P, P, P, C.c_size_t, P]),
     "vct_gather_probe": (C.c_int, [P, P, C.c_int64, C.c_int32, P, P]),
     "vct_workspace_create": (C.c_int, [C.c_size_t, C.POINTER(C.c_void_p)]),
     "vct_workspace_destroy": (C.c_int, [P]),

@@ -106,8 +106,10 @@ def samples_to_device(samples: np.ndarray, device="cuda") -> torch.Tensor:
 def cone_trace(desc: capi.ConeTracingDesc, eye, radiance: torch.Tensor, R: int, samples: torch.Tensor,
                light: capi.DirectionalLightDesc | None = None, shadow: torch.Tensor | None = None,
                shadow_desc: capi.DirectionalLightShadowDesc | None = None, diffuse: torch.Tensor | None = None,
-               specular: torch.Tensor | None = None, steps: torch.Tensor | None = None):
-    """VoxelConeTracingPass over `samples` ((n, 20) float32 vct_surface_sample records)."""
+               specular: torch.Tensor | None = None, steps: torch.Tensor | None = None,
+               diffuse_aperture: float = 0.0):
+    """VoxelConeTracingPass over `samples` ((n, 20) float32 vct_surface_sample records); a non-zero
+    `diffuse_aperture` (radians) replaces the shader's diffuse cone aperture (vct_cone_trace_opt)."""
     n = samples.shape[0]
     if diffuse is None:
         diffuse = torch.zeros((n, 4), dtype=torch.float32, device=samples.device)
@@ -119,8 +121,9 @@ def cone_trace(desc: capi.ConeTracingDesc, eye, radiance: torch.Tensor, R: int, 
     if shadow is not None:
         sm = capi.ShadowMap(shadow.data_ptr(), shadow.shape[1], shadow.shape[0])
     sd = shadow_desc or capi.DirectionalLightShadowDesc()
-    capi.call("vct_cone_trace", capi.ref(desc), capi.ref(cam), _ptr(radiance), R, capi.ref(sm), capi.ref(light),
-              capi.ref(sd), _ptr(samples), n, _ptr(diffuse), _ptr(specular), _ptr(steps), _stream())
+    opt = capi.TraceOptions(diffuse_aperture)
+    capi.call("vct_cone_trace_opt", capi.ref(desc), capi.ref(cam), _ptr(radiance), R, capi.ref(sm), capi.ref(light),
+              capi.ref(sd), _ptr(samples), n, _ptr(diffuse), _ptr(specular), _ptr(steps), capi.ref(opt), _stream())
     return diffuse, specular
 
 
@@ -204,8 +207,10 @@ def cone_trace_fast(desc: capi.ConeTracingDesc, eye, tex: RadianceTexture, sampl
                     light: capi.DirectionalLightDesc | None = None, shadow: torch.Tensor | None = None,
                     shadow_desc: capi.DirectionalLightShadowDesc | None = None,
                     diffuse: torch.Tensor | None = None, specular: torch.Tensor | None = None,
-                    steps: torch.Tensor | None = None, scratch: torch.Tensor | None = None):
-    """GB300 form of VoxelConeTracingPass: same inputs/outputs as cone_trace, sampling `tex`."""
+                    steps: torch.Tensor | None = None, scratch: torch.Tensor | None = None,
+                    diffuse_aperture: float = 0.0):
+    """GB300 form of VoxelConeTracingPass: same inputs/outputs as cone_trace, sampling `tex`; a non-zero
+    `diffuse_aperture` (radians) replaces the shader's diffuse cone aperture (vct_cone_trace_fast_opt)."""
     n = samples.shape[0]
     if diffuse is None:
         diffuse = torch.zeros((n, 4), dtype=torch.float32, device=samples.device)
@@ -221,9 +226,10 @@ def cone_trace_fast(desc: capi.ConeTracingDesc, eye, tex: RadianceTexture, sampl
     if shadow is not None:
         sm = capi.ShadowMap(shadow.data_ptr(), shadow.shape[1], shadow.shape[0])
     sd = shadow_desc or capi.DirectionalLightShadowDesc()
-    capi.call("vct_cone_trace_fast", capi.ref(desc), capi.ref(cam), tex.handle, capi.ref(sm), capi.ref(light),
-              capi.ref(sd), _ptr(samples), n, _ptr(diffuse), _ptr(specular), _ptr(steps), C.c_void_p(base),
-              avail, _stream())
+    opt = capi.TraceOptions(diffuse_aperture)
+    capi.call("vct_cone_trace_fast_opt", capi.ref(desc), capi.ref(cam), tex.handle, capi.ref(sm), capi.ref(light),
+              capi.ref(sd), _ptr(samples), n, _ptr(diffuse), _ptr(specular), _ptr(steps), capi.ref(opt),
+              C.c_void_p(base), avail, _stream())
     return diffuse, specular
 
 

@@ -45,6 +45,7 @@ struct TraceParams {
     vct_directional_light_shadow_desc shadow_desc;
     const float* shadow;  // may be null: visibility 1
     int shadow_w, shadow_h;
+    float diffuse_aperture;  // the diffuse cones' aperture: the shader's constant unless an option sets it
 };
 
 __device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }

@@ -8,9 +8,9 @@
 // texture form's: samples in a coherent order (normal class, then Morton),
 // the diffuse cones of 32 samples dealt to the lanes of a warp
 // (trace_deal.cuh), each cone marched by trace_cone; the specular cones one
-// per warp with 64 consecutive steps per round (trace_cone_warp_exact).  The
-// specular cone is traced wherever the shader traces it (every rendering
-// mode), the diffuse cones likewise.
+// per lane over a list grouped by aperture (so a warp's cones march nearly
+// the same number of steps).  The specular cone is traced wherever the
+// shader traces it (every rendering mode), the diffuse cones likewise.
 #include <cstring>
 
 #include <cub/cub.cuh>
@@ -41,51 +41,60 @@ __global__ void __launch_bounds__(32 * kExactWarps) k_exact_diffuse(TraceParams 
                                                                     unsigned long long* __restrict__ step_counter) {
     const bool c32 = P.d.enable_32_cones != 0;
     DealArgs D{&P, samples, n, order, 0u, (uint32_t)n, dout, sout, c32 ? 32 : 16, true, true};
-    const ExactDiffuseMarch<Atlas> march{T, &P.d, c32 ? kAperture32 : kAperture16,
+    const ExactDiffuseMarch<Atlas> march{T, &P.d, P.diffuse_aperture,
                                          fmaxf(kMinTraceStepFactor, P.d.min_trace_step_factor)};
     unsigned long long steps = 0;
     deal_diffuse<kExactWarps>(D, march, steps);
     add_steps(step_counter, steps);
 }
 
-// One warp per specular cone of the list (kept in the coherent order).
+// One lane per specular cone of the list.  The list is grouped by aperture
+// (then kept in the coherent order), and a cone's step count depends only on
+// its aperture (and the occlusion stop), so a warp's cones march in step.
 template <class Atlas>
-__global__ void __launch_bounds__(256) k_exact_specular(TraceParams P, Atlas T,
+__global__ void __launch_bounds__(128) k_exact_specular(TraceParams P, Atlas T,
                                                         const vct_surface_sample* __restrict__ samples,
                                                         const uint32_t* __restrict__ list,
                                                         const unsigned int* __restrict__ spec_count,
                                                         float* __restrict__ sout,
                                                         unsigned long long* __restrict__ step_counter) {
     const vct_cone_tracing_desc& d = P.d;
-    const int lane = threadIdx.x & 31;
     const int64_t m = *spec_count;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     unsigned long long steps = 0;
-    for (int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < m; c += nwarps) {
+    for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < m; c += (int64_t)gridDim.x * blockDim.x) {
         const uint32_t idx = __ldg(list + c);
         const GSample g = load_sample(samples + idx, P.eye);
         const float min_level = calc_min_level(d, g.wp);
         const float vs = d.voxel_size * exp2f(min_level);
         const float3 start = g.wp + g.normal * (vs * d.trace_start_offset);
         const float3 sdir = reflect3(f3(-g.view.x, -g.view.y, -g.view.z), g.normal);
-        const ConeGeo K = make_cone(d, start, sdir, fmaxf(g.roughness, kMinSpecularAperture), min_level, d.voxel_size);
-        const float4 r = trace_cone_warp_exact(T, d, K, kMaxTraceDistance, steps);
-        if (lane == 0) {
-            const float isi = d.indirect_specular_intensity;
-            const uint32_t mode = d.rendering_mode;
-            float4 S = make_float4(0.f, 0.f, 0.f, 1.f);  // write_outputs' specular output
-            if (mode == 6 || mode >= 8)
-                S = make_float4(0.f + r.x * g.specular_color.x * isi, 0.f + r.y * g.specular_color.y * isi,
-                                0.f + r.z * g.specular_color.z * isi, 1.f);
-            reinterpret_cast<float4*>(sout)[idx] = S;
-        }
+        const float4 r = trace_cone(T, d, start, sdir, fmaxf(g.roughness, kMinSpecularAperture), kMaxTraceDistance,
+                                    min_level, d.voxel_size, steps);
+        const float isi = d.indirect_specular_intensity;
+        const uint32_t mode = d.rendering_mode;
+        float4 S = make_float4(0.f, 0.f, 0.f, 1.f);  // write_outputs' specular output
+        if (mode == 6 || mode >= 8)
+            S = make_float4(0.f + r.x * g.specular_color.x * isi, 0.f + r.y * g.specular_color.y * isi,
+                            0.f + r.z * g.specular_color.z * isi, 1.f);
+        reinterpret_cast<float4*>(sout)[idx] = S;
     }
     add_steps(step_counter, steps);
 }
 
+// The specular list's groups: kSpecApertureBuckets log-spaced buckets of the
+// aperture max(roughness, 0.05) over [0.05, 1] (a cone's step count is about
+// proportional to 1 / aperture, so a bucket's cones march within ~10 % of the
+// same number of steps).  Measured against 256 linear buckets, against 128
+// log buckets and against also splitting by the cone's direction: within a
+// few per cent, this one the fastest on random normals.
+constexpr int kSpecApertureBuckets = 32;
+constexpr int kSpecKeyBits = 6;  // keys < 32: specular; 32: not specular
+
 // Specular classification of the ordered samples (the shader traces a
 // specular cone where depth != 1 and the sample has a specular colour and
-// metalness): key 0 for specular samples, 256 otherwise, and their count.
+// metalness): specular samples get their aperture bucket as the key, the
+// others kSpecApertureBuckets; their count.  A stable radix sort of the keys
+// then lists the specular samples grouped, each group in the coherent order.
 __global__ void k_exact_spec_keys(const vct_surface_sample* __restrict__ samples, int64_t n,
                                   const uint32_t* __restrict__ order, uint32_t* __restrict__ spec_key,
                                   unsigned int* __restrict__ spec_count) {
@@ -96,10 +105,16 @@ __global__ void k_exact_spec_keys(const vct_surface_sample* __restrict__ samples
         bool spec = false;
         if (pos < n) {
             const float4* q = reinterpret_cast<const float4*>(samples + __ldg(order + pos));
-            const float4 a = __ldg(q + 0), d = __ldg(q + 3);
+            const float4 a = __ldg(q + 0), c = __ldg(q + 2), d = __ldg(q + 3);
             spec = a.w != 1.0f && (d.x > 1e-6f || d.y > 1e-6f || d.z > 1e-6f) && d.w > 1e-6f;
+            uint32_t key = (uint32_t)kSpecApertureBuckets;
+            if (spec) {
+                const float ap = fminf(fmaxf(c.w, kMinSpecularAperture), 1.0f);  // NaN -> the minimum
+                const float lb = __log2f(ap * (1.0f / kMinSpecularAperture)) * (1.0f / 4.321928f);  // log_20
+                key = (uint32_t)min(max((int)(lb * (float)kSpecApertureBuckets), 0), kSpecApertureBuckets - 1);
+            }
+            spec_key[pos] = key;
         }
-        if (pos < n) spec_key[pos] = spec ? 0u : 256u;
         const unsigned bal = __ballot_sync(0xffffffffu, spec);
         if (lane == 0 && bal) atomicAdd(spec_count, (unsigned)__popc(bal));
     }
@@ -187,6 +202,7 @@ int fill_trace_params(TraceParams& P, const vct_cone_tracing_desc* desc, const v
     VCT_CHECK_ARG(desc && cam && light, "cone trace: null descriptor");
     VCT_CHECK_ARG(desc->voxel_size > 0.0f && desc->volume_dimension >= 1.0f, "cone trace: bad voxel size / dimension");
     P.d = *desc;
+    P.diffuse_aperture = desc->enable_32_cones ? kAperture32 : kAperture16;
     for (int a = 0; a < 3; ++a) P.eye[a] = cam->eye_pos[a];
     P.light = *light;
     if (shadow && shadow->depth) {
@@ -205,10 +221,79 @@ int fill_trace_params(TraceParams& P, const vct_cone_tracing_desc* desc, const v
     return VCT_OK;
 }
 
-// The samples in the coherent order (normal class, then Morton), the
-// specular ones listed in that order, then the diffuse and specular kernels.
-// Scratch is stream-ordered (cudaMallocAsync, freed after the kernels).
-// Counts of 2^30 samples or more run in chunks (the orders are 32-bit).
+int exact_plan(const vct_surface_sample* samples, int64_t n, const vct_cone_tracing_desc& d, ExactPlan* plan,
+               cudaStream_t st) {
+    plan->order = nullptr;
+    plan->spec_list = nullptr;
+    plan->spec_count = nullptr;
+    plan->block = nullptr;
+    plan->order_block = nullptr;
+    SampleOrder so;
+    int rc = sample_coherent_order(samples, n, d, &so, st);
+    if (rc != VCT_OK) return rc;
+    size_t temp = 0;
+    cudaError_t e = cub::DeviceRadixSort::SortPairs(nullptr, temp, (uint32_t*)nullptr, (uint32_t*)nullptr,
+                                                    (uint32_t*)nullptr, (uint32_t*)nullptr, (int)n, 0, kSpecKeyBits,
+                                                    st);
+    const size_t arr4 = (4 * (size_t)n + 255) & ~(size_t)255;
+    char* b = nullptr;
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&b, 4 * arr4 + 256 + temp, st);
+    if (e != cudaSuccess) {
+        if (so.block) cudaFreeAsync(so.block, st);
+        return cuda_fail(e, "cone trace scratch");
+    }
+    uint32_t* identity = (uint32_t*)b;  // the order of a single sample (the coherent order needs n >= 2)
+    uint32_t* spec_key = (uint32_t*)(b + arr4);
+    uint32_t* spec_key_out = (uint32_t*)(b + 2 * arr4);
+    plan->spec_list = (uint32_t*)(b + 3 * arr4);
+    plan->spec_count = (unsigned int*)(b + 4 * arr4);
+    void* sort_temp = b + 4 * arr4 + 256;
+    plan->block = b;
+    plan->order_block = so.block;
+    plan->order = so.order;
+    if (!plan->order) {
+        const uint32_t zero = 0;
+        e = cudaMemcpyAsync(identity, &zero, sizeof(zero), cudaMemcpyHostToDevice, st);
+        plan->order = identity;
+    }
+    if (e == cudaSuccess) e = cudaMemsetAsync(plan->spec_count, 0, sizeof(unsigned int), st);
+    const int64_t gb = (n + 255) / 256;
+    if (e == cudaSuccess) {
+        k_exact_spec_keys<<<(int)(gb > 152 * 16 ? 152 * 16 : gb), 256, 0, st>>>(samples, n, plan->order, spec_key,
+                                                                               plan->spec_count);
+        e = cudaGetLastError();
+    }
+    // stable radix sort of the group keys: the specular samples first, by group, the order kept within
+    if (e == cudaSuccess)
+        e = cub::DeviceRadixSort::SortPairs(sort_temp, temp, spec_key, spec_key_out, plan->order, plan->spec_list,
+                                            (int)n, 0, kSpecKeyBits, st);
+    if (e != cudaSuccess) {
+        exact_plan_free(plan, st);
+        return cuda_fail(e, "exact trace plan");
+    }
+    return VCT_OK;
+}
+
+void exact_plan_free(ExactPlan* plan, cudaStream_t st) {
+    if (plan->block) cudaFreeAsync(plan->block, st);
+    if (plan->order_block) cudaFreeAsync(plan->order_block, st);
+    plan->block = plan->order_block = nullptr;
+}
+
+int apply_trace_options(TraceParams& P, const vct_trace_options* o) {
+    if (!o) return VCT_OK;
+    VCT_CHECK_ARG(o->reserved[0] == 0.0f && o->reserved[1] == 0.0f && o->reserved[2] == 0.0f,
+                  "cone trace options: reserved fields must be zero");
+    VCT_CHECK_ARG(o->diffuse_aperture == 0.0f || (o->diffuse_aperture > 0.0f && o->diffuse_aperture < 3.14159265f),
+                  "cone trace options: the diffuse aperture must be 0 or lie in (0, pi)");
+    if (o->diffuse_aperture != 0.0f) P.diffuse_aperture = o->diffuse_aperture;
+    return VCT_OK;
+}
+
+// The plan (coherent order, aperture-grouped specular list), then the
+// diffuse and specular kernels.  Scratch is stream-ordered (cudaMallocAsync,
+// freed after the kernels).  Counts of 2^30 samples or more run in chunks
+// (the orders are 32-bit).
 template <class Atlas>
 static int launch_exact(const TraceParams& P, const Atlas& T, const vct_surface_sample* samples, int64_t n,
                         float* dout, float* sout, unsigned long long* cone_steps, cudaStream_t st) {
@@ -216,57 +301,20 @@ static int launch_exact(const TraceParams& P, const Atlas& T, const vct_surface_
     for (int64_t off = 0; off < n; off += kChunk) {
         const int64_t m = n - off < kChunk ? n - off : kChunk;
         const vct_surface_sample* smp = samples + off;
-        SampleOrder so;
-        int rc = sample_coherent_order(smp, m, P.d, &so, st);
+        ExactPlan plan;
+        int rc = exact_plan(smp, m, P.d, &plan, st);
         if (rc != VCT_OK) return rc;
-        size_t temp = 0;
-        cudaError_t e = cub::DeviceRadixSort::SortPairs(nullptr, temp, (uint32_t*)nullptr, (uint32_t*)nullptr,
-                                                        (uint32_t*)nullptr, (uint32_t*)nullptr, (int)m, 8, 9, st);
-        const size_t arr4 = (4 * (size_t)m + 255) & ~(size_t)255;
-        char* b = nullptr;
-        if (e == cudaSuccess) e = cudaMallocAsync((void**)&b, 4 * arr4 + 256 + temp, st);
-        if (e != cudaSuccess) {
-            if (so.block) cudaFreeAsync(so.block, st);
-            return cuda_fail(e, "cone trace scratch");
-        }
-        uint32_t* identity = (uint32_t*)b;  // used when the coherent order is the identity (one sample)
-        uint32_t* spec_key = (uint32_t*)(b + arr4);
-        uint32_t* spec_key_out = (uint32_t*)(b + 2 * arr4);
-        uint32_t* spec_list = (uint32_t*)(b + 3 * arr4);
-        unsigned int* spec_count = (unsigned int*)(b + 4 * arr4);
-        void* sort_temp = b + 4 * arr4 + 256;
-        const uint32_t* order = so.order;
-        if (!order) {
-            // n == 1 (the coherent order is only built for n >= 2)
-            const uint32_t zero = 0;
-            e = cudaMemcpyAsync(identity, &zero, sizeof(zero), cudaMemcpyHostToDevice, st);
-            order = identity;
-        }
-        if (e == cudaSuccess) e = cudaMemsetAsync(spec_count, 0, sizeof(unsigned int), st);
-        const int64_t gb = (m + 255) / 256;
-        if (e == cudaSuccess) {
-            k_exact_spec_keys<<<(int)(gb > 152 * 16 ? 152 * 16 : gb), 256, 0, st>>>(smp, m, order, spec_key,
-                                                                                   spec_count);
-            e = cudaGetLastError();
-        }
-        // stable partition (one radix pass on bit 8): specular samples first, the order kept
-        if (e == cudaSuccess)
-            e = cub::DeviceRadixSort::SortPairs(sort_temp, temp, spec_key, spec_key_out, order, spec_list, (int)m, 8, 9,
-                                                st);
         const int64_t gdw = (m + 32 * kExactWarps - 1) / (32 * kExactWarps);
+        k_exact_diffuse<<<(int)(gdw > 152 * 16 ? 152 * 16 : gdw), 32 * kExactWarps, 0, st>>>(
+            P, T, smp, m, plan.order, dout + 4 * off, sout + 4 * off, cone_steps);
+        cudaError_t e = cudaGetLastError();
         if (e == cudaSuccess) {
-            k_exact_diffuse<<<(int)(gdw > 152 * 16 ? 152 * 16 : gdw), 32 * kExactWarps, 0, st>>>(
-                P, T, smp, m, order, dout + 4 * off, sout + 4 * off, cone_steps);
+            const int64_t gl = (m + 127) / 128;
+            k_exact_specular<<<(int)(gl > 152 * 16 ? 152 * 16 : gl), 128, 0, st>>>(
+                P, T, smp, plan.spec_list, plan.spec_count, sout + 4 * off, cone_steps);
             e = cudaGetLastError();
         }
-        const int64_t gw = (m * 32 + 255) / 256;
-        if (e == cudaSuccess) {
-            k_exact_specular<<<(int)(gw > 152 * 32 ? 152 * 32 : gw), 256, 0, st>>>(P, T, smp, spec_list, spec_count,
-                                                                                  sout + 4 * off, cone_steps);
-            e = cudaGetLastError();
-        }
-        cudaFreeAsync(b, st);
-        if (so.block) cudaFreeAsync(so.block, st);
+        exact_plan_free(&plan, st);
         if (e != cudaSuccess) return cuda_fail(e, "exact cone trace");
     }
     return VCT_OK;
@@ -279,6 +327,16 @@ extern "C" int vct_cone_trace(const vct_cone_tracing_desc* desc, const vct_cam_m
                               const vct_directional_light_shadow_desc* light_shadow,
                               const vct_surface_sample* samples, int64_t n, float* dout, float* sout,
                               unsigned long long* cone_steps, void* stream) {
+    return vct_cone_trace_opt(desc, cam, radiance_atlas, R, shadow, light, light_shadow, samples, n, dout, sout,
+                              cone_steps, nullptr, stream);
+}
+
+extern "C" int vct_cone_trace_opt(const vct_cone_tracing_desc* desc, const vct_cam_matrix* cam,
+                                  const uint32_t* radiance_atlas, int32_t R, const vct_shadow_map* shadow,
+                                  const vct_directional_light_desc* light,
+                                  const vct_directional_light_shadow_desc* light_shadow,
+                                  const vct_surface_sample* samples, int64_t n, float* dout, float* sout,
+                                  unsigned long long* cone_steps, const vct_trace_options* options, void* stream) {
     VCT_CHECK_ARG(radiance_atlas && valid_resolution(R), "vct_cone_trace: bad radiance atlas / resolution");
     VCT_CHECK_ARG(n >= 0, "vct_cone_trace: negative sample count");
     if (n == 0) return VCT_OK;
@@ -288,6 +346,7 @@ extern "C" int vct_cone_trace(const vct_cone_tracing_desc* desc, const vct_cam_m
     TraceParams P;
     int rc = fill_trace_params(P, desc, cam, shadow, light, light_shadow);
     if (rc != VCT_OK) return rc;
+    if ((rc = apply_trace_options(P, options)) != VCT_OK) return rc;
     ExactAtlas T{radiance_atlas, AtlasDims(R)};
     return launch_exact(P, T, samples, n, dout, sout, cone_steps, as_stream(stream));
 }

@@ -28,6 +28,14 @@ __device__ __forceinline__ int wrap_rep(int i, int n) {
     return m < 0 ? m + n : m;
 }
 
+// REPEAT of a texel index that a sampler coordinate in [0, 1) produces
+// (i in [-1, n]): one compare and select on that range; the general
+// modulo for anything else, so no index leaves [0, n).
+__device__ __forceinline__ int wrap_tap(int i, int n) {
+    const int m = i < 0 ? i + n : (i >= n ? i - n : i);
+    return (unsigned)m < (unsigned)n ? m : wrap_rep(i, n);
+}
+
 __device__ __forceinline__ float4 lerp4(float4 p, float4 q, float t) {
     return make_float4(p.x + (q.x - p.x) * t, p.y + (q.y - p.y) * t, p.z + (q.z - p.z) * t, p.w + (q.w - p.w) * t);
 }
@@ -39,9 +47,9 @@ __device__ __forceinline__ float4 texture3d(const Atlas& T, float ux, float uy, 
     float u = ux * (float)A.W - 0.5f, v = uy * (float)A.H - 0.5f, w = uz * (float)A.D - 0.5f;
     float fu = floorf(u), fv = floorf(v), fw = floorf(w);
     float a = u - fu, b = v - fv, c = w - fw;
-    int i0 = wrap_rep((int)fu, A.W), i1 = wrap_rep((int)fu + 1, A.W);
-    int j0 = wrap_rep((int)fv, A.H), j1 = wrap_rep((int)fv + 1, A.H);
-    int k0 = wrap_rep((int)fw, A.D), k1 = wrap_rep((int)fw + 1, A.D);
+    int i0 = wrap_tap((int)fu, A.W), i1 = wrap_tap((int)fu + 1, A.W);
+    int j0 = wrap_tap((int)fv, A.H), j1 = wrap_tap((int)fv + 1, A.H);
+    int k0 = wrap_tap((int)fw, A.D), k1 = wrap_tap((int)fw + 1, A.D);
     float4 x00 = lerp4(T.fetch(i0, j0, k0), T.fetch(i1, j0, k0), a);
     float4 x10 = lerp4(T.fetch(i0, j1, k0), T.fetch(i1, j1, k0), a);
     float4 x01 = lerp4(T.fetch(i0, j0, k1), T.fetch(i1, j0, k1), a);
@@ -106,7 +114,10 @@ __device__ float4 trace_cone(const Atlas& T, const vct_cone_tracing_desc& d, flo
         vs = uvs * exp2f(cur_level);
         float correction = seg / vs;
         float rx = s.x * correction, ry = s.y * correction, rz = s.z * correction;
-        float opacity = clampf(1.0f - powf(1.0f - s.w, correction), 0.0f, 1.0f);
+        // a filtered alpha rounded above 1 (the face weights sum to 1 + ulp) would make the base of pow
+        // negative, which GLSL leaves undefined (NaN, then clamped to a transparent 0 on hardware); the
+        // base is taken as 0 there: the sample is opaque
+        float opacity = clampf(1.0f - powf(fmaxf(1.0f - s.w, 0.0f), correction), 0.0f, 1.0f);
         float k = clampf(1.0f - result.w, 0.0f, 1.0f);
         result = make_float4(result.x + k * rx, result.y + k * ry, result.z + k * rz, result.w + k * opacity);
         occlusion = occlusion + (1.0f - occlusion) * opacity / (1.0f + (step + vs) * d.occlusion_decay);
@@ -118,9 +129,27 @@ __device__ float4 trace_cone(const Atlas& T, const vct_cone_tracing_desc& d, flo
     return make_float4(result.x, result.y, result.z, 1.0f - occlusion);
 }
 
+// The visiting plan of the exact forms and their adjoint: the samples in the
+// coherent order (normal class, then Morton) and the specular samples listed
+// grouped by aperture (log-spaced buckets of max(roughness, 0.05)), each group
+// in the coherent order, with their count (device).  A cone's step count is
+// about proportional to 1 / aperture, so the 32 cones of a warp taken from
+// one group march nearly the same number of steps.  Stream-ordered scratch:
+// release it with exact_plan_free after the last kernel that reads it.
+struct ExactPlan {
+    const uint32_t* order;
+    uint32_t* spec_list;
+    unsigned int* spec_count;
+    void* block;
+    void* order_block;
+};
+int exact_plan(const vct_surface_sample* samples, int64_t n, const vct_cone_tracing_desc& d, ExactPlan* plan,
+               cudaStream_t st);
+void exact_plan_free(ExactPlan* plan, cudaStream_t st);
+
 // ---------------------------------------------------------------------------
 // traceCone split into its volume-independent geometry, its step schedule
-// and one step, for kernels that march a cone's steps on several lanes.
+// and one step, for the adjoint's recomputation of a march.
 
 // The cone as trace_cone sets it up (start already offset by half a step).
 struct ConeGeo {
@@ -163,13 +192,6 @@ __device__ __forceinline__ void sched_advance(Sched& s, const ConeGeo& K) {
     s.diameter = s.step * K.coef;
 }
 
-// One step of the loop at schedule s: the filtered sample scaled by the
-// opacity correction (rgb), the corrected opacity and the occlusion divisor
-// q = 1 + (step + vs) * decay.
-struct ExactStep {
-    float r, g, b, op, q;
-};
-
 // Everything one step computes: its tap geometry (position, the two levels
 // and the mix fraction), the filtered sample, the opacity correction, the raw
 // and clamped opacity and the occlusion divisor.
@@ -199,119 +221,10 @@ __device__ __forceinline__ StepDetail exact_step_detail(const Atlas& T, const vc
                         lo.z * (1.0f - fr) + hi.z * fr, lo.w * (1.0f - fr) + hi.w * fr);
     const float vs = K.uvs * exp2f(cur_level);
     e.correction = s.seg / vs;
-    e.op_raw = 1.0f - powf(1.0f - e.smp.w, e.correction);
+    e.op_raw = 1.0f - powf(fmaxf(1.0f - e.smp.w, 0.0f), e.correction);  // base >= 0 as in trace_cone
     e.op = clampf(e.op_raw, 0.0f, 1.0f);
     e.q = 1.0f + (s.step + vs) * d.occlusion_decay;
     return e;
-}
-
-template <class Atlas>
-__device__ __forceinline__ ExactStep exact_step(const Atlas& T, const vct_cone_tracing_desc& d, const ConeGeo& K,
-                                                const Sched& s) {
-    const StepDetail e = exact_step_detail(T, d, K, s);
-    return ExactStep{e.smp.x * e.correction, e.smp.y * e.correction, e.smp.z * e.correction, e.op, e.q};
-}
-
-// A run of steps composited front to back: rgb and alpha by the "over"
-// operator, t = the product of (1 - op / q) (1 - occlusion).
-struct Composite {
-    float r, g, b, a, t;
-};
-
-__device__ __forceinline__ Composite over(const Composite& p, const Composite& q) {
-    const float k = clampf(1.0f - p.a, 0.0f, 1.0f);
-    return Composite{p.r + k * q.r, p.g + k * q.g, p.b + k * q.b, p.a + k * q.a, p.t * q.t};
-}
-
-__device__ __forceinline__ Composite as_composite(const ExactStep& e) {
-    return Composite{e.r, e.g, e.b, e.op, 1.0f - e.op / e.q};
-}
-
-__device__ __forceinline__ Composite shfl_composite(const Composite& c, int src) {
-    return Composite{__shfl_sync(0xffffffffu, c.r, src), __shfl_sync(0xffffffffu, c.g, src),
-                     __shfl_sync(0xffffffffu, c.b, src), __shfl_sync(0xffffffffu, c.a, src),
-                     __shfl_sync(0xffffffffu, c.t, src)};
-}
-
-// Consecutive steps of one cone per lane in the warp-cooperative march.
-constexpr int kExactStepsPerLane = 2;
-
-// traceCone marched by a whole warp, 64 steps per round: lane j takes steps
-// 2j, 2j + 1 of the round.  The schedule is a serial FP32 recurrence, so each
-// lane advances it from the round's first step to its own (the positions are
-// the loop's, bit for bit); the composite is the associative "over" operator
-// and 1 - occlusion a product, so a warp scan composes the lanes.  The first
-// lane whose composite reaches occlusion 1 marches its steps again with the
-// loop's own update from the state before them and stops where the loop
-// does.  Returns (rgb, 1 - occlusion) to every lane.
-template <class Atlas>
-__device__ float4 trace_cone_warp_exact(const Atlas& T, const vct_cone_tracing_desc& d, const ConeGeo& K,
-                                        float max_dist, unsigned long long& steps) {
-    constexpr int S = kExactStepsPerLane;
-    const int lane = threadIdx.x & 31;
-    const Composite id{0.0f, 0.0f, 0.0f, 0.0f, 1.0f};
-    Composite carried = id;
-    Sched round0 = first_sched(K);
-    unsigned long long it = 0;
-    for (;;) {
-        Sched s = round0;
-        for (int k = 0; k < S * lane; ++k) sched_advance(s, K);
-        const Sched mine = s;
-        Composite x = id;
-        int nvalid = 0;
-#pragma unroll
-        for (int k = 0; k < S; ++k) {
-            if (s.step < max_dist) {
-                x = over(x, as_composite(exact_step(T, d, K, s)));
-                ++nvalid;
-            }
-            sched_advance(s, K);
-        }
-        // inclusive scan of the lanes' composites
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const Composite p = shfl_composite(x, (lane - o) & 31);
-            if (lane >= o) x = over(p, x);
-        }
-        const Composite after = over(carried, x);
-        const unsigned tmask = __ballot_sync(0xffffffffu, nvalid > 0 && (1.0f - after.t) >= 1.0f);
-        if (tmask) {  // occlusion reaches 1 within lane L's steps: the loop stops after that step
-            const int L = __ffs(tmask) - 1;
-            const Composite prior = shfl_composite(x, (lane - 1) & 31);
-            Composite y = carried;
-            int done = 0;
-            if (lane == L) {
-                const Composite before = lane == 0 ? carried : over(carried, prior);
-                float4 result = make_float4(before.r, before.g, before.b, before.a);
-                float occ = 1.0f - before.t;
-                Sched q = mine;
-                for (int k = 0; k < S && q.step < max_dist && occ < 1.0f; ++k) {
-                    const ExactStep e = exact_step(T, d, K, q);
-                    const float kk = clampf(1.0f - result.w, 0.0f, 1.0f);
-                    result = make_float4(result.x + kk * e.r, result.y + kk * e.g, result.z + kk * e.b,
-                                         result.w + kk * e.op);
-                    occ = occ + (1.0f - occ) * e.op / e.q;
-                    ++done;
-                    sched_advance(q, K);
-                }
-                y = Composite{result.x, result.y, result.z, result.w, 1.0f - occ};
-            }
-            carried = shfl_composite(y, L);
-            it += (unsigned long long)(S * L + __shfl_sync(0xffffffffu, done, L));
-            break;
-        }
-        carried = shfl_composite(after, 31);
-        int nv = nvalid;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) nv += __shfl_xor_sync(0xffffffffu, nv, o);
-        it += (unsigned long long)nv;
-        if (nv < 32 * S) break;  // maxDistance reached within the round
-        round0 = Sched{__shfl_sync(0xffffffffu, s.step, 31), __shfl_sync(0xffffffffu, s.seg, 31),
-                       __shfl_sync(0xffffffffu, s.diameter, 31)};
-    }
-    if (lane == 0) steps += it;
-    const float occlusion = 1.0f - carried.t;
-    return make_float4(carried.r, carried.g, carried.b, 1.0f - occlusion);
 }
 
 }  // namespace vct

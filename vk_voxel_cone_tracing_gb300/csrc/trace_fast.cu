@@ -32,6 +32,7 @@ int texture_format(const vct_texture_s* t);
 int fill_trace_params(TraceParams& P, const vct_cone_tracing_desc* desc, const vct_cam_matrix* cam,
                       const vct_shadow_map* shadow, const vct_directional_light_desc* light,
                       const vct_directional_light_shadow_desc* light_shadow);
+int apply_trace_options(TraceParams& P, const vct_trace_options* o);
 
 struct FastConsts {
     float uvs, inv_uvs, min_radius, inv_min_radius, inv_min_radius2, decay, start_off;
@@ -120,7 +121,8 @@ __device__ __forceinline__ float4 trace_cone_fast(cudaTextureObject_t tex, const
         }
         vs = uvs * ex2_approx(cl);
         const float corr = __fdividef(seg, vs);
-        const float opacity = __saturatef(1.0f - ex2_approx(corr * __log2f(1.0f - s.w)));
+        // base clamped at 0 like the exact form: alpha rounded above 1 is opaque, not NaN -> 0
+        const float opacity = __saturatef(1.0f - ex2_approx(corr * __log2f(fmaxf(1.0f - s.w, 0.0f))));
         const float k = __saturatef(1.0f - result.w);
         result = make_float4(fmaf(k * s.x, corr, result.x), fmaf(k * s.y, corr, result.y),
                              fmaf(k * s.z, corr, result.z), fmaf(k, opacity, result.w));
@@ -228,7 +230,7 @@ __device__ __forceinline__ ConeStep cone_step(cudaTextureObject_t tex, const Fas
     }
     const float vs = C.uvs * ex2_approx(cl);
     const float corr = __fdividef(sg, vs);
-    const float opacity = __saturatef(1.0f - ex2_approx(corr * __log2f(1.0f - smp.w)));
+    const float opacity = __saturatef(1.0f - ex2_approx(corr * __log2f(fmaxf(1.0f - smp.w, 0.0f))));
     return ConeStep{smp.x * corr, smp.y * corr, smp.z * corr, opacity,
                     1.0f - __fdividef(opacity, fmaf(st + vs, C.decay, 1.0f))};
 }
@@ -487,7 +489,7 @@ static int plan_scratch(int64_t n, void* base, FastScratch& s) {
     return VCT_OK;
 }
 
-static void fill_fast_consts(FastConsts& C, const vct_cone_tracing_desc& d) {
+static void fill_fast_consts(FastConsts& C, const vct_cone_tracing_desc& d, float diffuse_aperture) {
     C.uvs = d.voxel_size;
     C.inv_uvs = 1.0f / d.voxel_size;
     C.min_radius = d.voxel_size * d.volume_dimension * 0.5f;
@@ -497,7 +499,7 @@ static void fill_fast_consts(FastConsts& C, const vct_cone_tracing_desc& d) {
     C.start_off = d.trace_start_offset;
     const bool c32 = d.enable_32_cones != 0;
     C.ncones = c32 ? 32 : 16;
-    C.aperture_diffuse = c32 ? kAperture32 : kAperture16;
+    C.aperture_diffuse = diffuse_aperture;
     C.coef_diffuse = 2.0f * tanf(C.aperture_diffuse * 0.5f);
     C.sf_diffuse = d.min_trace_step_factor > kMinTraceStepFactor ? d.min_trace_step_factor : kMinTraceStepFactor;
     C.cx = d.volume_center[0];
@@ -535,6 +537,17 @@ extern "C" int vct_cone_trace_fast(const vct_cone_tracing_desc* desc, const vct_
                                    const vct_surface_sample* samples, int64_t n, float* dout, float* sout,
                                    unsigned long long* cone_steps, void* scratch, size_t scratch_bytes,
                                    void* stream) {
+    return vct_cone_trace_fast_opt(desc, cam, radiance, shadow, light, light_shadow, samples, n, dout, sout,
+                                   cone_steps, nullptr, scratch, scratch_bytes, stream);
+}
+
+extern "C" int vct_cone_trace_fast_opt(const vct_cone_tracing_desc* desc, const vct_cam_matrix* cam,
+                                       vct_texture_s* radiance, const vct_shadow_map* shadow,
+                                       const vct_directional_light_desc* light,
+                                       const vct_directional_light_shadow_desc* light_shadow,
+                                       const vct_surface_sample* samples, int64_t n, float* dout, float* sout,
+                                       unsigned long long* cone_steps, const vct_trace_options* options,
+                                       void* scratch, size_t scratch_bytes, void* stream) {
     vct::NvtxRange nvtx_range("vct_cone_trace_fast");
     VCT_CHECK_ARG(radiance, "vct_cone_trace_fast: null radiance texture");
     VCT_CHECK_ARG(n >= 0 && n <= 0x7fffffffLL, "vct_cone_trace_fast: sample count out of range");
@@ -546,13 +559,14 @@ extern "C" int vct_cone_trace_fast(const vct_cone_tracing_desc* desc, const vct_
     FastArgs A;
     int rc = fill_trace_params(A.P, desc, cam, shadow, light, light_shadow);
     if (rc != VCT_OK) return rc;
+    if ((rc = apply_trace_options(A.P, options)) != VCT_OK) return rc;
     VCT_CHECK_ARG((float)texture_resolution(radiance) == desc->volume_dimension,
                   "vct_cone_trace_fast: volume dimension differs from the texture's clipmap resolution");
     FastScratch S;
     rc = plan_scratch(n, scratch, S);
     if (rc != VCT_OK) return rc;
     VCT_CHECK_ARG(scratch_bytes >= S.total, "vct_cone_trace_fast: scratch buffer too small");
-    fill_fast_consts(A.C, *desc);
+    fill_fast_consts(A.C, *desc, A.P.diffuse_aperture);
     A.tex = texture_object(radiance);
     A.samples = samples;
     A.n = n;
@@ -600,7 +614,7 @@ extern "C" int vct_gather_probe(const vct_cone_tracing_desc* desc, vct_texture_s
                   "vct_gather_probe: volume dimension differs from the texture's clipmap resolution");
     FastArgs A;
     memset(&A, 0, sizeof(A));
-    fill_fast_consts(A.C, *desc);
+    fill_fast_consts(A.C, *desc, desc->enable_32_cones ? kAperture32 : kAperture16);
     A.tex = texture_object(radiance);
     cudaStream_t st = as_stream(stream);
     const int block = 256, grid = 152 * 8;

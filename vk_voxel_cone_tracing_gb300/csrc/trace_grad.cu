@@ -25,16 +25,12 @@
 // Same FP32 expressions as the forward kernels (this unit is built with
 // -fmad=false like them), so the recomputed steps are the forward's.
 //
-// Diffuse cones: one lane per (cone, sample), cone-major, the warp's lanes in
-// lock step (all diffuse cones share one step schedule); a checkpoint of the
-// march state every 32 steps, each segment recomputed from its checkpoint and
-// walked backward with the recurrences above in sequential form.
-// Specular cones (57 to thousands of steps): one warp per cone, 64 steps per
-// round as in the forward kernel; a forward pass keeps the schedule and the
-// composite at each round's start in shared memory, and a reverse pass over
-// the rounds recomputes each round's steps, forms T_i, U_i by a warp scan
-// from the round's start and R_i, V_i by a reverse warp scan from the rounds
-// after it, and scatters.
+// Each cone is walked by one lane, the warp's lanes in lock step: a
+// checkpoint of the march state every 32 steps, each segment recomputed from
+// its checkpoint and walked backward with the recurrences above in
+// sequential form.  Diffuse cones all share one step schedule; specular
+// cones are taken from the exact forward's aperture-grouped list, so a
+// warp's cones also march nearly the same number of steps.
 #include "trace_exact.cuh"
 
 namespace vct {
@@ -47,8 +43,6 @@ namespace {
 
 constexpr int kSegSteps = 32;
 constexpr int kMaxSegments = 256;  // 8192 steps per cone: the specular cone at R = 1024 takes ~7.1k
-constexpr int kMaxRounds = kMaxSegments * kSegSteps / (32 * kExactStepsPerLane);
-constexpr int kSpecWarps = 4;      // warps per block of the specular adjoint
 
 struct MarchState {
     float step, seg, diameter, alpha, occ;
@@ -64,9 +58,9 @@ __device__ __forceinline__ void texture3d_grad(float4* __restrict__ G, const Atl
     float u = ux * (float)A.W - 0.5f, v = uy * (float)A.H - 0.5f, w = uz * (float)A.D - 0.5f;
     float fu = floorf(u), fv = floorf(v), fw = floorf(w);
     float a = u - fu, b = v - fv, c = w - fw;
-    int i0 = wrap_rep((int)fu, A.W), i1 = wrap_rep((int)fu + 1, A.W);
-    int j0 = wrap_rep((int)fv, A.H), j1 = wrap_rep((int)fv + 1, A.H);
-    int k0 = wrap_rep((int)fw, A.D), k1 = wrap_rep((int)fw + 1, A.D);
+    int i0 = wrap_tap((int)fu, A.W), i1 = wrap_tap((int)fu + 1, A.W);
+    int j0 = wrap_tap((int)fv, A.H), j1 = wrap_tap((int)fv + 1, A.H);
+    int k0 = wrap_tap((int)fw, A.D), k1 = wrap_tap((int)fw + 1, A.D);
     const float wi[2] = {1.0f - a, a}, wj[2] = {1.0f - b, b}, wk[2] = {1.0f - c, c};
     const int ii[2] = {i0, i1}, jj[2] = {j0, j1}, kk[2] = {k0, k1};
 #pragma unroll
@@ -140,7 +134,7 @@ __device__ __forceinline__ StepDetail march_step(const F4Atlas& T, const vct_con
     return e;
 }
 
-// The adjoint of one diffuse cone per lane: gC (rgb) and gO (d/d occlusion)
+// The adjoint of one cone per lane: gC (rgb) and gO (d/d occlusion)
 // at the end of the march.  The warp's lanes run in lock step: every loop
 // runs to the warp's longest march and a lane sits out the steps its cone
 // does not have (or all of them when `active` is false).  The forward
@@ -202,161 +196,6 @@ __device__ void cone_backward_lane(const F4Atlas& T, float4* __restrict__ G, con
     }
 }
 
-// The suffix of a march from some step to its end: P = prod (1 - op),
-// R = sum_j prod_{m<j} (1 - op_m) c_j gC . s_j.rgb, V = prod (1 - op / q).
-struct Suffix {
-    float P, R, V;
-};
-
-// `a` followed by `b`.
-__device__ __forceinline__ Suffix then(const Suffix& a, const Suffix& b) {
-    return Suffix{a.P * b.P, a.R + a.P * b.R, a.V * b.V};
-}
-
-__device__ __forceinline__ Suffix step_suffix(const StepDetail& e, float3 gC) {
-    const float w = (gC.x * e.smp.x + gC.y * e.smp.y + gC.z * e.smp.z) * e.correction;
-    return Suffix{1.0f - e.op, w, 1.0f - e.op / e.q};
-}
-
-__device__ __forceinline__ Suffix shfl_suffix(const Suffix& s, int src) {
-    return Suffix{__shfl_sync(0xffffffffu, s.P, src), __shfl_sync(0xffffffffu, s.R, src),
-                  __shfl_sync(0xffffffffu, s.V, src)};
-}
-
-// The state at the first step of a round: the schedule and the composite of
-// the steps before it (its alpha a = 1 - T and its t = U).
-struct RoundStart {
-    float step, seg, diameter, a, t;
-};
-
-// The adjoint of one cone marched by the whole warp (steps over the lanes).
-// `rounds` is this warp's shared-memory array of kMaxRounds round starts.
-__device__ void cone_backward_warp(const F4Atlas& T, float4* __restrict__ G, const vct_cone_tracing_desc& d,
-                                   const ConeGeo& K, float3 gC, float gO, float max_dist,
-                                   RoundStart* __restrict__ rounds, int* __restrict__ err) {
-    constexpr int S = kExactStepsPerLane;
-    const int lane = threadIdx.x & 31;
-    const Composite id{0.0f, 0.0f, 0.0f, 0.0f, 1.0f};
-    // forward: the rounds' starts and the number of steps the loop takes
-    Composite carried = id;
-    Sched round0 = first_sched(K);
-    int nsteps = 0, nrounds = 0;
-    for (;;) {
-        if (nrounds == kMaxRounds) {
-            if (lane == 0) atomicOr(err, 1);
-            return;
-        }
-        if (lane == 0) rounds[nrounds] = RoundStart{round0.step, round0.seg, round0.diameter, carried.a, carried.t};
-        Sched s = round0;
-        for (int k = 0; k < S * lane; ++k) sched_advance(s, K);
-        const Sched mine = s;
-        Composite x = id;
-        int nvalid = 0;
-#pragma unroll
-        for (int k = 0; k < S; ++k) {
-            if (s.step < max_dist) {
-                x = over(x, as_composite(exact_step(T, d, K, s)));
-                ++nvalid;
-            }
-            sched_advance(s, K);
-        }
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const Composite p = shfl_composite(x, (lane - o) & 31);
-            if (lane >= o) x = over(p, x);
-        }
-        const Composite after = over(carried, x);
-        ++nrounds;
-        const unsigned tmask = __ballot_sync(0xffffffffu, nvalid > 0 && (1.0f - after.t) >= 1.0f);
-        if (tmask) {  // the loop stops within lane L's steps (the forward kernel's rule)
-            const int L = __ffs(tmask) - 1;
-            const Composite prior = shfl_composite(x, (lane - 1) & 31);
-            int done = 0;
-            if (lane == L) {
-                const Composite before = lane == 0 ? carried : over(carried, prior);
-                float occ = 1.0f - before.t;
-                Sched q = mine;
-                for (int k = 0; k < S && q.step < max_dist && occ < 1.0f; ++k) {
-                    const ExactStep e = exact_step(T, d, K, q);
-                    occ = occ + (1.0f - occ) * e.op / e.q;
-                    ++done;
-                    sched_advance(q, K);
-                }
-            }
-            nsteps += S * L + __shfl_sync(0xffffffffu, done, L);
-            break;
-        }
-        carried = shfl_composite(after, 31);
-        int nv = nvalid;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) nv += __shfl_xor_sync(0xffffffffu, nv, o);
-        nsteps += nv;
-        if (nv < 32 * S) break;
-        round0 = Sched{__shfl_sync(0xffffffffu, s.step, 31), __shfl_sync(0xffffffffu, s.seg, 31),
-                       __shfl_sync(0xffffffffu, s.diameter, 31)};
-    }
-    __syncwarp();
-    // reverse: rounds last to first, carrying the suffix of the rounds after
-    Suffix tail{1.0f, 0.0f, 1.0f};
-    for (int r = nrounds - 1; r >= 0; --r) {
-        const RoundStart rs = rounds[r];
-        Sched s{rs.step, rs.seg, rs.diameter};
-        for (int k = 0; k < S * lane; ++k) sched_advance(s, K);
-        const int first = r * 32 * S + S * lane;  // this lane's first step index
-        StepDetail e[S];
-        bool valid[S];
-        Composite x = id;
-        Suffix own{1.0f, 0.0f, 1.0f};
-#pragma unroll
-        for (int k = 0; k < S; ++k) {
-            valid[k] = first + k < nsteps;
-            if (valid[k]) {
-                e[k] = exact_step_detail(T, d, K, s);
-                x = over(x, Composite{e[k].smp.x * e[k].correction, e[k].smp.y * e[k].correction,
-                                      e[k].smp.z * e[k].correction, e[k].op, 1.0f - e[k].op / e[k].q});
-                own = then(own, step_suffix(e[k], gC));
-            }
-            sched_advance(s, K);
-        }
-        // exclusive prefix composite of the lanes before this one, from the round's start
-        Composite pre = x;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const Composite p = shfl_composite(pre, (lane - o) & 31);
-            if (lane >= o) pre = over(p, pre);
-        }
-        Composite before = shfl_composite(pre, (lane - 1) & 31);
-        const Composite start{0.0f, 0.0f, 0.0f, rs.a, rs.t};
-        before = lane == 0 ? start : over(start, before);
-        // inclusive suffix of the lanes from this one to the round's end, then the rounds after
-        Suffix suf = own;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const Suffix q = shfl_suffix(suf, (lane + o) & 31);
-            if (lane + o < 32) suf = then(suf, q);
-        }
-        Suffix after = shfl_suffix(suf, (lane + 1) & 31);
-        after = lane == 31 ? tail : then(after, tail);
-        const Suffix round_total = then(shfl_suffix(suf, 0), tail);
-        // this lane's steps, last first: the suffix after step k, the prefix before it
-        Suffix rest = after;
-#pragma unroll
-        for (int k = S - 1; k >= 0; --k) {
-            if (!valid[k]) continue;
-            Composite pk = before;
-            for (int j = 0; j < k; ++j)
-                if (valid[j]) pk = over(pk, Composite{0.0f, 0.0f, 0.0f, e[j].op, 1.0f - e[j].op / e[j].q});
-            const float Tk = clampf(1.0f - pk.a, 0.0f, 1.0f), Uk = pk.t;
-            const float c = e[k].correction;
-            const float gop = -Tk * rest.R + gO * Uk * rest.V / e[k].q;
-            const float4 gs = make_float4(gC.x * Tk * c, gC.y * Tk * c, gC.z * Tk * c, gop * opacity_slope(e[k]));
-            scatter_step(G, T.A, d, K, e[k].pos, e[k].lower, e[k].upper, e[k].fr, gs);
-            rest = then(step_suffix(e[k], gC), rest);
-        }
-        tail = round_total;
-    }
-}
-
 // dL/d(indirect) -> the diffuse cones' gC and gO; false when the mode does
 // not read the volume through the diffuse cones.
 __device__ __forceinline__ bool diffuse_seeds(const TraceParams& P, const GSample& g, float4 GD, float cos_t, int nc,
@@ -414,39 +253,152 @@ __global__ void __launch_bounds__(128) k_cone_backward_diffuse(TraceParams P, F4
         float3 gC = f3(0.f, 0.f, 0.f);
         float gO = 0.0f;
         active = active && diffuse_seeds(P, g, gd[i], cos_t, nc, gC, gO);
-        const ConeGeo K = make_cone(d, start, dir, c32 ? kAperture32 : kAperture16, min_level,
+        const ConeGeo K = make_cone(d, start, dir, P.diffuse_aperture, min_level,
                                     fmaxf(kMinTraceStepFactor, d.min_trace_step_factor));
         cone_backward_lane(T, G, d, K, gC, gO, active, kMaxTraceDistance, err);
     }
 }
 
-// One warp per sample in the coherent order; samples without a specular cone
-// (or a zero specular gradient) are skipped by the whole warp.
-__global__ void __launch_bounds__(32 * kSpecWarps) k_cone_backward_specular(
+// The diffuse cones of 32 samples at a time: a warp takes 32 consecutive
+// samples of the coherent order and deals their (sample, cone) pairs with
+// cos >= 0 to its lanes in rounds, cone-major; all diffuse cones share one
+// step schedule, so the lanes of a round walk in step.  Nearby samples' cones
+// scatter into the same region of the gradient atlas while it is in L2
+// (the cone-major kernel above sweeps the whole atlas once per cone).
+constexpr int kTileWarps = 4;
+
+__global__ void __launch_bounds__(32 * kTileWarps) k_cone_backward_diffuse_tiles(
     TraceParams P, F4Atlas T, const vct_surface_sample* __restrict__ samples, int64_t n,
-    const uint32_t* __restrict__ order, const float4* __restrict__ gsp, float4* __restrict__ G,
+    const uint32_t* __restrict__ order, const float4* __restrict__ gd, float4* __restrict__ G,
     int* __restrict__ err) {
-    __shared__ RoundStart s_rounds[kSpecWarps][kMaxRounds];
+    __shared__ float4 s_start[kTileWarps][32];  // start, min_level
+    __shared__ float4 s_norm[kTileWarps][32];   // normal, AO seed
+    __shared__ float4 s_seed[kTileWarps][32];   // rgb seed
+    __shared__ int s_cincl[kTileWarps][32];
+    __shared__ uint32_t s_cmask[kTileWarps][32];
     const vct_cone_tracing_desc& d = P.d;
-    const int w = threadIdx.x >> 5;
-    const int64_t nwarps = (int64_t)gridDim.x * kSpecWarps;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const bool c32 = d.enable_32_cones != 0;
+    const int nc = c32 ? 32 : 16;
+    const uint32_t mode = d.rendering_mode;
+    const float sf = fmaxf(kMinTraceStepFactor, d.min_trace_step_factor);
+    const int64_t nwarps = (int64_t)gridDim.x * kTileWarps;
+    for (int64_t base = ((int64_t)blockIdx.x * kTileWarps + w) * 32; base < n; base += nwarps * 32) {
+        const int64_t pos = base + lane;
+        bool valid = pos < n;
+        const int64_t i = valid ? (order ? (int64_t)__ldg(order + pos) : pos) : 0;
+        uint32_t mask = 0;
+        float4 start4 = make_float4(0.f, 0.f, 0.f, 0.f), norm4 = start4, seed4 = start4;
+        if (valid) {
+            const GSample g = load_sample(samples + i, P.eye);
+            valid = g.depth != 1.0f;
+            if (valid) {
+                // dL/d(indirect): D.rgb = direct * ind.w + ind.rgb (modes 5 and the default), direct * ind.w
+                // (4), ind.w (7); the others do not read the volume
+                const float4 GD = gd[i];
+                float3 g_ind = f3(0.f, 0.f, 0.f);
+                float g_ao = 0.0f;
+                const bool rgb_mode = mode == 5 || mode >= 8;
+                if (rgb_mode) g_ind = f3(GD.x, GD.y, GD.z);
+                if (rgb_mode || mode == 4) {
+                    const float3 direct = direct_term(P, g);
+                    g_ao = GD.x * direct.x + GD.y * direct.y + GD.z * direct.z;
+                } else if (mode == 7) {
+                    g_ao = GD.x + GD.y + GD.z;
+                }
+                const float min_level = calc_min_level(d, g.wp);
+                const float vs = d.voxel_size * exp2f(min_level);
+                const float3 st = g.wp + g.normal * (vs * d.trace_start_offset);
+                start4 = make_float4(st.x, st.y, st.z, min_level);
+                norm4 = make_float4(g.normal.x, g.normal.y, g.normal.z, g_ao);
+                seed4 = make_float4(g_ind.x * (g.diffuse_color.x * d.indirect_diffuse_intensity),
+                                    g_ind.y * (g.diffuse_color.y * d.indirect_diffuse_intensity),
+                                    g_ind.z * (g.diffuse_color.z * d.indirect_diffuse_intensity), 0.0f);
+                if (!(seed4.x == 0.0f && seed4.y == 0.0f && seed4.z == 0.0f && g_ao == 0.0f))
+                    for (int c = 0; c < nc; ++c) {
+                        const float3 dir = c32 ? f3(c_dirs32[c][0], c_dirs32[c][1], c_dirs32[c][2])
+                                               : f3(c_dirs16[c][0], c_dirs16[c][1], c_dirs16[c][2]);
+                        if (dot3(g.normal, dir) >= 0.0f) mask |= 1u << c;
+                    }
+            }
+        }
+        uint32_t my_cmask = 0;
+        for (int c = 0; c < nc; ++c) {
+            const uint32_t cm = __ballot_sync(0xffffffffu, (mask >> c) & 1u);
+            if (lane == c) my_cmask = cm;
+        }
+        int cincl = __popc(my_cmask);
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, cincl, o);
+            if (lane >= o) cincl += t;
+        }
+        const int total = __shfl_sync(0xffffffffu, cincl, 31);
+        s_start[w][lane] = start4;
+        s_norm[w][lane] = norm4;
+        s_seed[w][lane] = seed4;
+        s_cincl[w][lane] = cincl;
+        s_cmask[w][lane] = my_cmask;
+        __syncwarp();
+        for (int r0 = 0; r0 < total; r0 += 32) {  // warp-uniform
+            const int k = r0 + lane;
+            const bool active = k < total;
+            int lo = 0, hi = 31;  // the cone whose inclusive prefix first exceeds k
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (s_cincl[w][mid] > k) hi = mid;
+                else lo = mid + 1;
+            }
+            const int cone = active ? lo : 0;
+            const uint32_t cm = s_cmask[w][cone];
+            const int j = k - (s_cincl[w][cone] - __popc(cm));
+            const int sl = active ? (int)__fns(cm, 0, j + 1) : 0;  // the sample's lane
+            const float3 dir = c32 ? f3(c_dirs32[cone][0], c_dirs32[cone][1], c_dirs32[cone][2])
+                                   : f3(c_dirs16[cone][0], c_dirs16[cone][1], c_dirs16[cone][2]);
+            const float4 st = s_start[w][sl], nn = s_norm[w][sl], sd4 = s_seed[w][sl];
+            const float cos_t = dot3(f3(nn.x, nn.y, nn.z), dir);
+            const float wgt = cos_t / (float)nc;
+            const float3 gC = f3(sd4.x * wgt, sd4.y * wgt, sd4.z * wgt);
+            const float gO = -(nn.w * wgt * d.ambient_occlusion_factor);  // the cone returns 1 - occlusion
+            const ConeGeo K = make_cone(d, f3(st.x, st.y, st.z), dir, P.diffuse_aperture, st.w, sf);
+            cone_backward_lane(T, G, d, K, gC, gO, active, kMaxTraceDistance, err);
+        }
+        __syncwarp();
+    }
+}
+
+// Diffuse adjoint: sample tiles (k_cone_backward_diffuse_tiles) or cone-major
+// slots (k_cone_backward_diffuse).
+constexpr bool kGradDiffuseTiles = true;
+
+// One lane per specular cone of the aperture-grouped list (a warp's cones
+// share their step schedule, so the lock-step walk keeps its lanes busy).
+__global__ void __launch_bounds__(128) k_cone_backward_specular(
+    TraceParams P, F4Atlas T, const vct_surface_sample* __restrict__ samples, const uint32_t* __restrict__ list,
+    const unsigned int* __restrict__ spec_count, const float4* __restrict__ gsp, float4* __restrict__ G,
+    int* __restrict__ err) {
+    const vct_cone_tracing_desc& d = P.d;
     if (!(d.rendering_mode == 6 || d.rendering_mode >= 8)) return;
-    for (int64_t u = (int64_t)blockIdx.x * kSpecWarps + w; u < n; u += nwarps) {
-        const int64_t i = order ? (int64_t)__ldg(order + u) : u;
+    const int lane = threadIdx.x & 31;
+    const int64_t m = *spec_count;
+    // warp-uniform trip count: a warp's lanes enter cone_backward_lane together
+    for (int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x - lane; t0 < m;
+         t0 += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t t = t0 + lane;
+        bool active = t < m;
+        const uint32_t i = __ldg(list + (active ? t : t0));
         const GSample g = load_sample(samples + i, P.eye);
-        if (g.depth == 1.0f || !has_specular_cone(g)) continue;
         const float4 GS = gsp[i];
         const float isi = d.indirect_specular_intensity;
         const float3 gC = f3(GS.x * g.specular_color.x * isi, GS.y * g.specular_color.y * isi,
                              GS.z * g.specular_color.z * isi);
-        if (gC.x == 0.0f && gC.y == 0.0f && gC.z == 0.0f) continue;
+        active = active && !(gC.x == 0.0f && gC.y == 0.0f && gC.z == 0.0f);
         const float min_level = calc_min_level(d, g.wp);
         const float vs = d.voxel_size * exp2f(min_level);
         const float3 start = g.wp + g.normal * (vs * d.trace_start_offset);
         const float3 sdir = reflect3(f3(-g.view.x, -g.view.y, -g.view.z), g.normal);
         const ConeGeo K = make_cone(d, start, sdir, fmaxf(g.roughness, kMinSpecularAperture), min_level, d.voxel_size);
-        cone_backward_warp(T, G, d, K, gC, 0.0f, kMaxTraceDistance, s_rounds[w], err);
-        __syncwarp();
+        cone_backward_lane(T, G, d, K, gC, 0.0f, active, kMaxTraceDistance, err);
     }
 }
 
@@ -481,28 +433,35 @@ extern "C" int vct_cone_trace_backward(const vct_cone_tracing_desc* desc, const 
     const int nc = desc->enable_32_cones ? 32 : 16;
     int64_t blocks = (n * nc + 127) / 128;
     if (blocks > 152 * 32) blocks = 152 * 32;
-    int64_t sblocks = (n + kSpecWarps - 1) / kSpecWarps;
-    if (sblocks > 152 * 16) sblocks = 152 * 16;
-    SampleOrder so;
-    rc = sample_coherent_order(samples, n, P.d, &so, st);
+    ExactPlan plan;
+    rc = exact_plan(samples, n, P.d, &plan, st);
     if (rc != VCT_OK) {
         cudaFreeAsync(err, st);
         return rc;
     }
     float4* G = reinterpret_cast<float4*>(grad_atlas4);
-    k_cone_backward_diffuse<<<(int)blocks, 128, 0, st>>>(P, T, samples, n, so.order,
-                                                          reinterpret_cast<const float4*>(grad_diffuse), G, err);
+    if (kGradDiffuseTiles) {
+        int64_t tblocks = (n + 32 * kTileWarps - 1) / (32 * kTileWarps);
+        if (tblocks > 152 * 16) tblocks = 152 * 16;
+        k_cone_backward_diffuse_tiles<<<(int)tblocks, 32 * kTileWarps, 0, st>>>(
+            P, T, samples, n, plan.order, reinterpret_cast<const float4*>(grad_diffuse), G, err);
+    } else {
+        k_cone_backward_diffuse<<<(int)blocks, 128, 0, st>>>(P, T, samples, n, plan.order,
+                                                              reinterpret_cast<const float4*>(grad_diffuse), G, err);
+    }
     cudaError_t le = cudaGetLastError();
     if (le == cudaSuccess) {
-        k_cone_backward_specular<<<(int)sblocks, 32 * kSpecWarps, 0, st>>>(
-            P, T, samples, n, so.order, reinterpret_cast<const float4*>(grad_specular), G, err);
+        int64_t lblocks = (n + 127) / 128;
+        if (lblocks > 152 * 32) lblocks = 152 * 32;
+        k_cone_backward_specular<<<(int)lblocks, 128, 0, st>>>(P, T, samples, plan.spec_list, plan.spec_count,
+                                                               reinterpret_cast<const float4*>(grad_specular), G, err);
         le = cudaGetLastError();
     }
     int h_err = 0;
     cudaError_t ce = cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, st);
     cudaError_t se = cudaStreamSynchronize(st);
     cudaFreeAsync(err, st);
-    if (so.block) cudaFreeAsync(so.block, st);
+    exact_plan_free(&plan, st);
     if (le != cudaSuccess) return cuda_fail(le, "vct_cone_trace_backward kernels");
     if (ce != cudaSuccess) return cuda_fail(ce, "vct_cone_trace_backward readback");
     if (se != cudaSuccess) return cuda_fail(se, "vct_cone_trace_backward");
