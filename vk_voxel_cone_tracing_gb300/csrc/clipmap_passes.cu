@@ -207,101 +207,18 @@ __global__ void k_downsample(uint32_t* __restrict__ atlas, AtlasDims A, int3 pmi
     }
 }
 
-// copyAlphaImage.comp then radianceDownSample.comp for one level l >= 1, in
-// one pass over the level's R^3 interior (x fastest), all faces: every texel
-// takes the opacity atlas's alpha, and the texels the downsample writes --
-// the (R/2)^3 block from the previous region's corner / 2 on, toroidally --
-// then blend the 2x2x2 composite of level l-1 with that updated texel exactly
-// as k_downsample<1> does.  Same result as the two passes in sequence.
-__global__ void __launch_bounds__(128, 8) k_alpha_downsample(uint32_t* __restrict__ rad, const uint32_t* __restrict__ opa, AtlasDims A,
-                                   int3 pmin, int level, int band, int lg, cudaSurfaceObject_t mirror,
-                                   const uint32_t* __restrict__ touched) {
-    const int half = A.R >> 1;
-    const uint32_t n = 1u << (3 * lg);
-    const int pm[3] = {pmin.x, pmin.y, pmin.z};
-    const float inv = 1.0f / __fadd_rn((float)band, 1.0f);
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        int w[3];
-        cube_texel(t, lg, w[0], w[1], w[2]);
-        int cur[3], ps[3];
-        bool target = true;
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            const int g = (w[a] - (pm[a] >> 1)) & (A.R - 1);  // this texel's downsample thread, if g < R/2
-            target = target && g < half;
-            cur[a] = (pm[a] >> 1) + g;
-            ps[a] = ds_wrap(cur[a] << 1, A.R) + 1;
-        }
-        ps[1] += A.rb * (level - 1);
-        float lerp = 0.0f;
-        if (target) {  // lerpFactor (opacityDownSample.comp:55-64)
-            float dist[3];
-            bool any_ge = false;
-#pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                float center = __fadd_rn((float)(pm[a] >> 1), (float)(half >> 1));
-                dist[a] = __fsub_rn(fabsf(__fsub_rn(__fadd_rn((float)cur[a], 0.5f), center)), 0.5f);
-                any_ge |= dist[a] >= (float)((half >> 1) - band);
-            }
-            if (any_ge) {
-                lerp = __fadd_rn(__fsub_rn(fmaxf(dist[0], fmaxf(dist[1], dist[2])), (float)((half >> 1) - band)), 1.0f);
-                lerp = __fmul_rn(lerp, inv);
-            }
-        }
-        // all six faces' texels and alphas first (independent loads in flight)
-        const int64_t w0 = A.index(w[0] + 1, w[1] + 1 + A.rb * level, w[2] + 1);
-        uint32_t own6[6];
-#pragma unroll
-        for (int f = 0; f < 6; ++f)
-            own6[f] = rgb_of(rad, touched, w0 + A.rb * f) | (__ldg(opa + w0 + A.rb * f) & 0xff000000u);
-        const int my = w[1] + 1 + A.rb * level, mz = w[2] + 1;
-        if (!target) {
-#pragma unroll
-            for (int f = 0; f < 6; ++f) {
-                rad[w0 + A.rb * f] = own6[f];
-                if (mirror) surf3Dwrite(own6[f], mirror, (w[0] + 1 + A.rb * f) * 4, my, mz);
-            }
-            continue;
-        }
-#pragma unroll 1
-        for (int f = 0; f < 6; ++f) {  // the composite path: one face at a time keeps 8 blocks per SM resident
-            const int64_t wi = w0 + A.rb * f;
-            const uint32_t own_raw = own6[f];
-            uint32_t raw[8];
-#pragma unroll
-            for (int i = 0; i < 8; ++i)
-                raw[i] = rad[A.index(ps[0] + (i & 1) + A.rb * f, ps[1] + ((i >> 1) & 1), ps[2] + ((i >> 2) & 1))];
-            float s[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const uint32_t r0 = raw[c_pairs[f][k][0]], r1 = raw[c_pairs[f][k][1]];
-                const float tt = __fsub_rn(1.0f, unorm8_load(r0, 3));
-#pragma unroll
-                for (int c = 0; c < 4; ++c) {
-                    const float a0 = unorm8_load(r0, c);
-                    const float b = __fmul_rn(tt, unorm8_load(r1, c));
-                    s[c] = (k == 0) ? __fadd_rn(a0, b) : __fadd_rn(__fadd_rn(s[c], a0), b);
-                }
-            }
-            uint32_t out = 0;
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                const float res = __fmul_rn(s[c], 0.25f);
-                out |= unorm8_store(mix_rn(res, unorm8_load(own_raw, c), lerp)) << (8 * c);
-            }
-            rad[wi] = out;
-            if (mirror) surf3Dwrite(out, mirror, (w[0] + 1 + A.rb * f) * 4, my, mz);
-        }
-    }
-}
-
-// The same pass in two loops of one launch: (a) copy-alpha of the level's
-// texels outside the downsample's target block (cube_texel order, as
-// k_alpha_downsample), (b) the (R/2)^3 target block in a compact index
-// space (x fastest), each target taking its copy-alpha value as the blend's
-// own texel -- every lane of a loop does the same kind of work.  The target
-// block depends only on level l - 1, which earlier launches finished.
-__global__ void __launch_bounds__(128, 8) k_alpha_downsample_split(uint32_t* __restrict__ rad,
+// copyAlphaImage.comp then radianceDownSample.comp for one level l >= 1 in
+// one launch, same result as the two passes in sequence.  Two grid-stride
+// loops: (a) copy-alpha of the level's R^3 interior texels outside the
+// downsample's target block (the (R/2)^3 block from the previous region's
+// corner / 2 on, toroidally), in cube_texel order; (b) the target block in a
+// compact index space (x fastest): each target takes its copy-alpha value
+// as the blend's own texel and blends the 2x2x2 composite of level l - 1
+// with it as k_downsample<1> does -- every lane of a loop does the same kind
+// of work (one loop over the mixed texels was 3 % slower per frame at
+// R = 256).  The target block depends only on level l - 1, which earlier
+// launches finished.  All six faces per thread.
+__global__ void __launch_bounds__(128, 8) k_alpha_downsample(uint32_t* __restrict__ rad,
                                                                     const uint32_t* __restrict__ opa, AtlasDims A,
                                                                     int3 pmin, int level, int band, int lg,
                                                                     cudaSurfaceObject_t mirror,
@@ -393,10 +310,6 @@ __global__ void __launch_bounds__(128, 8) k_alpha_downsample_split(uint32_t* __r
     }
 }
 
-// k_alpha_downsample (one loop, target and copy texels mixed) or
-// k_alpha_downsample_split (a copy loop and a target loop).
-constexpr bool kAlphaDownsampleSplit = true;
-
 static int grid_for(int64_t n, int block) {
     int64_t g = (n + block - 1) / block;
     if (g > 152 * 64) g = 152 * 64;
@@ -462,12 +375,8 @@ int copy_alpha_downsample_pass(uint32_t* radiance, const uint32_t* opacity, cons
     const int64_t n = (int64_t)A.R * A.R * A.R;
     int3 pm = make_int3(d->prev_region_min_corner[0], d->prev_region_min_corner[1], d->prev_region_min_corner[2]);
     const int lg = 31 - __builtin_clz((unsigned)A.R);
-    if (kAlphaDownsampleSplit)
-        k_alpha_downsample_split<<<grid_for(n, 128), 128, 0, st>>>(radiance, opacity, A, pm, d->clip_level,
-                                                                   d->downsample_region_size, lg, mirror, touched);
-    else
-        k_alpha_downsample<<<grid_for(n, 128), 128, 0, st>>>(radiance, opacity, A, pm, d->clip_level,
-                                                            d->downsample_region_size, lg, mirror, touched);
+    k_alpha_downsample<<<grid_for(n, 128), 128, 0, st>>>(radiance, opacity, A, pm, d->clip_level,
+                                                        d->downsample_region_size, lg, mirror, touched);
     VCT_LAUNCH_CHECK();
     return VCT_OK;
 }

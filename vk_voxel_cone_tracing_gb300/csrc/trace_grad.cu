@@ -259,118 +259,6 @@ __global__ void __launch_bounds__(128) k_cone_backward_diffuse(TraceParams P, F4
     }
 }
 
-// The diffuse cones of 32 samples at a time: a warp takes 32 consecutive
-// samples of the coherent order and deals their (sample, cone) pairs with
-// cos >= 0 to its lanes in rounds, cone-major; all diffuse cones share one
-// step schedule, so the lanes of a round walk in step.  Nearby samples' cones
-// scatter into the same region of the gradient atlas while it is in L2
-// (the cone-major kernel above sweeps the whole atlas once per cone).
-constexpr int kTileWarps = 4;
-
-__global__ void __launch_bounds__(32 * kTileWarps) k_cone_backward_diffuse_tiles(
-    TraceParams P, F4Atlas T, const vct_surface_sample* __restrict__ samples, int64_t n,
-    const uint32_t* __restrict__ order, const float4* __restrict__ gd, float4* __restrict__ G,
-    int* __restrict__ err) {
-    __shared__ float4 s_start[kTileWarps][32];  // start, min_level
-    __shared__ float4 s_norm[kTileWarps][32];   // normal, AO seed
-    __shared__ float4 s_seed[kTileWarps][32];   // rgb seed
-    __shared__ int s_cincl[kTileWarps][32];
-    __shared__ uint32_t s_cmask[kTileWarps][32];
-    const vct_cone_tracing_desc& d = P.d;
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const bool c32 = d.enable_32_cones != 0;
-    const int nc = c32 ? 32 : 16;
-    const uint32_t mode = d.rendering_mode;
-    const float sf = fmaxf(kMinTraceStepFactor, d.min_trace_step_factor);
-    const int64_t nwarps = (int64_t)gridDim.x * kTileWarps;
-    for (int64_t base = ((int64_t)blockIdx.x * kTileWarps + w) * 32; base < n; base += nwarps * 32) {
-        const int64_t pos = base + lane;
-        bool valid = pos < n;
-        const int64_t i = valid ? (order ? (int64_t)__ldg(order + pos) : pos) : 0;
-        uint32_t mask = 0;
-        float4 start4 = make_float4(0.f, 0.f, 0.f, 0.f), norm4 = start4, seed4 = start4;
-        if (valid) {
-            const GSample g = load_sample(samples + i, P.eye);
-            valid = g.depth != 1.0f;
-            if (valid) {
-                // dL/d(indirect): D.rgb = direct * ind.w + ind.rgb (modes 5 and the default), direct * ind.w
-                // (4), ind.w (7); the others do not read the volume
-                const float4 GD = gd[i];
-                float3 g_ind = f3(0.f, 0.f, 0.f);
-                float g_ao = 0.0f;
-                const bool rgb_mode = mode == 5 || mode >= 8;
-                if (rgb_mode) g_ind = f3(GD.x, GD.y, GD.z);
-                if (rgb_mode || mode == 4) {
-                    const float3 direct = direct_term(P, g);
-                    g_ao = GD.x * direct.x + GD.y * direct.y + GD.z * direct.z;
-                } else if (mode == 7) {
-                    g_ao = GD.x + GD.y + GD.z;
-                }
-                const float min_level = calc_min_level(d, g.wp);
-                const float vs = d.voxel_size * exp2f(min_level);
-                const float3 st = g.wp + g.normal * (vs * d.trace_start_offset);
-                start4 = make_float4(st.x, st.y, st.z, min_level);
-                norm4 = make_float4(g.normal.x, g.normal.y, g.normal.z, g_ao);
-                seed4 = make_float4(g_ind.x * (g.diffuse_color.x * d.indirect_diffuse_intensity),
-                                    g_ind.y * (g.diffuse_color.y * d.indirect_diffuse_intensity),
-                                    g_ind.z * (g.diffuse_color.z * d.indirect_diffuse_intensity), 0.0f);
-                if (!(seed4.x == 0.0f && seed4.y == 0.0f && seed4.z == 0.0f && g_ao == 0.0f))
-                    for (int c = 0; c < nc; ++c) {
-                        const float3 dir = c32 ? f3(c_dirs32[c][0], c_dirs32[c][1], c_dirs32[c][2])
-                                               : f3(c_dirs16[c][0], c_dirs16[c][1], c_dirs16[c][2]);
-                        if (dot3(g.normal, dir) >= 0.0f) mask |= 1u << c;
-                    }
-            }
-        }
-        uint32_t my_cmask = 0;
-        for (int c = 0; c < nc; ++c) {
-            const uint32_t cm = __ballot_sync(0xffffffffu, (mask >> c) & 1u);
-            if (lane == c) my_cmask = cm;
-        }
-        int cincl = __popc(my_cmask);
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int t = __shfl_up_sync(0xffffffffu, cincl, o);
-            if (lane >= o) cincl += t;
-        }
-        const int total = __shfl_sync(0xffffffffu, cincl, 31);
-        s_start[w][lane] = start4;
-        s_norm[w][lane] = norm4;
-        s_seed[w][lane] = seed4;
-        s_cincl[w][lane] = cincl;
-        s_cmask[w][lane] = my_cmask;
-        __syncwarp();
-        for (int r0 = 0; r0 < total; r0 += 32) {  // warp-uniform
-            const int k = r0 + lane;
-            const bool active = k < total;
-            int lo = 0, hi = 31;  // the cone whose inclusive prefix first exceeds k
-            while (lo < hi) {
-                const int mid = (lo + hi) >> 1;
-                if (s_cincl[w][mid] > k) hi = mid;
-                else lo = mid + 1;
-            }
-            const int cone = active ? lo : 0;
-            const uint32_t cm = s_cmask[w][cone];
-            const int j = k - (s_cincl[w][cone] - __popc(cm));
-            const int sl = active ? (int)__fns(cm, 0, j + 1) : 0;  // the sample's lane
-            const float3 dir = c32 ? f3(c_dirs32[cone][0], c_dirs32[cone][1], c_dirs32[cone][2])
-                                   : f3(c_dirs16[cone][0], c_dirs16[cone][1], c_dirs16[cone][2]);
-            const float4 st = s_start[w][sl], nn = s_norm[w][sl], sd4 = s_seed[w][sl];
-            const float cos_t = dot3(f3(nn.x, nn.y, nn.z), dir);
-            const float wgt = cos_t / (float)nc;
-            const float3 gC = f3(sd4.x * wgt, sd4.y * wgt, sd4.z * wgt);
-            const float gO = -(nn.w * wgt * d.ambient_occlusion_factor);  // the cone returns 1 - occlusion
-            const ConeGeo K = make_cone(d, f3(st.x, st.y, st.z), dir, P.diffuse_aperture, st.w, sf);
-            cone_backward_lane(T, G, d, K, gC, gO, active, kMaxTraceDistance, err);
-        }
-        __syncwarp();
-    }
-}
-
-// Diffuse adjoint: sample tiles (k_cone_backward_diffuse_tiles) or cone-major
-// slots (k_cone_backward_diffuse).
-constexpr bool kGradDiffuseTiles = true;
-
 // One lane per specular cone of the aperture-grouped list (a warp's cones
 // share their step schedule, so the lock-step walk keeps its lanes busy).
 __global__ void __launch_bounds__(128) k_cone_backward_specular(
@@ -440,15 +328,8 @@ extern "C" int vct_cone_trace_backward(const vct_cone_tracing_desc* desc, const 
         return rc;
     }
     float4* G = reinterpret_cast<float4*>(grad_atlas4);
-    if (kGradDiffuseTiles) {
-        int64_t tblocks = (n + 32 * kTileWarps - 1) / (32 * kTileWarps);
-        if (tblocks > 152 * 16) tblocks = 152 * 16;
-        k_cone_backward_diffuse_tiles<<<(int)tblocks, 32 * kTileWarps, 0, st>>>(
-            P, T, samples, n, plan.order, reinterpret_cast<const float4*>(grad_diffuse), G, err);
-    } else {
-        k_cone_backward_diffuse<<<(int)blocks, 128, 0, st>>>(P, T, samples, n, plan.order,
-                                                              reinterpret_cast<const float4*>(grad_diffuse), G, err);
-    }
+    k_cone_backward_diffuse<<<(int)blocks, 128, 0, st>>>(P, T, samples, n, plan.order,
+                                                          reinterpret_cast<const float4*>(grad_diffuse), G, err);
     cudaError_t le = cudaGetLastError();
     if (le == cudaSuccess) {
         int64_t lblocks = (n + 127) / 128;
