@@ -618,6 +618,72 @@ def other_forms(dev, stream, R, regs, desc, radiance, samples, light, shadow, ls
     return out
 
 
+def batched_trace_phase(dev, jobs, keep, ctxs, streams, grids):
+    """The traces of the batch on their own: every scene's clipmap is rebuilt by its frame and copied into a
+    texture of its own, then the 64 traces run (a) as 64 vct_cone_trace_fast calls back to back on one stream
+    and (b) as one vct_cone_trace_fast_batch call (one launch per stage over the work queue of all jobs).
+    CUDA events, median of 5; the outputs of (a) and (b) are compared bit for bit."""
+    import torch
+    from vk_voxel_cone_tracing_gb300 import capi, clipmap, engine
+    stream = torch.cuda.current_stream()
+    texes, descs, outs, records = [], [], [], []
+    for i, j in enumerate(jobs):
+        engine.batch_submit([j], 1)
+        ctx = ctxs[(i % streams, int(grids[i]))]
+        b = ctx.buffers()
+        R = int(grids[i])
+        tex = clipmap.RadianceTexture(R).update(ctx.atlas("radiance"))
+        r0 = b.regions[0]
+        d = capi.ConeTracingDesc.from_buffer_copy(bytes(keep[i][3]))
+        for a in range(3):
+            d.volume_center[a] = float(np.float32(r0.min_corner[a]) * np.float32(r0.voxel_size) +
+                                       (np.float32(r0.extent[a]) * np.float32(r0.voxel_size)) * np.float32(0.5))
+        d.voxel_size = r0.voxel_size
+        d.volume_dimension = float(R)
+        smp = keep[i][2]
+        n = smp.shape[0]
+        o = (torch.empty((n, 4), device=dev), torch.empty((n, 4), device=dev),
+             torch.empty((n, 4), device=dev), torch.empty((n, 4), device=dev))
+        shadow = engine._device_view(b.shadow_depth, (1024, 1024)).view(torch.float32).clone()
+        texes.append(tex)
+        descs.append(d)
+        outs.append((o, shadow, j.light, j.light_shadow))
+        records.append(clipmap.trace_job(d, keep[i][6], tex, smp, o[2], o[3], light=j.light, shadow=shadow,
+                                         shadow_desc=j.light_shadow))
+    torch.cuda.synchronize()
+    scratch_one = clipmap.fast_scratch(max(k[2].shape[0] for k in keep), dev)
+
+    def separate():
+        for i in range(len(jobs)):
+            o, shadow, light, lsd = outs[i]
+            clipmap.cone_trace_fast(descs[i], keep[i][6], texes[i], keep[i][2], light=light, shadow=shadow,
+                                    shadow_desc=lsd, diffuse=o[0], specular=o[1], scratch=scratch_one)
+
+    arr = (capi.TraceJob * len(records))(*records)
+    need = capi.lib().vct_cone_trace_fast_batch_scratch_bytes(ctypes_void(arr), len(records))
+    scratch_all = torch.empty(need + 256, dtype=torch.uint8, device=dev)
+
+    def batched():
+        clipmap.cone_trace_fast_batch(records, scratch_all)
+
+    separate()
+    batched()
+    torch.cuda.synchronize()
+    equal = all(torch.equal(o[0], o[2]) and torch.equal(o[1], o[3]) for o, *_ in outs)
+    sep_ms = statistics.median(events_ms(stream, separate, 5)[0])
+    bat_ms = statistics.median(events_ms(stream, batched, 5)[0])
+    for t in texes:
+        t.close()
+    return {"separate_calls_ms": sep_ms, "one_batched_call_ms": bat_ms, "outputs_bit_equal": equal,
+            "note": "trace phase only: the 64 scenes' traces as 64 vct_cone_trace_fast calls on one stream vs one "
+                    "vct_cone_trace_fast_batch call; CUDA events, median of 5"}
+
+
+def ctypes_void(arr):
+    import ctypes as C
+    return C.cast(arr, C.c_void_p)
+
+
 def batched_scenes(dev, streams: int = 4, n_scenes: int = 64, seed: int = 4):
     """Configuration 4: independent scenes (triangles log-uniform 10k-500k, clipmap R in {64, 128, 256},
     G-buffer samples log-uniform 4k-256k), one full frame + one trace each, submitted as one batch over
@@ -647,7 +713,7 @@ def batched_scenes(dev, streams: int = 4, n_scenes: int = 64, seed: int = 4):
         sout = torch.empty_like(dout)
         st = torch.zeros(1, dtype=torch.int64, device=dev)
         jobs.append(engine.batch_job(ctxs[(i % streams, R)], ds, cam, light, lsd, td, cam, smp, dout, sout, st))
-        keep.append((sc, ds, smp, td, dout, sout))
+        keep.append((sc, ds, smp, td, dout, sout, cam))
         steps.append(st)
     engine.batch_submit(jobs, streams)  # warm-up: workspaces and trace scratch reach their sizes
     torch.cuda.synchronize()
@@ -663,6 +729,7 @@ def batched_scenes(dev, streams: int = 4, n_scenes: int = 64, seed: int = 4):
         t0 = time.perf_counter()
         engine.batch_submit([j], 1)
         per.append((time.perf_counter() - t0) * 1e3)
+    trace_phase = batched_trace_phase(dev, jobs, keep, ctxs, streams, grids)
     for c in ctxs.values():
         c.close()
     return {"scenes": n_scenes, "triangles": int(tris.sum()), "samples": int(nsamp.sum()),
@@ -670,6 +737,7 @@ def batched_scenes(dev, streams: int = 4, n_scenes: int = 64, seed: int = 4):
             "cone_samples": cone_samples, "batched_ms": batched, "one_at_a_time_ms": sequential,
             "batched_cone_samples_per_s": cone_samples / (batched * 1e-3),
             "per_scene_ms": {"p50": float(np.percentile(per, 50)), "p99": float(np.percentile(per, 99))},
+            "trace_phase": trace_phase,
             "note": "each job: a full clipmap frame (voxelise, shadow, inject, mips) + the fast trace of its "
                     "samples; host wall clock, the submission synchronises"}
 

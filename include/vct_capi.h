@@ -428,6 +428,38 @@ int vct_cone_trace_fast_opt(const vct_cone_tracing_desc* desc, const vct_cam_mat
                             float* specular_out, unsigned long long* cone_steps, const vct_trace_options* options,
                             void* scratch, size_t scratch_bytes, void* stream);
 
+/* One trace of a batch: the arguments of vct_cone_trace_fast for one
+ * clipmap (its radiance texture, desc, camera eye, lighting) and one sample
+ * set with its outputs.  Host struct; the pointers are device pointers. */
+typedef struct vct_trace_job {
+    vct_cone_tracing_desc desc;
+    float eye[3];
+    vct_texture radiance;
+    vct_shadow_map shadow;      /* depth NULL: visibility 1 */
+    vct_directional_light_desc light;
+    vct_directional_light_shadow_desc light_shadow;
+    const vct_surface_sample* samples;
+    int64_t sample_count;
+    float* diffuse_out;
+    float* specular_out;
+    unsigned long long* cone_steps; /* may be NULL; added to */
+} vct_trace_job;
+
+/* The batched form of the cone-tracing pass (no counterpart in the
+ * reference, which traces one view of one scene per pass): every job of
+ * `jobs` in one launch per stage over a device work queue.  The jobs'
+ * samples share one coherent order in which each job holds a 32-aligned
+ * segment, so each warp-sized item of the diffuse kernel and each specular
+ * cone names one job, whose record (texture, constants, lighting, outputs)
+ * the kernels read from a device job table.  Every job's outputs equal, bit
+ * for bit, those of vct_cone_trace_fast on that job alone.  Scratch: caller
+ * provided, 256-byte aligned, vct_cone_trace_fast_batch_scratch_bytes bytes
+ * (negative: too many samples or jobs: at most 65,536 jobs and 2^31 - 1
+ * samples after each job's count is rounded up to a multiple of 32). */
+int64_t vct_cone_trace_fast_batch_scratch_bytes(const vct_trace_job* jobs_host, int32_t job_count);
+int vct_cone_trace_fast_batch(const vct_trace_job* jobs_host, int32_t job_count, void* scratch, size_t scratch_bytes,
+                              void* stream);
+
 /* Calibration probe for the trace's roofline; no counterpart in the
  * reference.  Times (CUDA events on `stream`, after one warm-up launch) a
  * kernel that marches `cones` synthetic cones of `steps_per_cone` steps, one
@@ -826,5 +858,6 @@ VCT_STATIC_ASSERT(sizeof(vct_batch_job) == 264, "vct_batch_job is 264 B");
 VCT_STATIC_ASSERT(sizeof(vct_gltf_shade_material) == 80, "GltfShadeMaterial is 80 B");
 VCT_STATIC_ASSERT(sizeof(vct_surface_sample) == 80, "surface sample is 80 B");
 VCT_STATIC_ASSERT(sizeof(vct_trace_options) == 16, "vct_trace_options is 16 B");
+VCT_STATIC_ASSERT(sizeof(vct_trace_job) == 296, "vct_trace_job is 296 B");
 
 #endif /* VCT_CAPI_H */

@@ -27,8 +27,11 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
           "-Xptxas", "-O3",
           "--expt-relaxed-constexpr", "-I", str(INCLUDE)]
-# Units that mirror FP32 shader arithmetic op for op.
-NO_FMA = {"clipmap_passes.cu", "trace_exact.cu", "raster.cu", "svo.cu", "svo_trace.cu", "composite.cu", "trace_grad.cu"}
+# Units that mirror FP32 shader arithmetic op for op, and the texture-form trace: its device functions are
+# inlined into the single and the batched kernels, and with multiply-add contraction left to the compiler the
+# two could round a sample's diffuse sum differently (by one unit in the last place) from the same inputs.
+NO_FMA = {"clipmap_passes.cu", "trace_exact.cu", "raster.cu", "svo.cu", "svo_trace.cu", "composite.cu", "trace_grad.cu",
+          "trace_fast.cu"}
 
 
 def nvcc() -> str:

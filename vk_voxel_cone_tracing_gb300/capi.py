@@ -169,11 +169,19 @@ class BatchJob(C.Structure):
                 ("specular_out", C.c_void_p), ("cone_steps", C.c_void_p)]
 
 
+class TraceJob(C.Structure):
+    """vct_trace_job: one trace of a vct_cone_trace_fast_batch call."""
+    _fields_ = [("desc", ConeTracingDesc), ("eye", f3), ("radiance", C.c_void_p), ("shadow", ShadowMap),
+                ("light", DirectionalLightDesc), ("light_shadow", DirectionalLightShadowDesc),
+                ("samples", C.c_void_p), ("sample_count", C.c_int64), ("diffuse_out", C.c_void_p),
+                ("specular_out", C.c_void_p), ("cone_steps", C.c_void_p)]
+
+
 STRUCT_SIZES = {
     ClipmapRegion: 28, VoxelizationDesc: 64, DownSampleDesc: 24, ImageCleaningDesc: 36, CopyAlphaDesc: 12,
     BorderWrappingDesc: 16, ConeTracingDesc: 52, CamMatrix: 144, DirectionalLightDesc: 32,
     DirectionalLightShadowDesc: 136, GltfShadeMaterial: 80, Scene: 104, SpecularFilterDesc: 16, Config: 24,
-    ContextBuffers: 216, BatchJob: 264, AdamDesc: 40, TraceOptions: 16,
+    ContextBuffers: 216, BatchJob: 264, AdamDesc: 40, TraceOptions: 16, TraceJob: 296,
 }
 
 # Every entry point of include/vct_capi.h: name -> (restype, argtypes).
@@ -208,6 +216,8 @@ _SIGS: dict[str, tuple] = {
     "vct_cone_trace_fast_scratch_bytes": (C.c_int64, [C.c_int64]),
     "vct_cone_trace_fast": (C.c_int, [P, P, P, P, P, P, P, C.c_int64, P, P, P, P, C.c_size_t, P]),
     "vct_cone_trace_fast_opt": (C.c_int, [P, P, P, P, P, P, P, C.c_int64, P, P, P, P, P, C.c_size_t, P]),
+    "vct_cone_trace_fast_batch_scratch_bytes": (C.c_int64, [P, C.c_int32]),
+    "vct_cone_trace_fast_batch": (C.c_int, [P, C.c_int32, P, C.c_size_t, P]),
     "vct_gather_probe": (C.c_int, [P, P, C.c_int64, C.c_int32, P, P]),
     "vct_workspace_create": (C.c_int, [C.c_size_t, C.POINTER(C.c_void_p)]),
     "vct_workspace_destroy": (C.c_int, [P]),

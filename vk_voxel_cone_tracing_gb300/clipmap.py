@@ -233,6 +233,40 @@ def cone_trace_fast(desc: capi.ConeTracingDesc, eye, tex: RadianceTexture, sampl
     return diffuse, specular
 
 
+def trace_job(desc: capi.ConeTracingDesc, eye, tex: RadianceTexture, samples: torch.Tensor,
+              diffuse: torch.Tensor, specular: torch.Tensor, light: capi.DirectionalLightDesc | None = None,
+              shadow: torch.Tensor | None = None, shadow_desc: capi.DirectionalLightShadowDesc | None = None,
+              steps: torch.Tensor | None = None) -> capi.TraceJob:
+    """One vct_trace_job record (the tensors must outlive the batched call)."""
+    j = capi.TraceJob()
+    j.desc = desc
+    j.eye = capi.f3(*[float(x) for x in eye])
+    j.radiance = tex.handle
+    j.shadow = capi.ShadowMap(shadow.data_ptr(), shadow.shape[1], shadow.shape[0]) if shadow is not None else \
+        capi.ShadowMap(None, 0, 0)
+    j.light = light or capi.DirectionalLightDesc(capi.f3(0.3, -1.0, 0.2), 1.0, capi.f3(1, 1, 1), 0)
+    j.light_shadow = shadow_desc or capi.DirectionalLightShadowDesc()
+    j.samples = samples.data_ptr() if samples.numel() else None
+    j.sample_count = samples.shape[0]
+    j.diffuse_out = diffuse.data_ptr() if diffuse.numel() else None
+    j.specular_out = specular.data_ptr() if specular.numel() else None
+    j.cone_steps = steps.data_ptr() if steps is not None else None
+    return j
+
+
+def cone_trace_fast_batch(jobs: list, scratch: torch.Tensor | None = None) -> None:
+    """vct_cone_trace_fast_batch over a list of trace_job records (one launch per stage for every job)."""
+    arr = (capi.TraceJob * max(1, len(jobs)))(*jobs)
+    need = capi.lib().vct_cone_trace_fast_batch_scratch_bytes(C.cast(arr, C.c_void_p), len(jobs))
+    if need < 0:
+        raise ValueError("too many samples for one batched trace")
+    if scratch is None or scratch.numel() < need + 256:
+        scratch = torch.empty(need + 256, dtype=torch.uint8, device="cuda")
+    base = _aligned(scratch)
+    capi.call("vct_cone_trace_fast_batch", C.cast(arr, C.c_void_p), len(jobs), C.c_void_p(base),
+              scratch.data_ptr() + scratch.numel() - base, _stream())
+
+
 def gather_probe(desc: capi.ConeTracingDesc, tex: RadianceTexture, cones: int = 152 * 1024, steps_per_cone: int = 64) -> float:
     """Measured cone-sample rate of the pure fetch pattern (vct_gather_probe): the trace's speed of light."""
     rate = C.c_double(0.0)

@@ -18,6 +18,9 @@
 //      RGBA16F storage, FP32 compositing.
 // Scratch memory (sort keys, orders, cub temporary storage) is provided by
 // the caller; vct_cone_trace_fast_scratch_bytes() gives its size.
+#include <cstring>
+#include <vector>
+
 #include <cub/cub.cuh>
 
 #include "trace_deal.cuh"
@@ -146,19 +149,31 @@ __device__ __forceinline__ uint32_t spread10(uint32_t v) {
     return v;
 }
 
+__device__ __forceinline__ uint32_t morton_key(const vct_surface_sample* __restrict__ s, const FastConsts& C) {
+    const float* p = s->position;
+    const float q = 0.5f * C.inv_uvs;  // two level-0 voxels per cell
+    int x = __float2int_rd((p[0] - C.cx) * q) + 512, y = __float2int_rd((p[1] - C.cy) * q) + 512,
+        z = __float2int_rd((p[2] - C.cz) * q) + 512;
+    x = min(max(x, 0), 1023);
+    y = min(max(y, 0), 1023);
+    z = min(max(z, 0), 1023);
+    return spread10(x) | (spread10(y) << 1) | (spread10(z) << 2);
+}
+
 __global__ void k_morton_keys(const vct_surface_sample* __restrict__ s, int64_t n, FastConsts C,
                               uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const float* p = s[i].position;
-        const float q = 0.5f * C.inv_uvs;  // two level-0 voxels per cell
-        int x = __float2int_rd((p[0] - C.cx) * q) + 512, y = __float2int_rd((p[1] - C.cy) * q) + 512,
-            z = __float2int_rd((p[2] - C.cz) * q) + 512;
-        x = min(max(x, 0), 1023);
-        y = min(max(y, 0), 1023);
-        z = min(max(z, 0), 1023);
-        keys[i] = spread10(x) | (spread10(y) << 1) | (spread10(z) << 2);
+        keys[i] = morton_key(s + i, C);
         vals[i] = (uint32_t)i;
     }
+}
+
+// The shader traces a specular cone where depth != 1 and the sample has a
+// specular colour and metalness.
+__device__ __forceinline__ bool traces_specular(const vct_surface_sample* __restrict__ s) {
+    const float4* p = reinterpret_cast<const float4*>(s);
+    const float4 a = __ldg(p + 0), d = __ldg(p + 3);
+    return a.w != 1.0f && (d.x > 1e-6f || d.y > 1e-6f || d.z > 1e-6f) && d.w > 1e-6f;
 }
 
 // Specular classification of the Morton-ordered samples (the shader traces
@@ -172,11 +187,7 @@ __global__ void k_spec_keys(const __grid_constant__ FastArgs A, const uint32_t* 
          base += (int64_t)gridDim.x * blockDim.x) {
         const int64_t pos = base + lane;
         bool spec = false;
-        if (pos < A.n && A.C.need_specular) {
-            const float4* p = reinterpret_cast<const float4*>(A.samples + __ldg(order + pos));
-            const float4 a = __ldg(p + 0), d = __ldg(p + 3);
-            spec = a.w != 1.0f && (d.x > 1e-6f || d.y > 1e-6f || d.z > 1e-6f) && d.w > 1e-6f;
-        }
+        if (pos < A.n && A.C.need_specular) spec = traces_specular(A.samples + __ldg(order + pos));
         if (pos < A.n) spec_key[pos] = spec ? 0u : 256u;
         const unsigned bal = __ballot_sync(0xffffffffu, spec);
         if (lane == 0 && bal) atomicAdd(spec_count, (unsigned)__popc(bal));
@@ -364,35 +375,132 @@ __device__ __forceinline__ float4 trace_cone_warp(cudaTextureObject_t tex, const
 // Consecutive steps of one specular cone per lane.
 constexpr int kSpecStepsPerLane = 2;
 
+// Sample idx's specular cone on the calling warp; lane 0 writes its output.
+__device__ __forceinline__ void specular_cone_warp(const FastArgs& A, uint32_t idx, unsigned long long& steps) {
+    const TraceParams& P = A.P;
+    const FastConsts& C = A.C;
+    const GSample g = load_sample(A.samples + idx, P.eye);
+    const float min_level = calc_min_level(P.d, g.wp);
+    const float vs = C.uvs * exp2f(min_level);
+    const float3 start = g.wp + g.normal * (vs * C.start_off);
+    const float3 sdir = reflect3(f3(-g.view.x, -g.view.y, -g.view.z), g.normal);
+    const float ap = fmaxf(g.roughness, kMinSpecularAperture);
+    const float coef = 2.0f * tanf(ap * 0.5f);
+    const float4 r = trace_cone_warp<kSpecStepsPerLane>(A.tex, C, start, sdir, coef, min_level, C.uvs, steps);
+    if ((threadIdx.x & 31) == 0) {
+        const float isi = P.d.indirect_specular_intensity;
+        reinterpret_cast<float4*>(A.sout)[idx] = make_float4(r.x * g.specular_color.x * isi,
+                                                             r.y * g.specular_color.y * isi,
+                                                             r.z * g.specular_color.z * isi, 1.0f);
+    }
+}
+
 // One warp per specular cone of the list (the list is kept in Morton order).
 __global__ void __launch_bounds__(256, 4) k_trace_specular_warp(const __grid_constant__ FastArgs A, const uint32_t* __restrict__ list,
                                                              const unsigned int* __restrict__ spec_count) {
-    const TraceParams& P = A.P;
-    const FastConsts& C = A.C;
     const int lane = threadIdx.x & 31;
     const int64_t m = *spec_count;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     unsigned long long steps = 0;
-    for (int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < m; c += nwarps) {
-        const uint32_t idx = __ldg(list + c);
-        const GSample g = load_sample(A.samples + idx, P.eye);
-        const float min_level = calc_min_level(P.d, g.wp);
-        const float vs = C.uvs * exp2f(min_level);
-        const float3 start = g.wp + g.normal * (vs * C.start_off);
-        const float3 sdir = reflect3(f3(-g.view.x, -g.view.y, -g.view.z), g.normal);
-        const float ap = fmaxf(g.roughness, kMinSpecularAperture);
-        const float coef = 2.0f * tanf(ap * 0.5f);
-        const float4 r = trace_cone_warp<kSpecStepsPerLane>(A.tex, C, start, sdir, coef, min_level, C.uvs, steps);
-        if (lane == 0) {
-            const float isi = P.d.indirect_specular_intensity;
-            reinterpret_cast<float4*>(A.sout)[idx] =
-                make_float4(r.x * g.specular_color.x * isi, r.y * g.specular_color.y * isi,
-                            r.z * g.specular_color.z * isi, 1.0f);
-        }
-    }
+    for (int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < m; c += nwarps)
+        specular_cone_warp(A, __ldg(list + c), steps);
     if (A.steps) {
         for (int o = 16; o > 0; o >>= 1) steps += __shfl_xor_sync(0xffffffffu, steps, o);
         if (lane == 0 && steps) atomicAdd(A.steps, steps);
+    }
+}
+
+// ------------------------------------------------------------ batched form
+// One trace over many jobs (clipmaps and sample sets) through a work queue:
+// a table of job records and a global, padded index space in which job j
+// owns the 32-aligned segment [bases[j], bases[j + 1]) (its count of samples
+// rounded up to a multiple of 32; the rest is padding).  One radix sort of
+// keys (job, Morton code of the sample, padding last) gives a coherent order
+// in which each job keeps its segment, so every 32-position warp item of the
+// diffuse kernel and every specular cone names one job.  The table travels as
+// a kernel parameter (constant bank, like the single trace's arguments: a
+// record read from global memory cost the specular kernel 1.4 KB of register
+// spills per thread), so it holds up to kBatchJobs jobs per launch.
+struct BatchJob {
+    FastArgs A;
+    uint32_t base, count;
+};
+constexpr int kBatchJobs = 48;
+struct BatchTable {
+    int njobs;
+    uint32_t bases[kBatchJobs + 1];
+    BatchJob jobs[kBatchJobs];
+};
+static_assert(sizeof(BatchTable) < 30000, "the batch table must fit the kernel parameter space");
+
+// The job whose segment holds global position g.
+__device__ __forceinline__ int batch_job_of(const BatchTable& T, uint32_t g) {
+    int lo = 0, hi = T.njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (T.bases[mid] <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void k_batch_keys(const __grid_constant__ BatchTable T, uint32_t total,
+                             unsigned long long* __restrict__ keys, uint32_t* __restrict__ vals) {
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+        const int j = batch_job_of(T, g);
+        const BatchJob& J = T.jobs[j];
+        const uint32_t i = g - J.base;
+        const uint32_t key = i < J.count ? morton_key(J.A.samples + i, J.A.C) : (1u << 30);
+        keys[g] = ((unsigned long long)j << 31) | key;
+        vals[g] = g;
+    }
+}
+
+__global__ void k_batch_spec_keys(const __grid_constant__ BatchTable T, uint32_t total,
+                                  const uint32_t* __restrict__ order, uint32_t* __restrict__ spec_key,
+                                  unsigned int* __restrict__ spec_count) {
+    const int lane = threadIdx.x & 31;
+    for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x - lane; b < total; b += gridDim.x * blockDim.x) {
+        const uint32_t pos = b + lane;
+        bool spec = false;
+        if (pos < total) {
+            const uint32_t g = __ldg(order + pos);
+            const BatchJob& J = T.jobs[batch_job_of(T, g)];
+            const uint32_t i = g - J.base;
+            spec = i < J.count && J.A.C.need_specular && traces_specular(J.A.samples + i);
+            spec_key[pos] = spec ? 0u : 256u;
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, spec);
+        if (lane == 0 && bal) atomicAdd(spec_count, (unsigned)__popc(bal));
+    }
+}
+
+__global__ void __launch_bounds__(256) k_batch_diffuse(const __grid_constant__ BatchTable T, uint32_t total,
+                                                       const uint32_t* __restrict__ order) {
+    const int64_t nwarps = (int64_t)gridDim.x * kWarpsPerBlock;
+    for (int64_t base = ((int64_t)blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5)) * 32; base < total;
+         base += nwarps * 32) {
+        const BatchJob& J = T.jobs[batch_job_of(T, (uint32_t)base)];  // warp-uniform: 32-aligned segments
+        const FastArgs& A = J.A;
+        DealArgs D{&A.P, A.samples, (int64_t)total, order, J.base, J.count, A.dout, A.sout, A.C.ncones,
+                   A.C.need_diffuse != 0, A.C.need_specular != 0};
+        unsigned long long steps = 0;
+        deal_diffuse_warp<kWarpsPerBlock>(D, FastDiffuseMarch{A.tex, &A.C}, base, steps);
+        add_steps(A.steps, steps);
+    }
+}
+
+__global__ void __launch_bounds__(256, 4) k_batch_specular(const __grid_constant__ BatchTable T,
+                                                           const uint32_t* __restrict__ list,
+                                                           const unsigned int* __restrict__ spec_count) {
+    const int64_t m = *spec_count;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < m; c += nwarps) {
+        const uint32_t g = __ldg(list + c);
+        const BatchJob& J = T.jobs[batch_job_of(T, g)];
+        unsigned long long steps = 0;
+        specular_cone_warp(J.A, g - J.base, steps);
+        if (J.A.steps && (threadIdx.x & 31) == 0 && steps) atomicAdd(J.A.steps, steps);
     }
 }
 
@@ -602,6 +710,165 @@ extern "C" int vct_cone_trace_fast_opt(const vct_cone_tracing_desc* desc, const 
     VCT_LAUNCH_CHECK();
     k_trace_specular_warp<<<grid_s, 256, 0, st>>>(A, S.spec_list, S.spec_count);
     VCT_LAUNCH_CHECK();
+    return VCT_OK;
+}
+
+// ------------------------------------------------------------ batched form
+namespace {
+
+// Scratch of one chunk of kBatchJobs jobs; the whole call reuses the
+// largest chunk's layout (chunks run one after the other on the stream).
+struct BatchLayout {
+    uint32_t positions;  // padded global positions of the largest chunk
+    size_t keys_in, keys_out, vals_in, order, spec_key, spec_key_out, spec_list, spec_count, temp;
+    size_t temp_bytes, total;
+};
+
+int64_t padded(int64_t n) { return (n + 31) & ~int64_t(31); }
+
+int batch_layout(const vct_trace_job* jobs, int32_t njobs, BatchLayout& L) {
+    int64_t most = 0;
+    for (int c0 = 0; c0 < njobs; c0 += kBatchJobs) {
+        int64_t pos = 0;
+        for (int j = c0; j < njobs && j < c0 + kBatchJobs; ++j) {
+            if (jobs[j].sample_count < 0 || jobs[j].sample_count > 0x7fffffffLL)
+                return fail(VCT_E_BAD_ARG, "vct_cone_trace_fast_batch: a job's sample count is out of range");
+            pos += padded(jobs[j].sample_count);
+            if (pos > 0x7fffffffLL)
+                return fail(VCT_E_BAD_ARG,
+                            "vct_cone_trace_fast_batch: more than 2^31 - 1 samples (32-padded per job) in one chunk");
+        }
+        most = pos > most ? pos : most;
+    }
+    L.positions = (uint32_t)most;
+    int jb = 0;
+    while ((1 << jb) < kBatchJobs) ++jb;
+    size_t t1 = 0, t2 = 0;
+    cudaError_t e = cub::DeviceRadixSort::SortPairs(nullptr, t1, (unsigned long long*)nullptr,
+                                                    (unsigned long long*)nullptr, (uint32_t*)nullptr,
+                                                    (uint32_t*)nullptr, (int)L.positions, 0, 31 + jb);
+    if (e == cudaSuccess)
+        e = cub::DeviceRadixSort::SortPairs(nullptr, t2, (uint32_t*)nullptr, (uint32_t*)nullptr, (uint32_t*)nullptr,
+                                            (uint32_t*)nullptr, (int)L.positions, 8, 9);
+    if (e != cudaSuccess) return cuda_fail(e, "cub::DeviceRadixSort::SortPairs (size query)");
+    L.temp_bytes = t1 > t2 ? t1 : t2;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t at = off;
+        off += align256(bytes);
+        return at;
+    };
+    const size_t n = L.positions;
+    L.keys_in = take(8 * n);
+    L.keys_out = take(8 * n);
+    L.vals_in = take(4 * n);
+    L.order = take(4 * n);
+    L.spec_key = take(4 * n);
+    L.spec_key_out = take(4 * n);
+    L.spec_list = take(4 * n);
+    L.spec_count = take(sizeof(unsigned int));
+    L.temp = take(L.temp_bytes);
+    L.total = off;
+    return VCT_OK;
+}
+
+}  // namespace
+
+extern "C" int64_t vct_cone_trace_fast_batch_scratch_bytes(const vct_trace_job* jobs, int32_t job_count) {
+    if (job_count < 0 || (job_count > 0 && !jobs)) return -1;
+    BatchLayout L;
+    if (batch_layout(jobs, job_count, L) != VCT_OK) return -1;
+    return (int64_t)L.total;
+}
+
+extern "C" int vct_cone_trace_fast_batch(const vct_trace_job* jobs, int32_t job_count, void* scratch,
+                                         size_t scratch_bytes, void* stream) {
+    vct::NvtxRange nvtx_range("vct_cone_trace_fast_batch");
+    VCT_CHECK_ARG(job_count >= 0, "vct_cone_trace_fast_batch: negative job count");
+    if (job_count == 0) return VCT_OK;
+    VCT_CHECK_ARG(jobs, "vct_cone_trace_fast_batch: null job list");
+    BatchLayout L;
+    int rc = batch_layout(jobs, job_count, L);
+    if (rc != VCT_OK) return rc;
+    if (L.positions == 0) return VCT_OK;
+    VCT_CHECK_ARG(scratch && ((uintptr_t)scratch & 255) == 0,
+                  "vct_cone_trace_fast_batch: scratch must be 256-byte aligned");
+    VCT_CHECK_ARG(scratch_bytes >= L.total, "vct_cone_trace_fast_batch: scratch buffer too small");
+    // every job is checked before any work is enqueued
+    for (int j = 0; j < job_count; ++j) {
+        const vct_trace_job& t = jobs[j];
+        VCT_CHECK_ARG(t.radiance, "vct_cone_trace_fast_batch: a job has no radiance texture");
+        VCT_CHECK_ARG((float)texture_resolution(t.radiance) == t.desc.volume_dimension,
+                      "vct_cone_trace_fast_batch: a job's volume dimension differs from its texture's resolution");
+        if (t.sample_count > 0) {
+            VCT_CHECK_ARG(t.samples && t.diffuse_out && t.specular_out,
+                          "vct_cone_trace_fast_batch: a job has a null sample or output buffer");
+            VCT_CHECK_ARG((((uintptr_t)t.samples | (uintptr_t)t.diffuse_out | (uintptr_t)t.specular_out) & 15) == 0,
+                          "vct_cone_trace_fast_batch: sample/output buffers must be 16-byte aligned");
+        }
+    }
+    cudaStream_t st = as_stream(stream);
+    char* b = static_cast<char*>(scratch);
+    auto* keys_in = reinterpret_cast<unsigned long long*>(b + L.keys_in);
+    auto* keys_out = reinterpret_cast<unsigned long long*>(b + L.keys_out);
+    uint32_t* vals_in = reinterpret_cast<uint32_t*>(b + L.vals_in);
+    uint32_t* order = reinterpret_cast<uint32_t*>(b + L.order);
+    uint32_t* spec_key = reinterpret_cast<uint32_t*>(b + L.spec_key);
+    uint32_t* spec_key_out = reinterpret_cast<uint32_t*>(b + L.spec_key_out);
+    uint32_t* spec_list = reinterpret_cast<uint32_t*>(b + L.spec_list);
+    unsigned int* spec_count = reinterpret_cast<unsigned int*>(b + L.spec_count);
+    int jb = 0;
+    while ((1 << jb) < kBatchJobs) ++jb;
+    std::vector<BatchTable> tables((job_count + kBatchJobs - 1) / kBatchJobs);
+    for (size_t c = 0; c < tables.size(); ++c) {
+        BatchTable& T = tables[c];
+        memset(&T, 0, sizeof(T));
+        const int c0 = (int)c * kBatchJobs;
+        T.njobs = job_count - c0 < kBatchJobs ? job_count - c0 : kBatchJobs;
+        uint32_t pos = 0;
+        for (int k = 0; k < T.njobs; ++k) {
+            const vct_trace_job& t = jobs[c0 + k];
+            BatchJob& B = T.jobs[k];
+            vct_cam_matrix cam;
+            memset(&cam, 0, sizeof(cam));
+            for (int a = 0; a < 3; ++a) cam.eye_pos[a] = t.eye[a];
+            rc = fill_trace_params(B.A.P, &t.desc, &cam, t.shadow.depth ? &t.shadow : nullptr, &t.light,
+                                   &t.light_shadow);
+            if (rc != VCT_OK) return rc;
+            fill_fast_consts(B.A.C, t.desc, B.A.P.diffuse_aperture);
+            B.A.tex = texture_object(t.radiance);
+            B.A.samples = t.samples;
+            B.A.n = t.sample_count;
+            B.A.dout = t.diffuse_out;
+            B.A.sout = t.specular_out;
+            B.A.steps = t.cone_steps;
+            B.base = pos;
+            B.count = (uint32_t)t.sample_count;
+            T.bases[k] = pos;
+            pos += (uint32_t)padded(t.sample_count);
+        }
+        T.bases[T.njobs] = pos;
+        if (pos == 0) continue;
+        const int64_t n = pos;
+        const int g256 = (int)((n + 255) / 256 > 152 * 32 ? 152 * 32 : (n + 255) / 256);
+        k_batch_keys<<<g256, 256, 0, st>>>(T, pos, keys_in, vals_in);
+        VCT_LAUNCH_CHECK();
+        size_t tb = L.temp_bytes;
+        VCT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(b + L.temp, tb, keys_in, keys_out, vals_in, order, (int)n, 0,
+                                                     31 + jb, st));
+        VCT_CUDA_TRY(cudaMemsetAsync(spec_count, 0, sizeof(unsigned int), st));
+        k_batch_spec_keys<<<(g256 > 152 * 16 ? 152 * 16 : g256), 256, 0, st>>>(T, pos, order, spec_key, spec_count);
+        VCT_LAUNCH_CHECK();
+        tb = L.temp_bytes;
+        // stable partition (one radix pass on bit 8): specular positions first, the coherent order kept
+        VCT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(b + L.temp, tb, spec_key, spec_key_out, order, spec_list,
+                                                     (int)n, 8, 9, st));
+        k_batch_diffuse<<<(g256 > 152 * 8 ? 152 * 8 : g256), 256, 0, st>>>(T, pos, order);
+        VCT_LAUNCH_CHECK();
+        const int64_t gw = (n * 32 + 255) / 256;
+        k_batch_specular<<<(int)(gw > 152 * 64 ? 152 * 64 : gw), 256, 0, st>>>(T, spec_list, spec_count);
+        VCT_LAUNCH_CHECK();
+    }
     return VCT_OK;
 }
 
