@@ -451,11 +451,13 @@ typedef struct vct_trace_job {
  * samples share one coherent order in which each job holds a 32-aligned
  * segment, so each warp-sized item of the diffuse kernel and each specular
  * cone names one job, whose record (texture, constants, lighting, outputs)
- * the kernels read from a device job table.  Every job's outputs equal, bit
- * for bit, those of vct_cone_trace_fast on that job alone.  Scratch: caller
- * provided, 256-byte aligned, vct_cone_trace_fast_batch_scratch_bytes bytes
- * (negative: too many samples or jobs: at most 65,536 jobs and 2^31 - 1
- * samples after each job's count is rounded up to a multiple of 32). */
+ * the kernels read from a job table passed as a kernel parameter (constant
+ * memory).  A table holds 64 jobs: longer lists run as consecutive launches
+ * of 64 jobs each on `stream`.  Every job's outputs equal, bit for bit,
+ * those of vct_cone_trace_fast on that job alone.  Scratch: caller provided,
+ * 256-byte aligned, vct_cone_trace_fast_batch_scratch_bytes bytes (negative:
+ * a bad count, or more than 2^31 - 1 samples in one group of 64 jobs after
+ * each job's count is rounded up to a multiple of 32). */
 int64_t vct_cone_trace_fast_batch_scratch_bytes(const vct_trace_job* jobs_host, int32_t job_count);
 int vct_cone_trace_fast_batch(const vct_trace_job* jobs_host, int32_t job_count, void* scratch, size_t scratch_bytes,
                               void* stream);

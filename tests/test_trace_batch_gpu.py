@@ -68,7 +68,7 @@ def test_batched_trace_more_jobs_than_one_table(cuda, oracle):
     """More jobs than one kernel-parameter table holds: the call runs them in chunks, same results."""
     torch = cuda
     from vk_voxel_cone_tracing_gb300 import clipmap
-    spec = [(16, 50 + 7 * k, 8, 0) for k in range(53)]
+    spec = [(16, 50 + 7 * k, 8, 0) for k in range(70)]
     J = _jobs(torch, oracle, spec)
     records, pairs = [], []
     for j in J:

@@ -418,20 +418,27 @@ __global__ void __launch_bounds__(256, 4) k_trace_specular_warp(const __grid_con
 // keys (job, Morton code of the sample, padding last) gives a coherent order
 // in which each job keeps its segment, so every 32-position warp item of the
 // diffuse kernel and every specular cone names one job.  The table travels as
-// a kernel parameter (constant bank, like the single trace's arguments: a
-// record read from global memory cost the specular kernel 1.4 KB of register
-// spills per thread), so it holds up to kBatchJobs jobs per launch.
+// a kernel parameter (constant bank, like the single trace's arguments), so
+// it holds up to kBatchJobs jobs per launch; longer lists run in chunks.
 struct BatchJob {
     FastArgs A;
     uint32_t base, count;
 };
-constexpr int kBatchJobs = 48;
+constexpr int kBatchJobs = 64;
 struct BatchTable {
     int njobs;
     uint32_t bases[kBatchJobs + 1];
     BatchJob jobs[kBatchJobs];
 };
-static_assert(sizeof(BatchTable) < 30000, "the batch table must fit the kernel parameter space");
+// kernel parameters may take 32,764 bytes (CUDA 12.1+, compute capability 7.0+); the kernels add at most 24
+static_assert(sizeof(BatchTable) + 24 <= 32764, "the batch table must fit the kernel parameter space");
+
+// Lane 0's value on every lane.  The batched kernels pass their job index
+// through it: with a job index the compiler cannot prove warp-uniform, the
+// job's texture handle is divergent and every fetch loops over the distinct
+// handles of the warp (1.4 KB of register spills per thread in the specular
+// kernel, and 2.4x its time).
+__device__ __forceinline__ int warp_uniform(int v) { return __shfl_sync(0xffffffffu, v, 0); }
 
 // The job whose segment holds global position g.
 __device__ __forceinline__ int batch_job_of(const BatchTable& T, uint32_t g) {
@@ -480,7 +487,7 @@ __global__ void __launch_bounds__(256) k_batch_diffuse(const __grid_constant__ B
     const int64_t nwarps = (int64_t)gridDim.x * kWarpsPerBlock;
     for (int64_t base = ((int64_t)blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5)) * 32; base < total;
          base += nwarps * 32) {
-        const BatchJob& J = T.jobs[batch_job_of(T, (uint32_t)base)];  // warp-uniform: 32-aligned segments
+        const BatchJob& J = T.jobs[warp_uniform(batch_job_of(T, (uint32_t)base))];  // 32-aligned segments: one job
         const FastArgs& A = J.A;
         DealArgs D{&A.P, A.samples, (int64_t)total, order, J.base, J.count, A.dout, A.sout, A.C.ncones,
                    A.C.need_diffuse != 0, A.C.need_specular != 0};
@@ -497,7 +504,7 @@ __global__ void __launch_bounds__(256, 4) k_batch_specular(const __grid_constant
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < m; c += nwarps) {
         const uint32_t g = __ldg(list + c);
-        const BatchJob& J = T.jobs[batch_job_of(T, g)];
+        const BatchJob& J = T.jobs[warp_uniform(batch_job_of(T, g))];
         unsigned long long steps = 0;
         specular_cone_warp(J.A, g - J.base, steps);
         if (J.A.steps && (threadIdx.x & 31) == 0 && steps) atomicAdd(J.A.steps, steps);
