@@ -9,14 +9,19 @@
 
 #include "../../include/vct_capi.h"
 
-// Device scratch arena of the raster / SVO passes (vct_workspace), and a
+// Device scratch arena of the raster / SVO passes (vct_workspace), a
 // second buffer that outlives a pass within one frame (the frame's
-// touched-texel bitmap).
+// touched-texel bitmap), and a side stream with two events on which a frame
+// runs the opacity passes that are independent of the shadow and injection
+// passes beside them (created on first use, on the device current then).
 struct vct_workspace_s {
     void* ptr = nullptr;
     size_t bytes = 0;
     void* aux = nullptr;
     size_t aux_bytes = 0;
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+    int side_device = -1;
 };
 
 namespace vct {

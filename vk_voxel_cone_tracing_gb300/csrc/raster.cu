@@ -1150,12 +1150,12 @@ static void launch_cover(const RasterArgs& A, const TilePlan& plan, uint2* count
 }
 
 // Injection shading, one thread per covered sample: writes its face records
-// (texel key, traversal position, colour) at the scanned record offset; the
-// records that the fragment shader does not produce get a key that sorts
-// past every texel.
+// (texel key, colour) at the scanned record offset; the records that the
+// fragment shader does not produce (a fragment in shadow produces none) get
+// the invalid key and are dropped before the sort.
 __global__ void __launch_bounds__(256) k_inject_shade(const __grid_constant__ RasterArgs A, const FragDesc* __restrict__ frags,
                                                       uint32_t nfrag, uint32_t* __restrict__ keys,
-                                                      uint32_t* __restrict__ order, float4* __restrict__ rgb) {
+                                                      float4* __restrict__ rgb) {
     for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < nfrag; f += gridDim.x * blockDim.x) {
         const FragDesc d = frags[f];
         const uint32_t rec = __float_as_uint(d.p.w), meta = __float_as_uint(d.n.w);
@@ -1167,8 +1167,7 @@ __global__ void __launch_bounds__(256) k_inject_shade(const __grid_constant__ Ra
         for (uint32_t i = 0; i < per; ++i) {
             const bool v = (int)i < k;
             keys[rec + i] = v ? upd[i].key : A.invalid_key;
-            order[rec + i] = rec + i;
-            rgb[rec + i] = v ? make_float4(upd[i].r, upd[i].g, upd[i].b, 0.0f) : make_float4(0.f, 0.f, 0.f, 0.f);
+            if (v) rgb[rec + i] = make_float4(upd[i].r, upd[i].g, upd[i].b, 0.0f);
         }
     }
 }
@@ -1190,12 +1189,23 @@ __global__ void __launch_bounds__(256) k_svo_shade(const __grid_constant__ Raste
 
 // Boundaries of the texel runs in the sorted record keys over positions
 // [0, n]: every position whose key differs from its predecessor, plus 0 and
-// n, so run h is [heads[h], heads[h + 1]).  The invalid-key run is skipped by
-// the fold.
+// n, so run h is [heads[h], heads[h + 1]).  (The fold would skip a run of
+// invalid keys; the compaction before the sort leaves none.)
 struct RunHead {
     const uint32_t* keys;
     uint32_t n;
     __device__ bool operator()(uint32_t i) const { return i == 0 || i == n || keys[i - 1] != keys[i]; }
+};
+
+// The records the fragment shader produced (stable compaction before the sort).
+struct ValidKey {
+    uint32_t invalid;
+    __device__ bool operator()(uint32_t k) const { return k != invalid; }
+};
+struct ValidRecord {
+    const uint32_t* keys;
+    uint32_t invalid;
+    __device__ bool operator()(uint32_t i) const { return keys[i] != invalid; }
 };
 
 struct SumU2 {
@@ -1472,6 +1482,7 @@ struct InjectState {
     FragDesc* fr = nullptr;
     float4* rgb = nullptr;
     uint32_t *kin = nullptr, *kout = nullptr, *vin = nullptr, *vout = nullptr, *heads = nullptr, *nheads = nullptr;
+    uint32_t* nvalid = nullptr;
     void* stmp = nullptr;
     size_t sort_bytes = 0, select_bytes = 0;
     int key_bits = 0;
@@ -1501,6 +1512,13 @@ static int inject_prepare(RasterArgs& C, RasterArgs& I, vct_workspace_s* ws, cud
     VCT_CUDA_TRY(cub::DeviceSelect::If(nullptr, S->select_bytes, thrust::counting_iterator<uint32_t>(0u),
                                        (uint32_t*)nullptr, (uint32_t*)nullptr, (int64_t)nrec + 1,
                                        RunHead{nullptr, nrec}));
+    size_t sel_keys = 0, sel_recs = 0;
+    VCT_CUDA_TRY(cub::DeviceSelect::If(nullptr, sel_keys, (uint32_t*)nullptr, (uint32_t*)nullptr, (uint32_t*)nullptr,
+                                       (int64_t)nrec, ValidKey{0u}));
+    VCT_CUDA_TRY(cub::DeviceSelect::If(nullptr, sel_recs, thrust::counting_iterator<uint32_t>(0u), (uint32_t*)nullptr,
+                                       (uint32_t*)nullptr, (int64_t)nrec, ValidRecord{nullptr, 0u}));
+    if (sel_keys > S->select_bytes) S->select_bytes = sel_keys;
+    if (sel_recs > S->select_bytes) S->select_bytes = sel_recs;
     const size_t r4 = a256(4 * (size_t)nrec + 4);
     const size_t need = off + a256(sizeof(FragDesc) * (size_t)nfrag) + a256(16 * (size_t)nrec) + 5 * r4 + 256 +
                         a256(S->sort_bytes > S->select_bytes ? S->sort_bytes : S->select_bytes);
@@ -1519,6 +1537,7 @@ static int inject_prepare(RasterArgs& C, RasterArgs& I, vct_workspace_s* ws, cud
     S->vout = (uint32_t*)(p + 3 * r4);
     S->heads = (uint32_t*)(p + 4 * r4);
     S->nheads = (uint32_t*)(p + 5 * r4);
+    S->nvalid = (uint32_t*)(p + 5 * r4 + 128);
     S->stmp = p + 5 * r4 + 256;
     launch_cover<K_INJECT, P_WRITE>(I, S->plan, counts, offs, S->fr, nullptr, st);
     VCT_LAUNCH_CHECK();
@@ -1526,19 +1545,32 @@ static int inject_prepare(RasterArgs& C, RasterArgs& I, vct_workspace_s* ws, cud
 }
 
 // Shade the emitted samples into face records (needs the light and shadow
-// map in `I`), sort them stably by texel and fold every texel's run.
+// map in `I`), keep the records the shader produced (stable compaction: the
+// keys, and their record indices as the sort's values), sort them stably by
+// texel and fold every texel's run.  The count of kept records is read back
+// for the sort (a frame keeps the GPU busy meanwhile with its opacity mips on
+// the side stream).
 static int inject_finish(const RasterArgs& I, const InjectState& S, uint32_t* touched, cudaStream_t st) {
     if (S.nfrag == 0) return VCT_OK;
     const uint32_t nfrag = S.nfrag, nrec = S.nrec;
-    k_inject_shade<<<grid_of(nfrag, 256), 256, 0, st>>>(I, S.fr, nfrag, S.kin, S.vin, S.rgb);
+    k_inject_shade<<<grid_of(nfrag, 256), 256, 0, st>>>(I, S.fr, nfrag, S.kin, S.rgb);
     VCT_LAUNCH_CHECK();
-    size_t tb = S.sort_bytes;
-    VCT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(S.stmp, tb, S.kin, S.kout, S.vin, S.vout, (int)nrec, 0, S.key_bits, st));
+    size_t tb = S.select_bytes;
+    VCT_CUDA_TRY(cub::DeviceSelect::If(S.stmp, tb, S.kin, S.kout, S.nvalid, (int64_t)nrec, ValidKey{I.invalid_key}, st));
+    tb = S.select_bytes;
+    VCT_CUDA_TRY(cub::DeviceSelect::If(S.stmp, tb, thrust::counting_iterator<uint32_t>(0u), S.vout, S.nvalid,
+                                       (int64_t)nrec, ValidRecord{S.kin, I.invalid_key}, st));
+    uint32_t nv = 0;
+    VCT_CUDA_TRY(cudaMemcpyAsync(&nv, S.nvalid, sizeof(nv), cudaMemcpyDeviceToHost, st));
+    VCT_CUDA_TRY(cudaStreamSynchronize(st));
+    if (nv == 0) return VCT_OK;
+    tb = S.sort_bytes;
+    VCT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(S.stmp, tb, S.kout, S.kin, S.vout, S.vin, (int)nv, 0, S.key_bits, st));
     tb = S.select_bytes;
     VCT_CUDA_TRY(cub::DeviceSelect::If(S.stmp, tb, thrust::counting_iterator<uint32_t>(0u), S.heads, S.nheads,
-                                       (int64_t)nrec + 1, RunHead{S.kout, nrec}, st));
-    k_inject_fold<<<grid_of(nrec, 256), 256, 0, st>>>(S.kout, S.vout, S.rgb, S.heads, S.nheads, I.invalid_key, I.atlas,
-                                                      touched);
+                                       (int64_t)nv + 1, RunHead{S.kin, nv}, st));
+    k_inject_fold<<<grid_of(nv, 256), 256, 0, st>>>(S.kin, S.vin, S.rgb, S.heads, S.nheads, I.invalid_key, I.atlas,
+                                                    touched);
     VCT_LAUNCH_CHECK();
     return VCT_OK;
 }
@@ -1598,6 +1630,14 @@ extern "C" int vct_workspace_destroy(vct_workspace_s* w) {
         cudaError_t e2 = cudaFree(w->aux);
         if (e == cudaSuccess) e = e2;
     }
+    if (w->side) {
+        cudaError_t e2 = cudaStreamSynchronize(w->side);
+        if (e == cudaSuccess) e = e2;
+        e2 = cudaStreamDestroy(w->side);
+        if (e == cudaSuccess) e = e2;
+    }
+    if (w->fork) cudaEventDestroy(w->fork);
+    if (w->join) cudaEventDestroy(w->join);
     delete w;
     if (e != cudaSuccess) return cuda_fail(e, "cudaFree (workspace)");
     return VCT_OK;
@@ -2103,6 +2143,43 @@ namespace vct {
 // opacity + count + emit, opacity mips, border, clear of the due radiance
 // levels, then shading, sort and fold.  The results equal the passes run one
 // by one in the reference's order.
+// The workspace's side stream, created on first use on the current device
+// (non-blocking, with its fork and join events); null when the current
+// device is not the one it was created on (the frame then runs serially).
+static cudaStream_t side_stream(vct_workspace_s* ws) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    if (ws->side) return ws->side_device == dev ? ws->side : nullptr;
+    cudaStream_t s = nullptr;
+    cudaEvent_t a = nullptr, b = nullptr;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+    if (cudaEventCreateWithFlags(&a, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b, cudaEventDisableTiming) != cudaSuccess) {
+        if (a) cudaEventDestroy(a);
+        cudaStreamDestroy(s);
+        return nullptr;
+    }
+    ws->side = s;
+    ws->fork = a;
+    ws->join = b;
+    ws->side_device = dev;
+    return s;
+}
+
+// `side` continues after everything enqueued on `st` so far.
+static int fork_side(vct_workspace_s* ws, cudaStream_t side, cudaStream_t st) {
+    VCT_CUDA_TRY(cudaEventRecord(ws->fork, st));
+    VCT_CUDA_TRY(cudaStreamWaitEvent(side, ws->fork, 0));
+    return VCT_OK;
+}
+
+// `st` continues after everything enqueued on `side` so far.
+static int join_side(vct_workspace_s* ws, cudaStream_t side, cudaStream_t st) {
+    VCT_CUDA_TRY(cudaEventRecord(ws->join, side));
+    VCT_CUDA_TRY(cudaStreamWaitEvent(st, ws->join, 0));
+    return VCT_OK;
+}
+
 int frame_raster_passes(const vct_scene* scene, const vct_frame_desc* f, const vct_clipmap_region regions[6],
                         uint32_t due, const vct_clipmap_region* slabs, const int32_t* slab_levels, int nslabs,
                         uint32_t* opacity, uint32_t* radiance, float* shadow_depth, vct_workspace_s* ws,
@@ -2128,8 +2205,15 @@ int frame_raster_passes(const vct_scene* scene, const vct_frame_desc* f, const v
     uint32_t* touched = (uint32_t*)ws->aux;
     VCT_CUDA_TRY(cudaMemsetAsync(touched, 0, bm_bytes, st));
     *touched_out = touched;
-    if (toroidal) rc = clear_slabs(opacity, R, slabs, slab_levels, nslabs, stream);
-    else rc = vct_clear_atlas(opacity, R, stream);
+    // Two stretches run on the side stream, beside the main stream's work that
+    // does not touch the opacity atlas: the opacity clear beside the shadow
+    // pass, and the opacity mips + border wrap beside the injection's shading,
+    // sort and fold.  The results are those of the serial order.
+    cudaStream_t side = side_stream(ws);
+    cudaStream_t ost = side ? side : st;  // the opacity clear's stream
+    if (side && (rc = fork_side(ws, side, st)) != VCT_OK) return rc;
+    if (toroidal) rc = clear_slabs(opacity, R, slabs, slab_levels, nslabs, ost);
+    else rc = vct_clear_atlas(opacity, R, ost);
     if (rc != VCT_OK) return rc;
     vct_shadow_map sm = {nullptr, 0, 0};
     if (f->shadow_width > 0) {
@@ -2141,6 +2225,7 @@ int frame_raster_passes(const vct_scene* scene, const vct_frame_desc* f, const v
         sm.height = f->shadow_height;
     }
     if ((rc = check_scene(scene)) != VCT_OK) return rc;
+    if (side && (rc = join_side(ws, side, st)) != VCT_OK) return rc;
     InjectState S;
     RasterArgs I;
     memset(&I, 0, sizeof(I));
@@ -2167,8 +2252,9 @@ int frame_raster_passes(const vct_scene* scene, const vct_frame_desc* f, const v
         }
         if (rc != VCT_OK) return rc;
     }
+    if (side && (rc = fork_side(ws, side, st)) != VCT_OK) return rc;
     if (!toroidal) {
-        if ((rc = vct_downsample_all(opacity, regions, R, VCT_DOWNSAMPLE_OPACITY, stream)) != VCT_OK) return rc;
+        if ((rc = vct_downsample_all(opacity, regions, R, VCT_DOWNSAMPLE_OPACITY, ost)) != VCT_OK) return rc;
     } else {
         // VoxelizationPass::onEndRenderPass: the mips of the levels that were revoxelised
         for (int l = 1; l < 6; ++l) {
@@ -2178,14 +2264,16 @@ int frame_raster_passes(const vct_scene* scene, const vct_frame_desc* f, const v
             d.clip_level = l;
             d.clipmap_resolution = R;
             d.downsample_region_size = VCT_DOWNSAMPLE_REGION_SIZE;
-            if ((rc = vct_downsample(opacity, &d, VCT_DOWNSAMPLE_OPACITY, stream)) != VCT_OK) return rc;
+            if ((rc = vct_downsample(opacity, &d, VCT_DOWNSAMPLE_OPACITY, ost)) != VCT_OK) return rc;
         }
     }
     vct_border_wrapping_desc bw = {(uint32_t)R, VCT_VOXEL_BORDER, VCT_FACE_COUNT, VCT_CLIP_LEVEL_COUNT};
-    if ((rc = vct_wrap_border(opacity, &bw, stream)) != VCT_OK) return rc;
+    if ((rc = vct_wrap_border(opacity, &bw, ost)) != VCT_OK) return rc;
     // the due radiance levels' clear is folded into the fold (texels start from
     // zero) and the copy-alpha / mip passes (unmarked texels read as zero rgb)
-    if (scene->triangle_count > 0) return inject_finish(I, S, touched, st);
+    if (scene->triangle_count > 0 && (rc = inject_finish(I, S, touched, st)) != VCT_OK) return rc;
+    // the copy-alpha and radiance mip passes that follow read the final opacity
+    if (side && (rc = join_side(ws, side, st)) != VCT_OK) return rc;
     return VCT_OK;
 }
 
