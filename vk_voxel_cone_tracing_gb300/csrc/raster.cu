@@ -477,12 +477,17 @@ __host__ __device__ inline bool clip_sub_triangle(const float4 c[3], int sub, Cl
 }
 
 // Clip-space vertices of item (tri, level) for the pass.
+// KIND is the pass's kind (A.kind) as a template argument, so each kernel
+// holds only its own projection (the G-buffer clipper's local arrays and the
+// other kinds' branches cost the coverage kernels instruction-cache misses
+// and a large stack frame).
+template <int KIND>
 __device__ inline bool item_setup(const RasterArgs& A, const WTri& w, int lvl, RSetup& rs, float3 pos[3]) {
     float4 c[3];
-    if (A.kind == K_SHADOW) {
+    if constexpr (KIND == K_SHADOW) {
 #pragma unroll
         for (int k = 0; k < 3; ++k) c[k] = mat_vec4(A.pv, w.p[k].x, w.p[k].y, w.p[k].z, 1.0f);
-    } else if (A.kind == K_GBUFFER) {  // `lvl` is the sub-triangle of the clipped triangle
+    } else if constexpr (KIND == K_GBUFFER) {  // `lvl` is the sub-triangle of the clipped triangle
         float4 h[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) h[k] = mat_vec4(A.pv, w.p[k].x, w.p[k].y, w.p[k].z, 1.0f);
@@ -493,7 +498,7 @@ __device__ inline bool item_setup(const RasterArgs& A, const WTri& w, int lvl, R
         }
 #pragma unroll
         for (int k = 0; k < 3; ++k) c[k] = make_float4(v[k].x / v[k].w, v[k].y / v[k].w, v[k].z / v[k].w, 1.0f);
-    } else if (A.kind == K_SVO) {
+    } else if constexpr (KIND == K_SVO) {
         float3 q[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
@@ -513,8 +518,8 @@ __device__ inline bool item_setup(const RasterArgs& A, const WTri& w, int lvl, R
         // triangles that cannot reach them, unless the fused pass also counts
         // the level's injection samples
         if ((A.slab_levels >> lvl) & 1u) {
-            const bool counted = A.kind == K_OPA_COUNT && ((A.count_levels >> lvl) & 1u);
-            if ((A.kind == K_OPACITY || A.kind == K_OPA_COUNT) && !counted && !tri_meets_slabs(A, lvl, w.p)) {
+            const bool counted = KIND == K_OPA_COUNT && ((A.count_levels >> lvl) & 1u);
+            if ((KIND == K_OPACITY || KIND == K_OPA_COUNT) && !counted && !tri_meets_slabs(A, lvl, w.p)) {
                 rs.ok = false;
                 return false;
             }
@@ -707,6 +712,7 @@ __global__ void k_tile_items(const uint32_t* __restrict__ tile_end, int64_t item
     }
 }
 
+template <int KIND>
 __global__ void k_item_tiles(const __grid_constant__ RasterArgs A, uint32_t* __restrict__ tiles) {
     for (int64_t item = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; item < A.items;
          item += (int64_t)gridDim.x * blockDim.x) {
@@ -716,7 +722,7 @@ __global__ void k_item_tiles(const __grid_constant__ RasterArgs A, uint32_t* __r
         WTri w = world_triangle(A.s, tri);
         RSetup rs;
         float3 pos[3];
-        tiles[item] = item_setup(A, w, lvl, rs, pos) ? tiles_of(rs) : 0u;
+        tiles[item] = item_setup<KIND>(A, w, lvl, rs, pos) ? tiles_of(rs) : 0u;
     }
 }
 
@@ -949,7 +955,7 @@ __global__ void __launch_bounds__(128, 6) k_cover(const __grid_constant__ Raster
             const WTri w = world_triangle(A.s, tri);
             RSetup rs;
             float3 pos[3];
-            bool live = item_setup(A, w, lvl, rs, pos);
+            bool live = item_setup<KIND>(A, w, lvl, rs, pos);
             const uint32_t mi = min(w.material, (uint32_t)max(A.s.material_count - 1, 0));
             uint32_t per = 1u;
             if (KIND == K_GBUFFER) live = live && !gbuffer_discarded(A, material_of(A.s, mi));
@@ -1409,7 +1415,15 @@ static int plan_tiles(RasterArgs& A, vct_workspace_s* ws, size_t& off, TilePlan*
     uint32_t* tile_end = (uint32_t*)(base + a256(4 * n));
     void* tmp = base + 2 * a256(4 * n);
     off = 2 * a256(4 * n) + a256(scan_bytes);
-    k_item_tiles<<<grid_of(n, 128), 128, 0, st>>>(A, counts);
+    switch (A.kind) {
+        case K_OPACITY: k_item_tiles<K_OPACITY><<<grid_of(n, 128), 128, 0, st>>>(A, counts); break;
+        case K_INJECT: k_item_tiles<K_INJECT><<<grid_of(n, 128), 128, 0, st>>>(A, counts); break;
+        case K_SHADOW: k_item_tiles<K_SHADOW><<<grid_of(n, 128), 128, 0, st>>>(A, counts); break;
+        case K_SVO: k_item_tiles<K_SVO><<<grid_of(n, 128), 128, 0, st>>>(A, counts); break;
+        case K_OPA_COUNT: k_item_tiles<K_OPA_COUNT><<<grid_of(n, 128), 128, 0, st>>>(A, counts); break;
+        case K_GBUFFER: k_item_tiles<K_GBUFFER><<<grid_of(n, 128), 128, 0, st>>>(A, counts); break;
+        default: return fail(VCT_E_BAD_ARG, "rasteriser: unknown pass kind");
+    }
     VCT_LAUNCH_CHECK();
     VCT_CUDA_TRY(cub::DeviceScan::InclusiveSum(tmp, scan_bytes, counts, tile_end, (int)n, st));
     uint32_t total = 0;
