@@ -916,6 +916,36 @@ __device__ inline uint32_t cover_pixel(const TileRegs& t, const TileSlot& T, int
     return mask;
 }
 
+// The covered samples of a warp's 32 pixels (lane i's pixel has coverage
+// mask `mask`), dealt one per lane in (pixel, sample) order, 32 per round:
+// fn(valid, o, s, r) runs on every lane (valid false on the lanes past the
+// last sample) for the r-th covered sample s of lane o's pixel.  Every lane
+// does the same per-sample work whatever its own pixel's coverage; fn may
+// shuffle (all lanes call it together).
+template <class Fn>
+__device__ __forceinline__ void for_each_covered(uint32_t mask, int lane, Fn&& fn) {
+    constexpr unsigned FULL = 0xffffffffu;
+    const uint32_t c = __popc(mask);
+    uint32_t incl = c;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t v = __shfl_up_sync(FULL, incl, d);
+        if (lane >= d) incl += v;
+    }
+    const uint32_t total = __shfl_sync(FULL, incl, 31), excl = incl - c;
+    for (uint32_t k0 = 0; k0 < total; k0 += 32u) {
+        const uint32_t k = k0 + (uint32_t)lane;
+        int o = 0;  // the first lane whose inclusive count exceeds k
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1)
+            if (__shfl_sync(FULL, incl, o + step - 1) <= k) o += step;
+        o = min(o, 31);
+        const uint32_t mo = __shfl_sync(FULL, mask, o), r = k - __shfl_sync(FULL, excl, o);
+        const bool valid = k < total;
+        fn(valid, o, valid ? (int)__fns(mo, 0u, (int)r + 1) : 0, r);
+    }
+}
+
 // Coverage kernels.  A warp takes 32 consecutive 8x8 tiles of (triangle,
 // level) items -- one per lane -- sets each up once into shared memory, then
 // flattens the (tile, pixel) pairs of all 32 tiles and walks them 32 at a
@@ -935,6 +965,8 @@ __global__ void __launch_bounds__(128, 6) k_cover(const __grid_constant__ Raster
                                                FragDesc* __restrict__ frags, int* __restrict__ err) {
     constexpr int NS = (KIND == K_SHADOW || KIND == K_GBUFFER) ? 1 : 8;
     constexpr bool RANKED = PHASE != P_DIRECT;
+    // the opacity writes run over the round's covered samples dealt to the lanes
+    constexpr bool FLAT_OPACITY = (KIND == K_OPACITY || KIND == K_OPA_COUNT) && PHASE != P_WRITE;
     constexpr unsigned FULL = 0xffffffffu;
     __shared__ TileSlot slots[4][32];
     const int lane = threadIdx.x & 31;
@@ -1071,10 +1103,9 @@ __global__ void __launch_bounds__(128, 6) k_cover(const __grid_constant__ Raster
                 px = S[j].tx + (ox0 >> 8);
                 py = S[j].ty + (oy0 >> 8);
                 mask = cover_pixel<NS>(t, S[j], ox0, oy0);
-                if ((PHASE == P_DIRECT || KIND == K_OPA_COUNT) && mask) {
+                if (!FLAT_OPACITY && PHASE == P_DIRECT && mask) {
                     const TileSlot& T = S[j];
                     const int lvl = (int)(T.meta & 7u);
-                    int3 last_ic = make_int3(-1, -1, -1);  // opacity: the previous sample's voxel (stores are idempotent)
                     for (uint32_t m = mask; m; m &= m - 1u) {
                         const int s = __ffs(m) - 1;
                         float b[3], z;
@@ -1082,19 +1113,6 @@ __global__ void __launch_bounds__(128, 6) k_cover(const __grid_constant__ Raster
                                   oy0 + (NS == 1 ? 128 : c_sample_loc8[s][1]), b, z);
                         if (KIND == K_SHADOW) {
                             atomicMin(reinterpret_cast<unsigned int*>(A.depth) + (int64_t)py * A.W + px, __float_as_uint(z));
-                        } else if (KIND == K_OPACITY || KIND == K_OPA_COUNT) {
-                            const vct_voxelization_desc& d = A.vd[lvl];
-                            const float3 wp = interp3(b, T.p);
-                            if (wp.x < d.region_min_corner[0] || wp.y < d.region_min_corner[1] ||
-                                wp.z < d.region_min_corner[2] || wp.x > d.region_max_corner[0] ||
-                                wp.y > d.region_max_corner[1] || wp.z > d.region_max_corner[2])
-                                continue;
-                            if (((A.slab_levels >> lvl) & 1u) && !in_slabs(A, lvl, wp)) continue;
-                            const AtlasDims AD(A.R);
-                            const int3 ic = clip_image_coords(d, wp);
-                            if (ic.x == last_ic.x && ic.y == last_ic.y && ic.z == last_ic.z) continue;
-                            last_ic = ic;
-                            for (int f = 0; f < 6; ++f) A.atlas[AD.index(ic.x + (A.R + 2) * f, ic.y, ic.z)] = 0xFFFFFFFFu;
                         } else if (KIND == K_INJECT) {
                             const vct_gltf_shade_material mat = material_of(A.s, T.meta >> 3);
                             InjRecord upd[6];
@@ -1104,6 +1122,40 @@ __global__ void __launch_bounds__(128, 6) k_cover(const __grid_constant__ Raster
                         }
                     }
                 }
+            }
+            if constexpr (FLAT_OPACITY) {
+                // opacity: every covered sample inside its level's region (and
+                // slabs) marks its voxel on all six faces; a sample in the same
+                // voxel as the previous one of its pixel skips the (idempotent) stores
+                for_each_covered(mask, lane, [&](bool valid, int o, int s, uint32_t) {
+                    const int jo = __shfl_sync(FULL, j, o), oxo = __shfl_sync(FULL, ox0, o),
+                              oyo = __shfl_sync(FULL, oy0, o);
+                    int3 ic = make_int3(-1, -1, -1);
+                    bool keep = false;
+                    if (valid) {
+                        const TileSlot& T = S[jo];
+                        const int lvl = (int)(T.meta & 7u);
+                        float b[3], z;
+                        sample_bz(T.t, T, oxo + c_sample_loc8[s][0], oyo + c_sample_loc8[s][1], b, z);
+                        const vct_voxelization_desc& d = A.vd[lvl];
+                        const float3 wp = interp3(b, T.p);
+                        const bool inside = !(wp.x < d.region_min_corner[0] || wp.y < d.region_min_corner[1] ||
+                                              wp.z < d.region_min_corner[2] || wp.x > d.region_max_corner[0] ||
+                                              wp.y > d.region_max_corner[1] || wp.z > d.region_max_corner[2]) &&
+                                            !(((A.slab_levels >> lvl) & 1u) && !in_slabs(A, lvl, wp));
+                        if (inside) {
+                            ic = clip_image_coords(d, wp);
+                            keep = true;
+                        }
+                    }
+                    const int po = __shfl_up_sync(FULL, keep ? o : -1, 1), qx = __shfl_up_sync(FULL, ic.x, 1),
+                              qy = __shfl_up_sync(FULL, ic.y, 1), qz = __shfl_up_sync(FULL, ic.z, 1);
+                    const bool dup = lane > 0 && po == o && qx == ic.x && qy == ic.y && qz == ic.z;
+                    if (keep && !dup) {
+                        const AtlasDims AD(A.R);
+                        for (int f = 0; f < 6; ++f) A.atlas[AD.index(ic.x + (A.R + 2) * f, ic.y, ic.z)] = 0xFFFFFFFFu;
+                    }
+                });
             }
             if (RANKED) {
                 if (KIND == K_OPA_COUNT && act && !((A.count_levels >> (S[j].meta & 7u)) & 1u)) mask = 0u;
@@ -1122,21 +1174,24 @@ __global__ void __launch_bounds__(128, 6) k_cover(const __grid_constant__ Raster
                 __syncwarp();
                 if (last) S[j].done += ci - cx_first;
                 __syncwarp();
-                if (PHASE == P_WRITE && mask) {
-                    const TileSlot& T = S[j];
-                    uint32_t k = rank;
-                    for (uint32_t m = mask; m; m &= m - 1u) {
-                        const int s = __ffs(m) - 1;
-                        float b[3], z;
-                        sample_bz(t, T, ox0 + c_sample_loc8[s][0], oy0 + c_sample_loc8[s][1], b, z);
-                        const float3 p = interp3(b, T.p);
-                        const float3 nn = interp3(b, T.n);
-                        FragDesc d;
-                        d.p = make_float4(p.x, p.y, p.z, __uint_as_float(T.base_r + k * T.per));
-                        d.n = make_float4(nn.x, nn.y, nn.z, __uint_as_float(T.meta));
-                        frags[T.base_f + k] = d;
-                        ++k;
-                    }
+                if constexpr (PHASE == P_WRITE) {
+                    // the r-th covered sample of a pixel goes to its tile's slot rank + r
+                    for_each_covered(mask, lane, [&](bool valid, int o, int s, uint32_t r) {
+                        const int jo = __shfl_sync(FULL, j, o), oxo = __shfl_sync(FULL, ox0, o),
+                                  oyo = __shfl_sync(FULL, oy0, o);
+                        const uint32_t k = __shfl_sync(FULL, rank, o) + r;
+                        if (valid) {
+                            const TileSlot& T = S[jo];
+                            float b[3], z;
+                            sample_bz(T.t, T, oxo + c_sample_loc8[s][0], oyo + c_sample_loc8[s][1], b, z);
+                            const float3 p = interp3(b, T.p);
+                            const float3 nn = interp3(b, T.n);
+                            FragDesc d;
+                            d.p = make_float4(p.x, p.y, p.z, __uint_as_float(T.base_r + k * T.per));
+                            d.n = make_float4(nn.x, nn.y, nn.z, __uint_as_float(T.meta));
+                            frags[T.base_f + k] = d;
+                        }
+                    });
                 }
             }
         }
