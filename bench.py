@@ -326,6 +326,8 @@ def run_ours(args, world, rank, local):
     svo()
     svo_per, _ = events_ms(stream, svo, max(3, args.steps))
     frame_ms = statistics.median(frame_per)
+    opacity_r8 = frame_r8_opacity(dev, stream, ds, R, shadow, light, lsd, ws, radiance, frame_tex, args.steps) \
+        if args.form == "tex" else None
     # the conservative voxelisation mode over the same levels (into the opacity atlas; the frame after the
     # moving-camera runs below restores it)
     cons = lambda: passes.voxelize_opacity_conservative(ds, regs, R, opacity)
@@ -507,7 +509,8 @@ def run_ours(args, world, rank, local):
                        "texture": "kept current by the frame's copy-alpha and mip passes" if frame_tex is not None
                        else ("kept current by the frame's FP16 conversion and FP16 mip passes" if tex is not None
                              else "none (linear atlas)"),
-                       "voxelize_inject_mip_ms": frame_ms, "svo_ms": svo_ms, "svo_level": SVO_LEVEL,
+                       "voxelize_inject_mip_ms": frame_ms, "frame_r8_opacity": opacity_r8,
+                       "svo_ms": svo_ms, "svo_level": SVO_LEVEL,
                        "conservative_voxelize": {"ms": cons_ms, "voxels": cons_voxels,
                                                  "note": "triangle/box overlap mode (Schwarz & Seidel 2010), "
                                                          "6 levels of 256^3; voxels marked over all levels"},
@@ -562,6 +565,36 @@ def run_ours(args, world, rank, local):
         tex.close()
     if world > 1:
         dist.destroy_process_group()
+
+
+def frame_r8_opacity(dev, stream, ds, R, shadow, light, lsd, ws, radiance, tex, steps):
+    """The same frame with the one-byte opacity atlas (vct_frame_desc.opacity_format = R8): CUDA events,
+    median; its radiance atlas is compared bit for bit with the RGBA8 frame's (`radiance`, current)."""
+    import torch
+    from vk_voxel_cone_tracing_gb300 import capi, clipmap, passes
+    ref = radiance.clone()
+    op8, rad8 = clipmap.new_atlas_r8(R, dev), clipmap.new_atlas(R, dev)
+    tex8 = clipmap.RadianceTexture(R)
+
+    def frame8():
+        passes.clipmap_frame(ds, CAMERA, R, op8, rad8, shadow, light, lsd, ws, texture=tex8 if tex is not None else None,
+                             opacity_format=capi.OPACITY_R8)
+
+    for _ in range(2):
+        frame8()
+    per, _ = events_ms(stream, frame8, max(3, steps))
+    torch.cuda.synchronize()
+    equal = bool(torch.equal(rad8, ref))
+    tex8.close()
+    del op8, rad8, ref
+    return {"frame_ms": statistics.median(per), "radiance_bit_equal": equal,
+            "opacity_bytes": int(atlas_bytes(R) // 4),
+            "note": "opacity stored one byte per texel (alpha only): a quarter of the RGBA8 opacity atlas's clear, "
+                    "voxelisation, mip, border and copy-alpha traffic; radiance atlas and texture unchanged"}
+
+
+def atlas_bytes(R: int) -> int:
+    return 4 * (R + 2) * 36 * (R + 2) * (R + 2)
 
 
 def other_forms(dev, stream, R, regs, desc, radiance, samples, light, shadow, lsd, reps):

@@ -787,7 +787,9 @@ typedef struct vct_frame_desc {
                                                receives every radiance texel the frame's copy-alpha and
                                                mip passes write (the texture the fast trace samples) */
     int32_t revoxelization;                 /* VCT_REVOX_FULL (the reference as shipped) or VCT_REVOX_TOROIDAL */
-    int32_t reserved;
+    int32_t opacity_format;                 /* VCT_OPACITY_RGBA8 (the reference's atlas, 4 bytes per texel) or
+                                               VCT_OPACITY_R8 (1 byte per texel, alpha only; FULL revoxelisation
+                                               with the deterministic injection) */
     vct_clipmap_region* regions_state;      /* host, 6 regions: FULL writes the frame's regions here (may be
                                                NULL); TOROIDAL reads the previous frame's regions, moves them
                                                (vct_update_clip_regions) and writes them back (required) */
@@ -802,6 +804,16 @@ typedef struct vct_frame_desc {
  * hold the previous frame's voxels of `regions_state`. */
 #define VCT_REVOX_FULL 0
 #define VCT_REVOX_TOROIDAL 1
+
+/* Opacity atlas storage of a frame.  RGBA8: the reference's image
+ * (Voxelizer.cpp:159), uint32 texels.  R8: the same texel order at one byte
+ * per texel holding the alpha that copy-alpha, the mips and the border wrap
+ * read (the RGBA8 atlas's alpha bytes, bit for bit), a quarter of the clear,
+ * voxelisation, mip and copy-alpha traffic; the radiance atlas and texture
+ * are unchanged.  The `opacity` argument of vct_clipmap_frame then points at
+ * those bytes. */
+#define VCT_OPACITY_RGBA8 0
+#define VCT_OPACITY_R8 1
 
 /* Application::run's pre-pass sequence (VFS/Application.cpp:142-201):
  * VoxelizationPass (clear, voxelise all levels, opacity mips, border wrap),

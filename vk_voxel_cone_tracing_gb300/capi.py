@@ -38,6 +38,8 @@ INJECT_ATOMIC = 1
 
 REVOX_FULL = 0
 REVOX_TOROIDAL = 1
+OPACITY_RGBA8 = 0
+OPACITY_R8 = 1
 
 SVO_DETERMINISTIC = 0
 SVO_ATOMIC = 1
@@ -142,7 +144,7 @@ class FrameDesc(C.Structure):
     _fields_ = [("camera_pos", f3), ("clipmap_resolution", C.c_int32), ("frame_index", C.c_int32),
                 ("inject_mode", C.c_int32), ("shadow_width", C.c_int32), ("shadow_height", C.c_int32),
                 ("light", DirectionalLightDesc), ("light_shadow", DirectionalLightShadowDesc),
-                ("radiance_texture", C.c_void_p), ("revoxelization", C.c_int32), ("reserved", C.c_int32),
+                ("radiance_texture", C.c_void_p), ("revoxelization", C.c_int32), ("opacity_format", C.c_int32),
                 ("regions_state", C.c_void_p)]
 
 

@@ -37,6 +37,12 @@ def new_atlas(R: int, device="cuda") -> torch.Tensor:
     return torch.zeros(atlas_shape(R), dtype=torch.int32, device=device)
 
 
+def new_atlas_r8(R: int, device="cuda") -> torch.Tensor:
+    """A zeroed one-byte-per-texel opacity atlas (vct_frame_desc.opacity_format = OPACITY_R8), [D, H, W]."""
+    D, H, W = R + 2, 6 * (R + 2), 6 * (R + 2)
+    return torch.zeros((D, H, W), dtype=torch.uint8, device=device)
+
+
 def clip_regions(camera_pos, R: int, extent_l0: int = capi.VOXEL_EXTENT_L0):
     regs = (capi.ClipmapRegion * 6)()
     cam = (C.c_float * 3)(*[float(x) for x in camera_pos])

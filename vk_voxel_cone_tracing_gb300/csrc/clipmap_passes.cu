@@ -60,7 +60,18 @@ __device__ __forceinline__ void cube_texel(uint32_t t, int lg, int& x, int& y, i
     z = (int)(t >> (2 * lg));
 }
 
-__global__ void k_copy_alpha(uint32_t* __restrict__ dst, const uint32_t* __restrict__ src, AtlasDims A, int level,
+// The alpha byte of opacity texel i in the alpha position of an RGBA8 word:
+// the reference's RGBA8 opacity atlas (OT = uint32_t) or the one-byte-per-
+// texel form (OT = uint8_t, the same texel order), which holds the alpha only.
+__device__ __forceinline__ uint32_t opa_alpha(const uint32_t* __restrict__ opa, int64_t i) {
+    return __ldg(opa + i) & 0xff000000u;
+}
+__device__ __forceinline__ uint32_t opa_alpha(const uint8_t* __restrict__ opa, int64_t i) {
+    return (uint32_t)__ldg(opa + i) << 24;
+}
+
+template <class OT>
+__global__ void k_copy_alpha(uint32_t* __restrict__ dst, const OT* __restrict__ src, AtlasDims A, int level,
                              int lg, cudaSurfaceObject_t mirror, const uint32_t* __restrict__ touched) {
     const int f = blockIdx.y;
     const uint32_t n = 1u << (3 * lg);
@@ -71,7 +82,7 @@ __global__ void k_copy_alpha(uint32_t* __restrict__ dst, const uint32_t* __restr
         y += 1 + level * A.rb;
         z += 1;
         const int64_t i = A.index(x, y, z);
-        const uint32_t v = rgb_of(dst, touched, i) | (__ldg(src + i) & 0xff000000u);
+        const uint32_t v = rgb_of(dst, touched, i) | opa_alpha(src, i);
         dst[i] = v;
         if (mirror) surf3Dwrite(v, mirror, x * 4, y, z);
     }
@@ -85,7 +96,8 @@ __global__ void k_copy_alpha(uint32_t* __restrict__ dst, const uint32_t* __restr
 // reached.  One thread per (level, face, position of [0,R)^3 with a zero
 // coordinate): the z = 0 plane, then the y = 0 rows, then the x = 0 column,
 // x fastest where it varies.  Sources are interior texels, never written here.
-__global__ void k_wrap_border(uint32_t* __restrict__ atlas, AtlasDims A, int faces, int regions) {
+template <class T>
+__global__ void k_wrap_border(T* __restrict__ atlas, AtlasDims A, int faces, int regions) {
     // R <= 1024: (3R^2 - 3R + 1) * 36 < 2^27
     const uint32_t R = (uint32_t)A.R, lg = 31u - __clz(A.R);
     const uint32_t zf = R * R, yr = R * (R - 1u), shell = zf + yr + (R - 1u) * (R - 1u);
@@ -207,6 +219,69 @@ __global__ void k_downsample(uint32_t* __restrict__ atlas, AtlasDims A, int3 pmi
     }
 }
 
+// opacityDownSample.comp on the one-byte opacity form.  The RGBA8 pass reads
+// the children's alpha and the target's red byte (the level's own voxelised
+// value), and writes the result into green and alpha, keeping red.  Within a
+// full revoxelisation a target's red byte is read only by this pass, before
+// the store, and every other reader of the opacity atlas (the next level's
+// pass, the border wrap, copy-alpha) reads alpha; outside the target block
+// red == alpha (the voxeliser writes all four bytes).  So one byte per texel
+// -- the voxelised value until this pass stores the alpha over it -- gives
+// every reader the byte it reads from the RGBA8 atlas.  (The toroidal update
+// re-reads red of texels voxelised in earlier frames, so it keeps RGBA8.)
+__global__ void k_downsample_r8(uint8_t* __restrict__ atlas, AtlasDims A, int3 pmin, int level, int band, int lgh) {
+    const int half = A.R >> 1;
+    const uint32_t n = 1u << (3 * lgh), m = (1u << lgh) - 1u;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int gx = (int)(t & m);
+        const int gy = (int)((t >> lgh) & m);
+        const int gz = (int)(t >> (2 * lgh));
+        const int cur[3] = {(pmin.x >> 1) + gx, (pmin.y >> 1) + gy, (pmin.z >> 1) + gz};
+        const int pm[3] = {pmin.x, pmin.y, pmin.z};
+        int wpos[3], ps[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            wpos[a] = ds_wrap(cur[a], A.R) + 1;
+            ps[a] = ds_wrap(cur[a] << 1, A.R) + 1;
+        }
+        wpos[1] += A.rb * level;
+        ps[1] += A.rb * (level - 1);
+        float dist[3];
+        bool any_ge = false;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            float center = __fadd_rn((float)(pm[a] >> 1), (float)(half >> 1));
+            dist[a] = __fsub_rn(fabsf(__fsub_rn(__fadd_rn((float)cur[a], 0.5f), center)), 0.5f);
+            any_ge |= dist[a] >= (float)((half >> 1) - band);
+        }
+        float lerp = 0.0f;
+        const float inv = 1.0f / __fadd_rn((float)band, 1.0f);
+        if (any_ge) {
+            lerp = __fadd_rn(__fsub_rn(fmaxf(dist[0], fmaxf(dist[1], dist[2])), (float)((half >> 1) - band)), 1.0f);
+            lerp = __fmul_rn(lerp, inv);
+        }
+        for (int f = 0; f < 6; ++f) {
+            uint32_t raw[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+                raw[i] = (uint32_t)atlas[A.index(ps[0] + (i & 1) + A.rb * f, ps[1] + ((i >> 1) & 1), ps[2] + ((i >> 2) & 1))]
+                         << 24;
+            const int64_t wi = A.index(wpos[0] + A.rb * f, wpos[1], wpos[2]);
+            float s = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float a0 = unorm8_load(raw[c_pairs[f][k][0]], 3);
+                const float a1 = unorm8_load(raw[c_pairs[f][k][1]], 3);
+                const float tt = __fmul_rn(__fsub_rn(1.0f, a0), a1);
+                s = (k == 0) ? __fadd_rn(a0, tt) : __fadd_rn(__fadd_rn(s, a0), tt);
+            }
+            const float res = __fmul_rn(s, 0.25f);
+            const float own_r = unorm8_load((uint32_t)atlas[wi], 0);
+            atlas[wi] = (uint8_t)unorm8_store(mix_rn(res, own_r, lerp));
+        }
+    }
+}
+
 // copyAlphaImage.comp then radianceDownSample.comp for one level l >= 1 in
 // one launch, same result as the two passes in sequence.  Two grid-stride
 // loops: (a) copy-alpha of the level's R^3 interior texels outside the
@@ -218,8 +293,9 @@ __global__ void k_downsample(uint32_t* __restrict__ atlas, AtlasDims A, int3 pmi
 // of work (one loop over the mixed texels was 3 % slower per frame at
 // R = 256).  The target block depends only on level l - 1, which earlier
 // launches finished.  All six faces per thread.
+template <class OT>
 __global__ void __launch_bounds__(128, 8) k_alpha_downsample(uint32_t* __restrict__ rad,
-                                                                    const uint32_t* __restrict__ opa, AtlasDims A,
+                                                                    const OT* __restrict__ opa, AtlasDims A,
                                                                     int3 pmin, int level, int band, int lg,
                                                                     cudaSurfaceObject_t mirror,
                                                                     const uint32_t* __restrict__ touched) {
@@ -239,7 +315,7 @@ __global__ void __launch_bounds__(128, 8) k_alpha_downsample(uint32_t* __restric
         uint32_t own6[6];
 #pragma unroll
         for (int f = 0; f < 6; ++f)
-            own6[f] = rgb_of(rad, touched, w0 + A.rb * f) | (__ldg(opa + w0 + A.rb * f) & 0xff000000u);
+            own6[f] = rgb_of(rad, touched, w0 + A.rb * f) | opa_alpha(opa, w0 + A.rb * f);
         const int my = w[1] + 1 + A.rb * level, mz = w[2] + 1;
 #pragma unroll
         for (int f = 0; f < 6; ++f) {
@@ -279,7 +355,7 @@ __global__ void __launch_bounds__(128, 8) k_alpha_downsample(uint32_t* __restric
         uint32_t own6[6];
 #pragma unroll
         for (int f = 0; f < 6; ++f)
-            own6[f] = rgb_of(rad, touched, w0 + A.rb * f) | (__ldg(opa + w0 + A.rb * f) & 0xff000000u);
+            own6[f] = rgb_of(rad, touched, w0 + A.rb * f) | opa_alpha(opa, w0 + A.rb * f);
 #pragma unroll 1
         for (int f = 0; f < 6; ++f) {
             uint32_t raw[8];
@@ -344,8 +420,8 @@ extern "C" int vct_clear_region(uint32_t* atlas, const vct_image_cleaning_desc* 
 
 namespace vct {
 
-int copy_alpha_pass(uint32_t* dst, const uint32_t* src, const vct_copy_alpha_desc* d, cudaSurfaceObject_t mirror,
-                    const uint32_t* touched, cudaStream_t st) {
+int copy_alpha_pass(uint32_t* dst, const void* src, const vct_copy_alpha_desc* d, cudaSurfaceObject_t mirror,
+                    const uint32_t* touched, cudaStream_t st, bool src_r8) {
     VCT_CHECK_ARG(dst && src && d, "vct_copy_alpha: null argument");
     VCT_CHECK_ARG(valid_resolution(d->clipmap_resolution), "vct_copy_alpha: resolution must be a power of two in [8,1024]");
     VCT_CHECK_ARG(d->clip_level >= 0 && d->clip_level < VCT_CLIP_LEVEL_COUNT, "vct_copy_alpha: clip level out of range");
@@ -356,15 +432,19 @@ int copy_alpha_pass(uint32_t* dst, const uint32_t* src, const vct_copy_alpha_des
     const int lg = 31 - __builtin_clz((unsigned)A.R);
     const int64_t n = (int64_t)A.R * A.R * A.R;
     dim3 grid((unsigned)grid_for(n, 256), (unsigned)d->face_count);
-    k_copy_alpha<<<grid, 256, 0, st>>>(dst, src, A, d->clip_level, lg, mirror, touched);
+    if (src_r8)
+        k_copy_alpha<<<grid, 256, 0, st>>>(dst, static_cast<const uint8_t*>(src), A, d->clip_level, lg, mirror, touched);
+    else
+        k_copy_alpha<<<grid, 256, 0, st>>>(dst, static_cast<const uint32_t*>(src), A, d->clip_level, lg, mirror,
+                                           touched);
     VCT_LAUNCH_CHECK();
     return VCT_OK;
 }
 
-int copy_alpha_downsample_pass(uint32_t* radiance, const uint32_t* opacity, const vct_downsample_desc* d,
-                               cudaSurfaceObject_t mirror, const uint32_t* touched, cudaStream_t st) {
+int copy_alpha_downsample_pass(uint32_t* radiance, const void* opacity, const vct_downsample_desc* d,
+                               cudaSurfaceObject_t mirror, const uint32_t* touched, cudaStream_t st, bool opa_r8) {
     VCT_CHECK_ARG(radiance && opacity && d, "vct_copy_alpha_downsample: null argument");
-    VCT_CHECK_ARG(radiance != opacity, "vct_copy_alpha_downsample: radiance and opacity atlases must differ");
+    VCT_CHECK_ARG((const void*)radiance != opacity, "vct_copy_alpha_downsample: radiance and opacity atlases must differ");
     VCT_CHECK_ARG(valid_resolution(d->clipmap_resolution),
                   "vct_copy_alpha_downsample: resolution must be a power of two in [8,1024]");
     VCT_CHECK_ARG(d->clip_level >= 1 && d->clip_level < VCT_CLIP_LEVEL_COUNT,
@@ -375,8 +455,38 @@ int copy_alpha_downsample_pass(uint32_t* radiance, const uint32_t* opacity, cons
     const int64_t n = (int64_t)A.R * A.R * A.R;
     int3 pm = make_int3(d->prev_region_min_corner[0], d->prev_region_min_corner[1], d->prev_region_min_corner[2]);
     const int lg = 31 - __builtin_clz((unsigned)A.R);
-    k_alpha_downsample<<<grid_for(n, 128), 128, 0, st>>>(radiance, opacity, A, pm, d->clip_level,
-                                                        d->downsample_region_size, lg, mirror, touched);
+    if (opa_r8)
+        k_alpha_downsample<<<grid_for(n, 128), 128, 0, st>>>(radiance, static_cast<const uint8_t*>(opacity), A, pm,
+                                                            d->clip_level, d->downsample_region_size, lg, mirror,
+                                                            touched);
+    else
+        k_alpha_downsample<<<grid_for(n, 128), 128, 0, st>>>(radiance, static_cast<const uint32_t*>(opacity), A, pm,
+                                                            d->clip_level, d->downsample_region_size, lg, mirror,
+                                                            touched);
+    VCT_LAUNCH_CHECK();
+    return VCT_OK;
+}
+
+// The one-byte opacity form's mips 1..5 and border wrap (VoxelizationPass's
+// end-of-pass dispatches on that form).
+int opacity_r8_mips(uint8_t* atlas, const vct_clipmap_region regions[6], int R, cudaStream_t st) {
+    AtlasDims A(R);
+    const int half = A.R >> 1;
+    const int64_t n = (int64_t)half * half * half;
+    const int lgh = 31 - __builtin_clz((unsigned)half);
+    for (int l = 1; l < VCT_CLIP_LEVEL_COUNT; ++l) {
+        const int3 pm = make_int3(regions[l - 1].min_corner[0], regions[l - 1].min_corner[1], regions[l - 1].min_corner[2]);
+        k_downsample_r8<<<grid_for(n, 128), 128, 0, st>>>(atlas, A, pm, l, VCT_DOWNSAMPLE_REGION_SIZE, lgh);
+        VCT_LAUNCH_CHECK();
+    }
+    return VCT_OK;
+}
+
+int wrap_border_r8(uint8_t* atlas, int R, cudaStream_t st) {
+    AtlasDims A(R);
+    const int64_t shell = 3 * (int64_t)A.R * A.R - 3 * (int64_t)A.R + 1;
+    const int64_t total = shell * VCT_FACE_COUNT * VCT_CLIP_LEVEL_COUNT;
+    k_wrap_border<<<grid_for(total, 256), 256, 0, st>>>(atlas, A, VCT_FACE_COUNT, VCT_CLIP_LEVEL_COUNT);
     VCT_LAUNCH_CHECK();
     return VCT_OK;
 }
@@ -394,7 +504,7 @@ static int mirror_surface(vct_texture_s* t, int R, const char* who, cudaSurfaceO
 }  // namespace vct
 
 extern "C" int vct_copy_alpha(uint32_t* dst, const uint32_t* src, const vct_copy_alpha_desc* d, void* stream) {
-    return copy_alpha_pass(dst, src, d, 0, nullptr, as_stream(stream));
+    return copy_alpha_pass(dst, src, d, 0, nullptr, as_stream(stream), false);
 }
 
 extern "C" int vct_copy_alpha_downsample(uint32_t* radiance, const uint32_t* opacity, const vct_downsample_desc* d,
@@ -404,7 +514,7 @@ extern "C" int vct_copy_alpha_downsample(uint32_t* radiance, const uint32_t* opa
     int rc = mirror_surface(mirror, d->clipmap_resolution,
                             "vct_copy_alpha_downsample: the mirror must be an RGBA8 texture of the same resolution", &surf);
     if (rc != VCT_OK) return rc;
-    return copy_alpha_downsample_pass(radiance, opacity, d, surf, nullptr, as_stream(stream));
+    return copy_alpha_downsample_pass(radiance, opacity, d, surf, nullptr, as_stream(stream), false);
 }
 
 extern "C" int vct_wrap_border(uint32_t* atlas, const vct_border_wrapping_desc* d, void* stream) {

@@ -41,10 +41,14 @@ int texture_format(const vct_texture_s* t);
 // `touched` (may be null): a bitmap over the atlas's texel indices; a texel
 // whose bit is clear is read as zero rgb (the frame's radiance clear folded
 // into these passes).
-int copy_alpha_pass(uint32_t* dst, const uint32_t* src, const vct_copy_alpha_desc* d, cudaSurfaceObject_t mirror,
-                    const uint32_t* touched, cudaStream_t st);
-int copy_alpha_downsample_pass(uint32_t* radiance, const uint32_t* opacity, const vct_downsample_desc* d,
-                               cudaSurfaceObject_t mirror, const uint32_t* touched, cudaStream_t st);
+// `opa_r8`: the opacity atlas is the one-byte-per-texel form (alpha only).
+int copy_alpha_pass(uint32_t* dst, const void* src, const vct_copy_alpha_desc* d, cudaSurfaceObject_t mirror,
+                    const uint32_t* touched, cudaStream_t st, bool src_r8);
+int copy_alpha_downsample_pass(uint32_t* radiance, const void* opacity, const vct_downsample_desc* d,
+                               cudaSurfaceObject_t mirror, const uint32_t* touched, cudaStream_t st, bool opa_r8);
+// The one-byte opacity form's mips 1..5 and border wrap (clipmap_passes.cu).
+int opacity_r8_mips(uint8_t* atlas, const vct_clipmap_region regions[6], int R, cudaStream_t st);
+int wrap_border_r8(uint8_t* atlas, int R, cudaStream_t st);
 
 // The frame's rasterised passes with the deterministic injection, up to the
 // fold (raster.cu): opacity clear + voxelisation + mips + border, shadow

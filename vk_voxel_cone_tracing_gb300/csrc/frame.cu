@@ -31,6 +31,11 @@ extern "C" int vct_clipmap_frame(const vct_scene* scene, const vct_frame_desc* f
                   "vct_clipmap_frame: bad revoxelization mode");
     const bool toroidal = f->revoxelization == VCT_REVOX_TOROIDAL;
     VCT_CHECK_ARG(!toroidal || f->regions_state, "vct_clipmap_frame: the toroidal mode needs regions_state");
+    VCT_CHECK_ARG(f->opacity_format == VCT_OPACITY_RGBA8 || f->opacity_format == VCT_OPACITY_R8,
+                  "vct_clipmap_frame: bad opacity format");
+    const bool r8 = f->opacity_format == VCT_OPACITY_R8;
+    VCT_CHECK_ARG(!r8 || (!toroidal && f->inject_mode == VCT_INJECT_DETERMINISTIC),
+                  "vct_clipmap_frame: the R8 opacity form needs the full revoxelisation and the deterministic injection");
     vct_clipmap_region regions[6];
     vct_clipmap_region slabs[18];
     int32_t slab_levels[18];
@@ -118,7 +123,7 @@ extern "C" int vct_clipmap_frame(const vct_scene* scene, const vct_frame_desc* f
     const cudaSurfaceObject_t mirror = f->radiance_texture ? vct::texture_surface(f->radiance_texture) : 0;
     if (due & 1u) {
         vct_copy_alpha_desc ca = {0, R, VCT_FACE_COUNT};
-        if ((rc = vct::copy_alpha_pass(radiance, opacity, &ca, mirror, touched, st)) != VCT_OK) return rc;
+        if ((rc = vct::copy_alpha_pass(radiance, opacity, &ca, mirror, touched, st, r8)) != VCT_OK) return rc;
     }
     for (int l = 1; l < 6; ++l) {
         if (!((due >> l) & 1u)) continue;
@@ -127,7 +132,8 @@ extern "C" int vct_clipmap_frame(const vct_scene* scene, const vct_frame_desc* f
         d.clip_level = l;
         d.clipmap_resolution = R;
         d.downsample_region_size = VCT_DOWNSAMPLE_REGION_SIZE;
-        if ((rc = vct::copy_alpha_downsample_pass(radiance, opacity, &d, mirror, touched, st)) != VCT_OK) return rc;
+        if ((rc = vct::copy_alpha_downsample_pass(radiance, opacity, &d, mirror, touched, st, r8)) != VCT_OK)
+            return rc;
     }
     return VCT_OK;
 }

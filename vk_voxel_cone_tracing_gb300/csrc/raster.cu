@@ -353,6 +353,7 @@ struct RasterArgs {
     // p.a <= slab_hi[l][a]; an empty interval has lo > hi)
     uint32_t slab_levels;
     float slab_lo[6][3], slab_hi[6][3];
+    int opa_r8;  // the opacity atlas holds one byte per texel (alpha only)
 };
 
 // A fragment at world position p of a slab-restricted level is kept when it
@@ -1153,7 +1154,12 @@ __global__ void __launch_bounds__(128, 6) k_cover(const __grid_constant__ Raster
                     const bool dup = lane > 0 && po == o && qx == ic.x && qy == ic.y && qz == ic.z;
                     if (keep && !dup) {
                         const AtlasDims AD(A.R);
-                        for (int f = 0; f < 6; ++f) A.atlas[AD.index(ic.x + (A.R + 2) * f, ic.y, ic.z)] = 0xFFFFFFFFu;
+                        if (A.opa_r8) {
+                            uint8_t* a8 = reinterpret_cast<uint8_t*>(A.atlas);
+                            for (int f = 0; f < 6; ++f) a8[AD.index(ic.x + (A.R + 2) * f, ic.y, ic.z)] = 0xFFu;
+                        } else {
+                            for (int f = 0; f < 6; ++f) A.atlas[AD.index(ic.x + (A.R + 2) * f, ic.y, ic.z)] = 0xFFFFFFFFu;
+                        }
                     }
                 });
             }
@@ -2281,7 +2287,10 @@ int frame_raster_passes(const vct_scene* scene, const vct_frame_desc* f, const v
     cudaStream_t side = side_stream(ws);
     cudaStream_t ost = side ? side : st;  // the opacity clear's stream
     if (side && (rc = fork_side(ws, side, st)) != VCT_OK) return rc;
+    const bool r8 = f->opacity_format == VCT_OPACITY_R8;  // (full revoxelisation only: checked by the caller)
     if (toroidal) rc = clear_slabs(opacity, R, slabs, slab_levels, nslabs, ost);
+    else if (r8) rc = cudaMemsetAsync(opacity, 0, (size_t)AtlasDims(R).texels(), ost) == cudaSuccess
+                          ? VCT_OK : fail(VCT_E_CUDA, "cudaMemsetAsync (opacity clear)");
     else rc = vct_clear_atlas(opacity, R, ost);
     if (rc != VCT_OK) return rc;
     vct_shadow_map sm = {nullptr, 0, 0};
@@ -2309,10 +2318,12 @@ int frame_raster_passes(const vct_scene* scene, const vct_frame_desc* f, const v
         if (toroidal) apply_slabs(C, P);
         C.items = scene->triangle_count * C.nlevels;
         C.atlas = opacity;
+        C.opa_r8 = r8 ? 1 : 0;
         C.count_levels = due;
         I = C;  // the injection's args over the same items
         I.kind = K_INJECT;
         I.atlas = radiance;
+        I.opa_r8 = 0;
         I.invalid_key = 0xffffffffu >> __builtin_clz((uint32_t)AtlasDims(R).texels());
         if ((rc = fill_light(I, &sm, &f->light, &f->light_shadow)) != VCT_OK) return rc;
         for (;;) {
@@ -2322,7 +2333,9 @@ int frame_raster_passes(const vct_scene* scene, const vct_frame_desc* f, const v
         if (rc != VCT_OK) return rc;
     }
     if (side && (rc = fork_side(ws, side, st)) != VCT_OK) return rc;
-    if (!toroidal) {
+    if (r8) {
+        if ((rc = opacity_r8_mips(reinterpret_cast<uint8_t*>(opacity), regions, R, ost)) != VCT_OK) return rc;
+    } else if (!toroidal) {
         if ((rc = vct_downsample_all(opacity, regions, R, VCT_DOWNSAMPLE_OPACITY, ost)) != VCT_OK) return rc;
     } else {
         // VoxelizationPass::onEndRenderPass: the mips of the levels that were revoxelised
@@ -2337,7 +2350,9 @@ int frame_raster_passes(const vct_scene* scene, const vct_frame_desc* f, const v
         }
     }
     vct_border_wrapping_desc bw = {(uint32_t)R, VCT_VOXEL_BORDER, VCT_FACE_COUNT, VCT_CLIP_LEVEL_COUNT};
-    if ((rc = vct_wrap_border(opacity, &bw, ost)) != VCT_OK) return rc;
+    if (r8) rc = wrap_border_r8(reinterpret_cast<uint8_t*>(opacity), R, ost);
+    else rc = vct_wrap_border(opacity, &bw, ost);
+    if (rc != VCT_OK) return rc;
     // the due radiance levels' clear is folded into the fold (texels start from
     // zero) and the copy-alpha / mip passes (unmarked texels read as zero rgb)
     if (scene->triangle_count > 0 && (rc = inject_finish(I, S, touched, st)) != VCT_OK) return rc;

@@ -222,11 +222,12 @@ def clipmap_frame(dscene: DeviceScene, camera_pos, R: int, opacity: torch.Tensor
                   shadow: torch.Tensor | None, light: capi.DirectionalLightDesc,
                   light_shadow: capi.DirectionalLightShadowDesc, ws: Workspace, frame_index: int = 0,
                   inject_mode: int = capi.INJECT_DETERMINISTIC, texture=None, revoxelization: int = capi.REVOX_FULL,
-                  regions_state=None):
+                  regions_state=None, opacity_format: int = capi.OPACITY_RGBA8):
     """vct_clipmap_frame: voxelise, mips, border, shadow depth, inject, copy alpha, radiance mips; `texture`
     (an RGBA8 RadianceTexture of resolution R) is kept equal to the radiance atlas's written texels.
     `regions_state` ((ClipmapRegion * 6), kept by the caller) persists the regions between frames: a FULL
-    frame writes them, a TOROIDAL frame moves them and revoxelises only the uncovered slabs."""
+    frame writes them, a TOROIDAL frame moves them and revoxelises only the uncovered slabs.  With
+    `opacity_format` OPACITY_R8, `opacity` is a uint8 atlas (clipmap.new_atlas_r8) holding the alpha only."""
     f = capi.FrameDesc()
     f.camera_pos = capi.f3(*camera_pos)
     f.clipmap_resolution = R
@@ -238,6 +239,7 @@ def clipmap_frame(dscene: DeviceScene, camera_pos, R: int, opacity: torch.Tensor
     f.light_shadow = light_shadow
     f.radiance_texture = texture.handle if texture is not None else None
     f.revoxelization = revoxelization
+    f.opacity_format = opacity_format
     f.regions_state = C.cast(regions_state, C.c_void_p) if regions_state is not None else None
     regs = (capi.ClipmapRegion * 6)()
     capi.call("vct_clipmap_frame", capi.ref(dscene.desc), capi.ref(f), _ptr(opacity), _ptr(radiance),
