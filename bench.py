@@ -648,6 +648,30 @@ def other_forms(dev, stream, R, regs, desc, radiance, samples, light, shadow, ls
     ce = int(ctr.item())
     out["exact_rgba8"] = {"trace_ms": te, "cone_samples": ce, "cone_samples_per_s": ce / (te * 1e-3),
                           "note": "the plain FP32 drop-in: software trilinear over the linear RGBA8 atlas"}
+    # the same exact arithmetic with its texels read through a texture holding the atlas (vct_cone_trace_tex);
+    # its outputs are compared bit for bit with the linear-atlas trace's
+    tex8 = clipmap.RadianceTexture(R).update(radiance)
+    ref_d, ref_s = dout.clone(), sout.clone()
+
+    def exact_tex_trace(counter=None):
+        clipmap.cone_trace_tex(desc, EYE, tex8, samples, light=light, shadow=shadow, shadow_desc=lsd,
+                               diffuse=dout, specular=sout, steps=counter)
+
+    ctr.zero_()
+    exact_tex_trace(ctr)
+    torch.cuda.synchronize()
+    equal = bool(torch.equal(dout, ref_d) and torch.equal(sout, ref_s))
+    exact_tex_trace()
+    tx = statistics.median(events_ms(stream, exact_tex_trace, reps)[0])
+    upd = statistics.median(events_ms(stream, lambda: tex8.update(radiance), reps)[0])
+    cx = int(ctr.item())
+    out["exact_rgba8_texel_reads"] = {
+        "trace_ms": tx, "cone_samples": cx, "cone_samples_per_s": cx / (tx * 1e-3), "texture_update_ms": upd,
+        "outputs_bit_equal_to_exact_rgba8": equal, "speedup_vs_exact_rgba8": te / tx,
+        "note": "vct_cone_trace_tex: the exact FP32 arithmetic, each texel one point-sampled texture fetch "
+                "(decoded exactly by the texture unit) from a texture holding the atlas (the one a frame keeps "
+                "current, or vct_texture_update: texture_update_ms)"}
+    tex8.close()
     return out
 
 

@@ -428,6 +428,19 @@ int vct_cone_trace_fast_opt(const vct_cone_tracing_desc* desc, const vct_cam_mat
                             float* specular_out, unsigned long long* cone_steps, const vct_trace_options* options,
                             void* scratch, size_t scratch_bytes, void* stream);
 
+/* The exact FP32 trace (vct_cone_trace_opt's arithmetic, in its order, and
+ * its results bit for bit) reading the RGBA8 atlas's texels through a radiance
+ * texture that holds them (vct_texture_update, or the texture a frame keeps
+ * current): each texel is one point-sampled texture fetch that the texture
+ * unit decodes exactly, instead of address arithmetic, a 4-byte load and a
+ * software unorm8 decode.  No counterpart in the reference beyond
+ * VoxelConeTracingPass::onUpdate (VoxelConeTracingPass.cpp:75-106). */
+int vct_cone_trace_tex(const vct_cone_tracing_desc* desc, const vct_cam_matrix* cam, vct_texture radiance,
+                       const vct_shadow_map* shadow, const vct_directional_light_desc* light,
+                       const vct_directional_light_shadow_desc* light_shadow, const vct_surface_sample* samples,
+                       int64_t sample_count, float* diffuse_out, float* specular_out, unsigned long long* cone_steps,
+                       const vct_trace_options* options, void* stream);
+
 /* One trace of a batch: the arguments of vct_cone_trace_fast for one
  * clipmap (its radiance texture, desc, camera eye, lighting) and one sample
  * set with its outputs.  Host struct; the pointers are device pointers. */

@@ -109,8 +109,11 @@ def _trace_all_forms(torch, oracle, rows, R, regions_np, rad_np, rad_dev, tex8, 
         mirror32[mode] = oracle.cone_trace(32, bytes(desc), eye, rad_np, R, samples, shadow=sh_np,
                                            shadow_desc_bytes=sd_bytes)[:2]
         de, se = clipmap.cone_trace(desc, eye, rad_dev, R, dev_s, light=light, shadow=sh_dev, shadow_desc=lsd)
+        dx, sx = clipmap.cone_trace_tex(desc, eye, tex8, dev_s, light=light, shadow=sh_dev, shadow_desc=lsd)
         df, sf = clipmap.cone_trace_fast(desc, eye, tex8, dev_s, light=light, shadow=sh_dev, shadow_desc=lsd)
         torch.cuda.synchronize()
+        # the exact arithmetic with its texels read through the texture: the same results, bit for bit
+        assert torch.equal(dx, de) and torch.equal(sx, se), mode
         exact[mode] = (de.cpu().numpy(), se.cpu().numpy())
         fast[mode] = (df.cpu().numpy(), sf.cpu().numpy())
         # the exact form follows the FP32 restatement sample by sample

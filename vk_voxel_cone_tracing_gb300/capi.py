@@ -203,6 +203,7 @@ _SIGS: dict[str, tuple] = {
     "vct_wrap_border": (C.c_int, [P, P, P]),
     "vct_cone_trace": (C.c_int, [P, P, P, C.c_int32, P, P, P, P, C.c_int64, P, P, P, P]),
     "vct_cone_trace_opt": (C.c_int, [P, P, P, C.c_int32, P, P, P, P, C.c_int64, P, P, P, P, P]),
+    "vct_cone_trace_tex": (C.c_int, [P, P, P, P, P, P, P, C.c_int64, P, P, P, P, P]),
     "vct_cone_trace_f32": (C.c_int, [P, P, P, C.c_int32, P, P, P, P, C.c_int64, P, P, P, P]),
     "vct_cone_trace_backward": (C.c_int, [P, P, P, C.c_int32, P, P, P, P, C.c_int64, P, P, P, P]),
     "vct_downsample_f32": (C.c_int, [P, P, C.c_int32, P]),

@@ -135,6 +135,30 @@ def cone_trace(desc: capi.ConeTracingDesc, eye, radiance: torch.Tensor, R: int, 
 
 # ----------------------------------------------------------------- fast form
 
+def cone_trace_tex(desc: capi.ConeTracingDesc, eye, tex: "RadianceTexture", samples: torch.Tensor,
+                   light: capi.DirectionalLightDesc | None = None, shadow: torch.Tensor | None = None,
+                   shadow_desc: capi.DirectionalLightShadowDesc | None = None, diffuse: torch.Tensor | None = None,
+                   specular: torch.Tensor | None = None, steps: torch.Tensor | None = None,
+                   diffuse_aperture: float = 0.0):
+    """cone_trace (the exact FP32 arithmetic, same results bit for bit) reading the texels through the RGBA8
+    texture `tex`, which must hold the atlas's texels (vct_cone_trace_tex)."""
+    n = samples.shape[0]
+    if diffuse is None:
+        diffuse = torch.zeros((n, 4), dtype=torch.float32, device=samples.device)
+    if specular is None:
+        specular = torch.zeros((n, 4), dtype=torch.float32, device=samples.device)
+    cam = cam_matrix(eye)
+    light = light or capi.DirectionalLightDesc(capi.f3(0.3, -1.0, 0.2), 1.0, capi.f3(1, 1, 1), 0)
+    sm = capi.ShadowMap(None, 0, 0)
+    if shadow is not None:
+        sm = capi.ShadowMap(shadow.data_ptr(), shadow.shape[1], shadow.shape[0])
+    sd = shadow_desc or capi.DirectionalLightShadowDesc()
+    opt = capi.TraceOptions(diffuse_aperture)
+    capi.call("vct_cone_trace_tex", capi.ref(desc), capi.ref(cam), tex.handle, capi.ref(sm), capi.ref(light),
+              capi.ref(sd), _ptr(samples), n, _ptr(diffuse), _ptr(specular), _ptr(steps), capi.ref(opt), _stream())
+    return diffuse, specular
+
+
 class RadianceTexture:
     """Hardware-filtered copy of a radiance atlas (vct_texture_*): RGBA8 or RGBA16F."""
 

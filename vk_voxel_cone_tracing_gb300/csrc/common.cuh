@@ -32,6 +32,8 @@ int workspace_reserve(vct_workspace_s* ws, size_t bytes);
 // Radiance texture accessors (textures.cu).
 cudaTextureObject_t texture_object(const vct_texture_s* t);
 cudaSurfaceObject_t texture_surface(const vct_texture_s* t);
+// RGBA8 only (0 otherwise): point filter, unnormalised coordinates, texels read as normalised floats.
+cudaTextureObject_t texture_texel_object(const vct_texture_s* t);
 int texture_resolution(const vct_texture_s* t);
 int texture_format(const vct_texture_s* t);
 

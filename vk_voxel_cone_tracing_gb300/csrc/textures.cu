@@ -16,12 +16,15 @@ struct vct_texture_s {
     cudaArray_t array = nullptr;
     cudaTextureObject_t tex = 0;
     cudaSurfaceObject_t surf = 0;  // the same array for direct texel stores
+    cudaTextureObject_t texel = 0; // RGBA8: the same array read texel by texel (point filter,
+                                   // unnormalised coordinates, unorm8 decoded to float)
 };
 
 namespace vct {
 
 cudaTextureObject_t texture_object(const vct_texture_s* t) { return t->tex; }
 cudaSurfaceObject_t texture_surface(const vct_texture_s* t) { return t->surf; }
+cudaTextureObject_t texture_texel_object(const vct_texture_s* t) { return t->texel; }
 int texture_resolution(const vct_texture_s* t) { return t->R; }
 int texture_format(const vct_texture_s* t) { return t->format; }
 
@@ -183,6 +186,12 @@ extern "C" int vct_texture_create(int32_t R, int32_t format, vct_texture_s** out
     td.readMode = format == 0 ? cudaReadModeNormalizedFloat : cudaReadModeElementType;
     td.normalizedCoords = 1;
     e = cudaCreateTextureObject(&t->tex, &rd, &td, nullptr);
+    if (e == cudaSuccess && format == 0) {
+        cudaTextureDesc tp = td;
+        tp.filterMode = cudaFilterModePoint;
+        tp.normalizedCoords = 0;
+        e = cudaCreateTextureObject(&t->texel, &rd, &tp, nullptr);
+    }
     if (e == cudaSuccess) e = cudaCreateSurfaceObject(&t->surf, &rd);
     if (e == cudaSuccess) {  // a defined starting content: all zero, like a fresh atlas
         k_surface_zero<<<grid_for16(A.texels(), 256), 256>>>(t->surf, A.W, A.H, A.D, format == 0 ? 4 : 8);
@@ -191,6 +200,7 @@ extern "C" int vct_texture_create(int32_t R, int32_t format, vct_texture_s** out
     }
     if (e != cudaSuccess) {
         if (t->surf) cudaDestroySurfaceObject(t->surf);
+        if (t->texel) cudaDestroyTextureObject(t->texel);
         if (t->tex) cudaDestroyTextureObject(t->tex);
         cudaFreeArray(t->array);
         delete t;
@@ -229,6 +239,7 @@ extern "C" int vct_texture_read(const vct_texture_s* t, void* atlas, void* strea
 extern "C" int vct_texture_destroy(vct_texture_s* t) {
     if (!t) return VCT_OK;
     if (t->surf) cudaDestroySurfaceObject(t->surf);
+    if (t->texel) cudaDestroyTextureObject(t->texel);
     cudaError_t e1 = cudaDestroyTextureObject(t->tex);
     cudaError_t e2 = cudaFreeArray(t->array);
     delete t;

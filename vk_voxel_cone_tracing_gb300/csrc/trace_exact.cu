@@ -351,6 +351,30 @@ extern "C" int vct_cone_trace_opt(const vct_cone_tracing_desc* desc, const vct_c
     return launch_exact(P, T, samples, n, dout, sout, cone_steps, as_stream(stream));
 }
 
+extern "C" int vct_cone_trace_tex(const vct_cone_tracing_desc* desc, const vct_cam_matrix* cam,
+                                  vct_texture_s* radiance, const vct_shadow_map* shadow,
+                                  const vct_directional_light_desc* light,
+                                  const vct_directional_light_shadow_desc* light_shadow,
+                                  const vct_surface_sample* samples, int64_t n, float* dout, float* sout,
+                                  unsigned long long* cone_steps, const vct_trace_options* options, void* stream) {
+    vct::NvtxRange nvtx_range("vct_cone_trace_tex");
+    VCT_CHECK_ARG(radiance && texture_format(radiance) == VCT_TEX_RGBA8,
+                  "vct_cone_trace_tex: the radiance texture must be RGBA8");
+    VCT_CHECK_ARG(n >= 0, "vct_cone_trace_tex: negative sample count");
+    if (n == 0) return VCT_OK;
+    VCT_CHECK_ARG(samples && dout && sout, "vct_cone_trace_tex: null sample or output buffer");
+    VCT_CHECK_ARG(((uintptr_t)samples & 15) == 0 && ((uintptr_t)dout & 15) == 0 && ((uintptr_t)sout & 15) == 0,
+                  "vct_cone_trace_tex: sample/output buffers must be 16-byte aligned");
+    TraceParams P;
+    int rc = fill_trace_params(P, desc, cam, shadow, light, light_shadow);
+    if (rc != VCT_OK) return rc;
+    if ((rc = apply_trace_options(P, options)) != VCT_OK) return rc;
+    VCT_CHECK_ARG((float)texture_resolution(radiance) == desc->volume_dimension,
+                  "vct_cone_trace_tex: volume dimension differs from the texture's clipmap resolution");
+    TexelAtlas T{texture_texel_object(radiance), AtlasDims(texture_resolution(radiance))};
+    return launch_exact(P, T, samples, n, dout, sout, cone_steps, as_stream(stream));
+}
+
 extern "C" int vct_cone_trace_f32(const vct_cone_tracing_desc* desc, const vct_cam_matrix* cam, const float* atlas4,
                                   int32_t R, const vct_shadow_map* shadow, const vct_directional_light_desc* light,
                                   const vct_directional_light_shadow_desc* light_shadow,

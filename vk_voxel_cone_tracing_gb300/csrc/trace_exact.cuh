@@ -16,6 +16,22 @@ struct ExactAtlas {
     __device__ __forceinline__ float4 fetch(int x, int y, int z) const { return unpack_rgba8(__ldg(p + A.index(x, y, z))); }
 };
 
+// The RGBA8 atlas's texels read through a radiance texture holding the same
+// texels (point filter at texel centres, unnormalised coordinates): one
+// texture instruction returns the four channels decoded to float by the
+// texture unit, in place of the 64-bit address arithmetic, the 4-byte load
+// and the four-channel decode.  The unit's unorm8 conversion gives c/255
+// correctly rounded, the float unorm8_decode computes (the tests compare whole
+// traces through both reads bit for bit), so the trace's arithmetic, in its
+// order, is unchanged.
+struct TexelAtlas {
+    cudaTextureObject_t t;
+    AtlasDims A;
+    __device__ __forceinline__ float4 fetch(int x, int y, int z) const {
+        return tex3D<float4>(t, (float)x + 0.5f, (float)y + 0.5f, (float)z + 0.5f);
+    }
+};
+
 // Float RGBA texels (16 B each), the layout of the FP16 form widened to FP32.
 struct F4Atlas {
     const float4* __restrict__ p;
