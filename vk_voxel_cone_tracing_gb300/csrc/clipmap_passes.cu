@@ -134,12 +134,17 @@ __global__ void k_wrap_border(T* __restrict__ atlas, AtlasDims A, int faces, int
 // blends with the level's own texel in the outer band and stores.
 __device__ __forceinline__ int ds_wrap(int p, int R) { return (p + R * (abs(p / R) + 1)) & (R - 1); }
 
-__constant__ int c_pairs[6][4][2] = {
-    {{0, 1}, {2, 3}, {4, 5}, {6, 7}}, {{1, 0}, {3, 2}, {5, 4}, {7, 6}}, {{0, 2}, {1, 3}, {4, 6}, {5, 7}},
-    {{2, 0}, {3, 1}, {6, 4}, {7, 5}}, {{0, 4}, {1, 5}, {2, 6}, {3, 7}}, {{4, 0}, {5, 1}, {6, 2}, {7, 3}}};
+}  // namespace vct
+#include "mip_pairs.cuh"
+namespace vct {
 
+// `prev` is `atlas` again, read only at level l - 1 (which this pass does not
+// write): as a second restrict pointer its loads are free to run ahead of the
+// stores of level l, so all six faces' 2x2x2 blocks are loaded before the
+// first store (one memory round trip per output voxel instead of six).
 template <int MODE>
-__global__ void k_downsample(uint32_t* __restrict__ atlas, AtlasDims A, int3 pmin, int level, int band, int lgh) {
+__global__ void k_downsample(uint32_t* __restrict__ atlas, const uint32_t* __restrict__ prev, AtlasDims A, int3 pmin,
+                             int level, int band, int lgh) {
     const int half = A.R >> 1;
     const uint32_t n = 1u << (3 * lgh), m = (1u << lgh) - 1u;
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
@@ -173,19 +178,27 @@ __global__ void k_downsample(uint32_t* __restrict__ atlas, AtlasDims A, int3 pmi
             lerp = __fmul_rn(lerp, inv);
         }
 
+        uint32_t raw6[6][8], own6[6];
+        const int64_t c0 = A.index(ps[0], ps[1], ps[2]), w0 = A.index(wpos[0], wpos[1], wpos[2]);
+        const int64_t dy = A.W, dz = (int64_t)A.W * A.H;
+#pragma unroll
         for (int f = 0; f < 6; ++f) {
-            uint32_t raw[8];
 #pragma unroll
             for (int i = 0; i < 8; ++i)
-                raw[i] = atlas[A.index(ps[0] + (i & 1) + A.rb * f, ps[1] + ((i >> 1) & 1), ps[2] + ((i >> 2) & 1))];
-            const int64_t wi = A.index(wpos[0] + A.rb * f, wpos[1], wpos[2]);
-            const uint32_t own_raw = atlas[wi];
+                raw6[f][i] = __ldg(prev + c0 + A.rb * f + (i & 1) + ((i >> 1) & 1) * dy + ((i >> 2) & 1) * dz);
+            own6[f] = atlas[w0 + A.rb * f];
+        }
+#pragma unroll
+        for (int f = 0; f < 6; ++f) {
+            const uint32_t* raw = raw6[f];
+            const int64_t wi = w0 + A.rb * f;
+            const uint32_t own_raw = own6[f];
             if (MODE == 0) {
                 float s = 0.0f;
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
-                    const float a0 = unorm8_load(raw[c_pairs[f][k][0]], 3);
-                    const float a1 = unorm8_load(raw[c_pairs[f][k][1]], 3);
+                    const float a0 = unorm8_load(raw[ds_pair(f, k, 0)], 3);
+                    const float a1 = unorm8_load(raw[ds_pair(f, k, 1)], 3);
                     const float tt = __fmul_rn(__fsub_rn(1.0f, a0), a1);
                     s = (k == 0) ? __fadd_rn(a0, tt) : __fadd_rn(__fadd_rn(s, a0), tt);
                 }
@@ -198,7 +211,7 @@ __global__ void k_downsample(uint32_t* __restrict__ atlas, AtlasDims A, int3 pmi
                 float s[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
-                    const uint32_t r0 = raw[c_pairs[f][k][0]], r1 = raw[c_pairs[f][k][1]];
+                    const uint32_t r0 = raw[ds_pair(f, k, 0)], r1 = raw[ds_pair(f, k, 1)];
                     const float tt = __fsub_rn(1.0f, unorm8_load(r0, 3));
 #pragma unroll
                     for (int c = 0; c < 4; ++c) {
@@ -229,7 +242,8 @@ __global__ void k_downsample(uint32_t* __restrict__ atlas, AtlasDims A, int3 pmi
 // -- the voxelised value until this pass stores the alpha over it -- gives
 // every reader the byte it reads from the RGBA8 atlas.  (The toroidal update
 // re-reads red of texels voxelised in earlier frames, so it keeps RGBA8.)
-__global__ void k_downsample_r8(uint8_t* __restrict__ atlas, AtlasDims A, int3 pmin, int level, int band, int lgh) {
+__global__ void k_downsample_r8(uint8_t* __restrict__ atlas, const uint8_t* __restrict__ prev, AtlasDims A, int3 pmin,
+                                int level, int band, int lgh) {
     const int half = A.R >> 1;
     const uint32_t n = 1u << (3 * lgh), m = (1u << lgh) - 1u;
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
@@ -260,23 +274,31 @@ __global__ void k_downsample_r8(uint8_t* __restrict__ atlas, AtlasDims A, int3 p
             lerp = __fadd_rn(__fsub_rn(fmaxf(dist[0], fmaxf(dist[1], dist[2])), (float)((half >> 1) - band)), 1.0f);
             lerp = __fmul_rn(lerp, inv);
         }
+        uint32_t raw6[6][8], own6[6];
+        const int64_t c0 = A.index(ps[0], ps[1], ps[2]), w0 = A.index(wpos[0], wpos[1], wpos[2]);
+        const int64_t dy = A.W, dz = (int64_t)A.W * A.H;
+#pragma unroll
         for (int f = 0; f < 6; ++f) {
-            uint32_t raw[8];
 #pragma unroll
             for (int i = 0; i < 8; ++i)
-                raw[i] = (uint32_t)atlas[A.index(ps[0] + (i & 1) + A.rb * f, ps[1] + ((i >> 1) & 1), ps[2] + ((i >> 2) & 1))]
-                         << 24;
-            const int64_t wi = A.index(wpos[0] + A.rb * f, wpos[1], wpos[2]);
+                raw6[f][i] = (uint32_t)__ldg(prev + c0 + A.rb * f + (i & 1) + ((i >> 1) & 1) * dy + ((i >> 2) & 1) * dz)
+                             << 24;
+            own6[f] = atlas[w0 + A.rb * f];
+        }
+#pragma unroll
+        for (int f = 0; f < 6; ++f) {
+            const uint32_t* raw = raw6[f];
+            const int64_t wi = w0 + A.rb * f;
             float s = 0.0f;
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                const float a0 = unorm8_load(raw[c_pairs[f][k][0]], 3);
-                const float a1 = unorm8_load(raw[c_pairs[f][k][1]], 3);
+                const float a0 = unorm8_load(raw[ds_pair(f, k, 0)], 3);
+                const float a1 = unorm8_load(raw[ds_pair(f, k, 1)], 3);
                 const float tt = __fmul_rn(__fsub_rn(1.0f, a0), a1);
                 s = (k == 0) ? __fadd_rn(a0, tt) : __fadd_rn(__fadd_rn(s, a0), tt);
             }
             const float res = __fmul_rn(s, 0.25f);
-            const float own_r = unorm8_load((uint32_t)atlas[wi], 0);
+            const float own_r = unorm8_load(own6[f], 0);
             atlas[wi] = (uint8_t)unorm8_store(mix_rn(res, own_r, lerp));
         }
     }
@@ -293,8 +315,14 @@ __global__ void k_downsample_r8(uint8_t* __restrict__ atlas, AtlasDims A, int3 p
 // of work (one loop over the mixed texels was 3 % slower per frame at
 // R = 256).  The target block depends only on level l - 1, which earlier
 // launches finished.  All six faces per thread.
+// Faces whose 2x2x2 blocks of level l - 1 a target loads together, ahead of
+// their stores (through `prev`, the radiance atlas again as a read-only
+// restrict pointer: level l - 1 is not written by this pass).
+constexpr int kAlphaDsFacesPerRound = 2;
+
 template <class OT>
 __global__ void __launch_bounds__(128, 8) k_alpha_downsample(uint32_t* __restrict__ rad,
+                                                                    const uint32_t* __restrict__ prev,
                                                                     const OT* __restrict__ opa, AtlasDims A,
                                                                     int3 pmin, int level, int band, int lg,
                                                                     cudaSurfaceObject_t mirror,
@@ -356,16 +384,24 @@ __global__ void __launch_bounds__(128, 8) k_alpha_downsample(uint32_t* __restric
 #pragma unroll
         for (int f = 0; f < 6; ++f)
             own6[f] = rgb_of(rad, touched, w0 + A.rb * f) | opa_alpha(opa, w0 + A.rb * f);
-#pragma unroll 1
-        for (int f = 0; f < 6; ++f) {
-            uint32_t raw[8];
+        const int64_t c0 = A.index(ps[0], ps[1], ps[2]);
+        const int64_t dy = A.W, dz = (int64_t)A.W * A.H;
+#pragma unroll
+        for (int f0 = 0; f0 < 6; f0 += kAlphaDsFacesPerRound) {
+          uint32_t rawr[kAlphaDsFacesPerRound][8];
+#pragma unroll
+          for (int h = 0; h < kAlphaDsFacesPerRound; ++h)
 #pragma unroll
             for (int i = 0; i < 8; ++i)
-                raw[i] = rad[A.index(ps[0] + (i & 1) + A.rb * f, ps[1] + ((i >> 1) & 1), ps[2] + ((i >> 2) & 1))];
+                rawr[h][i] = __ldg(prev + c0 + A.rb * (f0 + h) + (i & 1) + ((i >> 1) & 1) * dy + ((i >> 2) & 1) * dz);
+#pragma unroll
+          for (int h = 0; h < kAlphaDsFacesPerRound; ++h) {
+            const int f = f0 + h;
+            const uint32_t* raw = rawr[h];
             float sc[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                const uint32_t r0 = raw[c_pairs[f][k][0]], r1 = raw[c_pairs[f][k][1]];
+                const uint32_t r0 = raw[ds_pair(f, k, 0)], r1 = raw[ds_pair(f, k, 1)];
                 const float tt = __fsub_rn(1.0f, unorm8_load(r0, 3));
 #pragma unroll
                 for (int c = 0; c < 4; ++c) {
@@ -382,6 +418,7 @@ __global__ void __launch_bounds__(128, 8) k_alpha_downsample(uint32_t* __restric
             }
             rad[w0 + A.rb * f] = out;
             if (mirror) surf3Dwrite(out, mirror, (wpos[0] + A.rb * f) * 4, wpos[1], wpos[2]);
+          }
         }
     }
 }
@@ -456,11 +493,11 @@ int copy_alpha_downsample_pass(uint32_t* radiance, const void* opacity, const vc
     int3 pm = make_int3(d->prev_region_min_corner[0], d->prev_region_min_corner[1], d->prev_region_min_corner[2]);
     const int lg = 31 - __builtin_clz((unsigned)A.R);
     if (opa_r8)
-        k_alpha_downsample<<<grid_for(n, 128), 128, 0, st>>>(radiance, static_cast<const uint8_t*>(opacity), A, pm,
+        k_alpha_downsample<<<grid_for(n, 128), 128, 0, st>>>(radiance, radiance, static_cast<const uint8_t*>(opacity), A, pm,
                                                             d->clip_level, d->downsample_region_size, lg, mirror,
                                                             touched);
     else
-        k_alpha_downsample<<<grid_for(n, 128), 128, 0, st>>>(radiance, static_cast<const uint32_t*>(opacity), A, pm,
+        k_alpha_downsample<<<grid_for(n, 128), 128, 0, st>>>(radiance, radiance, static_cast<const uint32_t*>(opacity), A, pm,
                                                             d->clip_level, d->downsample_region_size, lg, mirror,
                                                             touched);
     VCT_LAUNCH_CHECK();
@@ -476,7 +513,7 @@ int opacity_r8_mips(uint8_t* atlas, const vct_clipmap_region regions[6], int R, 
     const int lgh = 31 - __builtin_clz((unsigned)half);
     for (int l = 1; l < VCT_CLIP_LEVEL_COUNT; ++l) {
         const int3 pm = make_int3(regions[l - 1].min_corner[0], regions[l - 1].min_corner[1], regions[l - 1].min_corner[2]);
-        k_downsample_r8<<<grid_for(n, 128), 128, 0, st>>>(atlas, A, pm, l, VCT_DOWNSAMPLE_REGION_SIZE, lgh);
+        k_downsample_r8<<<grid_for(n, 128), 128, 0, st>>>(atlas, atlas, A, pm, l, VCT_DOWNSAMPLE_REGION_SIZE, lgh);
         VCT_LAUNCH_CHECK();
     }
     return VCT_OK;
@@ -579,6 +616,7 @@ __global__ void k_downsample_f32(float4* __restrict__ atlas, AtlasDims A, int3 p
     const uint32_t n = 1u << (3 * lgh);
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         const DsSite st = ds_site(A, pmin, level, band, lgh, t);
+        #pragma unroll
         for (int f = 0; f < 6; ++f) {
             float4 v[8];
 #pragma unroll
@@ -589,7 +627,7 @@ __global__ void k_downsample_f32(float4* __restrict__ atlas, AtlasDims A, int3 p
                 float s = 0.0f;
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
-                    const float a0 = v[c_pairs[f][k][0]].w, a1 = v[c_pairs[f][k][1]].w;
+                    const float a0 = v[ds_pair(f, k, 0)].w, a1 = v[ds_pair(f, k, 1)].w;
                     const float tt = __fmul_rn(__fsub_rn(1.0f, a0), a1);
                     s = (k == 0) ? __fadd_rn(a0, tt) : __fadd_rn(__fadd_rn(s, a0), tt);
                 }
@@ -599,7 +637,7 @@ __global__ void k_downsample_f32(float4* __restrict__ atlas, AtlasDims A, int3 p
                 float s[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
-                    const float4 a0 = v[c_pairs[f][k][0]], a1 = v[c_pairs[f][k][1]];
+                    const float4 a0 = v[ds_pair(f, k, 0)], a1 = v[ds_pair(f, k, 1)];
                     const float tt = __fsub_rn(1.0f, a0.w);
                     const float av[4] = {a0.x, a0.y, a0.z, a0.w}, bv[4] = {a1.x, a1.y, a1.z, a1.w};
 #pragma unroll
@@ -632,6 +670,7 @@ __global__ void k_downsample_backward(const float4* __restrict__ atlas, float4* 
     const uint32_t n = 1u << (3 * lgh);
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         const DsSite st = ds_site(A, pmin, level, band, lgh, t);
+        #pragma unroll
         for (int f = 0; f < 6; ++f) {
             float4 v[8], gc[8];
 #pragma unroll
@@ -647,7 +686,7 @@ __global__ void k_downsample_backward(const float4* __restrict__ atlas, float4* 
                 const float gs = ga * (1.0f - st.lerp) * 0.25f;
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
-                    const int i0 = c_pairs[f][k][0], i1 = c_pairs[f][k][1];
+                    const int i0 = ds_pair(f, k, 0), i1 = ds_pair(f, k, 1);
                     gc[i0].w += gs * (1.0f - v[i1].w);
                     gc[i1].w += gs * (1.0f - v[i0].w);
                 }
@@ -657,7 +696,7 @@ __global__ void k_downsample_backward(const float4* __restrict__ atlas, float4* 
                 const float4 gs = make_float4(go.x * w, go.y * w, go.z * w, go.w * w);
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
-                    const int i0 = c_pairs[f][k][0], i1 = c_pairs[f][k][1];
+                    const int i0 = ds_pair(f, k, 0), i1 = ds_pair(f, k, 1);
                     const float tt = 1.0f - v[i0].w;
                     gc[i0].x += gs.x;
                     gc[i0].y += gs.y;
@@ -740,9 +779,11 @@ extern "C" int vct_downsample(uint32_t* atlas, const vct_downsample_desc* d, int
     int3 pm = make_int3(d->prev_region_min_corner[0], d->prev_region_min_corner[1], d->prev_region_min_corner[2]);
     const int lgh = 31 - __builtin_clz((unsigned)half);
     if (mode == VCT_DOWNSAMPLE_OPACITY)
-        k_downsample<0><<<grid_for(n, 128), 128, 0, as_stream(stream)>>>(atlas, A, pm, d->clip_level, d->downsample_region_size, lgh);
+        k_downsample<0><<<grid_for(n, 128), 128, 0, as_stream(stream)>>>(atlas, atlas, A, pm, d->clip_level,
+                                                                         d->downsample_region_size, lgh);
     else
-        k_downsample<1><<<grid_for(n, 128), 128, 0, as_stream(stream)>>>(atlas, A, pm, d->clip_level, d->downsample_region_size, lgh);
+        k_downsample<1><<<grid_for(n, 128), 128, 0, as_stream(stream)>>>(atlas, atlas, A, pm, d->clip_level,
+                                                                         d->downsample_region_size, lgh);
     VCT_LAUNCH_CHECK();
     return VCT_OK;
 }

@@ -72,9 +72,9 @@ __global__ void __launch_bounds__(256) k_rgba8_to_rgba16f(const uint32_t* __rest
 
 __device__ __forceinline__ int ds_wrap16(int p, int R) { return (p + R * (abs(p / R) + 1)) & (R - 1); }
 
-__constant__ int c_pairs16[6][4][2] = {
-    {{0, 1}, {2, 3}, {4, 5}, {6, 7}}, {{1, 0}, {3, 2}, {5, 4}, {7, 6}}, {{0, 2}, {1, 3}, {4, 6}, {5, 7}},
-    {{2, 0}, {3, 1}, {6, 4}, {7, 5}}, {{0, 4}, {1, 5}, {2, 6}, {3, 7}}, {{4, 0}, {5, 1}, {6, 2}, {7, 3}}};
+}  // namespace vct
+#include "mip_pairs.cuh"
+namespace vct {
 
 __device__ __forceinline__ float4 load_h4(const uint2* p, int64_t i) {
     uint2 v = p[i];
@@ -116,6 +116,7 @@ __global__ void k_downsample_f16(uint2* __restrict__ atlas, AtlasDims A, int3 pm
         if (any_ge)
             lerp = (fmaxf(dist[0], fmaxf(dist[1], dist[2])) - (float)((half >> 1) - band) + 1.0f) *
                    (1.0f / ((float)band + 1.0f));
+        #pragma unroll
         for (int f = 0; f < 6; ++f) {
             float4 v[8];
 #pragma unroll
@@ -126,7 +127,7 @@ __global__ void k_downsample_f16(uint2* __restrict__ atlas, AtlasDims A, int3 pm
             float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                const float4 a0 = v[c_pairs16[f][k][0]], a1 = v[c_pairs16[f][k][1]];
+                const float4 a0 = v[ds_pair(f, k, 0)], a1 = v[ds_pair(f, k, 1)];
                 const float tt = 1.0f - a0.w;
                 if (MODE == 0) {
                     s.w += a0.w + tt * a1.w;
