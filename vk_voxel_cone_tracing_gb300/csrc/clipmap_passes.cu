@@ -29,8 +29,8 @@ __global__ void k_clear_region(uint32_t* __restrict__ atlas, AtlasDims A, int3 r
 
 // ------------------------------------------------------------- copy alpha
 // copyAlphaImage.comp:16-30: dst.a = src.a over the R^3 interior, all faces.
-// Thread per texel of one face row (x fastest) -> coalesced 4-byte RMW.
-// blockIdx.y = face; R is a power of two, so the (x, y, z) split is shifts.
+// Thread per texel position (cube_texel order: coalesced 4-byte RMW), all
+// faces; R is a power of two, so the (x, y, z) split is shifts.
 // `mirror` (0 = none): a texture array's surface that receives the same texels.
 // `touched` (may be null): texels whose bit is clear read as zero rgb.
 // (Both words are loaded unconditionally and selected, so the loads of a
@@ -72,19 +72,26 @@ __device__ __forceinline__ uint32_t opa_alpha(const uint8_t* __restrict__ opa, i
 
 template <class OT>
 __global__ void k_copy_alpha(uint32_t* __restrict__ dst, const OT* __restrict__ src, AtlasDims A, int level,
-                             int lg, cudaSurfaceObject_t mirror, const uint32_t* __restrict__ touched) {
-    const int f = blockIdx.y;
+                             int lg, int faces, cudaSurfaceObject_t mirror, const uint32_t* __restrict__ touched) {
     const uint32_t n = 1u << (3 * lg);
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         int x, y, z;
         cube_texel(t, lg, x, y, z);
-        x += 1 + A.rb * f;
+        x += 1;
         y += 1 + level * A.rb;
         z += 1;
-        const int64_t i = A.index(x, y, z);
-        const uint32_t v = rgb_of(dst, touched, i) | opa_alpha(src, i);
-        dst[i] = v;
-        if (mirror) surf3Dwrite(v, mirror, x * 4, y, z);
+        const int64_t i0 = A.index(x, y, z);
+        // every face's texel loaded before the first store: six loads in flight per thread
+        uint32_t v[6];
+#pragma unroll
+        for (int f = 0; f < 6; ++f)
+            if (f < faces) v[f] = rgb_of(dst, touched, i0 + A.rb * f) | opa_alpha(src, i0 + A.rb * f);
+#pragma unroll
+        for (int f = 0; f < 6; ++f)
+            if (f < faces) {
+                dst[i0 + A.rb * f] = v[f];
+                if (mirror) surf3Dwrite(v[f], mirror, (x + A.rb * f) * 4, y, z);
+            }
     }
 }
 
@@ -468,12 +475,13 @@ int copy_alpha_pass(uint32_t* dst, const void* src, const vct_copy_alpha_desc* d
     if (d->face_count == 0) return VCT_OK;
     const int lg = 31 - __builtin_clz((unsigned)A.R);
     const int64_t n = (int64_t)A.R * A.R * A.R;
-    dim3 grid((unsigned)grid_for(n, 256), (unsigned)d->face_count);
+    const int grid = grid_for(n, 256);
     if (src_r8)
-        k_copy_alpha<<<grid, 256, 0, st>>>(dst, static_cast<const uint8_t*>(src), A, d->clip_level, lg, mirror, touched);
+        k_copy_alpha<<<grid, 256, 0, st>>>(dst, static_cast<const uint8_t*>(src), A, d->clip_level, lg, d->face_count,
+                                           mirror, touched);
     else
-        k_copy_alpha<<<grid, 256, 0, st>>>(dst, static_cast<const uint32_t*>(src), A, d->clip_level, lg, mirror,
-                                           touched);
+        k_copy_alpha<<<grid, 256, 0, st>>>(dst, static_cast<const uint32_t*>(src), A, d->clip_level, lg, d->face_count,
+                                           mirror, touched);
     VCT_LAUNCH_CHECK();
     return VCT_OK;
 }
