@@ -917,6 +917,11 @@ __device__ inline uint32_t cover_pixel(const TileRegs& t, const TileSlot& T, int
     return mask;
 }
 
+// Per-sample work of the coverage kernels (opacity stores, fragment
+// emission) over the round's covered samples dealt one per lane (true), or
+// over each lane's own pixel mask (false).
+constexpr bool kDealCoveredSamples = true;
+
 // The covered samples of a warp's 32 pixels (lane i's pixel has coverage
 // mask `mask`), dealt one per lane in (pixel, sample) order, 32 per round:
 // fn(valid, o, s, r) runs on every lane (valid false on the lanes past the
@@ -967,7 +972,7 @@ __global__ void __launch_bounds__(128, 6) k_cover(const __grid_constant__ Raster
     constexpr int NS = (KIND == K_SHADOW || KIND == K_GBUFFER) ? 1 : 8;
     constexpr bool RANKED = PHASE != P_DIRECT;
     // the opacity writes run over the round's covered samples dealt to the lanes
-    constexpr bool FLAT_OPACITY = (KIND == K_OPACITY || KIND == K_OPA_COUNT) && PHASE != P_WRITE;
+    constexpr bool FLAT_OPACITY = kDealCoveredSamples && (KIND == K_OPACITY || KIND == K_OPA_COUNT) && PHASE != P_WRITE;
     constexpr unsigned FULL = 0xffffffffu;
     __shared__ TileSlot slots[4][32];
     const int lane = threadIdx.x & 31;
@@ -1104,9 +1109,10 @@ __global__ void __launch_bounds__(128, 6) k_cover(const __grid_constant__ Raster
                 px = S[j].tx + (ox0 >> 8);
                 py = S[j].ty + (oy0 >> 8);
                 mask = cover_pixel<NS>(t, S[j], ox0, oy0);
-                if (!FLAT_OPACITY && PHASE == P_DIRECT && mask) {
+                if (!FLAT_OPACITY && (PHASE == P_DIRECT || KIND == K_OPA_COUNT) && mask) {
                     const TileSlot& T = S[j];
                     const int lvl = (int)(T.meta & 7u);
+                    int3 last_ic = make_int3(-1, -1, -1);  // opacity: the previous sample's voxel (stores are idempotent)
                     for (uint32_t m = mask; m; m &= m - 1u) {
                         const int s = __ffs(m) - 1;
                         float b[3], z;
@@ -1114,6 +1120,24 @@ __global__ void __launch_bounds__(128, 6) k_cover(const __grid_constant__ Raster
                                   oy0 + (NS == 1 ? 128 : c_sample_loc8[s][1]), b, z);
                         if (KIND == K_SHADOW) {
                             atomicMin(reinterpret_cast<unsigned int*>(A.depth) + (int64_t)py * A.W + px, __float_as_uint(z));
+                        } else if (KIND == K_OPACITY || KIND == K_OPA_COUNT) {
+                            const vct_voxelization_desc& d = A.vd[lvl];
+                            const float3 wp = interp3(b, T.p);
+                            if (wp.x < d.region_min_corner[0] || wp.y < d.region_min_corner[1] ||
+                                wp.z < d.region_min_corner[2] || wp.x > d.region_max_corner[0] ||
+                                wp.y > d.region_max_corner[1] || wp.z > d.region_max_corner[2])
+                                continue;
+                            if (((A.slab_levels >> lvl) & 1u) && !in_slabs(A, lvl, wp)) continue;
+                            const AtlasDims AD(A.R);
+                            const int3 ic = clip_image_coords(d, wp);
+                            if (ic.x == last_ic.x && ic.y == last_ic.y && ic.z == last_ic.z) continue;
+                            last_ic = ic;
+                            if (A.opa_r8) {
+                                uint8_t* a8 = reinterpret_cast<uint8_t*>(A.atlas);
+                                for (int f = 0; f < 6; ++f) a8[AD.index(ic.x + (A.R + 2) * f, ic.y, ic.z)] = 0xFFu;
+                            } else {
+                                for (int f = 0; f < 6; ++f) A.atlas[AD.index(ic.x + (A.R + 2) * f, ic.y, ic.z)] = 0xFFFFFFFFu;
+                            }
                         } else if (KIND == K_INJECT) {
                             const vct_gltf_shade_material mat = material_of(A.s, T.meta >> 3);
                             InjRecord upd[6];
@@ -1180,7 +1204,25 @@ __global__ void __launch_bounds__(128, 6) k_cover(const __grid_constant__ Raster
                 __syncwarp();
                 if (last) S[j].done += ci - cx_first;
                 __syncwarp();
-                if constexpr (PHASE == P_WRITE) {
+                if constexpr (PHASE == P_WRITE && !kDealCoveredSamples) {
+                    if (mask) {
+                        const TileSlot& T = S[j];
+                        uint32_t k = rank;
+                        for (uint32_t m = mask; m; m &= m - 1u) {
+                            const int s = __ffs(m) - 1;
+                            float b[3], z;
+                            sample_bz(t, T, ox0 + c_sample_loc8[s][0], oy0 + c_sample_loc8[s][1], b, z);
+                            const float3 p = interp3(b, T.p);
+                            const float3 nn = interp3(b, T.n);
+                            FragDesc d;
+                            d.p = make_float4(p.x, p.y, p.z, __uint_as_float(T.base_r + k * T.per));
+                            d.n = make_float4(nn.x, nn.y, nn.z, __uint_as_float(T.meta));
+                            frags[T.base_f + k] = d;
+                            ++k;
+                        }
+                    }
+                }
+                if constexpr (PHASE == P_WRITE && kDealCoveredSamples) {
                     // the r-th covered sample of a pixel goes to its tile's slot rank + r
                     for_each_covered(mask, lane, [&](bool valid, int o, int s, uint32_t r) {
                         const int jo = __shfl_sync(FULL, j, o), oxo = __shfl_sync(FULL, ox0, o),
