@@ -11,9 +11,10 @@
 
 // Device scratch arena of the raster / SVO passes (vct_workspace), a
 // second buffer that outlives a pass within one frame (the frame's
-// touched-texel bitmap), and a side stream with two events on which a frame
-// runs the opacity passes that are independent of the shadow and injection
-// passes beside them (created on first use, on the device current then).
+// touched-texel bitmap), and a side stream with two events and a workspace
+// of its own, on which a frame runs the passes that are independent of the
+// main stream's work beside them (created on first use, on the device
+// current then).
 struct vct_workspace_s {
     void* ptr = nullptr;
     size_t bytes = 0;
@@ -22,6 +23,7 @@ struct vct_workspace_s {
     cudaStream_t side = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
     int side_device = -1;
+    vct_workspace_s* side_ws = nullptr;  // the scratch of the passes run on the side stream
 };
 
 namespace vct {

@@ -1755,6 +1755,10 @@ extern "C" int vct_workspace_destroy(vct_workspace_s* w) {
     }
     if (w->fork) cudaEventDestroy(w->fork);
     if (w->join) cudaEventDestroy(w->join);
+    if (w->side_ws) {
+        const int rc = vct_workspace_destroy(w->side_ws);
+        if (rc != VCT_OK && e == cudaSuccess) e = cudaErrorUnknown;
+    }
     delete w;
     if (e != cudaSuccess) return cuda_fail(e, "cudaFree (workspace)");
     return VCT_OK;
@@ -2280,6 +2284,7 @@ static cudaStream_t side_stream(vct_workspace_s* ws) {
     ws->fork = a;
     ws->join = b;
     ws->side_device = dev;
+    ws->side_ws = new vct_workspace_s();
     return s;
 }
 
@@ -2322,30 +2327,33 @@ int frame_raster_passes(const vct_scene* scene, const vct_frame_desc* f, const v
     uint32_t* touched = (uint32_t*)ws->aux;
     VCT_CUDA_TRY(cudaMemsetAsync(touched, 0, bm_bytes, st));
     *touched_out = touched;
-    // Two stretches run on the side stream, beside the main stream's work that
-    // does not touch the opacity atlas: the opacity clear beside the shadow
-    // pass, and the opacity mips + border wrap beside the injection's shading,
-    // sort and fold.  The results are those of the serial order.
+    // Two stretches run on the side stream (with its own workspace), beside
+    // main-stream work they share no buffer with: the shadow pass beside the
+    // opacity clear, voxelisation and injection count / emission (the shadow
+    // map is read only by the injection's shading, after the join), and the
+    // opacity mips + border wrap beside the shading, sort and fold.  The
+    // results are those of the serial order.
     cudaStream_t side = side_stream(ws);
-    cudaStream_t ost = side ? side : st;  // the opacity clear's stream
+    cudaStream_t sst = side ? side : st;  // the shadow pass's stream
+    vct_workspace_s* sws = side ? ws->side_ws : ws;
     if (side && (rc = fork_side(ws, side, st)) != VCT_OK) return rc;
     const bool r8 = f->opacity_format == VCT_OPACITY_R8;  // (full revoxelisation only: checked by the caller)
-    if (toroidal) rc = clear_slabs(opacity, R, slabs, slab_levels, nslabs, ost);
-    else if (r8) rc = cudaMemsetAsync(opacity, 0, (size_t)AtlasDims(R).texels(), ost) == cudaSuccess
+    if (toroidal) rc = clear_slabs(opacity, R, slabs, slab_levels, nslabs, stream);
+    else if (r8) rc = cudaMemsetAsync(opacity, 0, (size_t)AtlasDims(R).texels(), st) == cudaSuccess
                           ? VCT_OK : fail(VCT_E_CUDA, "cudaMemsetAsync (opacity clear)");
-    else rc = vct_clear_atlas(opacity, R, ost);
+    else rc = vct_clear_atlas(opacity, R, stream);
     if (rc != VCT_OK) return rc;
     vct_shadow_map sm = {nullptr, 0, 0};
     if (f->shadow_width > 0) {
-        if ((rc = vct_shadow_depth(scene, &f->light_shadow, shadow_depth, f->shadow_width, f->shadow_height, ws,
-                                   stream)) != VCT_OK)
+        if ((rc = vct_shadow_depth(scene, &f->light_shadow, shadow_depth, f->shadow_width, f->shadow_height, sws,
+                                   sst)) != VCT_OK)
             return rc;
         sm.depth = shadow_depth;
         sm.width = f->shadow_width;
         sm.height = f->shadow_height;
     }
     if ((rc = check_scene(scene)) != VCT_OK) return rc;
-    if (side && (rc = join_side(ws, side, st)) != VCT_OK) return rc;
+    cudaStream_t ost = side ? side : st;  // the opacity mips' stream
     InjectState S;
     RasterArgs I;
     memset(&I, 0, sizeof(I));
@@ -2374,6 +2382,8 @@ int frame_raster_passes(const vct_scene* scene, const vct_frame_desc* f, const v
         }
         if (rc != VCT_OK) return rc;
     }
+    // the shading below reads the shadow map; the mips read the voxelised opacity
+    if (side && (rc = join_side(ws, side, st)) != VCT_OK) return rc;
     if (side && (rc = fork_side(ws, side, st)) != VCT_OK) return rc;
     if (r8) {
         if ((rc = opacity_r8_mips(reinterpret_cast<uint8_t*>(opacity), regions, R, ost)) != VCT_OK) return rc;
