@@ -196,6 +196,9 @@ __global__ void k_spec_keys(const __grid_constant__ FastArgs A, const uint32_t* 
 
 constexpr int kWarpsPerBlock = 8;
 
+// Run the specular cones on a second stream beside the diffuse kernel.
+constexpr bool kTraceSideStream = true;
+
 // The diffuse cones, dealt to the lanes of a warp (trace_deal.cuh), each
 // marched by trace_cone_fast.
 struct FastDiffuseMarch {
@@ -638,6 +641,46 @@ static void fill_fast_consts(FastConsts& C, const vct_cone_tracing_desc& d, floa
 
 using namespace vct;
 
+namespace {
+
+// The calling thread's second stream for the fast trace (non-blocking, with a
+// fork and a join event), created on first use on each device; the specular
+// cones run on it beside the diffuse kernel.  Null when it cannot be made
+// (the trace then runs serially on the caller's stream).
+struct TraceSide {
+    int device = -1;
+    cudaStream_t s = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+    ~TraceSide() {
+        if (s) cudaStreamDestroy(s);
+        if (fork) cudaEventDestroy(fork);
+        if (join) cudaEventDestroy(join);
+    }
+};
+
+TraceSide* trace_side() {
+    static thread_local TraceSide side[8];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 8) return nullptr;
+    TraceSide& t = side[dev];
+    if (!t.s) {
+        if (cudaStreamCreateWithFlags(&t.s, cudaStreamNonBlocking) != cudaSuccess) {
+            t.s = nullptr;
+            return nullptr;
+        }
+        if (cudaEventCreateWithFlags(&t.fork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&t.join, cudaEventDisableTiming) != cudaSuccess) {
+            cudaStreamDestroy(t.s);
+            t.s = nullptr;
+            return nullptr;
+        }
+        t.device = dev;
+    }
+    return &t;
+}
+
+}  // namespace
+
 extern "C" int64_t vct_cone_trace_fast_scratch_bytes(int64_t n) {
     if (n < 0 || n > 0x7fffffffLL) return -1;
     FastScratch s;
@@ -705,18 +748,30 @@ extern "C" int vct_cone_trace_fast_opt(const vct_cone_tracing_desc* desc, const 
         return VCT_OK;
     }
     const int grid_k = (int)(gd > 152 * 16 ? 152 * 16 : gd);
-    k_spec_keys<<<grid_k, 256, 0, st>>>(A, S.order, S.spec_key, S.spec_count);
+    // the specular classification, partition and cones on the second stream,
+    // beside the diffuse kernel (they share only the sorted order, read-only)
+    TraceSide* side = kTraceSideStream ? trace_side() : nullptr;
+    cudaStream_t ss = side ? side->s : st;
+    if (side) {
+        VCT_CUDA_TRY(cudaEventRecord(side->fork, st));
+        VCT_CUDA_TRY(cudaStreamWaitEvent(ss, side->fork, 0));
+    }
+    k_spec_keys<<<grid_k, 256, 0, ss>>>(A, S.order, S.spec_key, S.spec_count);
     VCT_LAUNCH_CHECK();
     tb = S.temp_bytes;
     // stable partition (one radix pass on bit 8): specular samples first, Morton order kept
     VCT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(S.temp, tb, S.spec_key, S.spec_key_out, S.order, S.spec_list, (int)n,
-                                                 8, 9, st));
+                                                 8, 9, ss));
     int64_t gw = (n * 32 + 255) / 256;
     const int grid_s = (int)(gw > 152 * 64 ? 152 * 64 : gw);
+    k_trace_specular_warp<<<grid_s, 256, 0, ss>>>(A, S.spec_list, S.spec_count);
+    VCT_LAUNCH_CHECK();
     k_trace_diffuse<<<grid_d, 256, 0, st>>>(A, S.order);
     VCT_LAUNCH_CHECK();
-    k_trace_specular_warp<<<grid_s, 256, 0, st>>>(A, S.spec_list, S.spec_count);
-    VCT_LAUNCH_CHECK();
+    if (side) {
+        VCT_CUDA_TRY(cudaEventRecord(side->join, ss));
+        VCT_CUDA_TRY(cudaStreamWaitEvent(st, side->join, 0));
+    }
     return VCT_OK;
 }
 
