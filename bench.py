@@ -290,6 +290,9 @@ def run_ours(args, world, rank, local):
     trace(samples, steps_ctr)
     torch.cuda.synchronize()
     cone_samples = int(steps_ctr.item())
+    # the launch-shape autotuner (result-neutral shapes) on these inputs, before the timed steps
+    tuning = clipmap.autotune_fast(desc, EYE, tex, samples, light=light, shadow=shadow, shadow_desc=lsd,
+                                   diffuse=dout, specular=sout, scratch=scratch) if tex is not None else None
     for _ in range(args.warmup):
         trace(samples)
     if world > 1:
@@ -505,7 +508,7 @@ def run_ours(args, world, rank, local):
                                    "1920x1080 G-buffer samples, 16 diffuse + 1 specular cone + VXAO",
                        "form": args.form, "R": R, "samples_per_step": n, "cone_samples_per_step": cone_samples,
                        "l2": "inputs larger than L2 (2.47 GB clipmap)",
-                       "texture_full_copy_ms": refresh_ms,
+                       "texture_full_copy_ms": refresh_ms, "trace_tuning": tuning,
                        "texture": "kept current by the frame's copy-alpha and mip passes" if frame_tex is not None
                        else ("kept current by the frame's FP16 conversion and FP16 mip passes" if tex is not None
                              else "none (linear atlas)"),

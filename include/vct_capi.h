@@ -441,6 +441,39 @@ int vct_cone_trace_tex(const vct_cone_tracing_desc* desc, const vct_cam_matrix* 
                        int64_t sample_count, float* diffuse_out, float* specular_out, unsigned long long* cone_steps,
                        const vct_trace_options* options, void* stream);
 
+/* Launch shape of vct_cone_trace_fast: the diffuse and specular kernels'
+ * grids in blocks (of 256 threads) per SM.  Every shape gives the same
+ * results bit for bit (grid-stride loops; no per-warp state crosses work
+ * items), so tuning changes only the time. */
+typedef struct vct_trace_tuning {
+    int32_t diffuse_blocks_per_sm;  /* default 8 */
+    int32_t specular_blocks_per_sm; /* default 64 */
+    float trace_ms;                 /* autotune: the chosen shape's median time on the tuning inputs */
+    float default_ms;               /* autotune: the default shape's */
+    int32_t tuned;                  /* 1 when the shape comes from vct_cone_trace_fast_autotune */
+    int32_t reserved;
+} vct_trace_tuning;
+
+/* Autotuner of the fast trace (no counterpart in the reference): times the
+ * trace of the given inputs (its arguments are vct_cone_trace_fast's; the
+ * outputs receive the trace's results) under the default shape and a few
+ * others -- specular grids of 16/32/64/128 blocks per SM, then diffuse grids of
+ * 4/8/16 with the best of those -- with CUDA events on `stream` (median of
+ * three after a warm-up; the call synchronises), and keeps the fastest for
+ * this device and the texture's clipmap resolution: later vct_cone_trace_fast
+ * calls there launch with it.  A context created with VCT_CONTEXT_AUTOTUNE
+ * runs it on its first trace. */
+int vct_cone_trace_fast_autotune(const vct_cone_tracing_desc* desc, const vct_cam_matrix* cam, vct_texture radiance,
+                                 const vct_shadow_map* shadow, const vct_directional_light_desc* light,
+                                 const vct_directional_light_shadow_desc* light_shadow,
+                                 const vct_surface_sample* samples, int64_t sample_count, float* diffuse_out,
+                                 float* specular_out, void* scratch, size_t scratch_bytes, vct_trace_tuning* out,
+                                 void* stream);
+/* The shape vct_cone_trace_fast uses at resolution R on the current device. */
+int vct_trace_tuning_get(int32_t R, vct_trace_tuning* out);
+/* Forget every tuned shape (back to the defaults). */
+int vct_trace_tuning_reset(void);
+
 /* One trace of a batch: the arguments of vct_cone_trace_fast for one
  * clipmap (its radiance texture, desc, camera eye, lighting) and one sample
  * set with its outputs.  Host struct; the pointers are device pointers. */
@@ -709,9 +742,17 @@ typedef struct vct_config {
     int32_t clipmap_resolution; /* R: power of two in [8, 1024] (the reference's DEFAULT_VOXEL_RESOLUTION) */
     int32_t shadow_width;       /* light depth map size; 0 x 0 = no shadow pass (visibility 1) */
     int32_t shadow_height;
-    int32_t reserved;
+    int32_t flags;              /* VCT_CONTEXT_* bits, 0 = the reference's behaviour */
     size_t workspace_bytes;     /* initial raster workspace (grows on demand) */
 } vct_config;
+
+/* vct_config.flags: AUTOTUNE -- the context's first trace runs
+ * vct_cone_trace_fast_autotune unless its resolution is already tuned on the
+ * device; OPACITY_R8 -- the context's opacity atlas is the one-byte form
+ * (VCT_OPACITY_R8: frames with the full revoxelisation and the deterministic
+ * injection only). */
+#define VCT_CONTEXT_AUTOTUNE 1
+#define VCT_CONTEXT_OPACITY_R8 2
 
 typedef struct vct_context_s* vct_context;
 
@@ -886,5 +927,6 @@ VCT_STATIC_ASSERT(sizeof(vct_gltf_shade_material) == 80, "GltfShadeMaterial is 8
 VCT_STATIC_ASSERT(sizeof(vct_surface_sample) == 80, "surface sample is 80 B");
 VCT_STATIC_ASSERT(sizeof(vct_trace_options) == 16, "vct_trace_options is 16 B");
 VCT_STATIC_ASSERT(sizeof(vct_trace_job) == 296, "vct_trace_job is 296 B");
+VCT_STATIC_ASSERT(sizeof(vct_trace_tuning) == 24, "vct_trace_tuning is 24 B");
 
 #endif /* VCT_CAPI_H */

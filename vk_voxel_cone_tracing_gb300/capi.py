@@ -38,6 +38,8 @@ INJECT_ATOMIC = 1
 
 REVOX_FULL = 0
 REVOX_TOROIDAL = 1
+CONTEXT_AUTOTUNE = 1
+CONTEXT_OPACITY_R8 = 2
 OPACITY_RGBA8 = 0
 OPACITY_R8 = 1
 
@@ -154,7 +156,12 @@ class ShadowMap(C.Structure):
 
 class Config(C.Structure):
     _fields_ = [("clipmap_resolution", C.c_int32), ("shadow_width", C.c_int32), ("shadow_height", C.c_int32),
-                ("reserved", C.c_int32), ("workspace_bytes", C.c_size_t)]
+                ("flags", C.c_int32), ("workspace_bytes", C.c_size_t)]
+
+
+class TraceTuning(C.Structure):
+    _fields_ = [("diffuse_blocks_per_sm", C.c_int32), ("specular_blocks_per_sm", C.c_int32), ("trace_ms", C.c_float),
+                ("default_ms", C.c_float), ("tuned", C.c_int32), ("reserved", C.c_int32)]
 
 
 class ContextBuffers(C.Structure):
@@ -183,7 +190,7 @@ STRUCT_SIZES = {
     ClipmapRegion: 28, VoxelizationDesc: 64, DownSampleDesc: 24, ImageCleaningDesc: 36, CopyAlphaDesc: 12,
     BorderWrappingDesc: 16, ConeTracingDesc: 52, CamMatrix: 144, DirectionalLightDesc: 32,
     DirectionalLightShadowDesc: 136, GltfShadeMaterial: 80, Scene: 104, SpecularFilterDesc: 16, Config: 24,
-    ContextBuffers: 216, BatchJob: 264, AdamDesc: 40, TraceOptions: 16, TraceJob: 296,
+    ContextBuffers: 216, BatchJob: 264, AdamDesc: 40, TraceOptions: 16, TraceJob: 296, TraceTuning: 24,
 }
 
 # Every entry point of include/vct_capi.h: name -> (restype, argtypes).
@@ -204,6 +211,9 @@ _SIGS: dict[str, tuple] = {
     "vct_cone_trace": (C.c_int, [P, P, P, C.c_int32, P, P, P, P, C.c_int64, P, P, P, P]),
     "vct_cone_trace_opt": (C.c_int, [P, P, P, C.c_int32, P, P, P, P, C.c_int64, P, P, P, P, P]),
     "vct_cone_trace_tex": (C.c_int, [P, P, P, P, P, P, P, C.c_int64, P, P, P, P, P]),
+    "vct_cone_trace_fast_autotune": (C.c_int, [P, P, P, P, P, P, P, C.c_int64, P, P, P, C.c_size_t, P, P]),
+    "vct_trace_tuning_get": (C.c_int, [C.c_int32, P]),
+    "vct_trace_tuning_reset": (C.c_int, []),
     "vct_cone_trace_f32": (C.c_int, [P, P, P, C.c_int32, P, P, P, P, C.c_int64, P, P, P, P]),
     "vct_cone_trace_backward": (C.c_int, [P, P, P, C.c_int32, P, P, P, P, C.c_int64, P, P, P, P]),
     "vct_downsample_f32": (C.c_int, [P, P, C.c_int32, P]),

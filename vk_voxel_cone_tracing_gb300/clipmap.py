@@ -263,6 +263,41 @@ def cone_trace_fast(desc: capi.ConeTracingDesc, eye, tex: RadianceTexture, sampl
     return diffuse, specular
 
 
+def autotune_fast(desc: capi.ConeTracingDesc, eye, tex: RadianceTexture, samples: torch.Tensor,
+                  light: capi.DirectionalLightDesc | None = None, shadow: torch.Tensor | None = None,
+                  shadow_desc: capi.DirectionalLightShadowDesc | None = None, diffuse: torch.Tensor | None = None,
+                  specular: torch.Tensor | None = None, scratch: torch.Tensor | None = None) -> dict:
+    """vct_cone_trace_fast_autotune: times the fast trace of these inputs under a few launch shapes (the results
+    are the same under every shape) and keeps the fastest for this device and the texture's resolution."""
+    n = samples.shape[0]
+    if diffuse is None:
+        diffuse = torch.zeros((n, 4), dtype=torch.float32, device=samples.device)
+    if specular is None:
+        specular = torch.zeros((n, 4), dtype=torch.float32, device=samples.device)
+    if scratch is None:
+        scratch = fast_scratch(n, samples.device)
+    base = _aligned(scratch)
+    cam = cam_matrix(eye)
+    light = light or capi.DirectionalLightDesc(capi.f3(0.3, -1.0, 0.2), 1.0, capi.f3(1, 1, 1), 0)
+    sm = capi.ShadowMap(shadow.data_ptr(), shadow.shape[1], shadow.shape[0]) if shadow is not None else \
+        capi.ShadowMap(None, 0, 0)
+    sd = shadow_desc or capi.DirectionalLightShadowDesc()
+    t = capi.TraceTuning()
+    capi.call("vct_cone_trace_fast_autotune", capi.ref(desc), capi.ref(cam), tex.handle, capi.ref(sm), capi.ref(light),
+              capi.ref(sd), _ptr(samples), n, _ptr(diffuse), _ptr(specular), C.c_void_p(base),
+              scratch.data_ptr() + scratch.numel() - base, capi.ref(t), _stream())
+    return {"diffuse_blocks_per_sm": t.diffuse_blocks_per_sm, "specular_blocks_per_sm": t.specular_blocks_per_sm,
+            "trace_ms": t.trace_ms, "default_ms": t.default_ms}
+
+
+def trace_tuning(R: int) -> dict:
+    """vct_trace_tuning_get: the launch shape the fast trace uses at resolution R on the current device."""
+    t = capi.TraceTuning()
+    capi.call("vct_trace_tuning_get", R, capi.ref(t))
+    return {"diffuse_blocks_per_sm": t.diffuse_blocks_per_sm, "specular_blocks_per_sm": t.specular_blocks_per_sm,
+            "tuned": bool(t.tuned)}
+
+
 def trace_job(desc: capi.ConeTracingDesc, eye, tex: RadianceTexture, samples: torch.Tensor,
               diffuse: torch.Tensor, specular: torch.Tensor, light: capi.DirectionalLightDesc | None = None,
               shadow: torch.Tensor | None = None, shadow_desc: capi.DirectionalLightShadowDesc | None = None,

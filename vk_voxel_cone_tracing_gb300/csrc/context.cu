@@ -84,12 +84,24 @@ extern "C" int vct_create(const vct_config* cfg, vct_context_s** out) {
     VCT_CHECK_ARG(cfg->shadow_width >= 0 && cfg->shadow_height >= 0 && cfg->shadow_width <= 16384 &&
                       cfg->shadow_height <= 16384 && ((cfg->shadow_width == 0) == (cfg->shadow_height == 0)),
                   "vct_create: bad shadow map size");
+    VCT_CHECK_ARG((cfg->flags & ~(VCT_CONTEXT_AUTOTUNE | VCT_CONTEXT_OPACITY_R8)) == 0, "vct_create: unknown flags");
     auto* c = new vct_context_s();
     c->cfg = *cfg;
     const int R = cfg->clipmap_resolution;
     int rc = VCT_OK;
-    if ((rc = vct_atlas_alloc(R, VCT_TEX_RGBA8, (void**)&c->opacity)) != VCT_OK ||
-        (rc = vct_atlas_alloc(R, VCT_TEX_RGBA8, (void**)&c->radiance)) != VCT_OK ||
+    if (cfg->flags & VCT_CONTEXT_OPACITY_R8) {  // one byte per texel, zeroed like a fresh atlas
+        const size_t bytes = (size_t)AtlasDims(R).texels();
+        cudaError_t e = cudaMalloc((void**)&c->opacity, bytes);
+        if (e == cudaSuccess) e = cudaMemset(c->opacity, 0, bytes);
+        if (e != cudaSuccess) {
+            release(c);
+            return cuda_fail(e, "cudaMalloc / cudaMemset (R8 opacity atlas)");
+        }
+    } else if ((rc = vct_atlas_alloc(R, VCT_TEX_RGBA8, (void**)&c->opacity)) != VCT_OK) {
+        release(c);
+        return rc;
+    }
+    if ((rc = vct_atlas_alloc(R, VCT_TEX_RGBA8, (void**)&c->radiance)) != VCT_OK ||
         (rc = vct_texture_create(R, VCT_TEX_RGBA8, &c->texture)) != VCT_OK ||
         (rc = vct_workspace_create(cfg->workspace_bytes, &c->ws)) != VCT_OK) {
         release(c);
@@ -148,6 +160,7 @@ extern "C" int vct_context_frame(vct_context_s* c, const vct_scene* scene, const
     f.light = *light;
     f.light_shadow = *light_shadow;
     f.radiance_texture = c->texture;
+    f.opacity_format = (c->cfg.flags & VCT_CONTEXT_OPACITY_R8) ? VCT_OPACITY_R8 : VCT_OPACITY_RGBA8;
     // the first frame of an instance is always a full revoxelisation
     f.revoxelization = (revoxelization == VCT_REVOX_TOROIDAL && c->have_regions) ? VCT_REVOX_TOROIDAL : VCT_REVOX_FULL;
     f.regions_state = c->regions;
@@ -187,6 +200,15 @@ extern "C" int vct_context_trace(vct_context_s* c, const vct_cone_tracing_desc* 
     d.voxel_size = r0.voxel_size;
     d.volume_dimension = (float)c->cfg.clipmap_resolution;
     vct_shadow_map sm = {c->shadow, c->cfg.shadow_width, c->cfg.shadow_height};
+    if ((c->cfg.flags & VCT_CONTEXT_AUTOTUNE) && sample_count > 0) {
+        vct_trace_tuning t;
+        int rc = vct_trace_tuning_get(c->cfg.clipmap_resolution, &t);
+        if (rc == VCT_OK && !t.tuned)
+            rc = vct_cone_trace_fast_autotune(&d, cam, c->texture, c->shadow ? &sm : nullptr, light, light_shadow,
+                                              samples, sample_count, diffuse_out, specular_out, c->scratch,
+                                              c->scratch_bytes, &t, stream);
+        if (rc != VCT_OK) return rc;
+    }
     return vct_cone_trace_fast(&d, cam, c->texture, c->shadow ? &sm : nullptr, light, light_shadow, samples,
                                sample_count, diffuse_out, specular_out, cone_steps, c->scratch, c->scratch_bytes,
                                stream);

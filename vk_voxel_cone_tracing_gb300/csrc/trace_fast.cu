@@ -19,6 +19,7 @@
 // Scratch memory (sort keys, orders, cub temporary storage) is provided by
 // the caller; vct_cone_trace_fast_scratch_bytes() gives its size.
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include <cub/cub.cuh>
@@ -699,55 +700,65 @@ extern "C" int vct_cone_trace_fast(const vct_cone_tracing_desc* desc, const vct_
                                    cone_steps, nullptr, scratch, scratch_bytes, stream);
 }
 
-extern "C" int vct_cone_trace_fast_opt(const vct_cone_tracing_desc* desc, const vct_cam_matrix* cam,
-                                       vct_texture_s* radiance, const vct_shadow_map* shadow,
-                                       const vct_directional_light_desc* light,
-                                       const vct_directional_light_shadow_desc* light_shadow,
-                                       const vct_surface_sample* samples, int64_t n, float* dout, float* sout,
-                                       unsigned long long* cone_steps, const vct_trace_options* options,
-                                       void* scratch, size_t scratch_bytes, void* stream) {
-    vct::NvtxRange nvtx_range("vct_cone_trace_fast");
-    VCT_CHECK_ARG(radiance, "vct_cone_trace_fast: null radiance texture");
-    VCT_CHECK_ARG(n >= 0 && n <= 0x7fffffffLL, "vct_cone_trace_fast: sample count out of range");
-    if (n == 0) return VCT_OK;
-    VCT_CHECK_ARG(samples && dout && sout, "vct_cone_trace_fast: null sample or output buffer");
-    VCT_CHECK_ARG(((uintptr_t)samples & 15) == 0 && ((uintptr_t)dout & 15) == 0 && ((uintptr_t)sout & 15) == 0,
-                  "vct_cone_trace_fast: sample/output buffers must be 16-byte aligned");
-    VCT_CHECK_ARG(scratch && ((uintptr_t)scratch & 255) == 0, "vct_cone_trace_fast: scratch must be 256-byte aligned");
-    FastArgs A;
-    int rc = fill_trace_params(A.P, desc, cam, shadow, light, light_shadow);
-    if (rc != VCT_OK) return rc;
-    if ((rc = apply_trace_options(A.P, options)) != VCT_OK) return rc;
-    VCT_CHECK_ARG((float)texture_resolution(radiance) == desc->volume_dimension,
-                  "vct_cone_trace_fast: volume dimension differs from the texture's clipmap resolution");
-    FastScratch S;
-    rc = plan_scratch(n, scratch, S);
-    if (rc != VCT_OK) return rc;
-    VCT_CHECK_ARG(scratch_bytes >= S.total, "vct_cone_trace_fast: scratch buffer too small");
-    fill_fast_consts(A.C, *desc, A.P.diffuse_aperture);
-    A.tex = texture_object(radiance);
-    A.samples = samples;
-    A.n = n;
-    A.dout = dout;
-    A.sout = sout;
-    A.steps = cone_steps;
-    cudaStream_t st = as_stream(stream);
+namespace {
+
+// Launch shape of the fast trace: the grids of the diffuse and specular
+// kernels in blocks (of 256 threads) per SM.  Result-neutral: both kernels
+// are grid-stride loops in which a sample's diffuse item and a specular cone
+// get the same arithmetic whichever warp takes them, and the step counter is
+// an integer sum.
+struct FastShape {
+    int diffuse_per_sm = 8, specular_per_sm = 64;
+};
+
+int sm_count() {
+    static int counts[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+    if (!counts[dev]) {
+        int c = 0;
+        if (cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || c <= 0) c = 152;
+        counts[dev] = c;
+    }
+    return counts[dev];
+}
+
+// Shapes chosen by vct_cone_trace_fast_autotune, per (device, log2 R).
+std::mutex g_shape_mutex;
+FastShape g_shapes[8][11];
+bool g_tuned[8][11];
+
+int log2_res(int R) { return 31 - __builtin_clz((unsigned)R); }
+
+FastShape fast_shape(int R) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 8) return FastShape{};
+    std::lock_guard<std::mutex> lock(g_shape_mutex);
+    const int l = log2_res(R);
+    return g_tuned[dev][l] ? g_shapes[dev][l] : FastShape{};
+}
+
+// The trace pipeline after argument checks: Morton keys and sort, specular
+// classification and partition, the diffuse and specular kernels.
+int launch_fast(const FastArgs& A, const FastScratch& S, int64_t n, FastShape sh, cudaStream_t st) {
+    const int sms = sm_count();
     const int block = 256;
     int64_t g = (n + block - 1) / block;
-    const int grid_keys = (int)(g > 152 * 32 ? 152 * 32 : g);
-    k_morton_keys<<<grid_keys, block, 0, st>>>(samples, n, A.C, S.keys_in, S.vals_in);
+    const int grid_keys = (int)(g > (int64_t)sms * 32 ? (int64_t)sms * 32 : g);
+    k_morton_keys<<<grid_keys, block, 0, st>>>(A.samples, n, A.C, S.keys_in, S.vals_in);
     VCT_LAUNCH_CHECK();
     size_t tb = S.temp_bytes;
     VCT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(S.temp, tb, S.keys_in, S.keys_out, S.vals_in, S.order, (int)n, 0, 30, st));
     VCT_CUDA_TRY(cudaMemsetAsync(S.spec_count, 0, sizeof(unsigned int), st));
     int64_t gd = (n + 255) / 256;
-    const int grid_d = (int)(gd > 152 * 8 ? 152 * 8 : gd);
+    const int64_t cap_d = (int64_t)sms * sh.diffuse_per_sm;
+    const int grid_d = (int)(gd > cap_d ? cap_d : gd);
     if (!A.C.need_specular) {
         k_trace_diffuse<<<grid_d, 256, 0, st>>>(A, S.order);
         VCT_LAUNCH_CHECK();
         return VCT_OK;
     }
-    const int grid_k = (int)(gd > 152 * 16 ? 152 * 16 : gd);
+    const int grid_k = (int)(gd > (int64_t)sms * 16 ? (int64_t)sms * 16 : gd);
     // the specular classification, partition and cones on the second stream,
     // beside the diffuse kernel (they share only the sorted order, read-only)
     TraceSide* side = kTraceSideStream ? trace_side() : nullptr;
@@ -763,7 +774,8 @@ extern "C" int vct_cone_trace_fast_opt(const vct_cone_tracing_desc* desc, const 
     VCT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(S.temp, tb, S.spec_key, S.spec_key_out, S.order, S.spec_list, (int)n,
                                                  8, 9, ss));
     int64_t gw = (n * 32 + 255) / 256;
-    const int grid_s = (int)(gw > 152 * 64 ? 152 * 64 : gw);
+    const int64_t cap_s = (int64_t)sms * sh.specular_per_sm;
+    const int grid_s = (int)(gw > cap_s ? cap_s : gw);
     k_trace_specular_warp<<<grid_s, 256, 0, ss>>>(A, S.spec_list, S.spec_count);
     VCT_LAUNCH_CHECK();
     k_trace_diffuse<<<grid_d, 256, 0, st>>>(A, S.order);
@@ -772,6 +784,161 @@ extern "C" int vct_cone_trace_fast_opt(const vct_cone_tracing_desc* desc, const 
         VCT_CUDA_TRY(cudaEventRecord(side->join, ss));
         VCT_CUDA_TRY(cudaStreamWaitEvent(st, side->join, 0));
     }
+    return VCT_OK;
+}
+
+// Argument checks and the kernels' argument block of one fast trace.
+int prepare_fast(const vct_cone_tracing_desc* desc, const vct_cam_matrix* cam, vct_texture_s* radiance,
+                 const vct_shadow_map* shadow, const vct_directional_light_desc* light,
+                 const vct_directional_light_shadow_desc* light_shadow, const vct_surface_sample* samples, int64_t n,
+                 float* dout, float* sout, unsigned long long* cone_steps, const vct_trace_options* options,
+                 void* scratch, size_t scratch_bytes, FastArgs& A, FastScratch& S) {
+    VCT_CHECK_ARG(samples && dout && sout, "vct_cone_trace_fast: null sample or output buffer");
+    VCT_CHECK_ARG(((uintptr_t)samples & 15) == 0 && ((uintptr_t)dout & 15) == 0 && ((uintptr_t)sout & 15) == 0,
+                  "vct_cone_trace_fast: sample/output buffers must be 16-byte aligned");
+    VCT_CHECK_ARG(scratch && ((uintptr_t)scratch & 255) == 0, "vct_cone_trace_fast: scratch must be 256-byte aligned");
+    int rc = fill_trace_params(A.P, desc, cam, shadow, light, light_shadow);
+    if (rc != VCT_OK) return rc;
+    if ((rc = apply_trace_options(A.P, options)) != VCT_OK) return rc;
+    VCT_CHECK_ARG((float)texture_resolution(radiance) == desc->volume_dimension,
+                  "vct_cone_trace_fast: volume dimension differs from the texture's clipmap resolution");
+    rc = plan_scratch(n, scratch, S);
+    if (rc != VCT_OK) return rc;
+    VCT_CHECK_ARG(scratch_bytes >= S.total, "vct_cone_trace_fast: scratch buffer too small");
+    fill_fast_consts(A.C, *desc, A.P.diffuse_aperture);
+    A.tex = texture_object(radiance);
+    A.samples = samples;
+    A.n = n;
+    A.dout = dout;
+    A.sout = sout;
+    A.steps = cone_steps;
+    return VCT_OK;
+}
+
+}  // namespace
+
+extern "C" int vct_cone_trace_fast_opt(const vct_cone_tracing_desc* desc, const vct_cam_matrix* cam,
+                                       vct_texture_s* radiance, const vct_shadow_map* shadow,
+                                       const vct_directional_light_desc* light,
+                                       const vct_directional_light_shadow_desc* light_shadow,
+                                       const vct_surface_sample* samples, int64_t n, float* dout, float* sout,
+                                       unsigned long long* cone_steps, const vct_trace_options* options,
+                                       void* scratch, size_t scratch_bytes, void* stream) {
+    vct::NvtxRange nvtx_range("vct_cone_trace_fast");
+    VCT_CHECK_ARG(radiance, "vct_cone_trace_fast: null radiance texture");
+    VCT_CHECK_ARG(n >= 0 && n <= 0x7fffffffLL, "vct_cone_trace_fast: sample count out of range");
+    if (n == 0) return VCT_OK;
+    FastArgs A;
+    FastScratch S;
+    int rc = prepare_fast(desc, cam, radiance, shadow, light, light_shadow, samples, n, dout, sout, cone_steps,
+                          options, scratch, scratch_bytes, A, S);
+    if (rc != VCT_OK) return rc;
+    return launch_fast(A, S, n, fast_shape(texture_resolution(radiance)), as_stream(stream));
+}
+
+extern "C" int vct_cone_trace_fast_autotune(const vct_cone_tracing_desc* desc, const vct_cam_matrix* cam,
+                                            vct_texture_s* radiance, const vct_shadow_map* shadow,
+                                            const vct_directional_light_desc* light,
+                                            const vct_directional_light_shadow_desc* light_shadow,
+                                            const vct_surface_sample* samples, int64_t n, float* dout, float* sout,
+                                            void* scratch, size_t scratch_bytes, vct_trace_tuning* out,
+                                            void* stream) {
+    vct::NvtxRange nvtx_range("vct_cone_trace_fast_autotune");
+    VCT_CHECK_ARG(radiance && out, "vct_cone_trace_fast_autotune: null argument");
+    VCT_CHECK_ARG(n > 0 && n <= 0x7fffffffLL, "vct_cone_trace_fast_autotune: sample count out of range");
+    int dev = 0;
+    VCT_CUDA_TRY(cudaGetDevice(&dev));
+    VCT_CHECK_ARG(dev >= 0 && dev < 8, "vct_cone_trace_fast_autotune: device index above 7");
+    FastArgs A;
+    FastScratch S;
+    int rc = prepare_fast(desc, cam, radiance, shadow, light, light_shadow, samples, n, dout, sout, nullptr,
+                          nullptr, scratch, scratch_bytes, A, S);
+    if (rc != VCT_OK) return rc;
+    cudaStream_t st = as_stream(stream);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    VCT_CUDA_TRY(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return fail(VCT_E_CUDA, "vct_cone_trace_fast_autotune: cudaEventCreate");
+    }
+    // median of three timed traces after one warm-up, per shape
+    auto time_shape = [&](FastShape sh, float* ms) -> int {
+        float t[3];
+        for (int k = -1; k < 3; ++k) {
+            if (k >= 0 && cudaEventRecord(e0, st) != cudaSuccess) return fail(VCT_E_CUDA, "cudaEventRecord");
+            int r = launch_fast(A, S, n, sh, st);
+            if (r != VCT_OK) return r;
+            if (k >= 0) {
+                if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                    cudaEventElapsedTime(&t[k], e0, e1) != cudaSuccess)
+                    return fail(VCT_E_CUDA, "vct_cone_trace_fast_autotune: event timing");
+            }
+        }
+        const float lo = fminf(t[0], fminf(t[1], t[2])), hi = fmaxf(t[0], fmaxf(t[1], t[2]));
+        *ms = t[0] + t[1] + t[2] - lo - hi;
+        return VCT_OK;
+    };
+    // the specular grid first (the larger kernel), then the diffuse grid with it
+    const int spec_c[] = {16, 32, 64, 128}, diff_c[] = {4, 8, 16};
+    FastShape best;
+    float best_ms = 0.0f, default_ms = 0.0f;
+    rc = time_shape(best, &default_ms);
+    best_ms = default_ms;
+    for (int i = 0; rc == VCT_OK && i < 4; ++i) {
+        FastShape c = best;
+        c.specular_per_sm = spec_c[i];
+        if (c.specular_per_sm == best.specular_per_sm && c.diffuse_per_sm == best.diffuse_per_sm) continue;
+        float ms = 0.0f;
+        rc = time_shape(c, &ms);
+        if (rc == VCT_OK && ms < best_ms) best = c, best_ms = ms;
+    }
+    for (int i = 0; rc == VCT_OK && A.C.need_diffuse && i < 3; ++i) {
+        FastShape c = best;
+        c.diffuse_per_sm = diff_c[i];
+        if (c.diffuse_per_sm == best.diffuse_per_sm) continue;
+        float ms = 0.0f;
+        rc = time_shape(c, &ms);
+        if (rc == VCT_OK && ms < best_ms) best = c, best_ms = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != VCT_OK) return rc;
+    {
+        std::lock_guard<std::mutex> lock(g_shape_mutex);
+        const int l = log2_res(texture_resolution(radiance));
+        g_shapes[dev][l] = best;
+        g_tuned[dev][l] = true;
+    }
+    out->diffuse_blocks_per_sm = best.diffuse_per_sm;
+    out->specular_blocks_per_sm = best.specular_per_sm;
+    out->trace_ms = best_ms;
+    out->default_ms = default_ms;
+    out->tuned = 1;
+    out->reserved = 0;
+    return VCT_OK;
+}
+
+extern "C" int vct_trace_tuning_get(int32_t R, vct_trace_tuning* out) {
+    VCT_CHECK_ARG(out && valid_resolution(R), "vct_trace_tuning_get: bad argument");
+    int dev = 0;
+    VCT_CUDA_TRY(cudaGetDevice(&dev));
+    const FastShape sh = fast_shape(R);
+    out->diffuse_blocks_per_sm = sh.diffuse_per_sm;
+    out->specular_blocks_per_sm = sh.specular_per_sm;
+    out->trace_ms = 0.0f;
+    out->default_ms = 0.0f;
+    {
+        std::lock_guard<std::mutex> lock(g_shape_mutex);
+        out->tuned = dev >= 0 && dev < 8 && g_tuned[dev][log2_res(R)] ? 1 : 0;
+    }
+    out->reserved = 0;
+    return VCT_OK;
+}
+
+extern "C" int vct_trace_tuning_reset(void) {
+    std::lock_guard<std::mutex> lock(g_shape_mutex);
+    for (auto& row : g_tuned)
+        for (bool& t : row) t = false;
     return VCT_OK;
 }
 

@@ -16,12 +16,15 @@ from .clipmap import _ptr, _stream
 
 
 class Context:
-    def __init__(self, R: int, shadow_size: int = 2048, workspace_bytes: int = 0):
-        cfg = capi.Config(R, shadow_size, shadow_size, 0, workspace_bytes)
+    def __init__(self, R: int, shadow_size: int = 2048, workspace_bytes: int = 0, flags: int = 0):
+        """`flags`: capi.CONTEXT_AUTOTUNE (tune the fast trace's launch shape on the first trace),
+        capi.CONTEXT_OPACITY_R8 (one-byte opacity atlas)."""
+        cfg = capi.Config(R, shadow_size, shadow_size, flags, workspace_bytes)
         h = C.c_void_p()
         capi.call("vct_create", capi.ref(cfg), C.byref(h))
         self.handle = h
         self.R = R
+        self.flags = flags
 
     def buffers(self) -> capi.ContextBuffers:
         b = capi.ContextBuffers()
@@ -29,10 +32,13 @@ class Context:
         return b
 
     def atlas(self, which: str) -> torch.Tensor:
-        """A torch view of the instance's opacity or radiance atlas (int32, [D, H, W])."""
+        """A torch view of the instance's opacity or radiance atlas (int32, [D, H, W]; a CONTEXT_OPACITY_R8
+        context's opacity atlas as uint8)."""
         b = self.buffers()
         ptr = b.opacity if which == "opacity" else b.radiance
         D, H, W = self.R + 2, 6 * (self.R + 2), 6 * (self.R + 2)
+        if which == "opacity" and self.flags & capi.CONTEXT_OPACITY_R8:
+            return _device_view(ptr, (D, H, W), "|u1")
         return _device_view(ptr, (D, H, W))
 
     def reset(self) -> None:
@@ -70,13 +76,13 @@ class Context:
             pass
 
 
-def _device_view(ptr: int, shape) -> torch.Tensor:
-    """A torch int32 tensor over device memory owned by the library (no copy)."""
+def _device_view(ptr: int, shape, typestr: str = "<i4") -> torch.Tensor:
+    """A torch tensor (int32 unless `typestr` says otherwise) over device memory owned by the library (no copy)."""
     import numpy as np
     n = int(np.prod(shape))
 
     class _Iface:
-        __cuda_array_interface__ = {"shape": tuple(shape), "typestr": "<i4", "data": (int(ptr), False),
+        __cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr, "data": (int(ptr), False),
                                     "version": 2, "strides": None}
     t = torch.as_tensor(_Iface(), device="cuda")
     assert t.numel() == n
