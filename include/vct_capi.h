@@ -12,7 +12,14 @@
  * cudaFreeAsync before the call returns) in the per-sample traces
  * (vct_cone_trace, vct_cone_trace_f32, vct_cone_trace_backward,
  * vct_svo_cone_trace: the samples' processing order) and vct_sq_error.
- * vct_gather_probe allocates and frees a small device buffer and two events.
+ * vct_gather_probe allocates and frees a small device buffer and two events,
+ * vct_cone_trace_fast_autotune two events.  vct_cone_trace_fast (and the
+ * calls built on it) creates, on its first call in a thread on a device, one
+ * non-blocking stream and two events for that thread, kept until the thread
+ * ends: the specular cones run on it beside the diffuse kernel, joined back
+ * to the caller's stream before the call returns.  A raster workspace
+ * (vct_workspace) likewise creates a side stream, two events and a second
+ * workspace on first use by vct_clipmap_frame.
  * vct_cone_trace_fast_noalloc never calls cudaMalloc: its scratch is a static
  * device array that the runtime commits when the array's module loads (see
  * that function).
@@ -391,10 +398,12 @@ int64_t vct_cone_trace_fast_scratch_bytes(int64_t sample_count);
 
 /* VoxelConeTracingPass::onUpdate (VFS/RenderPass/Clipmap/VoxelConeTracingPass.cpp:75-106),
  * GB300 form: samples visited in Morton order, diffuse cones compacted per
- * warp, specular cones bucketed by roughness, the clipmap sampled through
- * `radiance` (hardware trilinear filter), FP32 compositing.  Same inputs and
- * outputs as vct_cone_trace; `scratch` is 256-byte aligned device memory of
- * at least vct_cone_trace_fast_scratch_bytes(sample_count) bytes. */
+ * warp, specular cones one per warp (on the calling thread's second stream,
+ * joined back to `stream`), the clipmap sampled through `radiance` (hardware
+ * trilinear filter), FP32 compositing.  Same inputs and outputs as
+ * vct_cone_trace; `scratch` is 256-byte aligned device memory of at least
+ * vct_cone_trace_fast_scratch_bytes(sample_count) bytes, in use until the
+ * work the call enqueues on `stream` completes. */
 int vct_cone_trace_fast(const vct_cone_tracing_desc* desc, const vct_cam_matrix* cam, vct_texture radiance,
                         const vct_shadow_map* shadow, const vct_directional_light_desc* light,
                         const vct_directional_light_shadow_desc* light_shadow,
