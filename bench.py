@@ -767,7 +767,7 @@ def batched_scenes(dev, streams: int = 4, n_scenes: int = 64, seed: int = 4):
     `streams` streams (vct_batch_submit) and one scene at a time; host wall clock around each submission
     (it returns when the work is done)."""
     import torch
-    from vk_voxel_cone_tracing_gb300 import clipmap, engine, passes
+    from vk_voxel_cone_tracing_gb300 import capi, clipmap, engine, passes
     from vk_voxel_cone_tracing_gb300.scene import room_scene, surface_samples, default_trace_desc
     rng = np.random.default_rng(seed)
     tris = np.exp(rng.uniform(np.log(1e4), np.log(5e5), n_scenes)).astype(int)
@@ -807,7 +807,22 @@ def batched_scenes(dev, streams: int = 4, n_scenes: int = 64, seed: int = 4):
         engine.batch_submit([j], 1)
         per.append((time.perf_counter() - t0) * 1e3)
     trace_phase = batched_trace_phase(dev, jobs, keep, ctxs, streams, grids)
+    ref_out = [(k[4].clone(), k[5].clone()) for k in keep]
     for c in ctxs.values():
+        c.close()
+    # the same batch with contexts that keep their opacity atlas one byte per texel (VCT_CONTEXT_OPACITY_R8)
+    ctx8 = {(t, int(R)): engine.Context(int(R), shadow_size=1024, flags=capi.CONTEXT_OPACITY_R8)
+            for t in range(streams) for R in set(grids.tolist())}
+    jobs8 = [engine.batch_job(ctx8[(i % streams, int(grids[i]))], k[1], k[6], j.light, j.light_shadow, k[3], k[6],
+                              k[2], k[4], k[5]) for i, (j, k) in enumerate(zip(jobs, keep))]
+    engine.batch_submit(jobs8, streams)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    engine.batch_submit(jobs8, streams)
+    batched_r8 = (time.perf_counter() - t0) * 1e3
+    torch.cuda.synchronize()
+    r8_equal = all(torch.equal(k[4], a) and torch.equal(k[5], b) for k, (a, b) in zip(keep, ref_out))
+    for c in ctx8.values():
         c.close()
     return {"scenes": n_scenes, "triangles": int(tris.sum()), "samples": int(nsamp.sum()),
             "grids": {str(k): int((grids == k).sum()) for k in (64, 128, 256)}, "streams": streams,
@@ -815,6 +830,7 @@ def batched_scenes(dev, streams: int = 4, n_scenes: int = 64, seed: int = 4):
             "batched_cone_samples_per_s": cone_samples / (batched * 1e-3),
             "per_scene_ms": {"p50": float(np.percentile(per, 50)), "p99": float(np.percentile(per, 99))},
             "trace_phase": trace_phase,
+            "batched_r8_opacity_ms": batched_r8, "r8_outputs_bit_equal": r8_equal,
             "note": "each job: a full clipmap frame (voxelise, shadow, inject, mips) + the fast trace of its "
                     "samples; host wall clock, the submission synchronises"}
 
