@@ -992,6 +992,61 @@ def differentiable_volume(dev, R: int = 128, views: int = 16, res: int = 512, se
                     "recomputes each cone from 32-step checkpoints and scatters float4 atomics"}
 
 
+def profile_case(args):
+    """A small case for the ncu captures under profiles/ (no JSON line): the hall scene with `--triangles`
+    triangles at clipmap `--R`, the bench camera and light.
+      frame      two frames keeping the radiance texture current
+      frames     3 + 3 timed frames with the texture, without it, and with the R8 opacity form
+      trace      one frame, then three fast traces of `--samples` area-uniform samples
+      exact      one frame, then two exact traces on the linear atlas
+      exact_tex  one frame, then two exact traces reading the texels through the texture
+      adjoint    the differentiable workload at R = 64, one view (forward + adjoint)"""
+    import torch
+
+    from vk_voxel_cone_tracing_gb300 import build, capi, clipmap, passes
+    from vk_voxel_cone_tracing_gb300.scene import hall_scene, surface_samples
+    build.build()
+    if args.profile_case == "adjoint":
+        print(json.dumps(differentiable_volume(torch.device("cuda"), R=64, views=1, res=512, fit_iterations=0)))
+        return
+    R = args.R
+    scene = hall_scene(seed=2, target=args.triangles)
+    ds, ws = passes.DeviceScene(scene), passes.Workspace()
+    op, rad = clipmap.new_atlas(R), clipmap.new_atlas(R)
+    sh = torch.empty((SHADOW_RES, SHADOW_RES), dtype=torch.float32, device="cuda")
+    light, lsd = passes.light_desc(LIGHT_DIR), passes.light_shadow_desc(light_origin(), LIGHT_DIR)
+    tex = clipmap.RadianceTexture(R)
+    frame = lambda **kw: passes.clipmap_frame(ds, CAMERA, R, op, rad, sh, light, lsd, ws, **kw)
+    if args.profile_case == "frames":
+        op8 = clipmap.new_atlas_r8(R)
+        for kw in ({"texture": tex}, {}):
+            for _ in range(6):
+                frame(**kw)
+        for _ in range(6):
+            passes.clipmap_frame(ds, CAMERA, R, op8, rad, sh, light, lsd, ws, texture=tex,
+                                 opacity_format=capi.OPACITY_R8)
+        torch.cuda.synchronize()
+        return
+    for _ in range(2):
+        regs = frame(texture=tex)
+    if args.profile_case == "frame":
+        torch.cuda.synchronize()
+        return
+    desc = trace_desc_for(clipmap.regions_to_numpy(regs), R)
+    smp = clipmap.samples_to_device(surface_samples(scene, args.samples, seed=1))
+    steps = torch.zeros(1, dtype=torch.int64, device="cuda")
+    for k in range(3 if args.profile_case == "trace" else 2):
+        kw = dict(light=light, shadow=sh, shadow_desc=lsd, steps=steps if k == 0 else None)
+        if args.profile_case == "trace":
+            clipmap.cone_trace_fast(desc, EYE, tex, smp, **kw)
+        elif args.profile_case == "exact":
+            clipmap.cone_trace(desc, EYE, rad, R, smp, **kw)
+        else:
+            clipmap.cone_trace_tex(desc, EYE, tex, smp, **kw)
+    torch.cuda.synchronize()
+    print("cone samples per trace", int(steps.item()))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1005,7 +1060,13 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true",
                     help="skip the batched multi-scene, differentiable-form and large-SVO measurements")
+    ap.add_argument("--profile-case", choices=["frame", "frames", "trace", "exact", "exact_tex", "adjoint"],
+                    help="run a small case for an ncu capture instead of the benchmark (see profile_case)")
+    ap.add_argument("--triangles", type=int, default=1_000_000, help="hall scene size of --profile-case")
     args = ap.parse_args()
+    if args.profile_case:
+        profile_case(args)
+        return
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)

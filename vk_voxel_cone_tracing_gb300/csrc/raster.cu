@@ -689,6 +689,7 @@ struct TilePlan {
     const uint32_t* tile_end;   // inclusive prefix of the items' tile counts
     const uint32_t* tile_item;  // item of every tile
     uint32_t total;             // tiles
+    unsigned int* ticket;       // the next chunk of 32 tiles a coverage warp takes (zeroed per launch)
 };
 
 // Item of every tile: item i owns tiles [tile_end[i-1], tile_end[i]).  A warp
@@ -952,6 +953,13 @@ __device__ __forceinline__ void for_each_covered(uint32_t mask, int lane, Fn&& f
     }
 }
 
+// The next chunk of 32 tiles for the calling warp.
+__device__ __forceinline__ uint32_t next_chunk(unsigned int* ticket, int lane) {
+    uint32_t c = 0;
+    if (lane == 0) c = atomicAdd(ticket, 1u);
+    return __shfl_sync(0xffffffffu, c, 0);
+}
+
 // Coverage kernels.  A warp takes 32 consecutive 8x8 tiles of (triangle,
 // level) items -- one per lane -- sets each up once into shared memory, then
 // flattens the (tile, pixel) pairs of all 32 tiles and walks them 32 at a
@@ -980,7 +988,9 @@ __global__ void __launch_bounds__(128, 6) k_cover(const __grid_constant__ Raster
     const uint32_t* __restrict__ tile_end = plan.tile_end;
     const uint32_t total = plan.total;
     const uint32_t nchunks = (total + 31u) >> 5;
-    for (uint32_t ch = blockIdx.x * 4u + (threadIdx.x >> 5); ch < nchunks; ch += gridDim.x * 4u) {
+    // chunks are dealt to the warps as they free up (a ticket), so unequal chunks do not leave SMs idle at the
+    // end; every chunk's results depend only on its index
+    for (uint32_t ch = next_chunk(plan.ticket, lane); ch < nchunks; ch = next_chunk(plan.ticket, lane)) {
         const uint32_t g = ch * 32u + lane;
         uint32_t npx = 0;
         // the emit phase skips tiles whose count pass found no covered sample
@@ -1255,6 +1265,8 @@ static void launch_cover(const RasterArgs& A, const TilePlan& plan, uint2* count
     const uint32_t nchunks = (plan.total + 31u) >> 5;
     int blocks = (int)((nchunks + 3u) >> 2);
     blocks = blocks < 1 ? 1 : (blocks > 152 * 16 ? 152 * 16 : blocks);
+    // (an error of the zeroing is the thread's last error, which the callers' launch check reads)
+    cudaMemsetAsync(plan.ticket, 0, sizeof(unsigned int), st);
     k_cover<KIND, PHASE><<<blocks, 128, 0, st>>>(A, plan, counts, offs, frags, err);
 }
 
@@ -1539,6 +1551,8 @@ static int plan_tiles(RasterArgs& A, vct_workspace_s* ws, size_t& off, TilePlan*
     }
     uint32_t* tile_item = (uint32_t*)(base + off);
     off += a256(4 * (size_t)total);
+    unsigned int* ticket = (unsigned int*)(base + off);
+    off += 256;
     if (total) {
         k_tile_items<<<grid_of(n, 256), 256, 0, st>>>(tile_end, A.items, tile_item);
         VCT_LAUNCH_CHECK();
@@ -1546,6 +1560,7 @@ static int plan_tiles(RasterArgs& A, vct_workspace_s* ws, size_t& off, TilePlan*
     plan->tile_end = tile_end;
     plan->tile_item = tile_item;
     plan->total = total;
+    plan->ticket = ticket;
     return VCT_OK;
 }
 
