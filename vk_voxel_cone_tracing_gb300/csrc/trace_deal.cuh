@@ -147,9 +147,24 @@ __device__ __forceinline__ void deal_diffuse_warp(const DealArgs& A, const March
     }
 }
 
-// Every warp of the grid over the order, 32 positions at a time.
+// Every warp of the grid over the order, 32 positions at a time: with a
+// ticket (zeroed before the launch), the items go to the warps as they free
+// up; without one, by a static grid stride.
 template <int WARPS, class Marcher>
-__device__ __forceinline__ void deal_diffuse(const DealArgs& A, const Marcher& march, unsigned long long& steps) {
+__device__ __forceinline__ void deal_diffuse(const DealArgs& A, const Marcher& march, unsigned long long& steps,
+                                             unsigned int* ticket = nullptr) {
+    if (ticket) {
+        const int lane = threadIdx.x & 31;
+        for (;;) {
+            uint32_t it = 0;
+            if (lane == 0) it = atomicAdd(ticket, 1u);
+            it = __shfl_sync(0xffffffffu, it, 0);
+            const int64_t base = (int64_t)it * 32;
+            if (base >= A.n) break;
+            deal_diffuse_warp<WARPS>(A, march, base, steps);
+        }
+        return;
+    }
     const int64_t nwarps = (int64_t)gridDim.x * WARPS;
     for (int64_t base = ((int64_t)blockIdx.x * WARPS + (threadIdx.x >> 5)) * 32; base < A.n; base += nwarps * 32)
         deal_diffuse_warp<WARPS>(A, march, base, steps);

@@ -38,13 +38,14 @@ __global__ void __launch_bounds__(32 * kExactWarps) k_exact_diffuse(TraceParams 
                                                                     const vct_surface_sample* __restrict__ samples,
                                                                     int64_t n, const uint32_t* __restrict__ order,
                                                                     float* __restrict__ dout, float* __restrict__ sout,
-                                                                    unsigned long long* __restrict__ step_counter) {
+                                                                    unsigned long long* __restrict__ step_counter,
+                                                                    unsigned int* __restrict__ ticket) {
     const bool c32 = P.d.enable_32_cones != 0;
     DealArgs D{&P, samples, n, order, 0u, (uint32_t)n, dout, sout, c32 ? 32 : 16, true, true};
     const ExactDiffuseMarch<Atlas> march{T, &P.d, P.diffuse_aperture,
                                          fmaxf(kMinTraceStepFactor, P.d.min_trace_step_factor)};
     unsigned long long steps = 0;
-    deal_diffuse<kExactWarps>(D, march, steps);
+    deal_diffuse<kExactWarps>(D, march, steps, ticket);  // items to the warps as they free up
     add_steps(step_counter, steps);
 }
 
@@ -57,11 +58,20 @@ __global__ void __launch_bounds__(128) k_exact_specular(TraceParams P, Atlas T,
                                                         const uint32_t* __restrict__ list,
                                                         const unsigned int* __restrict__ spec_count,
                                                         float* __restrict__ sout,
-                                                        unsigned long long* __restrict__ step_counter) {
+                                                        unsigned long long* __restrict__ step_counter,
+                                                        unsigned int* __restrict__ ticket) {
     const vct_cone_tracing_desc& d = P.d;
     const int64_t m = *spec_count;
+    const int lane = threadIdx.x & 31;
     unsigned long long steps = 0;
-    for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < m; c += (int64_t)gridDim.x * blockDim.x) {
+    // 32 consecutive cones of the list to the warp at a time, as warps free up
+    for (;;) {
+        uint32_t c0 = 0;
+        if (lane == 0) c0 = atomicAdd(ticket, 32u);
+        c0 = __shfl_sync(0xffffffffu, c0, 0);
+        if ((int64_t)c0 >= m) break;
+        const int64_t c = (int64_t)c0 + lane;
+        if (c >= m) continue;
         const uint32_t idx = __ldg(list + c);
         const GSample g = load_sample(samples + idx, P.eye);
         const float min_level = calc_min_level(d, g.wp);
@@ -256,7 +266,8 @@ int exact_plan(const vct_surface_sample* samples, int64_t n, const vct_cone_trac
         e = cudaMemcpyAsync(identity, &zero, sizeof(zero), cudaMemcpyHostToDevice, st);
         plan->order = identity;
     }
-    if (e == cudaSuccess) e = cudaMemsetAsync(plan->spec_count, 0, sizeof(unsigned int), st);
+    // the specular count and the tickets of the specular and diffuse kernels
+    if (e == cudaSuccess) e = cudaMemsetAsync(plan->spec_count, 0, 3 * sizeof(unsigned int), st);
     const int64_t gb = (n + 255) / 256;
     if (e == cudaSuccess) {
         k_exact_spec_keys<<<(int)(gb > 152 * 16 ? 152 * 16 : gb), 256, 0, st>>>(samples, n, plan->order, spec_key,
@@ -306,12 +317,12 @@ static int launch_exact(const TraceParams& P, const Atlas& T, const vct_surface_
         if (rc != VCT_OK) return rc;
         const int64_t gdw = (m + 32 * kExactWarps - 1) / (32 * kExactWarps);
         k_exact_diffuse<<<(int)(gdw > 152 * 16 ? 152 * 16 : gdw), 32 * kExactWarps, 0, st>>>(
-            P, T, smp, m, plan.order, dout + 4 * off, sout + 4 * off, cone_steps);
+            P, T, smp, m, plan.order, dout + 4 * off, sout + 4 * off, cone_steps, plan.spec_count + 2);
         cudaError_t e = cudaGetLastError();
         if (e == cudaSuccess) {
             const int64_t gl = (m + 127) / 128;
             k_exact_specular<<<(int)(gl > 152 * 16 ? 152 * 16 : gl), 128, 0, st>>>(
-                P, T, smp, plan.spec_list, plan.spec_count, sout + 4 * off, cone_steps);
+                P, T, smp, plan.spec_list, plan.spec_count, sout + 4 * off, cone_steps, plan.spec_count + 1);
             e = cudaGetLastError();
         }
         exact_plan_free(&plan, st);
