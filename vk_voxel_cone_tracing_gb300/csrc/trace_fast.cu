@@ -523,15 +523,24 @@ __global__ void __launch_bounds__(256) k_batch_diffuse(const __grid_constant__ B
 
 __global__ void __launch_bounds__(256, 4) k_batch_specular(const __grid_constant__ BatchTable T,
                                                            const uint32_t* __restrict__ list,
-                                                           const unsigned int* __restrict__ spec_count) {
+                                                           const unsigned int* __restrict__ spec_count,
+                                                           unsigned int* __restrict__ ticket) {
     const int64_t m = *spec_count;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < m; c += nwarps) {
-        const uint32_t g = __ldg(list + c);
-        const BatchJob& J = T.jobs[warp_uniform(batch_job_of(T, g))];
-        unsigned long long steps = 0;
-        specular_cone_warp(J.A, g - J.base, steps);
-        if (J.A.steps && (threadIdx.x & 31) == 0 && steps) atomicAdd(J.A.steps, steps);
+    const int lane = threadIdx.x & 31;
+    // cones dealt to the warps by a ticket, as in the single trace
+    for (;;) {
+        uint32_t c0 = 0;
+        if (lane == 0) c0 = atomicAdd(ticket, (unsigned)kSpecConesPerTicket);
+        c0 = __shfl_sync(0xffffffffu, c0, 0);
+        if ((int64_t)c0 >= m) break;
+        const int64_t c1 = (int64_t)c0 + kSpecConesPerTicket < m ? (int64_t)c0 + kSpecConesPerTicket : m;
+        for (int64_t c = c0; c < c1; ++c) {
+            const uint32_t g = __ldg(list + c);
+            const BatchJob& J = T.jobs[warp_uniform(batch_job_of(T, g))];
+            unsigned long long steps = 0;
+            specular_cone_warp(J.A, g - J.base, steps);
+            if (J.A.steps && lane == 0 && steps) atomicAdd(J.A.steps, steps);
+        }
     }
 }
 
@@ -1016,7 +1025,7 @@ int batch_layout(const vct_trace_job* jobs, int32_t njobs, BatchLayout& L) {
     L.spec_key = take(4 * n);
     L.spec_key_out = take(4 * n);
     L.spec_list = take(4 * n);
-    L.spec_count = take(sizeof(unsigned int));
+    L.spec_count = take(2 * sizeof(unsigned int));
     L.temp = take(L.temp_bytes);
     L.total = off;
     return VCT_OK;
@@ -1106,7 +1115,7 @@ extern "C" int vct_cone_trace_fast_batch(const vct_trace_job* jobs, int32_t job_
         size_t tb = L.temp_bytes;
         VCT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(b + L.temp, tb, keys_in, keys_out, vals_in, order, (int)n, 0,
                                                      31 + jb, st));
-        VCT_CUDA_TRY(cudaMemsetAsync(spec_count, 0, sizeof(unsigned int), st));
+        VCT_CUDA_TRY(cudaMemsetAsync(spec_count, 0, 2 * sizeof(unsigned int), st));  // count and cone ticket
         k_batch_spec_keys<<<(g256 > 152 * 16 ? 152 * 16 : g256), 256, 0, st>>>(T, pos, order, spec_key, spec_count);
         VCT_LAUNCH_CHECK();
         tb = L.temp_bytes;
@@ -1116,7 +1125,8 @@ extern "C" int vct_cone_trace_fast_batch(const vct_trace_job* jobs, int32_t job_
         k_batch_diffuse<<<(g256 > 152 * 8 ? 152 * 8 : g256), 256, 0, st>>>(T, pos, order);
         VCT_LAUNCH_CHECK();
         const int64_t gw = (n * 32 + 255) / 256;
-        k_batch_specular<<<(int)(gw > 152 * 64 ? 152 * 64 : gw), 256, 0, st>>>(T, spec_list, spec_count);
+        k_batch_specular<<<(int)(gw > 152 * 64 ? 152 * 64 : gw), 256, 0, st>>>(T, spec_list, spec_count,
+                                                                                spec_count + 1);
         VCT_LAUNCH_CHECK();
     }
     return VCT_OK;
