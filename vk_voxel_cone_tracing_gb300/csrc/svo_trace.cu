@@ -96,10 +96,19 @@ __device__ float4 svo_trace_cone(const SvoScene& S, const vct_cone_tracing_desc&
 __global__ void __launch_bounds__(128) k_svo_trace(TraceParams P, SvoScene S, const vct_surface_sample* __restrict__ samples,
                                                    int64_t n, const uint32_t* __restrict__ order,
                                                    float* __restrict__ dout, float* __restrict__ sout,
-                                                   unsigned long long* __restrict__ step_counter) {
+                                                   unsigned long long* __restrict__ step_counter,
+                                                   unsigned int* __restrict__ ticket) {
     unsigned long long steps = 0;
     const vct_cone_tracing_desc& d = P.d;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    // 32 consecutive samples of the coherent order per warp, dealt by a ticket as warps free up
+    for (;;) {
+        uint32_t t0 = 0;
+        if (lane == 0) t0 = atomicAdd(ticket, 32u);
+        t0 = __shfl_sync(0xffffffffu, t0, 0);
+        if ((int64_t)t0 >= n) break;
+        const int64_t t = (int64_t)t0 + lane;
+        if (t >= n) continue;
         const int64_t i = order ? (int64_t)__ldg(order + t) : t;
         GSample g = load_sample(samples + i, P.eye);
         if (g.depth == 1.0f) continue;
@@ -216,8 +225,14 @@ extern "C" int vct_svo_cone_trace(const vct_cone_tracing_desc* desc, const vct_c
     if (rc != VCT_OK) return rc;
     int64_t blocks = (n + 127) / 128;
     if (blocks > 152 * 16) blocks = 152 * 16;
-    k_svo_trace<<<(int)blocks, 128, 0, st>>>(P, S, samples, n, so.order, dout, sout, cone_steps);
-    cudaError_t e = cudaGetLastError();
+    unsigned int* ticket = nullptr;
+    cudaError_t e = cudaMallocAsync((void**)&ticket, sizeof(unsigned int), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ticket, 0, sizeof(unsigned int), st);
+    if (e == cudaSuccess) {
+        k_svo_trace<<<(int)blocks, 128, 0, st>>>(P, S, samples, n, so.order, dout, sout, cone_steps, ticket);
+        e = cudaGetLastError();
+    }
+    if (ticket) cudaFreeAsync(ticket, st);
     if (so.block) cudaFreeAsync(so.block, st);
     if (e != cudaSuccess) return cuda_fail(e, "k_svo_trace");
     return VCT_OK;

@@ -147,13 +147,13 @@ __device__ __forceinline__ void deal_diffuse_warp(const DealArgs& A, const March
     }
 }
 
-// Every warp of the grid over the order, 32 positions at a time: with a
-// ticket (zeroed before the launch), the items go to the warps as they free
-// up; without one, by a static grid stride.
-template <int WARPS, class Marcher>
+// Every warp of the grid over the order, 32 positions at a time: with
+// TICKET (`ticket` zeroed before the launch), the items go to the warps as
+// they free up; without, by a static grid stride.
+template <int WARPS, bool TICKET = false, class Marcher>
 __device__ __forceinline__ void deal_diffuse(const DealArgs& A, const Marcher& march, unsigned long long& steps,
                                              unsigned int* ticket = nullptr) {
-    if (ticket) {
+    if constexpr (TICKET) {
         const int lane = threadIdx.x & 31;
         for (;;) {
             uint32_t it = 0;

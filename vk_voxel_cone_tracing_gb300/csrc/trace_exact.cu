@@ -23,6 +23,11 @@ namespace vct {
 
 constexpr int kExactWarps = 4;  // warps per block of the diffuse kernel
 
+// Tickets (work to warps as they free up) for the texture and float reads;
+// the linear RGBA8 atlas's loads run faster with the static deal.
+template <class Atlas>
+constexpr bool kExactTickets = !std::is_same<Atlas, ExactAtlas>::value;
+
 template <class Atlas>
 struct ExactDiffuseMarch {
     Atlas T;
@@ -46,7 +51,7 @@ __global__ void __launch_bounds__(32 * kExactWarps) k_exact_diffuse(TraceParams 
     const ExactDiffuseMarch<Atlas> march{T, &P.d, P.diffuse_aperture,
                                          fmaxf(kMinTraceStepFactor, P.d.min_trace_step_factor)};
     unsigned long long steps = 0;
-    deal_diffuse<kExactWarps>(D, march, steps, ticket);  // items to the warps as they free up
+    deal_diffuse<kExactWarps, kExactTickets<Atlas>>(D, march, steps, ticket);
     add_steps(step_counter, steps);
 }
 
@@ -65,13 +70,13 @@ __global__ void __launch_bounds__(128) k_exact_specular(TraceParams P, Atlas T,
     const int64_t m = *spec_count;
     const int lane = threadIdx.x & 31;
     unsigned long long steps = 0;
-    // with a ticket, 32 consecutive cones of the list to the warp at a time as warps free up; without, a
+    // with tickets, 32 consecutive cones of the list to the warp at a time as warps free up; without, a
     // static grid stride
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     int64_t c_static = (int64_t)blockIdx.x * blockDim.x + threadIdx.x - stride;
     for (;;) {
         int64_t c;
-        if (ticket) {
+        if constexpr (kExactTickets<Atlas>) {
             uint32_t c0 = 0;
             if (lane == 0) c0 = atomicAdd(ticket, 32u);
             c0 = __shfl_sync(0xffffffffu, c0, 0);
@@ -326,11 +331,8 @@ static int launch_exact(const TraceParams& P, const Atlas& T, const vct_surface_
         ExactPlan plan;
         int rc = exact_plan(smp, m, P.d, &plan, st);
         if (rc != VCT_OK) return rc;
-        // tickets (work to warps as they free up) for the texture and float reads; the linear RGBA8 atlas's
-        // loads measured 4 % faster with the static deal
-        constexpr bool kTickets = !std::is_same<Atlas, ExactAtlas>::value;
-        unsigned int* spec_ticket = kTickets ? plan.spec_count + 1 : nullptr;
-        unsigned int* diff_ticket = kTickets ? plan.spec_count + 2 : nullptr;
+        unsigned int* spec_ticket = plan.spec_count + 1;
+        unsigned int* diff_ticket = plan.spec_count + 2;
         const int64_t gdw = (m + 32 * kExactWarps - 1) / (32 * kExactWarps);
         k_exact_diffuse<<<(int)(gdw > 152 * 16 ? 152 * 16 : gdw), 32 * kExactWarps, 0, st>>>(
             P, T, smp, m, plan.order, dout + 4 * off, sout + 4 * off, cone_steps, diff_ticket);

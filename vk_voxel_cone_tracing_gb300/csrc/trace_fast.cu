@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(256) k_trace_diffuse(const __grid_constant__ F
                A.C.need_specular != 0};
     unsigned long long steps = 0;
     // (a ticket for the diffuse items measured no faster than the static stride: 8.69 against 8.66 ms per step)
-    deal_diffuse<kWarpsPerBlock>(D, FastDiffuseMarch{A.tex, &A.C}, steps, kDiffuseTickets ? ticket : nullptr);
+    deal_diffuse<kWarpsPerBlock, kDiffuseTickets>(D, FastDiffuseMarch{A.tex, &A.C}, steps, ticket);
     add_steps(A.steps, steps);
 }
 
