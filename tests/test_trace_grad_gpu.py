@@ -4,7 +4,7 @@ against the oracle's FP64 trace of the same atlas, and the adjoints
 reference gradients -- reverse-mode differentiation of the restated trace
 and mips (oracle/adjoint_oracle.hpp), compared entry by entry -- and against
 central finite differences of the FP64 oracle on a 32^3 clipmap with 256
-samples (the survey's check for this configuration).  The test volume keeps
+samples (the differentiable workload's 1e-4 finite-difference check).  The test volume keeps
 alpha below 0.3, so no clamp and no occlusion stop switches under the
 perturbations.
 
