@@ -95,6 +95,69 @@ __global__ void k_copy_alpha(uint32_t* __restrict__ dst, const OT* __restrict__ 
     }
 }
 
+// The same pass four texels at a time: each thread takes an aligned group of
+// four texels of a row (rows are 16-byte aligned: W = 6 (R + 2) is a multiple
+// of four), with 16-byte loads and stores and one 16-byte surface store; the
+// group's texels outside the faces' interiors (the border columns, which no
+// pass writes in the radiance atlas) are stored back unchanged.  A warp covers
+// 512 contiguous bytes of a row.
+__device__ __forceinline__ uint4 opa_alpha4(const uint32_t* __restrict__ opa, int64_t i) {
+    const uint4 v = __ldg(reinterpret_cast<const uint4*>(opa + i));
+    return make_uint4(v.x & 0xff000000u, v.y & 0xff000000u, v.z & 0xff000000u, v.w & 0xff000000u);
+}
+__device__ __forceinline__ uint4 opa_alpha4(const uint8_t* __restrict__ opa, int64_t i) {
+    const uint32_t b = __ldg(reinterpret_cast<const uint32_t*>(opa + i));
+    return make_uint4(b << 24, (b << 16) & 0xff000000u, (b << 8) & 0xff000000u, b & 0xff000000u);
+}
+
+template <class OT>
+__global__ void k_copy_alpha4(uint32_t* __restrict__ dst, const OT* __restrict__ src, AtlasDims A, int level,
+                              int faces, cudaSurfaceObject_t mirror, const uint32_t* __restrict__ touched) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t groups = (uint32_t)(A.rb * faces + 3) >> 2;  // x groups of a row
+    const uint32_t g32 = (groups + 31u) & ~31u;                  // a row's groups padded to whole warps
+    const uint32_t R = (uint32_t)A.R;
+    const uint32_t n = g32 * R * R;  // R <= 1024: < 2^31
+    // warp-uniform trip count: a warp's 32 groups lie in one row
+    for (uint32_t t0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; t0 < n; t0 += gridDim.x * blockDim.x) {
+        const uint32_t t = t0 + (uint32_t)lane;
+        const uint32_t gx = t % g32, r = t / g32;
+        const int y = (int)(r & (R - 1u)) + 1 + level * A.rb, z = (int)(r / R) + 1;
+        const int x0 = (int)gx * 4;
+        const bool valid = gx < groups;
+        const int64_t i = A.index(x0, y, z);
+        uint32_t v[4] = {0u, 0u, 0u, 0u};
+        if (valid) {
+            const uint4 d = *reinterpret_cast<const uint4*>(dst + i);
+            const uint4 a = opa_alpha4(src, i);
+            const uint32_t w = touched ? __ldg(touched + (i >> 5)) : 0xffffffffu;
+            v[0] = d.x, v[1] = d.y, v[2] = d.z, v[3] = d.w;
+            const uint32_t av[4] = {a.x, a.y, a.z, a.w};
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int x = x0 + k, xf = x % A.rb;
+                if (x < A.rb * faces && xf >= 1 && xf <= A.R)
+                    v[k] = (((w >> ((i + k) & 31)) & 1u) ? (v[k] & 0x00ffffffu) : 0u) | av[k];
+            }
+            *reinterpret_cast<uint4*>(dst + i) = make_uint4(v[0], v[1], v[2], v[3]);
+        }
+        if (mirror) {
+            // the texture's texel stores coalesced: in round k lane L stores texel 32 k + L of the warp's 128,
+            // which lane 8 k + L / 4 holds as its element L % 4
+            const int xw = (int)(gx - (uint32_t)lane) * 4;  // the warp's first texel
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int o = 8 * k + (lane >> 2), e = lane & 3;
+                const uint32_t c0 = __shfl_sync(0xffffffffu, v[0], o), c1 = __shfl_sync(0xffffffffu, v[1], o);
+                const uint32_t c2 = __shfl_sync(0xffffffffu, v[2], o), c3 = __shfl_sync(0xffffffffu, v[3], o);
+                const uint32_t c = e == 0 ? c0 : (e == 1 ? c1 : (e == 2 ? c2 : c3));
+                const int x = xw + 32 * k + lane;
+                if (t0 < n && (uint32_t)x < groups * 4u) surf3Dwrite(c, mirror, x * 4, y, z);
+            }
+        }
+    }
+}
+
 // ---------------------------------------------------------------- border
 // borderWrapping.comp:14-37: the dispatch covers ((R+2)>>3)*8 = R
 // invocations per axis (R a power of two >= 8), and an invocation whose
@@ -476,7 +539,17 @@ int copy_alpha_pass(uint32_t* dst, const void* src, const vct_copy_alpha_desc* d
     const int lg = 31 - __builtin_clz((unsigned)A.R);
     const int64_t n = (int64_t)A.R * A.R * A.R;
     const int grid = grid_for(n, 256);
-    if (src_r8)
+    const bool aligned = (((uintptr_t)dst | (uintptr_t)src) & 15) == 0;  // 16-byte row groups (R8: 4 bytes)
+    if (aligned) {
+        const int64_t n4 = (int64_t)((((A.rb * d->face_count + 3) >> 2) + 31) & ~31) * A.R * A.R;
+        const int grid4 = grid_for(n4, 256);
+        if (src_r8)
+            k_copy_alpha4<<<grid4, 256, 0, st>>>(dst, static_cast<const uint8_t*>(src), A, d->clip_level,
+                                                 d->face_count, mirror, touched);
+        else
+            k_copy_alpha4<<<grid4, 256, 0, st>>>(dst, static_cast<const uint32_t*>(src), A, d->clip_level,
+                                                 d->face_count, mirror, touched);
+    } else if (src_r8)
         k_copy_alpha<<<grid, 256, 0, st>>>(dst, static_cast<const uint8_t*>(src), A, d->clip_level, lg, d->face_count,
                                            mirror, touched);
     else
@@ -500,14 +573,14 @@ int copy_alpha_downsample_pass(uint32_t* radiance, const void* opacity, const vc
     const int64_t n = (int64_t)A.R * A.R * A.R;
     int3 pm = make_int3(d->prev_region_min_corner[0], d->prev_region_min_corner[1], d->prev_region_min_corner[2]);
     const int lg = 31 - __builtin_clz((unsigned)A.R);
+    const int grid = grid_for(n, 128);
+    const int band = d->downsample_region_size, l = d->clip_level;
     if (opa_r8)
-        k_alpha_downsample<<<grid_for(n, 128), 128, 0, st>>>(radiance, radiance, static_cast<const uint8_t*>(opacity), A, pm,
-                                                            d->clip_level, d->downsample_region_size, lg, mirror,
-                                                            touched);
+        k_alpha_downsample<<<grid, 128, 0, st>>>(radiance, radiance, static_cast<const uint8_t*>(opacity), A, pm, l,
+                                                 band, lg, mirror, touched);
     else
-        k_alpha_downsample<<<grid_for(n, 128), 128, 0, st>>>(radiance, radiance, static_cast<const uint32_t*>(opacity), A, pm,
-                                                            d->clip_level, d->downsample_region_size, lg, mirror,
-                                                            touched);
+        k_alpha_downsample<<<grid, 128, 0, st>>>(radiance, radiance, static_cast<const uint32_t*>(opacity), A, pm, l,
+                                                 band, lg, mirror, touched);
     VCT_LAUNCH_CHECK();
     return VCT_OK;
 }
