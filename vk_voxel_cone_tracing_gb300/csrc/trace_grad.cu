@@ -25,12 +25,16 @@
 // Same FP32 expressions as the forward kernels (this unit is built with
 // -fmad=false like them), so the recomputed steps are the forward's.
 //
-// Each cone is walked by one lane, the warp's lanes in lock step: a
-// checkpoint of the march state every 32 steps, each segment recomputed from
-// its checkpoint and walked backward with the recurrences above in
-// sequential form.  Diffuse cones all share one step schedule; specular
+// Each cone is walked by one lane, the warp's lanes in lock step: one march
+// forward keeps each of the first 64 steps' record (the state before the
+// step, its sample, opacity terms, position and levels) in device scratch,
+// and a checkpoint of the march state every 32 steps after those; the walk
+// backward with the recurrences above in sequential form reads the records,
+// and recomputes a later segment from its checkpoint.  Diffuse cones all share one step schedule; specular
 // cones are taken from the exact forward's aperture-grouped list, so a
 // warp's cones also march nearly the same number of steps.
+#include <algorithm>
+
 #include "trace_exact.cuh"
 
 namespace vct {
@@ -43,6 +47,17 @@ namespace {
 
 constexpr int kSegSteps = 32;
 constexpr int kMaxSegments = 256;  // 8192 steps per cone: the specular cone at R = 1024 takes ~7.1k
+
+// A cone's first kStoredSteps steps keep what the reverse walk reads in a
+// record block of the lane's warp (device scratch, one block per warp of the
+// grid, fields outermost and lanes innermost: a warp's store or load of a
+// field is one 128-byte line), so those segments are walked backward without
+// a second march; later segments are recomputed from checkpoints.
+constexpr int kStoredSteps = 64;
+static_assert(kStoredSteps % kSegSteps == 0, "stored steps are whole segments");
+enum RecField { kRecAlpha, kRecOcc, kRecCorr, kRecQ, kRecOp, kRecSlope, kRecR, kRecG, kRecB, kRecStep, kRecFr,
+                kRecLevels, kRecFields };
+constexpr size_t kRecWarpFloats = (size_t)kRecFields * kStoredSteps * 32;
 
 struct MarchState {
     float step, seg, diameter, alpha, occ;
@@ -137,12 +152,16 @@ __device__ __forceinline__ StepDetail march_step(const F4Atlas& T, const vct_con
 // The adjoint of one cone per lane: gC (rgb) and gO (d/d occlusion)
 // at the end of the march.  The warp's lanes run in lock step: every loop
 // runs to the warp's longest march and a lane sits out the steps its cone
-// does not have (or all of them when `active` is false).  The forward
-// recompute of a segment keeps each step, so the reverse walk reads no texels.
+// does not have (or all of them when `active` is false).  The reverse walk
+// reads no texels: a stored step's record, or the recompute of a later
+// segment, kept in local arrays.
+// `rec`: the warp's record block (kRecWarpFloats floats), written and read
+// by each lane for its own cone only.
 __device__ void cone_backward_lane(const F4Atlas& T, float4* __restrict__ G, const vct_cone_tracing_desc& d,
                                    const ConeGeo& K, float3 gC, float gO, bool active, float max_dist,
-                                   int* __restrict__ err) {
+                                   float* rec, int* __restrict__ err) {
     constexpr unsigned kFull = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
     MarchState ckpt[kMaxSegments];
     const Sched s0 = first_sched(K);
     MarchState m{s0.step, s0.seg, s0.diameter, 0.0f, 0.0f};
@@ -154,8 +173,25 @@ __device__ void cone_backward_lane(const F4Atlas& T, float4* __restrict__ G, con
             return;
         }
         if (running) {
-            if ((j % kSegSteps) == 0) ckpt[j / kSegSteps] = m;
-            march_step(T, d, K, m);
+            if ((j % kSegSteps) == 0 && j >= kStoredSteps) ckpt[j / kSegSteps] = m;
+            const float alpha0 = m.alpha, occ0 = m.occ, step0 = m.step;
+            const StepDetail e = march_step(T, d, K, m);
+            if (j < kStoredSteps) {
+                float* r = rec + (size_t)j * 32 + lane;
+                constexpr size_t F = (size_t)kStoredSteps * 32;  // one field's floats
+                r[kRecAlpha * F] = alpha0;
+                r[kRecOcc * F] = occ0;
+                r[kRecCorr * F] = e.correction;
+                r[kRecQ * F] = e.q;
+                r[kRecOp * F] = e.op;
+                r[kRecSlope * F] = opacity_slope(e);
+                r[kRecR * F] = e.smp.x;
+                r[kRecG * F] = e.smp.y;
+                r[kRecB * F] = e.smp.z;
+                r[kRecStep * F] = step0;
+                r[kRecFr * F] = e.fr;
+                r[kRecLevels * F] = __int_as_float((e.lower & 0xffff) | (e.upper << 16));
+            }
             ++n;
             running = m.step < max_dist && m.occ < 1.0f;
         }
@@ -167,6 +203,32 @@ __device__ void cone_backward_lane(const F4Atlas& T, float4* __restrict__ G, con
     for (int sidx = (nmax - 1) / kSegSteps; nmax > 0 && sidx >= 0; --sidx) {
         const int first = sidx * kSegSteps, last = min(nmax, first + kSegSteps);
         const int mine = min(n, first + kSegSteps);  // this lane's steps of the segment: first .. mine - 1
+        if (first < kStoredSteps) {  // warp-uniform: the segment's steps are in the record block
+            for (int i = last - 1; i >= first; --i) {
+                if (i >= mine) continue;
+                const float* rr = rec + (size_t)i * 32 + lane;
+                constexpr size_t F = (size_t)kStoredSteps * 32;
+                const float alpha = rr[kRecAlpha * F], occ = rr[kRecOcc * F];
+                const float c = rr[kRecCorr * F], q = rr[kRecQ * F], op = rr[kRecOp * F];
+                const float slope = rr[kRecSlope * F];
+                const float sr = rr[kRecR * F], sg = rr[kRecG * F], sb = rr[kRecB * F];
+                const float step = rr[kRecStep * F], fr = rr[kRecFr * F];
+                const int lv = __float_as_int(rr[kRecLevels * F]);
+                const float k_raw = 1.0f - alpha;
+                const float k = clampf(k_raw, 0.0f, 1.0f);
+                float4 gs;
+                gs.x = gC.x * k * c;
+                gs.y = gC.y * k * c;
+                gs.z = gC.z * k * c;
+                const float gop = gA * k + gO * (1.0f - occ) / q;
+                gs.w = gop * slope;
+                if (k_raw >= 0.0f && k_raw <= 1.0f) gA = gA - ((gC.x * sr + gC.y * sg + gC.z * sb) * c + gA * op);
+                gO = gO * (1.0f - op / q);
+                const float3 pos = K.start + K.dir * step;  // exact_step_detail's expression
+                scatter_step(G, T.A, d, K, pos, (int)(short)(lv & 0xffff), lv >> 16, fr, gs);
+            }
+            continue;
+        }
         MarchState r;
         if (first < n) r = ckpt[sidx];
         for (int i = first; i < last; ++i) {
@@ -225,8 +287,9 @@ __global__ void __launch_bounds__(128) k_cone_backward_diffuse(TraceParams P, F4
                                                                const vct_surface_sample* __restrict__ samples,
                                                                int64_t n, const uint32_t* __restrict__ order,
                                                                const float4* __restrict__ gd, float4* __restrict__ G,
-                                                               int* __restrict__ err) {
+                                                               float* rec_all, int* __restrict__ err) {
     const vct_cone_tracing_desc& d = P.d;
+    float* rec = rec_all + (size_t)((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kRecWarpFloats;
     const bool c32 = d.enable_32_cones != 0;
     const int nc = c32 ? 32 : 16;
     const int lane = threadIdx.x & 31;
@@ -255,7 +318,7 @@ __global__ void __launch_bounds__(128) k_cone_backward_diffuse(TraceParams P, F4
         active = active && diffuse_seeds(P, g, gd[i], cos_t, nc, gC, gO);
         const ConeGeo K = make_cone(d, start, dir, P.diffuse_aperture, min_level,
                                     fmaxf(kMinTraceStepFactor, d.min_trace_step_factor));
-        cone_backward_lane(T, G, d, K, gC, gO, active, kMaxTraceDistance, err);
+        cone_backward_lane(T, G, d, K, gC, gO, active, kMaxTraceDistance, rec, err);
     }
 }
 
@@ -264,8 +327,9 @@ __global__ void __launch_bounds__(128) k_cone_backward_diffuse(TraceParams P, F4
 __global__ void __launch_bounds__(128) k_cone_backward_specular(
     TraceParams P, F4Atlas T, const vct_surface_sample* __restrict__ samples, const uint32_t* __restrict__ list,
     const unsigned int* __restrict__ spec_count, const float4* __restrict__ gsp, float4* __restrict__ G,
-    int* __restrict__ err) {
+    float* rec_all, int* __restrict__ err) {
     const vct_cone_tracing_desc& d = P.d;
+    float* rec = rec_all + (size_t)((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kRecWarpFloats;
     if (!(d.rendering_mode == 6 || d.rendering_mode >= 8)) return;
     const int lane = threadIdx.x & 31;
     const int64_t m = *spec_count;
@@ -286,7 +350,7 @@ __global__ void __launch_bounds__(128) k_cone_backward_specular(
         const float3 start = g.wp + g.normal * (vs * d.trace_start_offset);
         const float3 sdir = reflect3(f3(-g.view.x, -g.view.y, -g.view.z), g.normal);
         const ConeGeo K = make_cone(d, start, sdir, fmaxf(g.roughness, kMinSpecularAperture), min_level, d.voxel_size);
-        cone_backward_lane(T, G, d, K, gC, 0.0f, active, kMaxTraceDistance, err);
+        cone_backward_lane(T, G, d, K, gC, 0.0f, active, kMaxTraceDistance, rec, err);
     }
 }
 
@@ -314,33 +378,46 @@ extern "C" int vct_cone_trace_backward(const vct_cone_tracing_desc* desc, const 
     int rc = fill_trace_params(P, desc, cam, shadow, light, light_shadow);
     if (rc != VCT_OK) return rc;
     cudaStream_t st = as_stream(stream);
+    const int nc = desc->enable_32_cones ? 32 : 16;
+    // grids of resident blocks (grid-stride loops): the record scratch holds one block per warp of the grid
+    int dev = 0, sms = 0, occ_d = 0, occ_s = 0;
+    VCT_CUDA_TRY(cudaGetDevice(&dev));
+    VCT_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    VCT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_d, k_cone_backward_diffuse, 128, 0));
+    VCT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, k_cone_backward_specular, 128, 0));
+    const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((n * nc + 127) / 128, (int64_t)sms * std::max(occ_d, 1)));
+    const int64_t lblocks = std::max<int64_t>(1, std::min<int64_t>((n + 127) / 128, (int64_t)sms * std::max(occ_s, 1)));
+    const size_t rec_bytes = (size_t)std::max(blocks, lblocks) * (128 / 32) * kRecWarpFloats * sizeof(float);
     int* err = nullptr;
     VCT_CUDA_TRY(cudaMallocAsync(&err, sizeof(int), st));
     VCT_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), st));
+    float* rec = nullptr;
+    if (cudaMallocAsync(&rec, rec_bytes, st) != cudaSuccess) {
+        cudaFreeAsync(err, st);
+        return fail(VCT_E_CUDA, "vct_cone_trace_backward: record scratch allocation failed");
+    }
     F4Atlas T{reinterpret_cast<const float4*>(atlas4), AtlasDims(R)};
-    const int nc = desc->enable_32_cones ? 32 : 16;
-    int64_t blocks = (n * nc + 127) / 128;
-    if (blocks > 152 * 32) blocks = 152 * 32;
     ExactPlan plan;
     rc = exact_plan(samples, n, P.d, &plan, st);
     if (rc != VCT_OK) {
+        cudaFreeAsync(rec, st);
         cudaFreeAsync(err, st);
         return rc;
     }
     float4* G = reinterpret_cast<float4*>(grad_atlas4);
     k_cone_backward_diffuse<<<(int)blocks, 128, 0, st>>>(P, T, samples, n, plan.order,
-                                                          reinterpret_cast<const float4*>(grad_diffuse), G, err);
+                                                          reinterpret_cast<const float4*>(grad_diffuse), G, rec, err);
     cudaError_t le = cudaGetLastError();
     if (le == cudaSuccess) {
-        int64_t lblocks = (n + 127) / 128;
-        if (lblocks > 152 * 32) lblocks = 152 * 32;
         k_cone_backward_specular<<<(int)lblocks, 128, 0, st>>>(P, T, samples, plan.spec_list, plan.spec_count,
-                                                               reinterpret_cast<const float4*>(grad_specular), G, err);
+                                                               reinterpret_cast<const float4*>(grad_specular), G, rec,
+                                                               err);
         le = cudaGetLastError();
     }
     int h_err = 0;
     cudaError_t ce = cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, st);
     cudaError_t se = cudaStreamSynchronize(st);
+    cudaFreeAsync(rec, st);
     cudaFreeAsync(err, st);
     exact_plan_free(&plan, st);
     if (le != cudaSuccess) return cuda_fail(le, "vct_cone_trace_backward kernels");
