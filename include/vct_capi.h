@@ -324,8 +324,8 @@ int vct_cone_trace_f32(const vct_cone_tracing_desc* desc, const vct_cam_matrix* 
  * each).  The number of march steps (the occlusion stop) and the clamps are
  * held at their forward values.  Synchronises `stream`; VCT_E_OVERFLOW if a
  * cone marches more than 8192 steps.  Its stream-ordered scratch includes the
- * march records of the first 64 steps of each resident warp's cones (96 KiB
- * per warp: about 230 MB on a 152-SM GPU). */
+ * march records of the first 128 steps of each resident warp's cones
+ * (192 KiB per warp: about 480 MB on a 152-SM GPU). */
 int vct_cone_trace_backward(const vct_cone_tracing_desc* desc, const vct_cam_matrix* cam, const float* atlas4,
                             int32_t R, const vct_shadow_map* shadow, const vct_directional_light_desc* light,
                             const vct_directional_light_shadow_desc* light_shadow,

@@ -26,7 +26,7 @@
 // -fmad=false like them), so the recomputed steps are the forward's.
 //
 // Each cone is walked by one lane, the warp's lanes in lock step: one march
-// forward keeps each of the first 64 steps' record (the state before the
+// forward keeps each of the first 128 steps' record (the state before the
 // step, its sample, opacity terms, position and levels) in device scratch,
 // and a checkpoint of the march state every 32 steps after those; the walk
 // backward with the recurrences above in sequential form reads the records,
@@ -53,11 +53,18 @@ constexpr int kMaxSegments = 256;  // 8192 steps per cone: the specular cone at 
 // grid, fields outermost and lanes innermost: a warp's store or load of a
 // field is one 128-byte line), so those segments are walked backward without
 // a second march; later segments are recomputed from checkpoints.
-constexpr int kStoredSteps = 64;
+constexpr int kStoredSteps = 128;
 static_assert(kStoredSteps % kSegSteps == 0, "stored steps are whole segments");
 enum RecField { kRecAlpha, kRecOcc, kRecCorr, kRecQ, kRecOp, kRecSlope, kRecR, kRecG, kRecB, kRecStep, kRecFr,
                 kRecLevels, kRecFields };
 constexpr size_t kRecWarpFloats = (size_t)kRecFields * kStoredSteps * 32;
+__device__ __forceinline__ void rec_put(float* p, float v) { *p = v; }
+__device__ __forceinline__ float rec_get(const float* p) { return *p; }
+
+// Diffuse cones per warp group: 0 deals them cone-major (each cone slot over
+// all samples of the coherent order in turn); T > 0 deals all slots of T
+// consecutive samples before the next T.
+constexpr int kDiffuseTile = 1024;
 
 struct MarchState {
     float step, seg, diameter, alpha, occ;
@@ -179,18 +186,18 @@ __device__ void cone_backward_lane(const F4Atlas& T, float4* __restrict__ G, con
             if (j < kStoredSteps) {
                 float* r = rec + (size_t)j * 32 + lane;
                 constexpr size_t F = (size_t)kStoredSteps * 32;  // one field's floats
-                r[kRecAlpha * F] = alpha0;
-                r[kRecOcc * F] = occ0;
-                r[kRecCorr * F] = e.correction;
-                r[kRecQ * F] = e.q;
-                r[kRecOp * F] = e.op;
-                r[kRecSlope * F] = opacity_slope(e);
-                r[kRecR * F] = e.smp.x;
-                r[kRecG * F] = e.smp.y;
-                r[kRecB * F] = e.smp.z;
-                r[kRecStep * F] = step0;
-                r[kRecFr * F] = e.fr;
-                r[kRecLevels * F] = __int_as_float((e.lower & 0xffff) | (e.upper << 16));
+                rec_put(r + kRecAlpha * F, alpha0);
+                rec_put(r + kRecOcc * F, occ0);
+                rec_put(r + kRecCorr * F, e.correction);
+                rec_put(r + kRecQ * F, e.q);
+                rec_put(r + kRecOp * F, e.op);
+                rec_put(r + kRecSlope * F, opacity_slope(e));
+                rec_put(r + kRecR * F, e.smp.x);
+                rec_put(r + kRecG * F, e.smp.y);
+                rec_put(r + kRecB * F, e.smp.z);
+                rec_put(r + kRecStep * F, step0);
+                rec_put(r + kRecFr * F, e.fr);
+                rec_put(r + kRecLevels * F, __int_as_float((e.lower & 0xffff) | (e.upper << 16)));
             }
             ++n;
             running = m.step < max_dist && m.occ < 1.0f;
@@ -208,12 +215,12 @@ __device__ void cone_backward_lane(const F4Atlas& T, float4* __restrict__ G, con
                 if (i >= mine) continue;
                 const float* rr = rec + (size_t)i * 32 + lane;
                 constexpr size_t F = (size_t)kStoredSteps * 32;
-                const float alpha = rr[kRecAlpha * F], occ = rr[kRecOcc * F];
-                const float c = rr[kRecCorr * F], q = rr[kRecQ * F], op = rr[kRecOp * F];
-                const float slope = rr[kRecSlope * F];
-                const float sr = rr[kRecR * F], sg = rr[kRecG * F], sb = rr[kRecB * F];
-                const float step = rr[kRecStep * F], fr = rr[kRecFr * F];
-                const int lv = __float_as_int(rr[kRecLevels * F]);
+                const float alpha = rec_get(rr + kRecAlpha * F), occ = rec_get(rr + kRecOcc * F);
+                const float c = rec_get(rr + kRecCorr * F), q = rec_get(rr + kRecQ * F), op = rec_get(rr + kRecOp * F);
+                const float slope = rec_get(rr + kRecSlope * F);
+                const float sr = rec_get(rr + kRecR * F), sg = rec_get(rr + kRecG * F), sb = rec_get(rr + kRecB * F);
+                const float step = rec_get(rr + kRecStep * F), fr = rec_get(rr + kRecFr * F);
+                const int lv = __float_as_int(rec_get(rr + kRecLevels * F));
                 const float k_raw = 1.0f - alpha;
                 const float k = clampf(k_raw, 0.0f, 1.0f);
                 float4 gs;
@@ -299,10 +306,20 @@ __global__ void __launch_bounds__(128) k_cone_backward_diffuse(TraceParams P, F4
          t0 += (int64_t)gridDim.x * blockDim.x) {
         const int64_t t = t0 + lane;
         bool active = t < total;
-        // cone-major: a warp's lanes march the same cone of consecutive samples in the coherent order (the same
-        // direction from neighbouring points: the lanes stay in step and share texels)
-        const int slot = active ? (int)(t / n) : 0;
-        const int64_t u = active ? t - (int64_t)slot * n : 0;
+        // a warp's lanes march the same cone of consecutive samples in the coherent order (the same direction
+        // from neighbouring points: the lanes stay in step and share texels), all cones of kDiffuseTile samples
+        // before the next kDiffuseTile (the resident warps' gradient scatter then stays near one patch)
+        int slot = 0;
+        int64_t u = 0;
+        if (active && kDiffuseTile > 0) {
+            const int64_t per = (int64_t)kDiffuseTile * nc, tile = t / per, base = tile * kDiffuseTile;
+            const int64_t len = min((int64_t)kDiffuseTile, n - base), r = t - tile * per;
+            slot = (int)(r / len);
+            u = base + (r - (int64_t)slot * len);
+        } else if (active) {
+            slot = (int)(t / n);
+            u = t - (int64_t)slot * n;
+        }
         const int64_t i = order ? (int64_t)__ldg(order + u) : u;
         const GSample g = load_sample(samples + i, P.eye);
         active = active && g.depth != 1.0f;
