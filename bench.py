@@ -989,7 +989,8 @@ def differentiable_volume(dev, R: int = 128, views: int = 16, res: int = 512, se
             "mips_ms": mips_ms, "mips_backward_ms": mips_bwd_ms,
             "fit": fit_result,
             "note": "float RGBA atlas (16 B per texel, 1.27 GB at R = 128), software trilinear; the adjoint "
-                    "recomputes each cone from 32-step checkpoints and scatters float4 atomics"}
+                    "marches each cone once, keeping its first 128 steps' records in device scratch (later segments "
+                    "recomputed from 32-step checkpoints), and scatters float4 atomics"}
 
 
 def profile_case(args):

@@ -10,7 +10,7 @@ with Adam.  One iteration:
     work  = mips(param)              vct_downsample_f32, levels 1..5 (radiance mode)
     out   = trace(work)              vct_cone_trace_f32 (diffuse and specular images)
     loss  = mean (out - target)^2    vct_sq_error, both images
-    grad  = trace^T(dL/d out)        vct_cone_trace_backward (march recomputed from checkpoints)
+    grad  = trace^T(dL/d out)        vct_cone_trace_backward (one march, its steps kept)
     grad  = mips^T(grad)             vct_downsample_backward, levels 5..1
     param = adam(param, grad)        vct_adam_step (RGB kept >= 0, alpha in [0, alpha_max])
 
